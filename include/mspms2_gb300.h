@@ -1,0 +1,248 @@
+/*
+ * mspms2_gb300.h - C ABI of the GB300 (sm_103a) nonbonded-force engine for mspms2.
+ *
+ * The engine evaluates, on one GPU, what the reference computes in
+ *   frclong()  (src/frclong.c:20-1233)  - all nonbonded forces into fxl/fyl/fzl:
+ *              LJ (src/ljfrc.c:21-71), Ewald real/exclusion and Wolf
+ *              (src/elecfrc.c:17-60), plain Coulomb (src/elecfrc.c:138-241),
+ *              Ewald reciprocal + self + vacuum dipole (src/frclong.c:988-1129),
+ *              Wolf self (src/frclong.c:1130-1143), solid-fluid potentials
+ *              (src/frclong.c:1145-1209, src/sffrc.c, the mylibtasos Fortran sources);
+ *   frcshort() (src/frcshort.c:20-91)  - bonded forces into fxs/fys/fzs
+ *              (src/bndfrc.c, src/aglfrc.c, src/dihfrc.c, src/impfrc.c).
+ *
+ * Plain C types only: pointers, sizes, doubles. Every call returns an mg_status
+ * (0 = success); mg_last_error() gives a one-line description of the last failure
+ * in the calling thread's most recently used context.
+ *
+ * Units are whatever the caller uses consistently; the reference passes its
+ * reduced units (length sigma_base A, energy epsilon_base K). Only the tabulated
+ * solid-fluid models convert to A/K internally, exactly like the reference
+ * (src/sffrc.c:1322-1337, src/sffrc.c:951-965), using mg_params.sigma_base and
+ * mg_params.epsilon_base.
+ *
+ * Threading: a context is used by one host thread at a time. Many contexts may
+ * coexist (each owns its device buffers and CUDA stream).
+ */
+#ifndef MSPMS2_GB300_H_
+#define MSPMS2_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MG_ABI_VERSION 1
+
+typedef int mg_status;
+enum {
+    MG_OK = 0,
+    MG_ERR_INVALID = 1,      /* bad argument or inconsistent input */
+    MG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    MG_ERR_NO_DEVICE = 3,    /* no usable sm_103 device */
+    MG_ERR_STATE = 4,        /* call order violated (e.g. compute before topology) */
+    MG_ERR_OUT_OF_GRID = 5,  /* a site left a solid-fluid table (reference: AtomID=-9999,
+                                mylibtasos/forces.f90:59-79; assert, src/sffrc.c:987) */
+    MG_ERR_NONFINITE = 6,    /* a force or energy came out NaN/Inf */
+    MG_ERR_CAPACITY = 7,     /* an internal list exceeded its capacity after retries */
+    MG_ERR_UNSUPPORTED = 8,  /* a model option the engine does not implement */
+    MG_ERR_ALLOC = 9         /* device or host allocation failed */
+};
+
+/* Precision of the pair/k-space/solid-fluid arithmetic. */
+enum {
+    MG_PREC_MIXED = 0,  /* FP32 pair math, FP64 per-atom force/energy accumulation,
+                           FP64 structure-factor accumulation */
+    MG_PREC_FP64 = 1    /* every step in FP64 (the plain-FP64 GPU path) */
+};
+
+/* Model selectors; the numeric values are the reference's (src/defs.h:129-170). */
+enum { MG_GHOST_NONE = 0, MG_GHOST_LJ = 1, MG_GHOST_FULL = 2 };
+enum { MG_BOND_NONE = 0, MG_BOND_HARMONIC = 1, MG_BOND_MORSE = 2, MG_BOND_FENE = 3 };
+enum { MG_ANGLE_NONE = 0, MG_ANGLE_HARMONIC = 1, MG_ANGLE_TR_WATER = 2 };
+enum { MG_DIH_NONE = 0, MG_DIH_OPLS = 1, MG_DIH_CHARMM = 2 };
+enum { MG_IMP_NONE = 0, MG_IMP_CHARMM = 1 };
+enum { MG_SF_NONE = 0, MG_SF_HYPERGEO = 1, MG_SF_ATOM_EXPLICIT = 2, MG_SF_TASOS = 3,
+       MG_SF_MY_INTERP = 4 };
+enum { MG_ELEC_NONE = 0, MG_ELEC_EWALD = 1, MG_ELEC_WOLF = 2, MG_ELEC_SIMPLE_COULOMB = 3 };
+enum { MG_EWALD_BC_TINFOIL = 1, MG_EWALD_BC_VACUUM = 2 };
+
+/* Reference behaviours reproduced by default (mg_params.compat, bit flags).
+ * Clearing a bit selects the corrected behaviour instead. */
+enum {
+    MG_COMPAT_NBP_INDEX = 1 << 0,   /* nbp pair read as nbp_idx[ndih] (src/frclong.c:793-794) */
+    MG_COMPAT_TASOS_DXYZ = 1 << 1,  /* Dxyz weights of corners (i,j,k+1)/(i+1,j+1,k) swapped
+                                       (mylibtasos/cubicauxiliary.f90:219-233 vs forces.f90:155-162) */
+    MG_COMPAT_TASOS_PE_FLIP = 1 << 2, /* PE = -F if F < 1.5*minPE (mylibtasos/forces.f90:167-171) */
+    MG_COMPAT_HYPERGEO_LAST = 1 << 3, /* hypergeo energy keeps the last tube only (src/sffrc.c:1201) */
+    MG_COMPAT_ALL = 0xF
+};
+
+/* One molecular species: the reference's SAMPLE_MOLECULE template
+ * (src/molevars.h:40-73) plus its molecule count (nmole_per_specie). Atoms of a
+ * molecule are contiguous, molecules of a species are contiguous and species follow
+ * each other in order, exactly as the reference lays out xx/yy/zz. */
+typedef struct mg_species {
+    int natom;                 /* sites per molecule */
+    int nmole;                 /* molecules of this species */
+    const int *ghost_type;     /* [natom] MG_GHOST_* */
+    const int *interp_type;    /* [natom] solid-fluid table id (Tasos: 1-based AtomID;
+                                  my-interp: 0-based, as after init_my_interp) */
+    const double *epsilon;     /* [natom] */
+    const double *sigma;       /* [natom] */
+    const double *charge;      /* [natom] */
+    const double *aw;          /* [natom] site mass (for centres of mass) */
+    int nbond;
+    const int *bond_idx;       /* [nbond*2] */
+    const int *bond_type;      /* [nbond] */
+    const double *bond_param;  /* [nbond*3]  Kb, Req, alpha */
+    int nangle;
+    const int *angle_idx;      /* [nangle*3] */
+    const int *angle_type;     /* [nangle] */
+    const double *angle_param; /* [nangle*5] agl_para_1..5 (Ktheta, Thetaeq, p3, p4, p5) */
+    int ndih;
+    const int *dih_idx;        /* [ndih*4] */
+    const int *dih_type;       /* [ndih] */
+    const double *dih_param;   /* [ndih*4]  c1..c4 */
+    int nimp;
+    const int *imp_idx;        /* [nimp*4] */
+    const int *imp_type;       /* [nimp] */
+    const double *imp_param;   /* [nimp*2]  komega, omega0 */
+    int nnbp;
+    const int *nbp_idx;        /* [nnbp*2] */
+} mg_species;
+
+/* Force-field parameters and the derived constants the reference keeps as globals
+ * (src/vars.h). The derived block is taken as given so that a caller that keeps
+ * stale constants (the reference's volume move does not refresh the Ewald box
+ * constants, src/volchg.c:30-77) gets the reference's numbers; mg_params_derive()
+ * fills it the way src/initvars.c:591-599 and :433-462 do. */
+typedef struct mg_params {
+    double rcutoff, rcuton, rcutoffelec;
+    int lj_switch;              /* isLJswitchOn */
+    double f0;                  /* 1-4 LJ scale */
+    int charge_type;            /* MG_ELEC_* */
+    double kappa;               /* Ewald/Wolf damping (reduced) */
+    int kmax[3];                /* KMAXX, KMAXY, KMAXZ */
+    int ksqmax;                 /* KSQMAX */
+    int ewald_bc;               /* MG_EWALD_BC_* */
+    double coulomb_prefactor;   /* reduced Coulomb constant */
+    int sf_type;                /* MG_SF_* */
+    double sigma_base, epsilon_base; /* unit scales used by the tabulated SF models */
+    unsigned compat;            /* MG_COMPAT_* */
+    double respa_split;         /* 0: reference split (short = bonded, long = nonbonded).
+                                   > 0: distance split radius; short also gets the
+                                   inter-molecular LJ/real-space pairs with r < respa_split */
+    /* derived (set by mg_params_derive or copied from the reference globals) */
+    double rcutoffsq, rcutonsq, rcutoffelecsq, roff2_minus_ron2_cube;
+    double shift1, shift4;
+    double wolfvcon1, wolfvcon2, wolfvcon3, wolffcon1, wolffcon2;
+    double bfactor_ewald, vfactor_ewald, twopi_lx, twopi_ly, twopi_lz, twopi_over_3v;
+} mg_params;
+
+/* Energies and virials written by mg_compute; names and meanings follow the
+ * reference globals (src/vars.h:164-205). uelec holds uewald/uwolf/ucoulomb. */
+typedef struct mg_energies {
+    double uvdw, ushift, ureal, uexcl, ufourier, uself, uvacuum, uelec;
+    double usflj, uotherff, uinter, virial_inter;
+    double ubond, uangle, udih, uimp, uintra, virial_intra;
+} mg_energies;
+
+enum { MG_TERMS_LONG = 1, MG_TERMS_SHORT = 2, MG_TERMS_ALL = 3 };
+
+typedef struct mg_options {
+    int device;          /* CUDA device ordinal */
+    int precision;       /* MG_PREC_* */
+    double skin;         /* Verlet skin added to the list radius (caller units); the list is
+                            rebuilt when any site moved more than skin/2. 0 = rebuild each call */
+    int deterministic;   /* nonzero: fixed-order reductions everywhere (default 1) */
+} mg_options;
+
+typedef struct mg_ctx mg_ctx;
+
+/* Statistics of the last mg_compute (for measurement; no effect on results). */
+typedef struct mg_stats {
+    long long pairs_within_cutoff;  /* inter-molecular site pairs with r < cutoff, counted once */
+    long long cluster_pairs;        /* i-cluster x j-cluster entries processed (full list) */
+    long long nclusters;
+    long long kvectors;             /* half-space k-vectors evaluated */
+    int list_rebuilt;               /* 1 if the neighbour list was rebuilt in this call */
+    int list_builds;                /* total builds since creation */
+    double kernel_ms[8];            /* per-stage device times of the last call, if timing is on:
+                                       0 list, 1 pair, 2 intra+bonded, 3 k-space S(k),
+                                       4 k-space force, 5 solid-fluid, 6 reductions, 7 total */
+} mg_stats;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+void mg_options_default(mg_options *opt);
+mg_status mg_create(mg_ctx **ctx, const mg_options *opt);
+mg_status mg_destroy(mg_ctx *ctx);
+const char *mg_last_error(const mg_ctx *ctx);
+int mg_abi_version(void);
+
+/* ---- system description -------------------------------------------------- */
+/* Fill the derived block of p from its primary fields and the box
+ * (src/initvars.c:591-599, :433-455, :462 for coulomb is left to the caller). */
+void mg_params_derive(mg_params *p, double lx, double ly, double lz);
+mg_status mg_set_topology(mg_ctx *ctx, int nspecies, const mg_species *species);
+mg_status mg_set_params(mg_ctx *ctx, const mg_params *p);
+mg_status mg_set_box(mg_ctx *ctx, double lx, double ly, double lz);
+/* Use the caller's CUDA stream (cudaStream_t passed as void*); NULL = the context's own. */
+mg_status mg_set_stream(mg_ctx *ctx, void *stream);
+mg_status mg_set_timing(mg_ctx *ctx, int enable);
+
+/* ---- solid-fluid models (src/sffrc.c) ------------------------------------ */
+/* Tasos tricubic-Hermite grid for AtomID `type` (1-based). `values` holds the
+ * node records in the reference's Fortran order FG(I,J,K) with I fastest
+ * (mylibtasos/grid.f90:81-93): 8 doubles per node (F, Dx, Dy, Dz, Dxy, Dxz, Dyz,
+ * Dxyz), nx*ny*nz nodes (nx = ngx+2 ...). Grid spacing hx,hy,hz (A); cuc is the
+ * z period used by the nanotube PBC (mylibtasos/pbc.f90:80-84). */
+mg_status mg_sf_tasos_set_grid(mg_ctx *ctx, int type, int nx, int ny, int nz,
+                               double hx, double hy, double hz, double cuc,
+                               const double *values);
+/* Hypergeometric smooth tubes (src/sffrc.c:16-78, 1092-1209), reduced units. */
+mg_status mg_sf_hypergeo_set(mg_ctx *ctx, int ntube, const double *cx, const double *cy,
+                             const double *radius, double solid_sigma, double solid_epsilon,
+                             double const_3pisq_theta);
+/* Explicit solid atoms (src/sffrc.c:81-142, 1213-1314), reduced units. */
+mg_status mg_sf_atom_explicit_set(mg_ctx *ctx, int nsolid, const double *sx, const double *sy,
+                                  const double *sz, double solid_sigma, double solid_epsilon);
+/* "My interp" 32-term per-cube polynomials (src/sffrc.c:228-748, 951-1089) for table
+ * `type` (0-based): coeff = [4][32][ncube] doubles (energy, fx, fy, fz), cube index
+ * ix*ncy*ncz + iy*ncz + iz; lengths in A. */
+mg_status mg_sf_myinterp_set(mg_ctx *ctx, int type, int ncx, int ncy, int ncz,
+                             double itvl_x, double itvl_y, double itvl_z,
+                             double xmin, double ymin, double zmax, const double *coeff);
+
+/* ---- evaluation ---------------------------------------------------------- */
+/* Host buffers. x/y/z: [natom] site positions (unwrapped, as the reference keeps them).
+ * terms: MG_TERMS_*. Long forces go to fxl/fyl/fzl, short to fxs/fys/fzs (each
+ * overwritten; a triple may be NULL when its terms are not requested). e may be NULL. */
+mg_status mg_compute(mg_ctx *ctx, const double *x, const double *y, const double *z, int terms,
+                     double *fxl, double *fyl, double *fzl,
+                     double *fxs, double *fys, double *fzs, mg_energies *e);
+/* Same with device pointers (inputs resident in HBM, outputs written on device). The
+ * energies are written to host memory after the call completes. */
+mg_status mg_compute_device(mg_ctx *ctx, const double *d_x, const double *d_y,
+                            const double *d_z, int terms,
+                            double *d_fxl, double *d_fyl, double *d_fzl,
+                            double *d_fxs, double *d_fys, double *d_fzs, mg_energies *e);
+mg_status mg_get_stats(const mg_ctx *ctx, mg_stats *s);
+/* Device status word of the last call: bit 0 out-of-grid, bit 1 non-finite result,
+ * bit 2 list overflow, bit 3 column overflow. */
+mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);
+
+/* ---- neighbour-list inspection (tests of the bit-exact list build) ----------- */
+/* Copies the cluster layout and cluster-pair list of the last build:
+ * cluster_atoms[ncl*8] (site index or -1), pairs[npairs*2] (i-cluster, j-cluster),
+ * shifts[npairs*3] (the periodic image in box lengths, integers). Pass NULL buffers
+ * to query ncl and npairs. */
+mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *cluster_atoms,
+                            int *pairs, int *shifts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MSPMS2_GB300_H_ */

@@ -1,0 +1,189 @@
+"""Seeded synthetic systems with the shapes of the benchmark workloads.
+
+No dataset is involved: every system is generated from a seed. Units: sigma_base = 1 A,
+epsilon_base = 1 K, mass_base = 1e-27 kg, so the reduced units are A and K and the
+reference-format files written by system.write_reference_dir round-trip exactly.
+
+  water_box      flexible SPC water: O-O LJ eps 0.1553 kcal/mol, sigma 3.166 A, q(O)=-0.82,
+                 q(H)=+0.41, harmonic O-H (r0 1.0 A, k 1059 kcal/mol/A^2), harmonic HOH
+                 (109.47 deg, 75.9 kcal/mol/rad^2), U = k/2 (x-x0)^2 as src/bndfrc.c:143-145
+                 and src/aglfrc.c:82-86 define it. Jittered cubic lattice (+-0.1 A) with
+                 uniform random (Haar) orientations.
+  water_c1       216 molecules, box 18.6 A, Wolf alpha 0.2/A, Rc 9 A.
+  water_c2       32,768 molecules, box 99.3 A, Ewald alpha 0.3/A, Rc 10 A, kmax 24,
+                 ksqmax 576 (spherical cut), RESPA split 7 A.
+  water_c4       4,096 molecules, box 49.66 A, Ewald alpha 0.3/A, Rc 10 A, kmax 12,
+                 ksqmax 144 (same reciprocal resolution as water_c2).
+  lj_replica     LJ fluid, rho* 0.8, rc 2.5 sigma, jittered FCC (batched-HMC replicas).
+  butane_box     united-atom n-butane (CH3 98 K/3.75 A, CH2 46 K/3.95 A), 1.54 A bonds,
+                 114 deg angle, OPLS torsion with the reference's own constants
+                 (cfg.mspms:18 of the reference checkout).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .system import (AVOGADRO, ELEC_EWALD, ELEC_NONE, ELEC_WOLF, GHOST_LJ, GHOST_NONE,
+                     KCALMOL_TO_K, Species, System)
+
+
+def _reduced_mass(kg_per_mol: float) -> float:
+    return (kg_per_mol / AVOGADRO) / 1.0e-27
+
+
+def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniform random rotation matrices from Haar-distributed unit quaternions."""
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1),
+    ], 1)
+
+
+def water_species(nmole: int) -> Species:
+    theta0 = 109.47 * math.pi / 180.0
+    tmpl = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [math.cos(theta0), math.sin(theta0), 0.0]])
+    aw_in = np.array([0.0159994, 0.0010079, 0.0010079])
+    sp = Species(
+        name="water", nmole=nmole, atom_names=["O", "H", "H"],
+        atom_type=np.array([0, 1, 1], np.int32), ghost=np.array([GHOST_NONE, GHOST_LJ, GHOST_LJ], np.int32),
+        interp=np.array([1, 2, 2], np.int32),
+        epsilon=np.array([0.1553 * KCALMOL_TO_K, 0.0, 0.0]), sigma=np.array([3.166, 0.0, 0.0]),
+        charge=np.array([-0.82, 0.41, 0.41]), aw=np.array([_reduced_mass(v) for v in aw_in]),
+        aw_input=aw_in, template_xyz=tmpl)
+    sp.bond_idx = np.array([[0, 1], [0, 2]], np.int32)
+    sp.bond_type = np.array([1, 1], np.int32)
+    kb = 1059.0 * KCALMOL_TO_K
+    sp.bond_param = np.array([[kb, 1.0, 0.0], [kb, 1.0, 0.0]])
+    sp.angle_idx = np.array([[1, 0, 2]], np.int32)
+    sp.angle_type = np.array([1], np.int32)
+    sp.angle_param = np.array([[75.9 * KCALMOL_TO_K, theta0, 0.0, 0.0, 0.0]])
+    return sp
+
+
+def water_box(nside: int, box: float, seed: int, charge_type: int, kappa: float, rc: float,
+              kmax: int = 0, ksqmax: int = 0, jitter: float = 0.1, name: str = "water",
+              site_jitter: float = 0.0) -> System:
+    rng = np.random.default_rng(seed)
+    n = nside ** 3
+    sp = water_species(n)
+    a = box / nside
+    g = np.arange(nside)
+    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
+    centres = (np.stack([cx.ravel(), cy.ravel(), cz.ravel()], 1) + 0.5) * a
+    centres += rng.uniform(-jitter, jitter, size=centres.shape)
+    rot = _random_rotations(rng, n)
+    sites = centres[:, None, :] + np.einsum("mij,aj->mai", rot, sp.template_xyz)
+    xyz = sites.reshape(-1, 3)
+    if site_jitter > 0:  # distort the rigid template so bonded terms are not at rest
+        xyz = xyz + rng.uniform(-site_jitter, site_jitter, size=xyz.shape)
+    s = System(species=[sp], box=np.array([box, box, box]), x=xyz[:, 0].copy(), y=xyz[:, 1].copy(),
+               z=xyz[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc, charge_type=charge_type,
+               kappa=kappa, kmax=(kmax, kmax, kmax), ksqmax=ksqmax, name=name, delt_fs=0.5)
+    return s
+
+
+def water_c1(seed: int = 2024) -> System:
+    return water_box(6, 18.6, seed, ELEC_WOLF, 0.2, 9.0, name="water_c1")
+
+
+def water_c2(seed: int = 2024) -> System:
+    s = water_box(32, 99.3, seed, ELEC_EWALD, 0.3, 10.0, kmax=24, ksqmax=576, name="water_c2")
+    s.respa_split = 7.0
+    s.nstep_inner = 4
+    return s
+
+
+def water_c4(seed: int = 2024) -> System:
+    return water_box(16, 49.66, seed, ELEC_EWALD, 0.3, 10.0, kmax=12, ksqmax=144, name="water_c4")
+
+
+def water_small(nside: int, box: float, seed: int, charge_type: int = ELEC_EWALD, kappa: float = 0.3,
+                rc: float | None = None, kmax: int = 5, ksqmax: int = 27,
+                site_jitter: float = 0.04) -> System:
+    """Small water boxes for oracle-sized parity tests (templates distorted by
+    +-site_jitter A so the bonded terms are exercised)."""
+    rc = rc if rc is not None else min(9.0, 0.5 * box - 1e-9)
+    return water_box(nside, box, seed, charge_type, kappa, rc, kmax=kmax, ksqmax=ksqmax,
+                     name=f"water{nside}", site_jitter=site_jitter)
+
+
+def lj_species(nmole: int) -> Species:
+    return Species(name="lj", nmole=nmole, atom_names=["A"], atom_type=np.array([0], np.int32),
+                   ghost=np.array([GHOST_NONE], np.int32), interp=np.array([1], np.int32),
+                   epsilon=np.array([1.0]), sigma=np.array([1.0]), charge=np.array([0.0]),
+                   aw=np.array([1.0]), aw_input=np.array([AVOGADRO * 1.0e-27]),
+                   template_xyz=np.zeros((1, 3)))
+
+
+def lj_replica(n: int, seed: int, rho: float = 0.8, rc: float = 2.5, jitter: float = 0.05) -> System:
+    """One LJ-fluid replica: n atoms on a jittered FCC lattice at reduced density rho."""
+    rng = np.random.default_rng(seed)
+    box = (n / rho) ** (1.0 / 3.0)
+    m = int(math.ceil((n / 4.0) ** (1.0 / 3.0)))
+    a = box / m
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.arange(m)
+    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
+    cells = np.stack([cx.ravel(), cy.ravel(), cz.ravel()], 1)
+    pts = ((cells[:, None, :] + base[None, :, :]).reshape(-1, 3) + 0.25) * a
+    pts = pts[rng.permutation(len(pts))[:n]]
+    pts = pts + rng.uniform(-jitter, jitter, size=pts.shape)
+    return System(species=[lj_species(n)], box=np.array([box, box, box]), x=pts[:, 0].copy(),
+                  y=pts[:, 1].copy(), z=pts[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc,
+                  charge_type=ELEC_NONE, name=f"lj{n}")
+
+
+def butane_species(nmole: int, charged: bool = False) -> Species:
+    """United-atom n-butane, CH3-CH2-CH2-CH3."""
+    th = 114.0 * math.pi / 180.0
+    b = 1.54
+    p0 = np.array([0.0, 0.0, 0.0])
+    p1 = np.array([b, 0.0, 0.0])
+    p2 = p1 + b * np.array([-math.cos(th), math.sin(th), 0.0])
+    p3 = p2 + b * np.array([1.0, 0.0, 0.0])
+    tmpl = np.array([p0, p1, p2, p3])
+    q = np.array([-0.1, 0.1, -0.1, 0.1]) if charged else np.zeros(4)
+    aw_in = np.array([0.015035, 0.014027, 0.014027, 0.015035])
+    sp = Species(name="butane", nmole=nmole, atom_names=["CH3", "CH2", "CH2", "CH3"],
+                 atom_type=np.array([0, 1, 1, 0], np.int32), ghost=np.zeros(4, np.int32),
+                 interp=np.array([1, 2, 2, 1], np.int32), epsilon=np.array([98.0, 46.0, 46.0, 98.0]),
+                 sigma=np.array([3.75, 3.95, 3.95, 3.75]), charge=q,
+                 aw=np.array([_reduced_mass(v) for v in aw_in]), aw_input=aw_in, template_xyz=tmpl)
+    sp.bond_idx = np.array([[0, 1], [1, 2], [2, 3]], np.int32)
+    sp.bond_type = np.ones(3, np.int32)
+    sp.bond_param = np.array([[130924.4893, b, 0.0]] * 3)
+    sp.angle_idx = np.array([[0, 1, 2], [1, 2, 3]], np.int32)
+    sp.angle_type = np.ones(2, np.int32)
+    sp.angle_param = np.array([[62500.0, th, 0.0, 0.0, 0.0]] * 2)
+    sp.dih_idx = np.array([[0, 1, 2, 3]], np.int32)
+    sp.dih_type = np.array([1], np.int32)
+    sp.dih_param = np.array([[0.0, 710.06, -136.38, 1582.64]])
+    return sp
+
+
+def butane_box(nside: int, box, seed: int, rc: float = 14.0, charged: bool = False,
+               jitter: float = 0.05, name: str = "butane", site_jitter: float = 0.0) -> System:
+    """Butane on a jittered cubic lattice of molecule centres, random orientations."""
+    rng = np.random.default_rng(seed)
+    box = np.broadcast_to(np.asarray(box, dtype=float), (3,)).copy()
+    n = nside ** 3
+    sp = butane_species(n, charged)
+    a = box / nside
+    g = np.arange(nside)
+    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
+    centres = (np.stack([cx.ravel(), cy.ravel(), cz.ravel()], 1) + 0.5) * a
+    centres += rng.uniform(-jitter, jitter, size=centres.shape)
+    rot = _random_rotations(rng, n)
+    tm = sp.template_xyz - sp.template_xyz.mean(0)
+    xyz = (centres[:, None, :] + np.einsum("mij,aj->mai", rot, tm)).reshape(-1, 3)
+    if site_jitter > 0:
+        xyz = xyz + rng.uniform(-site_jitter, site_jitter, size=xyz.shape)
+    return System(species=[sp], box=box, x=xyz[:, 0].copy(), y=xyz[:, 1].copy(), z=xyz[:, 2].copy(),
+                  rcuton=rc, rcutoff=rc, rcutoffelec=rc, f0=0.5, name=name, delt_fs=2.0,
+                  charge_type=ELEC_NONE)

@@ -1,0 +1,51 @@
+#!/bin/sh
+# Builds the reference mspms2 force layer (C part) into oracle/_ref/ as the pinning
+# oracle for the CPU restatement. TEST INFRASTRUCTURE ONLY.
+#
+# Sources are read where they lie under the reference checkout ($MSPMS2_REF, default
+# /root/reference). Two documented patches are applied to transient copies under
+# oracle/_ref/build/, which are deleted after compiling (nothing of the reference is
+# kept in the repository):
+#   1. src/frclong.c:86 - j atoms of molecule iMole+1 (the unpatched line pairs a
+#      molecule with itself for iMole >= 1 and returns NaN);
+#   2. src/molevars.h:6-13 - NATOM_MAX/NMOLE_MAX/NBOND_MAX/NANGLE_MAX raised so the
+#      benchmark systems fit.
+# Left out: src/mspms2.c (its main() is replaced by oracle/ref_harness.c) and
+# src/dftmcff.c (needs GSL). The Fortran grid library mylibtasos/ cannot be compiled
+# here (no gfortran); oracle/ref_stubs.c supplies its four entry points on top of the
+# C restatement in oracle/mspms_oracle.c.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${MSPMS2_REF:-/root/reference}
+OUT="$HERE/_ref"
+CC=${CC:-gcc}
+if [ ! -f "$REF/src/frclong.c" ]; then
+  echo "build_ref.sh: reference sources not found under $REF; skipping" >&2
+  exit 0
+fi
+rm -rf "$OUT/build"
+mkdir -p "$OUT/build/src"
+for f in "$REF"/src/*.c "$REF"/src/*.h; do
+  b=$(basename "$f")
+  case "$b" in mspms2.c|dftmcff.c) continue ;; esac
+  cp "$f" "$OUT/build/src/$b"
+done
+sed -i 's/jabs = jsum_atom + (jStartMole==DYNAMIC_ID ? jAtom : 0);/jabs = (jStartMole==DYNAMIC_ID ? iabs + jAtom : jsum_atom);/' "$OUT/build/src/frclong.c"
+grep -q 'jabs = (jStartMole==DYNAMIC_ID ? iabs + jAtom : jsum_atom);' "$OUT/build/src/frclong.c"
+sed -i -e 's/^#define NATOM_MAX.*/#define NATOM_MAX	200000/' \
+       -e 's/^#define NBOND_MAX.*/#define NBOND_MAX	200000/' \
+       -e 's/^#define NANGLE_MAX.*/#define NANGLE_MAX	200000/' \
+       -e 's/^#define NDIH_MAX.*/#define NDIH_MAX	200000/' \
+       -e 's/^#define NIMP_MAX.*/#define NIMP_MAX	200000/' \
+       -e 's/^#define NNBP_MAX.*/#define NNBP_MAX	200000/' \
+       -e 's/^#define NMOLE_MAX.*/#define NMOLE_MAX	70000/' "$OUT/build/src/molevars.h"
+CFLAGS="-std=gnu99 -O2 -fcommon -ffp-contract=off -w"
+OBJS=""
+for f in "$OUT"/build/src/*.c "$HERE/ref_harness.c" "$HERE/ref_stubs.c" "$HERE/mspms_oracle.c"; do
+  o="$OUT/build/$(basename "$f" .c).o"
+  $CC $CFLAGS -I"$OUT/build/src" -c "$f" -o "$o"
+  OBJS="$OBJS $o"
+done
+$CC -o "$OUT/mspms_ref_force" $OBJS -lm
+rm -rf "$OUT/build"
+echo "built $OUT/mspms_ref_force"

@@ -1,0 +1,209 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE).
+
+Only tests/, __graft_entry__.smoke() and bench.py (its cpu_baseline leg and the
+`--impl reference` arm) import this module; it is the checker, never the product.
+`run_reference_dir` runs the compiled reference (oracle/_ref/mspms_ref_force) when it
+exists; `Oracle` runs the C restatement (oracle/liboracle.so).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from mspms2_gb300.capi import ENERGY_NAMES, MgEnergies, MgParams, MgSpecies, SpeciesPack, system_params
+from mspms2_gb300.system import System, write_reference_dir
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "mspms_ref_force")
+
+_dp = C.POINTER(C.c_double)
+
+
+class OrcTasos(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("hx", C.c_double),
+                ("hy", C.c_double), ("hz", C.c_double), ("cuc", C.c_double), ("values", _dp),
+                ("min_pe", C.c_double)]
+
+
+class OrcMyInterp(C.Structure):
+    _fields_ = [("ncx", C.c_int), ("ncy", C.c_int), ("ncz", C.c_int), ("itvl_x", C.c_double),
+                ("itvl_y", C.c_double), ("itvl_z", C.c_double), ("xmin", C.c_double),
+                ("ymin", C.c_double), ("zmax", C.c_double), ("coeff", _dp)]
+
+
+class OrcSystem(C.Structure):
+    _fields_ = [("nspecies", C.c_int), ("sp", C.POINTER(MgSpecies)), ("p", MgParams),
+                ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+                ("ntasos", C.c_int), ("tasos", C.POINTER(OrcTasos)),
+                ("ntube", C.c_int), ("tube_x", _dp), ("tube_y", _dp), ("tube_r", _dp),
+                ("solid_sigma", C.c_double), ("solid_epsilon", C.c_double),
+                ("const_3pisq_theta", C.c_double),
+                ("nsolid", C.c_int), ("solid_x", _dp), ("solid_y", _dp), ("solid_z", _dp),
+                ("nmyinterp", C.c_int), ("myinterp", C.POINTER(OrcMyInterp))]
+
+
+class OrcWindow(C.Structure):
+    _fields_ = [("imol_begin", C.c_int), ("imol_end", C.c_int), ("k_stride", C.c_int),
+                ("skip_intra", C.c_int)]
+
+
+def build() -> str:
+    src = [os.path.join(HERE, f) for f in ("mspms_oracle.c", "nblist_oracle.c", "mspms_oracle.h")]
+    if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.orc_frclong.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, _dp, _dp, _dp,
+                                     C.POINTER(MgEnergies), C.POINTER(OrcWindow)]
+        _lib.orc_frcshort.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, _dp, _dp, _dp,
+                                      C.POINTER(MgEnergies)]
+        _lib.orc_count_pairs.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, C.c_double]
+        _lib.orc_count_pairs.restype = C.c_longlong
+        _lib.orc_tasos_force.argtypes = [C.POINTER(OrcTasos), C.c_uint, C.c_double, C.c_double,
+                                         C.c_double, _dp, _dp]
+        _lib.orc_tasos_min_pe.argtypes = [C.POINTER(OrcTasos)]
+        _lib.orc_tasos_min_pe.restype = C.c_double
+        _lib.orc_nblist_build.argtypes = [_dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_longlong]
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Oracle:
+    """The C restatement bound to one System."""
+
+    def __init__(self, system: System, params: MgParams | None = None):
+        self.system = system
+        self.pack = SpeciesPack(system)
+        self.keep = []
+        s = OrcSystem()
+        s.nspecies = self.pack.n
+        s.sp = C.cast(self.pack.array, C.POINTER(MgSpecies))
+        s.p = params if params is not None else system_params(system)
+        s.lx, s.ly, s.lz = (float(v) for v in system.box)
+        if system.tasos:
+            arr = (OrcTasos * len(system.tasos))()
+            for i, g in enumerate(system.tasos):
+                v = np.ascontiguousarray(g.values, dtype=np.float64)
+                self.keep.append(v)
+                arr[i].nx, arr[i].ny, arr[i].nz = g.nx, g.ny, g.nz
+                arr[i].hx, arr[i].hy, arr[i].hz, arr[i].cuc = g.hx, g.hy, g.hz, g.cuc
+                arr[i].values = _ptr(v)
+                arr[i].min_pe = float(v[..., 0].min())
+            self.keep.append(arr)
+            s.ntasos = len(system.tasos)
+            s.tasos = C.cast(arr, C.POINTER(OrcTasos))
+        if system.tube_xy_r is not None:
+            t = np.ascontiguousarray(system.tube_xy_r.T, dtype=np.float64)
+            self.keep.append(t)
+            s.ntube = t.shape[1]
+            s.tube_x, s.tube_y, s.tube_r = _ptr(t[0]), _ptr(t[1]), _ptr(t[2])
+        s.solid_sigma, s.solid_epsilon = system.solid_sigma, system.solid_epsilon
+        s.const_3pisq_theta = system.const_3pisq_theta
+        if system.solid_xyz is not None:
+            t = np.ascontiguousarray(system.solid_xyz.T, dtype=np.float64)
+            self.keep.append(t)
+            s.nsolid = t.shape[1]
+            s.solid_x, s.solid_y, s.solid_z = _ptr(t[0]), _ptr(t[1]), _ptr(t[2])
+        if system.myinterp:
+            arr = (OrcMyInterp * len(system.myinterp))()
+            for i, g in enumerate(system.myinterp):
+                c = np.ascontiguousarray(g.coeff, dtype=np.float64)
+                self.keep.append(c)
+                arr[i].ncx, arr[i].ncy, arr[i].ncz = g.ncx, g.ncy, g.ncz
+                arr[i].itvl_x, arr[i].itvl_y, arr[i].itvl_z = g.itvl
+                arr[i].xmin, arr[i].ymin, arr[i].zmax = g.xmin, g.ymin, g.zmax
+                arr[i].coeff = _ptr(c)
+            self.keep.append(arr)
+            s.nmyinterp = len(system.myinterp)
+            s.myinterp = C.cast(arr, C.POINTER(OrcMyInterp))
+        self.s = s
+
+    def frclong(self, x=None, y=None, z=None, window: OrcWindow | None = None):
+        sysm = self.system
+        x = np.ascontiguousarray(sysm.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(sysm.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(sysm.z if z is None else z, dtype=np.float64)
+        n = len(x)
+        f = np.zeros((3, n))
+        e = MgEnergies()
+        flags = lib().orc_frclong(C.byref(self.s), _ptr(x), _ptr(y), _ptr(z), _ptr(f[0]), _ptr(f[1]),
+                                  _ptr(f[2]), C.byref(e), C.byref(window) if window else None)
+        return f, e.as_dict(), flags
+
+    def frcshort(self, x=None, y=None, z=None):
+        sysm = self.system
+        x = np.ascontiguousarray(sysm.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(sysm.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(sysm.z if z is None else z, dtype=np.float64)
+        n = len(x)
+        f = np.zeros((3, n))
+        e = MgEnergies()
+        err = lib().orc_frcshort(C.byref(self.s), _ptr(x), _ptr(y), _ptr(z), _ptr(f[0]), _ptr(f[1]),
+                                 _ptr(f[2]), C.byref(e))
+        d = e.as_dict()
+        return f, {k: d[k] for k in ("ubond", "uangle", "udih", "uimp", "uintra", "virial_intra")}, err
+
+    def count_pairs(self, r: float) -> int:
+        s = self.system
+        x, y, z = (np.ascontiguousarray(v, dtype=np.float64) for v in (s.x, s.y, s.z))
+        return int(lib().orc_count_pairs(C.byref(self.s), _ptr(x), _ptr(y), _ptr(z), r * r))
+
+
+def read_ref_output(fn: str):
+    raw = open(fn, "rb").read()
+    n = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
+    a = np.frombuffer(raw[4:], dtype=np.float64)
+    fl = a[0:3 * n].reshape(3, n).copy()
+    fs = a[3 * n:6 * n].reshape(3, n).copy()
+    e = dict(zip(ENERGY_NAMES, a[6 * n:6 * n + 18]))
+    dnames = ["rcutoffsq", "rcutonsq", "rcutoffelecsq", "roff2_minus_ron2_cube", "shift1", "shift4",
+              "wolfvcon1", "wolfvcon2", "wolfvcon3", "wolffcon1", "wolffcon2", "bfactor_ewald",
+              "vfactor_ewald", "twopi_lx", "twopi_ly", "twopi_lz", "twopi_over_3v", "kappa",
+              "coulomb_prefactor", "boxlx", "boxly", "boxlz", "sigma_base", "epsilon_base"]
+    d = dict(zip(dnames, a[6 * n + 18:6 * n + 42]))
+    return fl, fs, e, d
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_BIN) and os.access(REF_BIN, os.X_OK)
+
+
+def run_reference_dir(path: str, repeat: int = 0):
+    """Run the compiled reference on a directory of reference-format inputs."""
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "out.bin")
+        p = subprocess.run([REF_BIN, path, out, str(repeat)], capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"reference failed: {p.stderr[-2000:]}")
+        res = read_ref_output(out)
+    timing = {}
+    for tok in p.stdout.split():
+        if "=" in tok:
+            k, v = tok.split("=", 1)
+            timing[k] = float(v)
+    return res, timing
+
+
+def run_reference_system(system: System, repeat: int = 0):
+    with tempfile.TemporaryDirectory() as td:
+        write_reference_dir(system, td)
+        return run_reference_dir(td, repeat)

@@ -1,0 +1,251 @@
+"""Generate the golden fixtures under tests/golden/ from the compiled reference.
+
+Each case is a system written in the reference's own input format, run through
+oracle/_ref/mspms_ref_force (the reference force layer built by oracle/build_ref.sh
+from the reference checkout), and stored as <case>.npz with:
+  the parsed system (mspms2_gb300.system.system_to_arrays),
+  ref_fl[3,n], ref_fs[3,n]  forces of frclong() / frcshort(),
+  ref_energies[18]          in mspms2_gb300.capi.ENERGY_NAMES order,
+  ref_derived[24]           derived globals after init_vars().
+Two cases use the reference's shipped inputs (Examples/Water and the root example);
+the rest are seeded synthetic systems chosen to reach every model switch.
+
+Run from the repository root:  python tests/golden/gen_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from mspms2_gb300 import configs  # noqa: E402
+from mspms2_gb300.system import (ELEC_EWALD, ELEC_NONE, ELEC_SIMPLE_COULOMB, ELEC_WOLF,  # noqa: E402
+                                 GHOST_FULL, SF_ATOM_EXPLICIT, SF_HYPERGEO, SF_MY_INTERP, SF_TASOS,
+                                 MyInterpGrid, Species, System, TasosGrid, read_reference_dir,
+                                 system_to_arrays, tasos_dims, write_reference_dir)
+from oracle.pyoracle import reference_available, run_reference_dir  # noqa: E402
+
+REF = os.environ.get("MSPMS2_REF", "/root/reference")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def lj_gas(n, box, seed, sigma=3.5, eps=50.0, xy_range=None, rc=None, avoid=None):
+    """n LJ sites on a jittered cubic lattice (spacing >= 1.05 sigma) inside the box, or
+    inside xy_range in x and y; `avoid(p)` rejects lattice points (near solid walls)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = (0.0, box) if xy_range is None else xy_range
+    a = 1.05 * sigma
+    gx = np.arange(lo + 0.5 * a, hi - 0.25 * a, a)
+    gz = np.arange(0.5 * a, box - 0.25 * a, a)
+    X, Y, Z = np.meshgrid(gx, gx, gz, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    if avoid is not None:
+        pts = pts[[not avoid(p) for p in pts]]
+    if len(pts) < n:
+        raise ValueError(f"lattice holds {len(pts)} sites < {n}")
+    pts = pts[rng.permutation(len(pts))[:n]] + rng.uniform(-0.05 * sigma, 0.05 * sigma, size=(n, 3))
+    sp = configs.lj_species(n)
+    sp.sigma = np.array([sigma])
+    sp.epsilon = np.array([eps])
+    rc = rc if rc is not None else 0.5 * box - 1e-6
+    return System(species=[sp], box=np.array([box, box, box]), x=pts[:, 0].copy(), y=pts[:, 1].copy(),
+                  z=pts[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc, name=f"ljgas{n}")
+
+
+def tasos_test_grid(auc, buc, cuc, seed):
+    """Smooth analytic field with exact derivatives, Dxyz perturbed so the reference's
+    corner pairing of Dxyz is visible."""
+    ngx, ngy, ngz, hx, hy, hz = tasos_dims(auc, buc, cuc)
+    x = np.arange(ngx + 2) * hx
+    y = np.arange(ngy + 2) * hy
+    z = np.arange(ngz + 2) * hz
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    a, b, c = 1.3, 0.9, 2 * np.pi / cuc
+    A = 400.0
+    sx, cx = np.sin(a * X), np.cos(a * X)
+    sy, cy = np.sin(b * Y), np.cos(b * Y)
+    sz, cz = np.sin(c * Z), np.cos(c * Z)
+    F = A * sx * cy * cz - 900.0 + 30.0 * (X - auc / 2) ** 2
+    v = np.zeros(F.shape + (8,))
+    v[..., 0] = F
+    v[..., 1] = A * a * cx * cy * cz + 60.0 * (X - auc / 2)
+    v[..., 2] = -A * b * sx * sy * cz
+    v[..., 3] = -A * c * sx * cy * sz
+    v[..., 4] = -A * a * b * cx * sy * cz
+    v[..., 5] = -A * a * c * cx * cy * sz
+    v[..., 6] = A * b * c * sx * sy * sz
+    rng = np.random.default_rng(seed)
+    v[..., 7] = A * a * b * c * cx * sy * sz + rng.normal(scale=50.0, size=F.shape)
+    return TasosGrid(ngx + 2, ngy + 2, ngz + 2, hx, hy, hz, cuc, v)
+
+
+def custom_molecule_system(seed, with_nbp=False):
+    """A 6-site molecule with ghosts (LJ and FULL), nbp pairs, CHARMM dihedral and
+    improper, FENE/harmonic/Morse bonds, harmonic angles; Wolf electrostatics."""
+    rng = np.random.default_rng(seed)
+    tmpl = np.array([[0, 0, 0], [1.5, 0, 0], [2.1, 1.3, 0], [3.5, 1.4, 0.4], [1.4, -1.2, 0.5],
+                     [4.2, 2.5, 0.3]], dtype=float)
+    sp = Species(name="hexa", nmole=0, atom_names=["A", "B", "C", "D", "E", "F"],
+                 atom_type=np.arange(6, dtype=np.int32),
+                 ghost=np.array([0, 0, 1, 0, 2, 0], np.int32), interp=np.ones(6, np.int32),
+                 epsilon=np.array([60.0, 45.0, 30.0, 80.0, 20.0, 55.0]),
+                 sigma=np.array([3.4, 3.6, 2.5, 3.8, 2.0, 3.3]),
+                 charge=np.array([-0.4, 0.3, 0.2, -0.3, 0.1, 0.1]),
+                 aw=np.array([12.0, 14.0, 1.0, 16.0, 1.0, 12.0]) * 1.66054,
+                 aw_input=np.array([12.0, 14.0, 1.0, 16.0, 1.0, 12.0]) * 1e-3, template_xyz=tmpl)
+    sp.aw = (sp.aw_input / 6.0221415e23) / 1.0e-27
+    sp.bond_idx = np.array([[0, 1], [1, 2], [2, 3], [1, 4], [3, 5]], np.int32)
+    sp.bond_type = np.array([1, 2, 3, 1, 1], np.int32)
+    sp.bond_param = np.array([[100000.0, 1.5, 0.0], [30000.0, 1.45, 2.0], [5000.0, 2.5, 0.0],
+                              [90000.0, 1.3, 0.0], [80000.0, 1.4, 0.0]])
+    sp.angle_idx = np.array([[0, 1, 2], [1, 2, 3], [0, 1, 4], [2, 3, 5]], np.int32)
+    sp.angle_type = np.ones(4, np.int32)
+    sp.angle_param = np.array([[40000.0, 1.9, 0, 0, 0], [35000.0, 2.0, 0, 0, 0], [30000.0, 1.95, 0, 0, 0],
+                               [20000.0, 2.1, 0, 0, 0]])
+    sp.dih_idx = np.array([[0, 1, 2, 3], [1, 2, 3, 5], [4, 1, 2, 3]], np.int32)
+    sp.dih_type = np.array([1, 2, 1], np.int32)
+    sp.dih_param = np.array([[0.0, 700.0, -130.0, 1500.0], [300.0, 3.0, 0.0, 0.0], [10.0, 200.0, 50.0, 300.0]])
+    sp.imp_idx = np.array([[1, 0, 2, 4]], np.int32)
+    sp.imp_type = np.array([1], np.int32)
+    sp.imp_param = np.array([[150.0, 35.0]])
+    if with_nbp:
+        sp.nbp_idx = np.array([[0, 3], [0, 5], [4, 5], [2, 5]], np.int32)
+    nside = 3
+    box = 16.0
+    sp.nmole = nside ** 3
+    g = np.arange(nside)
+    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
+    cen = (np.stack([cx.ravel(), cy.ravel(), cz.ravel()], 1) + 0.5) * (box / nside)
+    rot = configs._random_rotations(rng, sp.nmole)
+    xyz = (cen[:, None, :] + np.einsum("mij,aj->mai", rot, tmpl - tmpl.mean(0))).reshape(-1, 3)
+    return System(species=[sp], box=np.array([box] * 3), x=xyz[:, 0].copy(), y=xyz[:, 1].copy(),
+                  z=xyz[:, 2].copy(), rcuton=6.0, rcutoff=7.9, rcutoffelec=7.9, lj_switch=1, f0=0.5,
+                  charge_type=ELEC_WOLF, kappa=0.25, name="custom")
+
+
+def cases():
+    out = {}
+    out["water_example"] = ("dir", os.path.join(REF, "Examples", "Water"))
+    out["butane_root"] = ("dir", REF)
+    c1 = configs.water_box(6, 18.6, 11, ELEC_WOLF, 0.2, 9.0, name="water_c1", site_jitter=0.04)
+    out["water_wolf_216"] = ("sys", c1)
+    w = configs.water_small(4, 14.0, seed=12, charge_type=ELEC_EWALD, kappa=0.35, rc=6.5, kmax=5, ksqmax=27)
+    w.ewald_bc = 2
+    w.name = "water_vacuum"
+    out["water_ewald_vacuum"] = ("sys", w)
+    out["water_ewald_512"] = ("sys", configs.water_small(8, 24.8, seed=13, charge_type=ELEC_EWALD,
+                                                         kappa=0.3, rc=10.0, kmax=7, ksqmax=49))
+    sc = configs.water_small(4, 14.0, seed=14, charge_type=ELEC_SIMPLE_COULOMB, rc=6.5)
+    sc.name = "water_coulomb"
+    out["water_simple_coulomb"] = ("sys", sc)
+    st = configs.water_small(4, 13.0, seed=15, charge_type=ELEC_EWALD, kappa=0.35, rc=6.4, kmax=4, ksqmax=20)
+    st.x = st.x - st.box[0] * np.floor(st.x / st.box[0])  # per-site wrap breaks molecules apart
+    st.y = st.y - st.box[1] * np.floor(st.y / st.box[1])
+    st.z = st.z - st.box[2] * np.floor(st.z / st.box[2])
+    st.name = "water_wrapped"
+    out["water_wrapped_ewald"] = ("sys", st)
+    stw = configs.water_small(4, 13.0, seed=16, charge_type=ELEC_WOLF, kappa=0.25, rc=6.4)
+    stw.x = stw.x - stw.box[0] * np.floor(stw.x / stw.box[0])
+    stw.name = "water_wrapped_wolf"
+    out["water_wrapped_wolf"] = ("sys", stw)
+    bt = configs.butane_box(3, 16.0, seed=17, rc=7.9, charged=True, site_jitter=0.05)
+    bt.charge_type = ELEC_EWALD
+    bt.kappa = 0.3
+    bt.kmax = (4, 4, 4)
+    bt.ksqmax = 24
+    bt.lj_switch = 1
+    bt.rcuton = 6.5
+    bt.name = "butane_switch"
+    out["butane_ewald_switch"] = ("sys", bt)
+    out["custom_wolf"] = ("sys", custom_molecule_system(18))
+    cu = custom_molecule_system(19)
+    cu.charge_type = ELEC_EWALD
+    cu.kappa, cu.kmax, cu.ksqmax = 0.3, (4, 4, 4), 24
+    cu.name = "custom_ewald"
+    out["custom_ewald"] = ("sys", cu)
+    lj = configs.lj_replica(500, seed=20)
+    out["lj_fluid_500"] = ("sys", lj)
+    tubes = np.array([[4.0, 4.0, 3.0], [10.5, 9.0, 2.5], [7.0, 12.0, 1.8]])
+
+    def near_wall(p, tubes=tubes):
+        return any(abs(np.hypot(p[0] - t[0], p[1] - t[1]) - t[2]) < 2.2 for t in tubes)
+    hg = lj_gas(30, 14.0, seed=21, avoid=near_wall, sigma=2.5)
+    hg.sf_type = SF_HYPERGEO
+    hg.tube_xy_r = tubes
+    hg.solid_sigma, hg.solid_epsilon = 3.4, 28.0
+    hg.name = "hypergeo"
+    out["sf_hypergeo"] = ("sys", hg)
+    hl = lj_gas(20, 12.0, seed=22, sigma=2.5, avoid=lambda p: abs(np.hypot(p[0] - 6, p[1] - 6) - 2.0) < 1.5)
+    hl.sf_type = SF_HYPERGEO
+    hl.tube_xy_r = np.array([[6.0, 6.0, 2.0]])
+    hl.solid_sigma, hl.solid_epsilon = 3.4, 28.0
+    hl.compat = 0x7
+    hl.name = "hypergeo_sum"
+    out["sf_hypergeo_sum"] = ("sys", hl)
+    solid = np.random.default_rng(24).uniform(0, 14.0, size=(30, 3))
+
+    def near_solid(p, solid=solid):
+        d = solid - p
+        d -= 14.0 * np.rint(d / 14.0)
+        return (d ** 2).sum(1).min() < 2.6 ** 2
+    ae = lj_gas(20, 14.0, seed=23, avoid=near_solid, sigma=2.5)
+    ae.sf_type = SF_ATOM_EXPLICIT
+    ae.lj_switch = 1
+    ae.rcuton = 5.0
+    ae.solid_xyz = solid
+    ae.solid_sigma, ae.solid_epsilon = 3.4, 28.0
+    ae.name = "atom_explicit"
+    out["sf_atom_explicit"] = ("sys", ae)
+    ta = lj_gas(12, 12.0, seed=25, xy_range=(0.3, 3.7), sigma=1.0, eps=5.0)
+    ta.sf_type = SF_TASOS
+    ta.species[0].interp = np.array([1], np.int32)
+    ta.tasos_cell = (4.0, 4.0, 2.4595, 1.0)
+    ta.tasos = [tasos_test_grid(4.0, 4.0, 2.4595, 26)]
+    ta.name = "tasos"
+    out["sf_tasos"] = ("sys", ta)
+    mi = lj_gas(12, 12.0, seed=27, xy_range=(0.2, 3.8), sigma=1.0, eps=5.0)
+    mi.sf_type = SF_MY_INTERP
+    mi.species[0].interp = np.array([0], np.int32)
+    rng = np.random.default_rng(28)
+    ncx, ncy, ncz = 4, 4, 3
+    scale = np.array([1, .1, .1, .1, .01, .01, .01, .01, .01, .01] + [.001] * 10 + [1e-4] * 12)
+    coeff = rng.normal(size=(4, 32, ncx * ncy * ncz)) * (50.0 * scale)[None, :, None]
+    mi.myinterp = [MyInterpGrid(ncx, ncy, ncz, (1.0, 1.0, 1.0), 0.0, 0.0, 3.0, coeff)]
+    mi.name = "myinterp"
+    out["sf_myinterp"] = ("sys", mi)
+    return out
+
+
+def main():
+    if not reference_available():
+        sys.exit("oracle/_ref/mspms_ref_force missing: run `sh oracle/build_ref.sh` first")
+    only = set(sys.argv[1:])
+    for name, (kind, obj) in cases().items():
+        if only and name not in only:
+            continue
+        with tempfile.TemporaryDirectory() as td:
+            if kind == "dir":
+                src = obj
+            else:
+                write_reference_dir(obj, td)
+                src = td
+            system = read_reference_dir(src)
+            (fl, fs, e, d), _ = run_reference_dir(src)
+        arrays = system_to_arrays(system)
+        arrays["ref_fl"] = fl
+        arrays["ref_fs"] = fs
+        arrays["ref_energies"] = np.array(list(e.values()))
+        arrays["ref_derived"] = np.array(list(d.values()))
+        fn = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(fn, **arrays)
+        print(f"{name}: natom={system.natom} uinter={e['uinter']:.10g} uintra={e['uintra']:.10g} "
+              f"-> {os.path.getsize(fn)} bytes")
+
+
+if __name__ == "__main__":
+    main()
