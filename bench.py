@@ -1,0 +1,413 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 nonbonded-force engine on the 98,304-site SPC water system.
+
+Workload (one "step" = one complete force evaluation, frclong() + frcshort() of the
+reference, src/frclong.c:20 and src/frcshort.c:20): 32,768 flexible SPC water molecules,
+box 99.3 A, LJ + Ewald (alpha 0.3/A, real-space cutoff 10 A, kmax 24 per axis, spherical
+ksqmax 576), harmonic bonds and angles; seeded synthetic coordinates (jittered lattice,
+random orientations); mixed precision (FP32 pair arithmetic, FP64 accumulation).
+
+metric  pair interactions per second: inter-molecular site pairs inside the cutoff
+        (counted once) times steps, over the device time of the steps.
+value   inputs resident in HBM (mg_compute_device); L2 (129 MB) flushed by a 256 MiB
+        write before every step, each step timed alone with CUDA events on the stream the
+        engine launches on.
+e2e     the same through mg_compute with pinned host buffers: positions copied in and
+        forces copied out inside the timed region.
+Also reported: the plain-FP64 GPU path on the same workload, ns/day of the RESPA split
+(inner: bonded + pairs < 7 A, four 0.5 fs steps; outer: 7-10 A shell + reciprocal, 2 fs),
+the roofline of the dominant kernel and a bounded CPU baseline of the reference
+algorithm (the oracle port, single thread, extrapolated from a sampled window).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+SM_COUNT_NOMINAL = 152
+FP32_LANES_PER_SM = 128
+# algorithmic work per unit (work model)
+FLOP_PAIR = 55.0        # LJ + Ewald-real pair, counted once
+FLOP_K_S = 10.0         # per (half-space k-vector, site) in the S(k) pass
+FLOP_K_F = 12.0         # per (half-space k-vector, site) in the force pass
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="water_c2", choices=["water_c2", "water_c4", "water_c1"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-extras", action="store_true", help="skip FP64 path, RESPA and CPU baseline")
+    ap.add_argument("--cpu-sample-mols", type=int, default=256)
+    ap.add_argument("--cpu-k-stride", type=int, default=400)
+    return ap.parse_args()
+
+
+def make_system(name):
+    from mspms2_gb300 import configs
+    return {"water_c2": configs.water_c2, "water_c4": configs.water_c4, "water_c1": configs.water_c1}[name]()
+
+
+def pairs_in_cutoff(s):
+    """Inter-molecular site pairs (neither GHOST_FULL) with r < cutoff, counted once."""
+    from scipy.spatial import cKDTree
+    q, g, mol = s.site_arrays()
+    keep = g != 2
+    pts = np.stack([s.x, s.y, s.z], 1)[keep]
+    L = np.asarray(s.box, dtype=float)
+    pts = pts - L * np.floor(pts / L)
+    pts = np.minimum(pts, np.nextafter(L, 0))
+    r = max(s.rcutoff, s.rcutoffelec)
+    t = cKDTree(pts, boxsize=L)
+    total = (int(t.count_neighbors(t, r)) - len(pts)) // 2
+    intra = 0
+    for sp in s.species:
+        xyz = sp.template_xyz
+        a = np.where(sp.ghost != 2)[0]
+        d = np.linalg.norm(xyz[a][:, None] - xyz[a][None], axis=-1)
+        intra += int(np.triu(d < r, 1).sum()) * sp.nmole
+    return total - intra
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            p = [v.strip() for v in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        self.file.close()
+        os.unlink(self.file.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(system, sample_mols, k_stride, threads_note=1):
+    """Reference algorithm (oracle port of src/frclong.c / src/frcshort.c), single thread,
+    on a sampled window: i-molecules [0, sample_mols) of the O(N^2) pair loop and every
+    k_stride-th reciprocal vector; extrapolated to the full call."""
+    from oracle.pyoracle import Oracle, OrcWindow
+    o = Oracle(system)
+    M = system.nmole
+    w_pairs = OrcWindow(0, sample_mols, 1 << 30, 1)   # pair window, ~no k-space, no intra
+    t0 = time.perf_counter()
+    o.frclong(window=w_pairs)
+    t_pairs = time.perf_counter() - t0
+    w_k = OrcWindow(M, M + 1, k_stride, 1)            # no pairs, strided k-space
+    t0 = time.perf_counter()
+    o.frclong(window=w_k)
+    t_k = time.perf_counter() - t0
+    w_intra = OrcWindow(M, M + 1, 1 << 30, 0)         # intra + self terms only
+    t0 = time.perf_counter()
+    o.frclong(window=w_intra)
+    t_intra = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    o.frcshort()
+    t_short = time.perf_counter() - t0
+    # examined molecule pairs: sampled rows vs the whole upper triangle
+    sample = sum(M - 1 - i for i in range(min(sample_mols, M)))
+    total = M * (M - 1) // 2
+    kx, ky, kz = system.kmax
+    kfull = sum(1 for a in range(-kx, kx + 1) for b in range(-ky, ky + 1) for c in range(-kz, kz + 1)
+                if 0 < a * a + b * b + c * c <= system.ksqmax)
+    ksample = (kfull + k_stride - 1) // k_stride
+    t_full = t_pairs * total / max(sample, 1) + max(t_k - t_intra, 0.0) * kfull / max(ksample, 1) + t_intra + t_short
+    return {"t_step_s": t_full, "t_sampled_s": t_pairs + t_k + t_intra + t_short,
+            "sample": f"i-molecules 0..{sample_mols} of {M} in the O(N^2) pair loop, every {k_stride}th of "
+                      f"{kfull} k-vectors, full intra/bonded; extrapolated to one full call"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    system = make_system(args.workload)
+    npairs = pairs_in_cutoff(system)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(system, max(8, args.cpu_sample_mols // 8), args.cpu_k_stride * 8)
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
+        vals.append(npairs / last["t_step_s"])
+    wall = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": "pair_interactions_per_s", "value": value,
+            "unit": "pair-interactions/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * last["t_step_s"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "sites": system.natom, "pairs_in_cutoff": npairs},
+            "cpu_baseline": {"value": value, "unit": "pair-interactions/s", "cores": 1, "kind": "port",
+                             "sample": last["sample"], "host_cores": os.cpu_count()},
+            "e2e": {"value": value, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from mspms2_gb300 import build
+    from mspms2_gb300.engine import TERMS_ALL, TERMS_LONG, TERMS_SHORT, Engine
+
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    system = make_system(args.workload)
+    n = system.natom
+    stream = torch.cuda.current_stream()
+    eng = Engine(system, precision=args.precision, device=local_rank)
+    eng.set_stream(stream.cuda_stream)
+    pos = torch.tensor(np.stack([system.x, system.y, system.z]), dtype=torch.float64, device="cuda")
+    fl = torch.empty((3, n), dtype=torch.float64, device="cuda")
+    fs = torch.empty((3, n), dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    ptrs = (pos[0].data_ptr(), pos[1].data_ptr(), pos[2].data_ptr())
+
+    def step():
+        return eng.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local_rank)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    st = eng.stats()
+    npairs = st["pairs_within_cutoff"]
+    ms_step = statistics.mean(times)
+    if dist:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * npairs / (ms_step * 1e-3)
+
+    # per-stage device times (one more call with stage events on)
+    eng.set_timing(True)
+    flush.fill_(1.0)
+    step()
+    torch.cuda.synchronize()
+    kms = eng.stats()["kernel_ms"]
+    launches = eng.stats()["kernel_launches"]
+    eng.set_timing(False)
+
+    # e2e through mg_compute with pinned host buffers
+    hx = torch.from_numpy(np.ascontiguousarray(system.x)).pin_memory().numpy()
+    hy = torch.from_numpy(np.ascontiguousarray(system.y)).pin_memory().numpy()
+    hz = torch.from_numpy(np.ascontiguousarray(system.z)).pin_memory().numpy()
+    hfl = torch.empty((3, n), dtype=torch.float64).pin_memory().numpy()
+    hfs = torch.empty((3, n), dtype=torch.float64).pin_memory().numpy()
+    for _ in range(2):
+        eng.compute_into(hx, hy, hz, hfl, hfs)
+    e2e_times = []
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.compute_into(hx, hy, hz, hfl, hfs)
+        b.record(stream)
+        b.synchronize()
+        e2e_times.append(a.elapsed_time(b))
+    e2e_ms = statistics.mean(e2e_times)
+    e2e_value = world * npairs / (e2e_ms * 1e-3)
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # plain FP64 GPU path, same workload
+        eng64 = Engine(system, precision="fp64", device=local_rank)
+        eng64.set_stream(stream.cuda_stream)
+        eng64.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+        t64 = []
+        for k in range(max(2, min(3, args.steps))):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng64.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+            b.record(stream)
+            b.synchronize()
+            t64.append(a.elapsed_time(b))
+        fl64 = fl.clone()
+        eng64.close()
+        step()
+        torch.cuda.synchronize()
+        err = float(torch.linalg.vector_norm(fl - fl64) / torch.linalg.vector_norm(fl64))
+        ms64 = statistics.mean(t64)
+        extras["fp64_path"] = {"value": npairs / (ms64 * 1e-3), "ms_per_step": ms64,
+                               "mixed_over_fp64": ms64 / ms_step, "rms_rel_force_err_mixed_vs_fp64": err}
+        # RESPA distance split: 4 inner (0.5 fs) + 1 outer (2 fs) per outer step
+        if system.respa_split > 0:
+            engs = Engine(system, precision=args.precision, skin=1.0, device=local_rank)
+            engs.set_stream(stream.cuda_stream)
+            engs.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+            engs.set_timing(True)
+            engs.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_LONG)
+            engs.set_timing(False)
+
+            def timed(fn, reps):
+                ts = []
+                for _ in range(reps):
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    fn()
+                    b.record(stream)
+                    b.synchronize()
+                    ts.append(a.elapsed_time(b))
+                return statistics.mean(ts)
+
+            t_in = timed(lambda: engs.compute_device(*ptrs, None, fs.data_ptr(), TERMS_SHORT), 8)
+            t_out = timed(lambda: engs.compute_device(*ptrs, fl.data_ptr(), None, TERMS_LONG), 4)
+            eb = Engine(system, precision=args.precision, device=local_rank)
+            eb.set_stream(stream.cuda_stream)
+            eb.set_timing(True)
+            eb.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_LONG)
+            t_build = eb.stats()["kernel_ms"][0]
+            eb.close()
+            outer_ms = 4 * t_in + t_out + t_build / 10.0
+            extras["respa"] = {"inner_ms": t_in, "outer_ms": t_out, "list_build_ms": t_build,
+                               "outer_step_ms": outer_ms, "ns_per_day": 2e-6 / (outer_ms * 1e-3) * 86400,
+                               "note": "split 7 A, 4 x 0.5 fs inner + 2 fs outer, skin 1 A, list rebuilt "
+                                       "every 10 outer steps"}
+            engs.close()
+        cpu = cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
+        extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
+                                  "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],
+                                  "host_cores": os.cpu_count()}
+
+    # roofline of the dominant stage (FP32 pipe: no stage is a dense contraction)
+    kvec = st["kvectors"]
+    stages = {"pair": (kms[1], FLOP_PAIR * npairs), "kspace_sk": (kms[3], FLOP_K_S * kvec * n),
+              "kspace_force": (kms[4], FLOP_K_F * kvec * n)}
+    dom = max(stages, key=lambda k: stages[k][0])
+    t_ms, flops = stages[dom]
+    peak = SM_COUNT_NOMINAL * FP32_LANES_PER_SM * 2 * 2.07e9 / 1e12
+    achieved = flops / (t_ms * 1e-3) / 1e12 if t_ms > 0 else 0.0
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", f"traffic_{dom}_{args.workload}.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    if rank != 0:
+        return 0
+    line = {"metric": "pair_interactions_per_s", "value": value, "unit": "pair-interactions/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math / f64 accumulation"
+            if args.precision == "mixed" else "f64", "data": "synthetic (seeded lattice water)",
+            "config": {"workload": args.workload, "sites": n, "molecules": system.nmole, "box_A": float(system.box[0]),
+                       "rc_A": system.rcutoff, "ewald_alpha": system.kappa, "kmax": list(system.kmax),
+                       "ksqmax": system.ksqmax, "kvectors_half_space": kvec, "pairs_in_cutoff": npairs,
+                       "l2": "256 MiB flush before every step; steps timed one by one with CUDA events",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "pair-interactions/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": 3 * 8 * n, "d2h_bytes_per_step": 6 * 8 * n + 8 * 18},
+            "gpu_launches": launches * args.steps,
+            "stage_ms": {"list": kms[0], "pair": kms[1], "intra_bonded": kms[2], "kspace_sk": kms[3],
+                         "kspace_force": kms[4], "solid_fluid": kms[5], "reduce": kms[6], "total": kms[7]},
+            "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_basis": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz "
+                                       "(MEASURED_PEAKS.json holds no FP32 figure)"},
+            "clocks": clk}
+    if "cpu_baseline" in extras:
+        line["cpu_baseline"] = extras.pop("cpu_baseline")
+    line.update(extras)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

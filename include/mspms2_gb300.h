@@ -36,6 +36,12 @@ extern "C" {
 
 #define MG_ABI_VERSION 1
 
+#if defined(__GNUC__)
+#define MG_API __attribute__((visibility("default")))
+#else
+#define MG_API
+#endif
+
 typedef int mg_status;
 enum {
     MG_OK = 0,
@@ -171,27 +177,30 @@ typedef struct mg_stats {
     int list_rebuilt;               /* 1 if the neighbour list was rebuilt in this call */
     int list_builds;                /* total builds since creation */
     double kernel_ms[8];            /* per-stage device times of the last call, if timing is on:
-                                       0 list, 1 pair, 2 intra+bonded, 3 k-space S(k),
-                                       4 k-space force, 5 solid-fluid, 6 reductions, 7 total */
+                                       0 list build + packing, 1 pair kernel, 2 intra+bonded,
+                                       3 k-space phases + S(k), 4 S(k) reduction + k-space force,
+                                       5 solid-fluid, 6 reductions and checks, 7 total */
+    int kernel_launches;            /* kernels this library launched in the last call */
 } mg_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */
-void mg_options_default(mg_options *opt);
-mg_status mg_create(mg_ctx **ctx, const mg_options *opt);
-mg_status mg_destroy(mg_ctx *ctx);
-const char *mg_last_error(const mg_ctx *ctx);
-int mg_abi_version(void);
+MG_API void mg_options_default(mg_options *opt);
+MG_API mg_status mg_create(mg_ctx **ctx, const mg_options *opt);
+MG_API mg_status mg_destroy(mg_ctx *ctx);
+MG_API const char *mg_last_error(const mg_ctx *ctx);
+MG_API int mg_abi_version(void);
 
 /* ---- system description -------------------------------------------------- */
 /* Fill the derived block of p from its primary fields and the box
- * (src/initvars.c:591-599, :433-455, :462 for coulomb is left to the caller). */
-void mg_params_derive(mg_params *p, double lx, double ly, double lz);
-mg_status mg_set_topology(mg_ctx *ctx, int nspecies, const mg_species *species);
-mg_status mg_set_params(mg_ctx *ctx, const mg_params *p);
-mg_status mg_set_box(mg_ctx *ctx, double lx, double ly, double lz);
+ * (src/initvars.c:591-599, :433-455; coulomb_prefactor, :462, is a primary field). */
+MG_API void mg_params_derive(mg_params *p, double lx, double ly, double lz);
+/* Call mg_set_params first: the nbp bit of mg_params.compat is read here. */
+MG_API mg_status mg_set_topology(mg_ctx *ctx, int nspecies, const mg_species *species);
+MG_API mg_status mg_set_params(mg_ctx *ctx, const mg_params *p);
+MG_API mg_status mg_set_box(mg_ctx *ctx, double lx, double ly, double lz);
 /* Use the caller's CUDA stream (cudaStream_t passed as void*); NULL = the context's own. */
-mg_status mg_set_stream(mg_ctx *ctx, void *stream);
-mg_status mg_set_timing(mg_ctx *ctx, int enable);
+MG_API mg_status mg_set_stream(mg_ctx *ctx, void *stream);
+MG_API mg_status mg_set_timing(mg_ctx *ctx, int enable);
 
 /* ---- solid-fluid models (src/sffrc.c) ------------------------------------ */
 /* Tasos tricubic-Hermite grid for AtomID `type` (1-based). `values` holds the
@@ -199,20 +208,20 @@ mg_status mg_set_timing(mg_ctx *ctx, int enable);
  * (mylibtasos/grid.f90:81-93): 8 doubles per node (F, Dx, Dy, Dz, Dxy, Dxz, Dyz,
  * Dxyz), nx*ny*nz nodes (nx = ngx+2 ...). Grid spacing hx,hy,hz (A); cuc is the
  * z period used by the nanotube PBC (mylibtasos/pbc.f90:80-84). */
-mg_status mg_sf_tasos_set_grid(mg_ctx *ctx, int type, int nx, int ny, int nz,
+MG_API mg_status mg_sf_tasos_set_grid(mg_ctx *ctx, int type, int nx, int ny, int nz,
                                double hx, double hy, double hz, double cuc,
                                const double *values);
 /* Hypergeometric smooth tubes (src/sffrc.c:16-78, 1092-1209), reduced units. */
-mg_status mg_sf_hypergeo_set(mg_ctx *ctx, int ntube, const double *cx, const double *cy,
+MG_API mg_status mg_sf_hypergeo_set(mg_ctx *ctx, int ntube, const double *cx, const double *cy,
                              const double *radius, double solid_sigma, double solid_epsilon,
                              double const_3pisq_theta);
 /* Explicit solid atoms (src/sffrc.c:81-142, 1213-1314), reduced units. */
-mg_status mg_sf_atom_explicit_set(mg_ctx *ctx, int nsolid, const double *sx, const double *sy,
+MG_API mg_status mg_sf_atom_explicit_set(mg_ctx *ctx, int nsolid, const double *sx, const double *sy,
                                   const double *sz, double solid_sigma, double solid_epsilon);
 /* "My interp" 32-term per-cube polynomials (src/sffrc.c:228-748, 951-1089) for table
  * `type` (0-based): coeff = [4][32][ncube] doubles (energy, fx, fy, fz), cube index
  * ix*ncy*ncz + iy*ncz + iz; lengths in A. */
-mg_status mg_sf_myinterp_set(mg_ctx *ctx, int type, int ncx, int ncy, int ncz,
+MG_API mg_status mg_sf_myinterp_set(mg_ctx *ctx, int type, int ncx, int ncy, int ncz,
                              double itvl_x, double itvl_y, double itvl_z,
                              double xmin, double ymin, double zmax, const double *coeff);
 
@@ -220,27 +229,28 @@ mg_status mg_sf_myinterp_set(mg_ctx *ctx, int type, int ncx, int ncy, int ncz,
 /* Host buffers. x/y/z: [natom] site positions (unwrapped, as the reference keeps them).
  * terms: MG_TERMS_*. Long forces go to fxl/fyl/fzl, short to fxs/fys/fzs (each
  * overwritten; a triple may be NULL when its terms are not requested). e may be NULL. */
-mg_status mg_compute(mg_ctx *ctx, const double *x, const double *y, const double *z, int terms,
+MG_API mg_status mg_compute(mg_ctx *ctx, const double *x, const double *y, const double *z, int terms,
                      double *fxl, double *fyl, double *fzl,
                      double *fxs, double *fys, double *fzs, mg_energies *e);
 /* Same with device pointers (inputs resident in HBM, outputs written on device). The
  * energies are written to host memory after the call completes. */
-mg_status mg_compute_device(mg_ctx *ctx, const double *d_x, const double *d_y,
+MG_API mg_status mg_compute_device(mg_ctx *ctx, const double *d_x, const double *d_y,
                             const double *d_z, int terms,
                             double *d_fxl, double *d_fyl, double *d_fzl,
                             double *d_fxs, double *d_fys, double *d_fzs, mg_energies *e);
-mg_status mg_get_stats(const mg_ctx *ctx, mg_stats *s);
+MG_API mg_status mg_get_stats(const mg_ctx *ctx, mg_stats *s);
 /* Device status word of the last call: bit 0 out-of-grid, bit 1 non-finite result,
  * bit 2 list overflow, bit 3 column overflow. */
-mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);
+MG_API mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);
 
 /* ---- neighbour-list inspection (tests of the bit-exact list build) ----------- */
 /* Copies the cluster layout and cluster-pair list of the last build:
- * cluster_atoms[ncl*8] (site index or -1), pairs[npairs*2] (i-cluster, j-cluster),
- * shifts[npairs*3] (the periodic image in box lengths, integers). Pass NULL buffers
- * to query ncl and npairs. */
-mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *cluster_atoms,
-                            int *pairs, int *shifts);
+ * grid[3] = (columns along x, columns along y, small-box flag), cluster_atoms[ncl*8]
+ * (site index or -1), pairs[npairs*2] (i-cluster, j-cluster), shifts[npairs*3] (the
+ * periodic image of the j-cluster in box lengths). Pass NULL buffers to query ncl
+ * and npairs. */
+MG_API mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *grid,
+                            int *cluster_atoms, int *pairs, int *shifts);
 
 #ifdef __cplusplus
 }

@@ -65,7 +65,7 @@ class MgStats(C.Structure):
     _fields_ = [("pairs_within_cutoff", C.c_longlong), ("cluster_pairs", C.c_longlong),
                 ("nclusters", C.c_longlong), ("kvectors", C.c_longlong),
                 ("list_rebuilt", C.c_int), ("list_builds", C.c_int),
-                ("kernel_ms", C.c_double * 8)]
+                ("kernel_ms", C.c_double * 8), ("kernel_launches", C.c_int)]
 
 
 def params_struct(p: dict) -> MgParams:

@@ -1,0 +1,458 @@
+// mg_ewald.cu - Ewald reciprocal space (src/frclong.c:988-1048).
+//
+// The reference sums, for every k = (kx*TWOPI_LX, ky*TWOPI_LY, kz*TWOPI_LZ) with
+// 0 < kx^2+ky^2+kz^2 <= KSQMAX and |k_d| <= KMAX_d, S(k) = sum_j q_j e^{i k.r_j} and then
+// U = Vfactor*C * sum_k exp(-B k^2)/k^2 |S(k)|^2 and
+// F_i = sum_k 2 q_i Im(conj(S) e^{i k.r_i}) Vfactor*C*exp(-B k^2)/k^2 * k.
+// Here only the half space (kx > 0, or kx = 0 and ky > 0, or kx = ky = 0 and kz > 0)
+// is evaluated; S(-k) = conj S(k) gives the other half, so energy and forces carry a
+// factor 2.
+//
+// Phases: u_d = frac(x_d * TWOPI_L_d / 2pi) is turned once per site into a 32-bit (mixed)
+// or 64-bit (FP64 path) fixed-point fraction U; n*U modulo 2^32 (2^64) is then the exact
+// phase of harmonic n, so e^{2 pi i n u} = sincospi(2 n U / 2^32) needs no range reduction
+// and no recurrence. Tables per site: X[0..KMAXX], Y[0..KMAXY], Z[0..KMAXZ].
+//
+// k-vectors are grouped in rows (kx, ky) holding |kz| = 0..kzmax(kx,ky) with both signs
+// of kz. Structure factors: a thread owns (row, 8 consecutive |kz|) = up to 16 k-vectors;
+// the block stages a tile of site tables in shared memory and accumulates in R over the
+// tile, then in FP64; each block writes FP64 partial S for its site range; a
+// fixed-order reduction over site blocks gives S(k) (deterministic). Forces: a thread
+// owns a site and walks all rows, the coefficients c_k S(k) broadcast from shared memory.
+#include <math.h>
+
+#include <algorithm>
+
+#include "mg_internal.cuh"
+
+#define EW_TILE 64      // sites per shared-memory tile in the S(k) pass
+#define EW_CH 8         // |kz| values per thread in the S(k) pass
+#define EW_TPB 128      // threads per block in the S(k) pass
+#define EW_SITES 4096   // sites per block in the S(k) pass
+#define EW_FROWS 32     // rows staged per step in the force pass
+
+namespace {
+
+template <typename R>
+struct C2;
+template <>
+struct C2<float> {
+    typedef float2 T;
+};
+template <>
+struct C2<double> {
+    typedef double2 T;
+};
+
+template <typename T>
+__device__ __forceinline__ T cmul(T a, T b) {
+    T r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+// phase tables tab[d][n][site] = e^{2 pi i n u_d}
+__global__ void k_phase_f(int n, const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, double sx, double sy, double sz, int kx, int ky, int kz,
+                          float2 *__restrict__ tab) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const double pos[3] = {x[a], y[a], z[a]};
+    const double sc[3] = {sx, sy, sz};
+    const int km[3] = {kx, ky, kz};
+    size_t off = 0;
+    for (int d = 0; d < 3; d++) {
+        double t = pos[d] * sc[d];
+        t = t - floor(t);
+        double tu = t * 4294967296.0;
+        unsigned U = tu >= 4294967295.0 ? 0xffffffffu : (unsigned)tu;
+        for (int k = 0; k <= km[d]; k++) {
+            unsigned V = U * (unsigned)k;
+            float v = (float)(int)V * 4.656612873077393e-10f;  // 2^-31
+            float s, c;
+            sincospif(v, &s, &c);
+            tab[off + (size_t)k * n + a] = make_float2(c, s);
+        }
+        off += (size_t)(km[d] + 1) * n;
+    }
+}
+
+__global__ void k_phase_d(int n, const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, double sx, double sy, double sz, int kx, int ky, int kz,
+                          double2 *__restrict__ tab) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const double pos[3] = {x[a], y[a], z[a]};
+    const double sc[3] = {sx, sy, sz};
+    const int km[3] = {kx, ky, kz};
+    size_t off = 0;
+    for (int d = 0; d < 3; d++) {
+        double t = pos[d] * sc[d];
+        t = t - floor(t);
+        unsigned long long U = __double2ull_rz(t * 18446744073709551616.0);
+        for (int k = 0; k <= km[d]; k++) {
+            unsigned long long V = U * (unsigned long long)k;
+            double v = (double)(long long)V * 1.0842021724855044e-19;  // 2^-63
+            double s, c;
+            sincospi(v, &s, &c);
+            tab[off + (size_t)k * n + a] = make_double2(c, s);
+        }
+        off += (size_t)(km[d] + 1) * n;
+    }
+}
+
+struct EwArgs {
+    int n, nrows, nslots, ntasks;
+    int kx, ky, kz;  // KMAX per axis (table extents)
+    const int4 *rows;       // kx, ky, kzmax, half_only
+    const int *row_slot;    // first slot of each row
+    const int2 *tasks;      // (row, first |kz|)
+    const void *tab;
+    const double *q;
+    double *spart;          // [site blocks][nslots][2]
+    void *scoef;            // [nslots] R2: 4*Vfactor*C*kvec*S
+    double twopi[3];
+    double bfac, vfac, coul;
+    double *rows_e;
+    int row0;
+    double *f;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(EW_TPB) k_sk(EwArgs A) {
+    typedef typename C2<R>::T T2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *sX = (T2 *)smem_raw;
+    const int P = EW_TILE + 1;  // padded tile pitch
+    T2 *sY = sX + (size_t)(A.kx + 1) * P;
+    T2 *sZ = sY + (size_t)(A.ky + 1) * P;
+    R *sQ = (R *)(sZ + (size_t)(A.kz + 1) * P);
+    const T2 *tab = (const T2 *)A.tab;
+    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    const int task = blockIdx.x * EW_TPB + threadIdx.x;
+    int kx = 0, ky = 0, kzmax = -1, half = 0, kz0 = 0, slot0 = 0;
+    if (task < A.ntasks) {
+        int2 t = A.tasks[task];
+        int4 r = A.rows[t.x];
+        kx = r.x;
+        ky = r.y;
+        kzmax = r.z;
+        half = r.w;
+        kz0 = t.y;
+        slot0 = A.row_slot[t.x];
+    }
+    const int cnt = max(0, min(EW_CH, kzmax - kz0 + 1));
+    const int aky = ky < 0 ? -ky : ky;
+    const R ysign = ky < 0 ? (R)-1 : (R)1;
+    double accP[EW_CH][2], accM[EW_CH][2];
+#pragma unroll
+    for (int j = 0; j < EW_CH; j++) accP[j][0] = accP[j][1] = accM[j][0] = accM[j][1] = 0.0;
+    const int a_begin = blockIdx.y * EW_SITES, a_end = min(A.n, a_begin + EW_SITES);
+    for (int t0 = a_begin; t0 < a_end; t0 += EW_TILE) {
+        const int tn = min(EW_TILE, a_end - t0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < (A.kx + 1) * EW_TILE; i += EW_TPB) {
+            int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) sX[k * P + s] = tX[(size_t)k * A.n + t0 + s];
+        }
+        for (int i = threadIdx.x; i < (A.ky + 1) * EW_TILE; i += EW_TPB) {
+            int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) sY[k * P + s] = tY[(size_t)k * A.n + t0 + s];
+        }
+        for (int i = threadIdx.x; i < (A.kz + 1) * EW_TILE; i += EW_TPB) {
+            int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) sZ[k * P + s] = tZ[(size_t)k * A.n + t0 + s];
+        }
+        for (int s = threadIdx.x; s < tn; s += EW_TPB) sQ[s] = (R)A.q[t0 + s];
+        __syncthreads();
+        if (cnt == 0) continue;
+        R pP[EW_CH][2], pM[EW_CH][2];
+#pragma unroll
+        for (int j = 0; j < EW_CH; j++) pP[j][0] = pP[j][1] = pM[j][0] = pM[j][1] = (R)0;
+        for (int s = 0; s < tn; s++) {
+            T2 X = sX[kx * P + s];
+            T2 Y = sY[aky * P + s];
+            Y.y *= ysign;
+            const R q = sQ[s];
+            T2 Aq = cmul(X, Y);
+            Aq.x *= q;
+            Aq.y *= q;
+            T2 Z = sZ[kz0 * P + s];
+            const T2 Z1 = sZ[1 * P + s];
+#pragma unroll
+            for (int j = 0; j < EW_CH; j++) {
+                // A*Z and A*conj(Z) share four products
+                const R p1 = Aq.x * Z.x, p2 = Aq.y * Z.y, p3 = Aq.x * Z.y, p4 = Aq.y * Z.x;
+                pP[j][0] += p1 - p2;
+                pP[j][1] += p3 + p4;
+                pM[j][0] += p1 + p2;
+                pM[j][1] += p4 - p3;
+                Z = cmul(Z, Z1);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < EW_CH; j++) {
+            accP[j][0] += pP[j][0];
+            accP[j][1] += pP[j][1];
+            accM[j][0] += pM[j][0];
+            accM[j][1] += pM[j][1];
+        }
+    }
+    if (task >= A.ntasks) return;
+    double *out = A.spart + (size_t)blockIdx.y * A.nslots * 2;
+#pragma unroll
+    for (int j = 0; j < EW_CH; j++) {
+        if (j >= cnt) break;
+        int a = kz0 + j;
+        int sp = slot0 + 2 * a, sm = sp + 1;
+        out[2 * sp] = accP[j][0];
+        out[2 * sp + 1] = accP[j][1];
+        bool has_minus = (a > 0) && !half;
+        out[2 * sm] = has_minus ? accM[j][0] : 0.0;
+        out[2 * sm + 1] = has_minus ? accM[j][1] : 0.0;
+    }
+    (void)half;
+}
+
+// S(k) from the partials in site-block order; energy rows and force coefficients
+template <typename R>
+__global__ void k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row) {
+    typedef typename C2<R>::T T2;
+    double e[1] = {0.0};
+    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot < A.nslots) {
+        double sr = 0.0, si = 0.0;
+        for (int b = 0; b < nblk; b++) {
+            const double *p = A.spart + ((size_t)b * A.nslots + slot) * 2;
+            sr += p[0];
+            si += p[1];
+        }
+        int r = slot_row[slot];
+        int4 row = A.rows[r];
+        int local = slot - A.row_slot[r];
+        int a = local >> 1, minus = local & 1;
+        bool valid = a <= row.z && !(minus && (a == 0 || row.w)) && !(row.w && a == 0);
+        T2 c;
+        c.x = c.y = (R)0;
+        if (valid) {
+            double kz = minus ? -a : a;
+            double rkx = A.twopi[0] * row.x, rky = A.twopi[1] * row.y, rkz = A.twopi[2] * kz;
+            double rksq = rkx * rkx + rky * rky + rkz * rkz;
+            double kvec = exp(-A.bfac * rksq) / rksq;
+            e[0] = 2.0 * kvec * (sr * sr + si * si) * A.vfac * A.coul;
+            double cf = 4.0 * A.vfac * A.coul * kvec;
+            c.x = (R)(cf * sr);
+            c.y = (R)(cf * si);
+        }
+        ((T2 *)A.scoef)[slot] = c;
+    }
+    const int ids[1] = {E_UFOURIER};
+    mg_block_row<1>(e, ids, A.rows_e, A.row0 + blockIdx.x);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_kforce(EwArgs A, int maxslots_per_row) {
+    typedef typename C2<R>::T T2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *sC = (T2 *)smem_raw;  // [EW_FROWS][maxslots]
+    __shared__ int4 sRow[EW_FROWS];
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = a < A.n;
+    const T2 *tab = (const T2 *)A.tab;
+    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    const T2 Z1 = act ? tZ[(size_t)1 * A.n + a] : T2();
+    const R tx = (R)A.twopi[0], ty = (R)A.twopi[1], tz = (R)A.twopi[2];
+    double F[3] = {0, 0, 0};
+    for (int r0 = 0; r0 < A.nrows; r0 += EW_FROWS) {
+        const int nr = min(EW_FROWS, A.nrows - r0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nr * maxslots_per_row; i += blockDim.x) {
+            int rr = i / maxslots_per_row, s = i % maxslots_per_row;
+            int4 row = A.rows[r0 + rr];
+            int ns = 2 * (row.z + 1);
+            T2 v;
+            v.x = v.y = (R)0;
+            if (s < ns) v = ((const T2 *)A.scoef)[A.row_slot[r0 + rr] + s];
+            sC[rr * maxslots_per_row + s] = v;
+        }
+        if (threadIdx.x < nr) sRow[threadIdx.x] = A.rows[r0 + threadIdx.x];
+        __syncthreads();
+        if (!act) continue;
+        R fx = 0, fy = 0, fz = 0;
+        for (int rr = 0; rr < nr; rr++) {
+            const int4 row = sRow[rr];
+            T2 X = tX[(size_t)row.x * A.n + a];
+            T2 Y = tY[(size_t)(row.y < 0 ? -row.y : row.y) * A.n + a];
+            if (row.y < 0) Y.y = -Y.y;
+            const T2 Aa = cmul(X, Y);
+            const T2 *cs = sC + rr * maxslots_per_row;
+            T2 Z;
+            Z.x = (R)1;
+            Z.y = (R)0;
+            R gsum = 0, gz = 0;
+            for (int k = 0; k <= row.z; k++) {
+                const R p1 = Aa.x * Z.x, p2 = Aa.y * Z.y, p3 = Aa.x * Z.y, p4 = Aa.y * Z.x;
+                // W+ = A Z, W- = A conj(Z); g = Im(conj(cS) W) = cS.x W.y - cS.y W.x
+                const T2 cp = cs[2 * k], cm = cs[2 * k + 1];
+                const R gp = cp.x * (p3 + p4) - cp.y * (p1 - p2);
+                const R gm = cm.x * (p4 - p3) - cm.y * (p1 + p2);
+                gsum += gp + gm;
+                gz += (gp - gm) * (R)k;
+                Z = cmul(Z, Z1);
+            }
+            fx += gsum * (R)row.x;
+            fy += gsum * (R)row.y;
+            fz += gz;
+        }
+        F[0] += (double)fx * (double)tx;
+        F[1] += (double)fy * (double)ty;
+        F[2] += (double)fz * (double)tz;
+    }
+    if (!act) return;
+    const double q = A.q[a];
+    A.f[a] += q * F[0];
+    A.f[A.n + a] += q * F[1];
+    A.f[2 * A.n + a] += q * F[2];
+}
+
+}  // namespace
+
+// k-vector rows for the half space and the S(k)-pass tasks
+mg_status mg_ewald_setup(mg_ctx *c) {
+    const mg_params &p = c->params;
+    int KX = p.kmax[0], KY = p.kmax[1], KZ = p.kmax[2], KS = p.ksqmax;
+    std::vector<int> rows, slot_start, slot_row;
+    std::vector<int> tasks;
+    int nslots = 0;
+    long long kvec = 0;
+    int maxslots = 2;
+    for (int kx = 0; kx <= KX; kx++)
+        for (int ky = -KY; ky <= KY; ky++) {
+            if (kx == 0 && ky < 0) continue;
+            int rem = KS - kx * kx - ky * ky;
+            if (rem < 0) continue;
+            int kzmax = std::min(KZ, (int)floor(sqrt((double)rem)));
+            while ((kzmax + 1) <= KZ && (kzmax + 1) * (kzmax + 1) <= rem) kzmax++;
+            while (kzmax >= 0 && kzmax * kzmax > rem) kzmax--;
+            int half = (kx == 0 && ky == 0) ? 1 : 0;
+            if (half && kzmax < 1) continue;
+            if (kzmax < 0) continue;
+            int r = (int)(rows.size() / 4);
+            rows.push_back(kx);
+            rows.push_back(ky);
+            rows.push_back(kzmax);
+            rows.push_back(half);
+            slot_start.push_back(nslots);
+            int ns = 2 * (kzmax + 1);
+            for (int s = 0; s < ns; s++) slot_row.push_back(r);
+            nslots += ns;
+            maxslots = std::max(maxslots, ns);
+            kvec += half ? kzmax : 2 * kzmax + 1;
+            for (int k0 = 0; k0 <= kzmax; k0 += EW_CH) {
+                tasks.push_back(r);
+                tasks.push_back(k0);
+            }
+        }
+    c->nrows = (int)(rows.size() / 4);
+    c->nslots = nslots;
+    c->kvectors = kvec;
+    c->ntasks = (int)(tasks.size() / 2);
+    c->kmaxx = KX;
+    c->kmaxy = KY;
+    c->kmaxz = KZ;
+    c->h_rows = rows;
+    c->ewald_box[0] = c->lx;
+    c->ewald_box[1] = c->ly;
+    c->ewald_box[2] = c->lz;
+    if (c->nrows == 0) return MG_OK;
+    std::vector<int> packed(slot_start.size() + slot_row.size() + 1);
+    std::copy(slot_start.begin(), slot_start.end(), packed.begin());
+    std::copy(slot_row.begin(), slot_row.end(), packed.begin() + slot_start.size());
+    packed.back() = maxslots;
+    if (!mg_ensure(c, c->d_rows, sizeof(int) * rows.size()) || !mg_ensure(c, c->d_row_slot, sizeof(int) * packed.size()) ||
+        !mg_ensure(c, c->d_tasks, sizeof(int) * tasks.size()))
+        return MG_ERR_ALLOC;
+    MG_CUDA(cudaMemcpy(c->d_rows.p, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(c->d_row_slot.p, packed.data(), sizeof(int) * packed.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(c->d_tasks.p, tasks.data(), sizeof(int) * tasks.size(), cudaMemcpyHostToDevice));
+    return MG_OK;
+}
+
+mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl) {
+    if (c->nrows == 0) return MG_OK;
+    const mg_params &p = c->params;
+    const int n = c->natom;
+    const bool fp64 = c->opt.precision == MG_PREC_FP64;
+    const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
+    const int KX = c->kmaxx, KY = c->kmaxy, KZ = std::max(c->kmaxz, 1);
+    const size_t tab_entries = (size_t)(KX + 1 + KY + 1 + KZ + 1) * n;
+    const int nblk = (n + EW_SITES - 1) / EW_SITES;
+    if (!mg_ensure(c, c->d_phase, esz * tab_entries) ||
+        !mg_ensure(c, c->d_spart, sizeof(double) * 2 * (size_t)c->nslots * nblk) ||
+        !mg_ensure(c, c->d_scoef, esz * (size_t)c->nslots))
+        return MG_ERR_ALLOC;
+    const double twopi = 6.283185307179586;
+    double sc[3] = {p.twopi_lx / twopi, p.twopi_ly / twopi, p.twopi_lz / twopi};
+    cudaStream_t s = c->stream;
+    if (fp64)
+        k_phase_d<<<(n + 127) / 128, 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (double2 *)c->d_phase.p);
+    else
+        k_phase_f<<<(n + 127) / 128, 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)c->d_phase.p);
+    EwArgs A;
+    A.n = n;
+    A.nrows = c->nrows;
+    A.nslots = c->nslots;
+    A.ntasks = c->ntasks;
+    A.kx = KX;
+    A.ky = KY;
+    A.kz = KZ;
+    A.rows = (const int4 *)c->d_rows.p;
+    A.row_slot = (const int *)c->d_row_slot.p;
+    A.tasks = (const int2 *)c->d_tasks.p;
+    A.tab = c->d_phase.p;
+    A.q = (const double *)c->d_site_q.p;
+    A.spart = (double *)c->d_spart.p;
+    A.scoef = c->d_scoef.p;
+    A.twopi[0] = p.twopi_lx;
+    A.twopi[1] = p.twopi_ly;
+    A.twopi[2] = p.twopi_lz;
+    A.bfac = p.bfactor_ewald;
+    A.vfac = p.vfactor_ewald;
+    A.coul = p.coulomb_prefactor;
+    A.rows_e = (double *)c->d_epart.p;
+    A.f = fl;
+    const int P = EW_TILE + 1;
+    size_t smem = esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
+    dim3 grid((c->ntasks + EW_TPB - 1) / EW_TPB, nblk);
+    if (fp64) {
+        MG_CUDA(cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
+    } else {
+        MG_CUDA(cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
+    }
+    MG_CUDA(cudaGetLastError());
+    if (c->timing) cudaEventRecord(c->ev[4], s);
+    const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
+    int maxslots = 0;
+    for (int r = 0; r < c->nrows; r++) maxslots = std::max(maxslots, 2 * (c->h_rows[4 * r + 2] + 1));
+    unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
+    A.row0 = mg_reserve_rows(c, rblocks);
+    if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
+    if (fp64)
+        k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+    else
+        k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+    size_t fsmem = esz * (size_t)EW_FROWS * maxslots;
+    if (fp64) {
+        MG_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_kforce<double><<<(n + 255) / 256, 256, fsmem, s>>>(A, maxslots);
+    } else {
+        MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_kforce<float><<<(n + 255) / 256, 256, fsmem, s>>>(A, maxslots);
+    }
+    MG_CUDA(cudaGetLastError());
+    c->launches += 4;
+    return MG_OK;
+}

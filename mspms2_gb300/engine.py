@@ -1,0 +1,224 @@
+"""Host-side wrapper of the engine's C ABI (include/mspms2_gb300.h).
+
+`Engine(system)` mirrors what the reference does around its force layer: it takes the
+molecule templates and globals of a `System`, and `compute()` plays the role of one
+frclong() + frcshort() pair (src/frclong.c:20, src/frcshort.c:20) on the GPU, returning
+forces in the reference's layout (x/y/z arrays per site) and the reference's energy
+names. There is no CPU path: without the compiled library or an sm_103 device the
+constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import capi
+from .capi import MgEnergies, MgOptions, MgSpecies, MgStats, SpeciesPack
+from .system import SF_ATOM_EXPLICIT, SF_HYPERGEO, SF_MY_INTERP, SF_TASOS, System, derive_params
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmspms2_gb300.so")
+
+MG_OK, MG_ERR_NONFINITE = 0, 6
+TERMS_LONG, TERMS_SHORT, TERMS_ALL = 1, 2, 3
+PREC = {"mixed": 0, "fp64": 1}
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NO_DEVICE", 4: "STATE", 5: "OUT_OF_GRID", 6: "NONFINITE",
+          7: "CAPACITY", 8: "UNSUPPORTED", 9: "ALLOC"}
+
+_dp = C.POINTER(C.c_double)
+_lib = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mspms2_gb300 {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the in-tree CUDA library (build it first with mspms2_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise EngineError(2, f"{path} is missing; run mspms2_gb300.build.build()")
+    lib = C.CDLL(path)
+    V, I, D = C.c_void_p, C.c_int, C.c_double
+    lib.mg_create.argtypes = [C.POINTER(V), C.POINTER(MgOptions)]
+    lib.mg_destroy.argtypes = [V]
+    lib.mg_last_error.argtypes = [V]
+    lib.mg_last_error.restype = C.c_char_p
+    lib.mg_options_default.argtypes = [C.POINTER(MgOptions)]
+    lib.mg_params_derive.argtypes = [C.POINTER(capi.MgParams), D, D, D]
+    lib.mg_params_derive.restype = None
+    lib.mg_set_topology.argtypes = [V, I, C.POINTER(MgSpecies)]
+    lib.mg_set_params.argtypes = [V, C.POINTER(capi.MgParams)]
+    lib.mg_set_box.argtypes = [V, D, D, D]
+    lib.mg_set_stream.argtypes = [V, V]
+    lib.mg_set_timing.argtypes = [V, I]
+    lib.mg_sf_tasos_set_grid.argtypes = [V, I, I, I, I, D, D, D, D, _dp]
+    lib.mg_sf_hypergeo_set.argtypes = [V, I, _dp, _dp, _dp, D, D, D]
+    lib.mg_sf_atom_explicit_set.argtypes = [V, I, _dp, _dp, _dp, D, D]
+    lib.mg_sf_myinterp_set.argtypes = [V, I, I, I, I, D, D, D, D, D, D, _dp]
+    lib.mg_compute.argtypes = [V, _dp, _dp, _dp, I, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(MgEnergies)]
+    lib.mg_compute_device.argtypes = [V, V, V, V, I, V, V, V, V, V, V, C.POINTER(MgEnergies)]
+    lib.mg_get_stats.argtypes = [V, C.POINTER(MgStats)]
+    lib.mg_get_device_flags.argtypes = [V, C.POINTER(C.c_uint)]
+    lib.mg_debug_get_list.argtypes = [V, C.POINTER(I), C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I),
+                                      C.POINTER(I), C.POINTER(I)]
+    lib.mg_abi_version.restype = I
+    _lib = lib
+    return lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+class Engine:
+    """One system on one GPU."""
+
+    def __init__(self, system: System, precision: str = "mixed", skin: float = 0.0, device: int = 0,
+                 params: capi.MgParams | None = None):
+        self.lib = load_library()
+        self.system = system
+        self.n = system.natom
+        opt = MgOptions()
+        self.lib.mg_options_default(C.byref(opt))
+        opt.precision = PREC[precision]
+        opt.skin = skin
+        opt.device = device
+        self.ctx = C.c_void_p()
+        st = self.lib.mg_create(C.byref(self.ctx), C.byref(opt))
+        if st != MG_OK:
+            raise EngineError(st, "mg_create failed (an sm_103 GPU is required)")
+        self.precision = precision
+        self._pack = SpeciesPack(system)
+        self.params = params if params is not None else capi.system_params(system)
+        self._check(self.lib.mg_set_params(self.ctx, C.byref(self.params)))
+        self._check(self.lib.mg_set_topology(self.ctx, self._pack.n, self._pack.array))
+        self._check(self.lib.mg_set_box(self.ctx, *(float(v) for v in system.box)))
+        self._load_solid(system)
+
+    def _check(self, st: int) -> int:
+        if st != MG_OK:
+            raise EngineError(st, self.lib.mg_last_error(self.ctx).decode(errors="replace"))
+        return st
+
+    def _load_solid(self, s: System) -> None:
+        if s.sf_type == SF_TASOS:
+            for i, g in enumerate(s.tasos):
+                v = np.ascontiguousarray(g.values, dtype=np.float64)
+                self._check(self.lib.mg_sf_tasos_set_grid(self.ctx, i + 1, g.nx, g.ny, g.nz, g.hx, g.hy, g.hz,
+                                                          g.cuc, _p(v)))
+        elif s.sf_type == SF_HYPERGEO:
+            t = np.ascontiguousarray(np.asarray(s.tube_xy_r, dtype=np.float64).T)
+            self._check(self.lib.mg_sf_hypergeo_set(self.ctx, t.shape[1], _p(t[0]), _p(t[1]), _p(t[2]),
+                                                    s.solid_sigma, s.solid_epsilon, s.const_3pisq_theta))
+        elif s.sf_type == SF_ATOM_EXPLICIT:
+            t = np.ascontiguousarray(np.asarray(s.solid_xyz, dtype=np.float64).T)
+            self._check(self.lib.mg_sf_atom_explicit_set(self.ctx, t.shape[1], _p(t[0]), _p(t[1]), _p(t[2]),
+                                                         s.solid_sigma, s.solid_epsilon))
+        elif s.sf_type == SF_MY_INTERP:
+            for i, g in enumerate(s.myinterp):
+                c = np.ascontiguousarray(g.coeff, dtype=np.float64)
+                self._check(self.lib.mg_sf_myinterp_set(self.ctx, i, g.ncx, g.ncy, g.ncz, *g.itvl, g.xmin, g.ymin,
+                                                        g.zmax, _p(c)))
+
+    def set_box(self, lx: float, ly: float, lz: float, params: capi.MgParams | None = None) -> None:
+        if params is not None:
+            self.params = params
+            self._check(self.lib.mg_set_params(self.ctx, C.byref(params)))
+        self._check(self.lib.mg_set_box(self.ctx, lx, ly, lz))
+
+    def set_params(self, params: capi.MgParams) -> None:
+        self.params = params
+        self._check(self.lib.mg_set_params(self.ctx, C.byref(params)))
+
+    def set_stream(self, stream_handle: int) -> None:
+        self._check(self.lib.mg_set_stream(self.ctx, C.c_void_p(stream_handle)))
+
+    def set_timing(self, on: bool) -> None:
+        self._check(self.lib.mg_set_timing(self.ctx, 1 if on else 0))
+
+    def compute(self, x=None, y=None, z=None, terms: int = TERMS_ALL, allow_nonfinite: bool = False):
+        """Forces (long [3,n], short [3,n]) and energies for positions on the host."""
+        s = self.system
+        x = np.ascontiguousarray(s.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(s.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(s.z if z is None else z, dtype=np.float64)
+        fl = np.zeros((3, self.n))
+        fs = np.zeros((3, self.n))
+        e = MgEnergies()
+        st = self.lib.mg_compute(self.ctx, _p(x), _p(y), _p(z), terms, _p(fl[0]), _p(fl[1]), _p(fl[2]),
+                                 _p(fs[0]), _p(fs[1]), _p(fs[2]), C.byref(e))
+        if not (allow_nonfinite and st == MG_ERR_NONFINITE):
+            self._check(st)
+        return fl, fs, e.as_dict()
+
+    def compute_into(self, x: np.ndarray, y: np.ndarray, z: np.ndarray, fl: np.ndarray, fs: np.ndarray,
+                     terms: int = TERMS_ALL) -> dict:
+        """Host-buffer call with caller-owned (e.g. pinned) arrays; fl, fs are [3, n]."""
+        e = MgEnergies()
+        self._check(self.lib.mg_compute(self.ctx, _p(x), _p(y), _p(z), terms, _p(fl[0]), _p(fl[1]), _p(fl[2]),
+                                        _p(fs[0]), _p(fs[1]), _p(fs[2]), C.byref(e)))
+        return e.as_dict()
+
+    def compute_device(self, dx: int, dy: int, dz: int, dfl, dfs, terms: int = TERMS_ALL) -> dict:
+        """Device pointers in (x, y, z) and out (each force block a [3][n] FP64 array)."""
+        n = self.n
+        e = MgEnergies()
+        fl = [dfl, dfl + 8 * n, dfl + 16 * n] if dfl else [None] * 3
+        fs = [dfs, dfs + 8 * n, dfs + 16 * n] if dfs else [None] * 3
+        self._check(self.lib.mg_compute_device(self.ctx, dx, dy, dz, terms, *fl, *fs, C.byref(e)))
+        return e.as_dict()
+
+    def stats(self) -> dict:
+        st = MgStats()
+        self._check(self.lib.mg_get_stats(self.ctx, C.byref(st)))
+        return {"pairs_within_cutoff": st.pairs_within_cutoff, "cluster_pairs": st.cluster_pairs,
+                "nclusters": st.nclusters, "kvectors": st.kvectors, "list_rebuilt": st.list_rebuilt,
+                "list_builds": st.list_builds, "kernel_ms": list(st.kernel_ms),
+                "kernel_launches": st.kernel_launches}
+
+    def device_flags(self) -> int:
+        f = C.c_uint()
+        self._check(self.lib.mg_get_device_flags(self.ctx, C.byref(f)))
+        return f.value
+
+    def debug_list(self):
+        ncl, npairs = C.c_int(), C.c_longlong()
+        grid = (C.c_int * 3)()
+        self._check(self.lib.mg_debug_get_list(self.ctx, C.byref(ncl), C.byref(npairs), grid, None, None, None))
+        cl = np.zeros(ncl.value * 8, np.int32)
+        pairs = np.zeros(2 * npairs.value, np.int32)
+        shifts = np.zeros(3 * npairs.value, np.int32)
+        ip = C.POINTER(C.c_int)
+        self._check(self.lib.mg_debug_get_list(self.ctx, C.byref(ncl), C.byref(npairs), grid,
+                                               cl.ctypes.data_as(ip), pairs.ctypes.data_as(ip),
+                                               shifts.ctypes.data_as(ip)))
+        return {"grid": list(grid), "clusters": cl.reshape(-1, 8), "pairs": pairs.reshape(-1, 2),
+                "shifts": shifts.reshape(-1, 3)}
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None) and self.ctx.value:
+            self.lib.mg_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def derive(system: System) -> dict:
+    return derive_params(system)

@@ -87,11 +87,16 @@ int orc_tasos_force(const orc_tasos *g, unsigned compat, double x, double y, dou
                     double *pe, double force[3]);
 double orc_tasos_min_pe(const orc_tasos *g);
 
-/* CPU cluster-pair builder (same predicate, same op order as the GPU build). */
+/* CPU cluster-pair builder (same predicate, same op order as the GPU build); the
+ * second form takes the column grid and small-box choice of the build under test. */
 int orc_nblist_build(const double *x, const double *y, const double *z, int natom,
                      double lx, double ly, double lz, double rlist,
                      int *out_ncl, int *cluster_atoms, int cluster_cap,
                      long long *out_npairs, int *pairs, int *shifts, long long pair_cap);
+int orc_nblist_build2(const double *x, const double *y, const double *z, int natom, double lx,
+                      double ly, double lz, double rlist, int ncx, int ncy, int small, int *out_ncl,
+                      int *cluster_atoms, int cluster_cap, long long *out_npairs, int *pairs,
+                      int *shifts, long long pair_cap);
 
 #ifdef __cplusplus
 }

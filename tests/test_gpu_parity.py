@@ -1,0 +1,120 @@
+"""GPU parity: the engine, called through its C ABI, against the compiled reference's
+golden vectors and the CPU oracle.
+
+Tolerances (norm-wise relative error of each force block, relative error of each
+energy): FP64 path 1e-10; mixed path (FP32 pair arithmetic, FP64 accumulation) 1e-5,
+the force tolerance the benchmark contract states.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases
+from mspms2_gb300 import build
+from mspms2_gb300.capi import ENERGY_NAMES
+from mspms2_gb300.engine import TERMS_ALL, TERMS_LONG, TERMS_SHORT, Engine
+from mspms2_gb300.system import load_system
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-10, "mixed": 1e-5}
+LONG_E = ["uvdw", "ushift", "ureal", "uexcl", "ufourier", "uself", "uvacuum", "uelec", "usflj", "uinter",
+          "virial_inter"]
+SHORT_E = ["ubond", "uangle", "udih", "uimp", "uintra", "virial_intra"]
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    build.build()
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def energy_scale(ref):
+    return max(abs(v) for v in ref.values())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("case", golden_cases())
+def test_engine_matches_reference(case, prec):
+    s, d = load_system(os.path.join(GOLDEN, case + ".npz"))
+    ref = dict(zip(ENERGY_NAMES, d["ref_energies"]))
+    with Engine(s, precision=prec) as eng:
+        fl, fs, e = eng.compute()
+    tol = TOL[prec]
+    assert rel(fl, d["ref_fl"]) <= tol, (case, prec, rel(fl, d["ref_fl"]))
+    assert rel(fs, d["ref_fs"]) <= tol, (case, prec, rel(fs, d["ref_fs"]))
+    scale = energy_scale(ref)
+    for k in LONG_E + SHORT_E:
+        # each component to tol relative, or to tol of the largest energy when it is a
+        # small difference of large terms
+        assert abs(e[k] - ref[k]) <= tol * max(abs(ref[k]), 1e-3 * scale), (case, prec, k, e[k], ref[k])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_deterministic(prec):
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    with Engine(s, precision=prec) as eng:
+        a = eng.compute()
+        b = eng.compute()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert a[2] == b[2]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_respa_split_sums_to_full(prec):
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    with Engine(s, precision=prec) as full:
+        fl, fs, e = full.compute()
+    s.respa_split = 6.0
+    with Engine(s, precision=prec) as sp:
+        fl_o, _, e_o = sp.compute(terms=TERMS_LONG)
+        _, fs_i, e_i = sp.compute(terms=TERMS_SHORT)
+        fl_a, fs_a, e_a = sp.compute(terms=TERMS_ALL)
+    tol = TOL[prec]
+    assert rel(fl_o + fs_i, fl + fs) <= tol
+    assert rel(fl_a + fs_a, fl + fs) <= tol
+    for k in ("uvdw", "ureal", "uelec", "uinter", "virial_inter", "uintra"):
+        assert abs(e_o[k] + e_i[k] - (e[k] + (0 if k != "uinter" else 0))) <= tol * max(1.0, abs(e[k])) * 10, k
+        assert abs(e_a[k] - e[k]) <= tol * max(1.0, abs(e[k])) * 10, k
+
+
+def test_skin_reuse_matches_rebuild():
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    rng = np.random.default_rng(5)
+    x1, y1, z1 = (v + rng.uniform(-0.2, 0.2, size=v.shape) for v in (s.x, s.y, s.z))
+    with Engine(s, precision="fp64", skin=1.0) as a, Engine(s, precision="fp64") as b:
+        a.compute()
+        assert a.stats()["list_rebuilt"] == 1
+        fa = a.compute(x1, y1, z1)
+        assert a.stats()["list_rebuilt"] == 0
+        fb = b.compute(x1, y1, z1)
+    assert rel(fa[0], fb[0]) <= 1e-12 and rel(fa[1], fb[1]) <= 1e-12
+
+
+@pytest.mark.parametrize("case", ["water_ewald_512", "lj_fluid_500", "water_wolf_216"])
+def test_neighbour_list_bit_exact(case):
+    from oracle.pyoracle import nblist
+    s, _ = load_system(os.path.join(GOLDEN, case + ".npz"))
+    with Engine(s, precision="mixed") as eng:
+        eng.compute(terms=TERMS_LONG)
+        g = eng.debug_list()
+    rlist = max(s.rcutoff, s.rcutoffelec)
+    c = nblist(s.x, s.y, s.z, tuple(float(v) for v in s.box), rlist, g["grid"][0], g["grid"][1], g["grid"][2])
+    assert np.array_equal(g["clusters"], c["clusters"])
+    assert np.array_equal(g["pairs"], c["pairs"])
+    assert np.array_equal(g["shifts"], c["shifts"])
+
+
+def test_pair_count_matches_oracle():
+    from oracle.pyoracle import Oracle
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    with Engine(s, precision="fp64") as eng:
+        eng.compute(terms=TERMS_LONG)
+        npair = eng.stats()["pairs_within_cutoff"]
+    want = Oracle(s).count_pairs(max(s.rcutoff, s.rcutoffelec))
+    assert abs(npair - want) <= 2
