@@ -245,11 +245,12 @@ MG_API mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);
 
 /* ---- neighbour-list inspection (tests of the bit-exact list build) ----------- */
 /* Copies the cluster layout and cluster-pair list of the last build:
- * grid[3] = (columns along x, columns along y, small-box flag), cluster_atoms[ncl*8]
- * (site index or -1), pairs[npairs*2] (i-cluster, j-cluster), shifts[npairs*3] (the
- * periodic image of the j-cluster in box lengths). Pass NULL buffers to query ncl
- * and npairs. */
-MG_API mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *grid,
+ * grid[3] = (columns along x, columns along y, small-box flag), *zcap = the largest z
+ * extent of a cluster, cluster_atoms[ncl*8] (site index or -1), pairs[npairs*2]
+ * (i-cluster, j-cluster, grouped by i-cluster in search order), shifts[npairs*3] (the
+ * periodic image of the j-cluster in box lengths). Pass NULL buffers to query ncl and
+ * npairs. */
+MG_API mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *grid, double *zcap,
                             int *cluster_atoms, int *pairs, int *shifts);
 
 #ifdef __cplusplus

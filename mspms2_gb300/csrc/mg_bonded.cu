@@ -20,6 +20,7 @@ template <>
 struct M<float> {
     __device__ static float sqrt_(float x) { return sqrtf(x); }
     __device__ static float erfc_(float x) { return erfcf(x); }
+    __device__ static float erf_(float x) { return erff(x); }
     __device__ static float exp_(float x) { return expf(x); }
     __device__ static float log_(float x) { return logf(x); }
     __device__ static float acos_(float x) { return acosf(x); }
@@ -31,6 +32,7 @@ template <>
 struct M<double> {
     __device__ static double sqrt_(double x) { return sqrt(x); }
     __device__ static double erfc_(double x) { return erfc(x); }
+    __device__ static double erf_(double x) { return erf(x); }
     __device__ static double exp_(double x) { return exp(x); }
     __device__ static double log_(double x) { return log(x); }
     __device__ static double acos_(double x) { return acos(x); }
@@ -166,6 +168,31 @@ __global__ void k_intra(MolArgs A) {
                 }
             }
             if (ct == MG_ELEC_NONE) continue;
+            if (ip.kind == 0 && same && (ct == MG_ELEC_EWALD || ct == MG_ELEC_WOLF)) {
+                // Not straddling: the exclusion and the real-space term use the same vector
+                // (the minimum image changes nothing), and their forces, each ~C q q / r^2,
+                // nearly cancel. They are combined through erf = 1 - erfc before rounding;
+                // the two energies are still accumulated separately.
+                R r2 = (R)(dx * dx + dy * dy + dz * dz);
+                if (!(r2 < (R)p.rcutoffelecsq)) continue;
+                R r = M<R>::sqrt_(r2);
+                R kr = (R)p.kappa * r;
+                R bare = (R)p.coulomb_prefactor * qq / r;
+                R ex = M<R>::exp_(-kr * kr), ef = M<R>::erf_(kr), ec = M<R>::erfc_(kr);
+                R fsum;
+                if (ct == MG_ELEC_EWALD) {
+                    eng[1] += bare * ec;
+                    fsum = bare * ((R)2 * kr * ex * (R)0.5641895835477563 - ef) / r2;
+                } else {
+                    eng[1] += (R)p.coulomb_prefactor * qq *
+                              (ec / r + (R)p.wolfvcon1 + (R)p.wolfvcon2 * (r - (R)p.rcutoffelec));
+                    fsum = bare * (-ef / r2 + (R)p.wolffcon1 * ex / r + (R)p.wolffcon2);
+                    eng[4] += (double)(fsum * r2);
+                }
+                eng[2] += bare;
+                addf(A.f, n, ii, jj, (double)fsum * dx, (double)fsum * dy, (double)fsum * dz);
+                continue;
+            }
             if (ip.kind == 0) {
                 if (ct != MG_ELEC_EWALD && ct != MG_ELEC_WOLF) continue;
                 R r2 = (R)(dx * dx + dy * dy + dz * dz);
@@ -249,14 +276,18 @@ __global__ void k_bonded(MolArgs A) {
             const BondedTerm T = A.bonded[S.bonded_off + k];
             const int a0 = base + T.idx[0], a1 = base + T.idx[1], a2 = base + T.idx[2], a3 = base + T.idx[3];
             if (T.kind == 0) {
-                R rx = (R)(A.x[a0] - A.x[a1]), ry = (R)(A.y[a0] - A.y[a1]), rz = (R)(A.z[a0] - A.z[a1]);
-                R r2 = rx * rx + ry * ry + rz * rz, r = M<R>::sqrt_(r2), u, f;
+                // the bond length and its stretch r - r0 are formed in FP64: near equilibrium
+                // the stretch is a few ulps of r in FP32
+                const double dxd = A.x[a0] - A.x[a1], dyd = A.y[a0] - A.y[a1], dzd = A.z[a0] - A.z[a1];
+                const double r2d = dxd * dxd + dyd * dyd + dzd * dzd, rd = sqrt(r2d);
+                R rx = (R)dxd, ry = (R)dyd, rz = (R)dzd;
+                R r2 = (R)r2d, r = (R)rd, u, f;
                 if (T.type == MG_BOND_HARMONIC) {
-                    R dr = r - (R)T.p[1];
+                    R dr = (R)(rd - T.p[1]);
                     u = (R)0.5 * (R)T.p[0] * dr * dr;
                     f = -(R)T.p[0] * dr / r;
                 } else if (T.type == MG_BOND_MORSE) {
-                    R dr = r - (R)T.p[1];
+                    R dr = (R)(rd - T.p[1]);
                     R ex = M<R>::exp_(-(R)T.p[2] * dr);
                     R om = (R)1 - ex;
                     u = (R)T.p[0] * om * om;
@@ -292,13 +323,18 @@ __global__ void k_bonded(MolArgs A) {
                     fx[a1] -= (double)fxa + (double)fxc; fy[a1] -= (double)fya + (double)fyc; fz[a1] -= (double)fza + (double)fzc;
                     fx[a2] += fxc; fy[a2] += fyc; fz[a2] += fzc;
                 } else if (T.type == MG_ANGLE_TR_WATER) {
-                    R v13x = (R)(A.x[a0] - A.x[a2]), v13y = (R)(A.y[a0] - A.y[a2]), v13z = (R)(A.z[a0] - A.z[a2]);
-                    R v12x = (R)(A.x[a0] - A.x[a1]), v12y = (R)(A.y[a0] - A.y[a1]), v12z = (R)(A.z[a0] - A.z[a1]);
-                    R v23x = (R)(A.x[a1] - A.x[a2]), v23y = (R)(A.y[a1] - A.y[a2]), v23z = (R)(A.z[a1] - A.z[a2]);
-                    R r13 = M<R>::sqrt_(v13x * v13x + v13y * v13y + v13z * v13z);
-                    R r12 = M<R>::sqrt_(v12x * v12x + v12y * v12y + v12z * v12z);
-                    R r23 = M<R>::sqrt_(v23x * v23x + v23y * v23y + v23z * v23z);
-                    R d3 = r13 - (R)T.p[3], d1 = r12 - (R)T.p[4], d2 = r23 - (R)T.p[4];
+                    const double w13x = A.x[a0] - A.x[a2], w13y = A.y[a0] - A.y[a2], w13z = A.z[a0] - A.z[a2];
+                    const double w12x = A.x[a0] - A.x[a1], w12y = A.y[a0] - A.y[a1], w12z = A.z[a0] - A.z[a1];
+                    const double w23x = A.x[a1] - A.x[a2], w23y = A.y[a1] - A.y[a2], w23z = A.z[a1] - A.z[a2];
+                    R v13x = (R)w13x, v13y = (R)w13y, v13z = (R)w13z;
+                    R v12x = (R)w12x, v12y = (R)w12y, v12z = (R)w12z;
+                    R v23x = (R)w23x, v23y = (R)w23y, v23z = (R)w23z;
+                    // lengths and stretches in FP64 (see the bond case)
+                    const double l13 = sqrt(w13x * w13x + w13y * w13y + w13z * w13z);
+                    const double l12 = sqrt(w12x * w12x + w12y * w12y + w12z * w12z);
+                    const double l23 = sqrt(w23x * w23x + w23y * w23y + w23z * w23z);
+                    R r13 = (R)l13, r12 = (R)l12, r23 = (R)l23;
+                    R d3 = (R)(l13 - T.p[3]), d1 = (R)(l12 - T.p[4]), d2 = (R)(l23 - T.p[4]);
                     R kt = (R)T.p[0], krt = (R)T.p[1], krr = (R)T.p[2];
                     eng[1] += (double)((R)0.5 * kt * d3 * d3 + krt * d3 * (d1 + d2) + krr * d1 * d2);
                     R t1 = -kt * d3 / r13, t21 = -krt * d3 / r12, t22 = -krt * (d1 + d2) / r13, t3 = -krr * d2 / r12;

@@ -550,8 +550,10 @@ static void assemble_energies(mg_ctx *c, const double *E, int want_long, int wan
     }
 }
 
-static mg_status compute_impl(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
-                              double *fl, double *fs, mg_energies *e) {
+// One attempt; *retry is set when the list set-up must change and the call be repeated.
+static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
+                              double *fl, double *fs, mg_energies *e, bool *retry) {
+    *retry = false;
     if (!c->have_topology || !c->have_params || !c->have_box)
         return mg_fail(c, MG_ERR_STATE, "set topology, params and box before computing");
     const mg_params &p = c->params;
@@ -577,7 +579,7 @@ static mg_status compute_impl(mg_ctx *c, const double *dx, const double *dy, con
     }
     // energy partial rows: an upper bound of the blocks every stage may launch
     {
-        long long rows = (need_pairs ? (c->ncl + 3) / 4 : 0) + 4LL * ((c->nmole + 127) / 128) +
+        long long rows = (need_pairs ? (c->cl_cap + 3) / 4 : 0) + 4LL * ((c->nmole + 127) / 128) +
                          (c->natom + 127) / 128 + (c->nslots + 255) / 256 + 16;
         if (!mg_ensure(c, c->d_epart, sizeof(double) * E_NCOMP * (size_t)rows)) return MG_ERR_ALLOC;
         c->epart_cap = (int)(c->d_epart.bytes / (sizeof(double) * E_NCOMP));
@@ -612,11 +614,23 @@ static mg_status compute_impl(mg_ctx *c, const double *dx, const double *dy, con
     if (c->timing) cudaEventRecord(c->ev[7], s);
     double E[E_NCOMP + 8];
     unsigned flags[4];
+    int meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     MG_CUDA(cudaMemcpyAsync(E, c->d_eout.p, sizeof(double) * E_NCOMP, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaMemcpyAsync(flags, c->d_flags.p, sizeof(unsigned) * 4, cudaMemcpyDeviceToHost, s));
+    if (need_pairs) MG_CUDA(cudaMemcpyAsync(meta, c->d_meta.p, sizeof(meta), cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaStreamSynchronize(s));
     MG_CUDA(cudaGetLastError());
     c->last_flags = flags[0];
+    if (need_pairs) {
+        if (mg_list_retry(c, flags[0], meta)) {
+            *retry = true;
+            return MG_OK;
+        }
+        c->ncl = meta[0];
+        c->npairs = c->small_box ? (long long)meta[0] * meta[0] : *(long long *)(meta + 4);
+        c->list_rebuilt = meta[3] != c->list_builds;
+        c->list_builds = meta[3];
+    }
     mg_energies en;
     assemble_energies(c, E, want_long, want_short, &en);
     if (e) *e = en;
@@ -644,6 +658,16 @@ static mg_status compute_impl(mg_ctx *c, const double *dx, const double *dy, con
         return mg_fail(c, MG_ERR_CAPACITY, "neighbour-list capacity exceeded");
     if (flags[0] & MG_FLAG_NONFINITE) return mg_fail(c, MG_ERR_NONFINITE, "non-finite force");
     return MG_OK;
+}
+
+static mg_status compute_impl(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
+                              double *fl, double *fs, mg_energies *e) {
+    for (int attempt = 0; attempt < 6; attempt++) {
+        bool retry = false;
+        mg_status st = compute_once(c, dx, dy, dz, terms, fl, fs, e, &retry);
+        if (st || !retry) return st;
+    }
+    return mg_fail(c, MG_ERR_CAPACITY, "neighbour-list set-up did not converge");
 }
 
 extern "C" mg_status mg_compute_device(mg_ctx *c, const double *dx, const double *dy, const double *dz,

@@ -33,6 +33,7 @@
 #define MG_FLAG_LIST_OVERFLOW 4u
 #define MG_FLAG_COLUMN_OVERFLOW 8u
 #define MG_FLAG_IMPROPER_DEGENERATE 16u
+#define MG_FLAG_SMALL_BOX 32u  // a cluster pair needs two images: use the small-box list
 
 // per-site flags packed next to the molecule id
 #define MG_SITE_LJ 1        // takes part in LJ (ghost type NONE)
@@ -144,7 +145,12 @@ struct mg_ctx {
     bool list_valid = false;
     int list_builds = 0, list_rebuilt = 0;
     DevBuf d_col_count, d_col_start, d_col_fill, d_col_cl_start, d_col_sorted;
-    DevBuf d_cl_atom, d_cl_ref, d_cl_bb, d_cl_col;
+    DevBuf d_cl_atom, d_cl_ref, d_cl_bb, d_cl_col, d_cl_bbf, d_col_ncl, d_counter;
+    double zcap = 0;           // largest z extent of a cluster
+    bool small_box_forced = false;
+    int col_refine = 0;        // column-grid refinements after overflows
+    int cl_cap = 0;            // cluster capacity
+    long long pair_cap = 0;    // cluster-pair entry capacity
     DevBuf d_pair_start, d_pair_count, d_pair_j, d_pair_shift;
     DevBuf d_pack_pos, d_pack_lj, d_pack_info;
     // reciprocal space
@@ -198,6 +204,7 @@ mg_status mg_launch_coulomb_mole(mg_ctx *c, const double *dx, const double *dy, 
 mg_status mg_launch_sf(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl);
 mg_status mg_launch_reduce(mg_ctx *c);
 mg_status mg_launch_check(mg_ctx *c, const double *f, int n);
+bool mg_list_retry(mg_ctx *c, unsigned flags, const int *meta_host);
 
 // Energy partial rows: every block of every stage writes one full row of E_NCOMP
 // FP64 values (zeros outside its own components); rows are reserved in launch order

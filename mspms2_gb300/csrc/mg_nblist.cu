@@ -1,22 +1,39 @@
 // mg_nblist.cu - cluster build and cluster-pair (Verlet) list on the GPU.
 //
 // Replaces the O(N^2) site-pair scan of src/frclong.c:56-218 with a list of pairs of
-// 8-site clusters. The list is a deterministic function of the FP64 positions:
+// clusters of at most 8 sites. The list is a deterministic function of the FP64
+// positions:
 //   1. sites are binned into an ncx x ncy grid of columns by their wrapped FP64
-//      position (x - L*floor(x/L));
-//   2. each column is sorted by (wrapped z, site index) on chip, then cut into clusters
-//      of 8 consecutive sites (the last one padded with -1);
+//      position (x - L*floor(x/L)); the column width is min((8/density)^(1/3),
+//      0.75*rlist), so clusters stay compact even in dilute systems;
+//   2. each column is sorted by (wrapped z, site index) on chip and cut into clusters
+//      of consecutive sites: a new cluster starts after 8 sites or when a site lies more
+//      than the column width above the cluster's first site;
 //   3. an i-cluster lists j-cluster J under periodic image s when the FP64 distance
 //      between their bounding boxes is below rlist = max(rcutoff, rcutoffelec) + skin.
-// Every FP64 operation of the predicate uses explicit round-to-nearest intrinsics, so
-// the CPU builder in oracle/nblist_oracle.c reproduces the list bit for bit.
-// Boxes too small for one image per cluster pair fall back to an all-cluster-pairs
-// list with the minimum-image convention applied per site pair in the pair kernel.
+// The search runs one warp per i-cluster and one lane per candidate column; inside a
+// column the z-sorted clusters are bracketed by binary search. Each candidate is first
+// tested in FP32 against rlist^2 -/+ a margin that bounds the FP32 rounding error;
+// only candidates inside that band are decided by the FP64 predicate, evaluated with
+// explicit round-to-nearest intrinsics in the same order as the CPU builder of
+// oracle/nblist_oracle.c, so the two lists agree bit for bit. No step waits for the
+// host: capacities are checked on the device and reported in the status word, and with
+// a Verlet skin the rebuild decision (any site moved more than skin/2) is taken on the
+// device too. Boxes too small for one image per cluster pair use an all-cluster-pairs
+// list with the minimum image applied per site pair in the pair kernel.
 #include <math.h>
 
 #include <algorithm>
 
 #include "mg_internal.cuh"
+
+// d_meta layout (int units): [0] ncl, [1] max column count, [2] need-rebuild flag,
+// [3] builds since creation, [4..5] (64-bit) entries written
+#define META_NCL 0
+#define META_MAXCOL 1
+#define META_NEED 2
+#define META_BUILDS 3
+#define META_NPAIRS 4
 
 namespace {
 
@@ -31,10 +48,11 @@ __device__ __forceinline__ int column_of(double w, double cw, int nc) {
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
-__global__ void k_bin(int n, const double *__restrict__ x, const double *__restrict__ y,
+__global__ void k_bin(int n, int ncol, const double *__restrict__ x, const double *__restrict__ y,
                       const double *__restrict__ z, double lx, double ly, double lz, double cwx, double cwy,
                       int ncx, int ncy, double *__restrict__ xb, double *__restrict__ img,
-                      int *__restrict__ col_of, int *__restrict__ col_count) {
+                      int *__restrict__ col_of, int *__restrict__ col_count, const int *__restrict__ meta) {
+    if (!meta[META_NEED]) return;
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     double ix, iy, iz;
@@ -50,51 +68,53 @@ __global__ void k_bin(int n, const double *__restrict__ x, const double *__restr
     atomicAdd(&col_count[col], 1);
 }
 
-// single-block exclusive scans of the column counts; meta[0] = clusters, meta[1] = max column
-__global__ void k_scan_columns(int ncol, const int *__restrict__ count, int *__restrict__ start,
-                               int *__restrict__ cl_start, int *__restrict__ fill, int *__restrict__ meta) {
-    __shared__ int s_sum[1024], s_cl[1024], s_max[1024];
+__global__ void k_zero(int *__restrict__ p, int count, const int *__restrict__ meta) {
+    if (!meta[META_NEED]) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) p[i] = 0;
+}
+
+// single-block exclusive scan of `count` into `start` (start[nc] = total); also resets
+// `fill`; with max_out != null stores the largest count
+__global__ void k_scan(int nc, const int *__restrict__ count, int *__restrict__ start, int *__restrict__ fill,
+                       int *__restrict__ total_out, int *__restrict__ max_out, const int *__restrict__ meta) {
+    if (!meta[META_NEED]) return;
+    __shared__ int s_sum[1024], s_max[1024];
     int t = threadIdx.x, nt = blockDim.x;
-    int per = (ncol + nt - 1) / nt;
-    int b = t * per, e = min(ncol, b + per);
-    int sum = 0, cl = 0, mx = 0;
+    int per = (nc + nt - 1) / nt;
+    int b = t * per, e = min(nc, b + per);
+    int sum = 0, mx = 0;
     for (int i = b; i < e; i++) {
         sum += count[i];
-        cl += (count[i] + MG_CL - 1) / MG_CL;
         mx = max(mx, count[i]);
     }
     s_sum[t] = sum;
-    s_cl[t] = cl;
     s_max[t] = mx;
     __syncthreads();
     if (t == 0) {
-        int a = 0, c = 0, m = 0;
+        int a = 0, m = 0;
         for (int i = 0; i < nt; i++) {
-            int v = s_sum[i], w = s_cl[i];
+            int v = s_sum[i];
             s_sum[i] = a;
-            s_cl[i] = c;
             a += v;
-            c += w;
             m = max(m, s_max[i]);
         }
-        start[ncol] = a;
-        cl_start[ncol] = c;
-        meta[0] = c;
-        meta[1] = m;
+        start[nc] = a;
+        if (total_out) *total_out = a;
+        if (max_out) *max_out = m;
     }
     __syncthreads();
-    int a = s_sum[t], c = s_cl[t];
+    int a = s_sum[t];
     for (int i = b; i < e; i++) {
         start[i] = a;
-        cl_start[i] = c;
-        fill[i] = 0;
+        if (fill) fill[i] = 0;
         a += count[i];
-        c += (count[i] + MG_CL - 1) / MG_CL;
     }
 }
 
 __global__ void k_scatter(int n, const int *__restrict__ col_of, const int *__restrict__ start,
-                          int *__restrict__ fill, int *__restrict__ sorted) {
+                          int *__restrict__ fill, int *__restrict__ sorted, const int *__restrict__ meta) {
+    if (!meta[META_NEED]) return;
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     int col = col_of[a];
@@ -102,19 +122,21 @@ __global__ void k_scatter(int n, const int *__restrict__ col_of, const int *__re
     sorted[start[col] + slot] = a;
 }
 
-// One block per column: sort its sites by (wrapped z, index), cut them into clusters,
-// and compute each cluster's FP64 bounding box and centre.
-__global__ void k_sort_columns(int n, const int *__restrict__ start, const int *__restrict__ cl_start,
-                               const int *__restrict__ sorted, const double *__restrict__ xb,
-                               int *__restrict__ cl_atom, double *__restrict__ cl_ref,
-                               double *__restrict__ cl_bb, int *__restrict__ cl_col,
-                               unsigned *__restrict__ flags) {
+// One block per column: sort its sites by (wrapped z, index) in place and count the
+// clusters the cutting rule makes.
+__global__ void k_sort_columns(int n, const int *__restrict__ start, int *__restrict__ sorted,
+                               const double *__restrict__ xb, double zcap, int *__restrict__ col_ncl,
+                               unsigned *__restrict__ flags, const int *__restrict__ meta) {
+    if (!meta[META_NEED]) return;
     __shared__ double kz[MG_MAX_COLUMN];
     __shared__ int ki[MG_MAX_COLUMN];
     int col = blockIdx.x;
     int s0 = start[col], cnt = start[col + 1] - s0;
     if (cnt > MG_MAX_COLUMN) {
-        if (threadIdx.x == 0) atomicOr(flags, MG_FLAG_COLUMN_OVERFLOW);
+        if (threadIdx.x == 0) {
+            atomicOr(flags, MG_FLAG_COLUMN_OVERFLOW);
+            col_ncl[col] = 0;
+        }
         return;
     }
     int pow2 = 1;
@@ -123,14 +145,13 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, const int *
         if (i < cnt) {
             int a = sorted[s0 + i];
             ki[i] = a;
-            kz[i] = xb[2 * n + a];
+            kz[i] = xb[2 * (size_t)n + a];
         } else {
             ki[i] = 0x7fffffff;
             kz[i] = INFINITY;
         }
     }
     __syncthreads();
-    // bitonic sort on (z, index)
     for (int k = 2; k <= pow2; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < pow2; i += blockDim.x) {
@@ -151,32 +172,68 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, const int *
             __syncthreads();
         }
     }
-    int c0 = cl_start[col];
-    int ncl_col = (cnt + MG_CL - 1) / MG_CL;
-    for (int i = threadIdx.x; i < ncl_col * MG_CL; i += blockDim.x) cl_atom[(size_t)c0 * MG_CL + i] = i < cnt ? ki[i] : -1;
-    for (int q = threadIdx.x; q < ncl_col; q += blockDim.x) {
-        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (int s = 0; s < MG_CL; s++) {
-            int i = q * MG_CL + s;
-            if (i >= cnt) break;
-            int a = ki[i];
-            for (int d = 0; d < 3; d++) {
-                double v = xb[(size_t)d * n + a];
-                lo[d] = fmin(lo[d], v);
-                hi[d] = fmax(hi[d], v);
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) sorted[s0 + i] = ki[i];
+    if (threadIdx.x == 0) {
+        int ncl = 0, first = 0;
+        for (int i = 0; i < cnt; i++) {
+            if (i == 0 || i - first == MG_CL || __dsub_rn(kz[i], kz[first]) > zcap) {
+                ncl++;
+                first = i;
             }
         }
-        size_t cl = (size_t)c0 + q;
-        for (int d = 0; d < 3; d++) {
-            cl_bb[cl * 6 + d] = lo[d];
-            cl_bb[cl * 6 + 3 + d] = hi[d];
-            cl_ref[cl * 3 + d] = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
-        }
-        cl_col[cl] = col;
+        col_ncl[col] = ncl;
     }
 }
 
-// FP64 squared distance between two boxes along one axis, J shifted by s
+// One block per column: write the clusters (sites, FP64 and FP32 boxes, centre).
+__global__ void k_write_clusters(int n, const int *__restrict__ start, const int *__restrict__ sorted,
+                                 const int *__restrict__ cl_start, const double *__restrict__ xb, double zcap,
+                                 int cl_cap, int *__restrict__ cl_atom, double *__restrict__ cl_ref,
+                                 double *__restrict__ cl_bb, float *__restrict__ cl_bbf,
+                                 unsigned *__restrict__ flags, const int *__restrict__ meta) {
+    if (!meta[META_NEED]) return;
+    int col = blockIdx.x;
+    int s0 = start[col], cnt = start[col + 1] - s0;
+    if (cnt > MG_MAX_COLUMN || threadIdx.x != 0) return;
+    int c = cl_start[col];
+    int first = 0;
+    for (int i = 0; i <= cnt; i++) {
+        bool cut = (i == cnt) || (i > 0 && (i - first == MG_CL ||
+                                            __dsub_rn(xb[2 * (size_t)n + sorted[s0 + i]],
+                                                      xb[2 * (size_t)n + sorted[s0 + first]]) > zcap));
+        if (!cut) continue;
+        if (i > 0) {
+            if (c >= cl_cap) {
+                atomicOr(flags, MG_FLAG_LIST_OVERFLOW);
+                return;
+            }
+            double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int s = 0; s < MG_CL; s++) {
+                int idx = first + s;
+                int a = idx < i ? sorted[s0 + idx] : -1;
+                cl_atom[(size_t)c * MG_CL + s] = a;
+                if (a < 0) continue;
+                for (int d = 0; d < 3; d++) {
+                    double v = xb[(size_t)d * n + a];
+                    lo[d] = fmin(lo[d], v);
+                    hi[d] = fmax(hi[d], v);
+                }
+            }
+            for (int d = 0; d < 3; d++) {
+                cl_bb[(size_t)c * 6 + d] = lo[d];
+                cl_bb[(size_t)c * 6 + 3 + d] = hi[d];
+                cl_bbf[(size_t)c * 6 + d] = (float)lo[d];
+                cl_bbf[(size_t)c * 6 + 3 + d] = (float)hi[d];
+                cl_ref[(size_t)c * 3 + d] = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
+            }
+            c++;
+        }
+        first = i;
+    }
+}
+
+// FP64 squared gap between two boxes along one axis, J shifted by s (same op order as
+// the CPU builder)
 __device__ __forceinline__ double gap2(double loi, double hii, double loj, double hij, double s) {
     double a = __dsub_rn(__dadd_rn(loj, s), hii);
     double b = __dsub_rn(loi, __dadd_rn(hij, s));
@@ -184,134 +241,212 @@ __device__ __forceinline__ double gap2(double loi, double hii, double loj, doubl
     return __dmul_rn(g, g);
 }
 
+__device__ __forceinline__ float gap2f(float loi, float hii, float loj, float hij, float s) {
+    float a = (loj + s) - hii;
+    float b = loi - (hij + s);
+    float g = fmaxf(0.f, fmaxf(a, b));
+    return g * g;
+}
+
 struct SearchArgs {
-    int ncl, ncx, ncy;
-    double lx, ly, lz, cwx, cwy, rlist2, rlist;
+    int ncx, ncy;
+    double lx, ly, lz, cwx, cwy, rlist, rlist2;
+    float flo, fhi, fmarg;  // FP32 band [rlist^2 - m, rlist^2 + m] and a length margin
+    const int *meta;
+    int *meta_w;
     const double *bb, *ref;
+    const float *bbf;
     const int *col_cl_start;
-    const int *pair_start;  // null in the counting pass
-    int *count;
-    int *pair_j;
-    void *pair_shift;       // float4 or double4
-    int *pair_img;
+    int *pair_start, *pair_cnt, *pair_j, *pair_img;
+    void *pair_shift;
+    unsigned long long *counter;
+    long long cap;
     int fp64;
     unsigned *flags;
 };
 
-// Enumerate the (J, image) entries of i-cluster I in a fixed order:
-// column offsets in y then x ascending, clusters of a column in z order, z image -1,0,1.
-__device__ void search_cluster(const SearchArgs &A, int I, bool fill) {
-    const double *bi = A.bb + (size_t)I * 6;
-    double loi[3] = {bi[0], bi[1], bi[2]}, hii[3] = {bi[3], bi[4], bi[5]};
-    int cx0 = (int)floor(__ddiv_rn(__dsub_rn(loi[0], A.rlist), A.cwx));
-    int cx1 = (int)floor(__ddiv_rn(__dadd_rn(hii[0], A.rlist), A.cwx));
-    int cy0 = (int)floor(__ddiv_rn(__dsub_rn(loi[1], A.rlist), A.cwy));
-    int cy1 = (int)floor(__ddiv_rn(__dadd_rn(hii[1], A.rlist), A.cwy));
-    int cnt = 0;
-    long long out = fill ? A.pair_start[I] : 0;
-    const double *ri = A.ref + (size_t)I * 3;
-    for (int uy = cy0; uy <= cy1; uy++) {
-        int wy = uy % A.ncy;
-        if (wy < 0) wy += A.ncy;
-        int iy = (uy - wy) / A.ncy;  // image along y
-        double sy = __dmul_rn((double)iy, A.ly);
-        double gy = gap2(loi[1], hii[1], 0.0, 0.0, 0.0);  // placeholder, replaced below
-        (void)gy;
-        for (int ux = cx0; ux <= cx1; ux++) {
-            int wx = ux % A.ncx;
-            if (wx < 0) wx += A.ncx;
-            int ix = (ux - wx) / A.ncx;
-            double sx = __dmul_rn((double)ix, A.lx);
-            int col = wy * A.ncx + wx;
-            int j0 = A.col_cl_start[col], j1 = A.col_cl_start[col + 1];
-            for (int J = j0; J < j1; J++) {
-                const double *bj = A.bb + (size_t)J * 6;
-                double dxy = __dadd_rn(gap2(loi[0], hii[0], bj[0], bj[3], sx), gap2(loi[1], hii[1], bj[1], bj[4], sy));
-                if (!(dxy < A.rlist2)) continue;
-                int hits = 0;
-                for (int iz = -1; iz <= 1; iz++) {
-                    double sz = __dmul_rn((double)iz, A.lz);
-                    double d2 = __dadd_rn(dxy, gap2(loi[2], hii[2], bj[2], bj[5], sz));
-                    if (!(d2 < A.rlist2)) continue;
-                    hits++;
-                    if (fill) {
-                        const double *rj = A.ref + (size_t)J * 3;
-                        double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], sx));
-                        double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], sy));
-                        double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], sz));
-                        A.pair_j[out] = J;
-                        A.pair_img[out] = ((ix + 512) & 1023) | (((iy + 512) & 1023) << 10) | (((iz + 512) & 1023) << 20);
-                        if (A.fp64)
-                            ((double4 *)A.pair_shift)[out] = make_double4(s0, s1, s2, 0.0);
-                        else
-                            ((float4 *)A.pair_shift)[out] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
-                        out++;
-                    }
-                    cnt++;
-                }
-                if (hits > 1) atomicOr(A.flags, MG_FLAG_LIST_OVERFLOW);  // box too small for this mode
-            }
-        }
+// Hits of i-cluster I against the clusters of candidate column number `c` (row-major over
+// the column window). With out >= 0 the entries are written from index out on.
+__device__ int column_hits(const SearchArgs &A, int I, const double *bi, const float *bif, int cx0, int cy0,
+                           int nx, int c, long long out) {
+    const int uy = cy0 + c / nx, ux = cx0 + c % nx;
+    int wy = uy % A.ncy;
+    if (wy < 0) wy += A.ncy;
+    const int iy = (uy - wy) / A.ncy;
+    int wx = ux % A.ncx;
+    if (wx < 0) wx += A.ncx;
+    const int ix = (ux - wx) / A.ncx;
+    const double sx = __dmul_rn((double)ix, A.lx), sy = __dmul_rn((double)iy, A.ly);
+    // conservative column rejection: the column's sites lie within its x/y slab
+    {
+        float cx_lo = (float)(wx * A.cwx + sx) - A.fmarg, cx_hi = (float)((wx + 1) * A.cwx + sx) + A.fmarg;
+        float cy_lo = (float)(wy * A.cwy + sy) - A.fmarg, cy_hi = (float)((wy + 1) * A.cwy + sy) + A.fmarg;
+        float gx = fmaxf(0.f, fmaxf(cx_lo - bif[3], bif[0] - cx_hi));
+        float gy = fmaxf(0.f, fmaxf(cy_lo - bif[4], bif[1] - cy_hi));
+        if (gx * gx + gy * gy > A.fhi) return 0;
     }
-    if (!fill) A.count[I] = cnt;
+    const int col = wy * A.ncx + wx;
+    const int j0 = A.col_cl_start[col], j1 = A.col_cl_start[col + 1];
+    if (j0 == j1) return 0;
+    // z brackets per image: zhi_J + s >= zlo_I - r and zlo_J + s <= zhi_I + r
+    int lo3[3], hi3[3];
+    const float r = (float)A.rlist + A.fmarg;
+    for (int k = 0; k < 3; k++) {
+        const float s = (float)((k - 1) * A.lz);
+        const float zmin = bif[2] - r - s, zmax = bif[5] + r - s;
+        int a = j0, b = j1;  // first J with zhi >= zmin
+        while (a < b) {
+            int m = (a + b) >> 1;
+            if (A.bbf[(size_t)m * 6 + 5] < zmin) a = m + 1; else b = m;
+        }
+        int e = a, f = j1;  // first J with zlo > zmax
+        while (e < f) {
+            int m = (e + f) >> 1;
+            if (A.bbf[(size_t)m * 6 + 2] <= zmax) e = m + 1; else f = m;
+        }
+        lo3[k] = a;
+        hi3[k] = e;
+    }
+    int cnt = 0;
+    const int jlo = min(lo3[0], min(lo3[1], lo3[2])), jhi = max(hi3[0], max(hi3[1], hi3[2]));
+    const float sxf = (float)sx, syf = (float)sy;
+    for (int J = jlo; J < jhi; J++) {
+        bool inr = (J >= lo3[0] && J < hi3[0]) || (J >= lo3[1] && J < hi3[1]) || (J >= lo3[2] && J < hi3[2]);
+        if (!inr) continue;
+        const float *bjf = A.bbf + (size_t)J * 6;
+        float dxyf = gap2f(bif[0], bif[3], bjf[0], bjf[3], sxf) + gap2f(bif[1], bif[4], bjf[1], bjf[4], syf);
+        if (dxyf > A.fhi) continue;
+        const double *bj = A.bb + (size_t)J * 6;
+        int hits = 0;
+        for (int iz = -1; iz <= 1; iz++) {
+            float d2f = dxyf + gap2f(bif[2], bif[5], bjf[2], bjf[5], (float)(iz * A.lz));
+            bool hit;
+            if (d2f < A.flo) {
+                hit = true;
+            } else if (d2f > A.fhi) {
+                hit = false;
+            } else {  // FP64 decides, as the CPU builder does
+                double sz = __dmul_rn((double)iz, A.lz);
+                double dxy = __dadd_rn(gap2(bi[0], bi[3], bj[0], bj[3], sx), gap2(bi[1], bi[4], bj[1], bj[4], sy));
+                double d2 = __dadd_rn(dxy, gap2(bi[2], bi[5], bj[2], bj[5], sz));
+                hit = d2 < A.rlist2;
+            }
+            if (!hit) continue;
+            hits++;
+            if (out >= 0) {
+                const long long o = out + cnt;
+                const double *ri = A.ref + (size_t)I * 3, *rj = A.ref + (size_t)J * 3;
+                const double sz = __dmul_rn((double)iz, A.lz);
+                const double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], sx));
+                const double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], sy));
+                const double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], sz));
+                A.pair_j[o] = J;
+                A.pair_img[o] = ((ix + 512) & 1023) | (((iy + 512) & 1023) << 10) | (((iz + 512) & 1023) << 20);
+                if (A.fp64)
+                    ((double4 *)A.pair_shift)[o] = make_double4(s0, s1, s2, 0.0);
+                else
+                    ((float4 *)A.pair_shift)[o] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
+            }
+            cnt++;
+        }
+        if (hits > 1) atomicOr(A.flags, MG_FLAG_SMALL_BOX);
+    }
+    return cnt;
 }
 
-__global__ void k_search(SearchArgs A, int fill) {
-    int I = blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= A.ncl) return;
-    search_cluster(A, I, fill != 0);
+__global__ void k_search(SearchArgs A) {
+    if (!A.meta[META_NEED]) return;
+    const int lane = threadIdx.x & 31;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= A.meta[META_NCL]) return;
+    double bi[6];
+    float bif[6];
+    for (int d = 0; d < 6; d++) {
+        bi[d] = A.bb[(size_t)I * 6 + d];
+        bif[d] = A.bbf[(size_t)I * 6 + d];
+    }
+    const int cx0 = (int)floor(__ddiv_rn(__dsub_rn(bi[0], A.rlist), A.cwx));
+    const int cx1 = (int)floor(__ddiv_rn(__dadd_rn(bi[3], A.rlist), A.cwx));
+    const int cy0 = (int)floor(__ddiv_rn(__dsub_rn(bi[1], A.rlist), A.cwy));
+    const int cy1 = (int)floor(__ddiv_rn(__dadd_rn(bi[4], A.rlist), A.cwy));
+    const int nx = cx1 - cx0 + 1, ny = cy1 - cy0 + 1;
+    if (nx > A.ncx || ny > A.ncy) {  // a column would be visited twice: small-box mode
+        if (lane == 0) atomicOr(A.flags, MG_FLAG_SMALL_BOX);
+        return;
+    }
+    const int ncand = nx * ny;
+    int total = 0;
+    for (int base = 0; base < ncand; base += 32) {
+        int c = base + lane;
+        int h = c < ncand ? column_hits(A, I, bi, bif, cx0, cy0, nx, c, -1) : 0;
+        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+        total += h;
+    }
+    unsigned long long off = 0;
+    if (lane == 0) off = atomicAdd(A.counter, (unsigned long long)total);
+    off = __shfl_sync(0xffffffffu, off, 0);
+    if (lane == 0) {
+        A.pair_start[I] = (int)off;
+        A.pair_cnt[I] = total;
+    }
+    if ((long long)(off + total) > A.cap) {
+        if (lane == 0) atomicOr(A.flags, MG_FLAG_LIST_OVERFLOW);
+        if (lane == 0) A.pair_cnt[I] = 0;
+        return;
+    }
+    long long run = (long long)off;
+    for (int base = 0; base < ncand; base += 32) {
+        int c = base + lane;
+        int h = c < ncand ? column_hits(A, I, bi, bif, cx0, cy0, nx, c, -1) : 0;
+        int incl = h;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (h > 0) column_hits(A, I, bi, bif, cx0, cy0, nx, c, run + incl - h);
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
 }
 
 // small boxes: every (I, J) pair once, no image (minimum image per site pair later)
-__global__ void k_all_pairs(int ncl, const double *__restrict__ ref, int *__restrict__ pair_j,
-                            void *pair_shift, int *__restrict__ pair_img, int fp64) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (long long)ncl * ncl) return;
-    int I = (int)(e / ncl), J = (int)(e % ncl);
-    double s0 = __dsub_rn(ref[I * 3 + 0], ref[J * 3 + 0]);
-    double s1 = __dsub_rn(ref[I * 3 + 1], ref[J * 3 + 1]);
-    double s2 = __dsub_rn(ref[I * 3 + 2], ref[J * 3 + 2]);
-    pair_j[e] = J;
-    pair_img[e] = 512 | (512 << 10) | (512 << 20);
-    if (fp64)
-        ((double4 *)pair_shift)[e] = make_double4(s0, s1, s2, 0.0);
-    else
-        ((float4 *)pair_shift)[e] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
+__global__ void k_all_pairs(const int *__restrict__ meta, const double *__restrict__ ref, int *__restrict__ pair_start,
+                            int *__restrict__ pair_cnt, int *__restrict__ pair_j, void *pair_shift,
+                            int *__restrict__ pair_img, int fp64, long long cap, unsigned *__restrict__ flags) {
+    if (!meta[META_NEED]) return;
+    const int ncl = meta[META_NCL];
+    if ((long long)ncl * ncl > cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, MG_FLAG_LIST_OVERFLOW);
+        return;
+    }
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = t0; i < ncl; i += stride) {
+        pair_start[i] = (int)(i * ncl);
+        pair_cnt[i] = ncl;
+    }
+    for (long long e = t0; e < (long long)ncl * ncl; e += stride) {
+        int I = (int)(e / ncl), J = (int)(e % ncl);
+        double s0 = __dsub_rn(ref[I * 3 + 0], ref[J * 3 + 0]);
+        double s1 = __dsub_rn(ref[I * 3 + 1], ref[J * 3 + 1]);
+        double s2 = __dsub_rn(ref[I * 3 + 2], ref[J * 3 + 2]);
+        pair_j[e] = J;
+        pair_img[e] = 512 | (512 << 10) | (512 << 20);
+        if (fp64)
+            ((double4 *)pair_shift)[e] = make_double4(s0, s1, s2, 0.0);
+        else
+            ((float4 *)pair_shift)[e] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
+    }
 }
 
-// single-block exclusive scan of the per-cluster entry counts (64-bit total in meta)
-__global__ void k_scan_pairs(int ncl, const int *__restrict__ count, int *__restrict__ start,
-                             long long *__restrict__ total) {
-    __shared__ long long s[1024];
-    int t = threadIdx.x, nt = blockDim.x;
-    int per = (ncl + nt - 1) / nt;
-    int b = t * per, e = min(ncl, b + per);
-    long long sum = 0;
-    for (int i = b; i < e; i++) sum += count[i];
-    s[t] = sum;
-    __syncthreads();
-    if (t == 0) {
-        long long a = 0;
-        for (int i = 0; i < nt; i++) {
-            long long v = s[i];
-            s[i] = a;
-            a += v;
-        }
-        *total = a;
-    }
-    __syncthreads();
-    long long a = s[t];
-    for (int i = b; i < e; i++) {
-        start[i] = (int)a;
-        a += count[i];
-    }
-    if (t == nt - 1) start[ncl] = (int)a;
+__global__ void k_finish(int *__restrict__ meta, const unsigned long long *__restrict__ counter) {
+    if (!meta[META_NEED]) return;
+    meta[META_BUILDS] += 1;
+    *(long long *)(meta + META_NPAIRS) = (long long)*counter;
 }
 
-// max squared displacement since the build (> (skin/2)^2 triggers a rebuild)
+// any site moved more than skin/2 since the build -> rebuild
 __global__ void k_displacement(int n, const double *__restrict__ x, const double *__restrict__ y,
                                const double *__restrict__ z, const double *__restrict__ xb,
-                               const double *__restrict__ img, double half_skin2, unsigned *__restrict__ need) {
+                               const double *__restrict__ img, double half_skin2, int *__restrict__ meta) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     bool move = false;
     if (a < n) {
@@ -320,19 +455,19 @@ __global__ void k_displacement(int n, const double *__restrict__ x, const double
         double dz = (z[a] - img[2 * n + a]) - xb[2 * n + a];
         move = !(dx * dx + dy * dy + dz * dz <= half_skin2);
     }
-    if (__any_sync(0xffffffffu, move) && (threadIdx.x & 31) == 0) atomicOr(need, 1u);
+    if (__any_sync(0xffffffffu, move) && (threadIdx.x & 31) == 0) atomicOr(&meta[META_NEED], 1);
 }
 
 // Pack the per-slot pair-kernel operands from the current positions.
 template <typename R4, typename R2, typename R>
-__global__ void k_pack(int ncl, int n, const int *__restrict__ cl_atom, const double *__restrict__ cl_ref,
-                       const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
-                       const double *__restrict__ img, const double *__restrict__ q,
+__global__ void k_pack(int n, const int *__restrict__ meta, const int *__restrict__ cl_atom,
+                       const double *__restrict__ cl_ref, const double *__restrict__ x, const double *__restrict__ y,
+                       const double *__restrict__ z, const double *__restrict__ img, const double *__restrict__ q,
                        const double *__restrict__ hsig, const double *__restrict__ seps,
                        const int *__restrict__ mol, const int *__restrict__ sflags, R4 *__restrict__ pos,
                        R2 *__restrict__ lj, int *__restrict__ info) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= ncl * MG_CL) return;
+    if (s >= meta[META_NCL] * MG_CL) return;
     int a = cl_atom[s];
     int cl = s / MG_CL;
     if (a < 0) {
@@ -361,195 +496,165 @@ __global__ void k_pack(int ncl, int n, const int *__restrict__ cl_atom, const do
 
 }  // namespace
 
-static mg_status read_meta(mg_ctx *c, void *dst, size_t bytes) {
-    MG_CUDA(cudaMemcpyAsync(dst, c->d_meta.p, bytes, cudaMemcpyDeviceToHost, c->stream));
-    MG_CUDA(cudaStreamSynchronize(c->stream));
-    return MG_OK;
+// ---------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------
+static void choose_grid(mg_ctx *c, double rlist) {
+    double vol = c->lx * c->ly * c->lz;
+    double cw = std::min(cbrt(8.0 * vol / c->natom), 0.75 * rlist) / pow(1.5, c->col_refine);
+    c->ncx = std::max(1, (int)floor(c->lx / cw));
+    c->ncy = std::max(1, (int)floor(c->ly / cw));
+    c->zcap = cw;
+    c->small_box = c->small_box_forced || c->lx < 2.0 * rlist + 2.0 * (c->lx / c->ncx) ||
+                   c->ly < 2.0 * rlist + 2.0 * (c->ly / c->ncy) || c->lz < 2.0 * rlist + 2.0 * cw;
 }
 
-static mg_status build_list(mg_ctx *c, const double *dx, const double *dy, const double *dz, bool force_small) {
-    cudaStream_t s = c->stream;
-    int n = c->natom;
-    const mg_params &p = c->params;
-    double rlist = std::max(p.rcutoff, p.rcutoffelec) + std::max(c->opt.skin, 0.0);
-    double vol = c->lx * c->ly * c->lz;
-    double cw = cbrt(8.0 * vol / n);  // about one cluster per column section
-    int ncx = std::max(1, (int)floor(c->lx / cw));
-    int ncy = std::max(1, (int)floor(c->ly / cw));
-    bool small = force_small || c->lx < 2.0 * rlist + 2.0 * (c->lx / ncx) ||
-                 c->ly < 2.0 * rlist + 2.0 * (c->ly / ncy) || c->lz < 2.0 * rlist;
-    for (int attempt = 0; attempt < 6; attempt++) {
-        int ncol = ncx * ncy;
-        double cwx = c->lx / ncx, cwy = c->ly / ncy;
-        if (!mg_ensure(c, c->d_col_count, sizeof(int) * (ncol + 1)) ||
-            !mg_ensure(c, c->d_col_start, sizeof(int) * (ncol + 1)) ||
-            !mg_ensure(c, c->d_col_fill, sizeof(int) * (ncol + 1)) ||
-            !mg_ensure(c, c->d_col_cl_start, sizeof(int) * (ncol + 1)) ||
-            !mg_ensure(c, c->d_col_sorted, sizeof(int) * (size_t)n * 2) ||
-            !mg_ensure(c, c->d_xbuild, sizeof(double) * 3 * n) || !mg_ensure(c, c->d_img, sizeof(double) * 3 * n) ||
-            !mg_ensure(c, c->d_meta, 64))
-            return MG_ERR_ALLOC;
-        int *col_of = (int *)c->d_col_sorted.p + n;
-        MG_CUDA(cudaMemsetAsync(c->d_col_count.p, 0, sizeof(int) * (ncol + 1), s));
-        MG_CUDA(cudaMemsetAsync(c->d_flags.p, 0, 64, s));
-        k_bin<<<(n + 255) / 256, 256, 0, s>>>(n, dx, dy, dz, c->lx, c->ly, c->lz, cwx, cwy, ncx, ncy,
-                                               (double *)c->d_xbuild.p, (double *)c->d_img.p, col_of,
-                                               (int *)c->d_col_count.p);
-        k_scan_columns<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_count.p, (int *)c->d_col_start.p,
-                                          (int *)c->d_col_cl_start.p, (int *)c->d_col_fill.p, (int *)c->d_meta.p);
-        int meta[2];
-        mg_status st = read_meta(c, meta, sizeof(meta));
-        if (st) return st;
-        if (meta[1] > MG_MAX_COLUMN) {  // refine the column grid
-            ncx = std::max(ncx + 1, (int)(ncx * 1.5));
-            ncy = std::max(ncy + 1, (int)(ncy * 1.5));
-            continue;
-        }
-        int ncl = meta[0];
-        if (!mg_ensure(c, c->d_cl_atom, sizeof(int) * (size_t)ncl * MG_CL) ||
-            !mg_ensure(c, c->d_cl_ref, sizeof(double) * 3 * (size_t)ncl) ||
-            !mg_ensure(c, c->d_cl_bb, sizeof(double) * 6 * (size_t)ncl) ||
-            !mg_ensure(c, c->d_cl_col, sizeof(int) * (size_t)ncl) ||
-            !mg_ensure(c, c->d_pair_count, sizeof(int) * (size_t)(ncl + 1)) ||
-            !mg_ensure(c, c->d_pair_start, sizeof(int) * (size_t)(ncl + 1)))
-            return MG_ERR_ALLOC;
-        k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, col_of, (int *)c->d_col_start.p, (int *)c->d_col_fill.p,
-                                                  (int *)c->d_col_sorted.p);
-        k_sort_columns<<<ncol, 256, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_cl_start.p,
-                                           (int *)c->d_col_sorted.p, (double *)c->d_xbuild.p,
-                                           (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p,
-                                           (double *)c->d_cl_bb.p, (int *)c->d_cl_col.p, (unsigned *)c->d_flags.p);
-        bool fp64 = c->opt.precision == MG_PREC_FP64;
-        size_t ent = fp64 ? sizeof(double4) : sizeof(float4);
-        long long npairs;
-        if (small) {
-            npairs = (long long)ncl * ncl;
-            if (npairs > 0x7fffffffLL) return mg_fail(c, MG_ERR_CAPACITY, "cluster-pair list too large");
-            if (!mg_ensure(c, c->d_pair_j, sizeof(int) * npairs) || !mg_ensure(c, c->d_pair_shift, ent * npairs) ||
-                !mg_ensure(c, c->d_pair_img, sizeof(int) * npairs))
-                return MG_ERR_ALLOC;
-            std::vector<int> start(ncl + 1);
-            for (int i = 0; i <= ncl; i++) start[i] = i * ncl;
-            MG_CUDA(cudaMemcpyAsync(c->d_pair_start.p, start.data(), sizeof(int) * (ncl + 1), cudaMemcpyHostToDevice, s));
-            k_all_pairs<<<(unsigned)((npairs + 255) / 256), 256, 0, s>>>(ncl, (double *)c->d_cl_ref.p,
-                                                                         (int *)c->d_pair_j.p, c->d_pair_shift.p,
-                                                                         (int *)c->d_pair_img.p, fp64);
-            MG_CUDA(cudaStreamSynchronize(s));
-        } else {
-            SearchArgs A;
-            A.ncl = ncl;
-            A.ncx = ncx;
-            A.ncy = ncy;
-            A.lx = c->lx;
-            A.ly = c->ly;
-            A.lz = c->lz;
-            A.cwx = cwx;
-            A.cwy = cwy;
-            A.rlist = rlist;
-            A.rlist2 = rlist * rlist;
-            A.bb = (double *)c->d_cl_bb.p;
-            A.ref = (double *)c->d_cl_ref.p;
-            A.col_cl_start = (int *)c->d_col_cl_start.p;
-            A.pair_start = (int *)c->d_pair_start.p;
-            A.count = (int *)c->d_pair_count.p;
-            A.pair_j = nullptr;
-            A.pair_shift = nullptr;
-            A.pair_img = nullptr;
-            A.fp64 = fp64;
-            A.flags = (unsigned *)c->d_flags.p;
-            k_search<<<(ncl + 127) / 128, 128, 0, s>>>(A, 0);
-            k_scan_pairs<<<1, 1024, 0, s>>>(ncl, (int *)c->d_pair_count.p, (int *)c->d_pair_start.p,
-                                            (long long *)c->d_meta.p);
-            long long tot[1];
-            if ((st = read_meta(c, tot, sizeof(tot)))) return st;
-            unsigned fl = 0;
-            MG_CUDA(cudaMemcpy(&fl, c->d_flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
-            if (fl & MG_FLAG_COLUMN_OVERFLOW) {
-                ncx = std::max(ncx + 1, (int)(ncx * 1.5));
-                ncy = std::max(ncy + 1, (int)(ncy * 1.5));
-                continue;
-            }
-            if (fl & MG_FLAG_LIST_OVERFLOW) {  // more than one image per pair: small-box mode
-                small = true;
-                continue;
-            }
-            npairs = tot[0];
-            if (npairs > 0x7fffffffLL) return mg_fail(c, MG_ERR_CAPACITY, "cluster-pair list too large");
-            if (!mg_ensure(c, c->d_pair_j, sizeof(int) * npairs) || !mg_ensure(c, c->d_pair_shift, ent * npairs) ||
-                !mg_ensure(c, c->d_pair_img, sizeof(int) * npairs))
-                return MG_ERR_ALLOC;
-            A.pair_j = (int *)c->d_pair_j.p;
-            A.pair_shift = c->d_pair_shift.p;
-            A.pair_img = (int *)c->d_pair_img.p;
-            k_search<<<(ncl + 127) / 128, 128, 0, s>>>(A, 1);
-        }
-        unsigned fl = 0;
-        MG_CUDA(cudaMemcpyAsync(&fl, c->d_flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-        MG_CUDA(cudaStreamSynchronize(s));
-        if (fl & MG_FLAG_COLUMN_OVERFLOW) {
-            ncx = std::max(ncx + 1, (int)(ncx * 1.5));
-            ncy = std::max(ncy + 1, (int)(ncy * 1.5));
-            continue;
-        }
-        c->ncx = ncx;
-        c->ncy = ncy;
-        c->ncol = ncol;
-        c->ncl = ncl;
-        c->npairs = npairs;
-        c->small_box = small;
-        c->list_lx = c->lx;
-        c->list_ly = c->ly;
-        c->list_lz = c->lz;
-        c->list_rlist = rlist;
-        c->list_valid = true;
-        c->list_builds++;
-        c->list_rebuilt = 1;
-        c->launches += small ? 5 : 7;
-        MG_CUDA(cudaMemsetAsync(c->d_flags.p, 0, 64, s));
-        return MG_OK;
+// Size every list buffer for the current grid; called when the grid or capacity changes.
+static mg_status size_list(mg_ctx *c) {
+    int n = c->natom, ncol = c->ncx * c->ncy;
+    if (c->cl_cap < n / 4 + ncol + 16) c->cl_cap = n / 4 + ncol + 16;
+    if (c->cl_cap > n + ncol + 16) c->cl_cap = n + ncol + 16;
+    long long ncl = c->cl_cap;
+    if (c->small_box) {
+        if (c->pair_cap < ncl * ncl) c->pair_cap = ncl * ncl;
+    } else if (c->pair_cap == 0) {
+        double rho = n / (c->lx * c->ly * c->lz);
+        double r = c->list_rlist + 2.0 * c->zcap;
+        c->pair_cap = (long long)(ncl * (1.5 * 4.18879 * r * r * r * rho / MG_CL + 64));
     }
-    return mg_fail(c, MG_ERR_CAPACITY, "could not build the cluster list (column overflow)");
+    if (c->pair_cap > 0x7fffffffLL) return mg_fail(c, MG_ERR_CAPACITY, "cluster-pair list exceeds 2^31 entries");
+    bool fp64 = c->opt.precision == MG_PREC_FP64;
+    size_t ent = fp64 ? sizeof(double4) : sizeof(float4);
+    if (!mg_ensure(c, c->d_col_count, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_start, sizeof(int) * (ncol + 1)) ||
+        !mg_ensure(c, c->d_col_fill, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_cl_start, sizeof(int) * (ncol + 1)) ||
+        !mg_ensure(c, c->d_col_ncl, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_sorted, sizeof(int) * (size_t)n * 2) ||
+        !mg_ensure(c, c->d_xbuild, sizeof(double) * 3 * (size_t)n) || !mg_ensure(c, c->d_img, sizeof(double) * 3 * (size_t)n) ||
+        !mg_ensure(c, c->d_cl_atom, sizeof(int) * (size_t)ncl * MG_CL) || !mg_ensure(c, c->d_cl_ref, sizeof(double) * 3 * (size_t)ncl) ||
+        !mg_ensure(c, c->d_cl_bb, sizeof(double) * 6 * (size_t)ncl) || !mg_ensure(c, c->d_cl_bbf, sizeof(float) * 6 * (size_t)ncl) ||
+        !mg_ensure(c, c->d_pair_start, sizeof(int) * (size_t)(ncl + 1)) || !mg_ensure(c, c->d_pair_count, sizeof(int) * (size_t)(ncl + 1)) ||
+        !mg_ensure(c, c->d_pair_j, sizeof(int) * (size_t)c->pair_cap) || !mg_ensure(c, c->d_pair_shift, ent * (size_t)c->pair_cap) ||
+        !mg_ensure(c, c->d_pair_img, sizeof(int) * (size_t)c->pair_cap) || !mg_ensure(c, c->d_counter, 64))
+        return MG_ERR_ALLOC;
+    return MG_OK;
 }
 
 mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const double *dz) {
     const mg_params &p = c->params;
+    cudaStream_t s = c->stream;
+    const int n = c->natom;
     double rlist = std::max(p.rcutoff, p.rcutoffelec) + std::max(c->opt.skin, 0.0);
-    bool rebuild = !c->list_valid || c->list_lx != c->lx || c->list_ly != c->ly || c->list_lz != c->lz ||
-                   c->list_rlist != rlist || !(c->opt.skin > 0);
-    if (!rebuild) {
-        int n = c->natom;
+    if (!mg_ensure(c, c->d_meta, 64)) return MG_ERR_ALLOC;
+    int *meta = (int *)c->d_meta.p;
+    bool geometry = !c->list_valid || c->list_lx != c->lx || c->list_ly != c->ly || c->list_lz != c->lz ||
+                    c->list_rlist != rlist;
+    if (geometry) {
+        c->list_rlist = rlist;
+        c->list_lx = c->lx;
+        c->list_ly = c->ly;
+        c->list_lz = c->lz;
+        choose_grid(c, rlist);
+        mg_status st = size_list(c);
+        if (st) return st;
+    }
+    if (geometry || !(c->opt.skin > 0)) {
+        int one = 1;
+        MG_CUDA(cudaMemcpyAsync(meta + META_NEED, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    } else {
+        MG_CUDA(cudaMemsetAsync(meta + META_NEED, 0, sizeof(int), s));
         double hs = 0.5 * c->opt.skin;
-        unsigned *need = (unsigned *)c->d_flags.p + 8;
-        MG_CUDA(cudaMemsetAsync(need, 0, sizeof(unsigned), c->stream));
-        k_displacement<<<(n + 255) / 256, 256, 0, c->stream>>>(n, dx, dy, dz, (double *)c->d_xbuild.p,
-                                                                (double *)c->d_img.p, hs * hs, need);
-        unsigned h = 0;
-        MG_CUDA(cudaMemcpyAsync(&h, need, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-        MG_CUDA(cudaStreamSynchronize(c->stream));
-        rebuild = h != 0;
+        k_displacement<<<(n + 255) / 256, 256, 0, s>>>(n, dx, dy, dz, (double *)c->d_xbuild.p, (double *)c->d_img.p,
+                                                        hs * hs, meta);
         c->launches += 1;
     }
-    if (!rebuild) return MG_OK;
-    return build_list(c, dx, dy, dz, false);
+    const int ncx = c->ncx, ncy = c->ncy, ncol = ncx * ncy;
+    const double cwx = c->lx / ncx, cwy = c->ly / ncy;
+    int *col_of = (int *)c->d_col_sorted.p + n;
+    const bool fp64 = c->opt.precision == MG_PREC_FP64;
+    k_zero<<<(ncol + 255) / 256, 256, 0, s>>>((int *)c->d_col_count.p, ncol + 1, meta);
+    k_zero<<<1, 32, 0, s>>>((int *)c->d_counter.p, 4, meta);
+    k_bin<<<(n + 255) / 256, 256, 0, s>>>(n, ncol, dx, dy, dz, c->lx, c->ly, c->lz, cwx, cwy, ncx, ncy,
+                                           (double *)c->d_xbuild.p, (double *)c->d_img.p, col_of,
+                                           (int *)c->d_col_count.p, meta);
+    k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_count.p, (int *)c->d_col_start.p, (int *)c->d_col_fill.p, nullptr,
+                              meta + META_MAXCOL, meta);
+    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, col_of, (int *)c->d_col_start.p, (int *)c->d_col_fill.p,
+                                              (int *)c->d_col_sorted.p, meta);
+    k_sort_columns<<<ncol, 256, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, (double *)c->d_xbuild.p,
+                                       c->zcap, (int *)c->d_col_ncl.p, (unsigned *)c->d_flags.p, meta);
+    k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, nullptr, meta + META_NCL, nullptr,
+                              meta);
+    k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p,
+                                         (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p, c->zcap, c->cl_cap,
+                                         (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, (double *)c->d_cl_bb.p,
+                                         (float *)c->d_cl_bbf.p, (unsigned *)c->d_flags.p, meta);
+    if (c->small_box) {
+        long long tot = (long long)c->cl_cap * c->cl_cap;
+        unsigned blocks = (unsigned)std::min<long long>((tot + 255) / 256, 65535);
+        k_all_pairs<<<blocks, 256, 0, s>>>(meta, (double *)c->d_cl_ref.p, (int *)c->d_pair_start.p,
+                                           (int *)c->d_pair_count.p, (int *)c->d_pair_j.p, c->d_pair_shift.p,
+                                           (int *)c->d_pair_img.p, fp64, c->pair_cap, (unsigned *)c->d_flags.p);
+    } else {
+        SearchArgs A;
+        A.ncx = ncx;
+        A.ncy = ncy;
+        A.lx = c->lx;
+        A.ly = c->ly;
+        A.lz = c->lz;
+        A.cwx = cwx;
+        A.cwy = cwy;
+        A.rlist = rlist;
+        A.rlist2 = rlist * rlist;
+        // FP32 rounding of the boxes, shifts and gaps is below 8 u max(L) per gap
+        // (u = 2^-24); the band is four times the resulting bound on d^2
+        double L = std::max(c->lx, std::max(c->ly, c->lz));
+        double u = 5.960464477539063e-08;
+        double m = 4.0 * (3.0 * 2.0 * rlist * 8.0 * u * 2.0 * L + 6.0 * u * rlist * rlist) + 1e-30;
+        A.flo = (float)(rlist * rlist - m);
+        A.fhi = (float)(rlist * rlist + m);
+        A.fmarg = (float)(64.0 * u * 2.0 * L + 1e-6 * rlist);
+        A.meta = meta;
+        A.meta_w = meta;
+        A.bb = (double *)c->d_cl_bb.p;
+        A.bbf = (float *)c->d_cl_bbf.p;
+        A.ref = (double *)c->d_cl_ref.p;
+        A.col_cl_start = (int *)c->d_col_cl_start.p;
+        A.pair_start = (int *)c->d_pair_start.p;
+        A.pair_cnt = (int *)c->d_pair_count.p;
+        A.pair_j = (int *)c->d_pair_j.p;
+        A.pair_img = (int *)c->d_pair_img.p;
+        A.pair_shift = c->d_pair_shift.p;
+        A.counter = (unsigned long long *)c->d_counter.p;
+        A.cap = c->pair_cap;
+        A.fp64 = fp64;
+        A.flags = (unsigned *)c->d_flags.p;
+        unsigned blocks = (unsigned)(((long long)c->cl_cap * 32 + 127) / 128);
+        k_search<<<blocks, 128, 0, s>>>(A);
+    }
+    k_finish<<<1, 1, 0, s>>>(meta, (unsigned long long *)c->d_counter.p);
+    MG_CUDA(cudaGetLastError());
+    c->launches += 10;
+    c->list_valid = true;
+    return MG_OK;
 }
 
 mg_status mg_pack_clusters(mg_ctx *c, const double *dx, const double *dy, const double *dz) {
-    int ncl = c->ncl, n = c->natom;
+    int n = c->natom;
     bool fp64 = c->opt.precision == MG_PREC_FP64;
-    size_t slots = (size_t)ncl * MG_CL;
+    size_t slots = (size_t)c->cl_cap * MG_CL;
     if (!mg_ensure(c, c->d_pack_pos, slots * (fp64 ? sizeof(double4) : sizeof(float4))) ||
         !mg_ensure(c, c->d_pack_lj, slots * (fp64 ? sizeof(double2) : sizeof(float2))) ||
         !mg_ensure(c, c->d_pack_info, slots * sizeof(int)))
         return MG_ERR_ALLOC;
     unsigned blocks = (unsigned)((slots + 255) / 256);
+    const int *meta = (const int *)c->d_meta.p;
     if (fp64)
         k_pack<double4, double2, double><<<blocks, 256, 0, c->stream>>>(
-            ncl, n, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, dx, dy, dz, (double *)c->d_img.p,
+            n, meta, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, dx, dy, dz, (double *)c->d_img.p,
             (double *)c->d_site_q.p, (double *)c->d_site_hsig.p, (double *)c->d_site_seps.p, (int *)c->d_site_mol.p,
             (int *)c->d_site_flags.p, (double4 *)c->d_pack_pos.p, (double2 *)c->d_pack_lj.p, (int *)c->d_pack_info.p);
     else
         k_pack<float4, float2, float><<<blocks, 256, 0, c->stream>>>(
-            ncl, n, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, dx, dy, dz, (double *)c->d_img.p,
+            n, meta, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, dx, dy, dz, (double *)c->d_img.p,
             (double *)c->d_site_q.p, (double *)c->d_site_hsig.p, (double *)c->d_site_seps.p, (int *)c->d_site_mol.p,
             (int *)c->d_site_flags.p, (float4 *)c->d_pack_pos.p, (float2 *)c->d_pack_lj.p, (int *)c->d_pack_info.p);
     MG_CUDA(cudaGetLastError());
@@ -557,35 +662,73 @@ mg_status mg_pack_clusters(mg_ctx *c, const double *dx, const double *dy, const 
     return MG_OK;
 }
 
-extern "C" mg_status mg_debug_get_list(mg_ctx *c, int *ncl, long long *npairs, int *grid, int *cluster_atoms,
-                                       int *pairs, int *shifts) {
+// Adjust the list set-up after a call whose status word asked for it; returns true when
+// the call must be repeated.
+bool mg_list_retry(mg_ctx *c, unsigned flags, const int *meta_host) {
+    bool retry = false;
+    if (flags & MG_FLAG_COLUMN_OVERFLOW) {
+        c->col_refine += 1;
+        retry = true;
+    }
+    if (flags & MG_FLAG_SMALL_BOX) {
+        c->small_box_forced = true;
+        retry = true;
+    }
+    if (flags & MG_FLAG_LIST_OVERFLOW) {
+        long long need = *(const long long *)(meta_host + META_NPAIRS);
+        int ncl = meta_host[META_NCL];
+        if (ncl > c->cl_cap) c->cl_cap = ncl + ncl / 8 + 16;
+        if (need > c->pair_cap) c->pair_cap = need + need / 4 + 1024;
+        else c->pair_cap = c->pair_cap * 2;
+        retry = true;
+    }
+    if (retry) c->list_valid = false;
+    return retry;
+}
+
+extern "C" mg_status mg_debug_get_list(mg_ctx *c, int *ncl, long long *npairs, int *grid, double *zcap,
+                                       int *cluster_atoms, int *pairs, int *shifts) {
     if (!c || !ncl || !npairs) return MG_ERR_INVALID;
     cudaSetDevice(c->device);
-    *ncl = c->list_valid ? c->ncl : 0;
-    *npairs = c->list_valid ? c->npairs : 0;
+    *ncl = 0;
+    *npairs = 0;
+    if (zcap) *zcap = c->zcap;
     if (grid) {
         grid[0] = c->ncx;
         grid[1] = c->ncy;
         grid[2] = c->small_box ? 1 : 0;
     }
     if (!c->list_valid) return MG_OK;
+    int meta[8];
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    MG_CUDA(cudaMemcpy(meta, c->d_meta.p, sizeof(meta), cudaMemcpyDeviceToHost));
+    int n = meta[META_NCL];
+    std::vector<int> start(n), cnt(n);
+    MG_CUDA(cudaMemcpy(start.data(), c->d_pair_start.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    MG_CUDA(cudaMemcpy(cnt.data(), c->d_pair_count.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    long long tot = 0;
+    for (int I = 0; I < n; I++) tot += cnt[I];
+    *ncl = n;
+    *npairs = tot;
     if (cluster_atoms)
-        MG_CUDA(cudaMemcpy(cluster_atoms, c->d_cl_atom.p, sizeof(int) * (size_t)c->ncl * MG_CL, cudaMemcpyDeviceToHost));
+        MG_CUDA(cudaMemcpy(cluster_atoms, c->d_cl_atom.p, sizeof(int) * (size_t)n * MG_CL, cudaMemcpyDeviceToHost));
     if (pairs || shifts) {
-        std::vector<int> start(c->ncl + 1), pj(c->npairs), img(c->npairs);
-        MG_CUDA(cudaMemcpy(start.data(), c->d_pair_start.p, sizeof(int) * (c->ncl + 1), cudaMemcpyDeviceToHost));
-        MG_CUDA(cudaMemcpy(pj.data(), c->d_pair_j.p, sizeof(int) * c->npairs, cudaMemcpyDeviceToHost));
-        MG_CUDA(cudaMemcpy(img.data(), c->d_pair_img.p, sizeof(int) * c->npairs, cudaMemcpyDeviceToHost));
-        for (int I = 0; I < c->ncl; I++)
-            for (int e = start[I]; e < start[I + 1]; e++) {
+        long long used = *(long long *)(meta + META_NPAIRS);
+        if (c->small_box) used = (long long)n * n;
+        std::vector<int> pj(used), img(used);
+        MG_CUDA(cudaMemcpy(pj.data(), c->d_pair_j.p, sizeof(int) * used, cudaMemcpyDeviceToHost));
+        MG_CUDA(cudaMemcpy(img.data(), c->d_pair_img.p, sizeof(int) * used, cudaMemcpyDeviceToHost));
+        long long o = 0;
+        for (int I = 0; I < n; I++)
+            for (int e = start[I]; e < start[I] + cnt[I]; e++, o++) {
                 if (pairs) {
-                    pairs[2 * (size_t)e] = I;
-                    pairs[2 * (size_t)e + 1] = pj[e];
+                    pairs[2 * o] = I;
+                    pairs[2 * o + 1] = pj[e];
                 }
                 if (shifts) {
-                    shifts[3 * (size_t)e] = (img[e] & 1023) - 512;
-                    shifts[3 * (size_t)e + 1] = ((img[e] >> 10) & 1023) - 512;
-                    shifts[3 * (size_t)e + 2] = ((img[e] >> 20) & 1023) - 512;
+                    shifts[3 * o] = (img[e] & 1023) - 512;
+                    shifts[3 * o + 1] = ((img[e] >> 10) & 1023) - 512;
+                    shifts[3 * o + 2] = ((img[e] >> 20) & 1023) - 512;
                 }
             }
     }

@@ -47,8 +47,9 @@ struct RT<double> {
 };
 
 struct PairArgs {
-    int ncl, n;
-    const int *pair_start, *pair_j, *info, *cl_atom;
+    int n;
+    const int *meta;  // meta[0] = number of clusters of the current build
+    const int *pair_start, *pair_cnt, *pair_j, *info, *cl_atom;
     const void *pair_shift, *pos, *lj;
     double *fl, *fs;
     double rc2, rce2, rs2, rmax2;
@@ -72,7 +73,7 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     // FP64 accumulators: force (long, short) and energies
     double fL[3] = {0, 0, 0}, fS[3] = {0, 0, 0};
     double eng[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // uvdw ushift ureal vir (long), same (short), npair
-    if (I < A.ncl) {
+    if (I < A.meta[0]) {
         const V4 *pos = (const V4 *)A.pos;
         const V2 *lj = (const V2 *)A.lj;
         const V4 *shift = (const V4 *)A.pair_shift;
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
         R ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
         R e_vdw = 0, e_sh = 0, e_re = 0, e_vir = 0, s_vdw = 0, s_sh = 0, s_re = 0, s_vir = 0;
         int npair = 0;
-        const int e0 = A.pair_start[I], e1 = A.pair_start[I + 1];
+        const int e0 = A.pair_start[I], e1 = e0 + A.pair_cnt[I];
         int steps = 0;
         for (int e = e0; e < e1; e += 4) {
             const int me = e + (lane >> 3);
@@ -270,9 +271,10 @@ __global__ void k_check(const double *__restrict__ f, int n3, unsigned *__restri
 mg_status mg_launch_pair(mg_ctx *c, int want_long, int want_short, double *fl, double *fs) {
     const mg_params &p = c->params;
     PairArgs A;
-    A.ncl = c->ncl;
     A.n = c->natom;
+    A.meta = (const int *)c->d_meta.p;
     A.pair_start = (int *)c->d_pair_start.p;
+    A.pair_cnt = (int *)c->d_pair_count.p;
     A.pair_j = (int *)c->d_pair_j.p;
     A.pair_shift = c->d_pair_shift.p;
     A.pos = c->d_pack_pos.p;
@@ -304,7 +306,7 @@ mg_status mg_launch_pair(mg_ctx *c, int want_long, int want_short, double *fl, d
     A.f2 = p.wolffcon2;
     A.ljsw = p.lj_switch;
     A.mode = (want_long ? 1 : 0) | (want_short ? 2 : 0);
-    unsigned blocks = (unsigned)((c->ncl + PAIR_WPB - 1) / PAIR_WPB);
+    unsigned blocks = (unsigned)((c->cl_cap + PAIR_WPB - 1) / PAIR_WPB);
     if (blocks == 0) return MG_OK;
     A.rows = (double *)c->d_epart.p;
     A.row0 = mg_reserve_rows(c, blocks);

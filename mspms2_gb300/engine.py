@@ -66,8 +66,8 @@ def load_library(path: str = LIB_PATH):
     lib.mg_compute_device.argtypes = [V, V, V, V, I, V, V, V, V, V, V, C.POINTER(MgEnergies)]
     lib.mg_get_stats.argtypes = [V, C.POINTER(MgStats)]
     lib.mg_get_device_flags.argtypes = [V, C.POINTER(C.c_uint)]
-    lib.mg_debug_get_list.argtypes = [V, C.POINTER(I), C.POINTER(C.c_longlong), C.POINTER(I), C.POINTER(I),
-                                      C.POINTER(I), C.POINTER(I)]
+    lib.mg_debug_get_list.argtypes = [V, C.POINTER(I), C.POINTER(C.c_longlong), C.POINTER(I),
+                                      C.POINTER(D), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     lib.mg_abi_version.restype = I
     _lib = lib
     return lib
@@ -189,18 +189,19 @@ class Engine:
         return f.value
 
     def debug_list(self):
-        ncl, npairs = C.c_int(), C.c_longlong()
+        ncl, npairs, zcap = C.c_int(), C.c_longlong(), C.c_double()
         grid = (C.c_int * 3)()
-        self._check(self.lib.mg_debug_get_list(self.ctx, C.byref(ncl), C.byref(npairs), grid, None, None, None))
+        self._check(self.lib.mg_debug_get_list(self.ctx, C.byref(ncl), C.byref(npairs), grid, C.byref(zcap),
+                                               None, None, None))
         cl = np.zeros(ncl.value * 8, np.int32)
         pairs = np.zeros(2 * npairs.value, np.int32)
         shifts = np.zeros(3 * npairs.value, np.int32)
         ip = C.POINTER(C.c_int)
-        self._check(self.lib.mg_debug_get_list(self.ctx, C.byref(ncl), C.byref(npairs), grid,
+        self._check(self.lib.mg_debug_get_list(self.ctx, C.byref(ncl), C.byref(npairs), grid, C.byref(zcap),
                                                cl.ctypes.data_as(ip), pairs.ctypes.data_as(ip),
                                                shifts.ctypes.data_as(ip)))
-        return {"grid": list(grid), "clusters": cl.reshape(-1, 8), "pairs": pairs.reshape(-1, 2),
-                "shifts": shifts.reshape(-1, 3)}
+        return {"grid": list(grid), "zcap": zcap.value, "clusters": cl.reshape(-1, 8),
+                "pairs": pairs.reshape(-1, 2), "shifts": shifts.reshape(-1, 3)}
 
     def close(self) -> None:
         if getattr(self, "ctx", None) and self.ctx.value:

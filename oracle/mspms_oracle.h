@@ -94,7 +94,7 @@ int orc_nblist_build(const double *x, const double *y, const double *z, int nato
                      int *out_ncl, int *cluster_atoms, int cluster_cap,
                      long long *out_npairs, int *pairs, int *shifts, long long pair_cap);
 int orc_nblist_build2(const double *x, const double *y, const double *z, int natom, double lx,
-                      double ly, double lz, double rlist, int ncx, int ncy, int small, int *out_ncl,
+                      double ly, double lz, double rlist, int ncx, int ncy, int small, double zcap, int *out_ncl,
                       int *cluster_atoms, int cluster_cap, long long *out_npairs, int *pairs,
                       int *shifts, long long pair_cap);
 

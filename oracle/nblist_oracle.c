@@ -37,8 +37,9 @@ static double gap2(double loi, double hii, double loj, double hij, double s) {
 }
 
 int orc_nblist_build2(const double *x, const double *y, const double *z, int n, double lx, double ly,
-                      double lz, double rlist, int ncx, int ncy, int small, int *out_ncl, int *cluster_atoms,
-                      int cluster_cap, long long *out_npairs, int *pairs, int *shifts, long long pair_cap) {
+                      double lz, double rlist, int ncx, int ncy, int small, double zcap, int *out_ncl,
+                      int *cluster_atoms, int cluster_cap, long long *out_npairs, int *pairs, int *shifts,
+                      long long pair_cap) {
     double L[3] = {lx, ly, lz};
     const double *P[3] = {x, y, z};
     double *w = (double *)malloc(sizeof(double) * 3 * (size_t)n);
@@ -55,44 +56,56 @@ int orc_nblist_build2(const double *x, const double *y, const double *z, int n, 
         cnt[col[a]]++;
     }
     int *start = (int *)calloc((size_t)ncol + 1, sizeof(int));
-    int *clstart = (int *)calloc((size_t)ncol + 1, sizeof(int));
-    for (int c = 0; c < ncol; c++) {
-        start[c + 1] = start[c] + cnt[c];
-        clstart[c + 1] = clstart[c] + (cnt[c] + CL - 1) / CL;
-    }
-    int ncl = clstart[ncol];
-    *out_ncl = ncl;
+    for (int c = 0; c < ncol; c++) start[c + 1] = start[c] + cnt[c];
     key *keys = (key *)malloc(sizeof(key) * (size_t)(n > 0 ? n : 1));
     int *fill = (int *)calloc((size_t)ncol, sizeof(int));
     for (int a = 0; a < n; a++) {
         int c = col[a];
         keys[start[c] + fill[c]++] = (key){w[2 * (size_t)n + a], a};
     }
-    double *bb = (double *)malloc(sizeof(double) * 6 * (size_t)(ncl > 0 ? ncl : 1));
-    double *ref = (double *)malloc(sizeof(double) * 3 * (size_t)(ncl > 0 ? ncl : 1));
-    int *catoms = (int *)malloc(sizeof(int) * CL * (size_t)(ncl > 0 ? ncl : 1));
+    /* clusters: consecutive z-sorted sites of a column, cut after 8 sites or when a site
+       lies more than zcap above the cluster's first site */
+    int *clstart = (int *)calloc((size_t)ncol + 1, sizeof(int));
+    int ncl = 0;
     for (int c = 0; c < ncol; c++) {
         qsort(keys + start[c], (size_t)cnt[c], sizeof(key), key_cmp);
-        int nq = (cnt[c] + CL - 1) / CL;
-        for (int q = 0; q < nq; q++) {
-            int cl = clstart[c] + q;
-            double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            for (int s = 0; s < CL; s++) {
-                int i = q * CL + s;
-                int a = i < cnt[c] ? keys[start[c] + i].i : -1;
-                catoms[(size_t)cl * CL + s] = a;
-                if (a < 0) continue;
-                for (int d = 0; d < 3; d++) {
-                    double v = w[(size_t)d * n + a];
-                    lo[d] = fmin(lo[d], v);
-                    hi[d] = fmax(hi[d], v);
+        clstart[c] = ncl;
+        int first = 0;
+        for (int i = 0; i < cnt[c]; i++)
+            if (i == 0 || i - first == CL || keys[start[c] + i].z - keys[start[c] + first].z > zcap) {
+                ncl++;
+                first = i;
+            }
+    }
+    clstart[ncol] = ncl;
+    *out_ncl = ncl;
+    double *bb = (double *)malloc(sizeof(double) * 6 * (size_t)(ncl > 0 ? ncl : 1));
+    int *catoms = (int *)malloc(sizeof(int) * CL * (size_t)(ncl > 0 ? ncl : 1));
+    for (int c = 0; c < ncol; c++) {
+        int q = clstart[c], first = 0;
+        for (int i = 0; i <= cnt[c]; i++) {
+            int cut = (i == cnt[c]) || (i > 0 && (i - first == CL ||
+                                                  keys[start[c] + i].z - keys[start[c] + first].z > zcap));
+            if (!cut) continue;
+            if (i > 0) {
+                double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+                for (int s = 0; s < CL; s++) {
+                    int a = first + s < i ? keys[start[c] + first + s].i : -1;
+                    catoms[(size_t)q * CL + s] = a;
+                    if (a < 0) continue;
+                    for (int d = 0; d < 3; d++) {
+                        double v = w[(size_t)d * n + a];
+                        lo[d] = fmin(lo[d], v);
+                        hi[d] = fmax(hi[d], v);
+                    }
                 }
+                for (int d = 0; d < 3; d++) {
+                    bb[(size_t)q * 6 + d] = lo[d];
+                    bb[(size_t)q * 6 + 3 + d] = hi[d];
+                }
+                q++;
             }
-            for (int d = 0; d < 3; d++) {
-                bb[(size_t)cl * 6 + d] = lo[d];
-                bb[(size_t)cl * 6 + 3 + d] = hi[d];
-                ref[(size_t)cl * 3 + d] = 0.5 * (lo[d] + hi[d]);
-            }
+            first = i;
         }
     }
     if (cluster_atoms && ncl * CL <= cluster_cap) memcpy(cluster_atoms, catoms, sizeof(int) * CL * (size_t)ncl);
@@ -141,7 +154,7 @@ int orc_nblist_build2(const double *x, const double *y, const double *z, int n, 
     }
     *out_npairs = np;
     free(w); free(col); free(cnt); free(start); free(clstart); free(keys); free(fill);
-    free(bb); free(ref); free(catoms);
+    free(bb); free(catoms);
     return 0;
 }
 
@@ -150,11 +163,12 @@ int orc_nblist_build(const double *x, const double *y, const double *z, int nato
                      int cluster_cap, long long *out_npairs, int *pairs, int *shifts,
                      long long pair_cap) {
     double vol = lx * ly * lz;
-    double cw = cbrt(8.0 * vol / natom);
+    double cw = fmin(cbrt(8.0 * vol / natom), 0.75 * rlist);
     int ncx = (int)floor(lx / cw), ncy = (int)floor(ly / cw);
     if (ncx < 1) ncx = 1;
     if (ncy < 1) ncy = 1;
-    int small = lx < 2.0 * rlist + 2.0 * (lx / ncx) || ly < 2.0 * rlist + 2.0 * (ly / ncy) || lz < 2.0 * rlist;
-    return orc_nblist_build2(x, y, z, natom, lx, ly, lz, rlist, ncx, ncy, small, out_ncl, cluster_atoms,
+    int small = lx < 2.0 * rlist + 2.0 * (lx / ncx) || ly < 2.0 * rlist + 2.0 * (ly / ncy) ||
+                lz < 2.0 * rlist + 2.0 * cw;
+    return orc_nblist_build2(x, y, z, natom, lx, ly, lz, rlist, ncx, ncy, small, cw, out_ncl, cluster_atoms,
                              cluster_cap, out_npairs, pairs, shifts, pair_cap);
 }

@@ -209,23 +209,23 @@ def run_reference_system(system: System, repeat: int = 0):
         return run_reference_dir(td, repeat)
 
 
-def nblist(x, y, z, box, rlist, ncx, ncy, small):
+def nblist(x, y, z, box, rlist, ncx, ncy, small, zcap):
     """CPU cluster-pair list (same algorithm and FP64 op order as the GPU build)."""
     L = lib()
     L.orc_nblist_build2.argtypes = [_dp, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
-                                    C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
+                                    C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
                                     C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.c_longlong]
     x, y, z = (np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, z))
     n = len(x)
     ncl, npairs = C.c_int(), C.c_longlong()
     ip = C.POINTER(C.c_int)
-    L.orc_nblist_build2(_ptr(x), _ptr(y), _ptr(z), n, *box, rlist, ncx, ncy, small, C.byref(ncl), None, 0,
+    L.orc_nblist_build2(_ptr(x), _ptr(y), _ptr(z), n, *box, rlist, ncx, ncy, small, zcap, C.byref(ncl), None, 0,
                         C.byref(npairs), None, None, 0)
     cl = np.zeros(ncl.value * 8, np.int32)
     pairs = np.zeros(2 * npairs.value, np.int32)
     shifts = np.zeros(3 * npairs.value, np.int32)
-    L.orc_nblist_build2(_ptr(x), _ptr(y), _ptr(z), n, *box, rlist, ncx, ncy, small, C.byref(ncl),
+    L.orc_nblist_build2(_ptr(x), _ptr(y), _ptr(z), n, *box, rlist, ncx, ncy, small, zcap, C.byref(ncl),
                         cl.ctypes.data_as(ip), len(cl), C.byref(npairs), pairs.ctypes.data_as(ip),
                         shifts.ctypes.data_as(ip), npairs.value)
     return {"clusters": cl.reshape(-1, 8), "pairs": pairs.reshape(-1, 2), "shifts": shifts.reshape(-1, 3)}
