@@ -14,11 +14,16 @@
 // and no recurrence. Tables per site: X[0..KMAXX], Y[0..KMAXY], Z[0..KMAXZ].
 //
 // k-vectors are grouped in rows (kx, ky) holding |kz| = 0..kzmax(kx,ky) with both signs
-// of kz. Structure factors: a thread owns (row, 8 consecutive |kz|) = up to 16 k-vectors;
-// the block stages a tile of site tables in shared memory and accumulates in R over the
-// tile, then in FP64; each block writes FP64 partial S for its site range; a
-// fixed-order reduction over site blocks gives S(k) (deterministic). Forces: a thread
-// owns a site and walks all rows, the coefficients c_k S(k) broadcast from shared memory.
+// of kz. Structure factors: a thread owns (row, up to 8 consecutive |kz|) = up to 16
+// k-vectors, chunks balanced per row; tasks are sorted by length and each length group
+// padded to whole warps, so a warp runs one unrolled loop; the block stages tiles of
+// site tables in shared memory and sums its EW_SITES sites in R; a fixed-order FP64
+// reduction over site blocks gives S(k) (deterministic).
+// Forces: for one site and one row the kz sums are two complex polynomials in Z = e^{i
+// theta_z}, P(Z) = sum_a conj(c S+_a) Z^a and Q(Z) = sum_a c S-_a Z^a, and the z force
+// needs their derivatives; all four are evaluated by Horner's rule (16 FMA per |kz|, no
+// power recurrence). Four thread groups share the rows of a site; their partial forces
+// are combined in shared memory in a fixed order.
 #include <math.h>
 
 #include <algorithm>
@@ -26,10 +31,12 @@
 #include "mg_internal.cuh"
 
 #define EW_TILE 64      // sites per shared-memory tile in the S(k) pass
-#define EW_CH 8         // |kz| values per thread in the S(k) pass
+#define EW_CH 8         // |kz| values per thread in the S(k) pass (at most)
 #define EW_TPB 128      // threads per block in the S(k) pass
-#define EW_SITES 4096   // sites per block in the S(k) pass
+#define EW_SITES 512    // sites per block in the S(k) pass (summed in R)
 #define EW_FROWS 32     // rows staged per step in the force pass
+#define EW_FG 4         // thread groups sharing the rows of a site in the force pass
+#define EW_FSITES 64    // sites per force block (EW_FG * EW_FSITES threads)
 
 namespace {
 
@@ -38,10 +45,12 @@ struct C2;
 template <>
 struct C2<float> {
     typedef float2 T;
+    typedef float4 T4;
 };
 template <>
 struct C2<double> {
     typedef double2 T;
+    typedef double4 T4;
 };
 
 template <typename T>
@@ -49,6 +58,15 @@ __device__ __forceinline__ T cmul(T a, T b) {
     T r;
     r.x = a.x * b.x - a.y * b.y;
     r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+// x <- x*z + c
+template <typename T>
+__device__ __forceinline__ T cfma(T x, T z, T c) {
+    T r;
+    r.x = fma(x.x, z.x, fma(-x.y, z.y, c.x));
+    r.y = fma(x.x, z.y, fma(x.y, z.x, c.y));
     return r;
 }
 
@@ -106,12 +124,12 @@ struct EwArgs {
     int n, nrows, nslots, ntasks;
     int kx, ky, kz;  // KMAX per axis (table extents)
     const int4 *rows;       // kx, ky, kzmax, half_only
-    const int *row_slot;    // first slot of each row
-    const int2 *tasks;      // (row, first |kz|)
+    const int *row_slot;    // first slot of each row (two slots per |kz|: +kz, -kz)
+    const int4 *tasks;      // row, first |kz|, count, -
     const void *tab;
     const double *q;
-    double *spart;          // [site blocks][nslots][2]
-    void *scoef;            // [nslots] R2: 4*Vfactor*C*kvec*S
+    void *spart;            // [site blocks][nslots][2] R
+    void *scoef;            // [nslots] R2: plus slots conj(c S), minus slots c S
     double twopi[3];
     double bfac, vfac, coul;
     double *rows_e;
@@ -119,6 +137,37 @@ struct EwArgs {
     double *f;
 };
 
+// One tile of sites for a thread owning CH consecutive |kz| of one row: straight-line
+// code, A*Z and A*conj(Z) sharing four products, Z advanced by the site's Z1.
+template <typename R, int CH, typename T2>
+__device__ __forceinline__ void sk_tile(const T2 *sX, const T2 *sY, const T2 *sZ, const R *sQ, int P, int tn,
+                                        int kx, int aky, R ysign, int kz0, R (&pP)[EW_CH][2], R (&pM)[EW_CH][2]) {
+    for (int s = 0; s < tn; s++) {
+        T2 X = sX[kx * P + s];
+        T2 Y = sY[aky * P + s];
+        Y.y *= ysign;
+        const R q = sQ[s];
+        T2 Aq = cmul(X, Y);
+        Aq.x *= q;
+        Aq.y *= q;
+        T2 Z = sZ[kz0 * P + s];
+        const T2 Z1 = sZ[1 * P + s];
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            const R p1 = Aq.x * Z.x, p2 = Aq.y * Z.y, p3 = Aq.x * Z.y, p4 = Aq.y * Z.x;
+            pP[j][0] += p1 - p2;
+            pP[j][1] += p3 + p4;
+            pM[j][0] += p1 + p2;
+            pM[j][1] += p4 - p3;
+            if (j + 1 < CH) Z = cmul(Z, Z1);
+        }
+    }
+}
+
+// Structure-factor partials of one block of EW_SITES sites, summed in R (the block sum
+// of this stage); the cross-block sum is done in FP64 by k_sk_reduce. Task counts are
+// uniform within a warp (tasks sorted by count and padded per count to whole warps),
+// so the switch below does not diverge.
 template <typename R>
 __global__ void __launch_bounds__(EW_TPB) k_sk(EwArgs A) {
     typedef typename C2<R>::T T2;
@@ -131,23 +180,22 @@ __global__ void __launch_bounds__(EW_TPB) k_sk(EwArgs A) {
     const T2 *tab = (const T2 *)A.tab;
     const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
     const int task = blockIdx.x * EW_TPB + threadIdx.x;
-    int kx = 0, ky = 0, kzmax = -1, half = 0, kz0 = 0, slot0 = 0;
+    int kx = 0, ky = 0, half = 0, kz0 = 0, cnt = 0, slot0 = 0;
     if (task < A.ntasks) {
-        int2 t = A.tasks[task];
+        int4 t = A.tasks[task];
         int4 r = A.rows[t.x];
         kx = r.x;
         ky = r.y;
-        kzmax = r.z;
         half = r.w;
         kz0 = t.y;
+        cnt = t.z;
         slot0 = A.row_slot[t.x];
     }
-    const int cnt = max(0, min(EW_CH, kzmax - kz0 + 1));
     const int aky = ky < 0 ? -ky : ky;
     const R ysign = ky < 0 ? (R)-1 : (R)1;
-    double accP[EW_CH][2], accM[EW_CH][2];
+    R pP[EW_CH][2], pM[EW_CH][2];
 #pragma unroll
-    for (int j = 0; j < EW_CH; j++) accP[j][0] = accP[j][1] = accM[j][0] = accM[j][1] = 0.0;
+    for (int j = 0; j < EW_CH; j++) pP[j][0] = pP[j][1] = pM[j][0] = pM[j][1] = (R)0;
     const int a_begin = blockIdx.y * EW_SITES, a_end = min(A.n, a_begin + EW_SITES);
     for (int t0 = a_begin; t0 < a_end; t0 += EW_TILE) {
         const int tn = min(EW_TILE, a_end - t0);
@@ -166,53 +214,31 @@ __global__ void __launch_bounds__(EW_TPB) k_sk(EwArgs A) {
         }
         for (int s = threadIdx.x; s < tn; s += EW_TPB) sQ[s] = (R)A.q[t0 + s];
         __syncthreads();
-        if (cnt == 0) continue;
-        R pP[EW_CH][2], pM[EW_CH][2];
-#pragma unroll
-        for (int j = 0; j < EW_CH; j++) pP[j][0] = pP[j][1] = pM[j][0] = pM[j][1] = (R)0;
-        for (int s = 0; s < tn; s++) {
-            T2 X = sX[kx * P + s];
-            T2 Y = sY[aky * P + s];
-            Y.y *= ysign;
-            const R q = sQ[s];
-            T2 Aq = cmul(X, Y);
-            Aq.x *= q;
-            Aq.y *= q;
-            T2 Z = sZ[kz0 * P + s];
-            const T2 Z1 = sZ[1 * P + s];
-#pragma unroll
-            for (int j = 0; j < EW_CH; j++) {
-                // A*Z and A*conj(Z) share four products
-                const R p1 = Aq.x * Z.x, p2 = Aq.y * Z.y, p3 = Aq.x * Z.y, p4 = Aq.y * Z.x;
-                pP[j][0] += p1 - p2;
-                pP[j][1] += p3 + p4;
-                pM[j][0] += p1 + p2;
-                pM[j][1] += p4 - p3;
-                Z = cmul(Z, Z1);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < EW_CH; j++) {
-            accP[j][0] += pP[j][0];
-            accP[j][1] += pP[j][1];
-            accM[j][0] += pM[j][0];
-            accM[j][1] += pM[j][1];
+        switch (cnt) {
+        case 8: sk_tile<R, 8>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 7: sk_tile<R, 7>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 6: sk_tile<R, 6>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 5: sk_tile<R, 5>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 4: sk_tile<R, 4>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 3: sk_tile<R, 3>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 2: sk_tile<R, 2>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 1: sk_tile<R, 1>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        default: break;
         }
     }
-    if (task >= A.ntasks) return;
-    double *out = A.spart + (size_t)blockIdx.y * A.nslots * 2;
+    if (task >= A.ntasks || cnt == 0) return;
+    R *out = (R *)A.spart + (size_t)blockIdx.y * A.nslots * 2;
 #pragma unroll
     for (int j = 0; j < EW_CH; j++) {
         if (j >= cnt) break;
         int a = kz0 + j;
         int sp = slot0 + 2 * a, sm = sp + 1;
-        out[2 * sp] = accP[j][0];
-        out[2 * sp + 1] = accP[j][1];
+        out[2 * sp] = pP[j][0];
+        out[2 * sp + 1] = pP[j][1];
         bool has_minus = (a > 0) && !half;
-        out[2 * sm] = has_minus ? accM[j][0] : 0.0;
-        out[2 * sm + 1] = has_minus ? accM[j][1] : 0.0;
+        out[2 * sm] = has_minus ? pM[j][0] : (R)0;
+        out[2 * sm + 1] = has_minus ? pM[j][1] : (R)0;
     }
-    (void)half;
 }
 
 // S(k) from the partials in site-block order; energy rows and force coefficients
@@ -224,9 +250,9 @@ __global__ void k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row
     if (slot < A.nslots) {
         double sr = 0.0, si = 0.0;
         for (int b = 0; b < nblk; b++) {
-            const double *p = A.spart + ((size_t)b * A.nslots + slot) * 2;
-            sr += p[0];
-            si += p[1];
+            const R *p = (const R *)A.spart + ((size_t)b * A.nslots + slot) * 2;
+            sr += (double)p[0];
+            si += (double)p[1];
         }
         int r = slot_row[slot];
         int4 row = A.rows[r];
@@ -243,7 +269,7 @@ __global__ void k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row
             e[0] = 2.0 * kvec * (sr * sr + si * si) * A.vfac * A.coul;
             double cf = 4.0 * A.vfac * A.coul * kvec;
             c.x = (R)(cf * sr);
-            c.y = (R)(cf * si);
+            c.y = (R)(minus ? cf * si : -cf * si);  // plus slots hold conj(c S)
         }
         ((T2 *)A.scoef)[slot] = c;
     }
@@ -252,68 +278,92 @@ __global__ void k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_kforce(EwArgs A, int maxslots_per_row) {
+__global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa) {
     typedef typename C2<R>::T T2;
+    typedef typename C2<R>::T4 T4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2 *sC = (T2 *)smem_raw;  // [EW_FROWS][maxslots]
+    T4 *sC = (T4 *)smem_raw;  // [EW_FROWS][maxa]: conj(c S+_a), c S-_a
     __shared__ int4 sRow[EW_FROWS];
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double sF[EW_FG][3][EW_FSITES];
+    const int g = threadIdx.x / EW_FSITES, l = threadIdx.x % EW_FSITES;
+    const int a = blockIdx.x * EW_FSITES + l;
     const bool act = a < A.n;
     const T2 *tab = (const T2 *)A.tab;
     const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
-    const T2 Z1 = act ? tZ[(size_t)1 * A.n + a] : T2();
-    const R tx = (R)A.twopi[0], ty = (R)A.twopi[1], tz = (R)A.twopi[2];
+    T2 Z;
+    if (act) {
+        Z = tZ[(size_t)1 * A.n + a];
+    } else {
+        Z.x = (R)1;
+        Z.y = (R)0;
+    }
     double F[3] = {0, 0, 0};
+    const T4 *coef = (const T4 *)A.scoef;
     for (int r0 = 0; r0 < A.nrows; r0 += EW_FROWS) {
         const int nr = min(EW_FROWS, A.nrows - r0);
         __syncthreads();
-        for (int i = threadIdx.x; i < nr * maxslots_per_row; i += blockDim.x) {
-            int rr = i / maxslots_per_row, s = i % maxslots_per_row;
+        for (int i = threadIdx.x; i < nr * maxa; i += blockDim.x) {
+            int rr = i / maxa, s = i % maxa;
             int4 row = A.rows[r0 + rr];
-            int ns = 2 * (row.z + 1);
-            T2 v;
-            v.x = v.y = (R)0;
-            if (s < ns) v = ((const T2 *)A.scoef)[A.row_slot[r0 + rr] + s];
-            sC[rr * maxslots_per_row + s] = v;
+            T4 v;
+            v.x = v.y = v.z = v.w = (R)0;
+            if (s <= row.z) v = coef[A.row_slot[r0 + rr] / 2 + s];
+            sC[rr * maxa + s] = v;
         }
         if (threadIdx.x < nr) sRow[threadIdx.x] = A.rows[r0 + threadIdx.x];
         __syncthreads();
         if (!act) continue;
         R fx = 0, fy = 0, fz = 0;
-        for (int rr = 0; rr < nr; rr++) {
+        for (int rr = g; rr < nr; rr += EW_FG) {
             const int4 row = sRow[rr];
             T2 X = tX[(size_t)row.x * A.n + a];
             T2 Y = tY[(size_t)(row.y < 0 ? -row.y : row.y) * A.n + a];
             if (row.y < 0) Y.y = -Y.y;
             const T2 Aa = cmul(X, Y);
-            const T2 *cs = sC + rr * maxslots_per_row;
-            T2 Z;
-            Z.x = (R)1;
-            Z.y = (R)0;
-            R gsum = 0, gz = 0;
-            for (int k = 0; k <= row.z; k++) {
-                const R p1 = Aa.x * Z.x, p2 = Aa.y * Z.y, p3 = Aa.x * Z.y, p4 = Aa.y * Z.x;
-                // W+ = A Z, W- = A conj(Z); g = Im(conj(cS) W) = cS.x W.y - cS.y W.x
-                const T2 cp = cs[2 * k], cm = cs[2 * k + 1];
-                const R gp = cp.x * (p3 + p4) - cp.y * (p1 - p2);
-                const R gm = cm.x * (p4 - p3) - cm.y * (p1 + p2);
-                gsum += gp + gm;
-                gz += (gp - gm) * (R)k;
-                Z = cmul(Z, Z1);
+            const T4 *cs = sC + rr * maxa;
+            // Horner: p = P(Z), dp = P'(Z), q = Q(Z), dq = Q'(Z)
+            T4 top = cs[row.z];
+            T2 p, q, dp, dq;
+            p.x = top.x; p.y = top.y;
+            q.x = top.z; q.y = top.w;
+            dp.x = dp.y = dq.x = dq.y = (R)0;
+            for (int k = row.z - 1; k >= 0; k--) {
+                const T4 c = cs[k];
+                T2 cu, cv;
+                cu.x = c.x; cu.y = c.y;
+                cv.x = c.z; cv.y = c.w;
+                dp = cfma(dp, Z, p);
+                p = cfma(p, Z, cu);
+                dq = cfma(dq, Z, q);
+                q = cfma(q, Z, cv);
             }
+            // sum_a g+ + g- = Im(A p) + Im(A conj(q)); sum_a a (g+ - g-) = Im(A Z dp) - Im(A conj(Z dq))
+            const R gsum = (Aa.x * p.y + Aa.y * p.x) + (Aa.y * q.x - Aa.x * q.y);
+            const T2 zdp = cmul(Z, dp), zdq = cmul(Z, dq);
+            const R gz = (Aa.x * zdp.y + Aa.y * zdp.x) - (Aa.y * zdq.x - Aa.x * zdq.y);
             fx += gsum * (R)row.x;
             fy += gsum * (R)row.y;
             fz += gz;
         }
-        F[0] += (double)fx * (double)tx;
-        F[1] += (double)fy * (double)ty;
-        F[2] += (double)fz * (double)tz;
+        F[0] += (double)fx;
+        F[1] += (double)fy;
+        F[2] += (double)fz;
     }
-    if (!act) return;
+    sF[g][0][l] = F[0];
+    sF[g][1][l] = F[1];
+    sF[g][2][l] = F[2];
+    __syncthreads();
+    if (g != 0 || !act) return;
+    double fxs = 0, fys = 0, fzs = 0;
+    for (int k = 0; k < EW_FG; k++) {
+        fxs += sF[k][0][l];
+        fys += sF[k][1][l];
+        fzs += sF[k][2][l];
+    }
     const double q = A.q[a];
-    A.f[a] += q * F[0];
-    A.f[A.n + a] += q * F[1];
-    A.f[2 * A.n + a] += q * F[2];
+    A.f[a] += q * fxs * A.twopi[0];
+    A.f[A.n + a] += q * fys * A.twopi[1];
+    A.f[2 * A.n + a] += q * fzs * A.twopi[2];
 }
 
 }  // namespace
@@ -323,10 +373,9 @@ mg_status mg_ewald_setup(mg_ctx *c) {
     const mg_params &p = c->params;
     int KX = p.kmax[0], KY = p.kmax[1], KZ = p.kmax[2], KS = p.ksqmax;
     std::vector<int> rows, slot_start, slot_row;
-    std::vector<int> tasks;
+    std::vector<int4> tasks;
     int nslots = 0;
     long long kvec = 0;
-    int maxslots = 2;
     for (int kx = 0; kx <= KX; kx++)
         for (int ky = -KY; ky <= KY; ky++) {
             if (kx == 0 && ky < 0) continue;
@@ -347,17 +396,30 @@ mg_status mg_ewald_setup(mg_ctx *c) {
             int ns = 2 * (kzmax + 1);
             for (int s = 0; s < ns; s++) slot_row.push_back(r);
             nslots += ns;
-            maxslots = std::max(maxslots, ns);
             kvec += half ? kzmax : 2 * kzmax + 1;
-            for (int k0 = 0; k0 <= kzmax; k0 += EW_CH) {
-                tasks.push_back(r);
-                tasks.push_back(k0);
+            int nv = kzmax + 1;
+            int nch = (nv + EW_CH - 1) / EW_CH;
+            for (int h = 0, k0 = 0; h < nch; h++) {  // balanced chunks
+                int len = nv / nch + (h < nv % nch ? 1 : 0);
+                tasks.push_back(make_int4(r, k0, len, 0));
+                k0 += len;
             }
         }
+    std::stable_sort(tasks.begin(), tasks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
+    {  // pad each length group to whole warps with empty tasks (row 0, count 0)
+        std::vector<int4> padded;
+        padded.reserve(tasks.size() + 32 * EW_CH);
+        for (size_t i = 0; i < tasks.size(); i++) {
+            padded.push_back(tasks[i]);
+            if (i + 1 == tasks.size() || tasks[i + 1].z != tasks[i].z)
+                while (padded.size() % 32) padded.push_back(make_int4(0, 0, 0, 0));
+        }
+        tasks.swap(padded);
+    }
     c->nrows = (int)(rows.size() / 4);
     c->nslots = nslots;
     c->kvectors = kvec;
-    c->ntasks = (int)(tasks.size() / 2);
+    c->ntasks = (int)tasks.size();
     c->kmaxx = KX;
     c->kmaxy = KY;
     c->kmaxz = KZ;
@@ -366,16 +428,15 @@ mg_status mg_ewald_setup(mg_ctx *c) {
     c->ewald_box[1] = c->ly;
     c->ewald_box[2] = c->lz;
     if (c->nrows == 0) return MG_OK;
-    std::vector<int> packed(slot_start.size() + slot_row.size() + 1);
+    std::vector<int> packed(slot_start.size() + slot_row.size());
     std::copy(slot_start.begin(), slot_start.end(), packed.begin());
     std::copy(slot_row.begin(), slot_row.end(), packed.begin() + slot_start.size());
-    packed.back() = maxslots;
     if (!mg_ensure(c, c->d_rows, sizeof(int) * rows.size()) || !mg_ensure(c, c->d_row_slot, sizeof(int) * packed.size()) ||
-        !mg_ensure(c, c->d_tasks, sizeof(int) * tasks.size()))
+        !mg_ensure(c, c->d_tasks, sizeof(int4) * tasks.size()))
         return MG_ERR_ALLOC;
     MG_CUDA(cudaMemcpy(c->d_rows.p, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(c->d_row_slot.p, packed.data(), sizeof(int) * packed.size(), cudaMemcpyHostToDevice));
-    MG_CUDA(cudaMemcpy(c->d_tasks.p, tasks.data(), sizeof(int) * tasks.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(c->d_tasks.p, tasks.data(), sizeof(int4) * tasks.size(), cudaMemcpyHostToDevice));
     return MG_OK;
 }
 
@@ -389,7 +450,7 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     const size_t tab_entries = (size_t)(KX + 1 + KY + 1 + KZ + 1) * n;
     const int nblk = (n + EW_SITES - 1) / EW_SITES;
     if (!mg_ensure(c, c->d_phase, esz * tab_entries) ||
-        !mg_ensure(c, c->d_spart, sizeof(double) * 2 * (size_t)c->nslots * nblk) ||
+        !mg_ensure(c, c->d_spart, (esz / 2) * 2 * (size_t)c->nslots * nblk) ||
         !mg_ensure(c, c->d_scoef, esz * (size_t)c->nslots))
         return MG_ERR_ALLOC;
     const double twopi = 6.283185307179586;
@@ -409,10 +470,10 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     A.kz = KZ;
     A.rows = (const int4 *)c->d_rows.p;
     A.row_slot = (const int *)c->d_row_slot.p;
-    A.tasks = (const int2 *)c->d_tasks.p;
+    A.tasks = (const int4 *)c->d_tasks.p;
     A.tab = c->d_phase.p;
     A.q = (const double *)c->d_site_q.p;
-    A.spart = (double *)c->d_spart.p;
+    A.spart = c->d_spart.p;
     A.scoef = c->d_scoef.p;
     A.twopi[0] = p.twopi_lx;
     A.twopi[1] = p.twopi_ly;
@@ -435,8 +496,8 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     MG_CUDA(cudaGetLastError());
     if (c->timing) cudaEventRecord(c->ev[4], s);
     const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
-    int maxslots = 0;
-    for (int r = 0; r < c->nrows; r++) maxslots = std::max(maxslots, 2 * (c->h_rows[4 * r + 2] + 1));
+    int maxa = 1;
+    for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
     unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
     A.row0 = mg_reserve_rows(c, rblocks);
     if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
@@ -444,13 +505,14 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
         k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
     else
         k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
-    size_t fsmem = esz * (size_t)EW_FROWS * maxslots;
+    size_t fsmem = 2 * esz * (size_t)EW_FROWS * maxa;
+    unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
     if (fp64) {
         MG_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-        k_kforce<double><<<(n + 255) / 256, 256, fsmem, s>>>(A, maxslots);
+        k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
     } else {
         MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-        k_kforce<float><<<(n + 255) / 256, 256, fsmem, s>>>(A, maxslots);
+        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
     }
     MG_CUDA(cudaGetLastError());
     c->launches += 4;

@@ -13,15 +13,17 @@
 // float2 LJ pair and one int per lane) are staged in shared memory per step with
 // coalesced loads. The list is a full list (each pair seen from both clusters), so no
 // j-force scatter or atomic is needed: a lane accumulates only its own i-site force in
-// FP32 over at most 32 j-clusters, flushes into FP64 registers, and the four lanes of an
-// i-site are combined with warp shuffles at the end. Energies are halved for the
-// double counting. Every reduction has a fixed order, so results are bit-reproducible.
+// FP32 over at most 64 j-clusters, flushes into FP64 registers, and the four lanes of an
+// i-site are combined in FP64 with warp shuffles at the end. A lane's energy sums stay
+// in FP32 over its list and are reduced across lanes and blocks in FP64; they are halved
+// for the double counting. Every reduction has a fixed order, so results are
+// bit-reproducible.
 #include <math.h>
 
 #include "mg_internal.cuh"
 
 #define PAIR_WPB 4       // warps (i-clusters) per block
-#define PAIR_FLUSH 8     // list steps (4 j-clusters each) between FP64 flushes
+#define PAIR_FLUSH 16    // list steps (4 j-clusters each) between FP64 force flushes
 
 namespace {
 
@@ -178,15 +180,13 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                     }
                 }
             }
-            if (++steps == PAIR_FLUSH) {
+            if (++steps == PAIR_FLUSH) {  // per-lane energies stay in R until the end
                 steps = 0;
                 fL[0] += ax; fL[1] += ay; fL[2] += az;
-                eng[0] += e_vdw; eng[1] += e_sh; eng[2] += e_re; eng[3] += e_vir;
-                ax = ay = az = 0; e_vdw = e_sh = e_re = e_vir = 0;
+                ax = ay = az = 0;
                 if (SPLIT) {
                     fS[0] += bx; fS[1] += by; fS[2] += bz;
-                    eng[4] += s_vdw; eng[5] += s_sh; eng[6] += s_re; eng[7] += s_vir;
-                    bx = by = bz = 0; s_vdw = s_sh = s_re = s_vir = 0;
+                    bx = by = bz = 0;
                 }
             }
         }
