@@ -187,3 +187,29 @@ def butane_box(nside: int, box, seed: int, rc: float = 14.0, charged: bool = Fal
     return System(species=[sp], box=box, x=xyz[:, 0].copy(), y=xyz[:, 1].copy(), z=xyz[:, 2].copy(),
                   rcuton=rc, rcutoff=rc, rcutoffelec=rc, f0=0.5, name=name, delt_fs=2.0,
                   charge_type=ELEC_NONE)
+
+
+def ion_species(name: str, nmole: int, charge: float, epsilon: float = 0.0, sigma: float = 1.0) -> Species:
+    """A single-site charged species (one ion per molecule)."""
+    return Species(name=name, nmole=nmole, atom_names=[name], atom_type=np.array([0], np.int32),
+                   ghost=np.array([GHOST_NONE], np.int32), interp=np.array([1], np.int32),
+                   epsilon=np.array([epsilon]), sigma=np.array([sigma]), charge=np.array([charge]),
+                   aw=np.array([1.0]), aw_input=np.array([AVOGADRO * 1.0e-27]), template_xyz=np.zeros((1, 3)))
+
+
+def ion_box(nside: int, seed: int, kmax: int, ksqmax: int, rc: float = 1.5, spacing: float = 3.0,
+            jitter: float = 0.4, kappa: float = 0.3) -> System:
+    """nside^3 monovalent ions (half +1, half -1) on a jittered cubic lattice with Ewald
+    electrostatics: one site per molecule, so the cluster count equals the site count,
+    well above the list builder's first capacity estimate."""
+    rng = np.random.default_rng(seed)
+    g = np.arange(nside)
+    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
+    pts = (np.stack([cx.ravel(), cy.ravel(), cz.ravel()], 1) + 0.5) * spacing
+    pts = pts[rng.permutation(len(pts))] + rng.uniform(-jitter, jitter, size=pts.shape)
+    n = len(pts)
+    species = [ion_species("Na", n // 2, 1.0), ion_species("Cl", n - n // 2, -1.0)]
+    box = nside * spacing
+    return System(species=species, box=np.array([box, box, box]), x=pts[:, 0].copy(), y=pts[:, 1].copy(),
+                  z=pts[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc, charge_type=ELEC_EWALD,
+                  kappa=kappa, kmax=(kmax, kmax, kmax), ksqmax=ksqmax, name=f"ions{n}")

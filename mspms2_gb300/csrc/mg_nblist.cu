@@ -27,13 +27,15 @@
 
 #include "mg_internal.cuh"
 
-// d_meta layout (int units): [0] ncl, [1] max column count, [2] need-rebuild flag,
-// [3] builds since creation, [4..5] (64-bit) entries written
+// d_meta layout (int units): [0] ncl (0 when the clusters overflowed their buffers),
+// [1] max column count, [2] need-rebuild flag, [3] builds since creation, [4..5] (64-bit)
+// entries written, [6] clusters the build asked for
 #define META_NCL 0
 #define META_MAXCOL 1
 #define META_NEED 2
 #define META_BUILDS 3
 #define META_NPAIRS 4
+#define META_NCL_TOTAL 6
 
 namespace {
 
@@ -76,8 +78,13 @@ __global__ void k_zero(int *__restrict__ p, int count, const int *__restrict__ m
 
 // single-block exclusive scan of `count` into `start` (start[nc] = total); also resets
 // `fill`; with max_out != null stores the largest count
+// Exclusive scan of count[0..nc) into start (start[nc] = total). *total_out gets the total,
+// or 0 when it exceeds cap (cap >= 0): a cluster count above the buffers' capacity leaves
+// the build empty, so no later kernel of the call reads a cluster that was not written,
+// and the call is repeated with larger buffers sized from *total_raw.
 __global__ void k_scan(int nc, const int *__restrict__ count, int *__restrict__ start, int *__restrict__ fill,
-                       int *__restrict__ total_out, int *__restrict__ max_out, const int *__restrict__ meta) {
+                       int *__restrict__ total_out, int *__restrict__ max_out, int cap, int *__restrict__ total_raw,
+                       const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
     __shared__ int s_sum[1024], s_max[1024];
     int t = threadIdx.x, nt = blockDim.x;
@@ -100,7 +107,8 @@ __global__ void k_scan(int nc, const int *__restrict__ count, int *__restrict__ 
             m = max(m, s_max[i]);
         }
         start[nc] = a;
-        if (total_out) *total_out = a;
+        if (total_out) *total_out = (cap >= 0 && a > cap) ? 0 : a;
+        if (total_raw) *total_raw = a;
         if (max_out) *max_out = m;
     }
     __syncthreads();
@@ -371,7 +379,11 @@ __global__ void k_search(SearchArgs A) {
     const int cy1 = (int)floor(__ddiv_rn(__dadd_rn(bi[4], A.rlist), A.cwy));
     const int nx = cx1 - cx0 + 1, ny = cy1 - cy0 + 1;
     if (nx > A.ncx || ny > A.ncy) {  // a column would be visited twice: small-box mode
-        if (lane == 0) atomicOr(A.flags, MG_FLAG_SMALL_BOX);
+        if (lane == 0) {
+            atomicOr(A.flags, MG_FLAG_SMALL_BOX);
+            A.pair_start[I] = 0;  // the pair kernel of this (repeated) call sees no entries
+            A.pair_cnt[I] = 0;
+        }
         return;
     }
     const int ncand = nx * ny;
@@ -576,13 +588,13 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
                                            (double *)c->d_xbuild.p, (double *)c->d_img.p, col_of,
                                            (int *)c->d_col_count.p, meta);
     k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_count.p, (int *)c->d_col_start.p, (int *)c->d_col_fill.p, nullptr,
-                              meta + META_MAXCOL, meta);
+                              meta + META_MAXCOL, -1, nullptr, meta);
     k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, col_of, (int *)c->d_col_start.p, (int *)c->d_col_fill.p,
                                               (int *)c->d_col_sorted.p, meta);
     k_sort_columns<<<ncol, 256, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, (double *)c->d_xbuild.p,
                                        c->zcap, (int *)c->d_col_ncl.p, (unsigned *)c->d_flags.p, meta);
     k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, nullptr, meta + META_NCL, nullptr,
-                              meta);
+                              c->cl_cap, meta + META_NCL_TOTAL, meta);
     k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p,
                                          (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p, c->zcap, c->cl_cap,
                                          (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, (double *)c->d_cl_bb.p,
@@ -676,10 +688,16 @@ bool mg_list_retry(mg_ctx *c, unsigned flags, const int *meta_host) {
     }
     if (flags & MG_FLAG_LIST_OVERFLOW) {
         long long need = *(const long long *)(meta_host + META_NPAIRS);
-        int ncl = meta_host[META_NCL];
-        if (ncl > c->cl_cap) c->cl_cap = ncl + ncl / 8 + 16;
-        if (need > c->pair_cap) c->pair_cap = need + need / 4 + 1024;
-        else c->pair_cap = c->pair_cap * 2;
+        int ncl = meta_host[META_NCL_TOTAL];
+        if (ncl > c->cl_cap) {  // the clusters overflowed and the search did not run
+            int grown = ncl + ncl / 8 + 16;
+            c->pair_cap = (long long)((double)c->pair_cap * grown / c->cl_cap) + 1024;
+            c->cl_cap = grown;
+        } else if (need > c->pair_cap) {
+            c->pair_cap = need + need / 4 + 1024;
+        } else {
+            c->pair_cap = c->pair_cap * 2;
+        }
         retry = true;
     }
     if (retry) c->list_valid = false;
