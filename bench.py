@@ -38,7 +38,7 @@ import numpy as np  # noqa: E402
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 SM_COUNT_NOMINAL = 152
 FP32_LANES_PER_SM = 128
-# algorithmic work per unit (work model)
+# algorithmic work per unit (fixed constants of the work model; FP32 FLOP)
 FLOP_PAIR = 55.0        # LJ + Ewald-real pair, counted once
 FLOP_K_S = 10.0         # per (half-space k-vector, site) in the S(k) pass
 FLOP_K_F = 12.0         # per (half-space k-vector, site) in the force pass
