@@ -253,6 +253,38 @@ MG_API mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);
 MG_API mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *grid, double *zcap,
                             int *cluster_atoms, int *pairs, int *shifts);
 
+/* ---- reciprocal space without device allocation ---------------------------- */
+/* No counterpart in the reference: an extra entry point of this library.
+ *
+ * Ewald reciprocal-space energy and forces (the k-space part of src/frclong.c:988-1048,
+ * computed by the same kernels as mg_compute) for callers that may not allocate device
+ * memory: code that runs inside a pre-sized memory pool or a latency-bounded loop, where
+ * a cudaMalloc would either fail or stall every stream of the device. The call allocates
+ * no memory, on the device or the host: its scratch is one fixed array of
+ * MG_EWALD_STATIC_SCRATCH_BYTES per device inside this library's device code, which
+ * exists from the moment that code is loaded on the device.
+ *
+ * Device pointers: d_x, d_y, d_z, d_q [natom] positions and charges; d_f [3*natom] the
+ * forces (x block, then y, then z), overwritten; d_energy one double, overwritten with
+ * the reciprocal energy (mg_energies.ufourier), or NULL. Of p the fields kmax, ksqmax,
+ * coulomb_prefactor, bfactor_ewald, vfactor_ewald and twopi_l{x,y,z} are read.
+ * precision: MG_PREC_*. stream: a cudaStream_t as void*, NULL = the default stream; the
+ * call is asynchronous on it. err: optional buffer of err_len bytes for a one-line
+ * message when the call fails.
+ *
+ * The first call for a device does the set-up: it looks up the scratch address with that
+ * device current (which may load the device code there); make it before any stream
+ * capture. Every call selects `device` for its duration and restores the caller's. A call
+ * whose scratch would exceed the limit returns MG_ERR_CAPACITY and launches nothing.
+ * Nothing in the scratch needs to start at zero. Calls on one device share the scratch:
+ * two calls that are not ordered on the device (issued from different threads, or on
+ * streams not ordered by events) race on it and give wrong results. */
+#define MG_EWALD_STATIC_SCRATCH_BYTES (32u << 20)
+MG_API mg_status mg_ewald_recip_static(int device, void *stream, int precision, int natom,
+                                       const double *d_x, const double *d_y, const double *d_z,
+                                       const double *d_q, const mg_params *p, double *d_f,
+                                       double *d_energy, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,8 +25,11 @@
 // power recurrence). Four thread groups share the rows of a site; their partial forces
 // are combined in shared memory in a fixed order.
 #include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "mg_internal.cuh"
 
@@ -517,4 +520,299 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     MG_CUDA(cudaGetLastError());
     c->launches += 4;
     return MG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// mg_ewald_recip_static: the same reciprocal-space pass with no device allocation
+// ---------------------------------------------------------------------------------
+// Every piece of scratch (k-vector row and task tables, phase tables, S(k) partials and
+// coefficients, energy rows) is carved out of g_ew_scratch. Its device address is looked
+// up once per device, with that device current, and handed to the kernels as a plain
+// pointer. Each byte a kernel reads was written before in the same call, or (the row and
+// task tables) by an earlier call on the device with the same KMAX/KSQMAX, so nothing
+// has to start at zero. Calls on one device share the array; calls that are not ordered
+// on the device race on it.
+namespace {
+
+static __device__ __align__(256) unsigned char g_ew_scratch[MG_EWALD_STATIC_SCRATCH_BYTES];
+
+constexpr int EW_STATIC_MAX_DEVICES = 64;
+
+struct EwStaticDevice {
+    unsigned char *base = nullptr;  // device address of g_ew_scratch on this device
+    int key[4] = {-1, -1, -1, -1};  // KMAXX, KMAXY, KMAXZ, KSQMAX of the tables now in scratch
+};
+EwStaticDevice g_ew_static[EW_STATIC_MAX_DEVICES];
+std::mutex g_ew_static_mutex;
+
+// largest |kz| of row (kx, ky): min(KZ, floor(sqrt(rem))), rem = KSQMAX - kx^2 - ky^2 >= 0
+__host__ __device__ inline int ew_kzmax(int KZ, int rem) {
+    int k = 0;
+    while (k + 1 <= KZ && (k + 1) * (k + 1) <= rem) k++;
+    return k;
+}
+
+// Visits the half-space rows in the order of mg_ewald_setup: f(kx, ky, kzmax, half).
+template <typename F>
+__host__ __device__ inline void ew_for_rows(int KX, int KY, int KZ, int KS, F f) {
+    for (int kx = 0; kx <= KX; kx++)
+        for (int ky = -KY; ky <= KY; ky++) {
+            if (kx == 0 && ky < 0) continue;
+            int rem = KS - kx * kx - ky * ky;
+            if (rem < 0) continue;
+            int kzmax = ew_kzmax(KZ, rem);
+            int half = (kx == 0 && ky == 0) ? 1 : 0;
+            if (half && kzmax < 1) continue;
+            f(kx, ky, kzmax, half);
+        }
+}
+
+// length of chunk h of a row with nv |kz| values (balanced chunks of at most EW_CH)
+__host__ __device__ inline int ew_chunk_len(int nv, int h) {
+    int nch = (nv + EW_CH - 1) / EW_CH;
+    return nv / nch + (h < nv % nch ? 1 : 0);
+}
+
+struct EwCounts {
+    int nrows = 0, nslots = 0, ntasks = 0, maxa = 1;
+};
+
+EwCounts ew_count(int KX, int KY, int KZ, int KS) {
+    EwCounts c;
+    int by_len[EW_CH + 1] = {0};
+    ew_for_rows(KX, KY, KZ, KS, [&](int, int, int kzmax, int) {
+        int nv = kzmax + 1;
+        c.nrows++;
+        c.nslots += 2 * nv;
+        c.maxa = std::max(c.maxa, nv);
+        int nch = (nv + EW_CH - 1) / EW_CH;
+        for (int h = 0; h < nch; h++) by_len[ew_chunk_len(nv, h)]++;
+    });
+    for (int L = 1; L <= EW_CH; L++) c.ntasks += (by_len[L] + 31) / 32 * 32;
+    return c;
+}
+
+// Row table, packed slot table (first slot of each row, then the row of each slot) and
+// the task list sorted by length (longest first, rows ascending) with each length group
+// padded to whole warps: the same tables mg_ewald_setup builds on the host.
+__global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int4 *__restrict__ rows,
+                            int *__restrict__ row_slot, int4 *__restrict__ tasks) {
+    if (threadIdx.x == 0) {
+        int r = 0, slot = 0;
+        ew_for_rows(KX, KY, KZ, KS, [&](int kx, int ky, int kzmax, int half) {
+            rows[r] = make_int4(kx, ky, kzmax, half);
+            row_slot[r] = slot;
+            slot += 2 * (kzmax + 1);
+            r++;
+        });
+        int t = 0;
+        for (int L = EW_CH; L >= 1; L--) {
+            for (int q = 0; q < nrows; q++) {
+                int nv = rows[q].z + 1, nch = (nv + EW_CH - 1) / EW_CH;
+                for (int h = 0, k0 = 0; h < nch; h++) {
+                    int len = ew_chunk_len(nv, h);
+                    if (len == L) tasks[t++] = make_int4(q, k0, len, 0);
+                    k0 += len;
+                }
+            }
+            while (t % 32) tasks[t++] = make_int4(0, 0, 0, 0);
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nrows; q += blockDim.x) {
+        int s0 = row_slot[q], ns = 2 * (rows[q].z + 1);
+        for (int s = 0; s < ns; s++) row_slot[nrows + s0 + s] = q;
+    }
+}
+
+// fixed-order sum of the reciprocal energy over the S(k) reduction's block rows
+__global__ void k_ew_energy(const double *__restrict__ erows, int nrows, double *__restrict__ out) {
+    __shared__ double s[256];
+    double t = 0.0;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) t += erows[(size_t)r * E_NCOMP + E_UFOURIER];
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = s[0];
+}
+
+mg_status ew_static_fail(char *err, size_t err_len, mg_status code, const char *fmt, ...) {
+    if (err && err_len) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(err, err_len, fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+// selects a device for the duration of a call and restores the caller's on exit
+struct EwDeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    cudaError_t select(int dev) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return e;
+        if (prev == dev) return cudaSuccess;
+        e = cudaSetDevice(dev);
+        changed = e == cudaSuccess;
+        return e;
+    }
+    ~EwDeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+inline size_t ew_align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precision, int natom,
+                                           const double *d_x, const double *d_y, const double *d_z,
+                                           const double *d_q, const mg_params *p, double *d_f,
+                                           double *d_energy, char *err, size_t err_len) {
+#define EWS_CUDA(call, what)                                                                            \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            cudaGetLastError();                                                                         \
+            return ew_static_fail(err, err_len, MG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e_)); \
+        }                                                                                               \
+    } while (0)
+    if (err && err_len) err[0] = 0;
+    if (!p || natom < 0 || (precision != MG_PREC_MIXED && precision != MG_PREC_FP64))
+        return ew_static_fail(err, err_len, MG_ERR_INVALID, "invalid arguments (params, natom or precision)");
+    if (natom > 0 && (!d_x || !d_y || !d_z || !d_q || !d_f))
+        return ew_static_fail(err, err_len, MG_ERR_INVALID, "null device pointer");
+    const int KX = p->kmax[0], KY = p->kmax[1], KZ0 = p->kmax[2], KS = p->ksqmax;
+    if (KX < 0 || KY < 0 || KZ0 < 0 || KX > 255 || KY > 255 || KZ0 > 255 || KS < 0)
+        return ew_static_fail(err, err_len, MG_ERR_INVALID, "kmax must lie in [0, 255] and ksqmax be >= 0");
+    if (device < 0 || device >= EW_STATIC_MAX_DEVICES)
+        return ew_static_fail(err, err_len, MG_ERR_NO_DEVICE, "device %d out of range", device);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device >= ndev) {
+        cudaGetLastError();
+        return ew_static_fail(err, err_len, MG_ERR_NO_DEVICE, "no CUDA device %d", device);
+    }
+    EwDeviceGuard guard;
+    EWS_CUDA(guard.select(device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lock(g_ew_static_mutex);
+    EwStaticDevice &dev = g_ew_static[device];
+    if (!dev.base) {  // set-up, once per device, with the device current
+        int major = 0, minor = 0;
+        EWS_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device), "cudaDeviceGetAttribute");
+        EWS_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device), "cudaDeviceGetAttribute");
+        if (major != 10 || minor != 3)
+            return ew_static_fail(err, err_len, MG_ERR_NO_DEVICE, "device %d is sm_%d%d; the kernels are built for sm_103a",
+                                  device, major, minor);
+        void *ptr = nullptr;
+        EWS_CUDA(cudaGetSymbolAddress(&ptr, g_ew_scratch), "cudaGetSymbolAddress");
+        dev.base = (unsigned char *)ptr;
+    }
+    const bool fp64 = precision == MG_PREC_FP64;
+    const int n = natom;
+    const EwCounts ct = ew_count(KX, KY, KZ0, KS);
+    if (n == 0 || ct.nrows == 0) {  // nothing to sum: zero forces and energy
+        if (n > 0) EWS_CUDA(cudaMemsetAsync(d_f, 0, sizeof(double) * 3 * (size_t)n, s), "cudaMemsetAsync");
+        if (d_energy) EWS_CUDA(cudaMemsetAsync(d_energy, 0, sizeof(double), s), "cudaMemsetAsync");
+        return MG_OK;
+    }
+    // scratch layout: tables first (their offsets depend on KMAX/KSQMAX only), then the
+    // per-call arrays
+    const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
+    const int KZ = std::max(KZ0, 1);
+    const int nblk = (n + EW_SITES - 1) / EW_SITES;
+    const unsigned rblocks = (unsigned)((ct.nslots + 255) / 256);
+    size_t off = 0;
+    const size_t o_rows = off;
+    off += ew_align256(sizeof(int4) * (size_t)ct.nrows);
+    const size_t o_slot = off;
+    off += ew_align256(sizeof(int) * ((size_t)ct.nrows + ct.nslots));
+    const size_t o_tasks = off;
+    off += ew_align256(sizeof(int4) * (size_t)ct.ntasks);
+    const size_t o_tab = off;
+    off += ew_align256(esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * n);
+    const size_t o_spart = off;
+    off += ew_align256((esz / 2) * 2 * (size_t)ct.nslots * nblk);
+    const size_t o_coef = off;
+    off += ew_align256(esz * (size_t)ct.nslots);
+    const size_t o_erows = off;
+    off += ew_align256(sizeof(double) * E_NCOMP * (size_t)rblocks);
+    if (off > (size_t)MG_EWALD_STATIC_SCRATCH_BYTES)
+        return ew_static_fail(err, err_len, MG_ERR_CAPACITY,
+                              "%d sites with kmax (%d,%d,%d), ksqmax %d need %zu bytes of scratch; the limit is %u",
+                              n, KX, KY, KZ0, KS, off, (unsigned)MG_EWALD_STATIC_SCRATCH_BYTES);
+    unsigned char *base = dev.base;
+    int4 *rows = (int4 *)(base + o_rows);
+    int *row_slot = (int *)(base + o_slot);
+    int4 *tasks = (int4 *)(base + o_tasks);
+    const int key[4] = {KX, KY, KZ0, KS};
+    if (!std::equal(key, key + 4, dev.key)) {
+        k_ew_tables<<<1, 256, 0, s>>>(KX, KY, KZ0, KS, ct.nrows, rows, row_slot, tasks);
+        EWS_CUDA(cudaGetLastError(), "k_ew_tables launch");
+        std::copy(key, key + 4, dev.key);
+    }
+    EWS_CUDA(cudaMemsetAsync(d_f, 0, sizeof(double) * 3 * (size_t)n, s), "cudaMemsetAsync");
+    const double twopi = 6.283185307179586;
+    const double sc[3] = {p->twopi_lx / twopi, p->twopi_ly / twopi, p->twopi_lz / twopi};
+    void *tab = base + o_tab;
+    if (fp64)
+        k_phase_d<<<(n + 127) / 128, 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (double2 *)tab);
+    else
+        k_phase_f<<<(n + 127) / 128, 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)tab);
+    EwArgs A;
+    A.n = n;
+    A.nrows = ct.nrows;
+    A.nslots = ct.nslots;
+    A.ntasks = ct.ntasks;
+    A.kx = KX;
+    A.ky = KY;
+    A.kz = KZ;
+    A.rows = rows;
+    A.row_slot = row_slot;
+    A.tasks = tasks;
+    A.tab = tab;
+    A.q = d_q;
+    A.spart = base + o_spart;
+    A.scoef = base + o_coef;
+    A.twopi[0] = p->twopi_lx;
+    A.twopi[1] = p->twopi_ly;
+    A.twopi[2] = p->twopi_lz;
+    A.bfac = p->bfactor_ewald;
+    A.vfac = p->vfactor_ewald;
+    A.coul = p->coulomb_prefactor;
+    A.rows_e = (double *)(base + o_erows);
+    A.row0 = 0;
+    A.f = d_f;
+    const int P = EW_TILE + 1;
+    const size_t smem = esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
+    const dim3 grid((ct.ntasks + EW_TPB - 1) / EW_TPB, nblk);
+    const int *slot_row = row_slot + ct.nrows;
+    const size_t fsmem = 2 * esz * (size_t)EW_FROWS * ct.maxa;
+    const unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
+    if (fp64) {
+        EWS_CUDA(cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "cudaFuncSetAttribute");
+        k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
+        k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+        EWS_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem),
+                 "cudaFuncSetAttribute");
+        k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, ct.maxa);
+    } else {
+        EWS_CUDA(cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "cudaFuncSetAttribute");
+        k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
+        k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+        EWS_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem),
+                 "cudaFuncSetAttribute");
+        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, ct.maxa);
+    }
+    if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, d_energy);
+    EWS_CUDA(cudaGetLastError(), "kernel launch");
+    return MG_OK;
+#undef EWS_CUDA
 }
