@@ -369,13 +369,15 @@ def run_ours(args, rank, world, local_rank):
     t_ms, flops = stages[dom]
     peak = SM_COUNT_NOMINAL * FP32_LANES_PER_SM * 2 * 2.07e9 / 1e12
     achieved = flops / (t_ms * 1e-3) / 1e12 if t_ms > 0 else 0.0
+    # DRAM bytes per launch of that kernel from the committed ncu summary of this workload
     traffic = None
-    tf = os.path.join(ROOT, "profiles", f"traffic_{dom}_{args.workload}.json")
+    kernel_of = {"pair": "k_pair", "kspace_sk": "k_sk", "kspace_force": "k_kforce"}
+    tf = os.path.join(ROOT, "profiles", f"kernels_{args.workload}.md")
     if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get("dram_bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+        for ln in open(tf):
+            parts = ln.split()
+            if len(parts) == 4 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel_of[dom]:
+                traffic = float(parts[3])
     if rank != 0:
         return 0
     line = {"metric": "pair_interactions_per_s", "value": value, "unit": "pair-interactions/s", "n_gpus": world,

@@ -178,7 +178,7 @@ typedef struct mg_stats {
     int list_builds;                /* total builds since creation */
     double kernel_ms[8];            /* per-stage device times of the last call, if timing is on:
                                        0 list build + packing, 1 pair kernel, 2 intra+bonded,
-                                       3 k-space phases + S(k), 4 S(k) reduction + k-space force,
+                                       3 k-space phases + S(k) + its reduction, 4 k-space force,
                                        5 solid-fluid, 6 reductions and checks, 7 total */
     int kernel_launches;            /* kernels this library launched in the last call */
 } mg_stats;

@@ -30,10 +30,11 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "mg_internal.cuh"
 
-#define EW_TILE 64      // sites per shared-memory tile in the S(k) pass
+#define EW_TILE 32      // sites per shared-memory tile in the S(k) pass
 #define EW_CH 8         // |kz| values per thread in the S(k) pass (at most)
 #define EW_TPB 128      // threads per block in the S(k) pass
 #define EW_SITES 512    // sites per block in the S(k) pass (summed in R)
@@ -71,6 +72,33 @@ __device__ __forceinline__ T cfma(T x, T z, T c) {
     r.x = fma(x.x, z.x, fma(-x.y, z.y, c.x));
     r.y = fma(x.x, z.y, fma(x.y, z.x, c.y));
     return r;
+}
+
+// Two FP32 lanes in one 64-bit register for the packed f32x2 arithmetic of sm_100 and
+// later (one instruction, two independent IEEE round-to-nearest results).
+typedef unsigned long long f32x2;
+
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+
+__device__ __forceinline__ void up2(f32x2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+// a*b + c per lane
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
 }
 
 // phase tables tab[d][n][site] = e^{2 pi i n u_d}
@@ -140,29 +168,117 @@ struct EwArgs {
     double *f;
 };
 
+// FP32 tile with packed f32x2 arithmetic: lanes are two consecutive |kz| (j, j+1). Their
+// phases start from the table (Z^kz0, Z^(kz0+1)) and advance by W = Z^2, also from the
+// table; per lane pair and site, 8 packed FMAs accumulate S(+kz) and S(-kz) of both
+// |kz| and 4 advance the phases. An odd last |kz| is done in scalar FMAs.
+template <int CH>
+__device__ __forceinline__ void sk_tile_f32x2(const float2 *sX, const float2 *sY, const float2 *sZ, const float *sQ,
+                                              int P, int tn, int kx, int aky, float ysign, int kz0,
+                                              float (&pP)[EW_CH][2], float (&pM)[EW_CH][2]) {
+    constexpr int NP = CH / 2;
+    constexpr bool ODD = (CH & 1) != 0;
+    f32x2 Pr[NP > 0 ? NP : 1], Pi[NP > 0 ? NP : 1], Mr[NP > 0 ? NP : 1], Mi[NP > 0 ? NP : 1];
+#pragma unroll
+    for (int h = 0; h < NP; h++) {
+        Pr[h] = pk2(pP[2 * h][0], pP[2 * h + 1][0]);
+        Pi[h] = pk2(pP[2 * h][1], pP[2 * h + 1][1]);
+        Mr[h] = pk2(pM[2 * h][0], pM[2 * h + 1][0]);
+        Mi[h] = pk2(pM[2 * h][1], pM[2 * h + 1][1]);
+    }
+    float tPr = ODD ? pP[CH - 1][0] : 0.f, tPi = ODD ? pP[CH - 1][1] : 0.f;
+    float tMr = ODD ? pM[CH - 1][0] : 0.f, tMi = ODD ? pM[CH - 1][1] : 0.f;
+    for (int s = 0; s < tn; s++) {
+        float2 X = sX[kx * P + s];
+        float2 Y = sY[aky * P + s];
+        Y.y *= ysign;
+        const float q = sQ[s];
+        float2 Aq = cmul(X, Y);
+        Aq.x *= q;
+        Aq.y *= q;
+        const float2 Z0 = sZ[kz0 * P + s];
+        float ztx = Z0.x, zty = Z0.y;  // phase of the odd last |kz|
+        if (NP > 0) {
+            const f32x2 AX = pk2(Aq.x, Aq.x), AY = pk2(Aq.y, Aq.y);
+            const f32x2 NAX = pk2(-Aq.x, -Aq.x), NAY = pk2(-Aq.y, -Aq.y);
+            const float2 Z1 = sZ[(kz0 + 1) * P + s];
+            f32x2 Zx = pk2(Z0.x, Z1.x), Zy = pk2(Z0.y, Z1.y);
+            f32x2 WX = 0, WY = 0, NWY = 0;
+            if (CH >= 3) {
+                const float2 W = sZ[2 * P + s];
+                WX = pk2(W.x, W.x);
+                WY = pk2(W.y, W.y);
+                NWY = pk2(-W.y, -W.y);
+            }
+#pragma unroll
+            for (int h = 0; h < NP; h++) {
+                Pr[h] = fma2(AX, Zx, fma2(NAY, Zy, Pr[h]));  // + Ax Zx - Ay Zy
+                Pi[h] = fma2(AX, Zy, fma2(AY, Zx, Pi[h]));   // + Ax Zy + Ay Zx
+                Mr[h] = fma2(AX, Zx, fma2(AY, Zy, Mr[h]));   // + Ax Zx + Ay Zy
+                Mi[h] = fma2(AY, Zx, fma2(NAX, Zy, Mi[h]));  // + Ay Zx - Ax Zy
+                if (h + 1 < NP || ODD) {                     // Z <- Z W
+                    const f32x2 nZx = fma2(Zx, WX, mul2(Zy, NWY));
+                    const f32x2 nZy = fma2(Zx, WY, mul2(Zy, WX));
+                    Zx = nZx;
+                    Zy = nZy;
+                }
+            }
+            if (ODD) {
+                float hi;
+                up2(Zx, ztx, hi);
+                up2(Zy, zty, hi);
+            }
+        }
+        if (ODD) {
+            tPr = fmaf(Aq.x, ztx, fmaf(-Aq.y, zty, tPr));
+            tPi = fmaf(Aq.x, zty, fmaf(Aq.y, ztx, tPi));
+            tMr = fmaf(Aq.x, ztx, fmaf(Aq.y, zty, tMr));
+            tMi = fmaf(Aq.y, ztx, fmaf(-Aq.x, zty, tMi));
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < NP; h++) {
+        up2(Pr[h], pP[2 * h][0], pP[2 * h + 1][0]);
+        up2(Pi[h], pP[2 * h][1], pP[2 * h + 1][1]);
+        up2(Mr[h], pM[2 * h][0], pM[2 * h + 1][0]);
+        up2(Mi[h], pM[2 * h][1], pM[2 * h + 1][1]);
+    }
+    if (ODD) {
+        pP[CH - 1][0] = tPr;
+        pP[CH - 1][1] = tPi;
+        pM[CH - 1][0] = tMr;
+        pM[CH - 1][1] = tMi;
+    }
+}
+
 // One tile of sites for a thread owning CH consecutive |kz| of one row: straight-line
-// code, A*Z and A*conj(Z) sharing four products, Z advanced by the site's Z1.
+// code, A*Z and A*conj(Z) sharing four products, Z advanced by the site's Z1. FP32 goes
+// to the packed form above.
 template <typename R, int CH, typename T2>
 __device__ __forceinline__ void sk_tile(const T2 *sX, const T2 *sY, const T2 *sZ, const R *sQ, int P, int tn,
                                         int kx, int aky, R ysign, int kz0, R (&pP)[EW_CH][2], R (&pM)[EW_CH][2]) {
-    for (int s = 0; s < tn; s++) {
-        T2 X = sX[kx * P + s];
-        T2 Y = sY[aky * P + s];
-        Y.y *= ysign;
-        const R q = sQ[s];
-        T2 Aq = cmul(X, Y);
-        Aq.x *= q;
-        Aq.y *= q;
-        T2 Z = sZ[kz0 * P + s];
-        const T2 Z1 = sZ[1 * P + s];
+    if constexpr (std::is_same<R, float>::value) {
+        sk_tile_f32x2<CH>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM);
+    } else {
+        for (int s = 0; s < tn; s++) {
+            T2 X = sX[kx * P + s];
+            T2 Y = sY[aky * P + s];
+            Y.y *= ysign;
+            const R q = sQ[s];
+            T2 Aq = cmul(X, Y);
+            Aq.x *= q;
+            Aq.y *= q;
+            T2 Z = sZ[kz0 * P + s];
+            const T2 Z1 = sZ[1 * P + s];
 #pragma unroll
-        for (int j = 0; j < CH; j++) {
-            const R p1 = Aq.x * Z.x, p2 = Aq.y * Z.y, p3 = Aq.x * Z.y, p4 = Aq.y * Z.x;
-            pP[j][0] += p1 - p2;
-            pP[j][1] += p3 + p4;
-            pM[j][0] += p1 + p2;
-            pM[j][1] += p4 - p3;
-            if (j + 1 < CH) Z = cmul(Z, Z1);
+            for (int j = 0; j < CH; j++) {
+                const R p1 = Aq.x * Z.x, p2 = Aq.y * Z.y, p3 = Aq.x * Z.y, p4 = Aq.y * Z.x;
+                pP[j][0] += p1 - p2;
+                pP[j][1] += p3 + p4;
+                pM[j][0] += p1 + p2;
+                pM[j][1] += p4 - p3;
+                if (j + 1 < CH) Z = cmul(Z, Z1);
+            }
         }
     }
 }
@@ -497,10 +613,7 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
         k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
     }
     MG_CUDA(cudaGetLastError());
-    if (c->timing) cudaEventRecord(c->ev[4], s);
     const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
-    int maxa = 1;
-    for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
     unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
     A.row0 = mg_reserve_rows(c, rblocks);
     if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
@@ -508,6 +621,9 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
         k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
     else
         k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+    if (c->timing) cudaEventRecord(c->ev[4], s);
+    int maxa = 1;
+    for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
     size_t fsmem = 2 * esz * (size_t)EW_FROWS * maxa;
     unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
     if (fp64) {

@@ -600,7 +600,7 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
     if (want_short && (st = mg_launch_bonded(c, dx, dy, dz, fs))) return st;
     if (c->timing) cudaEventRecord(c->ev[3], s);
     if (want_long && p.charge_type == MG_ELEC_EWALD) {
-        if ((st = mg_launch_ewald(c, dx, dy, dz, fl))) return st;  // records ev[4] after S(k)
+        if ((st = mg_launch_ewald(c, dx, dy, dz, fl))) return st;  // records ev[4] after the S(k) reduction
         if (p.ewald_bc == MG_EWALD_BC_VACUUM && (st = mg_launch_vacuum(c, dx, dy, dz, fl))) return st;
     } else if (c->timing) {
         cudaEventRecord(c->ev[4], s);

@@ -76,9 +76,8 @@ __global__ void k_zero(int *__restrict__ p, int count, const int *__restrict__ m
     if (i < count) p[i] = 0;
 }
 
-// single-block exclusive scan of `count` into `start` (start[nc] = total); also resets
-// `fill`; with max_out != null stores the largest count
-// Exclusive scan of count[0..nc) into start (start[nc] = total). *total_out gets the total,
+// Single-block exclusive scan of count[0..nc) into start (start[nc] = total); also resets
+// `fill`, and with max_out != null stores the largest count. *total_out gets the total,
 // or 0 when it exceeds cap (cap >= 0): a cluster count above the buffers' capacity leaves
 // the build empty, so no later kernel of the call reads a cluster that was not written,
 // and the call is repeated with larger buffers sized from *total_raw.
@@ -130,11 +129,12 @@ __global__ void k_scatter(int n, const int *__restrict__ col_of, const int *__re
     sorted[start[col] + slot] = a;
 }
 
-// One block per column: sort its sites by (wrapped z, index) in place and count the
-// clusters the cutting rule makes.
+// One block per column: sort its sites by (wrapped z, index) in place, count the clusters
+// the cutting rule makes and record where each starts (cut[start + k] = first sorted
+// position of the column's cluster k).
 __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__restrict__ sorted,
                                const double *__restrict__ xb, double zcap, int *__restrict__ col_ncl,
-                               unsigned *__restrict__ flags, const int *__restrict__ meta) {
+                               int *__restrict__ cut, unsigned *__restrict__ flags, const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
     __shared__ double kz[MG_MAX_COLUMN];
     __shared__ int ki[MG_MAX_COLUMN];
@@ -185,6 +185,7 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
         int ncl = 0, first = 0;
         for (int i = 0; i < cnt; i++) {
             if (i == 0 || i - first == MG_CL || __dsub_rn(kz[i], kz[first]) > zcap) {
+                cut[s0 + ncl] = i;
                 ncl++;
                 first = i;
             }
@@ -193,50 +194,45 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
     }
 }
 
-// One block per column: write the clusters (sites, FP64 and FP32 boxes, centre).
+// One block per column, one thread per cluster of the column: write the clusters (sites,
+// FP64 and FP32 boxes, centre) from the cuts k_sort_columns recorded.
 __global__ void k_write_clusters(int n, const int *__restrict__ start, const int *__restrict__ sorted,
-                                 const int *__restrict__ cl_start, const double *__restrict__ xb, double zcap,
-                                 int cl_cap, int *__restrict__ cl_atom, double *__restrict__ cl_ref,
-                                 double *__restrict__ cl_bb, float *__restrict__ cl_bbf,
-                                 unsigned *__restrict__ flags, const int *__restrict__ meta) {
+                                 const int *__restrict__ cut, const int *__restrict__ col_ncl,
+                                 const int *__restrict__ cl_start, const double *__restrict__ xb, int cl_cap,
+                                 int *__restrict__ cl_atom, double *__restrict__ cl_ref, double *__restrict__ cl_bb,
+                                 float *__restrict__ cl_bbf, unsigned *__restrict__ flags,
+                                 const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
-    int col = blockIdx.x;
-    int s0 = start[col], cnt = start[col + 1] - s0;
-    if (cnt > MG_MAX_COLUMN || threadIdx.x != 0) return;
-    int c = cl_start[col];
-    int first = 0;
-    for (int i = 0; i <= cnt; i++) {
-        bool cut = (i == cnt) || (i > 0 && (i - first == MG_CL ||
-                                            __dsub_rn(xb[2 * (size_t)n + sorted[s0 + i]],
-                                                      xb[2 * (size_t)n + sorted[s0 + first]]) > zcap));
-        if (!cut) continue;
-        if (i > 0) {
-            if (c >= cl_cap) {
-                atomicOr(flags, MG_FLAG_LIST_OVERFLOW);
-                return;
-            }
-            double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-            for (int s = 0; s < MG_CL; s++) {
-                int idx = first + s;
-                int a = idx < i ? sorted[s0 + idx] : -1;
-                cl_atom[(size_t)c * MG_CL + s] = a;
-                if (a < 0) continue;
-                for (int d = 0; d < 3; d++) {
-                    double v = xb[(size_t)d * n + a];
-                    lo[d] = fmin(lo[d], v);
-                    hi[d] = fmax(hi[d], v);
-                }
-            }
-            for (int d = 0; d < 3; d++) {
-                cl_bb[(size_t)c * 6 + d] = lo[d];
-                cl_bb[(size_t)c * 6 + 3 + d] = hi[d];
-                cl_bbf[(size_t)c * 6 + d] = (float)lo[d];
-                cl_bbf[(size_t)c * 6 + 3 + d] = (float)hi[d];
-                cl_ref[(size_t)c * 3 + d] = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
-            }
-            c++;
+    const int col = blockIdx.x;
+    const int s0 = start[col], cnt = start[col + 1] - s0;
+    if (cnt > MG_MAX_COLUMN) return;
+    const int ncl = col_ncl[col], c0 = cl_start[col];
+    for (int k = threadIdx.x; k < ncl; k += blockDim.x) {
+        const int c = c0 + k;
+        if (c >= cl_cap) {
+            atomicOr(flags, MG_FLAG_LIST_OVERFLOW);
+            break;
         }
-        first = i;
+        const int first = cut[s0 + k], end = k + 1 < ncl ? cut[s0 + k + 1] : cnt;
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int s = 0; s < MG_CL; s++) {
+            const int idx = first + s;
+            const int a = idx < end ? sorted[s0 + idx] : -1;
+            cl_atom[(size_t)c * MG_CL + s] = a;
+            if (a < 0) continue;
+            for (int d = 0; d < 3; d++) {
+                const double v = xb[(size_t)d * n + a];
+                lo[d] = fmin(lo[d], v);
+                hi[d] = fmax(hi[d], v);
+            }
+        }
+        for (int d = 0; d < 3; d++) {
+            cl_bb[(size_t)c * 6 + d] = lo[d];
+            cl_bb[(size_t)c * 6 + 3 + d] = hi[d];
+            cl_bbf[(size_t)c * 6 + d] = (float)lo[d];
+            cl_bbf[(size_t)c * 6 + 3 + d] = (float)hi[d];
+            cl_ref[(size_t)c * 3 + d] = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
+        }
     }
 }
 
@@ -259,6 +255,8 @@ __device__ __forceinline__ float gap2f(float loi, float hii, float loj, float hi
 struct SearchArgs {
     int ncx, ncy;
     double lx, ly, lz, cwx, cwy, rlist, rlist2;
+    double nlx, nly, nlz;         // -lx, -ly, -lz: image shifts picked without FP64 arithmetic
+    float lxf, lyf, lzf, cwxf, cwyf;  // FP32 copies for the prefilters
     float flo, fhi, fmarg;  // FP32 band [rlist^2 - m, rlist^2 + m] and a length margin
     const int *meta;
     int *meta_w;
@@ -284,11 +282,13 @@ __device__ int column_hits(const SearchArgs &A, int I, const double *bi, const f
     int wx = ux % A.ncx;
     if (wx < 0) wx += A.ncx;
     const int ix = (ux - wx) / A.ncx;
-    const double sx = __dmul_rn((double)ix, A.lx), sy = __dmul_rn((double)iy, A.ly);
-    // conservative column rejection: the column's sites lie within its x/y slab
+    // image offsets (ix, iy in {-1, 0, 1}): exact in FP32 as (float)ix * (float)L
+    const float sxf = (float)ix * A.lxf, syf = (float)iy * A.lyf;
+    // conservative column rejection in FP32: the column's sites lie within its x/y slab;
+    // the FP32 error of the slab edges (~1e-5 A) is far inside the margin fmarg
     {
-        float cx_lo = (float)(wx * A.cwx + sx) - A.fmarg, cx_hi = (float)((wx + 1) * A.cwx + sx) + A.fmarg;
-        float cy_lo = (float)(wy * A.cwy + sy) - A.fmarg, cy_hi = (float)((wy + 1) * A.cwy + sy) + A.fmarg;
+        float cx_lo = fmaf((float)wx, A.cwxf, sxf) - A.fmarg, cx_hi = fmaf((float)(wx + 1), A.cwxf, sxf) + A.fmarg;
+        float cy_lo = fmaf((float)wy, A.cwyf, syf) - A.fmarg, cy_hi = fmaf((float)(wy + 1), A.cwyf, syf) + A.fmarg;
         float gx = fmaxf(0.f, fmaxf(cx_lo - bif[3], bif[0] - cx_hi));
         float gy = fmaxf(0.f, fmaxf(cy_lo - bif[4], bif[1] - cy_hi));
         if (gx * gx + gy * gy > A.fhi) return 0;
@@ -300,7 +300,7 @@ __device__ int column_hits(const SearchArgs &A, int I, const double *bi, const f
     int lo3[3], hi3[3];
     const float r = (float)A.rlist + A.fmarg;
     for (int k = 0; k < 3; k++) {
-        const float s = (float)((k - 1) * A.lz);
+        const float s = (float)(k - 1) * A.lzf;
         const float zmin = bif[2] - r - s, zmax = bif[5] + r - s;
         int a = j0, b = j1;  // first J with zhi >= zmin
         while (a < b) {
@@ -317,7 +317,6 @@ __device__ int column_hits(const SearchArgs &A, int I, const double *bi, const f
     }
     int cnt = 0;
     const int jlo = min(lo3[0], min(lo3[1], lo3[2])), jhi = max(hi3[0], max(hi3[1], hi3[2]));
-    const float sxf = (float)sx, syf = (float)sy;
     for (int J = jlo; J < jhi; J++) {
         bool inr = (J >= lo3[0] && J < hi3[0]) || (J >= lo3[1] && J < hi3[1]) || (J >= lo3[2] && J < hi3[2]);
         if (!inr) continue;
@@ -326,15 +325,18 @@ __device__ int column_hits(const SearchArgs &A, int I, const double *bi, const f
         if (dxyf > A.fhi) continue;
         const double *bj = A.bb + (size_t)J * 6;
         int hits = 0;
+        // ix * lx for ix in {-1, 0, 1}, selected rather than multiplied (FP64 is slow here)
+        const double sx = ix == 0 ? 0.0 : (ix > 0 ? A.lx : A.nlx);
+        const double sy = iy == 0 ? 0.0 : (iy > 0 ? A.ly : A.nly);
         for (int iz = -1; iz <= 1; iz++) {
-            float d2f = dxyf + gap2f(bif[2], bif[5], bjf[2], bjf[5], (float)(iz * A.lz));
+            float d2f = dxyf + gap2f(bif[2], bif[5], bjf[2], bjf[5], (float)iz * A.lzf);
             bool hit;
             if (d2f < A.flo) {
                 hit = true;
             } else if (d2f > A.fhi) {
                 hit = false;
             } else {  // FP64 decides, as the CPU builder does
-                double sz = __dmul_rn((double)iz, A.lz);
+                const double sz = iz == 0 ? 0.0 : (iz > 0 ? A.lz : A.nlz);
                 double dxy = __dadd_rn(gap2(bi[0], bi[3], bj[0], bj[3], sx), gap2(bi[1], bi[4], bj[1], bj[4], sy));
                 double d2 = __dadd_rn(dxy, gap2(bi[2], bi[5], bj[2], bj[5], sz));
                 hit = d2 < A.rlist2;
@@ -344,7 +346,7 @@ __device__ int column_hits(const SearchArgs &A, int I, const double *bi, const f
             if (out >= 0) {
                 const long long o = out + cnt;
                 const double *ri = A.ref + (size_t)I * 3, *rj = A.ref + (size_t)J * 3;
-                const double sz = __dmul_rn((double)iz, A.lz);
+                const double sz = iz == 0 ? 0.0 : (iz > 0 ? A.lz : A.nlz);
                 const double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], sx));
                 const double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], sy));
                 const double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], sz));
@@ -591,14 +593,17 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
                               meta + META_MAXCOL, -1, nullptr, meta);
     k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, col_of, (int *)c->d_col_start.p, (int *)c->d_col_fill.p,
                                               (int *)c->d_col_sorted.p, meta);
+    // the cluster cuts reuse col_of's storage, which k_scatter was the last to read
+    int *cut = col_of;
     k_sort_columns<<<ncol, 256, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, (double *)c->d_xbuild.p,
-                                       c->zcap, (int *)c->d_col_ncl.p, (unsigned *)c->d_flags.p, meta);
+                                       c->zcap, (int *)c->d_col_ncl.p, cut, (unsigned *)c->d_flags.p, meta);
     k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, nullptr, meta + META_NCL, nullptr,
                               c->cl_cap, meta + META_NCL_TOTAL, meta);
-    k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p,
-                                         (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p, c->zcap, c->cl_cap,
-                                         (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, (double *)c->d_cl_bb.p,
-                                         (float *)c->d_cl_bbf.p, (unsigned *)c->d_flags.p, meta);
+    k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, cut,
+                                         (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p,
+                                         c->cl_cap, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p,
+                                         (double *)c->d_cl_bb.p, (float *)c->d_cl_bbf.p, (unsigned *)c->d_flags.p,
+                                         meta);
     if (c->small_box) {
         long long tot = (long long)c->cl_cap * c->cl_cap;
         unsigned blocks = (unsigned)std::min<long long>((tot + 255) / 256, 65535);
@@ -614,6 +619,14 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         A.lz = c->lz;
         A.cwx = cwx;
         A.cwy = cwy;
+        A.nlx = -c->lx;
+        A.nly = -c->ly;
+        A.nlz = -c->lz;
+        A.lxf = (float)c->lx;
+        A.lyf = (float)c->ly;
+        A.lzf = (float)c->lz;
+        A.cwxf = (float)cwx;
+        A.cwyf = (float)cwy;
         A.rlist = rlist;
         A.rlist2 = rlist * rlist;
         // FP32 rounding of the boxes, shifts and gaps is below 8 u max(L) per gap
