@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa
         Z.x = (R)1;
         Z.y = (R)0;
     }
-    double F[3] = {0, 0, 0};
+    R Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};  // per-chunk sums accumulated as hi + lo
     const T4 *coef = (const T4 *)A.scoef;
     for (int r0 = 0; r0 < A.nrows; r0 += EW_FROWS) {
         const int nr = min(EW_FROWS, A.nrows - r0);
@@ -464,13 +464,11 @@ __global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa
             fy += gsum * (R)row.y;
             fz += gz;
         }
-        F[0] += (double)fx;
-        F[1] += (double)fy;
-        F[2] += (double)fz;
+        mg_acc2(Fh[0], Fl[0], fx);
+        mg_acc2(Fh[1], Fl[1], fy);
+        mg_acc2(Fh[2], Fl[2], fz);
     }
-    sF[g][0][l] = F[0];
-    sF[g][1][l] = F[1];
-    sF[g][2][l] = F[2];
+    for (int d = 0; d < 3; d++) sF[g][d][l] = (double)Fh[d] + (double)Fl[d];
     __syncthreads();
     if (g != 0 || !act) return;
     double fxs = 0, fys = 0, fzs = 0;

@@ -12,7 +12,7 @@
 //                                 per entry, row starts per i-cluster;
 //   reciprocal space              per-site phase tables e^{2 pi i n u} (n = 0..kmax per axis,
 //                                 complex FP32 or FP64), partial structure factors per site
-//                                 block (FP64), S(k) and force coefficients;
+//                                 block (FP32 or FP64), S(k) and force coefficients;
 //   energies                      per-block partial sums (FP64) reduced in a fixed order.
 #pragma once
 
@@ -20,6 +20,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mspms2_gb300.h"
@@ -211,17 +212,32 @@ bool mg_list_retry(mg_ctx *c, unsigned flags, const int *meta_host);
 // and summed in that fixed order by mg_launch_reduce.
 int mg_reserve_rows(mg_ctx *c, int nblocks);
 
-// per-block row writer: sums v[0..NC) over the block and stores them at row[ids[k]]
-template <int NC>
-__device__ __forceinline__ void mg_block_row(double (&v)[NC], const int (&ids)[NC], double *rows, int row) {
+// hi + lo += v exactly (Knuth's two-sum) in FP32, which keeps about 48 significant bits
+// without FP64 instructions (far slower than FP32 on this part); a plain addition in FP64
+template <typename R>
+__device__ __forceinline__ void mg_acc2(R &hi, R &lo, R v) {
+    if constexpr (std::is_same<R, float>::value) {
+        const float s = hi + v, bp = s - hi, ap = s - bp;
+        lo += (hi - ap) + (v - bp);
+        hi = s;
+    } else {
+        hi += v;
+    }
+}
+
+// per-block row writer: sums v[0..NC) over the block and stores them at row[ids[k]]. The
+// warp sums are taken in T (FP32 values are summed across the warp in FP32, since FP64 is
+// far slower on this part), the sums over warps in FP64, all in a fixed order.
+template <int NC, typename T>
+__device__ __forceinline__ void mg_block_row(T (&v)[NC], const int (&ids)[NC], double *rows, int row) {
     __shared__ double red[32][NC];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
-        double t = v[k];
+        T t = v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) red[w][k] = t;
+        if (lane == 0) red[w][k] = (double)t;
     }
     __syncthreads();
     double *out = rows + (size_t)row * E_NCOMP;

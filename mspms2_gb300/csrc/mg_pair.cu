@@ -13,17 +13,19 @@
 // float2 LJ pair and one int per lane) are staged in shared memory per step with
 // coalesced loads. The list is a full list (each pair seen from both clusters), so no
 // j-force scatter or atomic is needed: a lane accumulates only its own i-site force in
-// FP32 over at most 64 j-clusters, flushes into FP64 registers, and the four lanes of an
-// i-site are combined in FP64 with warp shuffles at the end. A lane's energy sums stay
-// in FP32 over its list and are reduced across lanes and blocks in FP64; they are halved
-// for the double counting. Every reduction has a fixed order, so results are
-// bit-reproducible.
+// FP32 over at most 64 j-clusters, then flushes it into an FP32 hi+lo pair by an exact
+// two-sum (about 48 significant bits, and no FP64 instruction, which is far slower than
+// FP32 on this part); the four lanes of an i-site are combined in FP64 with warp
+// shuffles at the end. A lane's energy sums stay in FP32 over its list, are summed
+// across the warp in FP32 and across warps and blocks in FP64; they are halved for the
+// double counting. The FP64 path accumulates in FP64 throughout. Every reduction has a
+// fixed order, so results are bit-reproducible.
 #include <math.h>
 
 #include "mg_internal.cuh"
 
 #define PAIR_WPB 4       // warps (i-clusters) per block
-#define PAIR_FLUSH 16    // list steps (4 j-clusters each) between FP64 force flushes
+#define PAIR_FLUSH 16    // list steps (4 j-clusters each) between force flushes
 
 namespace {
 
@@ -72,9 +74,9 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     __shared__ V4 s_shift[PAIR_WPB][4];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int I = blockIdx.x * PAIR_WPB + w;
-    // FP64 accumulators: force (long, short) and energies
-    double fL[3] = {0, 0, 0}, fS[3] = {0, 0, 0};
-    double eng[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // uvdw ushift ureal vir (long), same (short), npair
+    // force accumulators (hi + lo; long, short) and energies
+    R fLh[3] = {0, 0, 0}, fLl[3] = {0, 0, 0}, fSh[3] = {0, 0, 0}, fSl[3] = {0, 0, 0};
+    R eng[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // uvdw ushift ureal vir (long), same (short), npair
     if (I < A.meta[0]) {
         const V4 *pos = (const V4 *)A.pos;
         const V2 *lj = (const V2 *)A.lj;
@@ -182,19 +184,33 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
             }
             if (++steps == PAIR_FLUSH) {  // per-lane energies stay in R until the end
                 steps = 0;
-                fL[0] += ax; fL[1] += ay; fL[2] += az;
+                mg_acc2(fLh[0], fLl[0], ax);
+                mg_acc2(fLh[1], fLl[1], ay);
+                mg_acc2(fLh[2], fLl[2], az);
                 ax = ay = az = 0;
                 if (SPLIT) {
-                    fS[0] += bx; fS[1] += by; fS[2] += bz;
+                    mg_acc2(fSh[0], fSl[0], bx);
+                    mg_acc2(fSh[1], fSl[1], by);
+                    mg_acc2(fSh[2], fSl[2], bz);
                     bx = by = bz = 0;
                 }
             }
         }
-        fL[0] += ax; fL[1] += ay; fL[2] += az;
-        eng[0] += e_vdw; eng[1] += e_sh; eng[2] += e_re; eng[3] += e_vir;
-        fS[0] += bx; fS[1] += by; fS[2] += bz;
-        eng[4] += s_vdw; eng[5] += s_sh; eng[6] += s_re; eng[7] += s_vir;
-        eng[8] = (double)npair;
+        mg_acc2(fLh[0], fLl[0], ax);
+        mg_acc2(fLh[1], fLl[1], ay);
+        mg_acc2(fLh[2], fLl[2], az);
+        mg_acc2(fSh[0], fSl[0], bx);
+        mg_acc2(fSh[1], fSl[1], by);
+        mg_acc2(fSh[2], fSl[2], bz);
+        eng[0] = e_vdw; eng[1] = e_sh; eng[2] = e_re; eng[3] = e_vir;
+        eng[4] = s_vdw; eng[5] = s_sh; eng[6] = s_re; eng[7] = s_vir;
+        eng[8] = (R)npair;
+        double fL[3], fS[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            fL[k] = (double)fLh[k] + (double)fLl[k];
+            fS[k] = (double)fSh[k] + (double)fSl[k];
+        }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             fL[k] += __shfl_xor_sync(0xffffffffu, fL[k], 8);
@@ -221,7 +237,7 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
             }
         }
 #pragma unroll
-        for (int k = 0; k < 8; k++) eng[k] *= 0.5;  // every pair was seen from both sides
+        for (int k = 0; k < 8; k++) eng[k] *= (R)0.5;  // every pair was seen from both sides
     }
     const int ids[9] = {E_UVDW, E_USHIFT, E_UREAL, E_VIR, E_UVDW_S, E_USHIFT_S, E_UREAL_S, E_VIR_S, E_NPAIR};
     mg_block_row<9>(eng, ids, A.rows, A.row0 + blockIdx.x);
