@@ -253,6 +253,45 @@ MG_API mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);
 MG_API mg_status mg_debug_get_list(mg_ctx *ctx, int *ncl, long long *npairs, int *grid, double *zcap,
                             int *cluster_atoms, int *pairs, int *shifts);
 
+/* ---- device-resident integration (src/md.c, src/nvtnh.c) -------------------- */
+/* Schemes; the values are the reference's what_ensemble codes (src/defs.h:18-19). */
+enum {
+    MG_MD_NVE = 0,    /* vver(): velocity Verlet RESPA step (src/md.c:22-85) */
+    MG_MD_NVT_NH = 1  /* vver_nh_3(): Nose-Hoover RESPA step with implicit thermostat
+                         solves (src/nvtnh.c:11-271) */
+};
+
+/* Integration parameters, in the reference's reduced units and names (src/vars.h). */
+typedef struct mg_md_params {
+    int scheme;       /* MG_MD_* */
+    int nstep_inner;  /* short-force steps per outer step (nstep_inner) */
+    double delt;      /* outer step (delt after src/readins.c:73) */
+    double treq;      /* target temperature */
+    double qq, qqs;   /* thermostat masses, outer and inner (the MDNVT input section) */
+    double gg, ggs;   /* thermostat degrees of freedom (the reference sets both to nfree) */
+    int nfree;        /* 3*natom - nconstraint (src/initvars.c:588), for tinst */
+} mg_md_params;
+
+/* Thermostat scalars and the last step's kinetic quantities (src/vars.h:137-157). */
+typedef struct mg_md_state {
+    double ps, ss, pss, sss;          /* thermostat momenta and positions, outer and inner */
+    double ukin, tinst, unhts, unhtss;
+} mg_md_state;
+
+/* Values recorded per step by mg_md_run, in this order: ukin, uinter, uintra, ushift,
+ * ps, ss, pss, sss, tinst, unhts, unhtss, (unused). */
+#define MG_MD_LOG 12
+
+/* Runs nsteps steps of the scheme on the device, like the reference's main loop does with
+ * vver_nh_3() or vver() (src/mspms2.c:67-77): forces are evaluated first at the given
+ * positions, then every step kicks, drifts and re-evaluates forces with the positions,
+ * velocities and thermostat scalars kept in device memory. x/y/z and vx/vy/vz (host,
+ * [natom]) hold the start and are overwritten with the end; state likewise. log, if not
+ * NULL, receives (nsteps+1)*MG_MD_LOG doubles: the start, then every step. Site masses
+ * are the topology's aw. */
+MG_API mg_status mg_md_run(mg_ctx *ctx, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
+                           double *vx, double *vy, double *vz, mg_md_state *state, double *log);
+
 /* ---- reciprocal space without device allocation ---------------------------- */
 /* No counterpart in the reference: an extra entry point of this library.
  *

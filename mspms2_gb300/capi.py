@@ -68,6 +68,28 @@ class MgStats(C.Structure):
                 ("kernel_ms", C.c_double * 8), ("kernel_launches", C.c_int)]
 
 
+class MgMdParams(C.Structure):
+    _fields_ = [("scheme", C.c_int), ("nstep_inner", C.c_int), ("delt", C.c_double), ("treq", C.c_double),
+                ("qq", C.c_double), ("qqs", C.c_double), ("gg", C.c_double), ("ggs", C.c_double),
+                ("nfree", C.c_int)]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "MgMdParams":
+        return cls(**{k: d[k] for k, _ in cls._fields_})
+
+
+MD_STATE_NAMES = ["ps", "ss", "pss", "sss", "ukin", "tinst", "unhts", "unhtss"]
+MD_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "ps", "ss", "pss", "sss", "tinst", "unhts", "unhtss"]
+MD_LOG = 12
+
+
+class MgMdState(C.Structure):
+    _fields_ = [(n, C.c_double) for n in MD_STATE_NAMES]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n in MD_STATE_NAMES}
+
+
 def params_struct(p: dict) -> MgParams:
     m = MgParams()
     for name, ctype in PARAM_FIELDS:

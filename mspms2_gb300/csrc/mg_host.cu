@@ -85,7 +85,6 @@ extern "C" mg_status mg_create(mg_ctx **out, const mg_options *opt) {
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev <= c->opt.device || c->opt.device < 0) {
         cudaGetLastError();
-        static thread_local std::string last;
         delete c;
         return MG_ERR_NO_DEVICE;
     }
@@ -125,7 +124,9 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_pair_start, &c->d_pair_count, &c->d_pair_j, &c->d_pair_shift,
                       &c->d_pack_pos, &c->d_pack_lj, &c->d_pack_info, &c->d_rows, &c->d_row_slot,
                       &c->d_phase, &c->d_spart, &c->d_scoef, &c->d_tasks, &c->d_epart, &c->d_eout,
-                      &c->d_flags, &c->d_tasos, &c->d_myinterp, &c->d_tubes, &c->d_solid};
+                      &c->d_flags, &c->d_tasos, &c->d_myinterp, &c->d_tubes, &c->d_solid,
+                      &c->d_meta, &c->d_pair_img, &c->d_cl_bbf, &c->d_col_ncl, &c->d_counter,
+                      &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
     for (auto &b : c->myinterp_buf) mg_free(b);
@@ -660,7 +661,7 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
     return MG_OK;
 }
 
-static mg_status compute_impl(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
+mg_status mg_compute_forces(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
                               double *fl, double *fs, mg_energies *e) {
     for (int attempt = 0; attempt < 6; attempt++) {
         bool retry = false;
@@ -680,7 +681,7 @@ extern "C" mg_status mg_compute_device(mg_ctx *c, const double *dx, const double
     size_t nb = sizeof(double) * c->natom;
     if (!mg_ensure(c, c->d_fl, 3 * nb) || !mg_ensure(c, c->d_fs, 3 * nb)) return MG_ERR_ALLOC;
     double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
-    mg_status st = compute_impl(c, dx, dy, dz, terms, fl, fs, e);
+    mg_status st = mg_compute_forces(c, dx, dy, dz, terms, fl, fs, e);
     if (st && st != MG_ERR_NONFINITE) return st;
     cudaStream_t s = c->stream;
     if ((terms & MG_TERMS_LONG) && fxl && fyl && fzl) {
@@ -713,7 +714,7 @@ extern "C" mg_status mg_compute(mg_ctx *c, const double *x, const double *y, con
     MG_CUDA(cudaMemcpyAsync(dy, y, nb, cudaMemcpyHostToDevice, s));
     MG_CUDA(cudaMemcpyAsync(dz, z, nb, cudaMemcpyHostToDevice, s));
     double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
-    mg_status st = compute_impl(c, dx, dy, dz, terms, fl, fs, e);
+    mg_status st = mg_compute_forces(c, dx, dy, dz, terms, fl, fs, e);
     if (st && st != MG_ERR_NONFINITE) return st;
     if (terms & MG_TERMS_LONG) {
         MG_CUDA(cudaMemcpyAsync(fxl, fl, nb, cudaMemcpyDeviceToHost, s));

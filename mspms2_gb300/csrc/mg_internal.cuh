@@ -154,6 +154,9 @@ struct mg_ctx {
     long long pair_cap = 0;    // cluster-pair entry capacity
     DevBuf d_pair_start, d_pair_count, d_pair_j, d_pair_shift;
     DevBuf d_pack_pos, d_pack_lj, d_pack_info;
+    // integration (mg_md_run): velocities, solver work arrays, 1/mass, partial sums,
+    // thermostat scalars, per-step records
+    DevBuf d_md_v, d_md_work, d_md_rmass, d_md_part, d_md_dev, d_md_log;
     // reciprocal space
     int nrows = 0, nslots = 0, kmaxx = 0, kmaxy = 0, kmaxz = 0;
     long long kvectors = 0;
@@ -184,6 +187,10 @@ struct mg_ctx {
 mg_status mg_fail(mg_ctx *c, mg_status code, const std::string &msg);
 mg_status mg_cuda_fail(mg_ctx *c, cudaError_t e, const char *what);
 bool mg_ensure(mg_ctx *c, DevBuf &b, size_t bytes);
+// forces of the given terms at device positions into the context's [3][n] blocks fl/fs,
+// repeating the call when the neighbour-list set-up has to grow (mg_host.cu)
+mg_status mg_compute_forces(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
+                            double *fl, double *fs, mg_energies *e);
 void mg_free(DevBuf &b);
 
 #define MG_CUDA(call)                                                \

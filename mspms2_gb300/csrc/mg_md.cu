@@ -1,0 +1,468 @@
+// mg_md.cu - device-resident integration: the reference's velocity Verlet RESPA step
+// (vver, src/md.c:22-85) and its Nose-Hoover RESPA step with implicit thermostat
+// solves (vver_nh_3, src/nvtnh.c:11-271).
+//
+// Positions, velocities, forces and the thermostat scalars stay on the device for the
+// whole run; the host only orders the kernels, evaluates forces through the same path
+// as mg_compute_device and, once per batch of solver iterations, reads whether the
+// thermostat solve has converged. Sums over sites (sum m v^2 and the solver's delps)
+// are block partials reduced by one block in a fixed order, so a run is reproducible.
+//
+// Arithmetic follows the reference expression by expression in FP64 (r_mass = 1/aw,
+// f*r_mass, v^2/r_mass, ...). Reference behaviours kept:
+//  - the solver's convergence test reads the velocity arrays at index natom (a stale
+//    loop index, src/nvtnh.c:128-139 and :228-236), which the reference never writes,
+//    so only the thermostat test |(ps_new - ps_old)/ps_new| <= 1e-10 decides; at most
+//    100 iterations;
+//  - the thermostat predictor of the outer step uses sum m v^2 of the last inner solve.
+#include <math.h>
+
+#include <vector>
+
+#include "mg_internal.cuh"
+
+#define MD_TPB 256       // threads per block of the site kernels
+#define MD_ITER_BATCH 4  // solver iterations launched between convergence reads
+#define MD_MAX_ITER 100  // the reference's iteration limit
+#define MD_ERR 1.0e-10   // the reference's convergence tolerance
+
+namespace {
+
+// thermostat scalars and solver state, in device memory
+struct MdDev {
+    double ps, ss, pss, sss;  // thermostat momenta and positions (outer, inner)
+    double sumv2;             // the reference's running sum m v^2
+    double psn, pso, delps, di;
+    double ukin, tinst, unhts, unhtss;
+    int ready, iter;
+};
+
+struct MdArgs {
+    int n;
+    double *x, *y, *z;            // positions [n] each
+    double *v;                    // velocities [3][n]
+    double *vn, *vo, *b;          // solver work arrays [3][n]
+    const double *rmass;          // 1/aw per site
+    const double *fl, *fs;        // long and short forces [3][n]
+    double *part;                 // block partial sums
+    MdDev *s;
+};
+
+// sum of the block's values in a fixed order, written to part[blockIdx.x]
+__device__ __forceinline__ void block_partial(double v, double *part) {
+    __shared__ double red[MD_TPB];
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = MD_TPB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// fixed-order sum of nb block partials by one block
+__device__ double sum_partials(const double *part, int nb) {
+    __shared__ double red[MD_TPB];
+    double t = 0.0;
+    for (int i = threadIdx.x; i < nb; i += MD_TPB) t += part[i];
+    red[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = MD_TPB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    return red[0];
+}
+
+__global__ void k_md_rmass(int n, const double *__restrict__ aw, double *__restrict__ rmass) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) rmass[a] = 1.0 / aw[a];
+}
+
+// v += h (f r_mass - ps v) (ps = 0: plain kick); optional partial of sum m v^2 after it
+__global__ void k_md_kick(MdArgs A, const double *__restrict__ f, double h, int thermo, int want_sum) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        const double r = A.rmass[a], ps = thermo ? A.s->ps : 0.0;
+        const int n = A.n;
+        for (int d = 0; d < 3; d++) {
+            double v = A.v[d * n + a];
+            v = thermo ? v + h * (f[d * n + a] * r - ps * v) : v + h * f[d * n + a] * r;
+            A.v[d * n + a] = v;
+            m2 += v * v;
+        }
+        m2 /= r;
+    }
+    if (want_sum) block_partial(m2, A.part);
+}
+
+// inner step opening: partial of sum m v^2 (velocities before the kick), then
+// v += hs (fs r_mass - pss v), x += dts v  (pss = 0 without thermostat)
+__global__ void k_md_inner_drift(MdArgs A, double hs, double dts, int thermo) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        const double r = A.rmass[a], pss = thermo ? A.s->pss : 0.0;
+        const int n = A.n;
+        double *pos[3] = {A.x, A.y, A.z};
+        double s = 0.0;
+        for (int d = 0; d < 3; d++) {
+            double v = A.v[d * n + a];
+            s += v * v;
+            v = thermo ? v + hs * (A.fs[d * n + a] * r - pss * v) : v + hs * A.fs[d * n + a] * r;
+            A.v[d * n + a] = v;
+            pos[d][a] = pos[d][a] + dts * v;
+        }
+        m2 = s / r;
+    }
+    if (thermo) block_partial(m2, A.part);
+}
+
+// inner thermostat predictor (src/nvtnh.c:56-57)
+__global__ void k_md_inner_predict(MdArgs A, int nb, double ggs_treq, double dts, double dts_sqby2, double hs,
+                                   double qqs) {
+    const double sumv2 = sum_partials(A.part, nb);
+    if (threadIdx.x != 0) return;
+    MdDev *s = A.s;
+    s->sumv2 = sumv2;
+    s->sss = s->sss + s->pss * dts + (sumv2 - ggs_treq) * dts_sqby2 / qqs;
+    s->pss = s->pss + (sumv2 - ggs_treq) * hs / qqs;
+}
+
+// outer thermostat predictor (src/nvtnh.c:162-163), from the last inner solve's sum
+__global__ void k_md_outer_predict(MdDev *s, double gg_treq, double dt, double dt_sqby2, double h, double qq) {
+    s->ss = s->ss + s->ps * dt + (s->sumv2 - gg_treq) * dt_sqby2 / qq;
+    s->ps = s->ps + (s->sumv2 - gg_treq) * h / qq;
+}
+
+// ---- implicit thermostat solve (src/nvtnh.c:67-156 inner, :165-252 outer) ----------
+struct NhArgs {
+    const double *f;  // the forces of this solve
+    double h, dt, q, g_treq;
+    int inner;        // 1: pss (inner thermostat), 0: ps (outer)
+};
+
+__device__ __forceinline__ double &nh_ps(MdDev *s, int inner) { return inner ? s->pss : s->ps; }
+
+// vn = v and its sum m v^2; the scalar kernel below starts the iteration
+__global__ void k_nh_start(MdArgs A) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        const int n = A.n;
+        double s = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double v = A.v[d * n + a];
+            A.vn[d * n + a] = v;
+            s += v * v;
+        }
+        m2 = s / A.rmass[a];
+    }
+    block_partial(m2, A.part);
+}
+
+__global__ void k_nh_start_scalar(MdArgs A, int nb, int inner) {
+    const double sumv2 = sum_partials(A.part, nb);
+    if (threadIdx.x != 0) return;
+    A.s->sumv2 = sumv2;
+    A.s->psn = nh_ps(A.s, inner);
+    A.s->ready = 0;
+    A.s->iter = 0;
+}
+
+// vo = vn; b = -h (f r_mass - pso vo) - (v - vo); partial of sum (vo dt / q / r_mass) b
+__global__ void k_nh_residual(MdArgs A, NhArgs N) {
+    if (A.s->ready) return;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double t = 0.0;
+    if (a < A.n) {
+        const int n = A.n;
+        const double r = A.rmass[a], pso = A.s->psn;
+        for (int d = 0; d < 3; d++) {
+            const double vo = A.vn[d * n + a];
+            A.vo[d * n + a] = vo;
+            const double b = -N.h * (N.f[d * n + a] * r - pso * vo) - (A.v[d * n + a] - vo);
+            A.b[d * n + a] = b;
+            const double ri = vo * N.dt / N.q / r;
+            t += ri * b;
+        }
+    }
+    block_partial(t, A.part);
+}
+
+// Newton step of the thermostat momentum (src/nvtnh.c:99-102, :206-208)
+__global__ void k_nh_step_scalar(MdArgs A, NhArgs N, int nb) {
+    if (A.s->ready) return;
+    double delps = sum_partials(A.part, nb);
+    if (threadIdx.x != 0) return;
+    MdDev *s = A.s;
+    const double pso = s->psn, ps = nh_ps(s, N.inner);
+    const double di = -(pso * N.h + 1.0);
+    delps = delps - di * ((-s->sumv2 + N.g_treq) * N.h / N.q - (ps - pso));
+    delps = delps / (-N.dt * N.h * s->sumv2 / N.q + di);
+    s->pso = pso;
+    s->delps = delps;
+    s->di = di;
+}
+
+// vn += (b + h vo delps) / di and its sum m v^2
+__global__ void k_nh_update(MdArgs A, NhArgs N) {
+    if (A.s->ready) return;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        const int n = A.n;
+        const double delps = A.s->delps, di = A.s->di;
+        double s = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double vn = A.vn[d * n + a] + (A.b[d * n + a] + N.h * A.vo[d * n + a] * delps) / di;
+            A.vn[d * n + a] = vn;
+            s += vn * vn;
+        }
+        m2 = s / A.rmass[a];
+    }
+    block_partial(m2, A.part);
+}
+
+// new momentum and the reference's convergence test (thermostat only, see the header)
+__global__ void k_nh_check_scalar(MdArgs A, int nb) {
+    if (A.s->ready) return;
+    const double sumv2 = sum_partials(A.part, nb);
+    if (threadIdx.x != 0) return;
+    MdDev *s = A.s;
+    s->sumv2 = sumv2;
+    s->psn = s->pso + s->delps;
+    s->iter += 1;
+    const bool converged = !(fabs((s->psn - s->pso) / s->psn) > MD_ERR);
+    s->ready = (converged || s->iter >= MD_MAX_ITER) ? 1 : 0;
+}
+
+// v = vn; the thermostat takes the solved momentum
+__global__ void k_nh_finish(MdArgs A, int inner) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < 3 * A.n) A.v[a] = A.vn[a];
+    if (a == 0) nh_ps(A.s, inner) = A.s->psn;
+}
+
+// end-of-step scalars: thermostat energies, kinetic energy and temperature
+__global__ void k_md_step_scalars(MdDev *s, int nb_unused, double qq, double qqs, double gg_treq,
+                                  double ggs_treq, double nfree, int thermo, double *log_row) {
+    (void)nb_unused;
+    if (thermo) {
+        s->unhtss = (s->pss * s->pss * qqs) / 2.0 + ggs_treq * s->sss;
+        s->ukin = s->sumv2 / 2.0;
+        s->unhts = (s->ps * s->ps * qq) / 2.0 + gg_treq * s->ss;
+    }
+    s->tinst = 2.0 * s->ukin / nfree;
+    if (log_row) {
+        log_row[0] = s->ukin;
+        log_row[4] = s->ps;
+        log_row[5] = s->ss;
+        log_row[6] = s->pss;
+        log_row[7] = s->sss;
+        log_row[8] = s->tinst;
+        log_row[9] = s->unhts;
+        log_row[10] = s->unhtss;
+    }
+}
+
+// sum m v^2 / 2 of the current velocities into ukin (plain velocity Verlet, src/md.c:66-79)
+__global__ void k_md_ukin_scalar(MdArgs A, int nb) {
+    const double sumv2 = sum_partials(A.part, nb);
+    if (threadIdx.x == 0) A.s->ukin = sumv2 * 0.5;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------
+namespace {
+
+struct MdRun {
+    mg_ctx *c;
+    MdArgs A;
+    int nb;  // site blocks
+    cudaStream_t s;
+};
+
+mg_status nh_solve(MdRun &R, const double *f, double h, double dt, double q, double g_treq, int inner) {
+    mg_ctx *c = R.c;
+    NhArgs N;
+    N.f = f;
+    N.h = h;
+    N.dt = dt;
+    N.q = q;
+    N.g_treq = g_treq;
+    N.inner = inner;
+    k_nh_start<<<R.nb, MD_TPB, 0, R.s>>>(R.A);
+    k_nh_start_scalar<<<1, MD_TPB, 0, R.s>>>(R.A, R.nb, inner);
+    c->launches += 2;
+    for (int it = 0; it < MD_MAX_ITER; it += MD_ITER_BATCH) {
+        for (int k = 0; k < MD_ITER_BATCH; k++) {
+            k_nh_residual<<<R.nb, MD_TPB, 0, R.s>>>(R.A, N);
+            k_nh_step_scalar<<<1, MD_TPB, 0, R.s>>>(R.A, N, R.nb);
+            k_nh_update<<<R.nb, MD_TPB, 0, R.s>>>(R.A, N);
+            k_nh_check_scalar<<<1, MD_TPB, 0, R.s>>>(R.A, R.nb);
+        }
+        c->launches += 4 * MD_ITER_BATCH;
+        int ready = 0;
+        MG_CUDA(cudaMemcpyAsync(&ready, &R.A.s->ready, sizeof(int), cudaMemcpyDeviceToHost, R.s));
+        MG_CUDA(cudaStreamSynchronize(R.s));
+        if (ready) break;
+    }
+    k_nh_finish<<<(3 * R.A.n + MD_TPB - 1) / MD_TPB, MD_TPB, 0, R.s>>>(R.A, inner);
+    c->launches += 1;
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+}  // namespace
+
+extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, double *x, double *y, double *z,
+                               double *vx, double *vy, double *vz, mg_md_state *state, double *log) {
+    if (!c || !mp || !state || nsteps < 0 || !x || !y || !z || !vx || !vy || !vz) return MG_ERR_INVALID;
+    if (mp->scheme != MG_MD_NVE && mp->scheme != MG_MD_NVT_NH)
+        return mg_fail(c, MG_ERR_INVALID, "unknown integration scheme");
+    if (mp->nstep_inner < 1 || !(mp->delt > 0) || !(mp->nfree > 0))
+        return mg_fail(c, MG_ERR_INVALID, "nstep_inner, delt and nfree must be positive");
+    if (mp->scheme == MG_MD_NVT_NH && !(mp->qq > 0 && mp->qqs > 0))
+        return mg_fail(c, MG_ERR_INVALID, "thermostat masses must be positive");
+    if (!c->have_topology || !c->have_params || !c->have_box)
+        return mg_fail(c, MG_ERR_STATE, "set topology, params and box before integrating");
+    cudaSetDevice(c->device);
+    const int n = c->natom;
+    const size_t nb3 = sizeof(double) * 3 * (size_t)n;
+    const int nb = (n + MD_TPB - 1) / MD_TPB;
+    if (!mg_ensure(c, c->d_x, nb3) || !mg_ensure(c, c->d_fl, nb3) || !mg_ensure(c, c->d_fs, nb3) ||
+        !mg_ensure(c, c->d_md_v, nb3) || !mg_ensure(c, c->d_md_work, 3 * nb3) ||
+        !mg_ensure(c, c->d_md_rmass, sizeof(double) * n) || !mg_ensure(c, c->d_md_part, sizeof(double) * (nb + 1)) ||
+        !mg_ensure(c, c->d_md_dev, sizeof(MdDev)) ||
+        !mg_ensure(c, c->d_md_log, sizeof(double) * MG_MD_LOG * ((size_t)nsteps + 1)))
+        return MG_ERR_ALLOC;
+    cudaStream_t s = c->stream;
+    double *dx = (double *)c->d_x.p, *dy = dx + n, *dz = dy + n;
+    double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
+    double *v = (double *)c->d_md_v.p, *w = (double *)c->d_md_work.p;
+    double *dlog = (double *)c->d_md_log.p;
+    const size_t nb1 = sizeof(double) * n;
+    MG_CUDA(cudaMemcpyAsync(dx, x, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(dy, y, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(dz, z, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(v, vx, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(v + n, vy, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(v + 2 * n, vz, nb1, cudaMemcpyHostToDevice, s));
+    MdDev h0 = {};
+    h0.ps = state->ps;
+    h0.ss = state->ss;
+    h0.pss = state->pss;
+    h0.sss = state->sss;
+    h0.unhts = state->unhts;
+    h0.unhtss = state->unhtss;
+    MG_CUDA(cudaMemcpyAsync(c->d_md_dev.p, &h0, sizeof(MdDev), cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemsetAsync(dlog, 0, sizeof(double) * MG_MD_LOG * ((size_t)nsteps + 1), s));
+    MdRun R;
+    R.c = c;
+    R.nb = nb;
+    R.s = s;
+    MdArgs &A = R.A;
+    A.n = n;
+    A.x = dx;
+    A.y = dy;
+    A.z = dz;
+    A.v = v;
+    A.vn = w;
+    A.vo = w + 3 * (size_t)n;
+    A.b = w + 6 * (size_t)n;
+    A.rmass = (const double *)c->d_md_rmass.p;
+    A.fl = fl;
+    A.fs = fs;
+    A.part = (double *)c->d_md_part.p;
+    A.s = (MdDev *)c->d_md_dev.p;
+    k_md_rmass<<<nb, MD_TPB, 0, s>>>(n, (const double *)c->d_site_aw.p, (double *)c->d_md_rmass.p);
+    MG_CUDA(cudaGetLastError());
+
+    const bool nh = mp->scheme == MG_MD_NVT_NH;
+    const double dt = mp->delt, h = dt / 2.0, dts = dt / mp->nstep_inner, hs = dts / 2.0;
+    const double dt_sqby2 = dt * dt / 2.0, dts_sqby2 = dts * dts / 2.0;
+    const double gg_treq = mp->gg * mp->treq, ggs_treq = mp->ggs * mp->treq;
+    std::vector<double> hlog(MG_MD_LOG * ((size_t)nsteps + 1), 0.0);
+
+    // forces at the start, as the reference evaluates them before its loop
+    mg_energies e;
+    mg_status st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_ALL, fl, fs, &e);
+    if (st) return st;
+    double uinter = e.uinter, uintra = e.uintra, ushift = e.ushift;
+    // step 0 record: kinetic energy of the given velocities
+    k_nh_start<<<nb, MD_TPB, 0, s>>>(A);
+    k_md_ukin_scalar<<<1, MD_TPB, 0, s>>>(A, nb);
+    k_md_step_scalars<<<1, 1, 0, s>>>(A.s, nb, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 0, dlog);
+    hlog[1] = uinter;
+    hlog[2] = uintra;
+    hlog[3] = ushift;
+    for (int step = 1; step <= nsteps; step++) {
+        k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fl, h, nh ? 1 : 0, 0);
+        for (int ll = 0; ll < mp->nstep_inner; ll++) {
+            k_md_inner_drift<<<nb, MD_TPB, 0, s>>>(A, hs, dts, nh ? 1 : 0);
+            if (nh) k_md_inner_predict<<<1, MD_TPB, 0, s>>>(A, nb, ggs_treq, dts, dts_sqby2, hs, mp->qqs);
+            MG_CUDA(cudaGetLastError());
+            if ((st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_SHORT, fl, fs, &e))) return st;
+            uintra = e.uintra;
+            if (nh) {
+                if ((st = nh_solve(R, fs, hs, dts, mp->qqs, ggs_treq, 1))) return st;
+            } else {
+                k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fs, hs, 0, 0);
+            }
+        }
+        if (nh) k_md_outer_predict<<<1, 1, 0, s>>>(A.s, gg_treq, dt, dt_sqby2, h, mp->qq);
+        MG_CUDA(cudaGetLastError());
+        if ((st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_LONG, fl, fs, &e))) return st;
+        uinter = e.uinter;
+        ushift = e.ushift;
+        double *row = dlog + (size_t)step * MG_MD_LOG;
+        if (nh) {
+            if ((st = nh_solve(R, fl, h, dt, mp->qq, gg_treq, 0))) return st;
+            k_md_step_scalars<<<1, 1, 0, s>>>(A.s, nb, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 1, row);
+        } else {
+            k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fl, h, 0, 1);
+            k_md_ukin_scalar<<<1, MD_TPB, 0, s>>>(A, nb);
+            k_md_step_scalars<<<1, 1, 0, s>>>(A.s, nb, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 0, row);
+        }
+        MG_CUDA(cudaGetLastError());
+        hlog[(size_t)step * MG_MD_LOG + 1] = uinter;
+        hlog[(size_t)step * MG_MD_LOG + 2] = uintra;
+        hlog[(size_t)step * MG_MD_LOG + 3] = ushift;
+    }
+    MG_CUDA(cudaMemcpyAsync(x, dx, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(y, dy, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(z, dz, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vx, v, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vy, v + n, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vz, v + 2 * n, nb1, cudaMemcpyDeviceToHost, s));
+    MdDev hf;
+    MG_CUDA(cudaMemcpyAsync(&hf, c->d_md_dev.p, sizeof(MdDev), cudaMemcpyDeviceToHost, s));
+    std::vector<double> dl(hlog.size());
+    MG_CUDA(cudaMemcpyAsync(dl.data(), dlog, sizeof(double) * dl.size(), cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    MG_CUDA(cudaGetLastError());
+    state->ps = hf.ps;
+    state->ss = hf.ss;
+    state->pss = hf.pss;
+    state->sss = hf.sss;
+    state->ukin = hf.ukin;
+    state->tinst = hf.tinst;
+    state->unhts = hf.unhts;
+    state->unhtss = hf.unhtss;
+    if (log) {
+        for (size_t r = 0; r <= (size_t)nsteps; r++) {
+            double *o = log + r * MG_MD_LOG;
+            const double *d = dl.data() + r * MG_MD_LOG;
+            for (int k = 0; k < MG_MD_LOG; k++) o[k] = d[k];
+            o[1] = hlog[r * MG_MD_LOG + 1];
+            o[2] = hlog[r * MG_MD_LOG + 2];
+            o[3] = hlog[r * MG_MD_LOG + 3];
+        }
+    }
+    return MG_OK;
+}

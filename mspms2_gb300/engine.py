@@ -69,6 +69,8 @@ def load_library(path: str = LIB_PATH):
     lib.mg_debug_get_list.argtypes = [V, C.POINTER(I), C.POINTER(C.c_longlong), C.POINTER(I),
                                       C.POINTER(D), C.POINTER(I), C.POINTER(I), C.POINTER(I)]
     lib.mg_abi_version.restype = I
+    lib.mg_md_run.argtypes = [V, C.POINTER(capi.MgMdParams), I, _dp, _dp, _dp, _dp, _dp, _dp,
+                              C.POINTER(capi.MgMdState), _dp]
     _lib = lib
     return lib
 
@@ -174,6 +176,21 @@ class Engine:
         fs = [dfs, dfs + 8 * n, dfs + 16 * n] if dfs else [None] * 3
         self._check(self.lib.mg_compute_device(self.ctx, dx, dy, dz, terms, *fl, *fs, C.byref(e)))
         return e.as_dict()
+
+    def md_run(self, nsteps: int, md: dict, v, x=None, y=None, z=None, state: dict | None = None):
+        """nsteps of the reference's integrator on the device (mg_md_run): md holds the
+        mg_md_params fields (mspms2_gb300.system.md_params), v the [3, n] start velocities.
+        Returns (positions [3, n], velocities [3, n], state dict, log [(nsteps+1), 12])."""
+        s = self.system
+        pos = np.ascontiguousarray(np.stack([s.x if x is None else x, s.y if y is None else y,
+                                             s.z if z is None else z]), dtype=np.float64)
+        vel = np.ascontiguousarray(v, dtype=np.float64).copy()
+        st = capi.MgMdState(**(state or {}))
+        log = np.zeros((nsteps + 1, capi.MD_LOG))
+        mp = capi.MgMdParams.from_dict(md)
+        self._check(self.lib.mg_md_run(self.ctx, C.byref(mp), nsteps, _p(pos[0]), _p(pos[1]), _p(pos[2]),
+                                       _p(vel[0]), _p(vel[1]), _p(vel[2]), C.byref(st), _p(log)))
+        return pos, vel, st.as_dict(), log
 
     def stats(self) -> dict:
         st = MgStats()

@@ -131,6 +131,8 @@ class System:
     what_simulation: int = 0
     what_ensemble: int = 1
     nconstraint: int = 0
+    nh_qq: float = 1000.0  # Nose-Hoover masses of the MDNVT section (outer, inner)
+    nh_qqs: float = 1000.0
     nstep: int = 10
     # solid-fluid data
     tasos: list = field(default_factory=list)
@@ -214,6 +216,24 @@ def derive_params(s: System) -> dict:
 # ---------------------------------------------------------------------------------
 # reference file format
 # ---------------------------------------------------------------------------------
+BOLTZMANN = 1.3806505e-23  # J/K (src/defs.h:91)
+
+
+def time_base(s: System) -> float:
+    """Reduced time unit in fs (src/readins.c:37)."""
+    return math.sqrt(s.mass_base * 1.0e-27 / (s.epsilon_base * BOLTZMANN)) * s.sigma_base * 1.0e5
+
+
+def md_params(s: System) -> dict:
+    """mg_md_params of the system's MD settings: delt and treq reduced as src/readins.c:44-45
+    and :72-73 do, nfree = 3*natom - nconstraint (src/initvars.c:588), gg = ggs = nfree
+    and the MDNVT masses (src/initvars.c:321-338)."""
+    nfree = 3 * s.natom - s.nconstraint
+    return dict(scheme=s.what_ensemble, nstep_inner=s.nstep_inner, delt=s.delt_fs / time_base(s),
+                treq=s.treq_K / s.epsilon_base, qq=s.nh_qq, qqs=s.nh_qqs, gg=float(nfree), ggs=float(nfree),
+                nfree=nfree)
+
+
 def _first(line: str) -> str:
     return line.split()[0]
 
@@ -382,6 +402,9 @@ def read_reference_dir(path: str) -> System:
                nstep_inner=nstep_inner, what_simulation=what_sim, what_ensemble=what_ens,
                nconstraint=ncons, nstep=nstep, name=os.path.basename(os.path.normpath(path)))
 
+    k = _find_section(lines, "MDNVT")
+    if k is not None:
+        s.nh_qq, s.nh_qqs = (float(v) for v in lines[k].split()[:2])
     if charge_type in (ELEC_EWALD, ELEC_WOLF, ELEC_SIMPLE_COULOMB):
         k = _find_section(lines, "ELECTROSTATIC")
         if k is None:
@@ -477,7 +500,7 @@ def write_reference_dir(s: System, path: str, grid_names=None) -> None:
                   f"{s.ksqmax}", f"{s.ewald_bc}", f"{s.ewald_dim}"]
     else:
         lines += [_fmt(s.kappa / sb)]
-    lines += ["", "MDNVT", "1000.0 1000.0", "", "MDNPT", "1.0e3 1.0e3", ""]
+    lines += ["", "MDNVT", f"{_fmt(s.nh_qq)} {_fmt(s.nh_qqs)}", "", "MDNPT", "1.0e3 1.0e3", ""]
     if s.sf_type == SF_HYPERGEO:
         lines += ["HyperGeo", f"{len(s.tube_xy_r)}", _fmt(s.solid_sigma * sb), _fmt(s.solid_epsilon * eb)]
         lines += [" ".join(_fmt(v * sb) for v in row) for row in s.tube_xy_r]
@@ -572,6 +595,8 @@ def write_reference_dir(s: System, path: str, grid_names=None) -> None:
 _SCALARS = ["sigma_base", "epsilon_base", "mass_base", "rcuton", "rcutoff", "rcutoffelec", "lj_switch",
             "lj_lrc", "f0", "charge_type", "kappa", "ksqmax", "ewald_bc", "ewald_dim", "sf_type",
             "compat", "respa_split", "solid_sigma", "solid_epsilon", "name"]
+# MD settings, stored only when present in an archive (older archives lack them)
+_MD_SCALARS = ["treq_K", "delt_fs", "nstep_inner", "what_ensemble", "nconstraint", "nh_qq", "nh_qqs"]
 _SP_ARRAYS = ["atom_type", "ghost", "interp", "epsilon", "sigma", "charge", "aw", "aw_input",
               "template_xyz", "bond_idx", "bond_type", "bond_param", "angle_idx", "angle_type",
               "angle_param", "dih_idx", "dih_type", "dih_param", "imp_idx", "imp_type", "imp_param",
@@ -580,7 +605,7 @@ _SP_ARRAYS = ["atom_type", "ghost", "interp", "epsilon", "sigma", "charge", "aw"
 
 def system_to_arrays(s: System, prefix: str = "") -> dict:
     d = {}
-    for k in _SCALARS:
+    for k in _SCALARS + _MD_SCALARS:
         d[prefix + k] = np.array(getattr(s, k))
     d[prefix + "kmax"] = np.array(s.kmax)
     d[prefix + "box"] = np.asarray(s.box)
@@ -627,7 +652,7 @@ def system_from_arrays(d, prefix: str = "") -> System:
     xyz = np.array(g("xyz"), dtype=np.float64)
     s = System(species=species, box=np.array(g("box"), dtype=np.float64), x=xyz[0].copy(),
                y=xyz[1].copy(), z=xyz[2].copy())
-    for k in _SCALARS:
+    for k in _SCALARS + [k for k in _MD_SCALARS if prefix + k in d]:
         v = g(k)
         cur = getattr(s, k)
         setattr(s, k, str(v) if isinstance(cur, str) else type(cur)(v.item()))

@@ -87,6 +87,12 @@ int orc_tasos_force(const orc_tasos *g, unsigned compat, double x, double y, dou
                     double *pe, double force[3]);
 double orc_tasos_min_pe(const orc_tasos *g);
 
+/* Integrators (md_oracle.c): nsteps of vver() (src/md.c:22-85) or vver_nh_3()
+ * (src/nvtnh.c:11-271) as chosen by p->scheme, after one force evaluation at the start,
+ * with the same arguments and per-step record as mg_md_run. Returns 0. */
+int orc_md_run(const orc_system *s, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
+               double *vx, double *vy, double *vz, mg_md_state *state, double *log);
+
 /* CPU cluster-pair builder (same predicate, same op order as the GPU build); the
  * second form takes the column grid and small-box choice of the build under test. */
 int orc_nblist_build(const double *x, const double *y, const double *z, int natom,

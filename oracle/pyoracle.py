@@ -14,7 +14,8 @@ import tempfile
 
 import numpy as np
 
-from mspms2_gb300.capi import ENERGY_NAMES, MgEnergies, MgParams, MgSpecies, SpeciesPack, system_params
+from mspms2_gb300.capi import (ENERGY_NAMES, MD_LOG, MgEnergies, MgMdParams, MgMdState, MgParams, MgSpecies,
+                               SpeciesPack, system_params)
 from mspms2_gb300.system import System, write_reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -53,7 +54,8 @@ class OrcWindow(C.Structure):
 
 
 def build() -> str:
-    src = [os.path.join(HERE, f) for f in ("mspms_oracle.c", "nblist_oracle.c", "mspms_oracle.h")]
+    src = [os.path.join(HERE, f) for f in ("mspms_oracle.c", "nblist_oracle.c", "md_oracle.c", "mspms_oracle.h",
+                                           os.path.join("..", "include", "mspms2_gb300.h"))]
     if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB
@@ -74,6 +76,8 @@ def lib():
         _lib.orc_count_pairs.restype = C.c_longlong
         _lib.orc_tasos_force.argtypes = [C.POINTER(OrcTasos), C.c_uint, C.c_double, C.c_double,
                                          C.c_double, _dp, _dp]
+        _lib.orc_md_run.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgMdParams), C.c_int, _dp, _dp, _dp, _dp, _dp,
+                                    _dp, C.POINTER(MgMdState), _dp]
         _lib.orc_tasos_min_pe.argtypes = [C.POINTER(OrcTasos)]
         _lib.orc_tasos_min_pe.restype = C.c_double
         _lib.orc_nblist_build.argtypes = [_dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
@@ -162,6 +166,18 @@ class Oracle:
         d = e.as_dict()
         return f, {k: d[k] for k in ("ubond", "uangle", "udih", "uimp", "uintra", "virial_intra")}, err
 
+    def md_run(self, nsteps: int, md: dict, v, state: dict | None = None):
+        """The restated vver()/vver_nh_3() (oracle/md_oracle.c), same contract as
+        Engine.md_run: (positions, velocities, state, log)."""
+        sysm = self.system
+        pos = np.ascontiguousarray(np.stack([sysm.x, sysm.y, sysm.z]), dtype=np.float64)
+        vel = np.ascontiguousarray(v, dtype=np.float64).copy()
+        st = MgMdState(**(state or {}))
+        log = np.zeros((nsteps + 1, MD_LOG))
+        lib().orc_md_run(C.byref(self.s), C.byref(MgMdParams.from_dict(md)), nsteps, _ptr(pos[0]), _ptr(pos[1]),
+                         _ptr(pos[2]), _ptr(vel[0]), _ptr(vel[1]), _ptr(vel[2]), C.byref(st), _ptr(log))
+        return pos, vel, st.as_dict(), log
+
     def count_pairs(self, r: float) -> int:
         s = self.system
         x, y, z = (np.ascontiguousarray(v, dtype=np.float64) for v in (s.x, s.y, s.z))
@@ -181,6 +197,29 @@ def read_ref_output(fn: str):
               "coulomb_prefactor", "boxlx", "boxly", "boxlz", "sigma_base", "epsilon_base"]
     d = dict(zip(dnames, a[6 * n + 18:6 * n + 42]))
     return fl, fs, e, d
+
+
+def run_reference_md(path: str, nsteps: int) -> dict:
+    """Run the compiled reference's own integrator for the input's ensemble (harness md
+    mode, oracle/ref_harness.c) and parse its record."""
+    with tempfile.TemporaryDirectory() as td:
+        out, md = os.path.join(td, "out.bin"), os.path.join(td, "md.bin")
+        p = subprocess.run([REF_BIN, path, out, "0", "md", str(nsteps), md], capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"reference md run failed: {p.stderr[-2000:]}")
+        b = open(md, "rb").read()
+    n, nstep_inner, ens, ns = (int(v) for v in np.frombuffer(b[:16], np.int32))
+    sc = np.frombuffer(b[16:112])
+    off = 112
+    start = np.frombuffer(b[off:off + 48 * n]).reshape(6, n).copy()
+    off += 48 * n
+    log = np.frombuffer(b[off:off + 96 * (ns + 1)]).reshape(ns + 1, 12).copy()
+    off += 96 * (ns + 1)
+    end = np.frombuffer(b[off:off + 48 * n]).reshape(6, n).copy()
+    md = dict(scheme=ens, nstep_inner=nstep_inner, delt=sc[0], treq=sc[1], qq=sc[2], qqs=sc[3], gg=sc[4],
+              ggs=sc[5], nfree=int(sc[6]))
+    state = dict(ps=sc[7], ss=sc[8], pss=sc[9], sss=sc[10])
+    return {"md": md, "state": state, "start": start, "log": log, "end": end, "nsteps": ns}
 
 
 def reference_available() -> bool:

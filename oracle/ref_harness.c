@@ -9,6 +9,15 @@
  *   double energies[18] (mg_energies order); double derived[24] (see below).
  * With a repeat count R > 0 it then times R further frclong() calls and R frcshort()
  * calls and prints "frclong_s=<seconds per call> frcshort_s=<...>".
+ *
+ * With "md <nsteps> <md.bin>" after the repeat count it then runs nsteps steps of the
+ * reference's own integrator for the input's ensemble (what_ensemble NVT: vver_nh_3,
+ * src/nvtnh.c:11; NVE: vver, src/md.c:22), starting from the velocities init_vars()
+ * drew, and writes
+ *   int32 natom, nstep_inner, what_ensemble, nsteps; double scalars[12] = {delt, treq,
+ *   qq, qqs, gg, ggs, nfree, ps, ss, pss, sss, 0}; double x,y,z,vx,vy,vz[n] (start);
+ *   per step (0 = start, then 1..nsteps) double log[12] = {ukin, uinter, uintra, ushift,
+ *   ps, ss, pss, sss, tinst, unhts, unhtss, 0}; double x,y,z,vx,vy,vz[n] (end).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -19,6 +28,30 @@
 
 int opening();
 int fnValidateInput();
+int vver();
+int vver_nh_3();
+
+static void abs_path(const char *name, char *out, size_t len) {
+    if (name[0] != '/' && getcwd(out, len - 1)) {
+        snprintf(out + strlen(out), len - strlen(out), "/%s", name);
+    } else {
+        snprintf(out, len, "%s", name);
+    }
+}
+
+static void write_state(FILE *fp, int n) {
+    fwrite(xx, sizeof(double), n, fp);
+    fwrite(yy, sizeof(double), n, fp);
+    fwrite(zz, sizeof(double), n, fp);
+    fwrite(vx, sizeof(double), n, fp);
+    fwrite(vy, sizeof(double), n, fp);
+    fwrite(vz, sizeof(double), n, fp);
+}
+
+static void write_log(FILE *fp) {
+    double l[12] = {ukin, uinter, uintra, ushift, ps, ss, pss, sss, tinst, unhts, unhtss, 0.0};
+    fwrite(l, sizeof(double), 12, fp);
+}
 
 static double now_s(void) {
     struct timespec ts;
@@ -28,18 +61,18 @@ static double now_s(void) {
 
 int main(int argc, char **argv) {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s <dir> <out.bin> [repeat]\n", argv[0]);
+        fprintf(stderr, "usage: %s <dir> <out.bin> [repeat [md <nsteps> <md.bin>]]\n", argv[0]);
         return 2;
     }
-    const char *outname = argv[2];
     char outabs[4096];
-    if (outname[0] != '/') {
-        if (!getcwd(outabs, sizeof(outabs) - 1)) return 2;
-        snprintf(outabs + strlen(outabs), sizeof(outabs) - strlen(outabs), "/%s", outname);
-    } else {
-        snprintf(outabs, sizeof(outabs), "%s", outname);
-    }
+    abs_path(argv[2], outabs, sizeof(outabs));
     int repeat = argc > 3 ? atoi(argv[3]) : 0;
+    int md_steps = 0;
+    char mdabs[4096] = {0};
+    if (argc > 6 && !strcmp(argv[4], "md")) {
+        md_steps = atoi(argv[5]);
+        abs_path(argv[6], mdabs, sizeof(mdabs));
+    }
     if (chdir(argv[1]) != 0) { perror("chdir"); return 2; }
     opening();
     readins();
@@ -74,6 +107,25 @@ int main(int argc, char **argv) {
         for (int r = 0; r < repeat; r++) frcshort();
         double t2 = now_s();
         printf("frclong_s=%.9g frcshort_s=%.9g\n", (t1 - t0) / repeat, (t2 - t1) / repeat);
+    }
+    if (md_steps > 0) {
+        int (*scheme)() = what_ensemble == NVT ? vver_nh_3 : (what_ensemble == NVE ? vver : NULL);
+        if (!scheme) { fprintf(stderr, "md mode supports NVT and NVE only\n"); return 2; }
+        if (repeat > 0) { frclong(); frcshort(); }
+        FILE *fm = fopen(mdabs, "wb");
+        if (!fm) { perror("md out"); return 2; }
+        int hdr[4] = {n, nstep_inner, what_ensemble, md_steps};
+        fwrite(hdr, sizeof(int), 4, fm);
+        double sc[12] = {delt, treq, qq, qqs, gg, ggs, (double)nfree, ps, ss, pss, sss, 0.0};
+        fwrite(sc, sizeof(double), 12, fm);
+        write_state(fm, n);
+        write_log(fm);
+        for (int k = 0; k < md_steps; k++) {
+            scheme();
+            write_log(fm);
+        }
+        write_state(fm, n);
+        fclose(fm);
     }
     return 0;
 }

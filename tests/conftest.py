@@ -15,7 +15,27 @@ def pytest_configure(config):
 
 
 def golden_cases():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Force fixtures (frclong/frcshort outputs of the compiled reference)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("md_"))
+
+
+def md_golden_cases():
+    """Trajectory fixtures of the reference's integrators."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("md_"))
+
+
+def load_md_case(name):
+    """(system at the start, md params dict, start state dict, start velocities [3, n],
+    reference log [(nsteps+1), 12], reference end [6, n], nsteps)."""
+    import numpy as np
+    from mspms2_gb300.system import load_system
+    s, d = load_system(os.path.join(GOLDEN, name + ".npz"))
+    scheme, nstep_inner, nfree, nsteps = (int(v) for v in d["md_int"])
+    delt, treq, qq, qqs, gg, ggs = (float(v) for v in d["md_real"])
+    md = dict(scheme=scheme, nstep_inner=nstep_inner, delt=delt, treq=treq, qq=qq, qqs=qqs, gg=gg, ggs=ggs,
+              nfree=nfree)
+    state = dict(zip(("ps", "ss", "pss", "sss"), (float(v) for v in d["md_state0"])))
+    return s, md, state, np.array(d["md_v0"]), np.array(d["md_log"]), np.array(d["md_end"]), nsteps
 
 
 @pytest.fixture(scope="session")

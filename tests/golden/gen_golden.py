@@ -7,6 +7,11 @@ from the reference checkout), and stored as <case>.npz with:
   ref_fl[3,n], ref_fs[3,n]  forces of frclong() / frcshort(),
   ref_energies[18]          in mspms2_gb300.capi.ENERGY_NAMES order,
   ref_derived[24]           derived globals after init_vars().
+The md_* cases hold trajectories of the reference's own integrators instead (vver_nh_3 or
+vver, run by the harness's md mode): md_int (scheme, nstep_inner, nfree, nsteps), md_real
+(delt, treq, qq, qqs, gg, ggs), md_state0 (ps, ss, pss, sss), md_v0[3,n] start velocities
+(drawn by the reference's velinit), md_log[nsteps+1, 12] and md_end[6, n] (x, y, z, vx,
+vy, vz after the last step); the system's positions are the start.
 Two cases use the reference's shipped inputs (Examples/Water and the root example);
 the rest are seeded synthetic systems chosen to reach every model switch.
 
@@ -28,7 +33,7 @@ from mspms2_gb300.system import (ELEC_EWALD, ELEC_NONE, ELEC_SIMPLE_COULOMB, ELE
                                  GHOST_FULL, SF_ATOM_EXPLICIT, SF_HYPERGEO, SF_MY_INTERP, SF_TASOS,
                                  MyInterpGrid, Species, System, TasosGrid, read_reference_dir,
                                  system_to_arrays, tasos_dims, write_reference_dir)
-from oracle.pyoracle import reference_available, run_reference_dir  # noqa: E402
+from oracle.pyoracle import reference_available, run_reference_dir, run_reference_md  # noqa: E402
 
 REF = os.environ.get("MSPMS2_REF", "/root/reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -221,10 +226,52 @@ def cases():
     return out
 
 
+def md_cases():
+    """Trajectories of the reference's own integrators (harness md mode): case -> (system, nsteps)."""
+    out = {}
+    w = configs.water_box(6, 18.6, 11, ELEC_WOLF, 0.2, 9.0, name="md_water_nvt", site_jitter=0.04)
+    w.delt_fs, w.nstep_inner, w.what_ensemble = 0.5, 2, 1
+    out["md_water_nvt_216"] = (w, 10)
+    lj = configs.lj_replica(500, seed=30)
+    lj.treq_K, lj.delt_fs, lj.nstep_inner, lj.what_ensemble = 1.0, 0.005 * 851.0, 1, 0
+    lj.name = "md_lj_nve"
+    out["md_lj_nve_500"] = (lj, 10)
+    e = configs.water_small(8, 24.8, seed=13, charge_type=ELEC_EWALD, kappa=0.3, rc=10.0, kmax=7, ksqmax=49)
+    e.delt_fs, e.nstep_inner, e.what_ensemble = 2.0, 4, 1
+    e.nh_qq, e.nh_qqs = 5000.0, 2000.0
+    e.name = "md_water_ewald_respa"
+    out["md_water_ewald_respa_512"] = (e, 5)
+    return out
+
+
+def gen_md(only):
+    for name, (system, nsteps) in md_cases().items():
+        if only and name not in only:
+            continue
+        with tempfile.TemporaryDirectory() as td:
+            write_reference_dir(system, td)
+            parsed = read_reference_dir(td)
+            r = run_reference_md(td, nsteps)
+        parsed.x, parsed.y, parsed.z = (r["start"][k].copy() for k in range(3))
+        arrays = system_to_arrays(parsed)
+        md = r["md"]
+        arrays["md_int"] = np.array([md["scheme"], md["nstep_inner"], md["nfree"], r["nsteps"]])
+        arrays["md_real"] = np.array([md["delt"], md["treq"], md["qq"], md["qqs"], md["gg"], md["ggs"]])
+        arrays["md_state0"] = np.array([r["state"][k] for k in ("ps", "ss", "pss", "sss")])
+        arrays["md_v0"] = r["start"][3:]
+        arrays["md_log"] = r["log"]
+        arrays["md_end"] = r["end"]
+        fn = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(fn, **arrays)
+        print(f"{name}: natom={parsed.natom} steps={nsteps} tinst {r['log'][0, 8]:.6g} -> {r['log'][-1, 8]:.6g} "
+              f"-> {os.path.getsize(fn)} bytes")
+
+
 def main():
     if not reference_available():
         sys.exit("oracle/_ref/mspms_ref_force missing: run `sh oracle/build_ref.sh` first")
     only = set(sys.argv[1:])
+    gen_md(only)
     for name, (kind, obj) in cases().items():
         if only and name not in only:
             continue
