@@ -14,8 +14,9 @@ value   inputs resident in HBM (mg_compute_device); L2 (129 MB) flushed by a 256
         engine launches on.
 e2e     the same through mg_compute with pinned host buffers: positions copied in and
         forces copied out inside the timed region.
-Also reported: the plain-FP64 GPU path on the same workload, ns/day of the RESPA split
-(inner: bonded + pairs < 7 A, four 0.5 fs steps; outer: 7-10 A shell + reciprocal, 2 fs),
+Also reported: the plain-FP64 GPU path on the same workload; ns/day of the device-resident
+Nose-Hoover RESPA integrator (mg_md_run; inner: bonded + pairs < 7 A, four 0.5 fs steps;
+outer: 7-10 A shell + reciprocal, 2 fs) and the energy drift of an NVE run;
 the roofline of the dominant kernel and a bounded CPU baseline of the reference
 algorithm (the oracle port, single thread, extrapolated from a sampled window).
 """
@@ -208,6 +209,53 @@ def run_reference(args, rank):
     return 0
 
 
+def md_extras(system, split_r, precision, device, steps=10, drift_steps=20):
+    """ns/day of mg_md_run (NVT, vver_nh_3) and the energy drift of an NVE run (vver) on the
+    workload, from seeded Maxwell-Boltzmann velocities at 298 K with zero momentum."""
+    from mspms2_gb300.engine import Engine
+    from mspms2_gb300.system import md_params
+    s = system
+    s.respa_split = split_r
+    s.delt_fs, s.nstep_inner, s.treq_K = 2.0, 4, 298.0
+    md = md_params(s)
+    m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
+    v -= (v * m).sum(1, keepdims=True) / m.sum()
+    out = {}
+    with Engine(s, precision=precision, skin=1.0, device=device) as eng:
+        md["scheme"] = 1
+        pos, vel, st, _ = eng.md_run(2, md, v)  # warm-up: list, tables, solver
+        t0 = time.perf_counter()
+        pos, vel, st, log = eng.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2],
+                                       state={k: st[k] for k in ("ps", "ss", "pss", "sss")})
+        dt_wall = time.perf_counter() - t0
+        out["scheme"] = "NVT Nose-Hoover RESPA (vver_nh_3), 4 x 0.5 fs inner + 2 fs outer"
+        out["split_A"] = split_r
+        out["steps"] = steps
+        out["ms_per_outer_step"] = dt_wall / steps * 1e3
+        out["ns_per_day"] = steps * 2.0e-6 / dt_wall * 86400.0
+        out["tinst_K"] = [float(log[0, 8]), float(log[-1, 8])]
+        md["scheme"] = 0
+        start = (pos.copy(), vel.copy())
+        _, _, _, log = eng.md_run(drift_steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
+    with Engine(s, precision="fp64", skin=1.0, device=device) as e64:
+        _, _, _, log64 = e64.md_run(drift_steps, md, start[1], x=start[0][0], y=start[0][1], z=start[0][2])
+    s.respa_split = 0.0
+
+    def drift(lg):
+        h = lg[:, 0] + lg[:, 1] + lg[:, 2]  # ukin + uinter + uintra (K)
+        slope = float(np.polyfit(np.arange(len(h)) * 2.0, h, 1)[0])  # K per fs
+        return slope * 1e6 / (md["treq"] * s.natom)
+    out["nve_drift_kT_per_ns_per_atom"] = drift(log)
+    out["nve_drift_fp64_path"] = drift(log64)
+    out["nve_steps"] = drift_steps
+    out["note"] = ("device-resident: positions, velocities and thermostat scalars stay in HBM; timed with the "
+                   "wall clock around mg_md_run (host copies of the start and end included); drift from a "
+                   "linear fit of ukin + uinter + uintra over the NVE run")
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mspms2_gb300 import build
@@ -318,44 +366,11 @@ def run_ours(args, rank, world, local_rank):
         ms64 = statistics.mean(t64)
         extras["fp64_path"] = {"value": npairs / (ms64 * 1e-3), "ms_per_step": ms64,
                                "mixed_over_fp64": ms64 / ms_step, "rms_rel_force_err_mixed_vs_fp64": err}
-        # RESPA distance split: 4 inner (0.5 fs) + 1 outer (2 fs) per outer step
+        # device-resident NVT Nose-Hoover RESPA (mg_md_run, the reference's vver_nh_3):
+        # inner steps of 0.5 fs with bonded + pairs inside 7 A, outer 2 fs step with the
+        # 7-10 A shell and reciprocal space; Verlet skin 1 A
         if split_r > 0:
-            system.respa_split = split_r
-            engs = Engine(system, precision=args.precision, skin=1.0, device=local_rank)
-            system.respa_split = 0.0
-            engs.set_stream(stream.cuda_stream)
-            engs.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
-            engs.set_timing(True)
-            engs.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_LONG)
-            engs.set_timing(False)
-
-            def timed(fn, reps):
-                ts = []
-                for _ in range(reps):
-                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    a.record(stream)
-                    fn()
-                    b.record(stream)
-                    b.synchronize()
-                    ts.append(a.elapsed_time(b))
-                return statistics.mean(ts)
-
-            t_in = timed(lambda: engs.compute_device(*ptrs, None, fs.data_ptr(), TERMS_SHORT), 8)
-            t_out = timed(lambda: engs.compute_device(*ptrs, fl.data_ptr(), None, TERMS_LONG), 4)
-            system.respa_split = split_r
-            eb = Engine(system, precision=args.precision, device=local_rank)
-            system.respa_split = 0.0
-            eb.set_stream(stream.cuda_stream)
-            eb.set_timing(True)
-            eb.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_LONG)
-            t_build = eb.stats()["kernel_ms"][0]
-            eb.close()
-            outer_ms = 4 * t_in + t_out + t_build / 10.0
-            extras["respa"] = {"inner_ms": t_in, "outer_ms": t_out, "list_build_ms": t_build,
-                               "outer_step_ms": outer_ms, "ns_per_day": 2e-6 / (outer_ms * 1e-3) * 86400,
-                               "note": "split 7 A, 4 x 0.5 fs inner + 2 fs outer, skin 1 A, list rebuilt "
-                                       "every 10 outer steps"}
-            engs.close()
+            extras["respa"] = md_extras(system, split_r, args.precision, local_rank)
         cpu = cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
         extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
                                   "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],

@@ -59,8 +59,9 @@ enum {
 
 /* Precision of the pair/k-space/solid-fluid arithmetic. */
 enum {
-    MG_PREC_MIXED = 0,  /* FP32 pair math, FP64 per-atom force/energy accumulation,
-                           FP64 structure-factor accumulation */
+    MG_PREC_MIXED = 0,  /* FP32 pair, k-space and solid-fluid arithmetic; per-site forces and
+                           energies carried as exact FP32 hi+lo pairs or FP64; structure
+                           factors summed in FP32 per 512-site block, in FP64 across blocks */
     MG_PREC_FP64 = 1    /* every step in FP64 (the plain-FP64 GPU path) */
 };
 
@@ -279,7 +280,8 @@ typedef struct mg_md_state {
 } mg_md_state;
 
 /* Values recorded per step by mg_md_run, in this order: ukin, uinter, uintra, ushift,
- * ps, ss, pss, sss, tinst, unhts, unhtss, (unused). */
+ * ps, ss, pss, sss, tinst, unhts, unhtss, (unused). With a distance split
+ * (mg_params.respa_split > 0) uinter and ushift are the sums of both buckets. */
 #define MG_MD_LOG 12
 
 /* Runs nsteps steps of the scheme on the device, like the reference's main loop does with

@@ -393,14 +393,16 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
     mg_energies e;
     mg_status st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_ALL, fl, fs, &e);
     if (st) return st;
-    double uinter = e.uinter, uintra = e.uintra, ushift = e.ushift;
+    // with a distance split the short call also returns the inner pairs' share of
+    // uinter and ushift; the record holds the sum of both buckets
+    double uinter_l = e.uinter, uinter_s = 0.0, ushift_l = e.ushift, ushift_s = 0.0, uintra = e.uintra;
     // step 0 record: kinetic energy of the given velocities
     k_nh_start<<<nb, MD_TPB, 0, s>>>(A);
     k_md_ukin_scalar<<<1, MD_TPB, 0, s>>>(A, nb);
     k_md_step_scalars<<<1, 1, 0, s>>>(A.s, nb, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 0, dlog);
-    hlog[1] = uinter;
+    hlog[1] = uinter_l;
     hlog[2] = uintra;
-    hlog[3] = ushift;
+    hlog[3] = ushift_l;
     for (int step = 1; step <= nsteps; step++) {
         k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fl, h, nh ? 1 : 0, 0);
         for (int ll = 0; ll < mp->nstep_inner; ll++) {
@@ -409,6 +411,8 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
             MG_CUDA(cudaGetLastError());
             if ((st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_SHORT, fl, fs, &e))) return st;
             uintra = e.uintra;
+            uinter_s = e.uinter;
+            ushift_s = e.ushift;
             if (nh) {
                 if ((st = nh_solve(R, fs, hs, dts, mp->qqs, ggs_treq, 1))) return st;
             } else {
@@ -418,8 +422,8 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
         if (nh) k_md_outer_predict<<<1, 1, 0, s>>>(A.s, gg_treq, dt, dt_sqby2, h, mp->qq);
         MG_CUDA(cudaGetLastError());
         if ((st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_LONG, fl, fs, &e))) return st;
-        uinter = e.uinter;
-        ushift = e.ushift;
+        uinter_l = e.uinter;
+        ushift_l = e.ushift;
         double *row = dlog + (size_t)step * MG_MD_LOG;
         if (nh) {
             if ((st = nh_solve(R, fl, h, dt, mp->qq, gg_treq, 0))) return st;
@@ -430,9 +434,9 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
             k_md_step_scalars<<<1, 1, 0, s>>>(A.s, nb, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 0, row);
         }
         MG_CUDA(cudaGetLastError());
-        hlog[(size_t)step * MG_MD_LOG + 1] = uinter;
+        hlog[(size_t)step * MG_MD_LOG + 1] = uinter_l + uinter_s;
         hlog[(size_t)step * MG_MD_LOG + 2] = uintra;
-        hlog[(size_t)step * MG_MD_LOG + 3] = ushift;
+        hlog[(size_t)step * MG_MD_LOG + 3] = ushift_l + ushift_s;
     }
     MG_CUDA(cudaMemcpyAsync(x, dx, nb1, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaMemcpyAsync(y, dy, nb1, cudaMemcpyDeviceToHost, s));
