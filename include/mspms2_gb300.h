@@ -294,6 +294,34 @@ typedef struct mg_md_state {
 MG_API mg_status mg_md_run(mg_ctx *ctx, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
                            double *vx, double *vy, double *vz, mg_md_state *state, double *log);
 
+/* ---- solid-fluid potential grids (tools/sfgridgen.c:71-354) ----------------- */
+/* One unit cell of a solid, periodic in z only, and the solid-fluid Lennard-Jones
+ * parameters (Lorentz-Berthelot mixing), in A and K. */
+typedef struct mg_sfgrid_spec {
+    int nsolid;                       /* solid atoms in the cell (at most 2048) */
+    const double *sx, *sy, *sz;       /* their positions, A */
+    double uclx, ucly, uclz;          /* cell lengths, A */
+    double f_sigma, f_epsilon;        /* fluid site sigma (A), epsilon (K) */
+    double s_sigma, s_epsilon;        /* solid atom sigma (A), epsilon (K) */
+    double rcuton, rcutoff;           /* A */
+    int lj_switch;                    /* energy switch between rcuton and rcutoff */
+} mg_sfgrid_spec;
+
+/* The grids tools/sfgridgen.c writes (the my-interp model's input): nodes x = i*itvl,
+ * i < dims[0] = floor(uclx/itvl)+2 (likewise y, z), index i*dims[1]*dims[2] +
+ * j*dims[2] + k. out = 13 arrays of dims[0]*dims[1]*dims[2] doubles: energy (J/mol),
+ * dE/dx, dE/dy, dE/dz (J/mol/A), then the derivatives of the force -dE: xx xy xz yx yy
+ * yz zx zy zz. out == NULL only returns dims. precision: MG_PREC_*. Allocates device
+ * memory for the call. */
+MG_API mg_status mg_sfgrid_sfgridgen(int device, const mg_sfgrid_spec *spec, double itvl, int precision,
+                                     int *dims, double *out);
+/* A Tasos table (mylibtasos/grid.f90:81-93) of nx*ny*nz nodes at (i*hx, j*hy, k*hz):
+ * values[((k*ny + j)*nx + i)*8 + q] = F, Dx, Dy, Dz, Dxy, Dxz, Dyz, Dxyz for q = 0..7
+ * (K, K/A, K/A^2, K/A^3), ready for mg_sf_tasos_set_grid. No reference counterpart: the
+ * reference reads these tables from files made by a generator it does not include. */
+MG_API mg_status mg_sfgrid_tasos(int device, const mg_sfgrid_spec *spec, int nx, int ny, int nz, double hx,
+                                 double hy, double hz, int precision, double *values);
+
 /* ---- reciprocal space without device allocation ---------------------------- */
 /* No counterpart in the reference: an extra entry point of this library.
  *

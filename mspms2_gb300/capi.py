@@ -78,6 +78,13 @@ class MgMdParams(C.Structure):
         return cls(**{k: d[k] for k, _ in cls._fields_})
 
 
+class MgSfgridSpec(C.Structure):
+    _fields_ = [("nsolid", C.c_int), ("sx", _dp), ("sy", _dp), ("sz", _dp), ("uclx", C.c_double),
+                ("ucly", C.c_double), ("uclz", C.c_double), ("f_sigma", C.c_double), ("f_epsilon", C.c_double),
+                ("s_sigma", C.c_double), ("s_epsilon", C.c_double), ("rcuton", C.c_double),
+                ("rcutoff", C.c_double), ("lj_switch", C.c_int)]
+
+
 MD_STATE_NAMES = ["ps", "ss", "pss", "sss", "ukin", "tinst", "unhts", "unhtss"]
 MD_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "ps", "ss", "pss", "sss", "tinst", "unhts", "unhtss"]
 MD_LOG = 12

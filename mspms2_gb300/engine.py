@@ -71,6 +71,8 @@ def load_library(path: str = LIB_PATH):
     lib.mg_abi_version.restype = I
     lib.mg_md_run.argtypes = [V, C.POINTER(capi.MgMdParams), I, _dp, _dp, _dp, _dp, _dp, _dp,
                               C.POINTER(capi.MgMdState), _dp]
+    lib.mg_sfgrid_sfgridgen.argtypes = [I, C.POINTER(capi.MgSfgridSpec), D, I, C.POINTER(I), _dp]
+    lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     _lib = lib
     return lib
 
@@ -236,6 +238,43 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+def _sfgrid_spec(spec: dict):
+    atoms = np.ascontiguousarray(np.asarray(spec["atoms"], dtype=np.float64).T)
+    m = capi.MgSfgridSpec(nsolid=atoms.shape[1], sx=_p(atoms[0]), sy=_p(atoms[1]), sz=_p(atoms[2]),
+                          uclx=spec["ucl"][0], ucly=spec["ucl"][1], uclz=spec["ucl"][2], f_sigma=spec["f_sigma"],
+                          f_epsilon=spec["f_epsilon"], s_sigma=spec["s_sigma"], s_epsilon=spec["s_epsilon"],
+                          rcuton=spec["rcuton"], rcutoff=spec["rcutoff"], lj_switch=int(spec["lj_switch"]))
+    return m, atoms
+
+
+def sfgrid_sfgridgen(spec: dict, itvl: float, precision: str = "fp64", device: int = 0):
+    """The grids of the reference's tools/sfgridgen.c, computed on the GPU
+    (mg_sfgrid_sfgridgen): returns (dims, out[13, N])."""
+    lib = load_library()
+    m, keep = _sfgrid_spec(spec)
+    dims = (C.c_int * 3)()
+    st = lib.mg_sfgrid_sfgridgen(device, C.byref(m), itvl, PREC[precision], dims, None)
+    if st != MG_OK:
+        raise EngineError(st, "mg_sfgrid_sfgridgen")
+    out = np.zeros((13, dims[0] * dims[1] * dims[2]))
+    st = lib.mg_sfgrid_sfgridgen(device, C.byref(m), itvl, PREC[precision], dims, _p(out))
+    if st != MG_OK:
+        raise EngineError(st, "mg_sfgrid_sfgridgen")
+    return tuple(dims), out
+
+
+def sfgrid_tasos(spec: dict, nx: int, ny: int, nz: int, h, precision: str = "fp64", device: int = 0):
+    """A Tasos table (F, Dx, Dy, Dz, Dxy, Dxz, Dyz, Dxyz per node, K and A) computed on the
+    GPU (mg_sfgrid_tasos): returns values[nz, ny, nx, 8]."""
+    lib = load_library()
+    m, keep = _sfgrid_spec(spec)
+    out = np.zeros((nz, ny, nx, 8))
+    st = lib.mg_sfgrid_tasos(device, C.byref(m), nx, ny, nz, h[0], h[1], h[2], PREC[precision], _p(out))
+    if st != MG_OK:
+        raise EngineError(st, "mg_sfgrid_tasos")
+    return out
 
 
 def derive(system: System) -> dict:

@@ -10,6 +10,7 @@
 #      molecule with itself for iMole >= 1 and returns NaN);
 #   2. src/molevars.h:6-13 - NATOM_MAX/NMOLE_MAX/NBOND_MAX/NANGLE_MAX raised so the
 #      benchmark systems fit.
+# Also built: tools/sfgridgen.c (the solid-fluid grid generator) as oracle/_ref/sfgridgen.
 # Left out: src/mspms2.c (its main() is replaced by oracle/ref_harness.c) and
 # src/dftmcff.c (needs GSL). The Fortran grid library mylibtasos/ cannot be compiled
 # here (no gfortran); oracle/ref_stubs.c supplies its four entry points on top of the
@@ -49,3 +50,8 @@ done
 $CC -o "$OUT/mspms_ref_force" $OBJS -lm
 rm -rf "$OUT/build"
 echo "built $OUT/mspms_ref_force"
+# the reference's solid-fluid grid generator, unchanged, read where it lies
+if [ -f "$REF/tools/sfgridgen.c" ]; then
+  $CC -O2 -ffp-contract=off -w -o "$OUT/sfgridgen" "$REF/tools/sfgridgen.c" -lm
+  echo "built $OUT/sfgridgen"
+fi

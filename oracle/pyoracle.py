@@ -222,6 +222,36 @@ def run_reference_md(path: str, nsteps: int) -> dict:
     return {"md": md, "state": state, "start": start, "log": log, "end": end, "nsteps": ns}
 
 
+SFGRIDGEN_BIN = os.path.join(HERE, "_ref", "sfgridgen")
+
+
+def run_reference_sfgridgen(spec: dict, itvl: float):
+    """Run the reference's tools/sfgridgen.c (built into oracle/_ref by build_ref.sh) on a
+    spec (fluid/solid sigma and epsilon, rcuton, rcutoff, lj_switch, cell, atoms [n, 3])
+    and return (dims, out[13, N]) as the tool writes them."""
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "grid.in")
+        def r(v):
+            return repr(float(v))
+        with open(inp, "w") as f:
+            f.write(f"F {r(spec['f_sigma'])} {r(spec['f_epsilon'])}\n")
+            f.write(f"{r(itvl)} {r(spec['rcuton'])} {r(spec['rcutoff'])} {int(spec['lj_switch'])}\n")
+            ucl = spec["ucl"]
+            f.write(f"{len(spec['atoms'])} {r(ucl[0])} {r(ucl[1])} {r(ucl[2])}\n")
+            f.write(f"{r(spec['s_sigma'])} {r(spec['s_epsilon'])}\n")
+            for a in spec["atoms"]:
+                f.write(f"C {r(a[0])} {r(a[1])} {r(a[2])}\n")
+        p = subprocess.run([SFGRIDGEN_BIN, inp], cwd=td, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"sfgridgen failed: {p.stderr[-2000:]}")
+        b = open(os.path.join(td, "out.sfgridgen"), "rb").read()
+    head = np.frombuffer(b[:48])
+    ints = np.frombuffer(b[48:64], np.int32)
+    ntot, dims = int(ints[0]), tuple(int(v) for v in ints[1:4])
+    out = np.frombuffer(b[88:88 + 13 * 8 * ntot]).reshape(13, ntot).copy()
+    return dims, out, head
+
+
 def reference_available() -> bool:
     return os.path.exists(REF_BIN) and os.access(REF_BIN, os.X_OK)
 

@@ -16,7 +16,8 @@ def pytest_configure(config):
 
 def golden_cases():
     """Force fixtures (frclong/frcshort outputs of the compiled reference)."""
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("md_"))
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith(("md_", "sfgrid_")))
 
 
 def md_golden_cases():

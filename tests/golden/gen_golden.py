@@ -11,7 +11,9 @@ The md_* cases hold trajectories of the reference's own integrators instead (vve
 vver, run by the harness's md mode): md_int (scheme, nstep_inner, nfree, nsteps), md_real
 (delt, treq, qq, qqs, gg, ggs), md_state0 (ps, ss, pss, sss), md_v0[3,n] start velocities
 (drawn by the reference's velinit), md_log[nsteps+1, 12] and md_end[6, n] (x, y, z, vx,
-vy, vz after the last step); the system's positions are the start.
+vy, vz after the last step); the system's positions are the start. The sfgrid_* cases
+hold grids of the reference's tools/sfgridgen.c (atoms, cell, LJ parameters, dims and its
+13 output arrays).
 Two cases use the reference's shipped inputs (Examples/Water and the root example);
 the rest are seeded synthetic systems chosen to reach every model switch.
 
@@ -33,7 +35,8 @@ from mspms2_gb300.system import (ELEC_EWALD, ELEC_NONE, ELEC_SIMPLE_COULOMB, ELE
                                  GHOST_FULL, SF_ATOM_EXPLICIT, SF_HYPERGEO, SF_MY_INTERP, SF_TASOS,
                                  MyInterpGrid, Species, System, TasosGrid, read_reference_dir,
                                  system_to_arrays, tasos_dims, write_reference_dir)
-from oracle.pyoracle import reference_available, run_reference_dir, run_reference_md  # noqa: E402
+from oracle.pyoracle import (reference_available, run_reference_dir, run_reference_md,  # noqa: E402
+                             run_reference_sfgridgen)
 
 REF = os.environ.get("MSPMS2_REF", "/root/reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -244,6 +247,39 @@ def md_cases():
     return out
 
 
+def read_sfgridgen_input(fn):
+    """The reference's sfgridgen input format (tools/sfgridgen.c:111-121)."""
+    lines = [ln.split() for ln in open(fn) if ln.strip()]
+    f_sigma, f_eps = float(lines[0][1]), float(lines[0][2])
+    itvl, ron, roff, sw = float(lines[1][0]), float(lines[1][1]), float(lines[1][2]), int(lines[1][3])
+    n, ux, uy, uz = int(lines[2][0]), float(lines[2][1]), float(lines[2][2]), float(lines[2][3])
+    s_sigma, s_eps = float(lines[3][0]), float(lines[3][1])
+    atoms = np.array([[float(v) for v in ln[1:4]] for ln in lines[4:4 + n]])
+    return dict(f_sigma=f_sigma, f_epsilon=f_eps, rcuton=ron, rcutoff=roff, lj_switch=sw, ucl=(ux, uy, uz),
+                s_sigma=s_sigma, s_epsilon=s_eps, atoms=atoms), itvl
+
+
+def gen_sfgrid(only):
+    """Grids of the reference's own generator on its shipped nanotube cells: the CH3 cell
+    as given (no switch) and the CH2 cell with the energy switch on (12-14 A)."""
+    cases = {}
+    spec, _ = read_sfgridgen_input(os.path.join(REF, "tools", "CH3-SWNT11x11.in"))
+    cases["sfgrid_ch3_swnt"] = (spec, 1.0)
+    spec2, _ = read_sfgridgen_input(os.path.join(REF, "tools", "CH2-SWNT11x11.in"))
+    spec2.update(rcuton=12.0, rcutoff=14.0, lj_switch=1)
+    cases["sfgrid_ch2_switch"] = (spec2, 1.0)
+    for name, (spec, itvl) in cases.items():
+        if only and name not in only:
+            continue
+        dims, out, head = run_reference_sfgridgen(spec, itvl)
+        fn = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(fn, atoms=spec["atoms"], ucl=np.array(spec["ucl"]),
+                            lj=np.array([spec["f_sigma"], spec["f_epsilon"], spec["s_sigma"], spec["s_epsilon"],
+                                         spec["rcuton"], spec["rcutoff"], spec["lj_switch"], itvl]),
+                            dims=np.array(dims), out=out)
+        print(f"{name}: dims={dims} -> {os.path.getsize(fn)} bytes")
+
+
 def gen_md(only):
     for name, (system, nsteps) in md_cases().items():
         if only and name not in only:
@@ -272,6 +308,7 @@ def main():
         sys.exit("oracle/_ref/mspms_ref_force missing: run `sh oracle/build_ref.sh` first")
     only = set(sys.argv[1:])
     gen_md(only)
+    gen_sfgrid(only)
     for name, (kind, obj) in cases().items():
         if only and name not in only:
             continue
