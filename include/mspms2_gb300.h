@@ -294,6 +294,36 @@ typedef struct mg_md_state {
 MG_API mg_status mg_md_run(mg_ctx *ctx, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
                            double *vx, double *vy, double *vz, mg_md_state *state, double *log);
 
+/* ---- batched Hybrid Monte Carlo (src/hmc.c:23-40, src/dispmd.c:12-103) ------- */
+/* Lennard-Jones replicas (one site type, cubic boxes, reduced units). */
+typedef struct mg_hmc_params {
+    double eps, sigma, rcutoff;  /* LJ parameters and cutoff (no switch) */
+    double mass;                 /* site mass */
+    double treq;                 /* temperature */
+    double delt;                 /* velocity-Verlet step */
+    int nstep_md;                /* steps per move (nstep_md_per_hmc) */
+    unsigned long long seed;     /* key of the Philox streams (include/mg_philox.h) */
+    int rescale;                 /* 1: rescale the drawn velocities to exactly treq, as the
+                                    reference's velinit does (src/initvars.c:210-218);
+                                    0: plain Maxwell-Boltzmann draws */
+    int nconstraint;             /* nfree = 3 natom - nconstraint, for the rescaling */
+} mg_hmc_params;
+
+/* nmoves canonical HMC moves of every replica, all in one launch: per move Maxwell-
+ * Boltzmann velocities with zero momentum (velinit, src/initvars.c:151-229), nstep_md
+ * velocity-Verlet steps (vver, src/md.c:22-85) and the reference's Metropolis test on
+ * dH = (dU + dK + dUshift)/T (src/dispmd.c:48-66). Replica r has natom[r] sites in a
+ * cubic box box[r] >= 2 rcutoff; x/y/z hold all replicas one after another (host,
+ * in/out). Random draws are keyed by (seed, replica, move0 + move, atom), so a run of
+ * k moves followed by one with move0 = k equals one run of 2k moves. Out: accepted[r]
+ * (moves accepted), energy[r] (potential energy plus shift energy of the final state),
+ * dh_log[r*nmoves + m] if not NULL. Pair forces FP32, energies FP64. A replica's
+ * positions and cell list must fit in shared memory (about 8000 sites); larger give
+ * MG_ERR_CAPACITY. Allocates device memory for the call. */
+MG_API mg_status mg_hmc_batch(int device, const mg_hmc_params *p, int nrep, const int *natom, const double *box,
+                              double *x, double *y, double *z, int nmoves, int move0, int *accepted,
+                              double *dh_log, double *energy);
+
 /* ---- solid-fluid potential grids (tools/sfgridgen.c:71-354) ----------------- */
 /* One unit cell of a solid, periodic in z only, and the solid-fluid Lennard-Jones
  * parameters (Lorentz-Berthelot mixing), in A and K. */

@@ -85,6 +85,12 @@ class MgSfgridSpec(C.Structure):
                 ("rcutoff", C.c_double), ("lj_switch", C.c_int)]
 
 
+class MgHmcParams(C.Structure):
+    _fields_ = [("eps", C.c_double), ("sigma", C.c_double), ("rcutoff", C.c_double), ("mass", C.c_double),
+                ("treq", C.c_double), ("delt", C.c_double), ("nstep_md", C.c_int), ("seed", C.c_ulonglong),
+                ("rescale", C.c_int), ("nconstraint", C.c_int)]
+
+
 MD_STATE_NAMES = ["ps", "ss", "pss", "sss", "ukin", "tinst", "unhts", "unhtss"]
 MD_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "ps", "ss", "pss", "sss", "tinst", "unhts", "unhtss"]
 MD_LOG = 12

@@ -1,0 +1,487 @@
+// mg_hmc.cu - batched Hybrid Monte Carlo of Lennard-Jones replicas in one persistent
+// launch: the reference's hmc() canonical move (src/hmc.c:23-40) with md_move()
+// (src/dispmd.c:12-103) over vver() steps (src/md.c:22-85), for many independent boxes.
+//
+// One thread block runs whole replicas, taking the next one (largest first) from a work
+// counter. Per move it
+//   1. draws Maxwell-Boltzmann velocities sqrt(T)/sqrt(m) N(0,1) per component from the
+//      counter-based generator of include/mg_philox.h, removes the total momentum and,
+//      like the reference (velinit, src/initvars.c:151-229), optionally rescales them
+//      to exactly T; K0 = sum m v^2 / 2;
+//   2. evaluates forces and energy U0 (frclong) and runs nstep velocity-Verlet steps
+//      (a half kick, then per step: drift, forces, a full kick, the last one a half kick);
+//   3. takes dH = (dU + dK + dUshift) / T, the reference's sum with its +dUshift
+//      (src/dispmd.c:48-50), and accepts when dH <= 0 or a uniform draw < exp(-dH),
+//      otherwise restores the positions.
+// FP64 positions and velocities live in global memory (L2-resident for the whole batch);
+// FP32 copies of the positions, wrapped into the box, and a cell list live in shared
+// memory. Pair forces are FP32; energies, kinetic energies and dH are FP64. Cells of at
+// least rcutoff with three or more per axis give a 27-cell scan; smaller boxes use all
+// pairs with the minimum image. Each cell's atoms are kept in index order, so every sum
+// has a fixed order and a run is reproducible.
+#include <math.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "../../include/mg_philox.h"
+#include "mg_internal.cuh"
+
+#define HMC_TPB 512
+
+namespace {
+
+struct HmcArgs {
+    int nrep;
+    const int *order, *natom, *offset;
+    const double *box;
+    double *x, *y, *z, *vx, *vy, *vz, *ox, *oy, *oz;
+    int *counter;
+    int nmoves, move0, nstep;
+    double eps, sig2, rc, rc2, shift_pair, mass, treq, dt;
+    int rescale, nconstraint;
+    uint32_t key0, key1;
+    int *accepted;
+    double *dh_log, *energy;
+    int nmax, ncmax;
+};
+
+// fixed-order block sum of three doubles (thread 0 gets the result)
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &c) {
+    __shared__ double red[3][HMC_TPB];
+    red[0][threadIdx.x] = a;
+    red[1][threadIdx.x] = b;
+    red[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = HMC_TPB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+            red[2][threadIdx.x] += red[2][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    a = red[0][0];
+    b = red[1][0];
+    c = red[2][0];
+    __syncthreads();
+}
+
+struct Smem {
+    float4 *pos;  // [nmax] wrapped FP32 positions; w = cell index
+    int *list;    // [nmax] atoms by cell, index order within a cell
+    int *start;   // [ncmax + 1]
+    int *cnt;     // [ncmax]
+};
+
+__device__ __forceinline__ int cell_of(float v, float inv_w, int nc) {
+    int c = (int)(v * inv_w);
+    return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+// wrapped FP32 positions (and cells) of the replica into shared memory, then the list
+__device__ __forceinline__ void load_positions(const HmcArgs &A, const Smem &S, int off, int n, double L, int nc) {
+    const float Lf = (float)L, inv_w = nc > 0 ? (float)(nc / L) : 0.f;
+    const int ncell = nc * nc * nc;
+    for (int c = threadIdx.x; c < ncell; c += HMC_TPB) S.cnt[c] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+        double w[3] = {A.x[off + i], A.y[off + i], A.z[off + i]};
+        float p[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            double t = w[d] - L * floor(w[d] / L);
+            float f = (float)t;
+            p[d] = f < Lf ? f : 0.f;
+        }
+        int cell = 0;
+        if (nc > 0) {
+            cell = (cell_of(p[2], inv_w, nc) * nc + cell_of(p[1], inv_w, nc)) * nc + cell_of(p[0], inv_w, nc);
+            atomicAdd(&S.cnt[cell], 1);
+        }
+        S.pos[i] = make_float4(p[0], p[1], p[2], __int_as_float(cell));
+    }
+    __syncthreads();
+    if (nc == 0) return;
+    // exclusive scan of the counts by warp 0 (lanes own consecutive chunks)
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x, chunk = (ncell + 31) / 32;
+        const int b = lane * chunk, e = min(ncell, b + chunk);
+        int sum = 0;
+        for (int c = b; c < e; c++) sum += S.cnt[c];
+        int incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int run = incl - sum;
+        for (int c = b; c < e; c++) {
+            S.start[c] = run;
+            run += S.cnt[c];
+            S.cnt[c] = 0;  // reused as the fill counter
+        }
+        if (lane == 31) S.start[ncell] = incl;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+        const int cell = __float_as_int(S.pos[i].w);
+        const int slot = atomicAdd(&S.cnt[cell], 1);
+        S.list[S.start[cell] + slot] = i;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncell; c += HMC_TPB) {  // index order inside each cell
+        const int b = S.start[c], e = S.start[c + 1];
+        for (int k = b + 1; k < e; k++) {
+            const int v = S.list[k];
+            int m = k - 1;
+            while (m >= b && S.list[m] > v) {
+                S.list[m + 1] = S.list[m];
+                m--;
+            }
+            S.list[m + 1] = v;
+        }
+    }
+    __syncthreads();
+}
+
+// LJ force on atom i (FP32) and its pair energy / pair count (each pair seen twice)
+__device__ __forceinline__ void lj_add(float3 d, float sig2, float eps, float rc2, float &fx, float &fy, float &fz,
+                                       float &e, int &np) {
+    const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+    if (!(r2 < rc2)) return;
+    const float s2 = sig2 / r2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+    e += 4.f * eps * (s12 - s6);
+    const float f = 24.f * eps * (2.f * s12 - s6) / r2;
+    fx += f * d.x;
+    fy += f * d.y;
+    fz += f * d.z;
+    np += 1;
+}
+
+__device__ __forceinline__ void atom_force(const HmcArgs &A, const Smem &S, int i, int n, double L, int nc, float &fx, float &fy,
+                           float &fz, float &e, int &np) {
+    const float4 pi = S.pos[i];
+    const float Lf = (float)L, sig2 = (float)A.sig2, eps = (float)A.eps, rc2 = (float)A.rc2;
+    fx = fy = fz = e = 0.f;
+    np = 0;
+    if (nc == 0) {  // all pairs, minimum image
+        const float iL = 1.f / Lf;
+        for (int j = 0; j < n; j++) {
+            if (j == i) continue;
+            const float4 pj = S.pos[j];
+            float3 d = make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
+            d.x -= Lf * rintf(d.x * iL);
+            d.y -= Lf * rintf(d.y * iL);
+            d.z -= Lf * rintf(d.z * iL);
+            lj_add(d, sig2, eps, rc2, fx, fy, fz, e, np);
+        }
+        return;
+    }
+    const int ci = __float_as_int(pi.w);
+    const int cx = ci % nc, cy = (ci / nc) % nc, cz = ci / (nc * nc);
+    for (int dz = -1; dz <= 1; dz++) {
+        int uz = cz + dz;
+        const float sz = uz < 0 ? -Lf : (uz >= nc ? Lf : 0.f);
+        uz = (uz + nc) % nc;
+        for (int dy = -1; dy <= 1; dy++) {
+            int uy = cy + dy;
+            const float sy = uy < 0 ? -Lf : (uy >= nc ? Lf : 0.f);
+            uy = (uy + nc) % nc;
+            for (int dx = -1; dx <= 1; dx++) {
+                int ux = cx + dx;
+                const float sx = ux < 0 ? -Lf : (ux >= nc ? Lf : 0.f);
+                ux = (ux + nc) % nc;
+                const int c = (uz * nc + uy) * nc + ux;
+                for (int k = S.start[c]; k < S.start[c + 1]; k++) {
+                    const int j = S.list[k];
+                    if (j == i) continue;
+                    const float4 pj = S.pos[j];
+                    const float3 d = make_float3(pi.x - (pj.x + sx), pi.y - (pj.y + sy), pi.z - (pj.z + sz));
+                    lj_add(d, sig2, eps, rc2, fx, fy, fz, e, np);
+                }
+            }
+        }
+    }
+}
+
+// forces at the shared-memory positions, v += f h / m; optional energy (U, pair count)
+__device__ __forceinline__ void force_kick(const HmcArgs &A, const Smem &S, int off, int n, double L, int nc, double h,
+                           double *u_out, double *np_out) {
+    double esum = 0.0, nsum = 0.0, unused = 0.0;
+    const double hm = h / A.mass;
+    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+        float fx, fy, fz, e;
+        int np;
+        atom_force(A, S, i, n, L, nc, fx, fy, fz, e, np);
+        A.vx[off + i] += hm * (double)fx;
+        A.vy[off + i] += hm * (double)fy;
+        A.vz[off + i] += hm * (double)fz;
+        esum += (double)e;
+        nsum += (double)np;
+    }
+    if (u_out) {
+        block_sum3(esum, nsum, unused);
+        *u_out = 0.5 * esum;
+        *np_out = 0.5 * nsum;
+    }
+}
+
+__global__ void __launch_bounds__(HMC_TPB, 1) k_hmc(HmcArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem S;
+    S.pos = (float4 *)smem_raw;
+    S.list = (int *)(S.pos + A.nmax);
+    S.start = S.list + A.nmax;
+    S.cnt = S.start + A.ncmax + 1;
+    __shared__ int s_rep;
+    const uint32_t key[2] = {A.key0, A.key1};
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_rep = atomicAdd(A.counter, 1);
+        __syncthreads();
+        const int k = s_rep;
+        if (k >= A.nrep) break;
+        const int r = A.order[k], n = A.natom[r], off = A.offset[r];
+        const double L = A.box[r];
+        int nc = (int)floor(L / A.rc);
+        if (nc < 3) nc = 0;
+        int acc = 0;
+        double u_cur = 0.0;
+        for (int m = 0; m < A.nmoves; m++) {
+            const uint32_t mv = (uint32_t)(A.move0 + m);
+            // 1. velocities (velinit) and the saved positions
+            const double sd = sqrt(A.treq) / sqrt(A.mass);
+            double px = 0, py = 0, pz = 0;
+            for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                const uint32_t c0[4] = {(uint32_t)i, mv, 0u, (uint32_t)r}, c1[4] = {(uint32_t)i, mv, 1u, (uint32_t)r};
+                uint32_t w0[4], w1[4];
+                mg_philox4x32_10(c0, key, w0);
+                mg_philox4x32_10(c1, key, w1);
+                double g0, g1, g2, g3;
+                mg_gauss2(w0, &g0, &g1);
+                mg_gauss2(w1, &g2, &g3);
+                const double v0 = sd * g0, v1 = sd * g1, v2 = sd * g2;
+                A.vx[off + i] = v0;
+                A.vy[off + i] = v1;
+                A.vz[off + i] = v2;
+                px += v0 * A.mass;
+                py += v1 * A.mass;
+                pz += v2 * A.mass;
+                A.ox[off + i] = A.x[off + i];
+                A.oy[off + i] = A.y[off + i];
+                A.oz[off + i] = A.z[off + i];
+            }
+            block_sum3(px, py, pz);
+            const double sysm = A.mass * n;
+            px /= sysm;
+            py /= sysm;
+            pz /= sysm;
+            double k0 = 0, d0 = 0, d1 = 0;
+            for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                const double v0 = A.vx[off + i] - px, v1 = A.vy[off + i] - py, v2 = A.vz[off + i] - pz;
+                A.vx[off + i] = v0;
+                A.vy[off + i] = v1;
+                A.vz[off + i] = v2;
+                k0 += A.mass * (v0 * v0 + v1 * v1 + v2 * v2);
+            }
+            block_sum3(k0, d0, d1);
+            k0 *= 0.5;
+            if (A.rescale) {  // to exactly treq (src/initvars.c:208-227)
+                const double tinst = 2.0 * k0 / (3.0 * n - A.nconstraint);
+                const double scaling = sqrt(A.treq / tinst);
+                k0 = d0 = d1 = 0;
+                for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                    const double v0 = A.vx[off + i] * scaling, v1 = A.vy[off + i] * scaling;
+                    const double v2 = A.vz[off + i] * scaling;
+                    A.vx[off + i] = v0;
+                    A.vy[off + i] = v1;
+                    A.vz[off + i] = v2;
+                    k0 += A.mass * (v0 * v0 + v1 * v1 + v2 * v2);
+                }
+                block_sum3(k0, d0, d1);
+                k0 *= 0.5;
+            }
+            // 2. trajectory
+            double u0, n0, u1 = 0, n1 = 0;
+            load_positions(A, S, off, n, L, nc);
+            force_kick(A, S, off, n, L, nc, 0.5 * A.dt, &u0, &n0);
+            for (int s = 1; s <= A.nstep; s++) {
+                __syncthreads();
+                for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                    A.x[off + i] += A.dt * A.vx[off + i];
+                    A.y[off + i] += A.dt * A.vy[off + i];
+                    A.z[off + i] += A.dt * A.vz[off + i];
+                }
+                __syncthreads();
+                load_positions(A, S, off, n, L, nc);
+                const bool last = s == A.nstep;
+                force_kick(A, S, off, n, L, nc, last ? 0.5 * A.dt : A.dt, last ? &u1 : nullptr, last ? &n1 : nullptr);
+            }
+            __syncthreads();
+            double k1 = 0, e0 = 0, e1 = 0;
+            for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                const double v0 = A.vx[off + i], v1 = A.vy[off + i], v2 = A.vz[off + i];
+                k1 += A.mass * (v0 * v0 + v1 * v1 + v2 * v2);
+            }
+            block_sum3(k1, e0, e1);
+            k1 *= 0.5;
+            // 3. Metropolis test on the reference's energy difference
+            const double dh = ((u1 - u0) + (k1 - k0) + A.shift_pair * (n1 - n0)) / A.treq;
+            const uint32_t ca[4] = {0u, mv, 2u, (uint32_t)r};
+            uint32_t wa[4];
+            mg_philox4x32_10(ca, key, wa);
+            const double ua = mg_u01(wa[0], wa[1]);
+            const bool accept = dh <= 0.0 || ua < exp(-dh);
+            if (!accept) {
+                for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                    A.x[off + i] = A.ox[off + i];
+                    A.y[off + i] = A.oy[off + i];
+                    A.z[off + i] = A.oz[off + i];
+                }
+            }
+            acc += accept ? 1 : 0;
+            u_cur = accept ? u1 + A.shift_pair * n1 : u0 + A.shift_pair * n0;
+            if (threadIdx.x == 0 && A.dh_log) A.dh_log[(size_t)r * A.nmoves + m] = dh;
+        }
+        if (threadIdx.x == 0) {
+            A.accepted[r] = acc;
+            A.energy[r] = u_cur;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" mg_status mg_hmc_batch(int device, const mg_hmc_params *p, int nrep, const int *natom, const double *box,
+                                  double *x, double *y, double *z, int nmoves, int move0, int *accepted,
+                                  double *dh_log, double *energy) {
+    if (!p || nrep <= 0 || nmoves < 0 || move0 < 0 || !natom || !box || !x || !y || !z || !accepted || !energy)
+        return MG_ERR_INVALID;
+    if (!(p->eps >= 0) || !(p->sigma > 0) || !(p->rcutoff > 0) || !(p->mass > 0) || !(p->treq > 0) ||
+        !(p->delt > 0) || p->nstep_md < 1 || p->nconstraint < 0)
+        return MG_ERR_INVALID;
+    int nmax = 0, ncmax = 0;
+    long long total = 0;
+    for (int r = 0; r < nrep; r++) {
+        if (natom[r] < 2 || !(box[r] >= 2.0 * p->rcutoff)) return MG_ERR_INVALID;  // minimum image needs L >= 2 rc
+        nmax = std::max(nmax, natom[r]);
+        int nc = (int)floor(box[r] / p->rcutoff);
+        if (nc >= 3) ncmax = std::max(ncmax, nc * nc * nc);
+        total += natom[r];
+    }
+    const size_t smem = 16 * (size_t)nmax + 4 * (size_t)nmax + 4 * (2 * (size_t)ncmax + 1) + 16;
+    if (smem > 200 * 1024) return MG_ERR_CAPACITY;  // one replica's positions and cells stay on chip
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return MG_ERR_NO_DEVICE;
+    }
+    int major = 0, minor = 0, nsm = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    if (major != 10 || minor != 3) return MG_ERR_NO_DEVICE;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return MG_ERR_CUDA;
+    }
+    std::vector<int> offset(nrep), order(nrep);
+    long long o = 0;
+    for (int r = 0; r < nrep; r++) {
+        offset[r] = (int)o;
+        o += natom[r];
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return natom[a] > natom[b]; });
+    const size_t nb = sizeof(double) * (size_t)total;
+    std::vector<void *> bufs;
+    auto dalloc = [&](size_t bytes) -> void * {
+        void *q = nullptr;
+        if (cudaMalloc(&q, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        bufs.push_back(q);
+        return q;
+    };
+    mg_status st = MG_OK;
+    cudaStream_t s = nullptr;
+    double *d_state = (double *)dalloc(9 * nb);
+    int *d_int = (int *)dalloc(sizeof(int) * (3 * (size_t)nrep + 2 * (size_t)nrep + 1));
+    double *d_box = (double *)dalloc(sizeof(double) * nrep);
+    double *d_dh = (double *)dalloc(sizeof(double) * (size_t)nrep * std::max(nmoves, 1));
+    double *d_energy = (double *)dalloc(sizeof(double) * nrep);
+    if (!d_state || !d_int || !d_box || !d_dh || !d_energy || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) {
+        st = MG_ERR_ALLOC;
+    } else {
+        HmcArgs A;
+        A.nrep = nrep;
+        int *d_order = d_int, *d_natom = d_int + nrep, *d_offset = d_int + 2 * nrep, *d_acc = d_int + 3 * nrep;
+        A.counter = d_int + 5 * nrep;
+        A.order = d_order;
+        A.natom = d_natom;
+        A.offset = d_offset;
+        A.box = d_box;
+        A.x = d_state;
+        A.y = A.x + total;
+        A.z = A.y + total;
+        A.vx = A.z + total;
+        A.vy = A.vx + total;
+        A.vz = A.vy + total;
+        A.ox = A.vz + total;
+        A.oy = A.ox + total;
+        A.oz = A.oy + total;
+        A.nmoves = nmoves;
+        A.move0 = move0;
+        A.nstep = p->nstep_md;
+        A.eps = p->eps;
+        A.sig2 = p->sigma * p->sigma;
+        A.rc = p->rcutoff;
+        A.rc2 = p->rcutoff * p->rcutoff;
+        // shift energy of one pair inside the cutoff: eps sig^6 (sig^6 shift1 - 1) shift4,
+        // shift1 = (1/rcutoff)^6, shift4 = 4 shift1 (src/initvars.c:591-599, src/frclong.c)
+        const double shift1 = pow(1.0 / p->rcutoff, 6.0), sig6 = pow(p->sigma, 6.0);
+        A.shift_pair = p->eps * sig6 * (sig6 * shift1 - 1.0) * (4.0 * shift1);
+        A.mass = p->mass;
+        A.treq = p->treq;
+        A.dt = p->delt;
+        A.rescale = p->rescale;
+        A.nconstraint = p->nconstraint;
+        A.key0 = (uint32_t)(p->seed & 0xffffffffull);
+        A.key1 = (uint32_t)(p->seed >> 32);
+        A.accepted = d_acc;
+        A.dh_log = d_dh;
+        A.energy = d_energy;
+        A.nmax = nmax;
+        A.ncmax = ncmax;
+        cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_natom, natom, sizeof(int) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_offset, offset.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(A.counter, 0, sizeof(int), s);
+        cudaMemcpyAsync(d_box, box, sizeof(double) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(A.x, x, nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(A.y, y, nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(A.z, z, nb, cudaMemcpyHostToDevice, s);
+        if (cudaFuncSetAttribute(k_hmc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            st = MG_ERR_CUDA;
+        } else {
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hmc, HMC_TPB, smem);
+            const int blocks = std::max(1, std::min(nrep, nsm * std::max(per_sm, 1)));
+            k_hmc<<<blocks, HMC_TPB, smem, s>>>(A);
+            cudaMemcpyAsync(x, A.x, nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(y, A.y, nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(z, A.z, nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(accepted, d_acc, sizeof(int) * nrep, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(energy, d_energy, sizeof(double) * nrep, cudaMemcpyDeviceToHost, s);
+            if (dh_log && nmoves > 0)
+                cudaMemcpyAsync(dh_log, d_dh, sizeof(double) * (size_t)nrep * nmoves, cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) st = MG_ERR_CUDA;
+        }
+    }
+    cudaGetLastError();
+    for (void *q : bufs) cudaFree(q);
+    if (s) cudaStreamDestroy(s);
+    cudaSetDevice(prev);
+    return st;
+}

@@ -71,6 +71,8 @@ def load_library(path: str = LIB_PATH):
     lib.mg_abi_version.restype = I
     lib.mg_md_run.argtypes = [V, C.POINTER(capi.MgMdParams), I, _dp, _dp, _dp, _dp, _dp, _dp,
                               C.POINTER(capi.MgMdState), _dp]
+    lib.mg_hmc_batch.argtypes = [I, C.POINTER(capi.MgHmcParams), I, C.POINTER(I), _dp, _dp, _dp, _dp, I, I,
+                                 C.POINTER(I), _dp, _dp]
     lib.mg_sfgrid_sfgridgen.argtypes = [I, C.POINTER(capi.MgSfgridSpec), D, I, C.POINTER(I), _dp]
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     _lib = lib
@@ -275,6 +277,27 @@ def sfgrid_tasos(spec: dict, nx: int, ny: int, nz: int, h, precision: str = "fp6
     if st != MG_OK:
         raise EngineError(st, "mg_sfgrid_tasos")
     return out
+
+
+def hmc_batch(hp: dict, natom, box, x, y, z, nmoves: int, move0: int = 0, device: int = 0):
+    """nmoves canonical HMC moves of every Lennard-Jones replica in one launch
+    (mg_hmc_batch). natom[r], box[r] per replica; x/y/z hold all replicas one after
+    another and are returned updated. Returns (x, y, z, accepted[r], energy[r],
+    dh[r, nmoves])."""
+    lib = load_library()
+    natom = np.ascontiguousarray(natom, dtype=np.int32)
+    box = np.ascontiguousarray(box, dtype=np.float64)
+    x, y, z = (np.ascontiguousarray(v, dtype=np.float64).copy() for v in (x, y, z))
+    nrep = len(natom)
+    acc = np.zeros(nrep, np.int32)
+    energy = np.zeros(nrep)
+    dh = np.zeros((nrep, max(nmoves, 1)))
+    p = capi.MgHmcParams(**hp)
+    st = lib.mg_hmc_batch(device, C.byref(p), nrep, natom.ctypes.data_as(C.POINTER(C.c_int)), _p(box), _p(x), _p(y),
+                          _p(z), nmoves, move0, acc.ctypes.data_as(C.POINTER(C.c_int)), _p(dh), _p(energy))
+    if st != MG_OK:
+        raise EngineError(st, "mg_hmc_batch")
+    return x, y, z, acc, energy, dh[:, :nmoves]
 
 
 def derive(system: System) -> dict:

@@ -216,3 +216,110 @@ int orc_md_run(const orc_system *s, const mg_md_params *mp, int nsteps, double *
     free(buf);
     return 0;
 }
+
+/* ---- the canonical HMC move of one replica (src/hmc.c:23-40, src/dispmd.c:12-103) ------ */
+#include "../include/mg_philox.h"
+
+int orc_hmc_replica(const orc_system *s, const mg_hmc_params *hp, int replica, int move0, int nmoves, double *xx,
+                    double *yy, double *zz, int *accepted, double *dh_log, double *energy) {
+    const int n = orc_natom(s);
+    double *buf = (double *)calloc((size_t)n * 6, sizeof(double));
+    if (!buf) return -1;
+    double *vx = buf, *vy = buf + n, *vz = buf + 2 * n, *ox = buf + 3 * n, *oy = buf + 4 * n, *oz = buf + 5 * n;
+    const uint32_t key[2] = {(uint32_t)(hp->seed & 0xffffffffull), (uint32_t)(hp->seed >> 32)};
+    mg_md_params mp;
+    memset(&mp, 0, sizeof(mp));
+    mp.scheme = MG_MD_NVE;
+    mp.nstep_inner = 1;
+    mp.delt = hp->delt;
+    mp.treq = hp->treq;
+    mp.nfree = 3 * n - hp->nconstraint;
+    int acc = 0;
+    double e_cur = 0.0;
+    for (int m = 0; m < nmoves; m++) {
+        const uint32_t mv = (uint32_t)(move0 + m);
+        /* velinit (src/initvars.c:151-229) with the Philox streams */
+        const double stdv = sqrt(hp->treq) / sqrt(hp->mass);
+        double px = 0.0, py = 0.0, pz = 0.0, sysm = 0.0;
+        for (int i = 0; i < n; i++) {
+            const uint32_t c0[4] = {(uint32_t)i, mv, 0u, (uint32_t)replica}, c1[4] = {(uint32_t)i, mv, 1u, (uint32_t)replica};
+            uint32_t w0[4], w1[4];
+            double g0, g1, g2, g3;
+            mg_philox4x32_10(c0, key, w0);
+            mg_philox4x32_10(c1, key, w1);
+            mg_gauss2(w0, &g0, &g1);
+            mg_gauss2(w1, &g2, &g3);
+            vx[i] = stdv * g0;
+            vy[i] = stdv * g1;
+            vz[i] = stdv * g2;
+            px += vx[i] * hp->mass;
+            py += vy[i] * hp->mass;
+            pz += vz[i] * hp->mass;
+            sysm += hp->mass;
+            ox[i] = xx[i];
+            oy[i] = yy[i];
+            oz[i] = zz[i];
+        }
+        px /= sysm;
+        py /= sysm;
+        pz /= sysm;
+        double ukin = 0.0;
+        for (int i = 0; i < n; i++) {
+            vx[i] -= px;
+            vy[i] -= py;
+            vz[i] -= pz;
+            ukin += hp->mass * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        }
+        ukin = 0.5 * ukin;
+        if (hp->rescale) {
+            const double tinst = 2.0 * ukin / mp.nfree, scaling = sqrt(hp->treq / tinst);
+            ukin = 0.0;
+            for (int i = 0; i < n; i++) {
+                vx[i] *= scaling;
+                vy[i] *= scaling;
+                vz[i] *= scaling;
+                ukin += hp->mass * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+            }
+            ukin = 0.5 * ukin;
+        }
+        /* frclong + frcshort, then md_move over vver: orc_md_run evaluates the forces at
+         * the start and records U0 and U1 */
+        double log[2 * MG_MD_LOG];
+        mg_md_state st;
+        memset(&st, 0, sizeof(st));
+        double *lg = (double *)calloc((size_t)(hp->nstep_md + 1) * MG_MD_LOG, sizeof(double));
+        if (!lg) {
+            free(buf);
+            return -1;
+        }
+        orc_md_run(s, &mp, hp->nstep_md, xx, yy, zz, vx, vy, vz, &st, lg);
+        memcpy(log, lg, sizeof(double) * MG_MD_LOG);
+        memcpy(log + MG_MD_LOG, lg + (size_t)hp->nstep_md * MG_MD_LOG, sizeof(double) * MG_MD_LOG);
+        free(lg);
+        /* md_move's difference, with the reference's +d ushift (src/dispmd.c:48-50) */
+        const double du = (log[MG_MD_LOG + 1] - log[1]) + (log[MG_MD_LOG + 2] - log[2]) +
+                          (log[MG_MD_LOG + 0] - ukin) + (log[MG_MD_LOG + 3] - log[3]);
+        const double dh = du / hp->treq;
+        const uint32_t ca[4] = {0u, mv, 2u, (uint32_t)replica};
+        uint32_t wa[4];
+        mg_philox4x32_10(ca, key, wa);
+        const int accept = dh <= 0.0 || mg_u01(wa[0], wa[1]) < exp(-dh);
+        if (!accept) {
+            memcpy(xx, ox, sizeof(double) * n);
+            memcpy(yy, oy, sizeof(double) * n);
+            memcpy(zz, oz, sizeof(double) * n);
+        }
+        acc += accept;
+        e_cur = accept ? log[MG_MD_LOG + 1] + log[MG_MD_LOG + 3] : log[1] + log[3];
+        if (dh_log) dh_log[m] = dh;
+    }
+    *accepted = acc;
+    *energy = e_cur;
+    free(buf);
+    return 0;
+}
+
+/* the generator itself, for its known-answer test */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    mg_philox4x32_10(ctr, key, out);
+}

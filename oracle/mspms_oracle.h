@@ -93,6 +93,15 @@ double orc_tasos_min_pe(const orc_tasos *g);
 int orc_md_run(const orc_system *s, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
                double *vx, double *vy, double *vz, mg_md_state *state, double *log);
 
+/* One replica of mg_hmc_batch: nmoves canonical moves of the reference's hmc()
+ * (velinit with the Philox streams of include/mg_philox.h, frclong, md_move over vver,
+ * the Metropolis test of src/dispmd.c:48-66). Same outputs as mg_hmc_batch for that
+ * replica. Returns 0. */
+int orc_hmc_replica(const orc_system *s, const mg_hmc_params *p, int replica, int move0, int nmoves, double *x,
+                    double *y, double *z, int *accepted, double *dh_log, double *energy);
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
 /* CPU cluster-pair builder (same predicate, same op order as the GPU build); the
  * second form takes the column grid and small-box choice of the build under test. */
 int orc_nblist_build(const double *x, const double *y, const double *z, int natom,

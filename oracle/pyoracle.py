@@ -14,8 +14,8 @@ import tempfile
 
 import numpy as np
 
-from mspms2_gb300.capi import (ENERGY_NAMES, MD_LOG, MgEnergies, MgMdParams, MgMdState, MgParams, MgSpecies,
-                               SpeciesPack, system_params)
+from mspms2_gb300.capi import (ENERGY_NAMES, MD_LOG, MgEnergies, MgHmcParams, MgMdParams, MgMdState, MgParams,
+                               MgSpecies, SpeciesPack, system_params)
 from mspms2_gb300.system import System, write_reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -78,6 +78,10 @@ def lib():
                                          C.c_double, _dp, _dp]
         _lib.orc_md_run.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgMdParams), C.c_int, _dp, _dp, _dp, _dp, _dp,
                                     _dp, C.POINTER(MgMdState), _dp]
+        _lib.orc_hmc_replica.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgHmcParams), C.c_int, C.c_int, C.c_int,
+                                         _dp, _dp, _dp, C.POINTER(C.c_int), _dp, _dp]
+        _lib.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        _lib.orc_philox4x32_10.restype = None
         _lib.orc_tasos_min_pe.argtypes = [C.POINTER(OrcTasos)]
         _lib.orc_tasos_min_pe.restype = C.c_double
         _lib.orc_nblist_build.argtypes = [_dp, _dp, _dp, C.c_int, C.c_double, C.c_double,
@@ -177,6 +181,18 @@ class Oracle:
         lib().orc_md_run(C.byref(self.s), C.byref(MgMdParams.from_dict(md)), nsteps, _ptr(pos[0]), _ptr(pos[1]),
                          _ptr(pos[2]), _ptr(vel[0]), _ptr(vel[1]), _ptr(vel[2]), C.byref(st), _ptr(log))
         return pos, vel, st.as_dict(), log
+
+    def hmc_replica(self, hp: dict, replica: int, move0: int, nmoves: int):
+        """The restated canonical HMC moves of one replica (oracle/md_oracle.c): returns
+        (positions [3, n], accepted, energy, dh[nmoves])."""
+        sysm = self.system
+        pos = np.ascontiguousarray(np.stack([sysm.x, sysm.y, sysm.z]), dtype=np.float64)
+        acc = C.c_int()
+        energy = C.c_double()
+        dh = np.zeros(max(nmoves, 1))
+        lib().orc_hmc_replica(C.byref(self.s), C.byref(MgHmcParams(**hp)), replica, move0, nmoves, _ptr(pos[0]),
+                              _ptr(pos[1]), _ptr(pos[2]), C.byref(acc), _ptr(dh), C.byref(energy))
+        return pos, acc.value, energy.value, dh[:nmoves]
 
     def count_pairs(self, r: float) -> int:
         s = self.system
