@@ -256,6 +256,32 @@ def md_extras(system, split_r, precision, device, steps=10, drift_steps=20):
     return out
 
 
+def hmc_extras(device, nrep=512, nmoves=2, seed=2024):
+    """Batched HMC (mg_hmc_batch) on nrep Lennard-Jones replicas with seeded sizes drawn
+    uniformly from 200..5000 atoms (rho* 0.8, T* 1, rc 2.5 sigma, jittered FCC, 10-step
+    trajectories at dt* 0.005): HMC trajectories per second of the whole batch."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import hmc_batch
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(200, 5001, size=nrep)
+    reps = [configs.lj_replica(int(n), seed=seed + i) for i, n in enumerate(sizes)]
+    natom = [r.natom for r in reps]
+    box = [float(r.box[0]) for r in reps]
+    x, y, z = (np.concatenate([getattr(r, k) for r in reps]) for k in "xyz")
+    hp = dict(eps=1.0, sigma=1.0, rcutoff=2.5, mass=1.0, treq=1.0, delt=0.005, nstep_md=10, seed=seed, rescale=0,
+              nconstraint=0)
+    hmc_batch(hp, natom, box, x, y, z, 1, device=device)  # warm-up
+    t0 = time.perf_counter()
+    _, _, _, acc, _, _ = hmc_batch(hp, natom, box, x, y, z, nmoves, move0=1, device=device)
+    dt_wall = time.perf_counter() - t0
+    steps = nrep * nmoves * 10
+    return {"replicas": nrep, "atoms": int(sum(natom)), "moves_per_replica": nmoves,
+            "trajectories_per_s": nrep * nmoves / dt_wall, "atom_steps_per_s": float(sum(natom)) * nmoves * 10 / dt_wall,
+            "acceptance": float(acc.sum()) / (nrep * nmoves), "wall_s": dt_wall, "md_steps": steps,
+            "note": "one persistent launch per call (host copies of all replicas included); Maxwell-Boltzmann "
+                    "momenta without rescaling; FP32 pair forces, FP64 energies and Metropolis test"}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mspms2_gb300 import build
@@ -371,6 +397,7 @@ def run_ours(args, rank, world, local_rank):
         # 7-10 A shell and reciprocal space; Verlet skin 1 A
         if split_r > 0:
             extras["respa"] = md_extras(system, split_r, args.precision, local_rank)
+        extras["hmc_batch"] = hmc_extras(local_rank)
         cpu = cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
         extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
                                   "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],
