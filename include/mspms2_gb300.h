@@ -384,6 +384,38 @@ MG_API mg_status mg_ewald_recip_static(int device, void *stream, int precision, 
                                        const double *d_q, const mg_params *p, double *d_f,
                                        double *d_energy, char *err, size_t err_len);
 
+/* ---- adjoint: parameter gradients of a force loss ----------------------------- */
+/* No counterpart in the reference (which has no derivatives with respect to force-field
+ * parameters): the backward pass for force matching and parameter fitting.
+ *
+ * For host positions x, y, z [natom] and g = dL/dF (gx, gy, gz [natom]) of a loss L of
+ * the long forces F (those of mg_compute with MG_TERMS_LONG, i.e. of frclong()), writes
+ *   grad_eps[k]   = dL/d epsilon_k,  grad_sigma[k] = dL/d sigma_k,  grad_q[k] = dL/d q_k
+ * for every site class k, a class being one site of one species template (the template's
+ * epsilon[a], sigma[a], charge[a]), numbered species by species and site by site:
+ * k = natom(species 0) + ... + natom(species s-1) + a. *nclass gets the number of classes
+ * (at most 16). The pair terms are recomputed from the list of the forward evaluation
+ * that the call runs first (the forces themselves are not returned); every sum is in a
+ * fixed order, so results are reproducible. An epsilon of zero has no derivative (the
+ * mixing rule takes its square root): its entries are 0.
+ * Supported: no LJ switch, no distance split, no solid-fluid term, electrostatics none,
+ * Wolf, or Ewald with tin-foil boundaries; anything else returns MG_ERR_UNSUPPORTED. */
+MG_API mg_status mg_adjoint_params(mg_ctx *ctx, const double *x, const double *y, const double *z,
+                                   const double *gx, const double *gy, const double *gz,
+                                   double *grad_eps, double *grad_sigma, double *grad_q, int *nclass);
+
+/* No counterpart in the reference: Hessian-vector product of the long-range energy in
+ * positions, h = H v = -(dF/dr) v with F the long forces of mg_compute (MG_TERMS_LONG),
+ * for host positions x, y, z and displacements vx, vy, vz [natom]; hx, hy, hz [natom] are
+ * overwritten. Computed analytically from the pair terms of the forward evaluation that
+ * the call runs first and, for Ewald, from the structure factors weighted by q_j v_j.
+ * Where the reference keeps an integer-truncated vector for a molecule that spans the
+ * box, that term does not move with the sites and contributes nothing. Same model
+ * restrictions as mg_adjoint_params. */
+MG_API mg_status mg_adjoint_hvp(mg_ctx *ctx, const double *x, const double *y, const double *z,
+                                const double *vx, const double *vy, const double *vz,
+                                double *hx, double *hy, double *hz);
+
 #ifdef __cplusplus
 }
 #endif

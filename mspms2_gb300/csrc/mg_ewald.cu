@@ -930,3 +930,333 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     return MG_OK;
 #undef EWS_CUDA
 }
+
+// ---------------------------------------------------------------------------------
+// adjoint support: structure factors with arbitrary site weights, the k-space field and
+// the per-class reciprocal-space charge gradient (used by mg_adjoint.cu)
+// ---------------------------------------------------------------------------------
+namespace {
+
+// S_w(k) per slot from the block partials, summed in FP64 in block order
+template <typename R>
+__global__ void k_sk_sum(EwArgs A, int nblk, double2 *__restrict__ out) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= A.nslots) return;
+    double sr = 0.0, si = 0.0;
+    for (int b = 0; b < nblk; b++) {
+        const R *p = (const R *)A.spart + ((size_t)b * A.nslots + slot) * 2;
+        sr += (double)p[0];
+        si += (double)p[1];
+    }
+    out[slot] = make_double2(sr, si);
+}
+
+// sum over slots of cf Im(conj(T^c) (k . A)) per class c, as fixed-order block rows
+__global__ void k_kgrad(EwArgs A, const int *__restrict__ slot_row, const double2 *__restrict__ SA,
+                        const double2 *__restrict__ ST, int nclass, double *__restrict__ rows) {
+    __shared__ double red[256];
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    double cf = 0.0, bx = 0.0, by = 0.0;
+    if (slot < A.nslots) {
+        const int r = slot_row[slot];
+        const int4 row = A.rows[r];
+        const int local = slot - A.row_slot[r];
+        const int a = local >> 1, minus = local & 1;
+        const bool valid = a <= row.z && !(minus && (a == 0 || row.w)) && !(row.w && a == 0);
+        if (valid) {
+            const double kz = minus ? -a : a;
+            const double k0 = A.twopi[0] * row.x, k1 = A.twopi[1] * row.y, k2 = A.twopi[2] * kz;
+            const double rksq = k0 * k0 + k1 * k1 + k2 * k2;
+            cf = 4.0 * A.vfac * A.coul * exp(-A.bfac * rksq) / rksq;
+            const double2 ax = SA[slot], ay = SA[A.nslots + slot], az = SA[2 * A.nslots + slot];
+            bx = k0 * ax.x + k1 * ay.x + k2 * az.x;
+            by = k0 * ax.y + k1 * ay.y + k2 * az.y;
+        }
+    }
+    for (int c = 0; c < nclass; c++) {
+        double v = 0.0;
+        if (cf != 0.0) {
+            const double2 t = ST[(size_t)c * A.nslots + slot];
+            v = cf * (t.x * by - t.y * bx);
+        }
+        red[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) rows[(size_t)blockIdx.x * nclass + c] = red[0];
+        __syncthreads();
+    }
+}
+
+EwArgs ew_args(mg_ctx *c) {
+    const mg_params &p = c->params;
+    EwArgs A = {};
+    A.n = c->natom;
+    A.nrows = c->nrows;
+    A.nslots = c->nslots;
+    A.ntasks = c->ntasks;
+    A.kx = c->kmaxx;
+    A.ky = c->kmaxy;
+    A.kz = std::max(c->kmaxz, 1);
+    A.rows = (const int4 *)c->d_rows.p;
+    A.row_slot = (const int *)c->d_row_slot.p;
+    A.tasks = (const int4 *)c->d_tasks.p;
+    A.tab = c->d_phase.p;
+    A.q = (const double *)c->d_site_q.p;
+    A.spart = c->d_spart.p;
+    A.scoef = c->d_scoef.p;
+    A.twopi[0] = p.twopi_lx;
+    A.twopi[1] = p.twopi_ly;
+    A.twopi[2] = p.twopi_lz;
+    A.bfac = p.bfactor_ewald;
+    A.vfac = p.vfactor_ewald;
+    A.coul = p.coulomb_prefactor;
+    return A;
+}
+
+}  // namespace
+
+// S_w(k) of every slot for site weights w (device [n]), with the phase tables of the
+// last long-range evaluation
+mg_status mg_ewald_weighted_sk(mg_ctx *c, const double *w, double2 *out) {
+    if (c->nrows == 0) return MG_OK;
+    const bool fp64 = c->opt.precision == MG_PREC_FP64;
+    const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
+    EwArgs A = ew_args(c);
+    A.q = w;
+    const int nblk = (A.n + EW_SITES - 1) / EW_SITES;
+    const int P = EW_TILE + 1;
+    const size_t smem = esz * (size_t)(A.kx + 1 + A.ky + 1 + A.kz + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
+    dim3 grid((A.ntasks + EW_TPB - 1) / EW_TPB, nblk);
+    cudaStream_t s = c->stream;
+    const unsigned sb = (unsigned)((A.nslots + 255) / 256);
+    if (fp64) {
+        MG_CUDA(cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
+        k_sk_sum<double><<<sb, 256, 0, s>>>(A, nblk, out);
+    } else {
+        MG_CUDA(cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
+        k_sk_sum<float><<<sb, 256, 0, s>>>(A, nblk, out);
+    }
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+// the reciprocal-space force per unit charge (field[3][n], overwritten), from the
+// coefficients of the last long-range evaluation
+mg_status mg_ewald_field(mg_ctx *c, const double *ones, double *field) {
+    cudaStream_t s = c->stream;
+    MG_CUDA(cudaMemsetAsync(field, 0, sizeof(double) * 3 * (size_t)c->natom, s));
+    if (c->nrows == 0) return MG_OK;
+    const bool fp64 = c->opt.precision == MG_PREC_FP64;
+    const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
+    EwArgs A = ew_args(c);
+    A.q = ones;
+    A.f = field;
+    int maxa = 1;
+    for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
+    const size_t fsmem = 2 * esz * (size_t)EW_FROWS * maxa;
+    const unsigned fblocks = (unsigned)((A.n + EW_FSITES - 1) / EW_FSITES);
+    if (fp64) {
+        MG_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
+    } else {
+        MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
+    }
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
+
+// per-class sums over k of cf Im(conj(T^c) (k . A)) as block rows rows[nblocks][nclass]
+mg_status mg_ewald_kgrad(mg_ctx *c, const double2 *SA, const double2 *ST, int nclass, double *rows, int *nblocks) {
+    *nblocks = 0;
+    if (c->nrows == 0) return MG_OK;
+    EwArgs A = ew_args(c);
+    const unsigned b = (unsigned)((A.nslots + 255) / 256);
+    k_kgrad<<<b, 256, 0, c->stream>>>(A, (const int *)c->d_row_slot.p + c->nrows, SA, ST, nclass, rows);
+    MG_CUDA(cudaGetLastError());
+    *nblocks = (int)b;
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Hessian-vector product support: the directional derivative of the reciprocal-space
+// force F_i = q_i sum_k cf_k Im(conj(S_k) e^{ik.r_i}) k along site displacements v:
+//   dF_i = q_i sum_k cf_k k [ (k.v_i) Re(conj(S_k) e^{ik.r_i}) - Re(conj(S^v_k) e^{ik.r_i}) ]
+// with S^v_k = sum_j q_j (k.v_j) e^{ik.r_j}. The first term is q_i M_i v_i with the per-site
+// matrix M_i = sum_k cf_k Re(conj(S_k) e^{ik.r_i}) k k^T (k_khess, the k-force pass with
+// second derivatives of the row polynomials); the second is the k-force pass itself run
+// on the coefficients i cf_k S^v_k (k_hvcoef).
+// ---------------------------------------------------------------------------------
+namespace {
+
+template <typename R>
+__global__ void __launch_bounds__(EW_FG * EW_FSITES) k_khess(EwArgs A, int maxa, const double *__restrict__ v,
+                                                             double *__restrict__ out) {
+    typedef typename C2<R>::T T2;
+    typedef typename C2<R>::T4 T4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T4 *sC = (T4 *)smem_raw;
+    __shared__ int4 sRow[EW_FROWS];
+    __shared__ double sM[EW_FG][6][EW_FSITES];
+    const int g = threadIdx.x / EW_FSITES, l = threadIdx.x % EW_FSITES;
+    const int a = blockIdx.x * EW_FSITES + l;
+    const bool act = a < A.n;
+    const T2 *tab = (const T2 *)A.tab;
+    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    T2 Z;
+    if (act) {
+        Z = tZ[(size_t)1 * A.n + a];
+    } else {
+        Z.x = (R)1;
+        Z.y = (R)0;
+    }
+    double M[6] = {0, 0, 0, 0, 0, 0};  // xx xy yy xz yz zz in integer k units
+    const T4 *coef = (const T4 *)A.scoef;
+    for (int r0 = 0; r0 < A.nrows; r0 += EW_FROWS) {
+        const int nr = min(EW_FROWS, A.nrows - r0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nr * maxa; i += blockDim.x) {
+            int rr = i / maxa, s = i % maxa;
+            int4 row = A.rows[r0 + rr];
+            T4 c4;
+            c4.x = c4.y = c4.z = c4.w = (R)0;
+            if (s <= row.z) c4 = coef[A.row_slot[r0 + rr] / 2 + s];
+            sC[rr * maxa + s] = c4;
+        }
+        if (threadIdx.x < nr) sRow[threadIdx.x] = A.rows[r0 + threadIdx.x];
+        __syncthreads();
+        if (!act) continue;
+        R m[6] = {0, 0, 0, 0, 0, 0};
+        for (int rr = g; rr < nr; rr += EW_FG) {
+            const int4 row = sRow[rr];
+            T2 X = tX[(size_t)row.x * A.n + a];
+            T2 Y = tY[(size_t)(row.y < 0 ? -row.y : row.y) * A.n + a];
+            if (row.y < 0) Y.y = -Y.y;
+            const T2 Aa = cmul(X, Y);
+            const T4 *cs = sC + rr * maxa;
+            // Horner with the first and half the second derivative: p = P(Z), dp = P'(Z),
+            // hp = P''(Z)/2, and the same for Q
+            const T4 top = cs[row.z];
+            T2 p, q, dp, dq, hp, hq;
+            p.x = top.x; p.y = top.y;
+            q.x = top.z; q.y = top.w;
+            dp.x = dp.y = dq.x = dq.y = hp.x = hp.y = hq.x = hq.y = (R)0;
+            for (int k = row.z - 1; k >= 0; k--) {
+                const T4 c = cs[k];
+                T2 cu, cv;
+                cu.x = c.x; cu.y = c.y;
+                cv.x = c.z; cv.y = c.w;
+                hp = cfma(hp, Z, dp);
+                dp = cfma(dp, Z, p);
+                p = cfma(p, Z, cu);
+                hq = cfma(hq, Z, dq);
+                dq = cfma(dq, Z, q);
+                q = cfma(q, Z, cv);
+            }
+            // sum_a a c_a Z^a = Z P'(Z); sum_a a^2 c_a Z^a = Z P'(Z) + Z^2 P''(Z)
+            const T2 zdp = cmul(Z, dp), zdq = cmul(Z, dq);
+            const T2 z2 = cmul(Z, Z);
+            const T2 hp2 = cmul(z2, hp), hq2 = cmul(z2, hq);
+            T2 s2p, s2q;
+            s2p.x = zdp.x + (R)2 * hp2.x; s2p.y = zdp.y + (R)2 * hp2.y;
+            s2q.x = zdq.x + (R)2 * hq2.x; s2q.y = zdq.y + (R)2 * hq2.y;
+            // Re(A w) for plus slots, Re(A conj(w)) for minus slots (kz = -a)
+            const R r0s = (Aa.x * p.x - Aa.y * p.y) + (Aa.x * q.x + Aa.y * q.y);
+            const R r1s = (Aa.x * zdp.x - Aa.y * zdp.y) - (Aa.x * zdq.x + Aa.y * zdq.y);
+            const R r2s = (Aa.x * s2p.x - Aa.y * s2p.y) + (Aa.x * s2q.x + Aa.y * s2q.y);
+            const R kx = (R)row.x, ky = (R)row.y;
+            m[0] += kx * kx * r0s;
+            m[1] += kx * ky * r0s;
+            m[2] += ky * ky * r0s;
+            m[3] += kx * r1s;
+            m[4] += ky * r1s;
+            m[5] += r2s;
+        }
+        for (int k = 0; k < 6; k++) M[k] += (double)m[k];
+    }
+    for (int k = 0; k < 6; k++) sM[g][k][l] = M[k];
+    __syncthreads();
+    if (g != 0 || !act) return;
+    double t[6] = {0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < EW_FG; j++)
+        for (int k = 0; k < 6; k++) t[k] += sM[j][k][l];
+    const double tx = A.twopi[0], ty = A.twopi[1], tz = A.twopi[2];
+    const double xx = t[0] * tx * tx, xy = t[1] * tx * ty, yy = t[2] * ty * ty;
+    const double xz = t[3] * tx * tz, yz = t[4] * ty * tz, zz = t[5] * tz * tz;
+    const double vx = v[a], vy = v[A.n + a], vz = v[2 * A.n + a];
+    const double q = A.q[a];
+    out[a] += q * (xx * vx + xy * vy + xz * vz);
+    out[A.n + a] += q * (xy * vx + yy * vy + yz * vz);
+    out[2 * A.n + a] += q * (xz * vx + yz * vy + zz * vz);
+}
+
+// k-force coefficients i cf S^v_k, S^v_k = sum_d k_d SW_d(k), in the layout of k_sk_reduce
+// (plus slots conjugated)
+template <typename R>
+__global__ void k_hvcoef(EwArgs A, const int *__restrict__ slot_row, const double2 *__restrict__ SW,
+                         void *__restrict__ coef) {
+    typedef typename C2<R>::T T2;
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= A.nslots) return;
+    const int r = slot_row[slot];
+    const int4 row = A.rows[r];
+    const int local = slot - A.row_slot[r];
+    const int a = local >> 1, minus = local & 1;
+    const bool valid = a <= row.z && !(minus && (a == 0 || row.w)) && !(row.w && a == 0);
+    T2 c;
+    c.x = c.y = (R)0;
+    if (valid) {
+        const double kz = minus ? -a : a;
+        const double k0 = A.twopi[0] * row.x, k1 = A.twopi[1] * row.y, k2 = A.twopi[2] * kz;
+        const double rksq = k0 * k0 + k1 * k1 + k2 * k2;
+        const double cf = 4.0 * A.vfac * A.coul * exp(-A.bfac * rksq) / rksq;
+        const double2 sx = SW[slot], sy = SW[A.nslots + slot], sz = SW[2 * A.nslots + slot];
+        const double vr = k0 * sx.x + k1 * sy.x + k2 * sz.x, vi = k0 * sx.y + k1 * sy.y + k2 * sz.y;
+        // X = i cf S^v = cf (-vi, vr); plus slots hold conj(X)
+        c.x = (R)(-cf * vi);
+        c.y = (R)(minus ? cf * vr : -cf * vr);
+    }
+    ((T2 *)coef)[slot] = c;
+}
+
+}  // namespace
+
+// adds the directional derivative of the reciprocal-space force along v ([3][n]) to out,
+// given SW[3][nslots], the structure factors with weights q_j v_j,d, and scratch for one
+// coefficient array (nslots complex values of the working precision)
+mg_status mg_ewald_jvp(mg_ctx *c, const double *v, const double2 *SW, void *coef_scratch, double *out) {
+    if (c->nrows == 0) return MG_OK;
+    const bool fp64 = c->opt.precision == MG_PREC_FP64;
+    const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
+    EwArgs A = ew_args(c);
+    int maxa = 1;
+    for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
+    const size_t fsmem = 2 * esz * (size_t)EW_FROWS * maxa;
+    const unsigned fblocks = (unsigned)((A.n + EW_FSITES - 1) / EW_FSITES);
+    const unsigned sb = (unsigned)((A.nslots + 255) / 256);
+    const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
+    cudaStream_t s = c->stream;
+    EwArgs B = A;
+    B.scoef = coef_scratch;
+    B.f = out;
+    if (fp64) {
+        MG_CUDA(cudaFuncSetAttribute(k_khess<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_khess<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa, v, out);
+        k_hvcoef<double><<<sb, 256, 0, s>>>(A, slot_row, SW, coef_scratch);
+        MG_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(B, maxa);
+    } else {
+        MG_CUDA(cudaFuncSetAttribute(k_khess<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_khess<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa, v, out);
+        k_hvcoef<float><<<sb, 256, 0, s>>>(A, slot_row, SW, coef_scratch);
+        MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(B, maxa);
+    }
+    MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}

@@ -157,6 +157,8 @@ struct mg_ctx {
     // integration (mg_md_run): velocities, solver work arrays, 1/mass, partial sums,
     // thermostat scalars, per-step records
     DevBuf d_md_v, d_md_work, d_md_rmass, d_md_part, d_md_dev, d_md_log;
+    // adjoint (mg_adjoint_params): site classes and one carved scratch block
+    DevBuf d_adj_class, d_adj;
     // reciprocal space
     int nrows = 0, nslots = 0, kmaxx = 0, kmaxy = 0, kmaxz = 0;
     long long kvectors = 0;
@@ -207,6 +209,11 @@ mg_status mg_launch_intra(mg_ctx *c, const double *dx, const double *dy, const d
 mg_status mg_launch_bonded(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fs);
 mg_status mg_ewald_setup(mg_ctx *c);
 mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl);
+// adjoint support (mg_ewald.cu), valid after a long-range evaluation at the same positions
+mg_status mg_ewald_weighted_sk(mg_ctx *c, const double *w, double2 *out);
+mg_status mg_ewald_field(mg_ctx *c, const double *ones, double *field);
+mg_status mg_ewald_kgrad(mg_ctx *c, const double2 *SA, const double2 *ST, int nclass, double *rows, int *nblocks);
+mg_status mg_ewald_jvp(mg_ctx *c, const double *v, const double2 *SW, void *coef_scratch, double *out);
 mg_status mg_launch_vacuum(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl);
 mg_status mg_launch_coulomb_mole(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl);
 mg_status mg_launch_sf(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl);

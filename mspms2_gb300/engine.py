@@ -10,6 +10,7 @@ constructor raises.
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 import os
 
 import numpy as np
@@ -75,6 +76,8 @@ def load_library(path: str = LIB_PATH):
                                  C.POINTER(I), _dp, _dp]
     lib.mg_sfgrid_sfgridgen.argtypes = [I, C.POINTER(capi.MgSfgridSpec), D, I, C.POINTER(I), _dp]
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
+    lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
+    lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     _lib = lib
     return lib
 
@@ -195,6 +198,58 @@ class Engine:
         self._check(self.lib.mg_md_run(self.ctx, C.byref(mp), nsteps, _p(pos[0]), _p(pos[1]), _p(pos[2]),
                                        _p(vel[0]), _p(vel[1]), _p(vel[2]), C.byref(st), _p(log)))
         return pos, vel, st.as_dict(), log
+
+    def class_params(self):
+        """(epsilon, sigma, charge) per site class: one class per site of each species
+        template, numbered species by species (the order of mg_adjoint_params)."""
+        sp = self.system.species
+        return (np.concatenate([np.asarray(t.epsilon, float) for t in sp]),
+                np.concatenate([np.asarray(t.sigma, float) for t in sp]),
+                np.concatenate([np.asarray(t.charge, float) for t in sp]))
+
+    def set_class_params(self, eps, sigma, charge) -> None:
+        """Replaces the templates' epsilon, sigma and charge (arrays over the site classes)
+        and uploads the topology again."""
+        eps, sigma, charge = (np.asarray(a, dtype=np.float64).ravel() for a in (eps, sigma, charge))
+        new, off = [], 0
+        for t in self.system.species:
+            k = t.natom
+            new.append(dataclasses.replace(t, epsilon=eps[off:off + k].copy(), sigma=sigma[off:off + k].copy(),
+                                           charge=charge[off:off + k].copy()))
+            off += k
+        if off != len(eps) or off != len(sigma) or off != len(charge):
+            raise ValueError(f"expected {off} site classes")
+        self.system = dataclasses.replace(self.system, species=new)
+        self._pack = SpeciesPack(self.system)
+        self._check(self.lib.mg_set_topology(self.ctx, self._pack.n, self._pack.array))
+
+    def adjoint_params(self, g, x=None, y=None, z=None):
+        """dL/d(epsilon, sigma, charge) per site class for g = dL/dF_long ([3, n]) at the
+        given positions (mg_adjoint_params). Returns three arrays over the classes."""
+        s = self.system
+        x = np.ascontiguousarray(s.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(s.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(s.z if z is None else z, dtype=np.float64)
+        g = np.ascontiguousarray(g, dtype=np.float64).reshape(3, self.n)
+        nclass = sum(t.natom for t in s.species)
+        ge, gs, gq = np.zeros(nclass), np.zeros(nclass), np.zeros(nclass)
+        k = C.c_int(0)
+        self._check(self.lib.mg_adjoint_params(self.ctx, _p(x), _p(y), _p(z), _p(g[0]), _p(g[1]), _p(g[2]),
+                                               _p(ge), _p(gs), _p(gq), C.byref(k)))
+        assert k.value == nclass
+        return ge, gs, gq
+
+    def hessian_vector(self, v, x=None, y=None, z=None):
+        """H v = -(dF_long/dr) v ([3, n]) at the given positions (mg_adjoint_hvp)."""
+        s = self.system
+        x = np.ascontiguousarray(s.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(s.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(s.z if z is None else z, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(3, self.n)
+        h = np.zeros((3, self.n))
+        self._check(self.lib.mg_adjoint_hvp(self.ctx, _p(x), _p(y), _p(z), _p(v[0]), _p(v[1]), _p(v[2]),
+                                            _p(h[0]), _p(h[1]), _p(h[2])))
+        return h
 
     def stats(self) -> dict:
         st = MgStats()
