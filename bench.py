@@ -282,6 +282,40 @@ def hmc_extras(device, nrep=512, nmoves=2, seed=2024):
                     "momenta without rescaling; FP32 pair forces, FP64 energies and Metropolis test"}
 
 
+def adjoint_extras(system, precision, device, reps=3):
+    """Derivatives on the bench workload through the host API (positions and vectors in
+    host memory, copies included): one long-force evaluation (mg_compute, MG_TERMS_LONG),
+    the parameter adjoint (mg_adjoint_params, which runs that evaluation first) and the
+    Hessian-vector product (mg_adjoint_hvp, likewise). Wall-clock milliseconds per call."""
+    from mspms2_gb300.engine import TERMS_LONG, Engine
+    n = system.natom
+    rng = np.random.default_rng(17)
+    g = rng.standard_normal((3, n))
+    eng = Engine(system, precision=precision, device=device)
+    try:
+        eng.compute(terms=TERMS_LONG)
+        eng.adjoint_params(g)
+        eng.hessian_vector(g)
+
+        def wall(fn):
+            ts = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                fn()
+                ts.append((time.perf_counter() - t0) * 1e3)
+            return statistics.median(ts)
+
+        t_f = wall(lambda: eng.compute(terms=TERMS_LONG))
+        t_a = wall(lambda: eng.adjoint_params(g))
+        t_h = wall(lambda: eng.hessian_vector(g))
+        nclass = sum(t.natom for t in system.species)
+    finally:
+        eng.close()
+    return {"long_forces_ms": t_f, "adjoint_params_ms": t_a, "hvp_ms": t_h,
+            "adjoint_over_forces": t_a / t_f, "hvp_over_forces": t_h / t_f, "site_classes": nclass,
+            "note": "host API wall time, median of 3; each derivative call includes its forward evaluation"}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mspms2_gb300 import build
@@ -398,7 +432,8 @@ def run_ours(args, rank, world, local_rank):
         if split_r > 0:
             extras["respa"] = md_extras(system, split_r, args.precision, local_rank)
         extras["hmc_batch"] = hmc_extras(local_rank)
-        cpu = cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
+        extras["derivatives"] = adjoint_extras(system, args.precision, local_rank)
+        cpu =cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
         extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
                                   "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],
                                   "host_cores": os.cpu_count()}
