@@ -16,9 +16,11 @@ e2e     the same through mg_compute with pinned host buffers: positions copied i
         forces copied out inside the timed region.
 Also reported: the plain-FP64 GPU path on the same workload; ns/day of the device-resident
 Nose-Hoover RESPA integrator (mg_md_run; inner: bonded + pairs < 7 A, four 0.5 fs steps;
-outer: 7-10 A shell + reciprocal, 2 fs) and the energy drift of an NVE run;
-the roofline of the dominant kernel and a bounded CPU baseline of the reference
-algorithm (the oracle port, single thread, extrapolated from a sampled window).
+outer: 7-10 A shell + reciprocal, 2 fs) and the energy drift of an NVE run; batched HMC
+of 512 Lennard-Jones replicas; the cost of the adjoint and Hessian-vector product; force
+matching on 4096 waters (64 snapshots, loss + gradient, checked against the FP64 path and
+central differences); the roofline of the dominant kernel and a bounded CPU baseline of the
+reference algorithm (the oracle port, single thread, extrapolated from a sampled window).
 """
 from __future__ import annotations
 
@@ -316,6 +318,92 @@ def adjoint_extras(system, precision, device, reps=3):
             "note": "host API wall time, median of 3; each derivative call includes its forward evaluation"}
 
 
+def force_matching_extras(device, nsnap=64, stride=4, seed=2024):
+    """Force matching on 4096 SPC/Fw waters (12,288 sites, Ewald alpha 0.3, rc 10 A, kmax 12):
+    64 snapshots of an FP64 Nose-Hoover trajectory at 298 K (one every 4 steps of 0.5 fs from
+    the seeded lattice); targets = FP64 long forces at eps_OO, sigma_OO, q_O perturbed by 2%
+    Gaussian noise with q_H = -q_O/2; loss = mean squared force error over all snapshots.
+    Times one loss + gradient evaluation over the 64 snapshots (mg_force_match per snapshot,
+    host arrays) on the mixed and the FP64 path, and checks the gradient in (eps_O, sigma_O,
+    q_O) against the FP64 path and against central differences of the FP64 loss
+    (h = 1e-4 relative)."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import TERMS_LONG, Engine
+    from mspms2_gb300.system import md_params
+    s = configs.water_c4(seed)
+    s.delt_fs, s.nstep_inner, s.treq_K = 0.5, 1, 298.0
+    md = md_params(s)
+    md["scheme"] = 1
+    m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
+    v -= (v * m).sum(1, keepdims=True) / m.sum()
+    scale = 1.0 / (3 * s.natom * nsnap)
+
+    def tied(base, p):
+        e, sg, q = (a.copy() for a in base)
+        e[0], sg[0] = p[0], p[1]
+        q[:] = [p[2], -p[2] / 2, -p[2] / 2]
+        return e, sg, q
+
+    def fm_total(eng, snaps, targets):
+        loss, g = 0.0, np.zeros(3)
+        for x, t in zip(snaps, targets):
+            li, (ge, gs, gq) = eng.force_match(t, scale=scale, x=x[0], y=x[1], z=x[2])
+            loss += li
+            g += [ge[0], gs[0], gq[0] - 0.5 * (gq[1] + gq[2])]
+        return loss, g
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    snaps, targets = [], []
+    with Engine(s, precision="fp64", skin=1.0, device=device) as e64:
+        pos, vel, st = np.stack([s.x, s.y, s.z]), v, None
+        for _ in range(nsnap):
+            state = None if st is None else {k: st[k] for k in ("ps", "ss", "pss", "sss")}
+            pos, vel, st, _ = e64.md_run(stride, md, vel, x=pos[0], y=pos[1], z=pos[2], state=state)
+            snaps.append(pos.copy())
+        base = list(e64.class_params())
+        p0 = np.array([base[0][0], base[1][0], base[2][0]])
+        p_tgt = p0 * (1 + 0.02 * np.random.default_rng(seed + 1).standard_normal(3))
+        e64.set_class_params(*tied(base, p_tgt))
+        targets = [e64.compute(*x, terms=TERMS_LONG)[0] for x in snaps]
+        e64.set_class_params(*base)
+        fm_total(e64, snaps[:1], targets[:1])
+        t0 = time.perf_counter()
+        l64, g64 = fm_total(e64, snaps, targets)
+        t64 = time.perf_counter() - t0
+
+        def loss64(p):
+            e64.set_class_params(*tied(base, p))
+            return scale * sum(float(np.sum((e64.compute(*x, terms=TERMS_LONG)[0] - t) ** 2))
+                               for x, t in zip(snaps, targets))
+        fd = np.zeros(3)
+        for k in range(3):
+            h = 1e-4 * abs(p0[k])
+            pp, pm = p0.copy(), p0.copy()
+            pp[k] += h
+            pm[k] -= h
+            fd[k] = (loss64(pp) - loss64(pm)) / (2 * h)
+        e64.set_class_params(*base)
+    with Engine(s, precision="mixed", skin=1.0, device=device) as emx:
+        fm_total(emx, snaps[:2], targets[:2])
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            lmx, gmx = fm_total(emx, snaps, targets)
+            ts.append(time.perf_counter() - t0)
+        tmx = statistics.median(ts)
+    return {"workload": "water_c4 force matching", "sites": s.natom, "snapshots": nsnap,
+            "ms_per_gradient": tmx * 1e3, "snapshots_per_s": nsnap / tmx, "fp64_ms_per_gradient": t64 * 1e3,
+            "mixed_over_fp64": t64 / tmx, "loss": lmx, "loss_fp64": l64,
+            "grad_eps_sigma_qO": gmx.tolist(), "grad_rel_err_vs_fp64": rel(gmx, g64),
+            "grad_fp64_rel_err_vs_central_diff": rel(g64, fd), "grad_mixed_rel_err_vs_central_diff": rel(gmx, fd),
+            "note": "one mg_force_match per snapshot (forward + adjoint, host arrays, copies included); "
+                    "gradient in (eps_OO, sigma_OO, q_O) with q_H = -q_O/2; central differences h = 1e-4 relative"}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mspms2_gb300 import build
@@ -433,6 +521,7 @@ def run_ours(args, rank, world, local_rank):
             extras["respa"] = md_extras(system, split_r, args.precision, local_rank)
         extras["hmc_batch"] = hmc_extras(local_rank)
         extras["derivatives"] = adjoint_extras(system, args.precision, local_rank)
+        extras["force_matching"] = force_matching_extras(local_rank)
         cpu =cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
         extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
                                   "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],

@@ -404,6 +404,17 @@ MG_API mg_status mg_adjoint_params(mg_ctx *ctx, const double *x, const double *y
                                    const double *gx, const double *gy, const double *gz,
                                    double *grad_eps, double *grad_sigma, double *grad_q, int *nclass);
 
+/* No counterpart in the reference: one force-matching evaluation. For host positions
+ * x, y, z and target forces tx, ty, tz [natom], computes the long forces F, the loss
+ *   *loss = scale * sum over sites and components of (F - T)^2
+ * (scale = 1 / (3 natom) gives the mean squared force error) and its gradient with
+ * respect to the site-class parameters, as mg_adjoint_params does for g = 2 scale (F - T).
+ * The residual and g stay on the device: one forward evaluation and one adjoint pass. */
+MG_API mg_status mg_force_match(mg_ctx *ctx, const double *x, const double *y, const double *z,
+                                const double *tx, const double *ty, const double *tz, double scale,
+                                double *loss, double *grad_eps, double *grad_sigma, double *grad_q,
+                                int *nclass);
+
 /* No counterpart in the reference: Hessian-vector product of the long-range energy in
  * positions, h = H v = -(dF/dr) v with F the long forces of mg_compute (MG_TERMS_LONG),
  * for host positions x, y, z and displacements vx, vy, vz [natom]; hx, hy, hz [natom] are

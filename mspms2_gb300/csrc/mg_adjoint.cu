@@ -566,17 +566,13 @@ static IntraArgs intra_args(mg_ctx *c, const double *g) {
     return B;
 }
 
-extern "C" mg_status mg_adjoint_params(mg_ctx *c, const double *x, const double *y, const double *z,
-                                       const double *gx, const double *gy, const double *gz, double *grad_eps,
-                                       double *grad_sigma, double *grad_q, int *nclass_out) {
-    if (!c || !x || !y || !z || !gx || !gy || !gz || !grad_eps || !grad_sigma || !grad_q) return MG_ERR_INVALID;
-    int nclass = 0;
-    mg_status st = adj_forward(c, x, y, z, &nclass);
-    if (nclass_out) *nclass_out = nclass;
-    if (st) return st;
+// the parameter passes for g = dL/dF ([3][n], on the device) after adj_forward; waits for
+// the stream and writes the per-class sums
+static mg_status adj_params_dev(mg_ctx *c, int nclass, const double *g, double *grad_eps, double *grad_sigma,
+                                double *grad_q) {
+    mg_status st = MG_OK;
     const mg_params &p = c->params;
     const int n = c->natom;
-    const size_t nb = sizeof(double) * n;
     cudaStream_t s = c->stream;
     const bool ewald = p.charge_type == MG_ELEC_EWALD && c->nrows > 0;
     const unsigned pblocks = (unsigned)(((size_t)c->cl_cap * MG_CL + ADJ_TPB - 1) / ADJ_TPB);
@@ -584,18 +580,14 @@ extern "C" mg_status mg_adjoint_params(mg_ctx *c, const double *x, const double 
     const unsigned fblocks = ewald ? (unsigned)((n + ADJ_TPB - 1) / ADJ_TPB) : 0;
     const size_t ns = ewald ? (size_t)c->nslots : 0;
     const unsigned kblocks = (unsigned)((ns + 255) / 256);
-    // scratch in 8-byte units: g, weights, field, SA, ST, then the block rows
-    const size_t o_g = 0, o_w = o_g + 3 * (size_t)n, o_f = o_w + (ewald ? (4 + (size_t)nclass) * n : 0);
+    // scratch in 8-byte units: weights, field, SA, ST, then the block rows
+    const size_t o_w = 0, o_f = o_w + (ewald ? (4 + (size_t)nclass) * n : 0);
     const size_t o_sa = o_f + (ewald ? 3 * (size_t)n : 0), o_st = o_sa + 2 * 3 * ns;
     const size_t o_rp = o_st + 2 * (size_t)nclass * ns, o_ri = o_rp + (size_t)pblocks * 3 * nclass;
     const size_t o_rf = o_ri + (size_t)iblocks * 3 * nclass, o_rk = o_rf + (size_t)fblocks * nclass;
     const size_t total = o_rk + (size_t)kblocks * nclass;
     if (!mg_ensure(c, c->d_adj, sizeof(double) * total)) return MG_ERR_ALLOC;
     double *W = (double *)c->d_adj.p;
-    double *g = W + o_g;
-    MG_CUDA(cudaMemcpyAsync(g, gx, nb, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(g + n, gy, nb, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(g + 2 * n, gz, nb, cudaMemcpyHostToDevice, s));
     const bool fp64 = c->opt.precision == MG_PREC_FP64;
     if (pblocks) {
         AdjArgs A = pair_args(c, g);
@@ -651,6 +643,79 @@ extern "C" mg_status mg_adjoint_params(mg_ctx *c, const double *x, const double 
         for (int k = 0; k < nclass; k++) grad_q[k] += rf[(size_t)b * nclass + k];
     for (int b = 0; b < kb; b++)
         for (int k = 0; k < nclass; k++) grad_q[k] += rk[(size_t)b * nclass + k];
+    return MG_OK;
+}
+
+extern "C" mg_status mg_adjoint_params(mg_ctx *c, const double *x, const double *y, const double *z,
+                                       const double *gx, const double *gy, const double *gz, double *grad_eps,
+                                       double *grad_sigma, double *grad_q, int *nclass_out) {
+    if (!c || !x || !y || !z || !gx || !gy || !gz || !grad_eps || !grad_sigma || !grad_q) return MG_ERR_INVALID;
+    int nclass = 0;
+    mg_status st = adj_forward(c, x, y, z, &nclass);
+    if (nclass_out) *nclass_out = nclass;
+    if (st) return st;
+    const int n = c->natom;
+    const size_t nb = sizeof(double) * n;
+    if (!mg_ensure(c, c->d_adj_g, 6 * nb)) return MG_ERR_ALLOC;
+    double *g = (double *)c->d_adj_g.p;
+    cudaStream_t s = c->stream;
+    MG_CUDA(cudaMemcpyAsync(g, gx, nb, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(g + n, gy, nb, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(g + 2 * n, gz, nb, cudaMemcpyHostToDevice, s));
+    return adj_params_dev(c, nclass, g, grad_eps, grad_sigma, grad_q);
+}
+
+namespace {
+// residual of force matching: g = 2 scale (F - T) and per-block sums of (F - T)^2
+__global__ void __launch_bounds__(256) k_fm_residual(int n3, const double *__restrict__ f,
+                                                     const double *__restrict__ t, double scale,
+                                                     double *__restrict__ g, double *__restrict__ rows) {
+    __shared__ double red[256];
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    double d2 = 0.0;
+    if (i < n3) {
+        const double d = f[i] - t[i];
+        g[i] = 2.0 * scale * d;
+        d2 = d * d;
+    }
+    red[threadIdx.x] = d2;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) rows[blockIdx.x] = red[0];
+}
+}  // namespace
+
+extern "C" mg_status mg_force_match(mg_ctx *c, const double *x, const double *y, const double *z,
+                                    const double *tx, const double *ty, const double *tz, double scale,
+                                    double *loss, double *grad_eps, double *grad_sigma, double *grad_q,
+                                    int *nclass_out) {
+    if (!c || !x || !y || !z || !tx || !ty || !tz || !loss || !grad_eps || !grad_sigma || !grad_q)
+        return MG_ERR_INVALID;
+    int nclass = 0;
+    mg_status st = adj_forward(c, x, y, z, &nclass);
+    if (nclass_out) *nclass_out = nclass;
+    if (st) return st;
+    const int n = c->natom;
+    const size_t nb = sizeof(double) * n;
+    const unsigned rb = (unsigned)((3 * (size_t)n + 255) / 256);
+    if (!mg_ensure(c, c->d_adj_g, 6 * nb + sizeof(double) * rb)) return MG_ERR_ALLOC;
+    double *g = (double *)c->d_adj_g.p, *t = g + 3 * n, *rows = t + 3 * n;
+    cudaStream_t s = c->stream;
+    MG_CUDA(cudaMemcpyAsync(t, tx, nb, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(t + n, ty, nb, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(t + 2 * n, tz, nb, cudaMemcpyHostToDevice, s));
+    k_fm_residual<<<rb, 256, 0, s>>>(3 * n, (const double *)c->d_fl.p, t, scale, g, rows);
+    MG_CUDA(cudaGetLastError());
+    std::vector<double> h(rb);
+    MG_CUDA(cudaMemcpyAsync(h.data(), rows, sizeof(double) * rb, cudaMemcpyDeviceToHost, s));
+    // adj_params_dev waits for the stream, which completes the copy above
+    if ((st = adj_params_dev(c, nclass, g, grad_eps, grad_sigma, grad_q))) return st;
+    double sum = 0.0;
+    for (unsigned b = 0; b < rb; b++) sum += h[b];
+    *loss = scale * sum;
     return MG_OK;
 }
 

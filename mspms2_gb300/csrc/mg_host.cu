@@ -127,7 +127,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_flags, &c->d_tasos, &c->d_myinterp, &c->d_tubes, &c->d_solid,
                       &c->d_meta, &c->d_pair_img, &c->d_cl_bbf, &c->d_col_ncl, &c->d_counter,
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
-                      &c->d_adj_class, &c->d_adj};
+                      &c->d_adj_class, &c->d_adj, &c->d_adj_g};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
     for (auto &b : c->myinterp_buf) mg_free(b);

@@ -158,7 +158,7 @@ struct mg_ctx {
     // thermostat scalars, per-step records
     DevBuf d_md_v, d_md_work, d_md_rmass, d_md_part, d_md_dev, d_md_log;
     // adjoint (mg_adjoint_params): site classes and one carved scratch block
-    DevBuf d_adj_class, d_adj;
+    DevBuf d_adj_class, d_adj, d_adj_g;
     // reciprocal space
     int nrows = 0, nslots = 0, kmaxx = 0, kmaxy = 0, kmaxz = 0;
     long long kvectors = 0;

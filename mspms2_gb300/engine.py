@@ -78,6 +78,7 @@ def load_library(path: str = LIB_PATH):
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.mg_force_match.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, D, _dp, _dp, _dp, _dp, C.POINTER(I)]
     _lib = lib
     return lib
 
@@ -238,6 +239,23 @@ class Engine:
                                                _p(ge), _p(gs), _p(gq), C.byref(k)))
         assert k.value == nclass
         return ge, gs, gq
+
+    def force_match(self, target, scale=None, x=None, y=None, z=None):
+        """(loss, (dL/d eps, dL/d sigma, dL/d q) per class) for L = scale * sum (F_long - target)^2
+        (mg_force_match); scale defaults to 1 / (3 n), the mean squared force error."""
+        s = self.system
+        x = np.ascontiguousarray(s.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(s.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(s.z if z is None else z, dtype=np.float64)
+        t = np.ascontiguousarray(target, dtype=np.float64).reshape(3, self.n)
+        nclass = sum(sp.natom for sp in s.species)
+        ge, gs, gq = np.zeros(nclass), np.zeros(nclass), np.zeros(nclass)
+        loss = C.c_double(0.0)
+        k = C.c_int(0)
+        sc = 1.0 / (3 * self.n) if scale is None else float(scale)
+        self._check(self.lib.mg_force_match(self.ctx, _p(x), _p(y), _p(z), _p(t[0]), _p(t[1]), _p(t[2]), sc,
+                                            C.byref(loss), _p(ge), _p(gs), _p(gq), C.byref(k)))
+        return loss.value, (ge, gs, gq)
 
     def hessian_vector(self, v, x=None, y=None, z=None):
         """H v = -(dF_long/dr) v ([3, n]) at the given positions (mg_adjoint_hvp)."""

@@ -199,3 +199,52 @@ def test_hessian_is_symmetric():
         hu, hv = eng.hessian_vector(u), eng.hessian_vector(v)
     a, b = float(np.sum(u * hv)), float(np.sum(v * hu))
     assert abs(a - b) <= 1e-9 * max(abs(a), np.linalg.norm(hu) * np.linalg.norm(v)), (a, b)
+
+
+def test_force_match_matches_adjoint_and_differences():
+    # fused loss + gradient against the separate calls, and the tied-charge gradient
+    # (q_H = -q_O / 2) against central differences of the FP64 loss (h = 1e-4 relative)
+    s = load("water_ewald_512")
+    rng = np.random.default_rng(21)
+    with Engine(s, precision="fp64") as eng:
+        base = list(eng.class_params())
+        pert = [a * (1 + 0.02 * rng.standard_normal(a.shape)) for a in base]
+        pert[2] = np.array([pert[2][0], -pert[2][0] / 2, -pert[2][0] / 2])
+        eng.set_class_params(*pert)
+        target, _, _ = eng.compute(terms=TERMS_LONG)
+        eng.set_class_params(*base)
+        fl, _, _ = eng.compute(terms=TERMS_LONG)
+        scale = 1.0 / (3 * s.natom)
+        loss, grads = eng.force_match(target)
+        assert abs(loss - scale * np.sum((fl - target) ** 2)) <= 1e-12 * loss
+        sep = eng.adjoint_params(2 * scale * (fl - target))
+        for a, b in zip(grads, sep):
+            assert np.allclose(a, b, rtol=1e-12, atol=0)
+
+        def tied(p):  # (eps_O, sigma_O, q_O) -> class parameters
+            e, sg, q = (a.copy() for a in base)
+            e[0], sg[0] = p[0], p[1]
+            q[:] = [p[2], -p[2] / 2, -p[2] / 2]
+            return e, sg, q
+
+        p0 = np.array([base[0][0], base[1][0], base[2][0]])
+        g_tied = np.array([grads[0][0], grads[1][0], grads[2][0] - 0.5 * (grads[2][1] + grads[2][2])])
+        fd = np.zeros(3)
+        for k in range(3):
+            h = 1e-4 * abs(p0[k])
+            pp, pm = p0.copy(), p0.copy()
+            pp[k] += h
+            pm[k] -= h
+            eng.set_class_params(*tied(pp))
+            lp, _ = eng.force_match(target)
+            eng.set_class_params(*tied(pm))
+            lm, _ = eng.force_match(target)
+            fd[k] = (lp - lm) / (2 * h)
+        eng.set_class_params(*base)
+        assert nrel(g_tied, fd) <= 1e-4, (g_tied, fd)
+    with Engine(s, precision="mixed") as emx:
+        lmx, gmx = emx.force_match(target)
+    # the residual is ~2% of the force, so the mixed path's ~1e-6 force error is ~5e-5 of it
+    assert abs(lmx - loss) <= 1e-3 * loss, (lmx, loss)
+    gmx_tied = np.array([gmx[0][0], gmx[1][0], gmx[2][0] - 0.5 * (gmx[2][1] + gmx[2][2])])
+    assert nrel(gmx_tied, g_tied) <= 1e-4, (gmx_tied, g_tied)
