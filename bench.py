@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 path, RESPA and CPU baseline")
     ap.add_argument("--cpu-sample-mols", type=int, default=256)
     ap.add_argument("--cpu-k-stride", type=int, default=400)
+    ap.add_argument("--md-dt-sweep", action="store_true",
+                    help="print the NVE drift of the water system against the outer time step and exit")
     return ap.parse_args()
 
 
@@ -211,26 +213,36 @@ def run_reference(args, rank):
     return 0
 
 
-def md_extras(system, split_r, precision, device, steps=10, drift_steps=20):
-    """ns/day of mg_md_run (NVT, vver_nh_3) and the energy drift of an NVE run (vver) on the
-    workload, from seeded Maxwell-Boltzmann velocities at 298 K with zero momentum."""
+def md_extras(system, split_r, precision, device, steps=10, equil_steps=1000, nve_steps=500, fp64_steps=60):
+    """ns/day of mg_md_run (NVT, vver_nh_3) and the energy drift of NVE runs (vver) on the
+    workload, from seeded Maxwell-Boltzmann velocities at 298 K with zero momentum. The
+    drift is taken after an NVT equilibration of equil_steps outer steps (the lattice start
+    relaxes strongly): a linear fit of ukin + uinter + uintra over nve_steps outer steps on
+    the mixed path, and over the first fp64_steps from the same state on both paths."""
     from mspms2_gb300.engine import Engine
-    from mspms2_gb300.system import md_params
+    from mspms2_gb300.system import md_params, time_base
     s = system
     s.respa_split = split_r
     s.delt_fs, s.nstep_inner, s.treq_K = 2.0, 4, 298.0
     md = md_params(s)
+    # Nose-Hoover masses for a 100 fs coupling time, Q = g T tau^2 (a fixed Q would couple
+    # ever more stiffly as the system grows: Q = 1000 gives ~3 fs at 295k degrees of freedom)
+    tau = 100.0 / time_base(s)
+    md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
     m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
     rng = np.random.default_rng(7)
     v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
     v -= (v * m).sum(1, keepdims=True) / m.sum()
-    out = {}
+    out = {"nh_tau_fs": 100.0}
+
+    def keep(st):
+        return {k: st[k] for k in ("ps", "ss", "pss", "sss")}
+
     with Engine(s, precision=precision, skin=1.0, device=device) as eng:
         md["scheme"] = 1
         pos, vel, st, _ = eng.md_run(2, md, v)  # warm-up: list, tables, solver
         t0 = time.perf_counter()
-        pos, vel, st, log = eng.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2],
-                                       state={k: st[k] for k in ("ps", "ss", "pss", "sss")})
+        pos, vel, st, log = eng.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2], state=keep(st))
         dt_wall = time.perf_counter() - t0
         out["scheme"] = "NVT Nose-Hoover RESPA (vver_nh_3), 4 x 0.5 fs inner + 2 fs outer"
         out["split_A"] = split_r
@@ -238,23 +250,66 @@ def md_extras(system, split_r, precision, device, steps=10, drift_steps=20):
         out["ms_per_outer_step"] = dt_wall / steps * 1e3
         out["ns_per_day"] = steps * 2.0e-6 / dt_wall * 86400.0
         out["tinst_K"] = [float(log[0, 8]), float(log[-1, 8])]
+        pos, vel, st, log = eng.md_run(equil_steps, md, vel, x=pos[0], y=pos[1], z=pos[2], state=keep(st))
+        out["equilibration"] = {"outer_steps": equil_steps, "tinst_K_end": float(log[-1, 8])}
         md["scheme"] = 0
         start = (pos.copy(), vel.copy())
-        _, _, _, log = eng.md_run(drift_steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
+        _, _, _, log = eng.md_run(nve_steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
     with Engine(s, precision="fp64", skin=1.0, device=device) as e64:
-        _, _, _, log64 = e64.md_run(drift_steps, md, start[1], x=start[0][0], y=start[0][1], z=start[0][2])
+        _, _, _, log64 = e64.md_run(fp64_steps, md, start[1], x=start[0][0], y=start[0][1], z=start[0][2])
     s.respa_split = 0.0
 
-    def drift(lg):
-        h = lg[:, 0] + lg[:, 1] + lg[:, 2]  # ukin + uinter + uintra (K)
+    def series(lg):
+        return lg[:, 0] + lg[:, 1] + lg[:, 2]  # ukin + uinter + uintra (K)
+
+    def drift(h):
         slope = float(np.polyfit(np.arange(len(h)) * 2.0, h, 1)[0])  # K per fs
         return slope * 1e6 / (md["treq"] * s.natom)
-    out["nve_drift_kT_per_ns_per_atom"] = drift(log)
-    out["nve_drift_fp64_path"] = drift(log64)
-    out["nve_steps"] = drift_steps
+    h = series(log)
+    out["nve"] = {"outer_steps": nve_steps, "ps": nve_steps * 2.0e-3,
+                  "drift_kT_per_ns_per_atom": drift(h),
+                  "rms_fluctuation_kT_per_atom": float(np.std(h)) / (md["treq"] * s.natom),
+                  "window_steps": fp64_steps,
+                  "window_drift_mixed": drift(h[:fp64_steps + 1]), "window_drift_fp64": drift(series(log64)),
+                  "window_drift_of_mixed_minus_fp64": drift(h[:fp64_steps + 1] - series(log64))}
     out["note"] = ("device-resident: positions, velocities and thermostat scalars stay in HBM; timed with the "
                    "wall clock around mg_md_run (host copies of the start and end included); drift from a "
-                   "linear fit of ukin + uinter + uintra over the NVE run")
+                   "linear fit of ukin + uinter + uintra over the NVE run after the NVT equilibration")
+    return out
+
+
+def md_dt_sweep(precision="mixed", device=0, equil_steps=1000, ps=1.0):
+    """NVE energy drift of the water system against the outer time step, from one state
+    equilibrated by Nose-Hoover NVT (2 fs outer step, tau 100 fs): RESPA 2 fs / 4 x 0.5 fs,
+    1 fs / 2 x 0.5 fs and plain velocity Verlet at 0.5 fs, each over `ps` picoseconds."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import Engine
+    from mspms2_gb300.system import md_params, time_base
+    s = configs.water_c2()
+    s.delt_fs, s.nstep_inner, s.treq_K = 2.0, 4, 298.0
+    md = md_params(s)
+    tau = 100.0 / time_base(s)
+    md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
+    m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+    rng = np.random.default_rng(7)
+    v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
+    v -= (v * m).sum(1, keepdims=True) / m.sum()
+    out = {"workload": "water_c2", "precision": precision, "equilibration_outer_steps": equil_steps}
+    with Engine(s, precision=precision, skin=1.0, device=device) as eng:
+        md["scheme"] = 1
+        pos, vel, st, log = eng.md_run(equil_steps, md, v)
+        out["T_after_equilibration_K"] = float(log[-1, 8])
+        runs = []
+        for outer_fs, inner in [(2.0, 4), (1.0, 2), (0.5, 1)]:
+            mm = dict(md, scheme=0, delt=outer_fs / time_base(s), nstep_inner=inner)
+            n = int(round(ps * 1000.0 / outer_fs))
+            _, _, _, lg = eng.md_run(n, mm, vel, x=pos[0], y=pos[1], z=pos[2])
+            h = lg[:, 0] + lg[:, 1] + lg[:, 2]
+            slope = float(np.polyfit(np.arange(len(h)) * outer_fs, h, 1)[0])
+            runs.append({"outer_fs": outer_fs, "inner_steps": inner, "steps": n,
+                         "drift_kT_per_ns_per_atom": slope * 1e6 / (md["treq"] * s.natom),
+                         "rms_fluctuation_kT_per_atom": float(np.std(h)) / (md["treq"] * s.natom)})
+        out["nve"] = runs
     return out
 
 
@@ -581,6 +636,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank)
+    if args.md_dt_sweep:
+        from mspms2_gb300 import build
+        build.build()
+        if rank == 0:
+            print(json.dumps(md_dt_sweep(args.precision, local_rank)), flush=True)
+        return 0
     return run_ours(args, rank, world, local_rank)
 
 
