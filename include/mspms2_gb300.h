@@ -294,6 +294,39 @@ typedef struct mg_md_state {
 MG_API mg_status mg_md_run(mg_ctx *ctx, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
                            double *vx, double *vy, double *vz, mg_md_state *state, double *log);
 
+/* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
+/* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
+ * first stage whose T is below t_min (the reference tests T < t_min after the stage). A
+ * stage is velinit at T (src/initvars.c:151-229: Gaussian velocities sqrt(T/aw) g, total
+ * momentum removed, rescaled to T exactly), forces, n_tries vver_nh_3 steps with
+ * treq = T, then the thermostat scalars are reset to zero (src/siman.c:167-174). The
+ * Gaussians come from Philox4x32-10 (include/mg_philox.h), key = seed, counter = (site,
+ * stage, 0 or 1, 0x5349), in place of the reference's serial generator. */
+typedef struct mg_siman_params {
+    mg_md_params md;   /* scheme MG_MD_NVT_NH; md.treq is set per stage */
+    double t_initial;  /* reduced temperature of the first stage */
+    double t_min;      /* the last stage is the first one below t_min */
+    double mu_t;       /* cooling divisor (> 1) */
+    int n_tries;       /* vver_nh_3 steps per stage (iters_fixed_t only paces printing) */
+    int max_stages;    /* rows of stage_log; a longer schedule is refused */
+    uint64_t seed;
+} mg_siman_params;
+
+/* Values recorded per stage by mg_siman_run, at the end of the stage: T, ukin, uinter,
+ * uintra, ushift, tinst, unhts, unhtss. */
+#define MG_SIMAN_LOG 8
+
+/* Number of stages of the schedule, or -1 if it is invalid or needs more than limit. */
+MG_API int mg_siman_stage_count(double t_initial, double t_min, double mu_t, int limit);
+
+/* Runs the whole schedule on the device. x, y, z hold the start and receive the end;
+ * vx, vy, vz receive the final velocities; state holds the first stage's thermostat
+ * scalars and receives the last; *nstages the number of stages run; stage_log, if not
+ * NULL, nstages*MG_SIMAN_LOG doubles. */
+MG_API mg_status mg_siman_run(mg_ctx *ctx, const mg_siman_params *p, double *x, double *y, double *z,
+                              double *vx, double *vy, double *vz, mg_md_state *state, int *nstages,
+                              double *stage_log);
+
 /* ---- batched Hybrid Monte Carlo (src/hmc.c:23-40, src/dispmd.c:12-103) ------- */
 /* Lennard-Jones replicas (one site type, cubic boxes, reduced units). */
 typedef struct mg_hmc_params {

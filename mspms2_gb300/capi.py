@@ -78,6 +78,19 @@ class MgMdParams(C.Structure):
         return cls(**{k: d[k] for k, _ in cls._fields_})
 
 
+class MgSimanParams(C.Structure):
+    _fields_ = [("md", MgMdParams), ("t_initial", C.c_double), ("t_min", C.c_double), ("mu_t", C.c_double),
+                ("n_tries", C.c_int), ("max_stages", C.c_int), ("seed", C.c_ulonglong)]
+
+    @classmethod
+    def from_dict(cls, md: dict, sched: dict) -> "MgSimanParams":
+        return cls(md=MgMdParams.from_dict(md), **sched)
+
+
+SIMAN_LOG_NAMES = ["T", "ukin", "uinter", "uintra", "ushift", "tinst", "unhts", "unhtss"]
+SIMAN_LOG = 8
+
+
 class MgSfgridSpec(C.Structure):
     _fields_ = [("nsolid", C.c_int), ("sx", _dp), ("sy", _dp), ("sz", _dp), ("uclx", C.c_double),
                 ("ucly", C.c_double), ("uclz", C.c_double), ("f_sigma", C.c_double), ("f_epsilon", C.c_double),

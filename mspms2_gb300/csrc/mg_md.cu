@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "mg_internal.cuh"
+#include "../../include/mg_philox.h"
 
 #define MD_TPB 256       // threads per block of the site kernels
 #define MD_ITER_BATCH 4  // solver iterations launched between convergence reads
@@ -34,6 +35,7 @@ struct MdDev {
     double sumv2;             // the reference's running sum m v^2
     double psn, pso, delps, di;
     double ukin, tinst, unhts, unhtss;
+    double vel[4];            // velinit: momentum shift (x, y, z) and the rescaling factor
     int ready, iter;
 };
 
@@ -273,6 +275,100 @@ __global__ void k_md_ukin_scalar(MdArgs A, int nb) {
     if (threadIdx.x == 0) A.s->ukin = sumv2 * 0.5;
 }
 
+// ---- velinit (src/initvars.c:151-229) on counter-based streams ------------------------
+// v = sqrt(treq / aw) g with g standard normal (Philox4x32-10, key = seed, counter =
+// (site, stage, purpose 0/1, tag)); partials [4][nb] of aw v (x, y, z) and of aw
+__global__ void k_vel_draw(MdArgs A, const double *__restrict__ aw, double treq, uint32_t k0, uint32_t k1,
+                           uint32_t stage, uint32_t tag, int nb) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double p[4] = {0.0, 0.0, 0.0, 0.0};
+    if (a < A.n) {
+        const uint32_t key[2] = {k0, k1};
+        const uint32_t c0[4] = {(uint32_t)a, stage, 0u, tag}, c1[4] = {(uint32_t)a, stage, 1u, tag};
+        uint32_t w0[4], w1[4];
+        double g0, g1, g2, g3;
+        mg_philox4x32_10(c0, key, w0);
+        mg_philox4x32_10(c1, key, w1);
+        mg_gauss2(w0, &g0, &g1);
+        mg_gauss2(w1, &g2, &g3);
+        const double m = aw[a], stdv = sqrt(treq) / sqrt(m);
+        const double v[3] = {stdv * g0, stdv * g1, stdv * g2};
+        for (int d = 0; d < 3; d++) {
+            A.v[d * A.n + a] = v[d];
+            p[d] = v[d] * m;
+        }
+        p[3] = m;
+    }
+    for (int k = 0; k < 4; k++) block_partial(p[k], A.part + (size_t)k * nb);
+}
+
+// momentum per unit mass of the system (the reference's px /= system_mass)
+__global__ void k_vel_momentum(MdArgs A, int nb) {
+    __shared__ double red[MD_TPB];
+    double out[4];
+    for (int k = 0; k < 4; k++) {
+        double t = 0.0;
+        for (int i = threadIdx.x; i < nb; i += MD_TPB) t += A.part[(size_t)k * nb + i];
+        red[threadIdx.x] = t;
+        __syncthreads();
+        for (int o = MD_TPB / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        out[k] = red[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; d++) A.s->vel[d] = out[d] / out[3];
+}
+
+// v -= P/M; partial of aw v^2
+__global__ void k_vel_shift(MdArgs A, const double *__restrict__ aw) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        double s2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double v = A.v[d * A.n + a] - A.s->vel[d];
+            A.v[d * A.n + a] = v;
+            s2 += v * v;
+        }
+        m2 = aw[a] * s2;
+    }
+    block_partial(m2, A.part);
+}
+
+// ukin, tinst and the factor that rescales the temperature to treq exactly
+__global__ void k_vel_scale_scalar(MdArgs A, int nb, double treq, double nfree) {
+    const double s2 = sum_partials(A.part, nb);
+    if (threadIdx.x != 0) return;
+    const double ukin = 0.5 * s2, tinst = 2.0 * ukin / nfree;
+    A.s->vel[3] = sqrt(treq / tinst);
+}
+
+// v *= scaling; partial of aw v^2 (the recomputed kinetic energy)
+__global__ void k_vel_scale(MdArgs A, const double *__restrict__ aw) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        const double sc = A.s->vel[3];
+        double s2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double v = A.v[d * A.n + a] * sc;
+            A.v[d * A.n + a] = v;
+            s2 += v * v;
+        }
+        m2 = aw[a] * s2;
+    }
+    block_partial(m2, A.part);
+}
+
+// the thermostat scalars a new annealing stage starts from (src/siman.c:167-174)
+__global__ void k_siman_reset(MdDev *s) {
+    s->ps = s->ss = s->pss = s->sss = 0.0;
+    s->unhts = s->unhtss = 0.0;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------
@@ -320,76 +416,58 @@ mg_status nh_solve(MdRun &R, const double *f, double h, double dt, double q, dou
 
 }  // namespace
 
-extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, double *x, double *y, double *z,
-                               double *vx, double *vy, double *vz, mg_md_state *state, double *log) {
-    if (!c || !mp || !state || nsteps < 0 || !x || !y || !z || !vx || !vy || !vz) return MG_ERR_INVALID;
-    if (mp->scheme != MG_MD_NVE && mp->scheme != MG_MD_NVT_NH)
-        return mg_fail(c, MG_ERR_INVALID, "unknown integration scheme");
-    if (mp->nstep_inner < 1 || !(mp->delt > 0) || !(mp->nfree > 0))
-        return mg_fail(c, MG_ERR_INVALID, "nstep_inner, delt and nfree must be positive");
-    if (mp->scheme == MG_MD_NVT_NH && !(mp->qq > 0 && mp->qqs > 0))
-        return mg_fail(c, MG_ERR_INVALID, "thermostat masses must be positive");
-    if (!c->have_topology || !c->have_params || !c->have_box)
-        return mg_fail(c, MG_ERR_STATE, "set topology, params and box before integrating");
-    cudaSetDevice(c->device);
+namespace {
+
+// buffers and the MdRun of an integration with log_rows per-step records
+mg_status md_prepare(mg_ctx *c, size_t log_rows, MdRun &R) {
     const int n = c->natom;
     const size_t nb3 = sizeof(double) * 3 * (size_t)n;
     const int nb = (n + MD_TPB - 1) / MD_TPB;
     if (!mg_ensure(c, c->d_x, nb3) || !mg_ensure(c, c->d_fl, nb3) || !mg_ensure(c, c->d_fs, nb3) ||
         !mg_ensure(c, c->d_md_v, nb3) || !mg_ensure(c, c->d_md_work, 3 * nb3) ||
-        !mg_ensure(c, c->d_md_rmass, sizeof(double) * n) || !mg_ensure(c, c->d_md_part, sizeof(double) * (nb + 1)) ||
+        !mg_ensure(c, c->d_md_rmass, sizeof(double) * n) ||
+        !mg_ensure(c, c->d_md_part, sizeof(double) * (4 * (size_t)nb + 4)) ||
         !mg_ensure(c, c->d_md_dev, sizeof(MdDev)) ||
-        !mg_ensure(c, c->d_md_log, sizeof(double) * MG_MD_LOG * ((size_t)nsteps + 1)))
+        !mg_ensure(c, c->d_md_log, sizeof(double) * MG_MD_LOG * log_rows))
         return MG_ERR_ALLOC;
-    cudaStream_t s = c->stream;
-    double *dx = (double *)c->d_x.p, *dy = dx + n, *dz = dy + n;
-    double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
-    double *v = (double *)c->d_md_v.p, *w = (double *)c->d_md_work.p;
-    double *dlog = (double *)c->d_md_log.p;
-    const size_t nb1 = sizeof(double) * n;
-    MG_CUDA(cudaMemcpyAsync(dx, x, nb1, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(dy, y, nb1, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(dz, z, nb1, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(v, vx, nb1, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(v + n, vy, nb1, cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemcpyAsync(v + 2 * n, vz, nb1, cudaMemcpyHostToDevice, s));
-    MdDev h0 = {};
-    h0.ps = state->ps;
-    h0.ss = state->ss;
-    h0.pss = state->pss;
-    h0.sss = state->sss;
-    h0.unhts = state->unhts;
-    h0.unhtss = state->unhtss;
-    MG_CUDA(cudaMemcpyAsync(c->d_md_dev.p, &h0, sizeof(MdDev), cudaMemcpyHostToDevice, s));
-    MG_CUDA(cudaMemsetAsync(dlog, 0, sizeof(double) * MG_MD_LOG * ((size_t)nsteps + 1), s));
-    MdRun R;
     R.c = c;
     R.nb = nb;
-    R.s = s;
+    R.s = c->stream;
     MdArgs &A = R.A;
+    double *w = (double *)c->d_md_work.p;
     A.n = n;
-    A.x = dx;
-    A.y = dy;
-    A.z = dz;
-    A.v = v;
+    A.x = (double *)c->d_x.p;
+    A.y = A.x + n;
+    A.z = A.y + n;
+    A.v = (double *)c->d_md_v.p;
     A.vn = w;
     A.vo = w + 3 * (size_t)n;
     A.b = w + 6 * (size_t)n;
     A.rmass = (const double *)c->d_md_rmass.p;
-    A.fl = fl;
-    A.fs = fs;
+    A.fl = (const double *)c->d_fl.p;
+    A.fs = (const double *)c->d_fs.p;
     A.part = (double *)c->d_md_part.p;
     A.s = (MdDev *)c->d_md_dev.p;
-    k_md_rmass<<<nb, MD_TPB, 0, s>>>(n, (const double *)c->d_site_aw.p, (double *)c->d_md_rmass.p);
+    k_md_rmass<<<nb, MD_TPB, 0, R.s>>>(n, (const double *)c->d_site_aw.p, (double *)c->d_md_rmass.p);
     MG_CUDA(cudaGetLastError());
+    return MG_OK;
+}
 
+// nsteps of the scheme from the device state of R: forces at the start (as the reference
+// evaluates them before its loop), the step-0 record and one record per step (device
+// rows dlog; uinter, uintra and ushift of every row in hlog)
+mg_status md_loop(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, double *hlog) {
+    mg_ctx *c = R.c;
+    MdArgs &A = R.A;
+    const int nb = R.nb;
+    cudaStream_t s = R.s;
+    double *dx = A.x, *dy = A.y, *dz = A.z;
+    double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
     const bool nh = mp->scheme == MG_MD_NVT_NH;
     const double dt = mp->delt, h = dt / 2.0, dts = dt / mp->nstep_inner, hs = dts / 2.0;
     const double dt_sqby2 = dt * dt / 2.0, dts_sqby2 = dts * dts / 2.0;
     const double gg_treq = mp->gg * mp->treq, ggs_treq = mp->ggs * mp->treq;
-    std::vector<double> hlog(MG_MD_LOG * ((size_t)nsteps + 1), 0.0);
-
-    // forces at the start, as the reference evaluates them before its loop
+    MG_CUDA(cudaMemsetAsync(dlog, 0, sizeof(double) * MG_MD_LOG * ((size_t)nsteps + 1), s));
     mg_energies e;
     mg_status st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_ALL, fl, fs, &e);
     if (st) return st;
@@ -438,12 +516,69 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
         hlog[(size_t)step * MG_MD_LOG + 2] = uintra;
         hlog[(size_t)step * MG_MD_LOG + 3] = ushift_l + ushift_s;
     }
-    MG_CUDA(cudaMemcpyAsync(x, dx, nb1, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(y, dy, nb1, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(z, dz, nb1, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(vx, v, nb1, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(vy, v + n, nb1, cudaMemcpyDeviceToHost, s));
-    MG_CUDA(cudaMemcpyAsync(vz, v + 2 * n, nb1, cudaMemcpyDeviceToHost, s));
+    return MG_OK;
+}
+
+// merges the device rows with the host-side energies into the caller's log
+void md_merge_log(const double *dl, const double *hlog, size_t rows, double *log) {
+    for (size_t r = 0; r < rows; r++) {
+        double *o = log + r * MG_MD_LOG;
+        const double *d = dl + r * MG_MD_LOG;
+        for (int k = 0; k < MG_MD_LOG; k++) o[k] = d[k];
+        o[1] = hlog[r * MG_MD_LOG + 1];
+        o[2] = hlog[r * MG_MD_LOG + 2];
+        o[3] = hlog[r * MG_MD_LOG + 3];
+    }
+}
+
+mg_status md_check(mg_ctx *c, const mg_md_params *mp) {
+    if (mp->scheme != MG_MD_NVE && mp->scheme != MG_MD_NVT_NH)
+        return mg_fail(c, MG_ERR_INVALID, "unknown integration scheme");
+    if (mp->nstep_inner < 1 || !(mp->delt > 0) || !(mp->nfree > 0))
+        return mg_fail(c, MG_ERR_INVALID, "nstep_inner, delt and nfree must be positive");
+    if (mp->scheme == MG_MD_NVT_NH && !(mp->qq > 0 && mp->qqs > 0))
+        return mg_fail(c, MG_ERR_INVALID, "thermostat masses must be positive");
+    if (!c->have_topology || !c->have_params || !c->have_box)
+        return mg_fail(c, MG_ERR_STATE, "set topology, params and box before integrating");
+    return MG_OK;
+}
+
+}  // namespace
+
+extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, double *x, double *y, double *z,
+                               double *vx, double *vy, double *vz, mg_md_state *state, double *log) {
+    if (!c || !mp || !state || nsteps < 0 || !x || !y || !z || !vx || !vy || !vz) return MG_ERR_INVALID;
+    mg_status st = md_check(c, mp);
+    if (st) return st;
+    cudaSetDevice(c->device);
+    const int n = c->natom;
+    MdRun R;
+    if ((st = md_prepare(c, (size_t)nsteps + 1, R))) return st;
+    cudaStream_t s = R.s;
+    double *dlog = (double *)c->d_md_log.p;
+    const size_t nb1 = sizeof(double) * n;
+    MG_CUDA(cudaMemcpyAsync(R.A.x, x, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.y, y, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.z, z, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.v, vx, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.v + n, vy, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.v + 2 * n, vz, nb1, cudaMemcpyHostToDevice, s));
+    MdDev h0 = {};
+    h0.ps = state->ps;
+    h0.ss = state->ss;
+    h0.pss = state->pss;
+    h0.sss = state->sss;
+    h0.unhts = state->unhts;
+    h0.unhtss = state->unhtss;
+    MG_CUDA(cudaMemcpyAsync(c->d_md_dev.p, &h0, sizeof(MdDev), cudaMemcpyHostToDevice, s));
+    std::vector<double> hlog(MG_MD_LOG * ((size_t)nsteps + 1), 0.0);
+    if ((st = md_loop(R, mp, nsteps, dlog, hlog.data()))) return st;
+    MG_CUDA(cudaMemcpyAsync(x, R.A.x, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(y, R.A.y, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(z, R.A.z, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vx, R.A.v, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vy, R.A.v + n, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vz, R.A.v + 2 * n, nb1, cudaMemcpyDeviceToHost, s));
     MdDev hf;
     MG_CUDA(cudaMemcpyAsync(&hf, c->d_md_dev.p, sizeof(MdDev), cudaMemcpyDeviceToHost, s));
     std::vector<double> dl(hlog.size());
@@ -458,15 +593,108 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
     state->tinst = hf.tinst;
     state->unhts = hf.unhts;
     state->unhtss = hf.unhtss;
-    if (log) {
-        for (size_t r = 0; r <= (size_t)nsteps; r++) {
-            double *o = log + r * MG_MD_LOG;
-            const double *d = dl.data() + r * MG_MD_LOG;
-            for (int k = 0; k < MG_MD_LOG; k++) o[k] = d[k];
-            o[1] = hlog[r * MG_MD_LOG + 1];
-            o[2] = hlog[r * MG_MD_LOG + 2];
-            o[3] = hlog[r * MG_MD_LOG + 3];
-        }
+    if (log) md_merge_log(dl.data(), hlog.data(), (size_t)nsteps + 1, log);
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// simulated annealing (src/siman.c:62-182): stages at T = t_initial / mu_t^k, each a
+// velinit at T, forces, n_tries Nose-Hoover RESPA steps and a reset of the thermostat
+// scalars; the run ends after the first stage whose T is below t_min.
+// ---------------------------------------------------------------------------------
+#define MG_SIMAN_TAG 0x5349u  // fourth Philox counter word of the annealing velocities
+
+extern "C" int mg_siman_stage_count(double t_initial, double t_min, double mu_t, int limit) {
+    if (!(t_initial > 0) || !(mu_t > 1.0) || !(t_min >= 0) || limit < 1) return -1;
+    double T = t_initial;
+    for (int k = 0; k < limit; k++) {
+        if (T < t_min) return k + 1;
+        T /= mu_t;
     }
+    return -1;
+}
+
+extern "C" mg_status mg_siman_run(mg_ctx *c, const mg_siman_params *sp, double *x, double *y, double *z,
+                                  double *vx, double *vy, double *vz, mg_md_state *state, int *nstages,
+                                  double *stage_log) {
+    if (!c || !sp || !state || !nstages || !x || !y || !z || !vx || !vy || !vz) return MG_ERR_INVALID;
+    if (sp->md.scheme != MG_MD_NVT_NH) return mg_fail(c, MG_ERR_INVALID, "annealing runs the Nose-Hoover scheme");
+    if (sp->n_tries < 0) return mg_fail(c, MG_ERR_INVALID, "n_tries must not be negative");
+    mg_md_params mp = sp->md;
+    mp.treq = sp->t_initial;
+    mg_status st = md_check(c, &mp);
+    if (st) return st;
+    const int nst = mg_siman_stage_count(sp->t_initial, sp->t_min, sp->mu_t, sp->max_stages);
+    if (nst < 0)
+        return mg_fail(c, MG_ERR_CAPACITY, "the schedule needs more than max_stages stages (or is invalid)");
+    cudaSetDevice(c->device);
+    const int n = c->natom;
+    MdRun R;
+    if ((st = md_prepare(c, (size_t)sp->n_tries + 1, R))) return st;
+    cudaStream_t s = R.s;
+    double *dlog = (double *)c->d_md_log.p;
+    const size_t nb1 = sizeof(double) * n;
+    MG_CUDA(cudaMemcpyAsync(R.A.x, x, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.y, y, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.z, z, nb1, cudaMemcpyHostToDevice, s));
+    MdDev h0 = {};
+    h0.ps = state->ps;
+    h0.ss = state->ss;
+    h0.pss = state->pss;
+    h0.sss = state->sss;
+    h0.unhts = state->unhts;
+    h0.unhtss = state->unhtss;
+    MG_CUDA(cudaMemcpyAsync(c->d_md_dev.p, &h0, sizeof(MdDev), cudaMemcpyHostToDevice, s));
+    const double *aw = (const double *)c->d_site_aw.p;
+    const uint32_t k0 = (uint32_t)(sp->seed & 0xffffffffull), k1 = (uint32_t)(sp->seed >> 32);
+    std::vector<double> hlog(MG_MD_LOG * ((size_t)sp->n_tries + 1), 0.0), last(MG_MD_LOG);
+    double T = sp->t_initial;
+    for (int k = 0; k < nst; k++) {
+        mp.treq = T;
+        if (k > 0) k_siman_reset<<<1, 1, 0, s>>>(R.A.s);
+        k_vel_draw<<<R.nb, MD_TPB, 0, s>>>(R.A, aw, T, k0, k1, (uint32_t)k, MG_SIMAN_TAG, R.nb);
+        k_vel_momentum<<<1, MD_TPB, 0, s>>>(R.A, R.nb);
+        k_vel_shift<<<R.nb, MD_TPB, 0, s>>>(R.A, aw);
+        k_vel_scale_scalar<<<1, MD_TPB, 0, s>>>(R.A, R.nb, T, (double)mp.nfree);
+        k_vel_scale<<<R.nb, MD_TPB, 0, s>>>(R.A, aw);
+        MG_CUDA(cudaGetLastError());
+        c->launches += 6;
+        if ((st = md_loop(R, &mp, sp->n_tries, dlog, hlog.data()))) return st;
+        MG_CUDA(cudaMemcpyAsync(last.data(), dlog + (size_t)sp->n_tries * MG_MD_LOG, sizeof(double) * MG_MD_LOG,
+                                cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        if (stage_log) {
+            double *o = stage_log + (size_t)k * MG_SIMAN_LOG;
+            const double *hl = hlog.data() + (size_t)sp->n_tries * MG_MD_LOG;
+            o[0] = T;
+            o[1] = last[0];   // ukin
+            o[2] = hl[1];     // uinter
+            o[3] = hl[2];     // uintra
+            o[4] = hl[3];     // ushift
+            o[5] = last[8];   // tinst
+            o[6] = last[9];   // unhts
+            o[7] = last[10];  // unhtss
+        }
+        T /= sp->mu_t;
+    }
+    MG_CUDA(cudaMemcpyAsync(x, R.A.x, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(y, R.A.y, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(z, R.A.z, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vx, R.A.v, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vy, R.A.v + n, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vz, R.A.v + 2 * n, nb1, cudaMemcpyDeviceToHost, s));
+    MdDev hf;
+    MG_CUDA(cudaMemcpyAsync(&hf, c->d_md_dev.p, sizeof(MdDev), cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    MG_CUDA(cudaGetLastError());
+    state->ps = hf.ps;
+    state->ss = hf.ss;
+    state->pss = hf.pss;
+    state->sss = hf.sss;
+    state->ukin = hf.ukin;
+    state->tinst = hf.tinst;
+    state->unhts = hf.unhts;
+    state->unhtss = hf.unhtss;
+    *nstages = nst;
     return MG_OK;
 }

@@ -78,6 +78,10 @@ def load_library(path: str = LIB_PATH):
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.mg_siman_run.argtypes = [V, C.POINTER(capi.MgSimanParams), _dp, _dp, _dp, _dp, _dp, _dp,
+                                 C.POINTER(capi.MgMdState), C.POINTER(I), _dp]
+    lib.mg_siman_stage_count.argtypes = [D, D, D, I]
+    lib.mg_siman_stage_count.restype = I
     lib.mg_force_match.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, D, _dp, _dp, _dp, _dp, C.POINTER(I)]
     _lib = lib
     return lib
@@ -268,6 +272,22 @@ class Engine:
         self._check(self.lib.mg_adjoint_hvp(self.ctx, _p(x), _p(y), _p(z), _p(v[0]), _p(v[1]), _p(v[2]),
                                             _p(h[0]), _p(h[1]), _p(h[2])))
         return h
+
+    def siman_run(self, md: dict, sched: dict, x=None, y=None, z=None, state: dict | None = None):
+        """The reference's simulated annealing on the device (mg_siman_run): md holds the
+        mg_md_params fields (scheme NVT), sched t_initial, t_min, mu_t, n_tries, max_stages
+        and seed. Returns (positions [3, n], velocities [3, n], state, stage log [nstages, 8])."""
+        s = self.system
+        pos = np.ascontiguousarray(np.stack([s.x if x is None else x, s.y if y is None else y,
+                                             s.z if z is None else z]), dtype=np.float64)
+        vel = np.zeros((3, self.n))
+        st = capi.MgMdState(**(state or {}))
+        sp = capi.MgSimanParams.from_dict(md, sched)
+        log = np.zeros((max(1, sched["max_stages"]), capi.SIMAN_LOG))
+        k = C.c_int(0)
+        self._check(self.lib.mg_siman_run(self.ctx, C.byref(sp), _p(pos[0]), _p(pos[1]), _p(pos[2]), _p(vel[0]),
+                                          _p(vel[1]), _p(vel[2]), C.byref(st), C.byref(k), _p(log)))
+        return pos, vel, st.as_dict(), log[:k.value]
 
     def stats(self) -> dict:
         st = MgStats()

@@ -323,3 +323,101 @@ int orc_hmc_replica(const orc_system *s, const mg_hmc_params *hp, int replica, i
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     mg_philox4x32_10(ctr, key, out);
 }
+
+/* ---- simulated annealing (src/siman.c:62-182) -------------------------------------- *
+ * Stages at T = t_initial / mu_t^k until the first stage below t_min has run; each stage
+ * is velinit (src/initvars.c:151-229) with the Philox streams of the engine (counter =
+ * (site, stage, 0 or 1, 0x5349)) in place of gaussran(), then n_tries vver_nh_3 steps
+ * at treq = T, then the thermostat scalars are reset (src/siman.c:167-174). */
+int orc_siman_run(const orc_system *s, const mg_siman_params *sp, double *xx, double *yy, double *zz, double *vx,
+                  double *vy, double *vz, mg_md_state *st, int *nstages, double *stage_log) {
+    const int n = orc_natom(s);
+    double *aw = (double *)calloc((size_t)n, sizeof(double));
+    double *lg = (double *)calloc((size_t)(sp->n_tries + 1) * MG_MD_LOG, sizeof(double));
+    if (!aw || !lg) {
+        free(aw);
+        free(lg);
+        return -1;
+    }
+    double sysm = 0.0;
+    for (int q = 0, a = 0; q < s->nspecies; q++)
+        for (int m = 0; m < s->sp[q].nmole; m++)
+            for (int k = 0; k < s->sp[q].natom; k++) {
+                aw[a] = s->sp[q].aw[k];
+                sysm += aw[a];
+                a++;
+            }
+    const uint32_t key[2] = {(uint32_t)(sp->seed & 0xffffffffull), (uint32_t)(sp->seed >> 32)};
+    int nst = 0;
+    double T = sp->t_initial;
+    for (;;) {
+        if (nst >= sp->max_stages) {
+            free(aw);
+            free(lg);
+            return -2;
+        }
+        if (nst > 0) {
+            st->ps = st->ss = st->pss = st->sss = 0.0;
+            st->unhts = st->unhtss = 0.0;
+        }
+        double px = 0.0, py = 0.0, pz = 0.0;
+        const double stdvtmp = sqrt(T);
+        for (int i = 0; i < n; i++) {
+            const uint32_t c0[4] = {(uint32_t)i, (uint32_t)nst, 0u, 0x5349u};
+            const uint32_t c1[4] = {(uint32_t)i, (uint32_t)nst, 1u, 0x5349u};
+            uint32_t w0[4], w1[4];
+            double g0, g1, g2, g3;
+            mg_philox4x32_10(c0, key, w0);
+            mg_philox4x32_10(c1, key, w1);
+            mg_gauss2(w0, &g0, &g1);
+            mg_gauss2(w1, &g2, &g3);
+            const double stdv = stdvtmp / sqrt(aw[i]);
+            vx[i] = stdv * g0;
+            vy[i] = stdv * g1;
+            vz[i] = stdv * g2;
+            px += vx[i] * aw[i];
+            py += vy[i] * aw[i];
+            pz += vz[i] * aw[i];
+        }
+        px /= sysm;
+        py /= sysm;
+        pz /= sysm;
+        double ukin = 0.0;
+        for (int i = 0; i < n; i++) {
+            vx[i] -= px;
+            vy[i] -= py;
+            vz[i] -= pz;
+            ukin += aw[i] * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        }
+        ukin = 0.5 * ukin;
+        const double scaling = sqrt(T / (2.0 * ukin / sp->md.nfree));
+        for (int i = 0; i < n; i++) {
+            vx[i] *= scaling;
+            vy[i] *= scaling;
+            vz[i] *= scaling;
+        }
+        mg_md_params mp = sp->md;
+        mp.treq = T;
+        orc_md_run(s, &mp, sp->n_tries, xx, yy, zz, vx, vy, vz, st, lg);
+        if (stage_log) {
+            const double *r = lg + (size_t)sp->n_tries * MG_MD_LOG;
+            double *o = stage_log + (size_t)nst * MG_SIMAN_LOG;
+            o[0] = T;
+            o[1] = r[0];
+            o[2] = r[1];
+            o[3] = r[2];
+            o[4] = r[3];
+            o[5] = r[8];
+            o[6] = r[9];
+            o[7] = r[10];
+        }
+        nst++;
+        const int done = T < sp->t_min;
+        T /= sp->mu_t;
+        if (done) break;
+    }
+    *nstages = nst;
+    free(aw);
+    free(lg);
+    return 0;
+}

@@ -14,8 +14,8 @@ import tempfile
 
 import numpy as np
 
-from mspms2_gb300.capi import (ENERGY_NAMES, MD_LOG, MgEnergies, MgHmcParams, MgMdParams, MgMdState, MgParams,
-                               MgSpecies, SpeciesPack, system_params)
+from mspms2_gb300.capi import (ENERGY_NAMES, MD_LOG, SIMAN_LOG, MgEnergies, MgHmcParams, MgMdParams, MgMdState,
+                               MgParams, MgSimanParams, MgSpecies, SpeciesPack, system_params)
 from mspms2_gb300.system import System, write_reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -80,6 +80,8 @@ def lib():
                                     _dp, C.POINTER(MgMdState), _dp]
         _lib.orc_hmc_replica.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgHmcParams), C.c_int, C.c_int, C.c_int,
                                          _dp, _dp, _dp, C.POINTER(C.c_int), _dp, _dp]
+        _lib.orc_siman_run.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgSimanParams), _dp, _dp, _dp, _dp, _dp, _dp,
+                                       C.POINTER(MgMdState), C.POINTER(C.c_int), _dp]
         _lib.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         _lib.orc_philox4x32_10.restype = None
         _lib.orc_tasos_min_pe.argtypes = [C.POINTER(OrcTasos)]
@@ -193,6 +195,22 @@ class Oracle:
         lib().orc_hmc_replica(C.byref(self.s), C.byref(MgHmcParams(**hp)), replica, move0, nmoves, _ptr(pos[0]),
                               _ptr(pos[1]), _ptr(pos[2]), C.byref(acc), _ptr(dh), C.byref(energy))
         return pos, acc.value, energy.value, dh[:nmoves]
+
+    def siman_run(self, md: dict, sched: dict, state: dict | None = None):
+        """The restated simulated annealing (oracle/md_oracle.c), same contract as
+        Engine.siman_run: (positions, velocities, state, stage log)."""
+        sysm = self.system
+        pos = np.ascontiguousarray(np.stack([sysm.x, sysm.y, sysm.z]), dtype=np.float64)
+        vel = np.zeros((3, sysm.natom))
+        st = MgMdState(**(state or {}))
+        log = np.zeros((max(1, sched["max_stages"]), SIMAN_LOG))
+        k = C.c_int(0)
+        rc = lib().orc_siman_run(C.byref(self.s), C.byref(MgSimanParams.from_dict(md, sched)), _ptr(pos[0]),
+                                 _ptr(pos[1]), _ptr(pos[2]), _ptr(vel[0]), _ptr(vel[1]), _ptr(vel[2]), C.byref(st),
+                                 C.byref(k), _ptr(log))
+        if rc != 0:
+            raise RuntimeError(f"orc_siman_run failed ({rc})")
+        return pos, vel, st.as_dict(), log[:k.value]
 
     def count_pairs(self, r: float) -> int:
         s = self.system

@@ -1,0 +1,97 @@
+"""Simulated annealing (siman, src/siman.c:62-182): stages of velinit + Nose-Hoover RESPA
+at decreasing temperatures.
+
+CPU: the library's stage count (mg_siman_stage_count, callable without a GPU) matches the
+oracle's restated loop, which ends after the first stage below t_min; velinit of the
+oracle gives zero momentum and exactly the stage temperature.
+GPU: mg_siman_run, through the C ABI, reproduces the oracle's run (same Philox streams)
+stage by stage. Tolerances as for the integrators: FP64 path 1e-9, mixed path 1e-5.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from mspms2_gb300.capi import SIMAN_LOG_NAMES
+from mspms2_gb300.system import load_system, md_params
+
+
+def water():
+    s, _ = load_system(os.path.join(GOLDEN, "water_wolf_216.npz"))
+    s.delt_fs, s.nstep_inner = 0.5, 2
+    md = md_params(s)
+    md["scheme"] = 1
+    return s, md
+
+
+def sched(s, **kw):
+    d = dict(t_initial=600.0 / s.epsilon_base, t_min=300.0 / s.epsilon_base, mu_t=1.3, n_tries=3, max_stages=8,
+             seed=20240611)
+    d.update(kw)
+    return d
+
+
+def test_stage_count_matches_oracle_loop():
+    from mspms2_gb300 import build
+    from oracle.pyoracle import Oracle
+    lib = C.CDLL(build.build())
+    lib.mg_siman_stage_count.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int]
+    lib.mg_siman_stage_count.restype = C.c_int
+    for t0, tmin, mu in [(600.0, 300.0, 1.3), (500.0, 499.0, 1.001), (300.0, 300.0, 1.1), (300.0, 299.0, 2.0)]:
+        T, k = t0, 0
+        while True:
+            k += 1
+            if T < tmin:
+                break
+            T /= mu
+        assert lib.mg_siman_stage_count(t0, tmin, mu, 10000) == k
+    assert lib.mg_siman_stage_count(600.0, 300.0, 1.3, 3) == -1   # needs 4 stages
+    assert lib.mg_siman_stage_count(600.0, 300.0, 1.0, 100) == -1  # no cooling
+    # the oracle's restated loop runs the same number of stages, at these temperatures
+    s, md = water()
+    s.species[0].nmole = 8  # a small box keeps the CPU run short
+    n = 3 * 8
+    s.x, s.y, s.z = s.x[:n], s.y[:n], s.z[:n]
+    pos, vel, st, log = Oracle(s).siman_run(md, sched(s, n_tries=1))
+    assert len(log) == lib.mg_siman_stage_count(600.0, 300.0, 1.3, 8) == 4
+    assert np.allclose(log[:, 0], 600.0 / 1.3 ** np.arange(4), rtol=1e-15)
+
+
+def test_oracle_velinit_zero_momentum_and_temperature():
+    from oracle.pyoracle import Oracle
+    s, md = water()
+    pos, vel, st, log = Oracle(s).siman_run(md, sched(s, n_tries=0, t_min=599.0, max_stages=2))
+    m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+    assert np.abs((vel * m).sum(1)).max() <= 1e-12 * np.abs(vel * m).sum()
+    T = (m * (vel ** 2).sum(0)).sum() / md["nfree"]
+    assert abs(T - log[-1, 0]) <= 1e-12 * T
+    assert abs(log[-1, 5] - log[-1, 0]) <= 1e-12 * log[-1, 0]  # tinst after 0 steps
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_engine_siman_matches_oracle(prec):
+    from mspms2_gb300 import build
+    from mspms2_gb300.engine import Engine
+    from oracle.pyoracle import Oracle
+    build.build()
+    s, md = water()
+    sc = sched(s)
+    start = np.stack([s.x, s.y, s.z]).copy()
+    rpos, rvel, rst, rlog = Oracle(s).siman_run(md, sc)
+    with Engine(s, precision=prec) as eng:
+        pos, vel, st, log = eng.siman_run(md, sc)
+    tol = 1e-9 if prec == "fp64" else 1e-5
+    assert log.shape == rlog.shape
+    escale = np.abs(rlog[:, 1:5]).max()
+    for k, name in enumerate(SIMAN_LOG_NAMES):
+        scale = escale if name in ("uinter", "uintra", "ushift") else max(np.abs(rlog[:, k]).max(), 1e-300)
+        err = np.abs(log[:, k] - rlog[:, k]).max() / scale
+        assert err <= tol, (prec, name, err)
+    d = np.linalg.norm((pos - start) - (rpos - start)) / np.linalg.norm(rpos - start)
+    assert d <= tol, (prec, "displacement", d)
+    assert np.linalg.norm(vel - rvel) / np.linalg.norm(rvel) <= tol
+    for k in ("ps", "pss"):
+        assert abs(st[k] - rst[k]) <= tol * max(abs(rst[k]), 1e-12), (prec, k, st[k], rst[k])
