@@ -294,6 +294,38 @@ typedef struct mg_md_state {
 MG_API mg_status mg_md_run(mg_ctx *ctx, const mg_md_params *p, int nsteps, double *x, double *y, double *z,
                            double *vx, double *vy, double *vz, mg_md_state *state, double *log);
 
+/* ---- NPT (npt_respa, src/nptnh.c:10-234) ------------------------------------------ */
+/* Isotropic Nose-Hoover thermostat + barostat around a RESPA step: the operator
+ * npt_nh_operator() (src/nptnh.c:10-132) before and after the step, inner steps that
+ * scale positions by exp(dt_inner/2 vbs) around the drift and the box by exp(dt_inner vbs),
+ * with the LJ long-range correction (src/misc.c:131-148, terms of src/initvars.c:476-520
+ * when lj_lrc is set) and the Ewald box constants refreshed every inner step. */
+typedef struct mg_npt_params {
+    int nstep_inner;
+    double delt, treq, preq;  /* reduced: time, temperature, pressure (bar / pressure_base) */
+    double qts, qbs;          /* thermostat and barostat masses (MDNPT section) */
+    int nfree;                /* 3*natom - nconstraint */
+    int lj_lrc;               /* isLJlrcOn: add the LJ long-range pressure correction */
+} mg_npt_params;
+
+typedef struct mg_npt_state {
+    double vts, vbs, rts;     /* thermostat velocity, barostat velocity, thermostat position */
+    double utsbs, ukin, tinst, pinst;
+} mg_npt_state;
+
+/* Values recorded per step by mg_npt_run: ukin, uinter, uintra, ushift, vts, vbs, rts,
+ * utsbs, tinst, pinst, boxlx, boxv. Row 0 (the start) holds pinst of the start forces
+ * (the reference leaves pinst unset until its first step). */
+#define MG_NPT_LOG 12
+
+/* Runs nsteps npt_respa steps on the device. x, y, z, vx, vy, vz [natom] and box[3] hold
+ * the start and receive the end; the context's box and Ewald constants follow the box.
+ * state holds vts, vbs, rts at the start (init_npt_respa, src/initvars.c:378-380, sets
+ * vts = sqrt((nfree+1)/qts), vbs = sqrt((nfree+1)/qbs), rts = 0) and receives the end.
+ * log, if not NULL, receives (nsteps+1)*MG_NPT_LOG doubles. */
+MG_API mg_status mg_npt_run(mg_ctx *ctx, const mg_npt_params *p, int nsteps, double *x, double *y, double *z,
+                            double *vx, double *vy, double *vz, double *box, mg_npt_state *state, double *log);
+
 /* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
 /* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
  * first stage whose T is below t_min (the reference tests T < t_min after the stage). A

@@ -78,6 +78,26 @@ class MgMdParams(C.Structure):
         return cls(**{k: d[k] for k, _ in cls._fields_})
 
 
+class MgNptParams(C.Structure):
+    _fields_ = [("nstep_inner", C.c_int), ("delt", C.c_double), ("treq", C.c_double), ("preq", C.c_double),
+                ("qts", C.c_double), ("qbs", C.c_double), ("nfree", C.c_int), ("lj_lrc", C.c_int)]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "MgNptParams":
+        return cls(**{k: d[k] for k, _ in cls._fields_})
+
+
+class MgNptState(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("vts", "vbs", "rts", "utsbs", "ukin", "tinst", "pinst")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+NPT_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "vts", "vbs", "rts", "utsbs", "tinst", "pinst", "boxlx",
+                 "boxv"]
+
+
 class MgSimanParams(C.Structure):
     _fields_ = [("md", MgMdParams), ("t_initial", C.c_double), ("t_min", C.c_double), ("mu_t", C.c_double),
                 ("n_tries", C.c_int), ("max_stages", C.c_int), ("seed", C.c_ulonglong)]

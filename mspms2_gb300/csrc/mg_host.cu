@@ -297,6 +297,8 @@ extern "C" mg_status mg_set_topology(mg_ctx *c, int nspecies, const mg_species *
     c->nmole = nmole;
     c->nspecies = nspecies;
     c->species.clear();
+    c->h_tmpl_eps.clear();
+    c->h_tmpl_sig.clear();
     c->h_site_mol.assign(natom, 0);
     c->h_site_species.assign(natom, 0);
     c->h_site_rel.assign(natom, 0);
@@ -374,6 +376,8 @@ extern "C" mg_status mg_set_topology(mg_ctx *c, int nspecies, const mg_species *
         }
         d.nbonded = (int)bonded.size() - d.bonded_off;
         c->max_mol_atoms = std::max(c->max_mol_atoms, S.natom);
+        c->h_tmpl_eps.emplace_back(S.epsilon, S.epsilon + S.natom);
+        c->h_tmpl_sig.emplace_back(S.sigma, S.sigma + S.natom);
         for (int m = 0; m < S.nmole; m++, mole++)
             for (int a = 0; a < S.natom; a++, site++) {
                 c->h_site_mol[site] = mole;

@@ -120,6 +120,7 @@ struct mg_ctx {
     int natom = 0, nmole = 0, nspecies = 0;
     std::vector<SpeciesDev> species;
     std::vector<int> h_site_mol, h_site_species, h_site_rel;
+    std::vector<std::vector<double>> h_tmpl_eps, h_tmpl_sig;  // per species template (LJ corrections)
     std::vector<double> h_site_q;
     double sum_q2 = 0.0;
     int max_mol_atoms = 0;

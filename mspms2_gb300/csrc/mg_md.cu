@@ -363,6 +363,45 @@ __global__ void k_vel_scale(MdArgs A, const double *__restrict__ aw) {
     block_partial(m2, A.part);
 }
 
+// ---- NPT (src/nptnh.c) ------------------------------------------------------------
+// partial of sum v^2 / r_mass (the operator's mvsq, src/nptnh.c:22-28)
+__global__ void k_npt_mvsq(MdArgs A) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double m2 = 0.0;
+    if (a < A.n) {
+        const int n = A.n;
+        m2 = (A.v[a] * A.v[a] + A.v[n + a] * A.v[n + a] + A.v[2 * n + a] * A.v[2 * n + a]) / A.rmass[a];
+    }
+    block_partial(m2, A.part);
+}
+
+__global__ void k_npt_mvsq_scalar(MdArgs A, int nb) {
+    const double t = sum_partials(A.part, nb);
+    if (threadIdx.x == 0) A.s->sumv2 = t;
+}
+
+// v *= AA (src/nptnh.c:89-94)
+__global__ void k_npt_scale_v(MdArgs A, double aa) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < 3 * A.n) A.v[a] = A.v[a] * aa;
+}
+
+// inner step of npt_respa (src/nptnh.c:155-176): v += hs fs r_mass, x = ((x AA) + dts v) AA
+__global__ void k_npt_inner(MdArgs A, double hs, double dts, double aa) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A.n) return;
+    const double r = A.rmass[a];
+    const int n = A.n;
+    double *pos[3] = {A.x, A.y, A.z};
+    for (int d = 0; d < 3; d++) {
+        const double v = A.v[d * n + a] + (hs * A.fs[d * n + a] * r);
+        A.v[d * n + a] = v;
+        double x = pos[d][a] * aa;
+        x = x + dts * v;
+        pos[d][a] = x * aa;
+    }
+}
+
 // the thermostat scalars a new annealing stage starts from (src/siman.c:167-174)
 __global__ void k_siman_reset(MdDev *s) {
     s->ps = s->ss = s->pss = s->sss = 0.0;
@@ -696,5 +735,194 @@ extern "C" mg_status mg_siman_run(mg_ctx *c, const mg_siman_params *sp, double *
     state->unhts = hf.unhts;
     state->unhtss = hf.unhtss;
     *nstages = nst;
+    return MG_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// NPT: npt_respa (src/nptnh.c:134-234) around npt_nh_operator (src/nptnh.c:10-132). The
+// operator's scalar updates are a handful of FP64 operations on the host, in the
+// reference's order, from sum m v^2 reduced on the device; the host also owns the box,
+// which changes every inner step (list, k-vectors and Ewald constants follow it).
+// ---------------------------------------------------------------------------------
+namespace {
+
+struct NptScalars {
+    double vts, vbs, rts, utsbs, ukin, tinst, pinst, pljlrc;
+};
+
+// the LJ long-range pressure correction (src/misc.c:131-148) with the species-pair terms
+// of src/initvars.c:476-520
+double npt_pljlrc(const mg_ctx *c, int lj_lrc, double boxv) {
+    if (!lj_lrc) return 0.0;
+    const double pi = 3.141592653589793, rc = c->params.rcutoff;
+    const double t1 = (32.0 / 9.0) * pi * pow(rc, -9.0), t2 = -(16.0 / 3.0) * pi * pow(rc, -3.0);
+    double p = 0.0;
+    for (int m = 0; m < c->nspecies; m++)
+        for (int nn = 0; nn < c->nspecies; nn++) {
+            double term = 0.0;
+            for (size_t i = 0; i < c->h_tmpl_sig[m].size(); i++)
+                for (size_t j = 0; j < c->h_tmpl_sig[nn].size(); j++) {
+                    const double sij = 0.5 * (c->h_tmpl_sig[m][i] + c->h_tmpl_sig[nn][j]);
+                    const double eij = sqrt(c->h_tmpl_eps[m][i] * c->h_tmpl_eps[nn][j]);
+                    term += (pow(sij, 9.0) * t1 + pow(sij, 3.0) * t2) * (eij * pow(sij, 3.0));
+                }
+            p += (term * c->species[m].nmole * c->species[nn].nmole / boxv / boxv);
+        }
+    return p;
+}
+
+mg_status npt_operator(MdRun &R, const mg_npt_params *mp, double virial, double boxv, NptScalars &q) {
+    mg_ctx *c = R.c;
+    k_npt_mvsq<<<R.nb, MD_TPB, 0, R.s>>>(R.A);
+    k_npt_mvsq_scalar<<<1, MD_TPB, 0, R.s>>>(R.A, R.nb);
+    double mvsq = 0.0;
+    MG_CUDA(cudaMemcpyAsync(&mvsq, &R.A.s->sumv2, sizeof(double), cudaMemcpyDeviceToHost, R.s));
+    MG_CUDA(cudaStreamSynchronize(R.s));
+    const double nfree = mp->nfree, treq = mp->treq, qts = mp->qts, qbs = mp->qbs, preq = mp->preq;
+    const double N_plus1RT = (nfree + 1) * treq, one_3N = 1.0 + 3.0 / nfree;
+    const double dt_outer2 = mp->delt / 2.0, dt_outer4 = mp->delt / 4.0, dt_outer8 = mp->delt / 8.0;
+    const double pdiff = virial + q.pljlrc * boxv * 3.0 - preq * boxv * 3.0;
+    double Gts = (mvsq + qbs * q.vbs * q.vbs - N_plus1RT) / qts;
+    q.vts = q.vts + dt_outer4 * Gts;
+    const double BB = exp(-q.vts * dt_outer8);
+    q.vbs = q.vbs * BB;
+    double Gbs = (one_3N * mvsq + pdiff) / qbs;
+    q.vbs = q.vbs + dt_outer4 * Gbs;
+    q.vbs = q.vbs * BB;
+    q.rts = q.rts + dt_outer2 * q.vts;
+    const double AA = exp(-dt_outer2 * (q.vts + one_3N * q.vbs));
+    k_npt_scale_v<<<(3 * R.A.n + MD_TPB - 1) / MD_TPB, MD_TPB, 0, R.s>>>(R.A, AA);
+    MG_CUDA(cudaGetLastError());
+    c->launches += 3;
+    q.vbs = q.vbs * BB;
+    mvsq = mvsq * AA * AA;
+    Gbs = (one_3N * mvsq + pdiff) / qbs;
+    q.vbs = q.vbs + dt_outer4 * Gbs;
+    q.vbs = q.vbs * BB;
+    Gts = (mvsq + qbs * q.vbs * q.vbs - N_plus1RT) / qts;
+    q.vts = q.vts + dt_outer4 * Gts;
+    q.utsbs = 0.5 * qbs * q.vbs * q.vbs + 0.5 * qts * q.vts * q.vts + (nfree + 1) * treq * q.rts + preq * boxv;
+    q.ukin = mvsq / 2.0;
+    q.tinst = 2.0 * q.ukin / nfree;
+    q.pinst = R.A.n / boxv * q.tinst + virial / 3.0 / boxv + q.pljlrc;
+    return MG_OK;
+}
+
+// the new box and the box constants the reference refreshes (src/nptnh.c:178-199)
+void npt_set_box(mg_ctx *c, double lx, double ly, double lz) {
+    const double pi = 3.141592653589793;
+    c->lx = lx;
+    c->ly = ly;
+    c->lz = lz;
+    c->list_valid = false;
+    const double boxv = lx * ly * lz;
+    if (c->params.charge_type == MG_ELEC_EWALD) {
+        c->params.vfactor_ewald = 2.0 * pi / boxv;
+        c->params.twopi_lx = 2.0 * pi / lx;
+        c->params.twopi_ly = 2.0 * pi / ly;
+        c->params.twopi_lz = 2.0 * pi / lz;
+        c->params.twopi_over_3v = 2.0 * pi / 3.0 / boxv;
+    }
+}
+
+void npt_record(double *row, const NptScalars &q, const mg_energies &el, const mg_energies &es, double lx,
+                double boxv) {
+    if (!row) return;
+    const double r[MG_NPT_LOG] = {q.ukin,  el.uinter + es.uinter, es.uintra, el.ushift + es.ushift,
+                                  q.vts,   q.vbs,                 q.rts,     q.utsbs,
+                                  q.tinst, q.pinst,               lx,        boxv};
+    for (int k = 0; k < MG_NPT_LOG; k++) row[k] = r[k];
+}
+
+}  // namespace
+
+extern "C" mg_status mg_npt_run(mg_ctx *c, const mg_npt_params *mp, int nsteps, double *x, double *y, double *z,
+                                double *vx, double *vy, double *vz, double *box, mg_npt_state *state, double *log) {
+    if (!c || !mp || !state || !box || nsteps < 0 || !x || !y || !z || !vx || !vy || !vz) return MG_ERR_INVALID;
+    if (mp->nstep_inner < 1 || !(mp->delt > 0) || !(mp->nfree > 0) || !(mp->qts > 0 && mp->qbs > 0))
+        return mg_fail(c, MG_ERR_INVALID, "nstep_inner, delt, nfree and the masses must be positive");
+    if (!(box[0] > 0 && box[1] > 0 && box[2] > 0)) return mg_fail(c, MG_ERR_INVALID, "box lengths must be positive");
+    if (!c->have_topology || !c->have_params)
+        return mg_fail(c, MG_ERR_STATE, "set topology and params before integrating");
+    cudaSetDevice(c->device);
+    const int n = c->natom;
+    MdRun R;
+    mg_status st = md_prepare(c, 1, R);
+    if (st) return st;
+    cudaStream_t s = R.s;
+    const size_t nb1 = sizeof(double) * n;
+    MG_CUDA(cudaMemcpyAsync(R.A.x, x, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.y, y, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.z, z, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.v, vx, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.v + n, vy, nb1, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(R.A.v + 2 * n, vz, nb1, cudaMemcpyHostToDevice, s));
+    npt_set_box(c, box[0], box[1], box[2]);
+    c->have_box = true;
+    double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
+    const double h = mp->delt / 2.0, dts = mp->delt / mp->nstep_inner, hs = dts / 2.0;
+    double boxv = c->lx * c->ly * c->lz;
+    NptScalars q = {};
+    q.vts = state->vts;
+    q.vbs = state->vbs;
+    q.rts = state->rts;
+    q.pljlrc = npt_pljlrc(c, mp->lj_lrc, boxv);
+    mg_energies el, es;
+    if ((st = mg_compute_forces(c, R.A.x, R.A.y, R.A.z, MG_TERMS_ALL, fl, fs, &el))) return st;
+    es = el;
+    el.uintra = 0.0;
+    es.uinter = es.ushift = es.virial_inter = 0.0;
+    {  // start record: kinetic energy of the given velocities, pressure of the start forces
+        k_npt_mvsq<<<R.nb, MD_TPB, 0, s>>>(R.A);
+        k_npt_mvsq_scalar<<<1, MD_TPB, 0, s>>>(R.A, R.nb);
+        double mvsq = 0.0;
+        MG_CUDA(cudaMemcpyAsync(&mvsq, &R.A.s->sumv2, sizeof(double), cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        q.ukin = mvsq / 2.0;
+        q.tinst = 2.0 * q.ukin / mp->nfree;
+        q.utsbs = 0.5 * mp->qbs * q.vbs * q.vbs + 0.5 * mp->qts * q.vts * q.vts +
+                  (mp->nfree + 1) * mp->treq * q.rts + mp->preq * boxv;
+        q.pinst = n / boxv * q.tinst + (el.virial_inter + es.virial_intra) / 3.0 / boxv + q.pljlrc;
+        npt_record(log, q, el, es, c->lx, boxv);
+    }
+    for (int step = 1; step <= nsteps; step++) {
+        if ((st = npt_operator(R, mp, el.virial_inter + es.virial_inter + es.virial_intra, boxv, q))) return st;
+        k_md_kick<<<R.nb, MD_TPB, 0, s>>>(R.A, fl, h, 0, 0);
+        for (int ll = 0; ll < mp->nstep_inner; ll++) {
+            const double AA = exp(hs * q.vbs);
+            k_npt_inner<<<R.nb, MD_TPB, 0, s>>>(R.A, hs, dts, AA);
+            MG_CUDA(cudaGetLastError());
+            c->launches += 1;
+            const double ef = exp(dts * q.vbs);
+            npt_set_box(c, c->lx * ef, c->ly * ef, c->lz * ef);
+            boxv = c->lx * c->ly * c->lz;
+            q.pljlrc = npt_pljlrc(c, mp->lj_lrc, boxv);
+            if ((st = mg_compute_forces(c, R.A.x, R.A.y, R.A.z, MG_TERMS_SHORT, fl, fs, &es))) return st;
+            k_md_kick<<<R.nb, MD_TPB, 0, s>>>(R.A, fs, hs, 0, 0);
+        }
+        if ((st = mg_compute_forces(c, R.A.x, R.A.y, R.A.z, MG_TERMS_LONG, fl, fs, &el))) return st;
+        k_md_kick<<<R.nb, MD_TPB, 0, s>>>(R.A, fl, h, 0, 0);
+        MG_CUDA(cudaGetLastError());
+        if ((st = npt_operator(R, mp, el.virial_inter + es.virial_inter + es.virial_intra, boxv, q))) return st;
+        npt_record(log ? log + (size_t)step * MG_NPT_LOG : nullptr, q, el, es, c->lx, boxv);
+    }
+    MG_CUDA(cudaMemcpyAsync(x, R.A.x, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(y, R.A.y, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(z, R.A.z, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vx, R.A.v, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vy, R.A.v + n, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(vz, R.A.v + 2 * n, nb1, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaStreamSynchronize(s));
+    MG_CUDA(cudaGetLastError());
+    box[0] = c->lx;
+    box[1] = c->ly;
+    box[2] = c->lz;
+    state->vts = q.vts;
+    state->vbs = q.vbs;
+    state->rts = q.rts;
+    state->utsbs = q.utsbs;
+    state->ukin = q.ukin;
+    state->tinst = q.tinst;
+    state->pinst = q.pinst;
     return MG_OK;
 }

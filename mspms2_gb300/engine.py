@@ -78,6 +78,8 @@ def load_library(path: str = LIB_PATH):
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.mg_npt_run.argtypes = [V, C.POINTER(capi.MgNptParams), I, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                               C.POINTER(capi.MgNptState), _dp]
     lib.mg_siman_run.argtypes = [V, C.POINTER(capi.MgSimanParams), _dp, _dp, _dp, _dp, _dp, _dp,
                                  C.POINTER(capi.MgMdState), C.POINTER(I), _dp]
     lib.mg_siman_stage_count.argtypes = [D, D, D, I]
@@ -272,6 +274,23 @@ class Engine:
         self._check(self.lib.mg_adjoint_hvp(self.ctx, _p(x), _p(y), _p(z), _p(v[0]), _p(v[1]), _p(v[2]),
                                             _p(h[0]), _p(h[1]), _p(h[2])))
         return h
+
+    def npt_run(self, nsteps: int, npt: dict, v, state: dict, box=None, x=None, y=None, z=None):
+        """nsteps of the reference's npt_respa on the device (mg_npt_run): npt holds the
+        mg_npt_params fields (mspms2_gb300.system.npt_params), state vts, vbs, rts
+        (system.npt_state0 for a new run). Returns (positions [3, n], velocities [3, n],
+        box [3], state, log [(nsteps+1), 12])."""
+        s = self.system
+        pos = np.ascontiguousarray(np.stack([s.x if x is None else x, s.y if y is None else y,
+                                             s.z if z is None else z]), dtype=np.float64)
+        vel = np.ascontiguousarray(v, dtype=np.float64).copy()
+        bx = np.ascontiguousarray(s.box if box is None else box, dtype=np.float64).copy()
+        st = capi.MgNptState(**{k: state[k] for k in ("vts", "vbs", "rts")})
+        log = np.zeros((nsteps + 1, capi.MD_LOG))
+        self._check(self.lib.mg_npt_run(self.ctx, C.byref(capi.MgNptParams.from_dict(npt)), nsteps, _p(pos[0]),
+                                        _p(pos[1]), _p(pos[2]), _p(vel[0]), _p(vel[1]), _p(vel[2]), _p(bx),
+                                        C.byref(st), _p(log)))
+        return pos, vel, bx, st.as_dict(), log
 
     def siman_run(self, md: dict, sched: dict, x=None, y=None, z=None, state: dict | None = None):
         """The reference's simulated annealing on the device (mg_siman_run): md holds the

@@ -133,6 +133,8 @@ class System:
     nconstraint: int = 0
     nh_qq: float = 1000.0  # Nose-Hoover masses of the MDNVT section (outer, inner)
     nh_qqs: float = 1000.0
+    npt_qts: float = 1.0e3  # thermostat and barostat masses of the MDNPT section
+    npt_qbs: float = 1.0e3
     nstep: int = 10
     # solid-fluid data
     tasos: list = field(default_factory=list)
@@ -232,6 +234,26 @@ def md_params(s: System) -> dict:
     return dict(scheme=s.what_ensemble, nstep_inner=s.nstep_inner, delt=s.delt_fs / time_base(s),
                 treq=s.treq_K / s.epsilon_base, qq=s.nh_qq, qqs=s.nh_qqs, gg=float(nfree), ggs=float(nfree),
                 nfree=nfree)
+
+
+def pressure_base(s: System) -> float:
+    """Reduced pressure unit in bar (src/readins.c:39)."""
+    return BOLTZMANN * s.epsilon_base * 1.0e25 / (s.sigma_base ** 3)
+
+
+def npt_params(s: System) -> dict:
+    """mg_npt_params of the system's MD settings: delt, treq and preq reduced as
+    src/readins.c:44-47 and :72-73 do, nfree = 3*natom - nconstraint, the MDNPT masses
+    (src/initvars.c:375) and the LJ long-range correction switch (isLJlrcOn)."""
+    nfree = 3 * s.natom - s.nconstraint
+    return dict(nstep_inner=s.nstep_inner, delt=s.delt_fs / time_base(s), treq=s.treq_K / s.epsilon_base,
+                preq=s.preq_bar / pressure_base(s), qts=s.npt_qts, qbs=s.npt_qbs, nfree=nfree, lj_lrc=s.lj_lrc)
+
+
+def npt_state0(s: System) -> dict:
+    """The thermostat/barostat start of init_npt_respa (src/initvars.c:378-384)."""
+    nfree = 3 * s.natom - s.nconstraint
+    return dict(vts=math.sqrt((nfree + 1.0) / s.npt_qts), vbs=math.sqrt((nfree + 1.0) / s.npt_qbs), rts=0.0)
 
 
 def _first(line: str) -> str:
@@ -405,6 +427,9 @@ def read_reference_dir(path: str) -> System:
     k = _find_section(lines, "MDNVT")
     if k is not None:
         s.nh_qq, s.nh_qqs = (float(v) for v in lines[k].split()[:2])
+    k = _find_section(lines, "MDNPT")
+    if k is not None:
+        s.npt_qts, s.npt_qbs = (float(v) for v in lines[k].split()[:2])
     if charge_type in (ELEC_EWALD, ELEC_WOLF, ELEC_SIMPLE_COULOMB):
         k = _find_section(lines, "ELECTROSTATIC")
         if k is None:
@@ -500,7 +525,8 @@ def write_reference_dir(s: System, path: str, grid_names=None) -> None:
                   f"{s.ksqmax}", f"{s.ewald_bc}", f"{s.ewald_dim}"]
     else:
         lines += [_fmt(s.kappa / sb)]
-    lines += ["", "MDNVT", f"{_fmt(s.nh_qq)} {_fmt(s.nh_qqs)}", "", "MDNPT", "1.0e3 1.0e3", ""]
+    lines += ["", "MDNVT", f"{_fmt(s.nh_qq)} {_fmt(s.nh_qqs)}", "", "MDNPT", f"{_fmt(s.npt_qts)} {_fmt(s.npt_qbs)}",
+              ""]
     if s.sf_type == SF_HYPERGEO:
         lines += ["HyperGeo", f"{len(s.tube_xy_r)}", _fmt(s.solid_sigma * sb), _fmt(s.solid_epsilon * eb)]
         lines += [" ".join(_fmt(v * sb) for v in row) for row in s.tube_xy_r]
@@ -596,7 +622,8 @@ _SCALARS = ["sigma_base", "epsilon_base", "mass_base", "rcuton", "rcutoff", "rcu
             "lj_lrc", "f0", "charge_type", "kappa", "ksqmax", "ewald_bc", "ewald_dim", "sf_type",
             "compat", "respa_split", "solid_sigma", "solid_epsilon", "name"]
 # MD settings, stored only when present in an archive (older archives lack them)
-_MD_SCALARS = ["treq_K", "delt_fs", "nstep_inner", "what_ensemble", "nconstraint", "nh_qq", "nh_qqs"]
+_MD_SCALARS = ["treq_K", "delt_fs", "nstep_inner", "what_ensemble", "nconstraint", "nh_qq", "nh_qqs", "preq_bar",
+               "npt_qts", "npt_qbs"]
 _SP_ARRAYS = ["atom_type", "ghost", "interp", "epsilon", "sigma", "charge", "aw", "aw_input",
               "template_xyz", "bond_idx", "bond_type", "bond_param", "angle_idx", "angle_type",
               "angle_param", "dih_idx", "dih_type", "dih_param", "imp_idx", "imp_type", "imp_param",

@@ -421,3 +421,178 @@ int orc_siman_run(const orc_system *s, const mg_siman_params *sp, double *xx, do
     free(lg);
     return 0;
 }
+
+/* ---- NPT: npt_respa and npt_nh_operator (src/nptnh.c:10-234) ------------------------ */
+typedef struct npt_scalars {
+    double vts, vbs, rts, utsbs, ukin, tinst, pinst, pljlrc;
+} npt_scalars;
+
+/* sum over species pairs of the LJ pressure-correction terms (src/initvars.c:476-520)
+ * divided by V^2 in the reference's order (src/misc.c:131-148) */
+static double npt_pljlrc(const orc_system *s, int lj_lrc, double boxv) {
+    if (!lj_lrc) return 0.0;
+    const double pi = 3.141592653589793;
+    const double t1 = (32.0 / 9.0) * pi * pow(s->p.rcutoff, -9.0), t2 = -(16.0 / 3.0) * pi * pow(s->p.rcutoff, -3.0);
+    double p = 0.0;
+    for (int m = 0; m < s->nspecies; m++)
+        for (int nn = 0; nn < s->nspecies; nn++) {
+            double term = 0.0;
+            for (int i = 0; i < s->sp[m].natom; i++)
+                for (int j = 0; j < s->sp[nn].natom; j++) {
+                    const double sij = 0.5 * (s->sp[m].sigma[i] + s->sp[nn].sigma[j]);
+                    const double eij = sqrt(s->sp[m].epsilon[i] * s->sp[nn].epsilon[j]);
+                    term += (pow(sij, 9.0) * t1 + pow(sij, 3.0) * t2) * (eij * pow(sij, 3.0));
+                }
+            p += (term * s->sp[m].nmole * s->sp[nn].nmole / boxv / boxv);
+        }
+    return p;
+}
+
+static void npt_operator(const mg_npt_params *mp, int n, const double *rmass, double *vx, double *vy, double *vz,
+                         double virial, double boxv, npt_scalars *c) {
+    const double nfree = mp->nfree, treq = mp->treq, qts = mp->qts, qbs = mp->qbs, preq = mp->preq;
+    const double N_plus1RT = (nfree + 1) * treq, one_3N = 1.0 + 3.0 / nfree;
+    const double dt_outer2 = mp->delt / 2.0, dt_outer4 = mp->delt / 4.0, dt_outer8 = mp->delt / 8.0;
+    double mvsq = 0.0;
+    for (int ii = 0; ii < n; ii++) mvsq += (vx[ii] * vx[ii] + vy[ii] * vy[ii] + vz[ii] * vz[ii]) / rmass[ii];
+    const double pdiff = virial + c->pljlrc * boxv * 3.0 - preq * boxv * 3.0;
+    double Gts = (mvsq + qbs * c->vbs * c->vbs - N_plus1RT) / qts;
+    c->vts = c->vts + dt_outer4 * Gts;
+    const double BB = exp(-c->vts * dt_outer8);
+    c->vbs = c->vbs * BB;
+    double Gbs = (one_3N * mvsq + pdiff) / qbs;
+    c->vbs = c->vbs + dt_outer4 * Gbs;
+    c->vbs = c->vbs * BB;
+    c->rts = c->rts + dt_outer2 * c->vts;
+    const double AA = exp(-dt_outer2 * (c->vts + one_3N * c->vbs));
+    for (int ii = 0; ii < n; ii++) {
+        vx[ii] = vx[ii] * AA;
+        vy[ii] = vy[ii] * AA;
+        vz[ii] = vz[ii] * AA;
+    }
+    c->vbs = c->vbs * BB;
+    mvsq = mvsq * AA * AA;
+    Gbs = (one_3N * mvsq + pdiff) / qbs;
+    c->vbs = c->vbs + dt_outer4 * Gbs;
+    c->vbs = c->vbs * BB;
+    Gts = (mvsq + qbs * c->vbs * c->vbs - N_plus1RT) / qts;
+    c->vts = c->vts + dt_outer4 * Gts;
+    c->utsbs = 0.5 * qbs * c->vbs * c->vbs + 0.5 * qts * c->vts * c->vts + (nfree + 1) * treq * c->rts + preq * boxv;
+    c->ukin = mvsq / 2.0;
+    c->tinst = 2.0 * c->ukin / nfree;
+    const double pideal = n / boxv * c->tinst;
+    c->pinst = pideal + virial / 3.0 / boxv + c->pljlrc;
+}
+
+static void npt_record(double *row, const npt_scalars *c, double uinter, double uintra, double ushift, double lx,
+                       double boxv) {
+    if (!row) return;
+    const double r[12] = {c->ukin, uinter, uintra, ushift, c->vts, c->vbs, c->rts, c->utsbs, c->tinst, c->pinst,
+                          lx, boxv};
+    memcpy(row, r, sizeof(r));
+}
+
+int orc_npt_run(const orc_system *s0, const mg_npt_params *mp, int nsteps, double *xx, double *yy, double *zz,
+                double *vx, double *vy, double *vz, double *box, mg_npt_state *st, double *log) {
+    const int n = orc_natom(s0);
+    orc_system s = *s0;
+    s.lx = box[0];
+    s.ly = box[1];
+    s.lz = box[2];
+    double *buf = (double *)calloc((size_t)n * 7, sizeof(double));
+    if (!buf) return -1;
+    double *rmass = buf, *fxl = buf + n, *fyl = buf + 2 * n, *fzl = buf + 3 * n, *fxs = buf + 4 * n,
+           *fys = buf + 5 * n, *fzs = buf + 6 * n;
+    for (int q = 0, a = 0; q < s.nspecies; q++)
+        for (int m = 0; m < s.sp[q].nmole; m++)
+            for (int k = 0; k < s.sp[q].natom; k++) rmass[a++] = 1.0 / s.sp[q].aw[k];
+    const double pi = 3.141592653589793;
+    const double deltby2 = mp->delt / 2.0, delts = mp->delt / mp->nstep_inner, deltsby2 = delts / 2.0;
+    double boxv = s.lx * s.ly * s.lz;
+    npt_scalars c;
+    memset(&c, 0, sizeof(c));
+    c.vts = st->vts;
+    c.vbs = st->vbs;
+    c.rts = st->rts;
+    c.pljlrc = npt_pljlrc(&s, mp->lj_lrc, boxv);
+    mg_energies el, es;
+    orc_frclong(&s, xx, yy, zz, fxl, fyl, fzl, &el, NULL);
+    orc_frcshort(&s, xx, yy, zz, fxs, fys, fzs, &es);
+    {
+        double mvsq = 0.0;
+        for (int ii = 0; ii < n; ii++) mvsq += (vx[ii] * vx[ii] + vy[ii] * vy[ii] + vz[ii] * vz[ii]) / rmass[ii];
+        c.ukin = mvsq / 2.0;
+        c.tinst = 2.0 * c.ukin / mp->nfree;
+        c.utsbs = 0.5 * mp->qbs * c.vbs * c.vbs + 0.5 * mp->qts * c.vts * c.vts + (mp->nfree + 1) * mp->treq * c.rts +
+                  mp->preq * boxv;
+        c.pinst = n / boxv * c.tinst + (el.virial_inter + es.virial_intra) / 3.0 / boxv + c.pljlrc;
+    }
+    npt_record(log, &c, el.uinter, es.uintra, el.ushift, s.lx, boxv);
+    for (int step = 1; step <= nsteps; step++) {
+        npt_operator(mp, n, rmass, vx, vy, vz, el.virial_inter + es.virial_intra, boxv, &c);
+        for (int ii = 0; ii < n; ii++) {
+            vx[ii] += (deltby2 * fxl[ii] * rmass[ii]);
+            vy[ii] += (deltby2 * fyl[ii] * rmass[ii]);
+            vz[ii] += (deltby2 * fzl[ii] * rmass[ii]);
+        }
+        for (int ll = 0; ll < mp->nstep_inner; ll++) {
+            const double AA = exp(deltsby2 * c.vbs);
+            for (int ii = 0; ii < n; ii++) {
+                const double r_mass = rmass[ii];
+                vx[ii] += (deltsby2 * fxs[ii] * r_mass);
+                vy[ii] += (deltsby2 * fys[ii] * r_mass);
+                vz[ii] += (deltsby2 * fzs[ii] * r_mass);
+                xx[ii] = xx[ii] * AA;
+                yy[ii] = yy[ii] * AA;
+                zz[ii] = zz[ii] * AA;
+                xx[ii] = xx[ii] + delts * vx[ii];
+                yy[ii] = yy[ii] + delts * vy[ii];
+                zz[ii] = zz[ii] + delts * vz[ii];
+                xx[ii] = xx[ii] * AA;
+                yy[ii] = yy[ii] * AA;
+                zz[ii] = zz[ii] * AA;
+            }
+            const double expfactor = exp(delts * c.vbs);
+            s.lx = s.lx * expfactor;
+            s.ly = s.ly * expfactor;
+            s.lz = s.lz * expfactor;
+            boxv = s.lx * s.ly * s.lz;
+            c.pljlrc = npt_pljlrc(&s, mp->lj_lrc, boxv);
+            if (s.p.charge_type == MG_ELEC_EWALD) {
+                s.p.vfactor_ewald = 2.0 * pi / boxv;
+                s.p.twopi_lx = 2.0 * pi / s.lx;
+                s.p.twopi_ly = 2.0 * pi / s.ly;
+                s.p.twopi_lz = 2.0 * pi / s.lz;
+                s.p.twopi_over_3v = 2.0 * pi / 3.0 / boxv;
+            }
+            orc_frcshort(&s, xx, yy, zz, fxs, fys, fzs, &es);
+            for (int ii = 0; ii < n; ii++) {
+                const double r_mass = rmass[ii];
+                vx[ii] += (deltsby2 * fxs[ii] * r_mass);
+                vy[ii] += (deltsby2 * fys[ii] * r_mass);
+                vz[ii] += (deltsby2 * fzs[ii] * r_mass);
+            }
+        }
+        orc_frclong(&s, xx, yy, zz, fxl, fyl, fzl, &el, NULL);
+        for (int ii = 0; ii < n; ii++) {
+            const double r_mass = rmass[ii];
+            vx[ii] += (deltby2 * fxl[ii] * r_mass);
+            vy[ii] += (deltby2 * fyl[ii] * r_mass);
+            vz[ii] += (deltby2 * fzl[ii] * r_mass);
+        }
+        npt_operator(mp, n, rmass, vx, vy, vz, el.virial_inter + es.virial_intra, boxv, &c);
+        npt_record(log ? log + (size_t)step * 12 : NULL, &c, el.uinter, es.uintra, el.ushift, s.lx, boxv);
+    }
+    box[0] = s.lx;
+    box[1] = s.ly;
+    box[2] = s.lz;
+    st->vts = c.vts;
+    st->vbs = c.vbs;
+    st->rts = c.rts;
+    st->utsbs = c.utsbs;
+    st->ukin = c.ukin;
+    st->tinst = c.tinst;
+    st->pinst = c.pinst;
+    free(buf);
+    return 0;
+}

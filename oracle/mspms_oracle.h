@@ -101,6 +101,8 @@ int orc_hmc_replica(const orc_system *s, const mg_hmc_params *p, int replica, in
                     double *y, double *z, int *accepted, double *dh_log, double *energy);
 
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+int orc_npt_run(const orc_system *s, const mg_npt_params *p, int nsteps, double *x, double *y, double *z,
+                double *vx, double *vy, double *vz, double *box, mg_npt_state *st, double *log);
 int orc_siman_run(const orc_system *s, const mg_siman_params *p, double *x, double *y, double *z, double *vx,
                   double *vy, double *vz, mg_md_state *st, int *nstages, double *stage_log);
 

@@ -15,7 +15,8 @@ import tempfile
 import numpy as np
 
 from mspms2_gb300.capi import (ENERGY_NAMES, MD_LOG, SIMAN_LOG, MgEnergies, MgHmcParams, MgMdParams, MgMdState,
-                               MgParams, MgSimanParams, MgSpecies, SpeciesPack, system_params)
+                               MgNptParams, MgNptState, MgParams, MgSimanParams, MgSpecies, SpeciesPack,
+                               system_params)
 from mspms2_gb300.system import System, write_reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -80,6 +81,8 @@ def lib():
                                     _dp, C.POINTER(MgMdState), _dp]
         _lib.orc_hmc_replica.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgHmcParams), C.c_int, C.c_int, C.c_int,
                                          _dp, _dp, _dp, C.POINTER(C.c_int), _dp, _dp]
+        _lib.orc_npt_run.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgNptParams), C.c_int, _dp, _dp, _dp, _dp, _dp,
+                                     _dp, _dp, C.POINTER(MgNptState), _dp]
         _lib.orc_siman_run.argtypes = [C.POINTER(OrcSystem), C.POINTER(MgSimanParams), _dp, _dp, _dp, _dp, _dp, _dp,
                                        C.POINTER(MgMdState), C.POINTER(C.c_int), _dp]
         _lib.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
@@ -196,6 +199,22 @@ class Oracle:
                               _ptr(pos[1]), _ptr(pos[2]), C.byref(acc), _ptr(dh), C.byref(energy))
         return pos, acc.value, energy.value, dh[:nmoves]
 
+    def npt_run(self, nsteps: int, npt: dict, v, box, state: dict):
+        """The restated npt_respa (oracle/md_oracle.c), same contract as Engine.npt_run:
+        (positions, velocities, box, state, log)."""
+        sysm = self.system
+        pos = np.ascontiguousarray(np.stack([sysm.x, sysm.y, sysm.z]), dtype=np.float64)
+        vel = np.ascontiguousarray(v, dtype=np.float64).copy()
+        bx = np.ascontiguousarray(box, dtype=np.float64).copy()
+        st = MgNptState(**state)
+        log = np.zeros((nsteps + 1, MD_LOG))
+        rc = lib().orc_npt_run(C.byref(self.s), C.byref(MgNptParams.from_dict(npt)), nsteps, _ptr(pos[0]),
+                               _ptr(pos[1]), _ptr(pos[2]), _ptr(vel[0]), _ptr(vel[1]), _ptr(vel[2]), _ptr(bx),
+                               C.byref(st), _ptr(log))
+        if rc != 0:
+            raise RuntimeError(f"orc_npt_run failed ({rc})")
+        return pos, vel, bx, st.as_dict(), log
+
     def siman_run(self, md: dict, sched: dict, state: dict | None = None):
         """The restated simulated annealing (oracle/md_oracle.c), same contract as
         Engine.siman_run: (positions, velocities, state, stage log)."""
@@ -250,6 +269,11 @@ def run_reference_md(path: str, nsteps: int) -> dict:
     log = np.frombuffer(b[off:off + 96 * (ns + 1)]).reshape(ns + 1, 12).copy()
     off += 96 * (ns + 1)
     end = np.frombuffer(b[off:off + 48 * n]).reshape(6, n).copy()
+    if ens == 2:  # NPT: npt_respa (src/nptnh.c:134)
+        md = dict(nstep_inner=nstep_inner, delt=sc[0], treq=sc[1], qts=sc[2], qbs=sc[3], preq=sc[4],
+                  lj_lrc=int(sc[5]), nfree=int(sc[6]))
+        state = dict(vts=sc[7], vbs=sc[8], rts=sc[9], boxlx=sc[10], pljlrc=sc[11])
+        return {"md": md, "state": state, "start": start, "log": log, "end": end, "nsteps": ns, "npt": True}
     md = dict(scheme=ens, nstep_inner=nstep_inner, delt=sc[0], treq=sc[1], qq=sc[2], qqs=sc[3], gg=sc[4],
               ggs=sc[5], nfree=int(sc[6]))
     state = dict(ps=sc[7], ss=sc[8], pss=sc[9], sss=sc[10])

@@ -12,12 +12,15 @@
  *
  * With "md <nsteps> <md.bin>" after the repeat count it then runs nsteps steps of the
  * reference's own integrator for the input's ensemble (what_ensemble NVT: vver_nh_3,
- * src/nvtnh.c:11; NVE: vver, src/md.c:22), starting from the velocities init_vars()
- * drew, and writes
+ * src/nvtnh.c:11; NVE: vver, src/md.c:22; NPT: npt_respa, src/nptnh.c:134), starting
+ * from the velocities init_vars() drew, and writes
  *   int32 natom, nstep_inner, what_ensemble, nsteps; double scalars[12] = {delt, treq,
  *   qq, qqs, gg, ggs, nfree, ps, ss, pss, sss, 0}; double x,y,z,vx,vy,vz[n] (start);
  *   per step (0 = start, then 1..nsteps) double log[12] = {ukin, uinter, uintra, ushift,
  *   ps, ss, pss, sss, tinst, unhts, unhtss, 0}; double x,y,z,vx,vy,vz[n] (end).
+ * For NPT the scalars are {delt, treq, Qts, Qbs, preq, isLJlrcOn, nfree, vts, vbs, rts,
+ * boxlx, pljlrc} and the per-step record {ukin, uinter, uintra, ushift, vts, vbs, rts,
+ * utsbs, tinst, pinst, boxlx, boxv}.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -30,6 +33,7 @@ int opening();
 int fnValidateInput();
 int vver();
 int vver_nh_3();
+int npt_respa();
 
 static void abs_path(const char *name, char *out, size_t len) {
     if (name[0] != '/' && getcwd(out, len - 1)) {
@@ -49,6 +53,11 @@ static void write_state(FILE *fp, int n) {
 }
 
 static void write_log(FILE *fp) {
+    if (what_ensemble == NPT) {
+        double l[12] = {ukin, uinter, uintra, ushift, vts, vbs, rts, utsbs, tinst, pinst, boxlx, boxv};
+        fwrite(l, sizeof(double), 12, fp);
+        return;
+    }
     double l[12] = {ukin, uinter, uintra, ushift, ps, ss, pss, sss, tinst, unhts, unhtss, 0.0};
     fwrite(l, sizeof(double), 12, fp);
 }
@@ -109,14 +118,20 @@ int main(int argc, char **argv) {
         printf("frclong_s=%.9g frcshort_s=%.9g\n", (t1 - t0) / repeat, (t2 - t1) / repeat);
     }
     if (md_steps > 0) {
-        int (*scheme)() = what_ensemble == NVT ? vver_nh_3 : (what_ensemble == NVE ? vver : NULL);
-        if (!scheme) { fprintf(stderr, "md mode supports NVT and NVE only\n"); return 2; }
+        int (*scheme)() = what_ensemble == NVT ? vver_nh_3
+                          : (what_ensemble == NVE ? vver : (what_ensemble == NPT ? npt_respa : NULL));
+        if (!scheme) { fprintf(stderr, "md mode supports NVT, NVE and NPT only\n"); return 2; }
         if (repeat > 0) { frclong(); frcshort(); }
         FILE *fm = fopen(mdabs, "wb");
         if (!fm) { perror("md out"); return 2; }
         int hdr[4] = {n, nstep_inner, what_ensemble, md_steps};
         fwrite(hdr, sizeof(int), 4, fm);
         double sc[12] = {delt, treq, qq, qqs, gg, ggs, (double)nfree, ps, ss, pss, sss, 0.0};
+        if (what_ensemble == NPT) {
+            double snpt[12] = {delt, treq, Qts, Qbs, preq, (double)isLJlrcOn, (double)nfree, vts, vbs, rts, boxlx,
+                               pljlrc};
+            memcpy(sc, snpt, sizeof(sc));
+        }
         fwrite(sc, sizeof(double), 12, fm);
         write_state(fm, n);
         write_log(fm);

@@ -244,6 +244,18 @@ def md_cases():
     e.nh_qq, e.nh_qqs = 5000.0, 2000.0
     e.name = "md_water_ewald_respa"
     out["md_water_ewald_respa_512"] = (e, 5)
+    # NPT (npt_respa): Wolf water with the LJ long-range correction, 2 inner steps; Ewald
+    # water with 4 inner RESPA steps (the box, the k-vectors and the Ewald constants change
+    # every inner step)
+    pw = configs.water_box(6, 18.6, 17, ELEC_WOLF, 0.2, 9.0, name="md_water_npt", site_jitter=0.04)
+    pw.delt_fs, pw.nstep_inner, pw.what_ensemble, pw.lj_lrc = 0.5, 2, 2, 1
+    pw.preq_bar, pw.npt_qts, pw.npt_qbs = 1000.0, 2.0e4, 5.0e3
+    out["md_water_npt_216"] = (pw, 10)
+    pe = configs.water_small(8, 24.8, seed=19, charge_type=ELEC_EWALD, kappa=0.3, rc=10.0, kmax=7, ksqmax=49)
+    pe.delt_fs, pe.nstep_inner, pe.what_ensemble = 1.0, 4, 2
+    pe.preq_bar, pe.npt_qts, pe.npt_qbs = 1.0, 5.0e4, 2.0e3
+    pe.name = "md_water_ewald_npt"
+    out["md_water_ewald_npt_512"] = (pe, 5)
     return out
 
 
@@ -291,9 +303,14 @@ def gen_md(only):
         parsed.x, parsed.y, parsed.z = (r["start"][k].copy() for k in range(3))
         arrays = system_to_arrays(parsed)
         md = r["md"]
-        arrays["md_int"] = np.array([md["scheme"], md["nstep_inner"], md["nfree"], r["nsteps"]])
-        arrays["md_real"] = np.array([md["delt"], md["treq"], md["qq"], md["qqs"], md["gg"], md["ggs"]])
-        arrays["md_state0"] = np.array([r["state"][k] for k in ("ps", "ss", "pss", "sss")])
+        if r.get("npt"):
+            arrays["md_int"] = np.array([2, md["nstep_inner"], md["nfree"], r["nsteps"], md["lj_lrc"]])
+            arrays["md_real"] = np.array([md["delt"], md["treq"], md["qts"], md["qbs"], md["preq"]])
+            arrays["md_state0"] = np.array([r["state"][k] for k in ("vts", "vbs", "rts", "boxlx", "pljlrc")])
+        else:
+            arrays["md_int"] = np.array([md["scheme"], md["nstep_inner"], md["nfree"], r["nsteps"]])
+            arrays["md_real"] = np.array([md["delt"], md["treq"], md["qq"], md["qqs"], md["gg"], md["ggs"]])
+            arrays["md_state0"] = np.array([r["state"][k] for k in ("ps", "ss", "pss", "sss")])
         arrays["md_v0"] = r["start"][3:]
         arrays["md_log"] = r["log"]
         arrays["md_end"] = r["end"]
