@@ -326,6 +326,45 @@ typedef struct mg_npt_state {
 MG_API mg_status mg_npt_run(mg_ctx *ctx, const mg_npt_params *p, int nsteps, double *x, double *y, double *z,
                             double *vx, double *vy, double *vz, double *box, mg_npt_state *state, double *log);
 
+/* ---- trajectory file (trajectory(), src/dumpxyz.c:37-66) ------------------------ */
+/* Attaches a trajectory file in the reference's binary layout (trj.mspms) to the
+ * context: the header is written now; mg_md_run and mg_npt_run then append the frame
+ * before their first step (once per file, as src/mspms2.c:57-60 does) and a frame every
+ * `every` steps counted across calls (src/mspms2.c:123-126); mg_siman_run counts one step
+ * per stage, as the reference's loop does. Frames leave the device through two staging
+ * buffers, a copy stream and a writer thread, so the integrator does not wait for the
+ * file. atom_names: 5 bytes per template site, species by species (the reference's
+ * atom_name fields; shorter names NUL-padded). Site masses are the topology's aw. */
+MG_API mg_status mg_traj_open(mg_ctx *ctx, const char *path, int every, const char *atom_names);
+/* Waits for the queued frames, closes the file and detaches it; *nframes (optional)
+ * receives the number of frames written. */
+MG_API mg_status mg_traj_close(mg_ctx *ctx, long long *nframes);
+
+/* ---- checkpoint (saveit()/loadit(), src/loadsave.c:19-128) --------------------- */
+#define MG_NCOUNTS 40 /* NCOUNTS_MAX (src/defs.h:77) */
+typedef struct mg_checkpoint {
+    int natom;
+    double *x, *y, *z, *vx, *vy, *vz;            /* [natom], caller-owned */
+    double qq, ps, gg, ss, qqs, pss, ggs, sss;   /* Nose-Hoover (MDNVT) */
+    double vts, rts, vbs;                        /* NPT thermostat/barostat */
+    double boxlx, boxly, boxlz, boxv;
+    int equilibrium;                             /* bEquilibrium, stored as one byte */
+    int nframe, istep;
+    int counts[MG_NCOUNTS];
+    double accum[MG_NCOUNTS];                    /* the reference writes NCOUNTS_MAX doubles
+                                                    of its accum[NCOUNTS_MAX][8]: its first
+                                                    five rows */
+} mg_checkpoint;
+/* Writes the file byte for byte as saveit() does. */
+MG_API mg_status mg_checkpoint_save(const char *path, const mg_checkpoint *ck);
+/* Reads it as loadit() does: the counters (equilibrium .. accum) only with
+ * with_counters (a continued run, iStart_option CONTINUE). */
+MG_API mg_status mg_checkpoint_load(const char *path, mg_checkpoint *ck, int with_counters);
+/* Sets the context's box to the checkpoint's and drops everything the engine keeps for
+ * the old box (cluster list, k-vector tables). The Ewald box constants stay as
+ * mg_set_params gave them, as loadit() leaves its globals. */
+MG_API mg_status mg_checkpoint_apply(mg_ctx *ctx, const mg_checkpoint *ck);
+
 /* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
 /* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
  * first stage whose T is below t_min (the reference tests T < t_min after the stage). A

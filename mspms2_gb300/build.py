@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmspms2_gb300.so")
-SOURCES = ["mg_host.cu", "mg_nblist.cu", "mg_pair.cu", "mg_bonded.cu", "mg_ewald.cu", "mg_sf.cu", "mg_md.cu", "mg_sfgrid.cu", "mg_hmc.cu", "mg_adjoint.cu"]
+SOURCES = ["mg_host.cu", "mg_nblist.cu", "mg_pair.cu", "mg_bonded.cu", "mg_ewald.cu", "mg_sf.cu", "mg_md.cu", "mg_sfgrid.cu", "mg_hmc.cu", "mg_adjoint.cu", "mg_io.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-Xptxas", "-O3"]

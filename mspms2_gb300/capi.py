@@ -98,6 +98,21 @@ NPT_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "vts", "vbs", "rts", "uts
                  "boxv"]
 
 
+NCOUNTS = 40
+
+
+class MgCheckpoint(C.Structure):
+    _fields_ = ([("natom", C.c_int)] + [(k, _dp) for k in ("x", "y", "z", "vx", "vy", "vz")] +
+                [(k, C.c_double) for k in ("qq", "ps", "gg", "ss", "qqs", "pss", "ggs", "sss", "vts", "rts", "vbs",
+                                           "boxlx", "boxly", "boxlz", "boxv")] +
+                [("equilibrium", C.c_int), ("nframe", C.c_int), ("istep", C.c_int),
+                 ("counts", C.c_int * NCOUNTS), ("accum", C.c_double * NCOUNTS)])
+
+
+CHECKPOINT_SCALARS = ["qq", "ps", "gg", "ss", "qqs", "pss", "ggs", "sss", "vts", "rts", "vbs", "boxlx", "boxly",
+                      "boxlz", "boxv"]
+
+
 class MgSimanParams(C.Structure):
     _fields_ = [("md", MgMdParams), ("t_initial", C.c_double), ("t_min", C.c_double), ("mu_t", C.c_double),
                 ("n_tries", C.c_int), ("max_stages", C.c_int), ("seed", C.c_ulonglong)]

@@ -116,6 +116,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
     if (!c) return MG_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    mg_traj_destroy(c);
     DevBuf *bufs[] = {&c->d_site_mol, &c->d_site_q, &c->d_site_hsig, &c->d_site_seps, &c->d_site_flags,
                       &c->d_site_interp, &c->d_species, &c->d_intra, &c->d_bonded, &c->d_site_aw,
                       &c->d_x, &c->d_y, &c->d_z, &c->d_fl, &c->d_fs, &c->d_xbuild, &c->d_img,
@@ -299,6 +300,7 @@ extern "C" mg_status mg_set_topology(mg_ctx *c, int nspecies, const mg_species *
     c->species.clear();
     c->h_tmpl_eps.clear();
     c->h_tmpl_sig.clear();
+    c->h_tmpl_aw.clear();
     c->h_site_mol.assign(natom, 0);
     c->h_site_species.assign(natom, 0);
     c->h_site_rel.assign(natom, 0);
@@ -378,6 +380,8 @@ extern "C" mg_status mg_set_topology(mg_ctx *c, int nspecies, const mg_species *
         c->max_mol_atoms = std::max(c->max_mol_atoms, S.natom);
         c->h_tmpl_eps.emplace_back(S.epsilon, S.epsilon + S.natom);
         c->h_tmpl_sig.emplace_back(S.sigma, S.sigma + S.natom);
+        c->h_tmpl_aw.emplace_back();
+        for (int a = 0; a < S.natom; a++) c->h_tmpl_aw.back().push_back(S.aw ? S.aw[a] : 1.0);
         for (int m = 0; m < S.nmole; m++, mole++)
             for (int a = 0; a < S.natom; a++, site++) {
                 c->h_site_mol[site] = mole;

@@ -99,6 +99,7 @@ struct MyInterpDev {
 
 // ---- context ----------------------------------------------------------------------
 struct mg_ctx_s;
+struct MgTraj;  // trajectory writer (mg_io.cu)
 
 struct DevBuf {
     void *p = nullptr;
@@ -120,7 +121,7 @@ struct mg_ctx {
     int natom = 0, nmole = 0, nspecies = 0;
     std::vector<SpeciesDev> species;
     std::vector<int> h_site_mol, h_site_species, h_site_rel;
-    std::vector<std::vector<double>> h_tmpl_eps, h_tmpl_sig;  // per species template (LJ corrections)
+    std::vector<std::vector<double>> h_tmpl_eps, h_tmpl_sig, h_tmpl_aw;  // per species template
     std::vector<double> h_site_q;
     double sum_q2 = 0.0;
     int max_mol_atoms = 0;
@@ -160,6 +161,7 @@ struct mg_ctx {
     DevBuf d_md_v, d_md_work, d_md_rmass, d_md_part, d_md_dev, d_md_log;
     // adjoint (mg_adjoint_params): site classes and one carved scratch block
     DevBuf d_adj_class, d_adj, d_adj_g;
+    MgTraj *traj = nullptr;  // attached trajectory file, if any
     // reciprocal space
     int nrows = 0, nslots = 0, kmaxx = 0, kmaxy = 0, kmaxz = 0;
     long long kvectors = 0;
@@ -221,6 +223,11 @@ mg_status mg_launch_sf(mg_ctx *c, const double *dx, const double *dy, const doub
 mg_status mg_launch_reduce(mg_ctx *c);
 mg_status mg_launch_check(mg_ctx *c, const double *f, int n);
 bool mg_list_retry(mg_ctx *c, unsigned flags, const int *meta_host);
+// trajectory frames of device-resident runs (mg_io.cu): the frame before the first step
+// (once per file) and one frame every `every` steps
+mg_status mg_traj_start(mg_ctx *c, const double *d_x);
+mg_status mg_traj_tick(mg_ctx *c, const double *d_x);
+void mg_traj_destroy(mg_ctx *c);
 
 // Energy partial rows: every block of every stage writes one full row of E_NCOMP
 // FP64 values (zeros outside its own components); rows are reserved in launch order

@@ -495,7 +495,7 @@ mg_status md_prepare(mg_ctx *c, size_t log_rows, MdRun &R) {
 // nsteps of the scheme from the device state of R: forces at the start (as the reference
 // evaluates them before its loop), the step-0 record and one record per step (device
 // rows dlog; uinter, uintra and ushift of every row in hlog)
-mg_status md_loop(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, double *hlog) {
+mg_status md_loop(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, double *hlog, bool traj_steps) {
     mg_ctx *c = R.c;
     MdArgs &A = R.A;
     const int nb = R.nb;
@@ -554,6 +554,7 @@ mg_status md_loop(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, do
         hlog[(size_t)step * MG_MD_LOG + 1] = uinter_l + uinter_s;
         hlog[(size_t)step * MG_MD_LOG + 2] = uintra;
         hlog[(size_t)step * MG_MD_LOG + 3] = ushift_l + ushift_s;
+        if (traj_steps && (st = mg_traj_tick(c, dx))) return st;
     }
     return MG_OK;
 }
@@ -611,7 +612,8 @@ extern "C" mg_status mg_md_run(mg_ctx *c, const mg_md_params *mp, int nsteps, do
     h0.unhtss = state->unhtss;
     MG_CUDA(cudaMemcpyAsync(c->d_md_dev.p, &h0, sizeof(MdDev), cudaMemcpyHostToDevice, s));
     std::vector<double> hlog(MG_MD_LOG * ((size_t)nsteps + 1), 0.0);
-    if ((st = md_loop(R, mp, nsteps, dlog, hlog.data()))) return st;
+    if ((st = mg_traj_start(c, R.A.x))) return st;
+    if ((st = md_loop(R, mp, nsteps, dlog, hlog.data(), true))) return st;
     MG_CUDA(cudaMemcpyAsync(x, R.A.x, nb1, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaMemcpyAsync(y, R.A.y, nb1, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaMemcpyAsync(z, R.A.z, nb1, cudaMemcpyDeviceToHost, s));
@@ -698,7 +700,8 @@ extern "C" mg_status mg_siman_run(mg_ctx *c, const mg_siman_params *sp, double *
         k_vel_scale<<<R.nb, MD_TPB, 0, s>>>(R.A, aw);
         MG_CUDA(cudaGetLastError());
         c->launches += 6;
-        if ((st = md_loop(R, &mp, sp->n_tries, dlog, hlog.data()))) return st;
+        if ((st = md_loop(R, &mp, sp->n_tries, dlog, hlog.data(), false))) return st;
+        if ((st = mg_traj_tick(c, R.A.x))) return st;  // one step of the reference's loop per stage
         MG_CUDA(cudaMemcpyAsync(last.data(), dlog + (size_t)sp->n_tries * MG_MD_LOG, sizeof(double) * MG_MD_LOG,
                                 cudaMemcpyDeviceToHost, s));
         MG_CUDA(cudaStreamSynchronize(s));
@@ -885,6 +888,7 @@ extern "C" mg_status mg_npt_run(mg_ctx *c, const mg_npt_params *mp, int nsteps, 
         q.pinst = n / boxv * q.tinst + (el.virial_inter + es.virial_intra) / 3.0 / boxv + q.pljlrc;
         npt_record(log, q, el, es, c->lx, boxv);
     }
+    if ((st = mg_traj_start(c, R.A.x))) return st;
     for (int step = 1; step <= nsteps; step++) {
         if ((st = npt_operator(R, mp, el.virial_inter + es.virial_inter + es.virial_intra, boxv, q))) return st;
         k_md_kick<<<R.nb, MD_TPB, 0, s>>>(R.A, fl, h, 0, 0);
@@ -905,6 +909,7 @@ extern "C" mg_status mg_npt_run(mg_ctx *c, const mg_npt_params *mp, int nsteps, 
         MG_CUDA(cudaGetLastError());
         if ((st = npt_operator(R, mp, el.virial_inter + es.virial_inter + es.virial_intra, boxv, q))) return st;
         npt_record(log ? log + (size_t)step * MG_NPT_LOG : nullptr, q, el, es, c->lx, boxv);
+        if ((st = mg_traj_tick(c, R.A.x))) return st;
     }
     MG_CUDA(cudaMemcpyAsync(x, R.A.x, nb1, cudaMemcpyDeviceToHost, s));
     MG_CUDA(cudaMemcpyAsync(y, R.A.y, nb1, cudaMemcpyDeviceToHost, s));

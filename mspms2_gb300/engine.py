@@ -78,6 +78,11 @@ def load_library(path: str = LIB_PATH):
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.mg_traj_open.argtypes = [V, C.c_char_p, I, C.c_char_p]
+    lib.mg_traj_close.argtypes = [V, C.POINTER(C.c_longlong)]
+    lib.mg_checkpoint_save.argtypes = [C.c_char_p, C.POINTER(capi.MgCheckpoint)]
+    lib.mg_checkpoint_load.argtypes = [C.c_char_p, C.POINTER(capi.MgCheckpoint), I]
+    lib.mg_checkpoint_apply.argtypes = [V, C.POINTER(capi.MgCheckpoint)]
     lib.mg_npt_run.argtypes = [V, C.POINTER(capi.MgNptParams), I, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                C.POINTER(capi.MgNptState), _dp]
     lib.mg_siman_run.argtypes = [V, C.POINTER(capi.MgSimanParams), _dp, _dp, _dp, _dp, _dp, _dp,
@@ -275,6 +280,25 @@ class Engine:
                                             _p(h[0]), _p(h[1]), _p(h[2])))
         return h
 
+    def traj_open(self, path: str, every: int, names=None) -> None:
+        """Attaches the reference's trajectory file (mg_traj_open): the integrators then
+        write a frame before their first step and every `every` steps."""
+        names = names if names is not None else [nm for sp in self.system.species for nm in sp.atom_names]
+        buf = b"".join(str(nm).encode()[:5].ljust(5, b"\0") for nm in names)
+        self._check(self.lib.mg_traj_open(self.ctx, os.fsencode(path), every, buf))
+
+    def traj_close(self) -> int:
+        """Flushes and closes the trajectory file; returns the number of frames."""
+        k = C.c_longlong(0)
+        self._check(self.lib.mg_traj_close(self.ctx, C.byref(k)))
+        return k.value
+
+    def checkpoint_apply(self, ck: dict) -> None:
+        """The box of a loaded checkpoint (mg_checkpoint_apply): caches keyed on the box
+        are dropped."""
+        c, _keep = checkpoint_struct(ck)
+        self._check(self.lib.mg_checkpoint_apply(self.ctx, C.byref(c)))
+
     def npt_run(self, nsteps: int, npt: dict, v, state: dict, box=None, x=None, y=None, z=None):
         """nsteps of the reference's npt_respa on the device (mg_npt_run): npt holds the
         mg_npt_params fields (mspms2_gb300.system.npt_params), state vts, vbs, rts
@@ -410,6 +434,49 @@ def hmc_batch(hp: dict, natom, box, x, y, z, nmoves: int, move0: int = 0, device
     if st != MG_OK:
         raise EngineError(st, "mg_hmc_batch")
     return x, y, z, acc, energy, dh[:, :nmoves]
+
+
+def checkpoint_struct(ck: dict):
+    """mg_checkpoint of a dict (positions/velocities [natom] arrays, the scalars, counters);
+    returns the struct and the arrays that back its pointers."""
+    arrs = {k: np.ascontiguousarray(ck[k], dtype=np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    c = capi.MgCheckpoint()
+    c.natom = len(arrs["x"])
+    for k, a in arrs.items():
+        setattr(c, k, _p(a))
+    for k in capi.CHECKPOINT_SCALARS:
+        setattr(c, k, float(ck.get(k, 0.0)))
+    c.equilibrium = int(ck.get("equilibrium", 0))
+    c.nframe = int(ck.get("nframe", 0))
+    c.istep = int(ck.get("istep", 0))
+    for i, v in enumerate(ck.get("counts", [0] * capi.NCOUNTS)):
+        c.counts[i] = int(v)
+    for i, v in enumerate(ck.get("accum", [0.0] * capi.NCOUNTS)):
+        c.accum[i] = float(v)
+    return c, arrs
+
+
+def checkpoint_save(path: str, ck: dict) -> None:
+    """Writes the reference's checkpoint file (saveit layout) through mg_checkpoint_save."""
+    c, _keep = checkpoint_struct(ck)
+    st = load_library().mg_checkpoint_save(os.fsencode(path), C.byref(c))
+    if st != MG_OK:
+        raise EngineError(st, f"cannot write {path}")
+
+
+def checkpoint_load(path: str, natom: int, with_counters: bool = True) -> dict:
+    """Reads the reference's checkpoint file (loadit) through mg_checkpoint_load."""
+    ck = {k: np.zeros(natom) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    c, arrs = checkpoint_struct(ck)
+    st = load_library().mg_checkpoint_load(os.fsencode(path), C.byref(c), 1 if with_counters else 0)
+    if st != MG_OK:
+        raise EngineError(st, f"cannot read {path}")
+    out = dict(arrs)
+    for k in capi.CHECKPOINT_SCALARS:
+        out[k] = getattr(c, k)
+    out.update(equilibrium=c.equilibrium, nframe=c.nframe, istep=c.istep, counts=list(c.counts),
+               accum=list(c.accum))
+    return out
 
 
 def derive(system: System) -> dict:

@@ -252,15 +252,22 @@ def read_ref_output(fn: str):
     return fl, fs, e, d
 
 
-def run_reference_md(path: str, nsteps: int) -> dict:
+def run_reference_md(path: str, nsteps: int, trj_every: int = 0) -> dict:
     """Run the compiled reference's own integrator for the input's ensemble (harness md
-    mode, oracle/ref_harness.c) and parse its record."""
+    mode, oracle/ref_harness.c) and parse its record. With trj_every > 0 the result also
+    holds the bytes of the reference's trajectory file and of its checkpoint after the
+    run ("trj", "sav")."""
+    files = {}
     with tempfile.TemporaryDirectory() as td:
         out, md = os.path.join(td, "out.bin"), os.path.join(td, "md.bin")
-        p = subprocess.run([REF_BIN, path, out, "0", "md", str(nsteps), md], capture_output=True, text=True)
+        args = [REF_BIN, path, out, "0", "md", str(nsteps), md] + ([str(trj_every)] if trj_every > 0 else [])
+        p = subprocess.run(args, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"reference md run failed: {p.stderr[-2000:]}")
         b = open(md, "rb").read()
+        if trj_every > 0:
+            for k, fn in (("trj", "trj.mspms"), ("sav", "sav.mspms")):
+                files[k] = open(os.path.join(path, fn), "rb").read()
     n, nstep_inner, ens, ns = (int(v) for v in np.frombuffer(b[:16], np.int32))
     sc = np.frombuffer(b[16:112])
     off = 112
@@ -277,7 +284,7 @@ def run_reference_md(path: str, nsteps: int) -> dict:
     md = dict(scheme=ens, nstep_inner=nstep_inner, delt=sc[0], treq=sc[1], qq=sc[2], qqs=sc[3], gg=sc[4],
               ggs=sc[5], nfree=int(sc[6]))
     state = dict(ps=sc[7], ss=sc[8], pss=sc[9], sss=sc[10])
-    return {"md": md, "state": state, "start": start, "log": log, "end": end, "nsteps": ns}
+    return {"md": md, "state": state, "start": start, "log": log, "end": end, "nsteps": ns, **files}
 
 
 SFGRIDGEN_BIN = os.path.join(HERE, "_ref", "sfgridgen")

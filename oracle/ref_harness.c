@@ -21,6 +21,10 @@
  * For NPT the scalars are {delt, treq, Qts, Qbs, preq, isLJlrcOn, nfree, vts, vbs, rts,
  * boxlx, pljlrc} and the per-step record {ukin, uinter, uintra, ushift, vts, vbs, rts,
  * utsbs, tinst, pinst, boxlx, boxv}.
+ * A further argument trj_every > 0 makes the run write the reference's trajectory file
+ * (trj.mspms in the input directory, trajectory() of src/dumpxyz.c) the way its main loop
+ * does (src/mspms2.c:57-60, :123-126), and its checkpoint (saveit(), sav.mspms) after the
+ * last step with istep = nsteps.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -34,6 +38,8 @@ int fnValidateInput();
 int vver();
 int vver_nh_3();
 int npt_respa();
+int trajectory();
+int saveit();
 
 static void abs_path(const char *name, char *out, size_t len) {
     if (name[0] != '/' && getcwd(out, len - 1)) {
@@ -78,9 +84,11 @@ int main(int argc, char **argv) {
     int repeat = argc > 3 ? atoi(argv[3]) : 0;
     int md_steps = 0;
     char mdabs[4096] = {0};
+    int trj_every = 0;
     if (argc > 6 && !strcmp(argv[4], "md")) {
         md_steps = atoi(argv[5]);
         abs_path(argv[6], mdabs, sizeof(mdabs));
+        if (argc > 7) trj_every = atoi(argv[7]);
     }
     if (chdir(argv[1]) != 0) { perror("chdir"); return 2; }
     opening();
@@ -135,12 +143,20 @@ int main(int argc, char **argv) {
         fwrite(sc, sizeof(double), 12, fm);
         write_state(fm, n);
         write_log(fm);
+        if (trj_every > 0) trajectory();
         for (int k = 0; k < md_steps; k++) {
             scheme();
             write_log(fm);
+            istep = k + 1;
+            if (trj_every > 0 && istep % trj_every == 0) trajectory();
         }
         write_state(fm, n);
         fclose(fm);
+        if (trj_every > 0) {
+            fflush(fptrj);
+            istep = md_steps;
+            saveit();
+        }
     }
     return 0;
 }

@@ -7,11 +7,14 @@ from the reference checkout), and stored as <case>.npz with:
   ref_fl[3,n], ref_fs[3,n]  forces of frclong() / frcshort(),
   ref_energies[18]          in mspms2_gb300.capi.ENERGY_NAMES order,
   ref_derived[24]           derived globals after init_vars().
-The md_* cases hold trajectories of the reference's own integrators instead (vver_nh_3 or
-vver, run by the harness's md mode): md_int (scheme, nstep_inner, nfree, nsteps), md_real
-(delt, treq, qq, qqs, gg, ggs), md_state0 (ps, ss, pss, sss), md_v0[3,n] start velocities
-(drawn by the reference's velinit), md_log[nsteps+1, 12] and md_end[6, n] (x, y, z, vx,
-vy, vz after the last step); the system's positions are the start. The sfgrid_* cases
+The md_* cases hold trajectories of the reference's own integrators instead (vver_nh_3,
+vver or npt_respa, run by the harness's md mode): md_int (scheme, nstep_inner, nfree,
+nsteps[, lj_lrc]), md_real (delt, treq, qq, qqs, gg, ggs; NPT: delt, treq, Qts, Qbs,
+preq), md_state0 (ps, ss, pss, sss; NPT: vts, vbs, rts, boxlx, pljlrc), md_v0[3,n] start
+velocities (drawn by the reference's velinit), md_log[nsteps+1, 12] and md_end[6, n] (x,
+y, z, vx, vy, vz after the last step); the system's positions are the start. A case with
+trj_every also holds the bytes of the reference's trajectory file (ref_trj) and of its
+checkpoint after the last step (ref_sav). The sfgrid_* cases
 hold grids of the reference's tools/sfgridgen.c (atoms, cell, LJ parameters, dims and its
 13 output arrays).
 Two cases use the reference's shipped inputs (Examples/Water and the root example);
@@ -256,6 +259,17 @@ def md_cases():
     pe.preq_bar, pe.npt_qts, pe.npt_qbs = 1.0, 5.0e4, 2.0e3
     pe.name = "md_water_ewald_npt"
     out["md_water_ewald_npt_512"] = (pe, 5)
+    # trajectory and checkpoint files of the reference's own writers: two species (LJ ions
+    # with Ewald), NVT, a frame every 3 steps and the checkpoint after the last step
+    ions = configs.ion_box(4, seed=23, kmax=4, ksqmax=16, rc=7.5, spacing=4.0, jitter=0.3)
+    for sp, (eps, sig, q) in zip(ions.species, ((50.0, 2.6, 0.3), (120.0, 3.4, -0.3))):
+        sp.epsilon, sp.sigma, sp.charge = np.array([eps]), np.array([sig]), np.array([q])
+        sp.aw_input = sp.aw_input * 30.0  # ~18 amu
+        sp.aw = sp.aw * 30.0
+    ions.delt_fs, ions.nstep_inner, ions.what_ensemble = 1.0, 1, 1
+    ions.nh_qq = ions.nh_qqs = 500.0
+    ions.name = "md_ions_trj"
+    out["md_ions_trj_64"] = (ions, 10, 3)
     return out
 
 
@@ -293,13 +307,15 @@ def gen_sfgrid(only):
 
 
 def gen_md(only):
-    for name, (system, nsteps) in md_cases().items():
+    for name, case in md_cases().items():
+        system, nsteps = case[:2]
+        trj_every = case[2] if len(case) > 2 else 0
         if only and name not in only:
             continue
         with tempfile.TemporaryDirectory() as td:
             write_reference_dir(system, td)
             parsed = read_reference_dir(td)
-            r = run_reference_md(td, nsteps)
+            r = run_reference_md(td, nsteps, trj_every)
         parsed.x, parsed.y, parsed.z = (r["start"][k].copy() for k in range(3))
         arrays = system_to_arrays(parsed)
         md = r["md"]
@@ -312,6 +328,10 @@ def gen_md(only):
             arrays["md_real"] = np.array([md["delt"], md["treq"], md["qq"], md["qqs"], md["gg"], md["ggs"]])
             arrays["md_state0"] = np.array([r["state"][k] for k in ("ps", "ss", "pss", "sss")])
         arrays["md_v0"] = r["start"][3:]
+        if trj_every > 0:
+            arrays["trj_every"] = np.array(trj_every)
+            arrays["ref_trj"] = np.frombuffer(r["trj"], dtype=np.uint8)
+            arrays["ref_sav"] = np.frombuffer(r["sav"], dtype=np.uint8)
         arrays["md_log"] = r["log"]
         arrays["md_end"] = r["end"]
         fn = os.path.join(OUT, f"{name}.npz")
