@@ -19,8 +19,10 @@ Nose-Hoover RESPA integrator (mg_md_run; inner: bonded + pairs < 7 A, four 0.5 f
 outer: 7-10 A shell + reciprocal, 2 fs) and the energy drift of an NVE run; batched HMC
 of 512 Lennard-Jones replicas; the cost of the adjoint and Hessian-vector product; force
 matching on 4096 waters (64 snapshots, loss + gradient, checked against the FP64 path and
-central differences); the roofline of the dominant kernel and a bounded CPU baseline of the
-reference algorithm (the oracle port, single thread, extrapolated from a sampled window).
+central differences); 20,000 butane in a nanotube bundle with device-generated Tasos
+tables (pair throughput, solid-fluid gather against HBM, ns/day, FP64 path); the roofline
+of the dominant kernel and a bounded CPU baseline of the reference algorithm (the oracle
+port, single thread, extrapolated from a sampled window).
 """
 from __future__ import annotations
 
@@ -459,6 +461,108 @@ def force_matching_extras(device, nsnap=64, stride=4, seed=2024):
                     "gradient in (eps_OO, sigma_OO, q_O) with q_H = -q_O/2; central differences h = 1e-4 relative"}
 
 
+def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True):
+    """United-atom n-butane in a bundle of 7 (11,11) nanotubes (80,000 sites, LJ rc 14 A,
+    Tasos solid-fluid tables at 0.1 A over the 127 x 127 A bundle cell, generated on the
+    device): force steps timed like the headline (device-resident positions, L2 flushed,
+    CUDA events), the solid-fluid gather against the HBM roofline (64 FP32 table values,
+    256 B, per site), ns/day of Nose-Hoover RESPA (2 fs outer, 4 x 0.5 fs inner with the
+    bonded terms) and the plain-FP64 path on the same system."""
+    import torch
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import TERMS_ALL, Engine
+    from mspms2_gb300.system import md_params, time_base
+    s, tubes = configs.butane_in_tube_bundle()
+    per = tubes["period"]
+    nx = ny = 1271
+    nz = 25
+    h = (0.1, 0.1, per / (nz - 1))
+
+    def spec(sig, eps):
+        return dict(atoms=tubes["atoms"], ucl=(127.0, 127.0, per), f_sigma=sig, f_epsilon=eps, s_sigma=3.4,
+                    s_epsilon=28.0, rcuton=14.0, rcutoff=14.0, lj_switch=0)
+
+    n = s.natom
+    stream = torch.cuda.current_stream()
+    pos = torch.tensor(np.stack([s.x, s.y, s.z]), dtype=torch.float64, device="cuda")
+    fl = torch.empty((3, n), dtype=torch.float64, device="cuda")
+    fs = torch.empty((3, n), dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    ptrs = (pos[0].data_ptr(), pos[1].data_ptr(), pos[2].data_ptr())
+    out = {"workload": "butane_tube_bundle", "sites": n, "molecules": s.nmole, "rc_A": s.rcutoff,
+           "tasos_nodes_per_table": nx * ny * nz, "tasos_spacing_A": [h[0], h[1], h[2]]}
+
+    def timed(eng, k):
+        eng.set_stream(stream.cuda_stream)
+        for _ in range(warmup):
+            eng.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+        ts = []
+        for i in range(k):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.mean(ts)
+
+    with Engine(s, precision="mixed", device=device) as eng:
+        t0 = time.perf_counter()
+        eng.sf_tasos_generate(1, spec(3.75, 98.0), nx, ny, nz, h, per)
+        eng.sf_tasos_generate(2, spec(3.95, 46.0), nx, ny, nz, h, per)
+        out["table_generation_s"] = time.perf_counter() - t0
+        ms = timed(eng, steps)
+        st = eng.stats()
+        npairs = st["pairs_within_cutoff"]
+        eng.set_timing(True)
+        flush.fill_(1.0)
+        eng.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+        torch.cuda.synchronize()
+        kms = eng.stats()["kernel_ms"]
+        eng.set_timing(False)
+        f32 = torch.cat([fl, fs]).clone()
+        # ns/day of the RESPA integrator from seeded Maxwell-Boltzmann velocities at 300 K
+        s.delt_fs, s.nstep_inner = 2.0, 4
+        md = md_params(s)
+        md["scheme"] = 1
+        tau = 100.0 / time_base(s)
+        md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
+        m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+        v = np.random.default_rng(5).normal(size=(3, n)) * np.sqrt(md["treq"] / m)
+        v -= (v * m).sum(1, keepdims=True) / m.sum()
+        p1, v1, st1, _ = eng.md_run(1, md, v)
+        t0 = time.perf_counter()
+        eng.md_run(md_steps, md, v1, x=p1[0], y=p1[1], z=p1[2], state={k: st1[k] for k in ("ps", "ss", "pss", "sss")})
+        dt_md = time.perf_counter() - t0
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    nsf = n  # every butane site is of ghost type NONE
+    sf_gbs = nsf * 256.0 / (kms[5] * 1e-3) / 1e9 if kms[5] > 0 else None
+    out.update({"ms_per_step": ms, "pairs_in_cutoff": npairs, "value": npairs / (ms * 1e-3),
+                "unit": "pair-interactions/s",
+                "stage_ms": {"list": kms[0], "pair": kms[1], "intra_bonded": kms[2], "solid_fluid": kms[5],
+                             "total": kms[7]},
+                "sf_gather": {"bound": "hbm", "bytes_per_site": 256, "achieved_gbs": sf_gbs, "peak_gbs": hbm,
+                              "frac": (sf_gbs / hbm) if (sf_gbs and hbm) else None,
+                              "peak_basis": "of measured (MEASURED_PEAKS.json hbm_gbs)"},
+                "md": {"scheme": "NVT Nose-Hoover RESPA, 4 x 0.5 fs inner (bonded) + 2 fs outer", "steps": md_steps,
+                       "ms_per_outer_step": dt_md / md_steps * 1e3,
+                       "ns_per_day": md_steps * 2.0e-6 / dt_md * 86400.0}})
+    if fp64:
+        with Engine(s, precision="fp64", device=device) as e64:
+            t0 = time.perf_counter()
+            e64.sf_tasos_generate(1, spec(3.75, 98.0), nx, ny, nz, h, per)
+            e64.sf_tasos_generate(2, spec(3.95, 46.0), nx, ny, nz, h, per)
+            t_gen64 = time.perf_counter() - t0
+            ms64 = timed(e64, 3)
+            f64 = torch.cat([fl, fs]).clone()
+        err = float(torch.linalg.vector_norm(f32 - f64) / torch.linalg.vector_norm(f64))
+        out["fp64_path"] = {"ms_per_step": ms64, "mixed_over_fp64": ms64 / ms, "rms_rel_force_err_mixed_vs_fp64": err,
+                            "table_generation_s": t_gen64}
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from mspms2_gb300 import build
@@ -577,6 +681,7 @@ def run_ours(args, rank, world, local_rank):
         extras["hmc_batch"] = hmc_extras(local_rank)
         extras["derivatives"] = adjoint_extras(system, args.precision, local_rank)
         extras["force_matching"] = force_matching_extras(local_rank)
+        extras["c5_butane_tubes"] = c5_extras(local_rank)
         cpu =cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
         extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
                                   "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],

@@ -455,6 +455,11 @@ MG_API mg_status mg_sfgrid_sfgridgen(int device, const mg_sfgrid_spec *spec, dou
  * reference reads these tables from files made by a generator it does not include. */
 MG_API mg_status mg_sfgrid_tasos(int device, const mg_sfgrid_spec *spec, int nx, int ny, int nz, double hx,
                                  double hy, double hz, int precision, double *values);
+/* The same table evaluated on the context's device straight into its Tasos table `type`
+ * (as mg_sfgrid_tasos at the context's precision followed by mg_sf_tasos_set_grid with
+ * cell length cuc), with no copy through host memory. */
+MG_API mg_status mg_sf_tasos_generate(mg_ctx *ctx, int type, const mg_sfgrid_spec *spec, int nx, int ny, int nz,
+                                      double hx, double hy, double hz, double cuc);
 
 /* ---- reciprocal space without device allocation ---------------------------- */
 /* No counterpart in the reference: an extra entry point of this library.

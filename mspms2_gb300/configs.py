@@ -213,3 +213,68 @@ def ion_box(nside: int, seed: int, kmax: int, ksqmax: int, rc: float = 1.5, spac
     return System(species=species, box=np.array([box, box, box]), x=pts[:, 0].copy(), y=pts[:, 1].copy(),
                   z=pts[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc, charge_type=ELEC_EWALD,
                   kappa=kappa, kmax=(kmax, kmax, kmax), ksqmax=ksqmax, name=f"ions{n}")
+
+
+def armchair_tube(n: int, cx: float, cy: float, acc: float = 1.42):
+    """One axial period of an (n, n) armchair carbon nanotube centred at (cx, cy): 4n atoms
+    on a cylinder of radius 3 n acc / (2 pi); the period along z is sqrt(3) acc. Returns
+    (atoms [4n, 3], radius, period)."""
+    circ = 3.0 * acc * n
+    radius = circ / (2.0 * math.pi)
+    period = math.sqrt(3.0) * acc
+    pts = []
+    for k in range(n):
+        x0 = 3.0 * acc * k
+        for dx, z in ((0.0, 0.0), (acc, 0.0), (1.5 * acc, period / 2), (2.5 * acc, period / 2)):
+            th = 2.0 * math.pi * (x0 + dx) / circ
+            pts.append((cx + radius * math.cos(th), cy + radius * math.sin(th), z))
+    return np.array(pts), radius, period
+
+
+def butane_in_tube_bundle(seed: int = 2024, nmole: int = 20000, cell_xy: float = 127.0, box_z: float = 200.0,
+                          wall: float = 3.2, edge: float = 3.0, rc: float = 14.0):
+    """United-atom n-butane around and inside a hexagonal bundle of 7 rigid (11,11) carbon
+    nanotubes (diameter 14.9 A, 3.4 A wall-to-wall gaps), the bundle centred in a cell of
+    cell_xy x cell_xy A; the fluid box is cell_xy x cell_xy x box_z. Molecules stand along
+    the tube axis on a 4.2 x 4.2 x 6.45 A lattice, each turned about the axis by a seeded
+    random angle and flipped or not (closest contact between molecules 2.7 A); molecules
+    with a site within `wall` of a tube wall or within `edge` of the cell's x/y faces are
+    left out, and nmole of the rest (seeded choice) are kept. Returns (system, tubes) with
+    tubes = dict(atoms [n, 3] of one z period, period, radius, centres); the solid-fluid
+    tables (Tasos model, types 1 = CH3, 2 = CH2) are made from them on the device."""
+    rng = np.random.default_rng(seed)
+    tube, radius, period = armchair_tube(11, 0.0, 0.0)
+    spacing = 2.0 * radius + 3.4
+    c0 = cell_xy / 2.0
+    centres = [(c0, c0)] + [(c0 + spacing * math.cos(k * math.pi / 3), c0 + spacing * math.sin(k * math.pi / 3))
+                            for k in range(6)]
+    atoms = np.concatenate([tube + np.array([cx, cy, 0.0]) for cx, cy in centres])
+    nxy, nz = int(cell_xy // 4.2), int(box_z // 6.45)
+    g = np.stack(np.meshgrid(np.arange(nxy), np.arange(nxy), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    cen = (g + 0.5) * np.array([cell_xy / nxy, cell_xy / nxy, box_z / nz])
+    tm = butane_species(1).template_xyz
+    tm = tm - tm.mean(0)
+    base = np.stack([tm[:, 1], tm[:, 2], tm[:, 0]], 1)  # long axis along z, zig-zag along x
+    phi = rng.uniform(0.0, 2.0 * math.pi, len(cen))
+    flip = rng.choice([-1.0, 1.0], len(cen))
+    c, s_ = np.cos(phi)[:, None], np.sin(phi)[:, None]
+    sites = cen[:, None, :] + np.stack([base[None, :, 0] * c - base[None, :, 1] * s_,
+                                        base[None, :, 0] * s_ + base[None, :, 1] * c,
+                                        base[None, :, 2] * flip[:, None]], -1)  # [m, 4, 3]
+    keep = np.all((sites[..., 0] > edge) & (sites[..., 0] < cell_xy - edge) & (sites[..., 1] > edge) &
+                  (sites[..., 1] < cell_xy - edge), axis=1)
+    for cx, cy in centres:
+        rho = np.hypot(sites[..., 0] - cx, sites[..., 1] - cy)
+        keep &= np.all(np.abs(rho - radius) > wall, axis=1)
+    idx = np.flatnonzero(keep)
+    if len(idx) < nmole:
+        raise ValueError(f"only {len(idx)} molecules fit; lower nmole")
+    idx = np.sort(rng.permutation(idx)[:nmole])
+    xyz = sites[idx].reshape(-1, 3)
+    sp = butane_species(nmole)
+    s = System(species=[sp], box=np.array([cell_xy, cell_xy, box_z]), x=xyz[:, 0].copy(), y=xyz[:, 1].copy(),
+               z=xyz[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc, f0=0.5, name="butane_tube_bundle",
+               delt_fs=2.0, charge_type=ELEC_NONE)
+    s.sf_type = 3  # Tasos tables
+    s.treq_K = 300.0
+    return s, dict(atoms=atoms, period=period, radius=radius, centres=np.array(centres))

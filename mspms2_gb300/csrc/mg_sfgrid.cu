@@ -39,6 +39,8 @@ struct SgArgs {
     int nx, ny, nz;
     double x0, y0, z0, hx, hy, hz;
     double *out;          // sfgridgen: [13][nx*ny*nz]; Tasos: [nz][ny][nx][8]
+    float *out_f32;       // Tasos table written in FP32 instead (the mixed path's layout)
+    double *blockmin;     // per-block minimum of F (Tasos), or null
 };
 
 // g, g', g'', g''' of the switched LJ term at s = r^2 (derivatives with respect to s)
@@ -70,6 +72,9 @@ __device__ __forceinline__ void lj_s_derivs(R s, R sig2, R eps4, R ron2, R roff2
 }
 
 template <typename R>
+__device__ double sfgrid_node(const SgArgs &A, const double (*ss)[SG_MAX_SOLID], long long t);
+
+template <typename R>
 __global__ void __launch_bounds__(SG_TPB) k_sfgrid(SgArgs A) {
     __shared__ double ss[3][SG_MAX_SOLID];
     for (int i = threadIdx.x; i < A.nsolid; i += SG_TPB) {
@@ -80,7 +85,29 @@ __global__ void __launch_bounds__(SG_TPB) k_sfgrid(SgArgs A) {
     __syncthreads();
     const long long nn = (long long)A.nx * A.ny * A.nz;
     const long long t = (long long)blockIdx.x * SG_TPB + threadIdx.x;
+    if (A.blockmin) {  // every thread takes part in the block minimum below
+        double f0 = 10e10;  // the initial minPE of mylibtasos/grid.f90:75-97
+        if (t < nn) f0 = sfgrid_node<R>(A, ss, t);
+        __syncthreads();            // the solid atoms are no longer read:
+        double *smin = &ss[0][0];   // their first SG_TPB entries hold the block's minima
+        smin[threadIdx.x] = f0;
+        __syncthreads();
+        for (int o = SG_TPB / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) A.blockmin[blockIdx.x] = smin[0];
+        return;
+    }
     if (t >= nn) return;
+    sfgrid_node<R>(A, ss, t);
+}
+
+// one node: sums over the solid atoms and their z images, writes the node's values and
+// returns F
+template <typename R>
+__device__ double sfgrid_node(const SgArgs &A, const double (*ss)[SG_MAX_SOLID], long long t) {
+    const long long nn = (long long)A.nx * A.ny * A.nz;
     int ix, iy, iz;
     if (A.tasos) {  // I fastest
         ix = (int)(t % A.nx);
@@ -120,19 +147,19 @@ __global__ void __launch_bounds__(SG_TPB) k_sfgrid(SgArgs A) {
 #pragma unroll
     for (int k = 0; k < 11; k++) r[k] = (double)hi[k] + (double)lo[k];
     if (A.tasos) {  // F, Dx, Dy, Dz, Dxy, Dxz, Dyz, Dxyz
-        double *o = A.out + 8 * t;
-        o[0] = r[0];
-        o[1] = r[1];
-        o[2] = r[2];
-        o[3] = r[3];
-        o[4] = r[7];
-        o[5] = r[8];
-        o[6] = r[9];
-        o[7] = r[10];
+        const double v[8] = {r[0], r[1], r[2], r[3], r[7], r[8], r[9], r[10]};
+        if (A.out_f32) {
+            float *o = A.out_f32 + 8 * t;
+            for (int k = 0; k < 8; k++) o[k] = (float)v[k];
+        } else {
+            double *o = A.out + 8 * t;
+            for (int k = 0; k < 8; k++) o[k] = v[k];
+        }
     } else {  // Ene, dEx, dEy, dEz, dF = -Hessian: xx xy xz yx yy yz zx zy zz
         const double v[13] = {r[0], r[1], r[2], r[3], -r[4], -r[7], -r[8], -r[7], -r[5], -r[9], -r[8], -r[9], -r[6]};
         for (int k = 0; k < 13; k++) A.out[(size_t)k * nn + t] = v[k];
     }
+    return r[0];
 }
 
 mg_status run_grid(int device, const mg_sfgrid_spec *sp, SgArgs A, int precision, double *host_out, size_t out_doubles) {
@@ -246,4 +273,94 @@ extern "C" mg_status mg_sfgrid_tasos(int device, const mg_sfgrid_spec *sp, int n
     A.hy = hy;
     A.hz = hz;
     return run_grid(device, sp, A, precision, values, 8 * (size_t)nx * ny * nz);
+}
+
+namespace {
+__global__ void k_min_reduce(const double *__restrict__ in, int n, double *__restrict__ out) {
+    __shared__ double smin[256];
+    double m = 10e10;
+    for (int i = threadIdx.x; i < n; i += 256) m = fmin(m, in[i]);
+    smin[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = smin[0];
+}
+}  // namespace
+
+// A Tasos table evaluated on the device straight into the context's table `type`: the
+// same values as mg_sfgrid_tasos followed by mg_sf_tasos_set_grid, without the round
+// trip through host memory (1.3 GB per FP32 table for a 0.1 A grid over a 127 A bundle
+// cell). The table's minimum F (the PE flip threshold) is reduced on the device.
+extern "C" mg_status mg_sf_tasos_generate(mg_ctx *c, int type, const mg_sfgrid_spec *sp, int nx, int ny, int nz,
+                                         double hx, double hy, double hz, double cuc) {
+    if (!c || type < 1 || type > 64 || !spec_ok(sp) || nx < 3 || ny < 3 || nz < 3 || !(hx > 0 && hy > 0 && hz > 0) ||
+        !(cuc > 0))
+        return c ? mg_fail(c, MG_ERR_INVALID, "invalid Tasos grid") : MG_ERR_INVALID;
+    cudaSetDevice(c->device);
+    if ((int)c->tasos.size() < type) {
+        c->tasos.resize(type);
+        c->tasos_buf.resize(type);
+    }
+    const bool fp64 = c->opt.precision == MG_PREC_FP64;
+    const size_t nn = (size_t)nx * ny * nz;
+    if (!mg_ensure(c, c->tasos_buf[type - 1], (fp64 ? sizeof(double) : sizeof(float)) * 8 * nn)) return MG_ERR_ALLOC;
+    SgArgs A = base_args(sp, 1.0);  // K
+    A.tasos = 1;
+    A.nx = nx;
+    A.ny = ny;
+    A.nz = nz;
+    A.x0 = A.y0 = A.z0 = 0.0;
+    A.hx = hx;
+    A.hy = hy;
+    A.hz = hz;
+    if (fp64) A.out = (double *)c->tasos_buf[type - 1].p;
+    else A.out_f32 = (float *)c->tasos_buf[type - 1].p;
+    const size_t ns = (size_t)sp->nsolid;
+    std::vector<double> solid(3 * (ns ? ns : 1));
+    for (size_t i = 0; i < ns; i++) {
+        solid[i] = sp->sx[i];
+        solid[ns + i] = sp->sy[i];
+        solid[2 * ns + i] = sp->sz[i];
+    }
+    const unsigned blocks = (unsigned)((nn + SG_TPB - 1) / SG_TPB);
+    double *d_solid = nullptr, *d_min = nullptr;
+    cudaStream_t s = c->stream;
+    mg_status st = MG_OK;
+    if (cudaMalloc(&d_solid, sizeof(double) * solid.size()) != cudaSuccess ||
+        cudaMalloc(&d_min, sizeof(double) * ((size_t)blocks + 1)) != cudaSuccess) {
+        st = MG_ERR_ALLOC;
+    } else {
+        double mn = 0.0;
+        cudaMemcpyAsync(d_solid, solid.data(), sizeof(double) * solid.size(), cudaMemcpyHostToDevice, s);
+        A.solid = d_solid;
+        A.blockmin = d_min;
+        // the same arithmetic precision as mg_sfgrid_tasos with the context's precision
+        if (fp64) k_sfgrid<double><<<blocks, SG_TPB, 0, s>>>(A);
+        else k_sfgrid<float><<<blocks, SG_TPB, 0, s>>>(A);
+        k_min_reduce<<<1, 256, 0, s>>>(d_min, (int)blocks, d_min + blocks);
+        cudaMemcpyAsync(&mn, d_min + blocks, sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+            st = MG_ERR_CUDA;
+        } else {
+            TasosDev &t = c->tasos[type - 1];
+            t.nx = nx;
+            t.ny = ny;
+            t.nz = nz;
+            t.hx = hx;
+            t.hy = hy;
+            t.hz = hz;
+            t.cuc = cuc;
+            t.min_pe = mn;
+            t.values = c->tasos_buf[type - 1].p;
+        }
+    }
+    if (d_solid) cudaFree(d_solid);
+    if (d_min) cudaFree(d_min);
+    if (st) return mg_fail(c, st, "Tasos grid generation failed");
+    if (!mg_ensure(c, c->d_tasos, sizeof(TasosDev) * c->tasos.size())) return MG_ERR_ALLOC;
+    MG_CUDA(cudaMemcpy(c->d_tasos.p, c->tasos.data(), sizeof(TasosDev) * c->tasos.size(), cudaMemcpyHostToDevice));
+    return MG_OK;
 }

@@ -78,6 +78,7 @@ def load_library(path: str = LIB_PATH):
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.mg_sf_tasos_generate.argtypes = [V, I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, D]
     lib.mg_traj_open.argtypes = [V, C.c_char_p, I, C.c_char_p]
     lib.mg_traj_close.argtypes = [V, C.POINTER(C.c_longlong)]
     lib.mg_checkpoint_save.argtypes = [C.c_char_p, C.POINTER(capi.MgCheckpoint)]
@@ -279,6 +280,13 @@ class Engine:
         self._check(self.lib.mg_adjoint_hvp(self.ctx, _p(x), _p(y), _p(z), _p(v[0]), _p(v[1]), _p(v[2]),
                                             _p(h[0]), _p(h[1]), _p(h[2])))
         return h
+
+    def sf_tasos_generate(self, type_id: int, spec: dict, nx: int, ny: int, nz: int, h, cuc: float) -> None:
+        """Evaluates Tasos table type_id (1-based) on the device into the engine
+        (mg_sf_tasos_generate); spec as for sfgrid_tasos."""
+        c, _keep = _sfgrid_spec(spec)
+        self._check(self.lib.mg_sf_tasos_generate(self.ctx, type_id, C.byref(c), nx, ny, nz, float(h[0]), float(h[1]),
+                                                  float(h[2]), float(cuc)))
 
     def traj_open(self, path: str, every: int, names=None) -> None:
         """Attaches the reference's trajectory file (mg_traj_open): the integrators then

@@ -147,3 +147,33 @@ def test_gpu_tasos_table(prec):
         want = np.array([H[0, 1], H[0, 2], H[1, 2], T])
         got = v[k, j, i, 4:8]
         assert np.abs(got - want).max() <= tol * max(np.abs(want).max(), 1.0), (i, j, k, got, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_device_generated_table_matches_host_route(prec):
+    """mg_sf_tasos_generate (table evaluated into the engine on the device) gives the
+    engine the same table, bit for bit, as mg_sfgrid_tasos + mg_sf_tasos_set_grid."""
+    import ctypes as C
+
+    from mspms2_gb300 import build
+    from mspms2_gb300.engine import Engine, sfgrid_tasos
+    from mspms2_gb300.system import load_system
+    build.build()
+    s, _ = load_system(os.path.join(GOLDEN, "sf_tasos.npz"))  # sites inside the first 3 A of the cell
+    spec, _, _, _ = load("sfgrid_ch2_switch")
+    cuc = spec["ucl"][2]
+    nx = ny = 40
+    nz = 13
+    h = (0.2, 0.2, cuc / (nz - 1))
+    with Engine(s, precision=prec) as ea:
+        ea.sf_tasos_generate(1, spec, nx, ny, nz, h, cuc)
+        fa, _, ea_e = ea.compute()
+    v = np.ascontiguousarray(sfgrid_tasos(spec, nx, ny, nz, h, precision=prec), dtype=np.float64)
+    with Engine(s, precision=prec) as eb:
+        st = eb.lib.mg_sf_tasos_set_grid(eb.ctx, 1, nx, ny, nz, h[0], h[1], h[2], cuc,
+                                         v.ctypes.data_as(C.POINTER(C.c_double)))
+        assert st == 0
+        fb, _, eb_e = eb.compute()
+    assert np.array_equal(fa, fb)
+    assert ea_e["usflj"] == eb_e["usflj"] and ea_e["usflj"] != 0.0
