@@ -271,103 +271,100 @@ struct SearchArgs {
     unsigned *flags;
 };
 
-// Hits of i-cluster I against the clusters of candidate column number `c` (row-major over
-// the column window). With out >= 0 the entries are written from index out on.
-__device__ int column_hits(const SearchArgs &A, int I, const double *bi, const float *bif, int cx0, int cy0,
-                           int nx, int c, long long out) {
+// Images iz = -1, 0, 1 (bits 0, 1, 2) in which j-cluster J lies within rlist of i-cluster
+// I, for the column image (sx, sy): an FP32 band decides all but the borderline pairs,
+// which the exact FP64 predicate of the CPU builder decides.
+__device__ __forceinline__ unsigned cluster_images(const SearchArgs &A, const double *bi, const float *bif, int J,
+                                                   double sx, double sy, float sxf, float syf) {
+    const float *bjf = A.bbf + (size_t)J * 6;
+    const float dxyf = gap2f(bif[0], bif[3], bjf[0], bjf[3], sxf) + gap2f(bif[1], bif[4], bjf[1], bjf[4], syf);
+    if (dxyf > A.fhi) return 0u;
+    unsigned m = 0u;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float d2f = dxyf + gap2f(bif[2], bif[5], bjf[2], bjf[5], (float)(k - 1) * A.lzf);
+        bool hit;
+        if (d2f < A.flo) {
+            hit = true;
+        } else if (d2f > A.fhi) {
+            hit = false;
+        } else {  // FP64 decides, as the CPU builder does
+            const double *bj = A.bb + (size_t)J * 6;
+            const double sz = k == 1 ? 0.0 : (k == 2 ? A.lz : A.nlz);
+            double dxy = __dadd_rn(gap2(bi[0], bi[3], bj[0], bj[3], sx), gap2(bi[1], bi[4], bj[1], bj[4], sy));
+            double d2 = __dadd_rn(dxy, gap2(bi[2], bi[5], bj[2], bj[5], sz));
+            hit = d2 < A.rlist2;
+        }
+        if (hit) m |= 1u << k;
+    }
+    return m;
+}
+
+#define SEARCH_WPB 4     // warps (i-clusters) per block of k_search
+#define SEARCH_CAP 512   // entries one warp keeps in shared memory before it falls back
+
+// column number c of the window of an i-cluster: wrapped column indices, image offsets and
+// the conservative FP32 rejection of the column's x/y slab
+struct ColumnView {
+    int col, ix, iy;
+    float sxf, syf;
+    bool reject;
+};
+
+__device__ __forceinline__ ColumnView column_view(const SearchArgs &A, const float *bif, int cx0, int cy0, int nx,
+                                                  int c) {
+    ColumnView v;
     const int uy = cy0 + c / nx, ux = cx0 + c % nx;
     int wy = uy % A.ncy;
     if (wy < 0) wy += A.ncy;
-    const int iy = (uy - wy) / A.ncy;
+    v.iy = (uy - wy) / A.ncy;
     int wx = ux % A.ncx;
     if (wx < 0) wx += A.ncx;
-    const int ix = (ux - wx) / A.ncx;
+    v.ix = (ux - wx) / A.ncx;
     // image offsets (ix, iy in {-1, 0, 1}): exact in FP32 as (float)ix * (float)L
-    const float sxf = (float)ix * A.lxf, syf = (float)iy * A.lyf;
-    // conservative column rejection in FP32: the column's sites lie within its x/y slab;
-    // the FP32 error of the slab edges (~1e-5 A) is far inside the margin fmarg
-    {
-        float cx_lo = fmaf((float)wx, A.cwxf, sxf) - A.fmarg, cx_hi = fmaf((float)(wx + 1), A.cwxf, sxf) + A.fmarg;
-        float cy_lo = fmaf((float)wy, A.cwyf, syf) - A.fmarg, cy_hi = fmaf((float)(wy + 1), A.cwyf, syf) + A.fmarg;
-        float gx = fmaxf(0.f, fmaxf(cx_lo - bif[3], bif[0] - cx_hi));
-        float gy = fmaxf(0.f, fmaxf(cy_lo - bif[4], bif[1] - cy_hi));
-        if (gx * gx + gy * gy > A.fhi) return 0;
-    }
-    const int col = wy * A.ncx + wx;
-    const int j0 = A.col_cl_start[col], j1 = A.col_cl_start[col + 1];
-    if (j0 == j1) return 0;
-    // z brackets per image: zhi_J + s >= zlo_I - r and zlo_J + s <= zhi_I + r
-    int lo3[3], hi3[3];
-    const float r = (float)A.rlist + A.fmarg;
-    for (int k = 0; k < 3; k++) {
-        const float s = (float)(k - 1) * A.lzf;
-        const float zmin = bif[2] - r - s, zmax = bif[5] + r - s;
-        int a = j0, b = j1;  // first J with zhi >= zmin
-        while (a < b) {
-            int m = (a + b) >> 1;
-            if (A.bbf[(size_t)m * 6 + 5] < zmin) a = m + 1; else b = m;
-        }
-        int e = a, f = j1;  // first J with zlo > zmax
-        while (e < f) {
-            int m = (e + f) >> 1;
-            if (A.bbf[(size_t)m * 6 + 2] <= zmax) e = m + 1; else f = m;
-        }
-        lo3[k] = a;
-        hi3[k] = e;
-    }
-    int cnt = 0;
-    const int jlo = min(lo3[0], min(lo3[1], lo3[2])), jhi = max(hi3[0], max(hi3[1], hi3[2]));
-    for (int J = jlo; J < jhi; J++) {
-        bool inr = (J >= lo3[0] && J < hi3[0]) || (J >= lo3[1] && J < hi3[1]) || (J >= lo3[2] && J < hi3[2]);
-        if (!inr) continue;
-        const float *bjf = A.bbf + (size_t)J * 6;
-        float dxyf = gap2f(bif[0], bif[3], bjf[0], bjf[3], sxf) + gap2f(bif[1], bif[4], bjf[1], bjf[4], syf);
-        if (dxyf > A.fhi) continue;
-        const double *bj = A.bb + (size_t)J * 6;
-        int hits = 0;
-        // ix * lx for ix in {-1, 0, 1}, selected rather than multiplied (FP64 is slow here)
-        const double sx = ix == 0 ? 0.0 : (ix > 0 ? A.lx : A.nlx);
-        const double sy = iy == 0 ? 0.0 : (iy > 0 ? A.ly : A.nly);
-        for (int iz = -1; iz <= 1; iz++) {
-            float d2f = dxyf + gap2f(bif[2], bif[5], bjf[2], bjf[5], (float)iz * A.lzf);
-            bool hit;
-            if (d2f < A.flo) {
-                hit = true;
-            } else if (d2f > A.fhi) {
-                hit = false;
-            } else {  // FP64 decides, as the CPU builder does
-                const double sz = iz == 0 ? 0.0 : (iz > 0 ? A.lz : A.nlz);
-                double dxy = __dadd_rn(gap2(bi[0], bi[3], bj[0], bj[3], sx), gap2(bi[1], bi[4], bj[1], bj[4], sy));
-                double d2 = __dadd_rn(dxy, gap2(bi[2], bi[5], bj[2], bj[5], sz));
-                hit = d2 < A.rlist2;
-            }
-            if (!hit) continue;
-            hits++;
-            if (out >= 0) {
-                const long long o = out + cnt;
-                const double *ri = A.ref + (size_t)I * 3, *rj = A.ref + (size_t)J * 3;
-                const double sz = iz == 0 ? 0.0 : (iz > 0 ? A.lz : A.nlz);
-                const double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], sx));
-                const double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], sy));
-                const double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], sz));
-                A.pair_j[o] = J;
-                A.pair_img[o] = ((ix + 512) & 1023) | (((iy + 512) & 1023) << 10) | (((iz + 512) & 1023) << 20);
-                if (A.fp64)
-                    ((double4 *)A.pair_shift)[o] = make_double4(s0, s1, s2, 0.0);
-                else
-                    ((float4 *)A.pair_shift)[o] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
-            }
-            cnt++;
-        }
-        if (hits > 1) atomicOr(A.flags, MG_FLAG_SMALL_BOX);
-    }
-    return cnt;
+    v.sxf = (float)v.ix * A.lxf;
+    v.syf = (float)v.iy * A.lyf;
+    // the column's sites lie within its x/y slab; the FP32 error of the slab edges
+    // (~1e-5 A) is far inside the margin fmarg
+    const float cx_lo = fmaf((float)wx, A.cwxf, v.sxf) - A.fmarg, cx_hi = fmaf((float)(wx + 1), A.cwxf, v.sxf) + A.fmarg;
+    const float cy_lo = fmaf((float)wy, A.cwyf, v.syf) - A.fmarg, cy_hi = fmaf((float)(wy + 1), A.cwyf, v.syf) + A.fmarg;
+    const float gx = fmaxf(0.f, fmaxf(cx_lo - bif[3], bif[0] - cx_hi));
+    const float gy = fmaxf(0.f, fmaxf(cy_lo - bif[4], bif[1] - cy_hi));
+    v.reject = gx * gx + gy * gy > A.fhi;
+    v.col = wy * A.ncx + wx;
+    return v;
 }
 
-__global__ void k_search(SearchArgs A) {
+__device__ __forceinline__ double image_shift(int i, double l, double nl) { return i == 0 ? 0.0 : (i > 0 ? l : nl); }
+
+// writes entry o: j-cluster J in image (ix, iy, iz) of i-cluster I (reference point ri)
+__device__ __forceinline__ void put_entry(const SearchArgs &A, long long o, const double *ri, int J, int ix, int iy,
+                                          int iz) {
+    const double *rj = A.ref + (size_t)J * 3;
+    const double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], image_shift(ix, A.lx, A.nlx)));
+    const double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], image_shift(iy, A.ly, A.nly)));
+    const double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], image_shift(iz, A.lz, A.nlz)));
+    A.pair_j[o] = J;
+    A.pair_img[o] = ((ix + 512) & 1023) | (((iy + 512) & 1023) << 10) | (((iz + 512) & 1023) << 20);
+    if (A.fp64)
+        ((double4 *)A.pair_shift)[o] = make_double4(s0, s1, s2, 0.0);
+    else
+        ((float4 *)A.pair_shift)[o] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
+}
+
+// One warp per i-cluster. Entries are ordered by candidate column (row-major over the
+// column window), then j-cluster, then z image (-1, 0, 1), as the CPU builder orders them.
+// The warp takes 32 columns at a time (one lane per column: its rejection test and its
+// cluster range), lays their clusters out in that order and tests 32 of them at a time,
+// one per lane, so that many loads are in flight. Hits go to a shared-memory buffer and
+// are written after one reservation; a warp whose buffer would overflow counts and writes
+// in two passes instead.
+__global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
+    __shared__ int s_j[SEARCH_WPB][SEARCH_CAP];
+    __shared__ int s_code[SEARCH_WPB][SEARCH_CAP];  // image bits: (ix+1) | (iy+1) << 2 | (iz+1) << 4
     if (!A.meta[META_NEED]) return;
-    const int lane = threadIdx.x & 31;
-    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int I = blockIdx.x * SEARCH_WPB + w;
     if (I >= A.meta[META_NCL]) return;
     double bi[6];
     float bif[6];
@@ -389,36 +386,106 @@ __global__ void k_search(SearchArgs A) {
         return;
     }
     const int ncand = nx * ny;
-    int total = 0;
-    for (int base = 0; base < ncand; base += 32) {
-        int c = base + lane;
-        int h = c < ncand ? column_hits(A, I, bi, bif, cx0, cy0, nx, c, -1) : 0;
-        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-        total += h;
-    }
-    unsigned long long off = 0;
-    if (lane == 0) off = atomicAdd(A.counter, (unsigned long long)total);
-    off = __shfl_sync(0xffffffffu, off, 0);
-    if (lane == 0) {
-        A.pair_start[I] = (int)off;
-        A.pair_cnt[I] = total;
-    }
-    if ((long long)(off + total) > A.cap) {
-        if (lane == 0) atomicOr(A.flags, MG_FLAG_LIST_OVERFLOW);
-        if (lane == 0) A.pair_cnt[I] = 0;
-        return;
-    }
-    long long run = (long long)off;
-    for (int base = 0; base < ncand; base += 32) {
-        int c = base + lane;
-        int h = c < ncand ? column_hits(A, I, bi, bif, cx0, cy0, nx, c, -1) : 0;
-        int incl = h;
-        for (int o = 1; o < 32; o <<= 1) {
-            int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
+    const double *ri = A.ref + (size_t)I * 3;
+    // mode 0: into shared memory; 1: count only (buffer too small); 2: write from run
+    long long run = 0;
+    bool multi = false;
+    for (int mode = 0; mode < 3; mode++) {
+        for (int base = 0; base < ncand; base += 32) {
+            const int c = base + lane;
+            int cnt = 0, j0 = 0;
+            ColumnView v;
+            v.ix = v.iy = 0;
+            v.sxf = v.syf = 0.f;
+            if (c < ncand) {
+                v = column_view(A, bif, cx0, cy0, nx, c);
+                if (!v.reject) {
+                    j0 = A.col_cl_start[v.col];
+                    cnt = A.col_cl_start[v.col + 1] - j0;
+                }
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int excl = incl - cnt, T = __shfl_sync(0xffffffffu, incl, 31);
+            for (int t0 = 0; t0 < T; t0 += 32) {
+                const int t = t0 + lane;
+                int k = 0;  // the column lane of item t: the number of columns with incl <= t
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int probe = __shfl_sync(0xffffffffu, incl, k + step - 1);
+                    if (probe <= t) k += step;
+                }
+                k = min(k, 31);
+                const int jk = __shfl_sync(0xffffffffu, j0, k), ek = __shfl_sync(0xffffffffu, excl, k);
+                const int ixk = __shfl_sync(0xffffffffu, v.ix, k), iyk = __shfl_sync(0xffffffffu, v.iy, k);
+                const float sxf = __shfl_sync(0xffffffffu, v.sxf, k), syf = __shfl_sync(0xffffffffu, v.syf, k);
+                const int J = jk + (t - ek);
+                unsigned m = 0u;
+                if (t < T)
+                    m = cluster_images(A, bi, bif, J, image_shift(ixk, A.lx, A.nlx), image_shift(iyk, A.ly, A.nly),
+                                       sxf, syf);
+                const int h = __popc(m);
+                multi |= h > 1;
+                int hi = h;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int q = __shfl_up_sync(0xffffffffu, hi, o);
+                    if (lane >= o) hi += q;
+                }
+                if (h > 0) {
+                    long long o = run + hi - h;
+                    for (int b = 0; b < 3; b++) {
+                        if (!(m & (1u << b))) continue;
+                        if (mode == 0) {
+                            if (o < SEARCH_CAP) {
+                                s_j[w][o] = J;
+                                s_code[w][o] = (ixk + 1) | ((iyk + 1) << 2) | (b << 4);
+                            }
+                        } else if (mode == 2) {
+                            put_entry(A, o, ri, J, ixk, iyk, b - 1);
+                        }
+                        o++;
+                    }
+                }
+                run += __shfl_sync(0xffffffffu, hi, 31);
+            }
         }
-        if (h > 0) column_hits(A, I, bi, bif, cx0, cy0, nx, c, run + incl - h);
-        run += __shfl_sync(0xffffffffu, incl, 31);
+        if (mode == 2) return;
+        if (mode == 1 || run <= SEARCH_CAP) {
+            if (__any_sync(0xffffffffu, multi) && lane == 0) atomicOr(A.flags, MG_FLAG_SMALL_BOX);
+            const long long total = run;
+            unsigned long long off = 0;
+            if (lane == 0) off = atomicAdd(A.counter, (unsigned long long)total);
+            off = __shfl_sync(0xffffffffu, off, 0);
+            if (lane == 0) {
+                A.pair_start[I] = (int)off;
+                A.pair_cnt[I] = (int)total;
+            }
+            if ((long long)(off + total) > A.cap) {
+                if (lane == 0) {
+                    atomicOr(A.flags, MG_FLAG_LIST_OVERFLOW);
+                    A.pair_cnt[I] = 0;
+                }
+                return;
+            }
+            if (mode == 0) {  // the buffer holds every entry: write them out
+                __syncwarp();
+                for (int e = lane; e < (int)total; e += 32) {
+                    const int code = s_code[w][e];
+                    put_entry(A, (long long)off + e, ri, s_j[w][e], (code & 3) - 1, ((code >> 2) & 3) - 1,
+                              ((code >> 4) & 3) - 1);
+                }
+                return;
+            }
+            run = (long long)off;
+            mode = 1;  // next: the writing pass
+        } else {
+            run = 0;   // too many entries for the buffer: count again, then write
+        }
     }
 }
 
@@ -652,8 +719,8 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         A.cap = c->pair_cap;
         A.fp64 = fp64;
         A.flags = (unsigned *)c->d_flags.p;
-        unsigned blocks = (unsigned)(((long long)c->cl_cap * 32 + 127) / 128);
-        k_search<<<blocks, 128, 0, s>>>(A);
+        unsigned blocks = (unsigned)(((long long)c->cl_cap + SEARCH_WPB - 1) / SEARCH_WPB);
+        k_search<<<blocks, SEARCH_WPB * 32, 0, s>>>(A);
     }
     k_finish<<<1, 1, 0, s>>>(meta, (unsigned long long *)c->d_counter.p);
     MG_CUDA(cudaGetLastError());
