@@ -240,6 +240,27 @@ MG_API mg_status mg_compute_device(mg_ctx *ctx, const double *d_x, const double 
                             double *d_fxl, double *d_fyl, double *d_fzl,
                             double *d_fxs, double *d_fys, double *d_fzs, mg_energies *e);
 MG_API mg_status mg_get_stats(const mg_ctx *ctx, mg_stats *s);
+
+/* ---- autotuning (no reference counterpart) ------------------------------------- */
+/* The launch geometry the engine picks per system: the cell size of the neighbour-list
+ * grid (column width, as a factor of the default min((8 V/N)^(1/3), 0.75 r_list)), the
+ * cluster size (the largest z extent of a cluster, as a factor of the column width;
+ * clusters hold at most 8 sites) and the threads per site of the reciprocal-space force
+ * pass (2, 4 or 8). Results are reproducible for a given geometry; two geometries sum in
+ * different orders, so their results agree to rounding, not bit for bit. */
+typedef struct mg_tuning {
+    double cell_scale, zcap_scale;
+    int kforce_threads;
+    double ms_default, ms_tuned;  /* one evaluation with the default and the chosen geometry */
+    int configs_tried;
+} mg_tuning;
+/* Times evaluations of `terms` at host positions x, y, z over a small set of geometries
+ * (threads per site first, then cell size x cluster size) and keeps the fastest. */
+MG_API mg_status mg_autotune(mg_ctx *ctx, const double *x, const double *y, const double *z, int terms,
+                             mg_tuning *out);
+/* Applies a geometry found before (scales within 0.5..2, threads 2, 4 or 8). */
+MG_API mg_status mg_set_tuning(mg_ctx *ctx, const mg_tuning *t);
+MG_API mg_status mg_get_tuning(const mg_ctx *ctx, mg_tuning *t);
 /* Device status word of the last call: bit 0 out-of-grid, bit 1 non-finite result,
  * bit 2 list overflow, bit 3 column overflow. */
 MG_API mg_status mg_get_device_flags(const mg_ctx *ctx, unsigned *flags);

@@ -98,6 +98,14 @@ NPT_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "vts", "vbs", "rts", "uts
                  "boxv"]
 
 
+class MgTuning(C.Structure):
+    _fields_ = [("cell_scale", C.c_double), ("zcap_scale", C.c_double), ("kforce_threads", C.c_int),
+                ("ms_default", C.c_double), ("ms_tuned", C.c_double), ("configs_tried", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 NCOUNTS = 40
 
 

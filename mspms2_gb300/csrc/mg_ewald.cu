@@ -396,14 +396,15 @@ __global__ void k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row
     mg_block_row<1>(e, ids, A.rows_e, A.row0 + blockIdx.x);
 }
 
-template <typename R>
-__global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa) {
+// FG thread groups share the rows of a site (the threads per site; tuned per context)
+template <typename R, int FG = EW_FG>
+__global__ void __launch_bounds__(FG * EW_FSITES) k_kforce(EwArgs A, int maxa) {
     typedef typename C2<R>::T T2;
     typedef typename C2<R>::T4 T4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T4 *sC = (T4 *)smem_raw;  // [EW_FROWS][maxa]: conj(c S+_a), c S-_a
     __shared__ int4 sRow[EW_FROWS];
-    __shared__ double sF[EW_FG][3][EW_FSITES];
+    __shared__ double sF[FG][3][EW_FSITES];
     const int g = threadIdx.x / EW_FSITES, l = threadIdx.x % EW_FSITES;
     const int a = blockIdx.x * EW_FSITES + l;
     const bool act = a < A.n;
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa
         __syncthreads();
         if (!act) continue;
         R fx = 0, fy = 0, fz = 0;
-        for (int rr = g; rr < nr; rr += EW_FG) {
+        for (int rr = g; rr < nr; rr += FG) {
             const int4 row = sRow[rr];
             T2 X = tX[(size_t)row.x * A.n + a];
             T2 Y = tY[(size_t)(row.y < 0 ? -row.y : row.y) * A.n + a];
@@ -472,7 +473,7 @@ __global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa
     __syncthreads();
     if (g != 0 || !act) return;
     double fxs = 0, fys = 0, fzs = 0;
-    for (int k = 0; k < EW_FG; k++) {
+    for (int k = 0; k < FG; k++) {
         fxs += sF[k][0][l];
         fys += sF[k][1][l];
         fzs += sF[k][2][l];
@@ -481,6 +482,26 @@ __global__ void __launch_bounds__(EW_FG * EW_FSITES) k_kforce(EwArgs A, int maxa
     A.f[a] += q * fxs * A.twopi[0];
     A.f[A.n + a] += q * fys * A.twopi[1];
     A.f[2 * A.n + a] += q * fzs * A.twopi[2];
+}
+
+// k_kforce with fg threads per site (2, 4 or 8) and its dynamic shared memory
+template <typename R>
+cudaError_t launch_kforce(int fg, unsigned blocks, size_t smem, cudaStream_t s, const EwArgs &A, int maxa) {
+    cudaError_t e;
+    switch (fg) {
+    case 2:
+        e = cudaFuncSetAttribute(k_kforce<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_kforce<R, 2><<<blocks, 2 * EW_FSITES, smem, s>>>(A, maxa);
+        break;
+    case 8:
+        e = cudaFuncSetAttribute(k_kforce<R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_kforce<R, 8><<<blocks, 8 * EW_FSITES, smem, s>>>(A, maxa);
+        break;
+    default:
+        e = cudaFuncSetAttribute(k_kforce<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_kforce<R, 4><<<blocks, 4 * EW_FSITES, smem, s>>>(A, maxa);
+    }
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 }  // namespace
@@ -624,14 +645,10 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
     size_t fsmem = 2 * esz * (size_t)EW_FROWS * maxa;
     unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
-    if (fp64) {
-        MG_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-        k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
-    } else {
-        MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
-    }
-    MG_CUDA(cudaGetLastError());
+    if (fp64)
+        MG_CUDA(launch_kforce<double>(c->tune.kforce_threads, fblocks, fsmem, s, A, maxa));
+    else
+        MG_CUDA(launch_kforce<float>(c->tune.kforce_threads, fblocks, fsmem, s, A, maxa));
     c->launches += 4;
     return MG_OK;
 }

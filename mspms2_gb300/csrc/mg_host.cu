@@ -750,3 +750,121 @@ extern "C" mg_status mg_get_device_flags(const mg_ctx *c, unsigned *flags) {
     *flags = c->last_flags;
     return MG_OK;
 }
+
+// ---------------------------------------------------------------------------------
+// autotuning of the launch geometry
+// ---------------------------------------------------------------------------------
+static void tuning_out(const mg_ctx *c, mg_tuning *t) {
+    t->cell_scale = c->tune.cell_scale;
+    t->zcap_scale = c->tune.zcap_scale;
+    t->kforce_threads = c->tune.kforce_threads;
+}
+
+extern "C" mg_status mg_get_tuning(const mg_ctx *c, mg_tuning *t) {
+    if (!c || !t) return MG_ERR_INVALID;
+    memset(t, 0, sizeof(*t));
+    tuning_out(c, t);
+    return MG_OK;
+}
+
+extern "C" mg_status mg_set_tuning(mg_ctx *c, const mg_tuning *t) {
+    if (!c || !t) return MG_ERR_INVALID;
+    if (!(t->cell_scale >= 0.5 && t->cell_scale <= 2.0) || !(t->zcap_scale >= 0.5 && t->zcap_scale <= 2.0) ||
+        !(t->kforce_threads == 2 || t->kforce_threads == 4 || t->kforce_threads == 8))
+        return mg_fail(c, MG_ERR_INVALID, "tuning out of range (scales 0.5-2, threads 2, 4 or 8)");
+    c->tune.cell_scale = t->cell_scale;
+    c->tune.zcap_scale = t->zcap_scale;
+    c->tune.kforce_threads = t->kforce_threads;
+    c->tune.tuned = true;
+    c->list_valid = false;  // the grid follows the new geometry at the next call
+    return MG_OK;
+}
+
+extern "C" mg_status mg_autotune(mg_ctx *c, const double *x, const double *y, const double *z, int terms,
+                                 mg_tuning *out) {
+    if (!c || !x || !y || !z || !(terms & MG_TERMS_ALL)) return MG_ERR_INVALID;
+    if (!c->have_topology || !c->have_params || !c->have_box)
+        return mg_fail(c, MG_ERR_STATE, "set topology, params and box before tuning");
+    cudaSetDevice(c->device);
+    const size_t nb = sizeof(double) * c->natom;
+    if (!mg_ensure(c, c->d_x, 3 * nb) || !mg_ensure(c, c->d_fl, 3 * nb) || !mg_ensure(c, c->d_fs, 3 * nb))
+        return MG_ERR_ALLOC;
+    double *dx = (double *)c->d_x.p, *dy = dx + c->natom, *dz = dy + c->natom;
+    cudaStream_t s = c->stream;
+    MG_CUDA(cudaMemcpyAsync(dx, x, nb, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(dy, y, nb, cudaMemcpyHostToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(dz, z, nb, cudaMemcpyHostToDevice, s));
+    cudaEvent_t e0, e1;
+    MG_CUDA(cudaEventCreate(&e0));
+    MG_CUDA(cudaEventCreate(&e1));
+    int tried = 0;
+    // one evaluation (after one untimed call that rebuilds the list for the geometry):
+    // the fastest of three, so that one slow launch does not decide
+    auto timed = [&](float *ms) -> mg_status {
+        c->list_valid = false;
+        mg_status st = mg_compute_forces(c, dx, dy, dz, terms, (double *)c->d_fl.p, (double *)c->d_fs.p, nullptr);
+        if (st) return st;
+        float best = 1e30f;
+        for (int r = 0; r < 3; r++) {
+            MG_CUDA(cudaEventRecord(e0, s));
+            if ((st = mg_compute_forces(c, dx, dy, dz, terms, (double *)c->d_fl.p, (double *)c->d_fs.p, nullptr)))
+                return st;
+            MG_CUDA(cudaEventRecord(e1, s));
+            MG_CUDA(cudaEventSynchronize(e1));
+            float t = 0.f;
+            MG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+            best = std::min(best, t);
+        }
+        tried++;
+        *ms = best;
+        return MG_OK;
+    };
+    const MgTuning keep = c->tune;
+    c->tune = MgTuning();
+    float base = 0.f, ms = 0.f;
+    mg_status st = timed(&base);
+    MgTuning best = c->tune;
+    float best_ms = base;
+    if (!st && c->params.charge_type == MG_ELEC_EWALD && (terms & MG_TERMS_LONG)) {
+        for (int fg : {2, 8}) {
+            c->tune = best;
+            c->tune.kforce_threads = fg;
+            if ((st = timed(&ms))) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c->tune;
+            }
+        }
+    }
+    const double cells[3] = {0.8, 1.0, 1.25}, zcaps[3] = {0.75, 1.0, 1.5};
+    const MgTuning row = best;
+    for (int i = 0; i < 3 && !st; i++)
+        for (int j = 0; j < 3 && !st; j++) {
+            if (cells[i] == 1.0 && zcaps[j] == 1.0) continue;  // measured above
+            c->tune = row;
+            c->tune.cell_scale = cells[i];
+            c->tune.zcap_scale = zcaps[j];
+            if ((st = timed(&ms))) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c->tune;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) {
+        c->tune = keep;
+        c->list_valid = false;
+        return st;
+    }
+    c->tune = best;
+    c->tune.tuned = true;
+    c->list_valid = false;
+    if (out) {
+        tuning_out(c, out);
+        out->ms_default = base;
+        out->ms_tuned = best_ms;
+        out->configs_tried = tried;
+    }
+    return MG_OK;
+}

@@ -106,8 +106,17 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// launch geometry picked by mg_autotune (defaults until it runs)
+struct MgTuning {
+    double cell_scale = 1.0;   // list column width relative to the default
+    double zcap_scale = 1.0;   // cluster z extent relative to the column width
+    int kforce_threads = 4;    // threads per site in the k-space force pass (2, 4, 8)
+    bool tuned = false;
+};
+
 struct mg_ctx {
     mg_options opt;
+    MgTuning tune;
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;

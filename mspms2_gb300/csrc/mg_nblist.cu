@@ -582,12 +582,12 @@ __global__ void k_pack(int n, const int *__restrict__ meta, const int *__restric
 // ---------------------------------------------------------------------------------
 static void choose_grid(mg_ctx *c, double rlist) {
     double vol = c->lx * c->ly * c->lz;
-    double cw = std::min(cbrt(8.0 * vol / c->natom), 0.75 * rlist) / pow(1.5, c->col_refine);
+    double cw = std::min(cbrt(8.0 * vol / c->natom), 0.75 * rlist) * c->tune.cell_scale / pow(1.5, c->col_refine);
     c->ncx = std::max(1, (int)floor(c->lx / cw));
     c->ncy = std::max(1, (int)floor(c->ly / cw));
-    c->zcap = cw;
+    c->zcap = cw * c->tune.zcap_scale;
     c->small_box = c->small_box_forced || c->lx < 2.0 * rlist + 2.0 * (c->lx / c->ncx) ||
-                   c->ly < 2.0 * rlist + 2.0 * (c->ly / c->ncy) || c->lz < 2.0 * rlist + 2.0 * cw;
+                   c->ly < 2.0 * rlist + 2.0 * (c->ly / c->ncy) || c->lz < 2.0 * rlist + 2.0 * std::max(cw, c->zcap);
 }
 
 // Size every list buffer for the current grid; called when the grid or capacity changes.

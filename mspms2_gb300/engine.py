@@ -79,6 +79,9 @@ def load_library(path: str = LIB_PATH):
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.mg_sf_tasos_generate.argtypes = [V, I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, D]
+    lib.mg_autotune.argtypes = [V, _dp, _dp, _dp, I, C.POINTER(capi.MgTuning)]
+    lib.mg_set_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
+    lib.mg_get_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
     lib.mg_traj_open.argtypes = [V, C.c_char_p, I, C.c_char_p]
     lib.mg_traj_close.argtypes = [V, C.POINTER(C.c_longlong)]
     lib.mg_checkpoint_save.argtypes = [C.c_char_p, C.POINTER(capi.MgCheckpoint)]
@@ -287,6 +290,26 @@ class Engine:
         c, _keep = _sfgrid_spec(spec)
         self._check(self.lib.mg_sf_tasos_generate(self.ctx, type_id, C.byref(c), nx, ny, nz, float(h[0]), float(h[1]),
                                                   float(h[2]), float(cuc)))
+
+    def autotune(self, x=None, y=None, z=None, terms: int = TERMS_ALL) -> dict:
+        """Picks the launch geometry (cell size, cluster size, threads per site of the
+        k-space force pass) by timing evaluations at these positions (mg_autotune)."""
+        s = self.system
+        x = np.ascontiguousarray(s.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(s.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(s.z if z is None else z, dtype=np.float64)
+        t = capi.MgTuning()
+        self._check(self.lib.mg_autotune(self.ctx, _p(x), _p(y), _p(z), terms, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, cell_scale: float = 1.0, zcap_scale: float = 1.0, kforce_threads: int = 4) -> None:
+        t = capi.MgTuning(cell_scale=cell_scale, zcap_scale=zcap_scale, kforce_threads=kforce_threads)
+        self._check(self.lib.mg_set_tuning(self.ctx, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = capi.MgTuning()
+        self._check(self.lib.mg_get_tuning(self.ctx, C.byref(t)))
+        return t.as_dict()
 
     def traj_open(self, path: str, every: int, names=None) -> None:
         """Attaches the reference's trajectory file (mg_traj_open): the integrators then

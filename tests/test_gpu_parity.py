@@ -157,3 +157,40 @@ def test_pair_count_matches_oracle():
         npair = eng.stats()["pairs_within_cutoff"]
     want = Oracle(s).count_pairs(max(s.rcutoff, s.rcutoffelec))
     assert abs(npair - want) <= 2
+
+
+@pytest.mark.parametrize("geometry", [(0.8, 1.5, 2), (1.25, 0.75, 8)])
+def test_tuned_geometry_keeps_parity(geometry):
+    """Any launch geometry the autotuner may pick (cell size, cluster size, threads per
+    site of the k-space force pass) keeps the list bit-exact against the CPU builder on that
+    grid and the forces within the parity tolerances."""
+    from oracle.pyoracle import nblist
+    cell, zcap, fg = geometry
+    s, d = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    for prec in ("mixed", "fp64"):
+        with Engine(s, precision=prec) as eng:
+            eng.set_tuning(cell, zcap, fg)
+            fl, fs, e = eng.compute()
+            g = eng.debug_list()
+            assert eng.tuning()["kforce_threads"] == fg
+        assert rel(fl, d["ref_fl"]) <= TOL[prec], (prec, rel(fl, d["ref_fl"]))
+        assert rel(fs, d["ref_fs"]) <= TOL[prec]
+    rlist = max(s.rcutoff, s.rcutoffelec)
+    c = nblist(s.x, s.y, s.z, tuple(float(v) for v in s.box), rlist, g["grid"][0], g["grid"][1], g["grid"][2],
+               g["zcap"])
+    assert np.array_equal(g["clusters"], c["clusters"])
+    assert np.array_equal(g["pairs"], c["pairs"])
+    assert np.array_equal(g["shifts"], c["shifts"])
+
+
+def test_autotune_picks_a_valid_faster_geometry():
+    s, d = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    with Engine(s, precision="mixed") as eng:
+        t = eng.autotune()
+        assert t["kforce_threads"] in (2, 4, 8) and 0.5 <= t["cell_scale"] <= 2 and 0.5 <= t["zcap_scale"] <= 2
+        assert t["configs_tried"] == 11 and 0 < t["ms_tuned"] <= t["ms_default"]
+        fl, fs, e = eng.compute()
+        assert rel(fl, d["ref_fl"]) <= TOL["mixed"]
+        from mspms2_gb300.engine import EngineError
+        with pytest.raises(EngineError):
+            eng.set_tuning(3.0, 1.0, 4)
