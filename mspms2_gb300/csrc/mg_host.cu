@@ -128,7 +128,8 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_flags, &c->d_tasos, &c->d_myinterp, &c->d_tubes, &c->d_solid,
                       &c->d_meta, &c->d_pair_img, &c->d_cl_bbf, &c->d_col_ncl, &c->d_counter,
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
-                      &c->d_adj_class, &c->d_adj, &c->d_adj_g};
+                      &c->d_adj_class, &c->d_adj, &c->d_adj_g,
+                      &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
     for (auto &b : c->myinterp_buf) mg_free(b);
@@ -198,7 +199,7 @@ extern "C" mg_status mg_set_params(mg_ctx *c, const mg_params *p) {
     bool kchange = !c->have_params || memcmp(c->params.kmax, p->kmax, sizeof(p->kmax)) != 0 ||
                    c->params.ksqmax != p->ksqmax || c->params.charge_type != p->charge_type;
     bool listchange = !c->have_params || c->params.rcutoff != p->rcutoff ||
-                      c->params.rcutoffelec != p->rcutoffelec;
+                      c->params.rcutoffelec != p->rcutoffelec || c->params.respa_split != p->respa_split;
     c->params = *p;
     c->have_params = true;
     if (listchange) c->list_valid = false;

@@ -164,6 +164,9 @@ struct mg_ctx {
     int cl_cap = 0;            // cluster capacity
     long long pair_cap = 0;    // cluster-pair entry capacity
     DevBuf d_pair_start, d_pair_count, d_pair_j, d_pair_shift;
+    // inner sub-list of the distance split (cluster pairs within respa_split + skin)
+    DevBuf d_sub_start, d_sub_count, d_sub_j, d_sub_shift;
+    bool sub_ready = false;
     DevBuf d_pack_pos, d_pack_lj, d_pack_info;
     // integration (mg_md_run): velocities, solver work arrays, 1/mass, partial sums,
     // thermostat scalars, per-step records

@@ -489,6 +489,64 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
     }
 }
 
+// Inner sub-list for the short (RESPA inner) pair pass: per i-cluster, in list order, the
+// entries whose cluster boxes (at build positions, in the entry's image) lie within
+// rsub = respa_split + skin. Any site pair closer than respa_split now was closer than
+// rsub at the build, because no site has moved by more than skin/2 since; the FP32 test
+// has a small positive margin, so it keeps every such entry. One warp per i-cluster:
+// a counting pass, one reservation, an order-keeping compaction pass.
+__global__ void k_sublist(const int *__restrict__ meta, const int *__restrict__ pair_start,
+                          const int *__restrict__ pair_cnt, const int *__restrict__ pair_j,
+                          const void *__restrict__ pair_shift, const int *__restrict__ pair_img,
+                          const float *__restrict__ bbf, float lx, float ly, float lz, float rsub2, int fp64,
+                          int *__restrict__ sub_start, int *__restrict__ sub_cnt, int *__restrict__ sub_j,
+                          void *__restrict__ sub_shift, unsigned long long *__restrict__ counter) {
+    if (!meta[META_NEED]) return;
+    const int lane = threadIdx.x & 31;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= meta[META_NCL]) return;
+    const int e0 = pair_start[I], n = pair_cnt[I];
+    float bi[6];
+    for (int d = 0; d < 6; d++) bi[d] = bbf[(size_t)I * 6 + d];
+    auto keep = [&](int k) -> bool {
+        if (k >= n) return false;
+        const int e = e0 + k, J = pair_j[e], img = pair_img[e];
+        const float sh[3] = {(float)((img & 1023) - 512) * lx, (float)(((img >> 10) & 1023) - 512) * ly,
+                             (float)(((img >> 20) & 1023) - 512) * lz};
+        float d2 = 0.f;
+        for (int d = 0; d < 3; d++) {
+            const float lo = bbf[(size_t)J * 6 + d] + sh[d], hi = bbf[(size_t)J * 6 + 3 + d] + sh[d];
+            const float g = fmaxf(0.f, fmaxf(lo - bi[3 + d], bi[d] - hi));
+            d2 += g * g;
+        }
+        return d2 < rsub2;
+    };
+    int cnt = 0;
+    for (int b = 0; b < n; b += 32) cnt += __popc(__ballot_sync(0xffffffffu, keep(b + lane)));
+    unsigned long long off = 0;
+    if (lane == 0) off = atomicAdd(counter, (unsigned long long)cnt);
+    off = __shfl_sync(0xffffffffu, off, 0);
+    if (lane == 0) {
+        sub_start[I] = (int)off;
+        sub_cnt[I] = cnt;
+    }
+    long long run = (long long)off;
+    for (int b = 0; b < n; b += 32) {
+        const bool k = keep(b + lane);
+        const unsigned m = __ballot_sync(0xffffffffu, k);
+        if (k) {
+            const long long o = run + __popc(m & ((1u << lane) - 1u));
+            const int e = e0 + b + lane;
+            sub_j[o] = pair_j[e];
+            if (fp64)
+                ((double4 *)sub_shift)[o] = ((const double4 *)pair_shift)[e];
+            else
+                ((float4 *)sub_shift)[o] = ((const float4 *)pair_shift)[e];
+        }
+        run += __popc(m);
+    }
+}
+
 // small boxes: every (I, J) pair once, no image (minimum image per site pair later)
 __global__ void k_all_pairs(const int *__restrict__ meta, const double *__restrict__ ref, int *__restrict__ pair_start,
                             int *__restrict__ pair_cnt, int *__restrict__ pair_j, void *pair_shift,
@@ -723,6 +781,27 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         k_search<<<blocks, SEARCH_WPB * 32, 0, s>>>(A);
     }
     k_finish<<<1, 1, 0, s>>>(meta, (unsigned long long *)c->d_counter.p);
+    c->sub_ready = false;
+    if (p.respa_split > 0 && !c->small_box) {
+        // the inner sub-list of the distance split, rebuilt whenever the list is
+        const size_t ent = fp64 ? sizeof(double4) : sizeof(float4);
+        if (!mg_ensure(c, c->d_sub_start, sizeof(int) * ((size_t)c->cl_cap + 1)) ||
+            !mg_ensure(c, c->d_sub_count, sizeof(int) * ((size_t)c->cl_cap + 1)) ||
+            !mg_ensure(c, c->d_sub_j, sizeof(int) * (size_t)c->pair_cap) ||
+            !mg_ensure(c, c->d_sub_shift, ent * (size_t)c->pair_cap))
+            return MG_ERR_ALLOC;
+        const double rsub = p.respa_split + std::max(c->opt.skin, 0.0);
+        const float rsub2 = (float)(rsub * rsub) * 1.0001f + 1e-4f;
+        const unsigned blocks = (unsigned)(((long long)c->cl_cap * 32 + 127) / 128);
+        k_sublist<<<blocks, 128, 0, s>>>(meta, (int *)c->d_pair_start.p, (int *)c->d_pair_count.p,
+                                         (int *)c->d_pair_j.p, c->d_pair_shift.p, (int *)c->d_pair_img.p,
+                                         (float *)c->d_cl_bbf.p, (float)c->lx, (float)c->ly, (float)c->lz, rsub2,
+                                         fp64 ? 1 : 0, (int *)c->d_sub_start.p, (int *)c->d_sub_count.p,
+                                         (int *)c->d_sub_j.p, c->d_sub_shift.p,
+                                         (unsigned long long *)c->d_counter.p + 1);
+        c->launches += 1;
+        c->sub_ready = true;
+    }
     MG_CUDA(cudaGetLastError());
     c->launches += 10;
     c->list_valid = true;

@@ -293,6 +293,13 @@ mg_status mg_launch_pair(mg_ctx *c, int want_long, int want_short, double *fl, d
     A.pair_cnt = (int *)c->d_pair_count.p;
     A.pair_j = (int *)c->d_pair_j.p;
     A.pair_shift = c->d_pair_shift.p;
+    if (want_short && !want_long && c->sub_ready) {
+        // the inner pass of the distance split walks only the inner sub-list
+        A.pair_start = (int *)c->d_sub_start.p;
+        A.pair_cnt = (int *)c->d_sub_count.p;
+        A.pair_j = (int *)c->d_sub_j.p;
+        A.pair_shift = c->d_sub_shift.p;
+    }
     A.pos = c->d_pack_pos.p;
     A.lj = c->d_pack_lj.p;
     A.info = (int *)c->d_pack_info.p;

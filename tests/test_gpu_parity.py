@@ -194,3 +194,21 @@ def test_autotune_picks_a_valid_faster_geometry():
         from mspms2_gb300.engine import EngineError
         with pytest.raises(EngineError):
             eng.set_tuning(3.0, 1.0, 4)
+
+
+def test_inner_sublist_under_skin_reuse():
+    """The inner pass of the distance split walks a sub-list (cluster pairs within
+    respa_split + skin at the build). After sites move by less than skin/2 the reused
+    sub-list must still hold every inner pair: the short forces equal those of a fresh
+    build at the new positions."""
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    s.respa_split = 6.0
+    rng = np.random.default_rng(8)
+    x1, y1, z1 = (v + rng.uniform(-0.28, 0.28, size=v.shape) for v in (s.x, s.y, s.z))
+    with Engine(s, precision="fp64", skin=1.0) as a, Engine(s, precision="fp64") as b:
+        a.compute(terms=TERMS_SHORT)
+        _, fs_a, e_a = a.compute(x1, y1, z1, terms=TERMS_SHORT)
+        assert a.stats()["list_rebuilt"] == 0
+        _, fs_b, e_b = b.compute(x1, y1, z1, terms=TERMS_SHORT)
+    assert rel(fs_a, fs_b) <= 1e-12, rel(fs_a, fs_b)
+    assert abs(e_a["uinter"] - e_b["uinter"]) <= 1e-10 * abs(e_b["uinter"])
