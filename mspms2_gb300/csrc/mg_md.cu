@@ -19,6 +19,8 @@
 
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "mg_internal.cuh"
 #include "../../include/mg_philox.h"
 
@@ -247,6 +249,111 @@ __global__ void k_nh_finish(MdArgs A, int inner) {
     if (a == 0) nh_ps(A.s, inner) = A.s->psn;
 }
 
+// The whole implicit solve in one cooperative launch: the same arithmetic as the kernel
+// sequence above (k_nh_start ... k_nh_finish), with grid-wide barriers in place of kernel
+// boundaries and no host round trip per batch of iterations. Each block walks the same
+// 256-site chunks ("virtual blocks") the separate kernels use and every block sums the
+// partials in the same fixed order, so the result is identical for any grid size. Two
+// partial buffers alternate, so two barriers per iteration order every read before the
+// next write. The loop stops at the reference's 100 iterations like the host loop does.
+__device__ __forceinline__ void block_partial_at(double v, double *part, int idx) {
+    __shared__ double red2[MD_TPB];
+    red2[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = MD_TPB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red2[threadIdx.x] += red2[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[idx] = red2[0];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(MD_TPB) k_nh_solve_coop(MdArgs A, NhArgs N, int nb) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    double *pa = A.part, *pb = A.part + nb;
+    const int n = A.n;
+    for (int vb = blockIdx.x; vb < nb; vb += gridDim.x) {  // vn = v and sum m v^2
+        const int a = vb * MD_TPB + threadIdx.x;
+        double m2 = 0.0;
+        if (a < n) {
+            double s = 0.0;
+            for (int d = 0; d < 3; d++) {
+                const double v = A.v[d * n + a];
+                A.vn[d * n + a] = v;
+                s += v * v;
+            }
+            m2 = s / A.rmass[a];
+        }
+        block_partial_at(m2, pa, vb);
+    }
+    grid.sync();
+    double sumv2 = sum_partials(pa, nb);
+    __syncthreads();
+    const double ps = nh_ps(A.s, N.inner);  // the predicted momentum, fixed during the solve
+    double psn = ps, pso = ps, delps = 0.0, di = 0.0;
+    int iter = 0;
+    bool ready = false;
+    while (!ready) {
+        for (int vb = blockIdx.x; vb < nb; vb += gridDim.x) {  // residual (k_nh_residual)
+            const int a = vb * MD_TPB + threadIdx.x;
+            double t = 0.0;
+            if (a < n) {
+                const double r = A.rmass[a];
+                for (int d = 0; d < 3; d++) {
+                    const double vo = A.vn[d * n + a];
+                    A.vo[d * n + a] = vo;
+                    const double b = -N.h * (N.f[d * n + a] * r - psn * vo) - (A.v[d * n + a] - vo);
+                    A.b[d * n + a] = b;
+                    const double ri = vo * N.dt / N.q / r;
+                    t += ri * b;
+                }
+            }
+            block_partial_at(t, pb, vb);
+        }
+        grid.sync();
+        double dl = sum_partials(pb, nb);  // Newton step (k_nh_step_scalar)
+        __syncthreads();
+        pso = psn;
+        di = -(pso * N.h + 1.0);
+        dl = dl - di * ((-sumv2 + N.g_treq) * N.h / N.q - (ps - pso));
+        dl = dl / (-N.dt * N.h * sumv2 / N.q + di);
+        delps = dl;
+        for (int vb = blockIdx.x; vb < nb; vb += gridDim.x) {  // update (k_nh_update)
+            const int a = vb * MD_TPB + threadIdx.x;
+            double m2 = 0.0;
+            if (a < n) {
+                double s = 0.0;
+                for (int d = 0; d < 3; d++) {
+                    const double vn = A.vn[d * n + a] + (A.b[d * n + a] + N.h * A.vo[d * n + a] * delps) / di;
+                    A.vn[d * n + a] = vn;
+                    s += vn * vn;
+                }
+                m2 = s / A.rmass[a];
+            }
+            block_partial_at(m2, pa, vb);
+        }
+        grid.sync();
+        sumv2 = sum_partials(pa, nb);  // check (k_nh_check_scalar)
+        __syncthreads();
+        psn = pso + delps;
+        iter += 1;
+        const bool converged = !(fabs((psn - pso) / psn) > MD_ERR);
+        ready = converged || iter >= MD_MAX_ITER;
+    }
+    for (int i = blockIdx.x * MD_TPB + threadIdx.x; i < 3 * n; i += gridDim.x * MD_TPB) A.v[i] = A.vn[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        MdDev *s = A.s;
+        s->sumv2 = sumv2;
+        s->psn = psn;
+        s->pso = pso;
+        s->delps = delps;
+        s->di = di;
+        s->iter = iter;
+        s->ready = 1;
+        nh_ps(s, N.inner) = psn;
+    }
+}
+
 // end-of-step scalars: thermostat energies, kinetic energy and temperature
 __global__ void k_md_step_scalars(MdDev *s, int nb_unused, double qq, double qqs, double gg_treq,
                                   double ggs_treq, double nfree, int thermo, double *log_row) {
@@ -420,6 +527,7 @@ struct MdRun {
     MdArgs A;
     int nb;  // site blocks
     cudaStream_t s;
+    int coop_grid = 0;  // blocks of the cooperative solve (0: the device cannot run it)
 };
 
 mg_status nh_solve(MdRun &R, const double *f, double h, double dt, double q, double g_treq, int inner) {
@@ -431,6 +539,14 @@ mg_status nh_solve(MdRun &R, const double *f, double h, double dt, double q, dou
     N.q = q;
     N.g_treq = g_treq;
     N.inner = inner;
+    if (R.coop_grid > 0) {
+        int nb = R.nb;
+        void *args[] = {(void *)&R.A, (void *)&N, (void *)&nb};
+        MG_CUDA(cudaLaunchCooperativeKernel((const void *)k_nh_solve_coop, dim3(R.coop_grid), dim3(MD_TPB), args, 0,
+                                            R.s));
+        c->launches += 1;
+        return MG_OK;
+    }
     k_nh_start<<<R.nb, MD_TPB, 0, R.s>>>(R.A);
     k_nh_start_scalar<<<1, MD_TPB, 0, R.s>>>(R.A, R.nb, inner);
     c->launches += 2;
@@ -472,6 +588,15 @@ mg_status md_prepare(mg_ctx *c, size_t log_rows, MdRun &R) {
     R.c = c;
     R.nb = nb;
     R.s = c->stream;
+    {  // the cooperative solve needs every block of its grid resident at once
+        int coop = 0, sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nh_solve_coop, MD_TPB, 0) == cudaSuccess &&
+            per_sm > 0)
+            R.coop_grid = std::min(nb, per_sm * sms);
+        cudaGetLastError();
+    }
     MdArgs &A = R.A;
     double *w = (double *)c->d_md_work.p;
     A.n = n;
