@@ -386,6 +386,18 @@ MG_API mg_status mg_checkpoint_load(const char *path, mg_checkpoint *ck, int wit
  * mg_set_params gave them, as loadit() leaves its globals. */
 MG_API mg_status mg_checkpoint_apply(mg_ctx *ctx, const mg_checkpoint *ck);
 
+/* No reference counterpart: mg_md_run (and the stages of mg_siman_run) replay whole
+ * integration steps as one captured CUDA graph when they can: after an eager first force
+ * evaluation, one step is captured and replayed nsteps times, with the energies of every
+ * force call logged on the device and read after the run. Results are identical to the
+ * step-by-step path. The steps run step by step instead when a trajectory is attached,
+ * when the thermostat solve cannot run as a cooperative launch, or when a replayed step
+ * raised a flag that needs the host (list capacity, small box, non-finite force, a site
+ * off its table); then the start state is restored and the run repeated step by step.
+ * Enabled by default; mg_get_md_graphs reports how many steps the last run replayed. */
+MG_API mg_status mg_set_md_graphs(mg_ctx *ctx, int enable);
+MG_API mg_status mg_get_md_graphs(const mg_ctx *ctx, int *enabled, int *last_steps);
+
 /* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
 /* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
  * first stage whose T is below t_min (the reference tests T < t_min after the stage). A

@@ -129,7 +129,8 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_meta, &c->d_pair_img, &c->d_cl_bbf, &c->d_col_ncl, &c->d_counter,
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
                       &c->d_adj_class, &c->d_adj, &c->d_adj_g,
-                      &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift};
+                      &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift,
+                      &c->d_md_glog};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
     for (auto &b : c->myinterp_buf) mg_free(b);
@@ -562,9 +563,15 @@ static void assemble_energies(mg_ctx *c, const double *E, int want_long, int wan
 }
 
 // One attempt; *retry is set when the list set-up must change and the call be repeated.
-static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
-                              double *fl, double *fs, mg_energies *e, bool *retry) {
-    *retry = false;
+void mg_assemble_energies(mg_ctx *c, const double *E, int want_long, int want_short, mg_energies *e) {
+    assemble_energies(c, E, want_long, want_short, e);
+}
+
+// Every launch of one evaluation, in order, on the context's stream, with no host
+// synchronisation (so that it can also be captured into a graph): the raw energy
+// components end in d_eout, the error flags in d_flags, the list counts in d_meta.
+mg_status mg_enqueue_forces(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms, double *fl,
+                            double *fs) {
     if (!c->have_topology || !c->have_params || !c->have_box)
         return mg_fail(c, MG_ERR_STATE, "set topology, params and box before computing");
     const mg_params &p = c->params;
@@ -623,6 +630,20 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
     if (want_long && (st = mg_launch_check(c, fl, c->natom))) return st;
     if (want_short && (st = mg_launch_check(c, fs, c->natom))) return st;
     if (c->timing) cudaEventRecord(c->ev[7], s);
+    return MG_OK;
+}
+
+static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
+                              double *fl, double *fs, mg_energies *e, bool *retry) {
+    *retry = false;
+    mg_status st = mg_enqueue_forces(c, dx, dy, dz, terms, fl, fs);
+    if (st) return st;
+    const mg_params &p = c->params;
+    cudaStream_t s = c->stream;
+    int want_long = (terms & MG_TERMS_LONG) != 0;
+    int want_short = (terms & MG_TERMS_SHORT) != 0;
+    bool split = p.respa_split > 0;
+    bool need_pairs = want_long || (split && want_short);
     double E[E_NCOMP + 8];
     unsigned flags[4];
     int meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -867,5 +888,18 @@ extern "C" mg_status mg_autotune(mg_ctx *c, const double *x, const double *y, co
         out->ms_tuned = best_ms;
         out->configs_tried = tried;
     }
+    return MG_OK;
+}
+
+extern "C" mg_status mg_set_md_graphs(mg_ctx *c, int enable) {
+    if (!c) return MG_ERR_INVALID;
+    c->md_graphs = enable != 0;
+    return MG_OK;
+}
+
+extern "C" mg_status mg_get_md_graphs(const mg_ctx *c, int *enabled, int *last_steps) {
+    if (!c) return MG_ERR_INVALID;
+    if (enabled) *enabled = c->md_graphs ? 1 : 0;
+    if (last_steps) *last_steps = c->md_graph_steps;
     return MG_OK;
 }

@@ -171,6 +171,9 @@ struct mg_ctx {
     // integration (mg_md_run): velocities, solver work arrays, 1/mass, partial sums,
     // thermostat scalars, per-step records
     DevBuf d_md_v, d_md_work, d_md_rmass, d_md_part, d_md_dev, d_md_log;
+    DevBuf d_md_glog;          // graph replay: energy log, saved start state, step counter
+    bool md_graphs = true;     // run whole integrator steps as a replayed CUDA graph
+    int md_graph_steps = 0;    // steps the last run replayed as a graph (0: eager)
     // adjoint (mg_adjoint_params): site classes and one carved scratch block
     DevBuf d_adj_class, d_adj, d_adj_g;
     MgTraj *traj = nullptr;  // attached trajectory file, if any
@@ -208,6 +211,11 @@ bool mg_ensure(mg_ctx *c, DevBuf &b, size_t bytes);
 // repeating the call when the neighbour-list set-up has to grow (mg_host.cu)
 mg_status mg_compute_forces(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,
                             double *fl, double *fs, mg_energies *e);
+// the launches of one evaluation only (no readback, no retry; mg_host.cu)
+mg_status mg_enqueue_forces(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms, double *fl,
+                            double *fs);
+// the energies of a raw component vector E[E_NCOMP] as mg_compute reports them
+void mg_assemble_energies(mg_ctx *c, const double *E, int want_long, int want_short, mg_energies *e);
 void mg_free(DevBuf &b);
 
 #define MG_CUDA(call)                                                \

@@ -376,6 +376,42 @@ __global__ void k_md_step_scalars(MdDev *s, int nb_unused, double qq, double qqs
     }
 }
 
+// ---- graph replay of whole steps ---------------------------------------------------
+// The step's record row chosen by a device step counter (so that one captured step can
+// be replayed), then the counter moves on; otherwise k_md_step_scalars.
+__global__ void k_set_one(int *p) { *p = 1; }
+
+__global__ void k_graph_row(MdDev *s, double qq, double qqs, double gg_treq, double ggs_treq, double nfree,
+                            int thermo, double *dlog, int *counter) {
+    if (thermo) {
+        s->unhtss = (s->pss * s->pss * qqs) / 2.0 + ggs_treq * s->sss;
+        s->ukin = s->sumv2 / 2.0;
+        s->unhts = (s->ps * s->ps * qq) / 2.0 + gg_treq * s->ss;
+    }
+    s->tinst = 2.0 * s->ukin / nfree;
+    double *row = dlog + (size_t)(*counter) * MG_MD_LOG;
+    row[0] = s->ukin;
+    row[4] = s->ps;
+    row[5] = s->ss;
+    row[6] = s->pss;
+    row[7] = s->sss;
+    row[8] = s->tinst;
+    row[9] = s->unhts;
+    row[10] = s->unhtss;
+    *counter += 1;
+}
+
+// the raw energy components of one force call into the device log (slot `slot` of the
+// current step) and its error flags into a word that keeps them for the whole run
+__global__ void k_graph_energy(const double *__restrict__ eout, const unsigned *__restrict__ flags,
+                               double *__restrict__ elog, const int *__restrict__ counter, int calls, int slot,
+                               unsigned *__restrict__ sticky) {
+    const int t = threadIdx.x;
+    const size_t row = ((size_t)(*counter) * calls + slot) * E_NCOMP;
+    if (t < E_NCOMP) elog[row + t] = eout[t];
+    if (t == 0) *sticky |= flags[0];
+}
+
 // sum m v^2 / 2 of the current velocities into ukin (plain velocity Verlet, src/md.c:66-79)
 __global__ void k_md_ukin_scalar(MdArgs A, int nb) {
     const double sumv2 = sum_partials(A.part, nb);
@@ -620,6 +656,125 @@ mg_status md_prepare(mg_ctx *c, size_t log_rows, MdRun &R) {
 // nsteps of the scheme from the device state of R: forces at the start (as the reference
 // evaluates them before its loop), the step-0 record and one record per step (device
 // rows dlog; uinter, uintra and ushift of every row in hlog)
+#define MD_GRAPH_FALLBACK 1000  // the graph path did not run the steps: run them eagerly
+
+// Steps 1..nsteps by replaying one captured step. The device state at the start
+// (positions, velocities, thermostat scalars) is saved first; if the capture cannot be
+// made or a step of the replay raised a flag the eager loop handles (list or column
+// capacity, small box, non-finite force, a site off its table), the start state is
+// restored and MD_GRAPH_FALLBACK returned.
+mg_status md_graph_steps(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, double *hlog) {
+    mg_ctx *c = R.c;
+    MdArgs &A = R.A;
+    const int nb = R.nb, n = A.n;
+    cudaStream_t s = R.s;
+    double *dx = A.x, *dy = A.y, *dz = A.z;
+    double *fl = (double *)c->d_fl.p, *fs = (double *)c->d_fs.p;
+    const bool nh = mp->scheme == MG_MD_NVT_NH;
+    const double dt = mp->delt, h = dt / 2.0, dts = dt / mp->nstep_inner, hs = dts / 2.0;
+    const double dt_sqby2 = dt * dt / 2.0, dts_sqby2 = dts * dts / 2.0;
+    const double gg_treq = mp->gg * mp->treq, ggs_treq = mp->ggs * mp->treq;
+    const int calls = mp->nstep_inner + 1;
+    const size_t elog_n = ((size_t)nsteps + 1) * calls * E_NCOMP;
+    const size_t save_n = 6 * (size_t)n + (sizeof(MdDev) + 7) / 8;
+    if (!mg_ensure(c, c->d_md_glog, sizeof(double) * (elog_n + save_n) + 64)) return MG_ERR_ALLOC;
+    double *elog = (double *)c->d_md_glog.p, *save = elog + elog_n;
+    int *counter = (int *)(save + save_n);
+    unsigned *sticky = (unsigned *)(counter + 1);
+    MG_CUDA(cudaMemcpyAsync(save, dx, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(save + 3 * (size_t)n, A.v, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+    MG_CUDA(cudaMemcpyAsync(save + 6 * (size_t)n, A.s, sizeof(MdDev), cudaMemcpyDeviceToDevice, s));
+    MG_CUDA(cudaMemsetAsync(counter, 0, 64, s));
+    k_set_one<<<1, 1, 0, s>>>(counter);
+    auto restore = [&]() -> mg_status {
+        MG_CUDA(cudaMemcpyAsync(dx, save, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(A.v, save + 3 * (size_t)n, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+        MG_CUDA(cudaMemcpyAsync(A.s, save + 6 * (size_t)n, sizeof(MdDev), cudaMemcpyDeviceToDevice, s));
+        MG_CUDA(cudaStreamSynchronize(s));
+        c->list_valid = false;
+        return MD_GRAPH_FALLBACK;
+    };
+    // capture one step (the launches of the eager loop, in its order)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    mg_status st = MG_OK;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return restore();
+    }
+    k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fl, h, nh ? 1 : 0, 0);
+    for (int ll = 0; ll < mp->nstep_inner && !st; ll++) {
+        k_md_inner_drift<<<nb, MD_TPB, 0, s>>>(A, hs, dts, nh ? 1 : 0);
+        if (nh) k_md_inner_predict<<<1, MD_TPB, 0, s>>>(A, nb, ggs_treq, dts, dts_sqby2, hs, mp->qqs);
+        if ((st = mg_enqueue_forces(c, dx, dy, dz, MG_TERMS_SHORT, fl, fs))) break;
+        k_graph_energy<<<1, 32 * ((E_NCOMP + 31) / 32), 0, s>>>((const double *)c->d_eout.p,
+                                                                (const unsigned *)c->d_flags.p, elog, counter, calls,
+                                                                ll, sticky);
+        if (nh) {
+            if ((st = nh_solve(R, fs, hs, dts, mp->qqs, ggs_treq, 1))) break;
+        } else {
+            k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fs, hs, 0, 0);
+        }
+    }
+    if (!st) {
+        if (nh) k_md_outer_predict<<<1, 1, 0, s>>>(A.s, gg_treq, dt, dt_sqby2, h, mp->qq);
+        st = mg_enqueue_forces(c, dx, dy, dz, MG_TERMS_LONG, fl, fs);
+    }
+    if (!st) {
+        k_graph_energy<<<1, 32 * ((E_NCOMP + 31) / 32), 0, s>>>((const double *)c->d_eout.p,
+                                                                (const unsigned *)c->d_flags.p, elog, counter, calls,
+                                                                mp->nstep_inner, sticky);
+        if (nh) {
+            st = nh_solve(R, fl, h, dt, mp->qq, gg_treq, 0);
+            if (!st)
+                k_graph_row<<<1, 1, 0, s>>>(A.s, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 1, dlog,
+                                            counter);
+        } else {
+            k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fl, h, 0, 1);
+            k_md_ukin_scalar<<<1, MD_TPB, 0, s>>>(A, nb);
+            k_graph_row<<<1, 1, 0, s>>>(A.s, mp->qq, mp->qqs, gg_treq, ggs_treq, (double)mp->nfree, 0, dlog,
+                                        counter);
+        }
+    }
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    cudaGetLastError();
+    if (st || ce != cudaSuccess || !graph ||
+        cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        return restore();
+    }
+    bool launched = true;
+    for (int step = 1; step <= nsteps && launched; step++) launched = cudaGraphLaunch(exec, s) == cudaSuccess;
+    unsigned flags = 0;
+    std::vector<double> E((size_t)(nsteps + 1) * calls * E_NCOMP);
+    if (launched) {
+        MG_CUDA(cudaMemcpyAsync(&flags, sticky, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        MG_CUDA(cudaMemcpyAsync(E.data(), elog, sizeof(double) * E.size(), cudaMemcpyDeviceToHost, s));
+        launched = cudaStreamSynchronize(s) == cudaSuccess;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    c->launches += 1;
+    const unsigned bad = MG_FLAG_OUT_OF_GRID | MG_FLAG_NONFINITE | MG_FLAG_LIST_OVERFLOW | MG_FLAG_COLUMN_OVERFLOW |
+                         MG_FLAG_SMALL_BOX | MG_FLAG_IMPROPER_DEGENERATE;
+    if (!launched || (flags & bad)) {
+        cudaGetLastError();
+        return restore();
+    }
+    // the energies of every step, as the eager loop records them
+    for (int step = 1; step <= nsteps; step++) {
+        mg_energies el, es;
+        mg_assemble_energies(c, &E[((size_t)step * calls + mp->nstep_inner) * E_NCOMP], 1, 0, &el);
+        mg_assemble_energies(c, &E[((size_t)step * calls + mp->nstep_inner - 1) * E_NCOMP], 0, 1, &es);
+        hlog[(size_t)step * MG_MD_LOG + 1] = el.uinter + es.uinter;
+        hlog[(size_t)step * MG_MD_LOG + 2] = es.uintra;
+        hlog[(size_t)step * MG_MD_LOG + 3] = el.ushift + es.ushift;
+    }
+    c->md_graph_steps = nsteps;
+    return MG_OK;
+}
+
 mg_status md_loop(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, double *hlog, bool traj_steps) {
     mg_ctx *c = R.c;
     MdArgs &A = R.A;
@@ -645,6 +800,15 @@ mg_status md_loop(MdRun &R, const mg_md_params *mp, int nsteps, double *dlog, do
     hlog[1] = uinter_l;
     hlog[2] = uintra;
     hlog[3] = ushift_l;
+    c->md_graph_steps = 0;
+    // whole steps as a replayed graph where possible: no trajectory frames to hand to the
+    // host between steps, and the thermostat solve as one cooperative launch
+    if (c->md_graphs && nsteps >= 2 && !(traj_steps && c->traj) && (!nh || R.coop_grid > 0)) {
+        st = md_graph_steps(R, mp, nsteps, dlog, hlog);
+        if (st != MD_GRAPH_FALLBACK) return st;
+        // the start state is back: forces at the start again, then the eager loop
+        if ((st = mg_compute_forces(c, dx, dy, dz, MG_TERMS_ALL, fl, fs, &e))) return st;
+    }
     for (int step = 1; step <= nsteps; step++) {
         k_md_kick<<<nb, MD_TPB, 0, s>>>(A, fl, h, nh ? 1 : 0, 0);
         for (int ll = 0; ll < mp->nstep_inner; ll++) {

@@ -547,6 +547,8 @@ __global__ void k_sublist(const int *__restrict__ meta, const int *__restrict__ 
     }
 }
 
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
 // small boxes: every (I, J) pair once, no image (minimum image per site pair later)
 __global__ void k_all_pairs(const int *__restrict__ meta, const double *__restrict__ ref, int *__restrict__ pair_start,
                             int *__restrict__ pair_cnt, int *__restrict__ pair_j, void *pair_shift,
@@ -696,8 +698,8 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         if (st) return st;
     }
     if (geometry || !(c->opt.skin > 0)) {
-        int one = 1;
-        MG_CUDA(cudaMemcpyAsync(meta + META_NEED, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+        k_set_int<<<1, 1, 0, s>>>(meta + META_NEED, 1);
+        c->launches += 1;
     } else {
         MG_CUDA(cudaMemsetAsync(meta + META_NEED, 0, sizeof(int), s));
         double hs = 0.5 * c->opt.skin;

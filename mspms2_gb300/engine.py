@@ -79,6 +79,8 @@ def load_library(path: str = LIB_PATH):
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.mg_sf_tasos_generate.argtypes = [V, I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, D]
+    lib.mg_set_md_graphs.argtypes = [V, I]
+    lib.mg_get_md_graphs.argtypes = [V, C.POINTER(I), C.POINTER(I)]
     lib.mg_autotune.argtypes = [V, _dp, _dp, _dp, I, C.POINTER(capi.MgTuning)]
     lib.mg_set_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
     lib.mg_get_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
@@ -290,6 +292,16 @@ class Engine:
         c, _keep = _sfgrid_spec(spec)
         self._check(self.lib.mg_sf_tasos_generate(self.ctx, type_id, C.byref(c), nx, ny, nz, float(h[0]), float(h[1]),
                                                   float(h[2]), float(cuc)))
+
+    def set_md_graphs(self, enable: bool) -> None:
+        """Whole integrator steps as a replayed CUDA graph (default) or step by step."""
+        self._check(self.lib.mg_set_md_graphs(self.ctx, 1 if enable else 0))
+
+    def md_graph_steps(self) -> int:
+        """Steps the last integrator run replayed as a graph (0: it ran step by step)."""
+        en, last = C.c_int(), C.c_int()
+        self._check(self.lib.mg_get_md_graphs(self.ctx, C.byref(en), C.byref(last)))
+        return last.value
 
     def autotune(self, x=None, y=None, z=None, terms: int = TERMS_ALL) -> dict:
         """Picks the launch geometry (cell size, cluster size, threads per site of the

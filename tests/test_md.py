@@ -81,3 +81,24 @@ def test_engine_integrator_continues_like_one_run():
         pa, va, sta, _ = eng.md_run(8, md, v0, state=state)
     assert np.array_equal(p2, pa) and np.array_equal(v2, va)
     assert st2["ps"] == sta["ps"] and st2["pss"] == sta["pss"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("case", md_golden_cases())
+def test_graph_replay_matches_step_by_step(case, prec):
+    """Steps replayed as one captured CUDA graph give exactly the results of the same
+    steps launched one by one, and the replay path is the one that ran."""
+    from mspms2_gb300 import build
+    from mspms2_gb300.engine import Engine
+    build.build()
+    s, md, state, v0, ref_log, ref_end, nsteps = load_md_case(case)
+    out = {}
+    for graphs in (True, False):
+        with Engine(s, precision=prec) as eng:
+            eng.set_md_graphs(graphs)
+            out[graphs] = eng.md_run(nsteps, md, v0, state=state)
+            assert eng.md_graph_steps() == (nsteps if graphs else 0), (case, prec, graphs)
+    (p1, v1, s1, l1), (p2, v2, s2, l2) = out[True], out[False]
+    assert np.array_equal(p1, p2) and np.array_equal(v1, v2) and np.array_equal(l1, l2)
+    assert s1 == s2
