@@ -347,6 +347,33 @@ typedef struct mg_npt_state {
 MG_API mg_status mg_npt_run(mg_ctx *ctx, const mg_npt_params *p, int nsteps, double *x, double *y, double *z,
                             double *vx, double *vy, double *vz, double *box, mg_npt_state *state, double *log);
 
+/* ---- batched simulated annealing of Lennard-Jones replicas -------------------- */
+/* Many independent one-site LJ boxes of uneven size (reduced units, cubic boxes of at
+ * least 2 rcutoff, no switch) through the reference's siman() schedule
+ * (src/siman.c:62-182), all in one persistent launch: a thread block takes whole
+ * replicas, largest first. Each stage of the schedule (as mg_siman_run: T = t_initial /
+ * mu_t^k up to the first T below t_min) is velinit at T with the exact rescaling,
+ * n_tries vver_nh_3 steps with one inner step (src/nvtnh.c:11-271; a one-site fluid has
+ * no short forces) and the thermostat reset, gg = ggs = nfree = 3 natom - nconstraint.
+ * Replica r draws its velocities from mg_siman_run's Philox streams with the seed
+ * seed ^ (r * 0x9E3779B97F4A7C15), so mg_siman_run on that replica alone with that seed
+ * gives the same run up to the FP32 pair forces used here. Positions in and out; log:
+ * per replica and stage, MG_SIMAN_BATCH_LOG values at the stage end: T, ukin, uinter
+ * (LJ), ushift (the shift energy of the pairs inside the cutoff), tinst. */
+typedef struct mg_siman_batch_params {
+    double eps, sigma, rcutoff, mass;
+    double delt;                      /* outer step (one inner step) */
+    double qq, qqs;                   /* Nose-Hoover masses */
+    double t_initial, t_min, mu_t;
+    int n_tries, max_stages;
+    uint64_t seed;
+    int nconstraint;
+} mg_siman_batch_params;
+#define MG_SIMAN_BATCH_LOG 5
+MG_API mg_status mg_siman_batch(int device, const mg_siman_batch_params *p, int nrep, const int *natom,
+                                const double *box, double *x, double *y, double *z, int *nstages,
+                                double *stage_log);
+
 /* ---- trajectory file (trajectory(), src/dumpxyz.c:37-66) ------------------------ */
 /* Attaches a trajectory file in the reference's binary layout (trj.mspms) to the
  * context: the header is written now; mg_md_run and mg_npt_run then append the frame

@@ -147,6 +147,17 @@ class MgHmcParams(C.Structure):
                 ("rescale", C.c_int), ("nconstraint", C.c_int)]
 
 
+class MgSimanBatchParams(C.Structure):
+    _fields_ = [("eps", C.c_double), ("sigma", C.c_double), ("rcutoff", C.c_double), ("mass", C.c_double),
+                ("delt", C.c_double), ("qq", C.c_double), ("qqs", C.c_double), ("t_initial", C.c_double),
+                ("t_min", C.c_double), ("mu_t", C.c_double), ("n_tries", C.c_int), ("max_stages", C.c_int),
+                ("seed", C.c_ulonglong), ("nconstraint", C.c_int)]
+
+
+SIMAN_BATCH_LOG_NAMES = ["T", "ukin", "uinter", "ushift", "tinst"]
+SIMAN_BATCH_LOG = 5
+
+
 MD_STATE_NAMES = ["ps", "ss", "pss", "sss", "ukin", "tinst", "unhts", "unhtss"]
 MD_LOG_NAMES = ["ukin", "uinter", "uintra", "ushift", "ps", "ss", "pss", "sss", "tinst", "unhts", "unhtss"]
 MD_LOG = 12

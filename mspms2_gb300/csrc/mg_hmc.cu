@@ -351,7 +351,371 @@ __global__ void __launch_bounds__(HMC_TPB, 1) k_hmc(HmcArgs A) {
     }
 }
 
+// ---- batched simulated annealing (siman, src/siman.c:62-182) --------------------------
+struct SimanArgs {
+    int nrep, total;
+    const int *order, *natom, *offset;
+    const double *box;
+    double *x, *y, *z, *vx, *vy, *vz;   // [total]
+    double *f, *vn, *vo, *b;            // [3][total] each: forces, solver work arrays
+    int *counter;
+    int nst, n_tries, nconstraint;
+    double eps, sig2, rc, rc2, shift_pair, mass, dt, qq, qqs, t_initial, mu_t;
+    uint64_t seed;
+    double *log;                        // [nrep][nst][MG_SIMAN_BATCH_LOG]
+    int nmax, ncmax;
+};
+
+// FP32 LJ forces (shared-memory positions) into f, with the pair energy and pair count
+__device__ __forceinline__ void siman_forces(const SimanArgs &A, const HmcArgs &H, const Smem &S, int off, int n,
+                                             double L, int nc, double &u, double &np) {
+    const int total = A.total;
+    double esum = 0.0, nsum = 0.0, unused = 0.0;
+    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+        float fx, fy, fz, e;
+        int cnt;
+        atom_force(H, S, i, n, L, nc, fx, fy, fz, e, cnt);
+        A.f[off + i] = (double)fx;
+        A.f[total + off + i] = (double)fy;
+        A.f[2 * (size_t)total + off + i] = (double)fz;
+        esum += (double)e;
+        nsum += (double)cnt;
+    }
+    block_sum3(esum, nsum, unused);
+    u = 0.5 * esum;
+    np = 0.5 * nsum;
+}
+
+// The implicit Nose-Hoover solve of src/nvtnh.c:67-156 (inner) and :165-252 (outer) for
+// the block's replica, in the same arithmetic as the engine's solver kernels: Newton
+// iterations on the thermostat momentum with fixed-order block sums, at most 100, the
+// reference's test on the momentum alone. f == nullptr: zero forces (the short forces of
+// a one-site fluid). Returns the new momentum; sumv2 = sum m v^2 of the new velocities.
+__device__ double siman_nh_solve(const SimanArgs &A, int off, int n, const double *f, double h, double dt, double q,
+                                 double g_treq, double ps_pred, double &sumv2) {
+    const size_t total = (size_t)A.total;
+    const double r = 1.0 / A.mass;
+    double t0 = 0.0, d0 = 0.0, d1 = 0.0;
+    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+        const double v[3] = {A.vx[off + i], A.vy[off + i], A.vz[off + i]};
+        double s2 = 0.0;
+        for (int d = 0; d < 3; d++) {
+            A.vn[d * total + off + i] = v[d];
+            s2 += v[d] * v[d];
+        }
+        t0 += s2 / r;
+    }
+    block_sum3(t0, d0, d1);
+    sumv2 = t0;
+    double psn = ps_pred;
+    for (int iter = 1; iter <= 100; iter++) {
+        double ds = 0.0, e0 = 0.0, e1 = 0.0;
+        for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+            const double v[3] = {A.vx[off + i], A.vy[off + i], A.vz[off + i]};
+            for (int d = 0; d < 3; d++) {
+                const size_t k = d * total + off + i;
+                const double vo = A.vn[k];
+                A.vo[k] = vo;
+                const double fd = f ? f[k] : 0.0;
+                const double b = -h * (fd * r - psn * vo) - (v[d] - vo);
+                A.b[k] = b;
+                const double ri = vo * dt / q / r;
+                ds += ri * b;
+            }
+        }
+        block_sum3(ds, e0, e1);
+        const double pso = psn, di = -(pso * h + 1.0);
+        double delps = ds - di * ((-sumv2 + g_treq) * h / q - (ps_pred - pso));
+        delps = delps / (-dt * h * sumv2 / q + di);
+        double s2 = 0.0;
+        e0 = e1 = 0.0;
+        for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+            double m2 = 0.0;
+            for (int d = 0; d < 3; d++) {
+                const size_t k = d * total + off + i;
+                const double vn = A.vn[k] + (A.b[k] + h * A.vo[k] * delps) / di;
+                A.vn[k] = vn;
+                m2 += vn * vn;
+            }
+            s2 += m2 / r;
+        }
+        block_sum3(s2, e0, e1);
+        sumv2 = s2;
+        psn = pso + delps;
+        if (!(fabs((psn - pso) / psn) > 1.0e-10)) break;
+    }
+    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+        A.vx[off + i] = A.vn[off + i];
+        A.vy[off + i] = A.vn[total + off + i];
+        A.vz[off + i] = A.vn[2 * total + off + i];
+    }
+    __syncthreads();
+    return psn;
+}
+
+// One block runs whole replicas (largest first, from a work counter): every stage of the
+// schedule is velinit at T, forces, n_tries vver_nh_3 steps with one inner step (a
+// one-site fluid has no short forces) and the thermostat reset.
+__global__ void __launch_bounds__(HMC_TPB, 1) k_siman_batch(SimanArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem S;
+    S.pos = (float4 *)smem_raw;
+    S.list = (int *)(S.pos + A.nmax);
+    S.start = S.list + A.nmax;
+    S.cnt = S.start + A.ncmax + 1;
+    __shared__ int s_rep;
+    HmcArgs H;  // what the shared-memory position and force helpers read
+    H.x = A.x;
+    H.y = A.y;
+    H.z = A.z;
+    H.sig2 = A.sig2;
+    H.eps = A.eps;
+    H.rc2 = A.rc2;
+    const size_t total = (size_t)A.total;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_rep = atomicAdd(A.counter, 1);
+        __syncthreads();
+        const int kr = s_rep;
+        if (kr >= A.nrep) break;
+        const int rep = A.order[kr], n = A.natom[rep], off = A.offset[rep];
+        const double L = A.box[rep];
+        int nc = (int)floor(L / A.rc);
+        if (nc < 3) nc = 0;
+        const uint64_t seed = A.seed ^ ((uint64_t)rep * 0x9E3779B97F4A7C15ull);
+        const uint32_t key[2] = {(uint32_t)(seed & 0xffffffffull), (uint32_t)(seed >> 32)};
+        const double nfree = 3.0 * n - A.nconstraint, mass = A.mass, r = 1.0 / mass;
+        const double dt = A.dt, h = dt / 2.0, dts = dt, hs = dts / 2.0, dt_sqby2 = dt * dt / 2.0;
+        const double dts_sqby2 = dts * dts / 2.0;
+        double T = A.t_initial;
+        for (int k = 0; k < A.nst; k++) {
+            double ps = 0.0, ss = 0.0, pss = 0.0, sss = 0.0;  // stage 0 from zero, later ones reset
+            // velinit at T (src/initvars.c:151-229) on the Philox streams of mg_siman_run
+            const double stdv = sqrt(T) / sqrt(mass);
+            double px = 0.0, py = 0.0, pz = 0.0;
+            for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                const uint32_t c0[4] = {(uint32_t)i, (uint32_t)k, 0u, 0x5349u};
+                const uint32_t c1[4] = {(uint32_t)i, (uint32_t)k, 1u, 0x5349u};
+                uint32_t w0[4], w1[4];
+                double g0, g1, g2, g3;
+                mg_philox4x32_10(c0, key, w0);
+                mg_philox4x32_10(c1, key, w1);
+                mg_gauss2(w0, &g0, &g1);
+                mg_gauss2(w1, &g2, &g3);
+                const double v0 = stdv * g0, v1 = stdv * g1, v2 = stdv * g2;
+                A.vx[off + i] = v0;
+                A.vy[off + i] = v1;
+                A.vz[off + i] = v2;
+                px += v0 * mass;
+                py += v1 * mass;
+                pz += v2 * mass;
+            }
+            block_sum3(px, py, pz);
+            const double sysm = mass * n;
+            px /= sysm;
+            py /= sysm;
+            pz /= sysm;
+            double ukin = 0.0, d0 = 0.0, d1 = 0.0;
+            for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                const double v0 = A.vx[off + i] - px, v1 = A.vy[off + i] - py, v2 = A.vz[off + i] - pz;
+                A.vx[off + i] = v0;
+                A.vy[off + i] = v1;
+                A.vz[off + i] = v2;
+                ukin += mass * (v0 * v0 + v1 * v1 + v2 * v2);
+            }
+            block_sum3(ukin, d0, d1);
+            ukin = 0.5 * ukin;
+            const double scaling = sqrt(T / (2.0 * ukin / nfree));
+            for (int i = threadIdx.x; i < n; i += HMC_TPB) {
+                A.vx[off + i] *= scaling;
+                A.vy[off + i] *= scaling;
+                A.vz[off + i] *= scaling;
+            }
+            __syncthreads();
+            const double g_treq = nfree * T;  // gg = ggs = nfree (src/siman.c:167-174)
+            double u = 0.0, np = 0.0, sumv2 = 0.0;
+            load_positions(H, S, off, n, L, nc);
+            siman_forces(A, H, S, off, n, L, nc, u, np);
+            for (int st = 1; st <= A.n_tries; st++) {  // vver_nh_3 (src/nvtnh.c:11-271)
+                double sv = 0.0;
+                for (int i = threadIdx.x; i < n; i += HMC_TPB) {  // outer half kick
+                    for (int d = 0; d < 3; d++) {
+                        double *vd = d == 0 ? A.vx : (d == 1 ? A.vy : A.vz);
+                        const double v = vd[off + i];
+                        vd[off + i] = v + h * (A.f[d * total + off + i] * r - ps * v);
+                    }
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < n; i += HMC_TPB) {  // inner step: no short forces
+                    double s2 = 0.0;
+                    double *pos[3] = {A.x, A.y, A.z};
+                    for (int d = 0; d < 3; d++) {
+                        double *vd = d == 0 ? A.vx : (d == 1 ? A.vy : A.vz);
+                        double v = vd[off + i];
+                        s2 += v * v;
+                        v = v + hs * (0.0 * r - pss * v);
+                        vd[off + i] = v;
+                        pos[d][off + i] = pos[d][off + i] + dts * v;
+                    }
+                    sv += s2 / r;
+                }
+                d0 = d1 = 0.0;
+                block_sum3(sv, d0, d1);
+                sss = sss + pss * dts + (sv - g_treq) * dts_sqby2 / A.qqs;
+                pss = pss + (sv - g_treq) * hs / A.qqs;
+                pss = siman_nh_solve(A, off, n, nullptr, hs, dts, A.qqs, g_treq, pss, sumv2);
+                ss = ss + ps * dt + (sumv2 - g_treq) * dt_sqby2 / A.qq;
+                ps = ps + (sumv2 - g_treq) * h / A.qq;
+                load_positions(H, S, off, n, L, nc);
+                siman_forces(A, H, S, off, n, L, nc, u, np);
+                ps = siman_nh_solve(A, off, n, A.f, h, dt, A.qq, g_treq, ps, sumv2);
+            }
+            if (threadIdx.x == 0) {
+                double *o = A.log + ((size_t)rep * A.nst + k) * MG_SIMAN_BATCH_LOG;
+                o[0] = T;
+                o[1] = sumv2 / 2.0;  // ukin at the stage end
+                o[2] = u;            // uinter (LJ)
+                o[3] = A.shift_pair * np;
+                o[4] = sumv2 / nfree;
+            }
+            T /= A.mu_t;
+        }
+    }
+}
+
 }  // namespace
+
+extern "C" mg_status mg_siman_batch(int device, const mg_siman_batch_params *p, int nrep, const int *natom,
+                                    const double *box, double *x, double *y, double *z, int *nstages,
+                                    double *stage_log) {
+    if (!p || nrep <= 0 || !natom || !box || !x || !y || !z || !nstages || !stage_log) return MG_ERR_INVALID;
+    if (!(p->eps >= 0) || !(p->sigma > 0) || !(p->rcutoff > 0) || !(p->mass > 0) || !(p->delt > 0) ||
+        !(p->qq > 0) || !(p->qqs > 0) || p->n_tries < 0 || p->nconstraint < 0)
+        return MG_ERR_INVALID;
+    const int nst = mg_siman_stage_count(p->t_initial, p->t_min, p->mu_t, p->max_stages);
+    if (nst < 0) return MG_ERR_CAPACITY;
+    int nmax = 0, ncmax = 0;
+    long long total = 0;
+    for (int r = 0; r < nrep; r++) {
+        if (natom[r] < 2 || !(box[r] >= 2.0 * p->rcutoff) || 3 * natom[r] <= p->nconstraint) return MG_ERR_INVALID;
+        nmax = std::max(nmax, natom[r]);
+        int nc = (int)floor(box[r] / p->rcutoff);
+        if (nc >= 3) ncmax = std::max(ncmax, nc * nc * nc);
+        total += natom[r];
+    }
+    if (total > 0x7fffffffLL) return MG_ERR_CAPACITY;
+    const size_t smem = 16 * (size_t)nmax + 4 * (size_t)nmax + 4 * (2 * (size_t)ncmax + 1) + 16;
+    if (smem > 200 * 1024) return MG_ERR_CAPACITY;  // one replica's positions and cells stay on chip
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return MG_ERR_NO_DEVICE;
+    }
+    int major = 0, minor = 0, nsm = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    if (major != 10 || minor != 3) return MG_ERR_NO_DEVICE;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return MG_ERR_CUDA;
+    }
+    std::vector<int> offset(nrep), order(nrep);
+    long long o = 0;
+    for (int r = 0; r < nrep; r++) {
+        offset[r] = (int)o;
+        o += natom[r];
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return natom[a] > natom[b]; });
+    const size_t nb = sizeof(double) * (size_t)total;
+    std::vector<void *> bufs;
+    auto dalloc = [&](size_t bytes) -> void * {
+        void *q = nullptr;
+        if (cudaMalloc(&q, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        bufs.push_back(q);
+        return q;
+    };
+    mg_status st = MG_OK;
+    cudaStream_t s = nullptr;
+    const size_t nlog = (size_t)nrep * nst * MG_SIMAN_BATCH_LOG;
+    double *d_state = (double *)dalloc(18 * nb);
+    int *d_int = (int *)dalloc(sizeof(int) * (3 * (size_t)nrep + 1));
+    double *d_box = (double *)dalloc(sizeof(double) * nrep);
+    double *d_log = (double *)dalloc(sizeof(double) * nlog);
+    if (!d_state || !d_int || !d_box || !d_log || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) {
+        st = MG_ERR_ALLOC;
+    } else {
+        SimanArgs A;
+        A.nrep = nrep;
+        A.total = (int)total;
+        int *d_order = d_int, *d_natom = d_int + nrep, *d_offset = d_int + 2 * nrep;
+        A.counter = d_int + 3 * nrep;
+        A.order = d_order;
+        A.natom = d_natom;
+        A.offset = d_offset;
+        A.box = d_box;
+        A.x = d_state;
+        A.y = A.x + total;
+        A.z = A.y + total;
+        A.vx = A.z + total;
+        A.vy = A.vx + total;
+        A.vz = A.vy + total;
+        A.f = A.vz + total;
+        A.vn = A.f + 3 * total;
+        A.vo = A.vn + 3 * total;
+        A.b = A.vo + 3 * total;
+        A.nst = nst;
+        A.n_tries = p->n_tries;
+        A.nconstraint = p->nconstraint;
+        A.eps = p->eps;
+        A.sig2 = p->sigma * p->sigma;
+        A.rc = p->rcutoff;
+        A.rc2 = p->rcutoff * p->rcutoff;
+        // shift energy of one pair inside the cutoff, as for mg_hmc_batch
+        const double shift1 = pow(1.0 / p->rcutoff, 6.0), sig6 = pow(p->sigma, 6.0);
+        A.shift_pair = p->eps * sig6 * (sig6 * shift1 - 1.0) * (4.0 * shift1);
+        A.mass = p->mass;
+        A.dt = p->delt;
+        A.qq = p->qq;
+        A.qqs = p->qqs;
+        A.t_initial = p->t_initial;
+        A.mu_t = p->mu_t;
+        A.seed = p->seed;
+        A.log = d_log;
+        A.nmax = nmax;
+        A.ncmax = ncmax;
+        cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_natom, natom, sizeof(int) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_offset, offset.data(), sizeof(int) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(A.counter, 0, sizeof(int), s);
+        cudaMemcpyAsync(d_box, box, sizeof(double) * nrep, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(A.x, x, nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(A.y, y, nb, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(A.z, z, nb, cudaMemcpyHostToDevice, s);
+        if (cudaFuncSetAttribute(k_siman_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            st = MG_ERR_CUDA;
+        } else {
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_siman_batch, HMC_TPB, smem);
+            const int blocks = std::max(1, std::min(nrep, nsm * std::max(per_sm, 1)));
+            k_siman_batch<<<blocks, HMC_TPB, smem, s>>>(A);
+            cudaMemcpyAsync(x, A.x, nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(y, A.y, nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(z, A.z, nb, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(stage_log, d_log, sizeof(double) * nlog, cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) st = MG_ERR_CUDA;
+        }
+    }
+    cudaGetLastError();
+    for (void *q : bufs) cudaFree(q);
+    if (s) cudaStreamDestroy(s);
+    cudaSetDevice(prev);
+    *nstages = nst;
+    return st;
+}
 
 extern "C" mg_status mg_hmc_batch(int device, const mg_hmc_params *p, int nrep, const int *natom, const double *box,
                                   double *x, double *y, double *z, int nmoves, int move0, int *accepted,

@@ -74,6 +74,8 @@ def load_library(path: str = LIB_PATH):
                               C.POINTER(capi.MgMdState), _dp]
     lib.mg_hmc_batch.argtypes = [I, C.POINTER(capi.MgHmcParams), I, C.POINTER(I), _dp, _dp, _dp, _dp, I, I,
                                  C.POINTER(I), _dp, _dp]
+    lib.mg_siman_batch.argtypes = [I, C.POINTER(capi.MgSimanBatchParams), I, C.POINTER(I), _dp, _dp, _dp, _dp,
+                                   C.POINTER(I), _dp]
     lib.mg_sfgrid_sfgridgen.argtypes = [I, C.POINTER(capi.MgSfgridSpec), D, I, C.POINTER(I), _dp]
     lib.mg_sfgrid_tasos.argtypes = [I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, I, _dp]
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
@@ -477,6 +479,29 @@ def hmc_batch(hp: dict, natom, box, x, y, z, nmoves: int, move0: int = 0, device
     if st != MG_OK:
         raise EngineError(st, "mg_hmc_batch")
     return x, y, z, acc, energy, dh[:, :nmoves]
+
+
+def siman_batch(sp: dict, natom, box, x, y, z, device: int = 0):
+    """Simulated annealing of every Lennard-Jones replica in one launch
+    (mg_siman_batch). natom[r], box[r] per replica; x/y/z hold all replicas one after
+    another and are returned annealed. Returns (x, y, z, log[r, stage, 5]) with the
+    columns of capi.SIMAN_BATCH_LOG_NAMES at each stage end."""
+    lib = load_library()
+    natom = np.ascontiguousarray(natom, dtype=np.int32)
+    box = np.ascontiguousarray(box, dtype=np.float64)
+    x, y, z = (np.ascontiguousarray(v, dtype=np.float64).copy() for v in (x, y, z))
+    nrep = len(natom)
+    p = capi.MgSimanBatchParams(**sp)
+    log = np.zeros((nrep, max(p.max_stages, 1), capi.SIMAN_BATCH_LOG))
+    nst = C.c_int(0)
+    st = lib.mg_siman_batch(device, C.byref(p), nrep, natom.ctypes.data_as(C.POINTER(C.c_int)), _p(box), _p(x),
+                            _p(y), _p(z), C.byref(nst), _p(log))
+    if st != MG_OK:
+        raise EngineError(st, "mg_siman_batch")
+    k = nst.value
+    # the library writes [r][stage] with stage < k; rows are k long
+    log = log.reshape(-1)[:nrep * k * capi.SIMAN_BATCH_LOG].reshape(nrep, k, capi.SIMAN_BATCH_LOG).copy()
+    return x, y, z, log
 
 
 def checkpoint_struct(ck: dict):

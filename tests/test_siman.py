@@ -95,3 +95,46 @@ def test_engine_siman_matches_oracle(prec):
     assert np.linalg.norm(vel - rvel) / np.linalg.norm(rvel) <= tol
     for k in ("ps", "pss"):
         assert abs(st[k] - rst[k]) <= tol * max(abs(rst[k]), 1e-12), (prec, k, st[k], rst[k])
+
+
+BATCH = dict(eps=1.0, sigma=1.0, rcutoff=2.5, mass=1.0, delt=0.005, qq=50.0, qqs=50.0, t_initial=2.0, t_min=1.0,
+             mu_t=1.3, n_tries=5, max_stages=8, seed=0x5EED1234ABCD, nconstraint=0)
+
+
+def replica_seed(seed, r):
+    return (seed ^ (r * 0x9E3779B97F4A7C15)) & 0xFFFFFFFFFFFFFFFF
+
+
+@pytest.mark.gpu
+def test_siman_batch_matches_oracle_per_replica():
+    """mg_siman_batch anneals LJ replicas of uneven size (all-pairs and cell-list boxes)
+    in one launch; each replica against the oracle's siman run of that replica alone with
+    the replica's seed: stage log 1e-5 (energies against the stage's energy scale) and
+    positions to 1e-5 of the displacement (FP32 pair forces against FP64)."""
+    from mspms2_gb300 import build, configs
+    from mspms2_gb300.engine import siman_batch
+    from oracle.pyoracle import Oracle
+    build.build()
+    sizes = [200, 350, 500, 864]
+    reps = [configs.lj_replica(n, seed=70 + i) for i, n in enumerate(sizes)]
+    x, y, z = (np.concatenate([getattr(s, a) for s in reps]) for a in "xyz")
+    bx, by, bz, log = siman_batch(BATCH, sizes, [s.box[0] for s in reps], x, y, z)
+    assert log.shape == (4, 4, 5)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for r, s in enumerate(reps):
+        n = sizes[r]
+        md = dict(scheme=1, nstep_inner=1, delt=BATCH["delt"], treq=1.0, qq=BATCH["qq"], qqs=BATCH["qqs"],
+                  gg=3.0 * n, ggs=3.0 * n, nfree=3 * n)
+        sc = dict(t_initial=BATCH["t_initial"], t_min=BATCH["t_min"], mu_t=BATCH["mu_t"], n_tries=BATCH["n_tries"],
+                  max_stages=BATCH["max_stages"], seed=replica_seed(BATCH["seed"], r))
+        start = np.stack([s.x, s.y, s.z]).copy()
+        rpos, _, _, rlog = Oracle(s).siman_run(md, sc)
+        assert rlog.shape[0] == log.shape[1]
+        escale = np.abs(rlog[:, [2, 4]]).max()
+        for kk, ko in zip([0, 1, 2, 3, 4], [0, 1, 2, 4, 5]):
+            scale = escale if kk in (2, 3) else np.abs(rlog[:, ko]).max()
+            err = np.abs(log[r, :, kk] - rlog[:, ko]).max() / scale
+            assert err <= 1e-5, (r, SIMAN_LOG_NAMES[ko], err)
+        pos = np.stack([bx[off[r]:off[r + 1]], by[off[r]:off[r + 1]], bz[off[r]:off[r + 1]]])
+        d = np.linalg.norm((pos - start) - (rpos - start)) / np.linalg.norm(rpos - start)
+        assert d <= 1e-5, (r, d)
