@@ -341,6 +341,35 @@ def hmc_extras(device, nrep=512, nmoves=2, seed=2024):
                     "momenta without rescaling; FP32 pair forces, FP64 energies and Metropolis test"}
 
 
+def siman_batch_extras(device, nrep=512, n_tries=25, seed=2024):
+    """Batched simulated annealing (mg_siman_batch) of the same nrep Lennard-Jones replicas
+    as hmc_extras (200..5000 atoms, rho* 0.8, rc 2.5 sigma), annealed from T* = 2 to below
+    T* = 1 by T /= 1.3 (4 stages, as 600 K -> 300 K in the reference's siman), n_tries
+    Nose-Hoover steps at dt* 0.005 per stage: replica-stages and atom-steps per second of
+    the whole batch."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import siman_batch
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(200, 5001, size=nrep)
+    reps = [configs.lj_replica(int(n), seed=seed + i) for i, n in enumerate(sizes)]
+    natom = [r.natom for r in reps]
+    box = [float(r.box[0]) for r in reps]
+    x, y, z = (np.concatenate([getattr(r, k) for r in reps]) for k in "xyz")
+    sp = dict(eps=1.0, sigma=1.0, rcutoff=2.5, mass=1.0, delt=0.005, qq=50.0, qqs=50.0, t_initial=2.0, t_min=1.0,
+              mu_t=1.3, n_tries=n_tries, max_stages=8, seed=seed, nconstraint=0)
+    siman_batch(dict(sp, n_tries=1), natom, box, x, y, z, device=device)  # warm-up
+    t0 = time.perf_counter()
+    _, _, _, log = siman_batch(sp, natom, box, x, y, z, device=device)
+    dt_wall = time.perf_counter() - t0
+    nst = log.shape[1]
+    return {"replicas": nrep, "atoms": int(sum(natom)), "stages": nst, "steps_per_stage": n_tries,
+            "replica_stages_per_s": nrep * nst / dt_wall,
+            "atom_steps_per_s": float(sum(natom)) * nst * n_tries / dt_wall, "wall_s": dt_wall,
+            "final_tinst_mean": float(log[:, -1, 4].mean()), "final_T": float(log[0, -1, 0]),
+            "note": "one persistent launch per call (host copies of all replicas included); per stage velinit "
+                    "at T and n_tries vver_nh_3 steps; FP32 pair forces, FP64 thermostat and energies"}
+
+
 def adjoint_extras(system, precision, device, reps=3):
     """Derivatives on the bench workload through the host API (positions and vectors in
     host memory, copies included): one long-force evaluation (mg_compute, MG_TERMS_LONG),
@@ -682,6 +711,7 @@ def run_ours(args, rank, world, local_rank):
         if split_r > 0:
             extras["respa"] = md_extras(system, split_r, args.precision, local_rank)
         extras["hmc_batch"] = hmc_extras(local_rank)
+        extras["siman_batch"] = siman_batch_extras(local_rank)
         extras["derivatives"] = adjoint_extras(system, args.precision, local_rank)
         extras["force_matching"] = force_matching_extras(local_rank)
         extras["c5_butane_tubes"] = c5_extras(local_rank)
