@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <numeric>
 #include <type_traits>
 
 #include "mg_internal.cuh"
@@ -41,6 +42,10 @@
 #define EW_FROWS 32     // rows staged per step in the force pass
 #define EW_FG 4         // thread groups sharing the rows of a site in the force pass
 #define EW_FSITES 64    // sites per force block (EW_FG * EW_FSITES threads)
+#define EW_FCHUNK 16    // rows per chunk of the FP32 table force pass (accumulators per site)
+#define EW_FMM_TPB 128  // sites (threads) per block of the FP32 table force pass
+#define EW_FMM_MAXA 64  // largest kzmax + 1 the table force pass stages on chip
+#define EW_MAXSPLIT 16  // row-chunk ranges of the FP32 table force pass
 
 namespace {
 
@@ -151,6 +156,41 @@ __global__ void k_phase_d(int n, const double *__restrict__ x, const double *__r
     }
 }
 
+// largest |kz| of row (kx, ky): min(KZ, floor(sqrt(rem))), rem = KSQMAX - kx^2 - ky^2 >= 0
+__host__ __device__ inline int ew_kzmax(int KZ, int rem) {
+    int k = 0;
+    while (k + 1 <= KZ && (k + 1) * (k + 1) <= rem) k++;
+    return k;
+}
+
+// Visits the half-space rows, f(kx, ky, kzmax, half), in the order every table uses:
+// (kx, -ky), (kx, ky) for kx, ky >= 1; then (j, 0), (0, j) for j >= 1; then (0, 0). Both
+// rows of each of the first pairs have the same KSQMAX - kx^2 - ky^2, hence the same
+// kzmax, and so do (j, 0) and (0, j): rows 2u and 2u+1 form the units of the packed
+// force pass, of equal length unless KMAXX != KMAXY leaves one of (j, 0), (0, j) out.
+template <typename F>
+__host__ __device__ inline void ew_for_rows(int KX, int KY, int KZ, int KS, F f) {
+    auto visit = [&](int kx, int ky) {
+        const int rem = KS - kx * kx - ky * ky;
+        if (rem < 0) return;
+        const int half = (kx == 0 && ky == 0) ? 1 : 0;
+        const int kzmax = ew_kzmax(KZ, rem);
+        if (half && kzmax < 1) return;
+        f(kx, ky, kzmax, half);
+    };
+    for (int kx = 1; kx <= KX; kx++)
+        for (int ky = 1; ky <= KY; ky++) {
+            visit(kx, -ky);
+            visit(kx, ky);
+        }
+    const int J = KX > KY ? KX : KY;
+    for (int j = 1; j <= J; j++) {
+        if (j <= KX) visit(j, 0);
+        if (j <= KY) visit(0, j);
+    }
+    visit(0, 0);
+}
+
 struct EwArgs {
     int n, nrows, nslots, ntasks;
     int kx, ky, kz;  // KMAX per axis (table extents)
@@ -166,6 +206,17 @@ struct EwArgs {
     double *rows_e;
     int row0;
     double *f;
+    // FP32 table force pass: rows by kzmax (longest first) in chunks of EW_FCHUNK; the
+    // chunk coefficients start at coff[chunk] * EW_FCHUNK in fcoef; block row y of the
+    // grid takes chunks [csplit[y], csplit[y + 1]) and, if fsplit > 1, writes its partial
+    // forces to fpart[y][3][n]
+    const int *forder;  // [nrows] row at each force-order position
+    const int *rpos;    // [nrows] force-order position of each row
+    const int *coff;    // [nchunk + 1]
+    int nchunk, fsplit;
+    int csplit[EW_MAXSPLIT + 1];
+    float4 *fcoef;
+    double *fpart;
 };
 
 // FP32 tile with packed f32x2 arithmetic: lanes are two consecutive |kz| (j, j+1). Their
@@ -484,22 +535,389 @@ __global__ void __launch_bounds__(FG * EW_FSITES) k_kforce(EwArgs A, int maxa) {
     A.f[2 * A.n + a] += q * fzs * A.twopi[2];
 }
 
+// FP32 force pass on units of two rows (rows 2u and 2u+1 of the table order), one row
+// per lane of the packed f32x2 arithmetic: the site's Z is the same in both lanes, so
+// one Horner step of the unit is 16 packed FMAs where two rows took 32 scalar ones. Each
+// lane runs the nesting of k_kforce's cfma, and a row shorter than its partner reads
+// zero coefficients above its own top, which leave p, q, p', q' exactly as they were
+// (zero) until its top is reached: per row the lane gives k_kforce's bits. Units are
+// staged EW_FUNITS at a time as [unit][|kz|]{P coefficients, Q coefficients}, each a
+// (re of both rows, im of both rows) pair of f32x2.
+#define EW_FUNITS (EW_FROWS / 2)
+
+template <int FG>
+__global__ void __launch_bounds__(FG * EW_FSITES, 16 / FG) k_kforce_f2(EwArgs A, int maxa) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ulonglong2 *sC = (ulonglong2 *)smem_raw;  // [EW_FUNITS][maxa][2]
+    __shared__ int4 sRow[EW_FROWS];
+    __shared__ double sF[FG][3][EW_FSITES];
+    const int g = threadIdx.x / EW_FSITES, l = threadIdx.x % EW_FSITES;
+    const int a = blockIdx.x * EW_FSITES + l;
+    const bool act = a < A.n;
+    const float2 *tab = (const float2 *)A.tab;
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    const float2 Z = act ? tZ[(size_t)1 * A.n + a] : make_float2(1.f, 0.f);
+    const f32x2 ZX = pk2(Z.x, Z.x), ZY = pk2(Z.y, Z.y), NZY = pk2(-Z.y, -Z.y);
+    float Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};  // per-chunk sums accumulated as hi + lo
+    const float4 *coef = (const float4 *)A.scoef;
+    for (int r0 = 0; r0 < A.nrows; r0 += EW_FROWS) {
+        const int nr = min(EW_FROWS, A.nrows - r0);
+        const int nu = (nr + 1) / 2;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nu * maxa; i += blockDim.x) {
+            const int uu = i / maxa, s = i % maxa;
+            const int ra = r0 + 2 * uu, rb = ra + 1;
+            float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
+            if (s <= A.rows[ra].z) c0 = coef[A.row_slot[ra] / 2 + s];
+            if (2 * uu + 1 < nr && s <= A.rows[rb].z) c1 = coef[A.row_slot[rb] / 2 + s];
+            sC[2 * (uu * maxa + s)] = make_ulonglong2(pk2(c0.x, c1.x), pk2(c0.y, c1.y));
+            sC[2 * (uu * maxa + s) + 1] = make_ulonglong2(pk2(c0.z, c1.z), pk2(c0.w, c1.w));
+        }
+        if (threadIdx.x < 2 * nu)  // an absent second row of the last unit: (0, 0), no |kz|
+            sRow[threadIdx.x] = threadIdx.x < nr ? A.rows[r0 + threadIdx.x] : make_int4(0, 0, -1, 0);
+        __syncthreads();
+        if (!act) continue;
+        float fx = 0, fy = 0, fz = 0;
+        for (int uu = g; uu < nu; uu += FG) {
+            const int4 ra = sRow[2 * uu], rb = sRow[2 * uu + 1];
+            float2 X0 = tX[(size_t)ra.x * A.n + a], Y0 = tY[(size_t)(ra.y < 0 ? -ra.y : ra.y) * A.n + a];
+            float2 X1 = tX[(size_t)rb.x * A.n + a], Y1 = tY[(size_t)(rb.y < 0 ? -rb.y : rb.y) * A.n + a];
+            if (ra.y < 0) Y0.y = -Y0.y;
+            if (rb.y < 0) Y1.y = -Y1.y;
+            const float2 A0 = cmul(X0, Y0), A1 = cmul(X1, Y1);
+            const ulonglong2 *cs = sC + 2 * uu * maxa;
+            const int m = max(ra.z, rb.z);
+            const ulonglong2 tu = cs[2 * m], tv = cs[2 * m + 1];
+            f32x2 pr = tu.x, pi = tu.y, qr = tv.x, qi = tv.y;
+            f32x2 dpr = 0, dpi = 0, dqr = 0, dqi = 0;
+#pragma unroll 2
+            for (int k = m - 1; k >= 0; k--) {
+                const ulonglong2 cu = cs[2 * k], cv = cs[2 * k + 1];
+                // dp <- dp Z + p, p <- p Z + cu, dq <- dq Z + q, q <- q Z + cv
+                const f32x2 ndpr = fma2(dpr, ZX, fma2(dpi, NZY, pr));
+                const f32x2 ndpi = fma2(dpr, ZY, fma2(dpi, ZX, pi));
+                const f32x2 npr = fma2(pr, ZX, fma2(pi, NZY, cu.x));
+                const f32x2 npi = fma2(pr, ZY, fma2(pi, ZX, cu.y));
+                const f32x2 ndqr = fma2(dqr, ZX, fma2(dqi, NZY, qr));
+                const f32x2 ndqi = fma2(dqr, ZY, fma2(dqi, ZX, qi));
+                const f32x2 nqr = fma2(qr, ZX, fma2(qi, NZY, cv.x));
+                const f32x2 nqi = fma2(qr, ZY, fma2(qi, ZX, cv.y));
+                dpr = ndpr;
+                dpi = ndpi;
+                pr = npr;
+                pi = npi;
+                dqr = ndqr;
+                dqi = ndqi;
+                qr = nqr;
+                qi = nqi;
+            }
+            float2 p[2], q[2], dp[2], dq[2];
+            up2(pr, p[0].x, p[1].x);
+            up2(pi, p[0].y, p[1].y);
+            up2(qr, q[0].x, q[1].x);
+            up2(qi, q[0].y, q[1].y);
+            up2(dpr, dp[0].x, dp[1].x);
+            up2(dpi, dp[0].y, dp[1].y);
+            up2(dqr, dq[0].x, dq[1].x);
+            up2(dqi, dq[0].y, dq[1].y);
+            const float2 Aa[2] = {A0, A1};
+            const int4 rw[2] = {ra, rb};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float gsum = (Aa[h].x * p[h].y + Aa[h].y * p[h].x) + (Aa[h].y * q[h].x - Aa[h].x * q[h].y);
+                const float2 zdp = cmul(Z, dp[h]), zdq = cmul(Z, dq[h]);
+                const float gz = (Aa[h].x * zdp.y + Aa[h].y * zdp.x) - (Aa[h].y * zdq.x - Aa[h].x * zdq.y);
+                fx += gsum * (float)rw[h].x;
+                fy += gsum * (float)rw[h].y;
+                fz += gz;
+            }
+        }
+        mg_acc2(Fh[0], Fl[0], fx);
+        mg_acc2(Fh[1], Fl[1], fy);
+        mg_acc2(Fh[2], Fl[2], fz);
+    }
+    for (int d = 0; d < 3; d++) sF[g][d][l] = (double)Fh[d] + (double)Fl[d];
+    __syncthreads();
+    if (g != 0 || !act) return;
+    double fxs = 0, fys = 0, fzs = 0;
+    for (int k = 0; k < FG; k++) {
+        fxs += sF[k][0][l];
+        fys += sF[k][1][l];
+        fzs += sF[k][2][l];
+    }
+    const double q = A.q[a];
+    A.f[a] += q * fxs * A.twopi[0];
+    A.f[A.n + a] += q * fys * A.twopi[1];
+    A.f[2 * A.n + a] += q * fzs * A.twopi[2];
+}
+
+// FP32 force pass from the phase tables. For one site and one row, with z_a = Z^a from
+// the table and z^-a = conj(z^a), the row's kz sums are
+//   gsum = Im(A W),  W  = sum_a [ u_a z^a + conj(v_a) conj(z^a) ]
+//   gz   = Im(A W'), W' = sum_a a [ u_a z^a - conj(v_a) conj(z^a) ]
+// (u_a = conj(c S+_a), v_a = c S-_a, the same values k_kforce's Horner sums use). With
+// s = u + v, d = u - v per |kz|: W_r = sum zr s_r - zi s_i, W_i = sum zr d_i + zi d_r,
+// W'_r = sum a (zr d_r - zi d_i), W'_i = sum a (zi s_r + zr s_i): 8 FMAs per site, row
+// and |kz| against Horner's 16. k_fcoef stores (k0, k2, k1, k3) = (s_r, d_i, -s_i, d_r)
+// per [chunk][|kz|][row of the chunk]; a thread owns one site and the 16 rows of a chunk
+// (W in packed f32x2 as (W_r, W_i), W' in scalar FMAs, so both FP32 pipe halves work
+// from one broadcast 16-byte shared load per row and |kz|).
+__global__ void k_fcoef(EwArgs A) {
+    const int c = blockIdx.x;
+    const int m = A.rows[A.forder[c * EW_FCHUNK]].z;
+    const float4 *coef = (const float4 *)A.scoef;
+    float4 *out = A.fcoef + (size_t)A.coff[c] * EW_FCHUNK;
+    for (int i = threadIdx.x; i < (m + 1) * EW_FCHUNK; i += blockDim.x) {
+        const int a = i / EW_FCHUNK, p = c * EW_FCHUNK + i % EW_FCHUNK;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p < A.nrows) {
+            const int r = A.forder[p];
+            if (a <= A.rows[r].z) {
+                const float4 uv = coef[A.row_slot[r] / 2 + a];  // u_r, u_i, v_r, v_i
+                const float sr = uv.x + uv.z, si = uv.y + uv.w, dr = uv.x - uv.z, di = uv.y - uv.w;
+                v = make_float4(sr, di, -si, dr);
+            }
+        }
+        out[i] = v;
+    }
+}
+
+__global__ void __launch_bounds__(EW_FMM_TPB, 6) k_kforce_mm(EwArgs A, int maxa) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ulonglong2 *sK = (ulonglong2 *)smem_raw;                      // [maxa][EW_FCHUNK]
+    float2 *sZ = (float2 *)(sK + (size_t)maxa * EW_FCHUNK);       // [maxa][EW_FMM_TPB]
+    __shared__ int2 sR[EW_FCHUNK];                                // (kx, ky); (0, 0) pads
+    const int a_site = blockIdx.x * EW_FMM_TPB + threadIdx.x;
+    const bool act = a_site < A.n;
+    const int site = act ? a_site : A.n - 1;  // idle threads read a valid site, store nothing
+    const float2 *tab = (const float2 *)A.tab;
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    for (int k = 0; k < maxa; k++) sZ[k * EW_FMM_TPB + threadIdx.x] = tZ[(size_t)k * A.n + site];
+    float Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};  // per-chunk sums accumulated as hi + lo
+    const int c_lo = A.csplit[blockIdx.y], c_hi = A.csplit[blockIdx.y + 1];
+    for (int c = c_lo; c < c_hi; c++) {
+        const int m = A.rows[A.forder[c * EW_FCHUNK]].z;
+        __syncthreads();
+        const ulonglong2 *src = (const ulonglong2 *)(A.fcoef + (size_t)A.coff[c] * EW_FCHUNK);
+        for (int i = threadIdx.x; i < (m + 1) * EW_FCHUNK; i += EW_FMM_TPB) sK[i] = src[i];
+        if (threadIdx.x < EW_FCHUNK) {
+            const int p = c * EW_FCHUNK + threadIdx.x;
+            int2 kk = make_int2(0, 0);
+            if (p < A.nrows) {
+                const int4 r = A.rows[A.forder[p]];
+                kk = make_int2(r.x, r.y);
+            }
+            sR[threadIdx.x] = kk;
+        }
+        __syncthreads();
+        f32x2 W[EW_FCHUNK];
+        float Pr[EW_FCHUNK], Pi[EW_FCHUNK];
+#pragma unroll
+        for (int j = 0; j < EW_FCHUNK; j++) {
+            W[j] = 0;
+            Pr[j] = Pi[j] = 0.f;
+        }
+        for (int a = 0; a <= m; a++) {
+            const float2 z = sZ[a * EW_FMM_TPB + threadIdx.x];
+            const float fa = (float)a, azr = fa * z.x, azi = fa * z.y;
+            const f32x2 ZR = pk2(z.x, z.x), ZI = pk2(z.y, z.y);
+            const ulonglong2 *kr = sK + a * EW_FCHUNK;
+#pragma unroll
+            for (int j = 0; j < EW_FCHUNK; j++) {
+                const ulonglong2 kk = kr[j];  // (k0, k2), (k1, k3)
+                W[j] = fma2(ZI, kk.y, fma2(ZR, kk.x, W[j]));
+                float k0, k1, k2, k3;
+                up2(kk.x, k0, k2);
+                up2(kk.y, k1, k3);
+                Pr[j] = fmaf(azr, k3, fmaf(-azi, k2, Pr[j]));
+                Pi[j] = fmaf(azi, k0, fmaf(-azr, k1, Pi[j]));
+            }
+        }
+        float fx = 0, fy = 0, fz = 0;
+#pragma unroll
+        for (int j = 0; j < EW_FCHUNK; j++) {
+            const int2 kk = sR[j];
+            const float2 X = tX[(size_t)kk.x * A.n + site];
+            float2 Y = tY[(size_t)(kk.y < 0 ? -kk.y : kk.y) * A.n + site];
+            if (kk.y < 0) Y.y = -Y.y;
+            const float2 Aa = cmul(X, Y);
+            float wr, wi;
+            up2(W[j], wr, wi);
+            const float gsum = Aa.x * wi + Aa.y * wr;
+            fx += gsum * (float)kk.x;
+            fy += gsum * (float)kk.y;
+            fz += Aa.x * Pi[j] + Aa.y * Pr[j];
+        }
+        mg_acc2(Fh[0], Fl[0], fx);
+        mg_acc2(Fh[1], Fl[1], fy);
+        mg_acc2(Fh[2], Fl[2], fz);
+    }
+    if (!act) return;
+    if (A.fsplit == 1) {
+        const double q = A.q[a_site];
+        for (int d = 0; d < 3; d++) A.f[(size_t)d * A.n + a_site] += q * ((double)Fh[d] + (double)Fl[d]) * A.twopi[d];
+    } else {
+        for (int d = 0; d < 3; d++)
+            A.fpart[((size_t)blockIdx.y * 3 + d) * A.n + a_site] = (double)Fh[d] + (double)Fl[d];
+    }
+}
+
+// forces from the partials of the row-chunk ranges, summed in range order
+__global__ void k_kforce_sum(EwArgs A) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A.n) return;
+    const double q = A.q[a];
+    for (int d = 0; d < 3; d++) {
+        double t = 0.0;
+        for (int y = 0; y < A.fsplit; y++) t += A.fpart[((size_t)y * 3 + d) * A.n + a];
+        A.f[(size_t)d * A.n + a] += q * t * A.twopi[d];
+    }
+}
+
+inline size_t fmm_smem(int maxa) { return (size_t)maxa * (EW_FCHUNK * sizeof(ulonglong2) + EW_FMM_TPB * sizeof(float2)); }
+
+// resident blocks of k_kforce_mm per SM x SMs, per device and dynamic shared memory size
+int fmm_slots(int maxa) {
+    static std::mutex mu;
+    static int cache_dev = -1, cache_maxa = -1, cache_slots = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev == cache_dev && maxa == cache_maxa) return cache_slots;
+    const size_t smem = fmm_smem(maxa);
+    int per_sm = 0, nsm = 0;
+    cudaFuncSetAttribute(k_kforce_mm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_kforce_mm, EW_FMM_TPB, smem);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    cache_dev = dev;
+    cache_maxa = maxa;
+    cache_slots = std::max(1, per_sm) * std::max(1, nsm);
+    return cache_slots;
+}
+
+// Splits the chunks into S ranges of about equal work (sum of kzmax + 1) and picks S in
+// [1, smax] so that site blocks x S fill the device's resident-block slots in whole
+// waves; returns S and fills csplit[0..S].
+int fmm_split(const std::vector<int> &chunk_kz, int n, int slots, int smax, int *csplit) {
+    const int nc = (int)chunk_kz.size();
+    const long long nb = (n + EW_FMM_TPB - 1) / EW_FMM_TPB;
+    smax = std::max(1, std::min(std::min(smax, EW_MAXSPLIT), nc));
+    int best = 1;
+    double best_eff = 0.0;
+    for (int S = 1; S <= smax; S++) {
+        const long long items = nb * S;
+        const long long rounds = (items + slots - 1) / slots;
+        const double eff = (double)items / (double)(rounds * slots);
+        if (eff > best_eff + 0.02) {
+            best_eff = eff;
+            best = S;
+        }
+    }
+    long long total = 0;
+    for (int k : chunk_kz) total += k + 1;
+    csplit[0] = 0;
+    long long acc = 0;
+    int c = 0;
+    for (int y = 1; y < best; y++) {
+        const long long target = total * y / best;
+        while (c < nc && acc + chunk_kz[c] + 1 <= target) {
+            acc += chunk_kz[c] + 1;
+            c++;
+        }
+        csplit[y] = std::max(c, csplit[y - 1]);
+    }
+    csplit[best] = nc;
+    return best;
+}
+
+// chunk kzmax (first row of each chunk) from a kzmax histogram of the rows
+std::vector<int> fmm_chunk_kz(const int *hist, int nrows) {
+    std::vector<int> out((nrows + EW_FCHUNK - 1) / EW_FCHUNK);
+    int pos = 0;
+    for (int k = 255; k >= 0; k--)
+        for (int i = 0; i < hist[k]; i++, pos++)
+            if (pos % EW_FCHUNK == 0) out[pos / EW_FCHUNK] = k;
+    return out;
+}
+
+// launches of the FP32 force pass for A (with the table pass: coefficients, forces and,
+// for a split, the sum)
+int fmm_launches(const EwArgs &A, int maxa) {
+    if (!A.fcoef || maxa > EW_FMM_MAXA) return 1;
+    return A.fsplit > 1 ? 3 : 2;
+}
+
+// The FP32 table force pass's tables and buffers of a context (none for the FP64 path
+// or rows longer than EW_FMM_MAXA, which take k_kforce); false if a buffer could not
+// be allocated.
+bool ew_force_fields(mg_ctx *c, EwArgs &A, int maxa) {
+    A.fcoef = nullptr;
+    A.fpart = nullptr;
+    A.fsplit = 1;
+    const int nr = c->nrows;
+    A.forder = (const int *)c->d_row_slot.p + nr + c->nslots;
+    A.rpos = A.forder + nr;
+    A.coff = A.rpos + nr;
+    A.nchunk = (int)c->h_chunk_kz.size();
+    A.csplit[0] = 0;
+    A.csplit[1] = A.nchunk;
+    if (c->opt.precision == MG_PREC_FP64 || maxa > EW_FMM_MAXA || A.nchunk == 0) return true;
+    size_t ncoef = 0;
+    for (int k : c->h_chunk_kz) ncoef += (size_t)(k + 1) * EW_FCHUNK;
+    if (!mg_ensure(c, c->d_fcoef, sizeof(float4) * ncoef)) return false;
+    A.fcoef = (float4 *)c->d_fcoef.p;
+    A.fsplit = fmm_split(c->h_chunk_kz, A.n, fmm_slots(maxa), EW_MAXSPLIT, A.csplit);
+    if (A.fsplit > 1) {
+        if (!mg_ensure(c, c->d_fpart, sizeof(double) * 3 * (size_t)A.fsplit * A.n)) return false;
+        A.fpart = (double *)c->d_fpart.p;
+    }
+    return true;
+}
+
 // k_kforce with fg threads per site (2, 4 or 8) and its dynamic shared memory
 template <typename R>
 cudaError_t launch_kforce(int fg, unsigned blocks, size_t smem, cudaStream_t s, const EwArgs &A, int maxa) {
     cudaError_t e;
-    switch (fg) {
-    case 2:
-        e = cudaFuncSetAttribute(k_kforce<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_kforce<R, 2><<<blocks, 2 * EW_FSITES, smem, s>>>(A, maxa);
-        break;
-    case 8:
-        e = cudaFuncSetAttribute(k_kforce<R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_kforce<R, 8><<<blocks, 8 * EW_FSITES, smem, s>>>(A, maxa);
-        break;
-    default:
-        e = cudaFuncSetAttribute(k_kforce<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_kforce<R, 4><<<blocks, 4 * EW_FSITES, smem, s>>>(A, maxa);
+    if constexpr (std::is_same<R, float>::value) {
+        if (A.fcoef && maxa <= EW_FMM_MAXA) {
+            if (A.n == 0 || A.nchunk == 0) return cudaSuccess;
+            k_fcoef<<<A.nchunk, 256, 0, s>>>(A);
+            const size_t msmem = fmm_smem(maxa);
+            e = cudaFuncSetAttribute(k_kforce_mm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem);
+            if (e != cudaSuccess) return e;
+            const dim3 grid((unsigned)((A.n + EW_FMM_TPB - 1) / EW_FMM_TPB), (unsigned)A.fsplit);
+            k_kforce_mm<<<grid, EW_FMM_TPB, msmem, s>>>(A, maxa);
+            if (A.fsplit > 1) k_kforce_sum<<<(A.n + 255) / 256, 256, 0, s>>>(A);
+            return cudaGetLastError();
+        }
+        switch (fg) {
+        case 2:
+            e = cudaFuncSetAttribute(k_kforce_f2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_kforce_f2<2><<<blocks, 2 * EW_FSITES, smem, s>>>(A, maxa);
+            break;
+        case 8:
+            e = cudaFuncSetAttribute(k_kforce_f2<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_kforce_f2<8><<<blocks, 8 * EW_FSITES, smem, s>>>(A, maxa);
+            break;
+        default:
+            e = cudaFuncSetAttribute(k_kforce_f2<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_kforce_f2<4><<<blocks, 4 * EW_FSITES, smem, s>>>(A, maxa);
+        }
+    } else {
+        switch (fg) {
+        case 2:
+            e = cudaFuncSetAttribute(k_kforce<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_kforce<R, 2><<<blocks, 2 * EW_FSITES, smem, s>>>(A, maxa);
+            break;
+        case 8:
+            e = cudaFuncSetAttribute(k_kforce<R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_kforce<R, 8><<<blocks, 8 * EW_FSITES, smem, s>>>(A, maxa);
+            break;
+        default:
+            e = cudaFuncSetAttribute(k_kforce<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_kforce<R, 4><<<blocks, 4 * EW_FSITES, smem, s>>>(A, maxa);
+        }
     }
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
@@ -514,35 +932,25 @@ mg_status mg_ewald_setup(mg_ctx *c) {
     std::vector<int4> tasks;
     int nslots = 0;
     long long kvec = 0;
-    for (int kx = 0; kx <= KX; kx++)
-        for (int ky = -KY; ky <= KY; ky++) {
-            if (kx == 0 && ky < 0) continue;
-            int rem = KS - kx * kx - ky * ky;
-            if (rem < 0) continue;
-            int kzmax = std::min(KZ, (int)floor(sqrt((double)rem)));
-            while ((kzmax + 1) <= KZ && (kzmax + 1) * (kzmax + 1) <= rem) kzmax++;
-            while (kzmax >= 0 && kzmax * kzmax > rem) kzmax--;
-            int half = (kx == 0 && ky == 0) ? 1 : 0;
-            if (half && kzmax < 1) continue;
-            if (kzmax < 0) continue;
-            int r = (int)(rows.size() / 4);
-            rows.push_back(kx);
-            rows.push_back(ky);
-            rows.push_back(kzmax);
-            rows.push_back(half);
-            slot_start.push_back(nslots);
-            int ns = 2 * (kzmax + 1);
-            for (int s = 0; s < ns; s++) slot_row.push_back(r);
-            nslots += ns;
-            kvec += half ? kzmax : 2 * kzmax + 1;
-            int nv = kzmax + 1;
-            int nch = (nv + EW_CH - 1) / EW_CH;
-            for (int h = 0, k0 = 0; h < nch; h++) {  // balanced chunks
-                int len = nv / nch + (h < nv % nch ? 1 : 0);
-                tasks.push_back(make_int4(r, k0, len, 0));
-                k0 += len;
-            }
+    ew_for_rows(KX, KY, KZ, KS, [&](int kx, int ky, int kzmax, int half) {
+        int r = (int)(rows.size() / 4);
+        rows.push_back(kx);
+        rows.push_back(ky);
+        rows.push_back(kzmax);
+        rows.push_back(half);
+        slot_start.push_back(nslots);
+        int ns = 2 * (kzmax + 1);
+        for (int s = 0; s < ns; s++) slot_row.push_back(r);
+        nslots += ns;
+        kvec += half ? kzmax : 2 * kzmax + 1;
+        int nv = kzmax + 1;
+        int nch = (nv + EW_CH - 1) / EW_CH;
+        for (int h = 0, k0 = 0; h < nch; h++) {  // balanced chunks
+            int len = nv / nch + (h < nv % nch ? 1 : 0);
+            tasks.push_back(make_int4(r, k0, len, 0));
+            k0 += len;
         }
+    });
     std::stable_sort(tasks.begin(), tasks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
     {  // pad each length group to whole warps with empty tasks (row 0, count 0)
         std::vector<int4> padded;
@@ -565,10 +973,29 @@ mg_status mg_ewald_setup(mg_ctx *c) {
     c->ewald_box[0] = c->lx;
     c->ewald_box[1] = c->ly;
     c->ewald_box[2] = c->lz;
+    c->h_chunk_kz.clear();
     if (c->nrows == 0) return MG_OK;
-    std::vector<int> packed(slot_start.size() + slot_row.size());
-    std::copy(slot_start.begin(), slot_start.end(), packed.begin());
-    std::copy(slot_row.begin(), slot_row.end(), packed.begin() + slot_start.size());
+    // force order of the FP32 table pass: rows by kzmax, longest first (ties in row order),
+    // then the chunks' coefficient offsets
+    const int nr = c->nrows;
+    std::vector<int> forder(nr), rpos(nr);
+    std::iota(forder.begin(), forder.end(), 0);
+    std::stable_sort(forder.begin(), forder.end(), [&](int a, int b) { return rows[4 * a + 2] > rows[4 * b + 2]; });
+    for (int q = 0; q < nr; q++) rpos[forder[q]] = q;
+    const int nchunk = (nr + EW_FCHUNK - 1) / EW_FCHUNK;
+    std::vector<int> coff(nchunk + 1, 0);
+    c->h_chunk_kz.resize(nchunk);
+    for (int k = 0; k < nchunk; k++) {
+        c->h_chunk_kz[k] = rows[4 * forder[k * EW_FCHUNK] + 2];
+        coff[k + 1] = coff[k] + c->h_chunk_kz[k] + 1;
+    }
+    std::vector<int> packed;
+    packed.reserve(slot_start.size() + slot_row.size() + 2 * nr + nchunk + 1);
+    packed.insert(packed.end(), slot_start.begin(), slot_start.end());
+    packed.insert(packed.end(), slot_row.begin(), slot_row.end());
+    packed.insert(packed.end(), forder.begin(), forder.end());
+    packed.insert(packed.end(), rpos.begin(), rpos.end());
+    packed.insert(packed.end(), coff.begin(), coff.end());
     if (!mg_ensure(c, c->d_rows, sizeof(int) * rows.size()) || !mg_ensure(c, c->d_row_slot, sizeof(int) * packed.size()) ||
         !mg_ensure(c, c->d_tasks, sizeof(int4) * tasks.size()))
         return MG_ERR_ALLOC;
@@ -598,7 +1025,7 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
         k_phase_d<<<(n + 127) / 128, 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (double2 *)c->d_phase.p);
     else
         k_phase_f<<<(n + 127) / 128, 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)c->d_phase.p);
-    EwArgs A;
+    EwArgs A = {};
     A.n = n;
     A.nrows = c->nrows;
     A.nslots = c->nslots;
@@ -645,11 +1072,13 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
     size_t fsmem = 2 * esz * (size_t)EW_FROWS * maxa;
     unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
-    if (fp64)
+    if (fp64) {
         MG_CUDA(launch_kforce<double>(c->tune.kforce_threads, fblocks, fsmem, s, A, maxa));
-    else
+    } else {
+        if (!ew_force_fields(c, A, maxa)) return mg_fail(c, MG_ERR_ALLOC, "k-space force buffers");
         MG_CUDA(launch_kforce<float>(c->tune.kforce_threads, fblocks, fsmem, s, A, maxa));
-    c->launches += 4;
+    }
+    c->launches += 3 + (fp64 ? 1 : fmm_launches(A, maxa));
     return MG_OK;
 }
 
@@ -676,28 +1105,6 @@ struct EwStaticDevice {
 EwStaticDevice g_ew_static[EW_STATIC_MAX_DEVICES];
 std::mutex g_ew_static_mutex;
 
-// largest |kz| of row (kx, ky): min(KZ, floor(sqrt(rem))), rem = KSQMAX - kx^2 - ky^2 >= 0
-__host__ __device__ inline int ew_kzmax(int KZ, int rem) {
-    int k = 0;
-    while (k + 1 <= KZ && (k + 1) * (k + 1) <= rem) k++;
-    return k;
-}
-
-// Visits the half-space rows in the order of mg_ewald_setup: f(kx, ky, kzmax, half).
-template <typename F>
-__host__ __device__ inline void ew_for_rows(int KX, int KY, int KZ, int KS, F f) {
-    for (int kx = 0; kx <= KX; kx++)
-        for (int ky = -KY; ky <= KY; ky++) {
-            if (kx == 0 && ky < 0) continue;
-            int rem = KS - kx * kx - ky * ky;
-            if (rem < 0) continue;
-            int kzmax = ew_kzmax(KZ, rem);
-            int half = (kx == 0 && ky == 0) ? 1 : 0;
-            if (half && kzmax < 1) continue;
-            f(kx, ky, kzmax, half);
-        }
-}
-
 // length of chunk h of a row with nv |kz| values (balanced chunks of at most EW_CH)
 __host__ __device__ inline int ew_chunk_len(int nv, int h) {
     int nch = (nv + EW_CH - 1) / EW_CH;
@@ -706,13 +1113,16 @@ __host__ __device__ inline int ew_chunk_len(int nv, int h) {
 
 struct EwCounts {
     int nrows = 0, nslots = 0, ntasks = 0, maxa = 1;
+    std::vector<int> chunk_kz;  // kzmax of each chunk of the FP32 table force pass
 };
 
 EwCounts ew_count(int KX, int KY, int KZ, int KS) {
     EwCounts c;
     int by_len[EW_CH + 1] = {0};
+    int hist[256] = {0};
     ew_for_rows(KX, KY, KZ, KS, [&](int, int, int kzmax, int) {
         int nv = kzmax + 1;
+        hist[kzmax]++;
         c.nrows++;
         c.nslots += 2 * nv;
         c.maxa = std::max(c.maxa, nv);
@@ -720,13 +1130,14 @@ EwCounts ew_count(int KX, int KY, int KZ, int KS) {
         for (int h = 0; h < nch; h++) by_len[ew_chunk_len(nv, h)]++;
     });
     for (int L = 1; L <= EW_CH; L++) c.ntasks += (by_len[L] + 31) / 32 * 32;
+    c.chunk_kz = fmm_chunk_kz(hist, c.nrows);
     return c;
 }
 
 // Row table, packed slot table (first slot of each row, then the row of each slot) and
 // the task list sorted by length (longest first, rows ascending) with each length group
 // padded to whole warps: the same tables mg_ewald_setup builds on the host.
-__global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int4 *__restrict__ rows,
+__global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int nslots, int4 *__restrict__ rows,
                             int *__restrict__ row_slot, int4 *__restrict__ tasks) {
     if (threadIdx.x == 0) {
         int r = 0, slot = 0;
@@ -748,6 +1159,25 @@ __global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int4 *__r
             }
             while (t % 32) tasks[t++] = make_int4(0, 0, 0, 0);
         }
+        // force order (kzmax descending, ties in row order) and chunk offsets, by a
+        // counting sort over kzmax <= 255
+        int *forder = row_slot + nrows + nslots, *rpos = forder + nrows, *coff = rpos + nrows;
+        int start[256];
+        for (int k = 0; k < 256; k++) start[k] = 0;
+        for (int q = 0; q < nrows; q++) start[rows[q].z]++;
+        for (int k = 255, run = 0; k >= 0; k--) {
+            const int h = start[k];
+            start[k] = run;
+            run += h;
+        }
+        for (int q = 0; q < nrows; q++) {
+            const int p = start[rows[q].z]++;
+            forder[p] = q;
+            rpos[q] = p;
+        }
+        const int nchunk = (nrows + EW_FCHUNK - 1) / EW_FCHUNK;
+        coff[0] = 0;
+        for (int k = 0; k < nchunk; k++) coff[k + 1] = coff[k] + rows[forder[k * EW_FCHUNK]].z + 1;
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nrows; q += blockDim.x) {
@@ -861,8 +1291,9 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     size_t off = 0;
     const size_t o_rows = off;
     off += ew_align256(sizeof(int4) * (size_t)ct.nrows);
-    const size_t o_slot = off;
-    off += ew_align256(sizeof(int) * ((size_t)ct.nrows + ct.nslots));
+    const int nchunk = (int)ct.chunk_kz.size();
+    const size_t o_slot = off;  // slot starts, slot rows, force order, its inverse, chunk offsets
+    off += ew_align256(sizeof(int) * ((size_t)3 * ct.nrows + ct.nslots + nchunk + 1));
     const size_t o_tasks = off;
     off += ew_align256(sizeof(int4) * (size_t)ct.ntasks);
     const size_t o_tab = off;
@@ -873,6 +1304,11 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     off += ew_align256(esz * (size_t)ct.nslots);
     const size_t o_erows = off;
     off += ew_align256(sizeof(double) * E_NCOMP * (size_t)rblocks);
+    const bool table_force = !fp64 && ct.maxa <= EW_FMM_MAXA;
+    size_t ncoef = 0;
+    for (int k : ct.chunk_kz) ncoef += (size_t)(k + 1) * EW_FCHUNK;
+    const size_t o_fcoef = off;
+    if (table_force) off += ew_align256(sizeof(float4) * ncoef);
     if (off > (size_t)MG_EWALD_STATIC_SCRATCH_BYTES)
         return ew_static_fail(err, err_len, MG_ERR_CAPACITY,
                               "%d sites with kmax (%d,%d,%d), ksqmax %d need %zu bytes of scratch; the limit is %u",
@@ -883,7 +1319,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     int4 *tasks = (int4 *)(base + o_tasks);
     const int key[4] = {KX, KY, KZ0, KS};
     if (!std::equal(key, key + 4, dev.key)) {
-        k_ew_tables<<<1, 256, 0, s>>>(KX, KY, KZ0, KS, ct.nrows, rows, row_slot, tasks);
+        k_ew_tables<<<1, 256, 0, s>>>(KX, KY, KZ0, KS, ct.nrows, ct.nslots, rows, row_slot, tasks);
         EWS_CUDA(cudaGetLastError(), "k_ew_tables launch");
         std::copy(key, key + 4, dev.key);
     }
@@ -895,7 +1331,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
         k_phase_d<<<(n + 127) / 128, 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (double2 *)tab);
     else
         k_phase_f<<<(n + 127) / 128, 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)tab);
-    EwArgs A;
+    EwArgs A = {};
     A.n = n;
     A.nrows = ct.nrows;
     A.nslots = ct.nslots;
@@ -919,6 +1355,24 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     A.rows_e = (double *)(base + o_erows);
     A.row0 = 0;
     A.f = d_f;
+    A.forder = row_slot + ct.nrows + ct.nslots;
+    A.rpos = A.forder + ct.nrows;
+    A.coff = A.rpos + ct.nrows;
+    A.nchunk = nchunk;
+    A.fsplit = 1;
+    A.csplit[0] = 0;
+    A.csplit[1] = nchunk;
+    if (table_force) {
+        A.fcoef = (float4 *)(base + o_fcoef);
+        // partial forces of a row split in what scratch is left
+        const size_t left = (size_t)MG_EWALD_STATIC_SCRATCH_BYTES - off;
+        const size_t per = sizeof(double) * 3 * (size_t)n;
+        const int smax = (int)std::min<size_t>(EW_MAXSPLIT, per ? left / per : 1);
+        if (smax >= 2) {
+            A.fsplit = fmm_split(ct.chunk_kz, n, fmm_slots(ct.maxa), smax, A.csplit);
+            if (A.fsplit > 1) A.fpart = (double *)(base + ew_align256(off));
+        }
+    }
     const int P = EW_TILE + 1;
     const size_t smem = esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
     const dim3 grid((ct.ntasks + EW_TPB - 1) / EW_TPB, nblk);
@@ -938,9 +1392,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
                  "cudaFuncSetAttribute");
         k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
         k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
-        EWS_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem),
-                 "cudaFuncSetAttribute");
-        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, ct.maxa);
+        EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
     }
     if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, d_energy);
     EWS_CUDA(cudaGetLastError(), "kernel launch");
@@ -1030,6 +1482,11 @@ EwArgs ew_args(mg_ctx *c) {
     A.bfac = p.bfactor_ewald;
     A.vfac = p.vfactor_ewald;
     A.coul = p.coulomb_prefactor;
+    const int maxa = c->h_chunk_kz.empty() ? 1 : c->h_chunk_kz[0] + 1;
+    if (!ew_force_fields(c, A, maxa)) {  // the Horner pass needs no extra buffers
+        A.fcoef = nullptr;
+        A.fsplit = 1;
+    }
     return A;
 }
 
@@ -1081,8 +1538,7 @@ mg_status mg_ewald_field(mg_ctx *c, const double *ones, double *field) {
         MG_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
         k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
     } else {
-        MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa);
+        MG_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, maxa));
     }
     MG_CUDA(cudaGetLastError());
     return MG_OK;
@@ -1271,8 +1727,7 @@ mg_status mg_ewald_jvp(mg_ctx *c, const double *v, const double2 *SW, void *coef
         MG_CUDA(cudaFuncSetAttribute(k_khess<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
         k_khess<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, maxa, v, out);
         k_hvcoef<float><<<sb, 256, 0, s>>>(A, slot_row, SW, coef_scratch);
-        MG_CUDA(cudaFuncSetAttribute(k_kforce<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-        k_kforce<float><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(B, maxa);
+        MG_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, B, maxa));
     }
     MG_CUDA(cudaGetLastError());
     return MG_OK;

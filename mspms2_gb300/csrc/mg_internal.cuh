@@ -182,6 +182,8 @@ struct mg_ctx {
     long long kvectors = 0;
     std::vector<int> h_rows;  // [nrows][4]: kx, ky, kzmax, half_only
     DevBuf d_rows, d_row_slot, d_phase, d_spart, d_scoef, d_tasks;
+    std::vector<int> h_chunk_kz;  // kzmax of each chunk of the FP32 table force pass
+    DevBuf d_fcoef, d_fpart;      // its coefficients and partial forces
     int ntasks = 0, sblocks_atoms = 0;
     double ewald_box[3] = {0, 0, 0};
     // energies
