@@ -42,7 +42,12 @@
 #define EW_FROWS 32     // rows staged per step in the force pass
 #define EW_FG 4         // thread groups sharing the rows of a site in the force pass
 #define EW_FSITES 64    // sites per force block (EW_FG * EW_FSITES threads)
-#define EW_FCHUNK 16    // rows per chunk of the FP32 table force pass (accumulators per site)
+#ifndef EW_FCHUNK
+#define EW_FCHUNK 12    // rows per chunk of the FP32 table force pass (accumulators per site)
+#endif
+#ifndef EW_FMM_MINB
+#define EW_FMM_MINB 6   // resident blocks per SM the table force pass is compiled for
+#endif
 #define EW_FMM_TPB 128  // sites (threads) per block of the FP32 table force pass
 #define EW_FMM_MAXA 64  // largest kzmax + 1 the table force pass stages on chip
 #define EW_MAXSPLIT 16  // row-chunk ranges of the FP32 table force pass
@@ -97,12 +102,6 @@ __device__ __forceinline__ void up2(f32x2 v, float &lo, float &hi) {
 __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
     f32x2 d;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-
-__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
-    f32x2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
 
@@ -168,27 +167,44 @@ __host__ __device__ inline int ew_kzmax(int KZ, int rem) {
 // rows of each of the first pairs have the same KSQMAX - kx^2 - ky^2, hence the same
 // kzmax, and so do (j, 0) and (0, j): rows 2u and 2u+1 form the units of the packed
 // force pass, of equal length unless KMAXX != KMAXY leaves one of (j, 0), (0, j) out.
+// (host and device callers each pass their own callables)
+#pragma nv_exec_check_disable
+template <typename F>
+__host__ __device__ inline void ew_visit_row(int KZ, int KS, int kx, int ky, F &f) {
+    const int rem = KS - kx * kx - ky * ky;
+    if (rem < 0) return;
+    const int half = (kx == 0 && ky == 0) ? 1 : 0;
+    const int kzmax = ew_kzmax(KZ, rem);
+    if (half && kzmax < 1) return;
+    f(kx, ky, kzmax, half);
+}
+
+#pragma nv_exec_check_disable
 template <typename F>
 __host__ __device__ inline void ew_for_rows(int KX, int KY, int KZ, int KS, F f) {
-    auto visit = [&](int kx, int ky) {
-        const int rem = KS - kx * kx - ky * ky;
-        if (rem < 0) return;
-        const int half = (kx == 0 && ky == 0) ? 1 : 0;
-        const int kzmax = ew_kzmax(KZ, rem);
-        if (half && kzmax < 1) return;
-        f(kx, ky, kzmax, half);
-    };
     for (int kx = 1; kx <= KX; kx++)
         for (int ky = 1; ky <= KY; ky++) {
-            visit(kx, -ky);
-            visit(kx, ky);
+            ew_visit_row(KZ, KS, kx, -ky, f);
+            ew_visit_row(KZ, KS, kx, ky, f);
         }
     const int J = KX > KY ? KX : KY;
     for (int j = 1; j <= J; j++) {
-        if (j <= KX) visit(j, 0);
-        if (j <= KY) visit(0, j);
+        if (j <= KX) ew_visit_row(KZ, KS, j, 0, f);
+        if (j <= KY) ew_visit_row(KZ, KS, 0, j, f);
     }
-    visit(0, 0);
+    ew_visit_row(KZ, KS, 0, 0, f);
+}
+
+// Chunks of the S(k) pass for a row with nv |kz| values: the pairs (0, 1), (2, 3), ...
+// split into ceil(pairs / 4) balanced runs, so that chunk h starts at an even |kz| and
+// holds at most EW_CH |kz| values (k0, len).
+__host__ __device__ inline int ew_nchunk(int nv) { return ((nv + 1) / 2 + 3) / 4; }
+__host__ __device__ inline void ew_chunk(int nv, int h, int &k0, int &len) {
+    const int np = (nv + 1) / 2, nch = (np + 3) / 4;
+    const int p0 = h * (np / nch) + (h < np % nch ? h : np % nch);
+    const int pl = np / nch + (h < np % nch ? 1 : 0);
+    k0 = 2 * p0;
+    len = 2 * pl < nv - k0 ? 2 * pl : nv - k0;
 }
 
 struct EwArgs {
@@ -219,98 +235,12 @@ struct EwArgs {
     double *fpart;
 };
 
-// FP32 tile with packed f32x2 arithmetic: lanes are two consecutive |kz| (j, j+1). Their
-// phases start from the table (Z^kz0, Z^(kz0+1)) and advance by W = Z^2, also from the
-// table; per lane pair and site, 8 packed FMAs accumulate S(+kz) and S(-kz) of both
-// |kz| and 4 advance the phases. An odd last |kz| is done in scalar FMAs.
-template <int CH>
-__device__ __forceinline__ void sk_tile_f32x2(const float2 *sX, const float2 *sY, const float2 *sZ, const float *sQ,
-                                              int P, int tn, int kx, int aky, float ysign, int kz0,
-                                              float (&pP)[EW_CH][2], float (&pM)[EW_CH][2]) {
-    constexpr int NP = CH / 2;
-    constexpr bool ODD = (CH & 1) != 0;
-    f32x2 Pr[NP > 0 ? NP : 1], Pi[NP > 0 ? NP : 1], Mr[NP > 0 ? NP : 1], Mi[NP > 0 ? NP : 1];
-#pragma unroll
-    for (int h = 0; h < NP; h++) {
-        Pr[h] = pk2(pP[2 * h][0], pP[2 * h + 1][0]);
-        Pi[h] = pk2(pP[2 * h][1], pP[2 * h + 1][1]);
-        Mr[h] = pk2(pM[2 * h][0], pM[2 * h + 1][0]);
-        Mi[h] = pk2(pM[2 * h][1], pM[2 * h + 1][1]);
-    }
-    float tPr = ODD ? pP[CH - 1][0] : 0.f, tPi = ODD ? pP[CH - 1][1] : 0.f;
-    float tMr = ODD ? pM[CH - 1][0] : 0.f, tMi = ODD ? pM[CH - 1][1] : 0.f;
-    for (int s = 0; s < tn; s++) {
-        float2 X = sX[kx * P + s];
-        float2 Y = sY[aky * P + s];
-        Y.y *= ysign;
-        const float q = sQ[s];
-        float2 Aq = cmul(X, Y);
-        Aq.x *= q;
-        Aq.y *= q;
-        const float2 Z0 = sZ[kz0 * P + s];
-        float ztx = Z0.x, zty = Z0.y;  // phase of the odd last |kz|
-        if (NP > 0) {
-            const f32x2 AX = pk2(Aq.x, Aq.x), AY = pk2(Aq.y, Aq.y);
-            const f32x2 NAX = pk2(-Aq.x, -Aq.x), NAY = pk2(-Aq.y, -Aq.y);
-            const float2 Z1 = sZ[(kz0 + 1) * P + s];
-            f32x2 Zx = pk2(Z0.x, Z1.x), Zy = pk2(Z0.y, Z1.y);
-            f32x2 WX = 0, WY = 0, NWY = 0;
-            if (CH >= 3) {
-                const float2 W = sZ[2 * P + s];
-                WX = pk2(W.x, W.x);
-                WY = pk2(W.y, W.y);
-                NWY = pk2(-W.y, -W.y);
-            }
-#pragma unroll
-            for (int h = 0; h < NP; h++) {
-                Pr[h] = fma2(AX, Zx, fma2(NAY, Zy, Pr[h]));  // + Ax Zx - Ay Zy
-                Pi[h] = fma2(AX, Zy, fma2(AY, Zx, Pi[h]));   // + Ax Zy + Ay Zx
-                Mr[h] = fma2(AX, Zx, fma2(AY, Zy, Mr[h]));   // + Ax Zx + Ay Zy
-                Mi[h] = fma2(AY, Zx, fma2(NAX, Zy, Mi[h]));  // + Ay Zx - Ax Zy
-                if (h + 1 < NP || ODD) {                     // Z <- Z W
-                    const f32x2 nZx = fma2(Zx, WX, mul2(Zy, NWY));
-                    const f32x2 nZy = fma2(Zx, WY, mul2(Zy, WX));
-                    Zx = nZx;
-                    Zy = nZy;
-                }
-            }
-            if (ODD) {
-                float hi;
-                up2(Zx, ztx, hi);
-                up2(Zy, zty, hi);
-            }
-        }
-        if (ODD) {
-            tPr = fmaf(Aq.x, ztx, fmaf(-Aq.y, zty, tPr));
-            tPi = fmaf(Aq.x, zty, fmaf(Aq.y, ztx, tPi));
-            tMr = fmaf(Aq.x, ztx, fmaf(Aq.y, zty, tMr));
-            tMi = fmaf(Aq.y, ztx, fmaf(-Aq.x, zty, tMi));
-        }
-    }
-#pragma unroll
-    for (int h = 0; h < NP; h++) {
-        up2(Pr[h], pP[2 * h][0], pP[2 * h + 1][0]);
-        up2(Pi[h], pP[2 * h][1], pP[2 * h + 1][1]);
-        up2(Mr[h], pM[2 * h][0], pM[2 * h + 1][0]);
-        up2(Mi[h], pM[2 * h][1], pM[2 * h + 1][1]);
-    }
-    if (ODD) {
-        pP[CH - 1][0] = tPr;
-        pP[CH - 1][1] = tPi;
-        pM[CH - 1][0] = tMr;
-        pM[CH - 1][1] = tMi;
-    }
-}
-
-// One tile of sites for a thread owning CH consecutive |kz| of one row: straight-line
-// code, A*Z and A*conj(Z) sharing four products, Z advanced by the site's Z1. FP32 goes
-// to the packed form above.
+// One tile of sites for a thread owning CH consecutive |kz| of one row (FP64 path):
+// straight-line code, A*Z and A*conj(Z) sharing four products, Z advanced by the site's Z1.
 template <typename R, int CH, typename T2>
 __device__ __forceinline__ void sk_tile(const T2 *sX, const T2 *sY, const T2 *sZ, const R *sQ, int P, int tn,
                                         int kx, int aky, R ysign, int kz0, R (&pP)[EW_CH][2], R (&pM)[EW_CH][2]) {
-    if constexpr (std::is_same<R, float>::value) {
-        sk_tile_f32x2<CH>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM);
-    } else {
+    {
         for (int s = 0; s < tn; s++) {
             T2 X = sX[kx * P + s];
             T2 Y = sY[aky * P + s];
@@ -409,6 +339,144 @@ __global__ void __launch_bounds__(EW_TPB) k_sk(EwArgs A) {
         out[2 * sm] = has_minus ? pM[j][0] : (R)0;
         out[2 * sm + 1] = has_minus ? pM[j][1] : (R)0;
     }
+}
+
+// FP32 structure factors from the phase tables. A thread owns one task (row, |kz| from
+// an even k0, at most EW_CH values): per site, with Aq = q X^kx Y^ky and z = Z^|kz| from
+// the table, the four real sums RR = sum Ar zr, II = sum Ai zi, RI = sum Ar zi and
+// IR = sum Ai zr give S(+kz) = (RR - II, RI + IR) and S(-kz) = (RR + II, IR - RI): 4 FMAs
+// per site and |kz| for both signs. The lanes of the packed f32x2 sums are |kz| = k,
+// k + 1; the tile stages Z as [site][pair]{zr_k, zr_k+1, zi_k, zi_k+1} (zero past KMAXZ).
+template <int NP>
+__device__ __forceinline__ void sk2_tile(const ulonglong2 *sZ, const float2 *sX, const float2 *sY, const float *sQ,
+                                         int NPP, int P, int tn, int kx, int aky, float ysign, int p0,
+                                         f32x2 (&RR)[EW_CH / 2], f32x2 (&II)[EW_CH / 2], f32x2 (&RI)[EW_CH / 2],
+                                         f32x2 (&IR)[EW_CH / 2]) {
+    for (int s = 0; s < tn; s++) {
+        const float2 X = sX[kx * P + s];
+        float2 Y = sY[aky * P + s];
+        Y.y *= ysign;
+        const float q = sQ[s];
+        float2 Aq = cmul(X, Y);
+        Aq.x *= q;
+        Aq.y *= q;
+        const f32x2 AR = pk2(Aq.x, Aq.x), AI = pk2(Aq.y, Aq.y);
+        const ulonglong2 *z = sZ + s * NPP + p0;
+#pragma unroll
+        for (int h = 0; h < NP; h++) {
+            const ulonglong2 zz = z[h];  // (zr_k, zr_k+1), (zi_k, zi_k+1)
+            RR[h] = fma2(AR, zz.x, RR[h]);
+            II[h] = fma2(AI, zz.y, II[h]);
+            RI[h] = fma2(AR, zz.y, RI[h]);
+            IR[h] = fma2(AI, zz.x, IR[h]);
+        }
+    }
+}
+
+#ifndef EW_SK2_MINB
+#define EW_SK2_MINB 6  // resident blocks per SM the FP32 S(k) pass is compiled for
+#endif
+__global__ void __launch_bounds__(EW_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int P = EW_TILE + 1;      // padded tile pitch
+    const int NPP = (A.kz + 2) / 2;  // |kz| pairs staged per site
+    ulonglong2 *sZ = (ulonglong2 *)smem_raw;
+    float2 *sX = (float2 *)(sZ + (size_t)EW_TILE * NPP);
+    float2 *sY = sX + (size_t)(A.kx + 1) * P;
+    float *sQ = (float *)(sY + (size_t)(A.ky + 1) * P);
+    const float2 *tab = (const float2 *)A.tab;
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    const int task = blockIdx.x * EW_TPB + threadIdx.x;
+    int kx = 0, ky = 0, half = 0, kz0 = 0, cnt = 0, slot0 = 0;
+    if (task < A.ntasks) {
+        const int4 t = A.tasks[task];
+        const int4 r = A.rows[t.x];
+        kx = r.x;
+        ky = r.y;
+        half = r.w;
+        kz0 = t.y;
+        cnt = t.z;
+        slot0 = A.row_slot[t.x];
+    }
+    const int aky = ky < 0 ? -ky : ky;
+    const float ysign = ky < 0 ? -1.f : 1.f;
+    const int np = (cnt + 1) / 2, p0 = kz0 / 2;
+    f32x2 RR[EW_CH / 2], II[EW_CH / 2], RI[EW_CH / 2], IR[EW_CH / 2];
+#pragma unroll
+    for (int h = 0; h < EW_CH / 2; h++) RR[h] = II[h] = RI[h] = IR[h] = 0;
+    const int a_begin = blockIdx.y * EW_SITES, a_end = min(A.n, a_begin + EW_SITES);
+    for (int t0 = a_begin; t0 < a_end; t0 += EW_TILE) {
+        const int tn = min(EW_TILE, a_end - t0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < (A.kx + 1) * EW_TILE; i += EW_TPB) {
+            const int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) sX[k * P + s] = tX[(size_t)k * A.n + t0 + s];
+        }
+        for (int i = threadIdx.x; i < (A.ky + 1) * EW_TILE; i += EW_TPB) {
+            const int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) sY[k * P + s] = tY[(size_t)k * A.n + t0 + s];
+        }
+        for (int i = threadIdx.x; i < NPP * EW_TILE; i += EW_TPB) {
+            const int pp = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) {
+                const int k = 2 * pp;
+                const float2 z0 = tZ[(size_t)k * A.n + t0 + s];
+                const float2 z1 = k + 1 <= A.kz ? tZ[(size_t)(k + 1) * A.n + t0 + s] : make_float2(0.f, 0.f);
+                sZ[s * NPP + pp] = make_ulonglong2(pk2(z0.x, z1.x), pk2(z0.y, z1.y));
+            }
+        }
+        for (int s = threadIdx.x; s < tn; s += EW_TPB) sQ[s] = (float)A.q[t0 + s];
+        __syncthreads();
+        switch (np) {
+        case 4: sk2_tile<4>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
+        case 3: sk2_tile<3>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
+        case 2: sk2_tile<2>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
+        case 1: sk2_tile<1>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
+        default: break;
+        }
+    }
+    if (task >= A.ntasks || cnt == 0) return;
+    float *out = (float *)A.spart + (size_t)blockIdx.y * A.nslots * 2;
+#pragma unroll
+    for (int h = 0; h < EW_CH / 2; h++) {
+        if (h >= np) break;
+        float rr[2], ii[2], ri[2], ir[2];
+        up2(RR[h], rr[0], rr[1]);
+        up2(II[h], ii[0], ii[1]);
+        up2(RI[h], ri[0], ri[1]);
+        up2(IR[h], ir[0], ir[1]);
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            const int j = 2 * h + l;
+            if (j >= cnt) break;
+            const int a = kz0 + j;
+            const int sp = slot0 + 2 * a, sm = sp + 1;
+            out[2 * sp] = rr[l] - ii[l];
+            out[2 * sp + 1] = ri[l] + ir[l];
+            const bool has_minus = (a > 0) && !half;
+            out[2 * sm] = has_minus ? rr[l] + ii[l] : 0.f;
+            out[2 * sm + 1] = has_minus ? ir[l] - ri[l] : 0.f;
+        }
+    }
+}
+
+// the S(k) pass of one precision over nblk site blocks
+template <typename R>
+cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
+    const dim3 grid((unsigned)((A.ntasks + EW_TPB - 1) / EW_TPB), (unsigned)nblk);
+    const int P = EW_TILE + 1;
+    cudaError_t e;
+    if constexpr (std::is_same<R, float>::value) {
+        const size_t smem = sizeof(ulonglong2) * EW_TILE * (size_t)((A.kz + 2) / 2) +
+                            sizeof(float2) * (size_t)(A.kx + 1 + A.ky + 1) * P + sizeof(float) * EW_TILE;
+        e = cudaFuncSetAttribute(k_sk2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_sk2<<<grid, EW_TPB, smem, s>>>(A);
+    } else {
+        const size_t smem = sizeof(double2) * (size_t)(A.kx + 1 + A.ky + 1 + A.kz + 1) * P + sizeof(double) * EW_TILE;
+        e = cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
+    }
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 // S(k) from the partials in site-block order; energy rows and force coefficients
@@ -682,7 +750,7 @@ __global__ void k_fcoef(EwArgs A) {
     }
 }
 
-__global__ void __launch_bounds__(EW_FMM_TPB, 6) k_kforce_mm(EwArgs A, int maxa) {
+__global__ void __launch_bounds__(EW_FMM_TPB, EW_FMM_MINB) k_kforce_mm(EwArgs A, int maxa) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ulonglong2 *sK = (ulonglong2 *)smem_raw;                      // [maxa][EW_FCHUNK]
     float2 *sZ = (float2 *)(sK + (size_t)maxa * EW_FCHUNK);       // [maxa][EW_FMM_TPB]
@@ -943,12 +1011,11 @@ mg_status mg_ewald_setup(mg_ctx *c) {
         for (int s = 0; s < ns; s++) slot_row.push_back(r);
         nslots += ns;
         kvec += half ? kzmax : 2 * kzmax + 1;
-        int nv = kzmax + 1;
-        int nch = (nv + EW_CH - 1) / EW_CH;
-        for (int h = 0, k0 = 0; h < nch; h++) {  // balanced chunks
-            int len = nv / nch + (h < nv % nch ? 1 : 0);
+        const int nv = kzmax + 1;
+        for (int h = 0; h < ew_nchunk(nv); h++) {
+            int k0, len;
+            ew_chunk(nv, h, k0, len);
             tasks.push_back(make_int4(r, k0, len, 0));
-            k0 += len;
         }
     });
     std::stable_sort(tasks.begin(), tasks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
@@ -1048,17 +1115,10 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     A.coul = p.coulomb_prefactor;
     A.rows_e = (double *)c->d_epart.p;
     A.f = fl;
-    const int P = EW_TILE + 1;
-    size_t smem = esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
-    dim3 grid((c->ntasks + EW_TPB - 1) / EW_TPB, nblk);
-    if (fp64) {
-        MG_CUDA(cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
-    } else {
-        MG_CUDA(cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
-    }
-    MG_CUDA(cudaGetLastError());
+    if (fp64)
+        MG_CUDA(launch_sk<double>(A, nblk, s));
+    else
+        MG_CUDA(launch_sk<float>(A, nblk, s));
     const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
     unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
     A.row0 = mg_reserve_rows(c, rblocks);
@@ -1105,12 +1165,6 @@ struct EwStaticDevice {
 EwStaticDevice g_ew_static[EW_STATIC_MAX_DEVICES];
 std::mutex g_ew_static_mutex;
 
-// length of chunk h of a row with nv |kz| values (balanced chunks of at most EW_CH)
-__host__ __device__ inline int ew_chunk_len(int nv, int h) {
-    int nch = (nv + EW_CH - 1) / EW_CH;
-    return nv / nch + (h < nv % nch ? 1 : 0);
-}
-
 struct EwCounts {
     int nrows = 0, nslots = 0, ntasks = 0, maxa = 1;
     std::vector<int> chunk_kz;  // kzmax of each chunk of the FP32 table force pass
@@ -1126,8 +1180,11 @@ EwCounts ew_count(int KX, int KY, int KZ, int KS) {
         c.nrows++;
         c.nslots += 2 * nv;
         c.maxa = std::max(c.maxa, nv);
-        int nch = (nv + EW_CH - 1) / EW_CH;
-        for (int h = 0; h < nch; h++) by_len[ew_chunk_len(nv, h)]++;
+        for (int h = 0; h < ew_nchunk(nv); h++) {
+            int k0, len;
+            ew_chunk(nv, h, k0, len);
+            by_len[len]++;
+        }
     });
     for (int L = 1; L <= EW_CH; L++) c.ntasks += (by_len[L] + 31) / 32 * 32;
     c.chunk_kz = fmm_chunk_kz(hist, c.nrows);
@@ -1150,11 +1207,11 @@ __global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int nslot
         int t = 0;
         for (int L = EW_CH; L >= 1; L--) {
             for (int q = 0; q < nrows; q++) {
-                int nv = rows[q].z + 1, nch = (nv + EW_CH - 1) / EW_CH;
-                for (int h = 0, k0 = 0; h < nch; h++) {
-                    int len = ew_chunk_len(nv, h);
+                const int nv = rows[q].z + 1;
+                for (int h = 0; h < ew_nchunk(nv); h++) {
+                    int k0, len;
+                    ew_chunk(nv, h, k0, len);
                     if (len == L) tasks[t++] = make_int4(q, k0, len, 0);
-                    k0 += len;
                 }
             }
             while (t % 32) tasks[t++] = make_int4(0, 0, 0, 0);
@@ -1373,24 +1430,17 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
             if (A.fsplit > 1) A.fpart = (double *)(base + ew_align256(off));
         }
     }
-    const int P = EW_TILE + 1;
-    const size_t smem = esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
-    const dim3 grid((ct.ntasks + EW_TPB - 1) / EW_TPB, nblk);
     const int *slot_row = row_slot + ct.nrows;
     const size_t fsmem = 2 * esz * (size_t)EW_FROWS * ct.maxa;
     const unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
     if (fp64) {
-        EWS_CUDA(cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "cudaFuncSetAttribute");
-        k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
+        EWS_CUDA(launch_sk<double>(A, nblk, s), "k_sk launch");
         k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
         EWS_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem),
                  "cudaFuncSetAttribute");
         k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, ct.maxa);
     } else {
-        EWS_CUDA(cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "cudaFuncSetAttribute");
-        k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
+        EWS_CUDA(launch_sk<float>(A, nblk, s), "k_sk launch");
         k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
         EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
     }
@@ -1497,22 +1547,16 @@ EwArgs ew_args(mg_ctx *c) {
 mg_status mg_ewald_weighted_sk(mg_ctx *c, const double *w, double2 *out) {
     if (c->nrows == 0) return MG_OK;
     const bool fp64 = c->opt.precision == MG_PREC_FP64;
-    const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
     EwArgs A = ew_args(c);
     A.q = w;
     const int nblk = (A.n + EW_SITES - 1) / EW_SITES;
-    const int P = EW_TILE + 1;
-    const size_t smem = esz * (size_t)(A.kx + 1 + A.ky + 1 + A.kz + 1) * P + (fp64 ? sizeof(double) : sizeof(float)) * EW_TILE;
-    dim3 grid((A.ntasks + EW_TPB - 1) / EW_TPB, nblk);
     cudaStream_t s = c->stream;
     const unsigned sb = (unsigned)((A.nslots + 255) / 256);
     if (fp64) {
-        MG_CUDA(cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
+        MG_CUDA(launch_sk<double>(A, nblk, s));
         k_sk_sum<double><<<sb, 256, 0, s>>>(A, nblk, out);
     } else {
-        MG_CUDA(cudaFuncSetAttribute(k_sk<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_sk<float><<<grid, EW_TPB, smem, s>>>(A);
+        MG_CUDA(launch_sk<float>(A, nblk, s));
         k_sk_sum<float><<<sb, 256, 0, s>>>(A, nblk, out);
     }
     MG_CUDA(cudaGetLastError());
