@@ -45,6 +45,9 @@
 #ifndef EW_FCHUNK
 #define EW_FCHUNK 12    // rows per chunk of the FP32 table force pass (accumulators per site)
 #endif
+#ifndef EW_SK2_MINB
+#define EW_SK2_MINB 3   // resident blocks per SM the FP32 S(k) pass is compiled for
+#endif
 #ifndef EW_FMM_MINB
 #define EW_FMM_MINB 6   // resident blocks per SM the table force pass is compiled for
 #endif
@@ -105,7 +108,24 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
     return d;
 }
 
-// phase tables tab[d][n][site] = e^{2 pi i n u_d}
+// FP32 phase tables: X [KMAXX + 1][n] and Y [KMAXY + 1][n] as float2 e^{2 pi i k u}, then,
+// from the first 16-byte boundary, Z as |kz| pairs [(KMAXZ + 2) / 2][n] of
+// {zr_2p, zr_2p+1, zi_2p, zi_2p+1} (zero past KMAXZ), so that one 16-byte load gives a
+// site's two |kz| in the lanes of the packed f32x2 sums.
+__host__ __device__ inline int ew_zpairs(int KZ) { return (KZ + 2) / 2; }
+__host__ __device__ inline size_t ew_zoff(int KX, int KY, int n) { return ((size_t)(KX + 1 + KY + 1) * n + 1) & ~(size_t)1; }
+__host__ __device__ inline size_t ew_tabf_entries(int KX, int KY, int KZ, int n) {
+    return ew_zoff(KX, KY, n) + (size_t)2 * ew_zpairs(KZ) * n;  // float2 units
+}
+
+__device__ __forceinline__ float2 ew_phase_f(unsigned U, int k) {
+    const unsigned V = U * (unsigned)k;
+    const float v = (float)(int)V * 4.656612873077393e-10f;  // 2^-31
+    float s, c;
+    sincospif(v, &s, &c);
+    return make_float2(c, s);
+}
+
 __global__ void k_phase_f(int n, const double *__restrict__ x, const double *__restrict__ y,
                           const double *__restrict__ z, double sx, double sy, double sz, int kx, int ky, int kz,
                           float2 *__restrict__ tab) {
@@ -113,22 +133,34 @@ __global__ void k_phase_f(int n, const double *__restrict__ x, const double *__r
     if (a >= n) return;
     const double pos[3] = {x[a], y[a], z[a]};
     const double sc[3] = {sx, sy, sz};
-    const int km[3] = {kx, ky, kz};
-    size_t off = 0;
+    unsigned U[3];
     for (int d = 0; d < 3; d++) {
         double t = pos[d] * sc[d];
         t = t - floor(t);
-        double tu = t * 4294967296.0;
-        unsigned U = tu >= 4294967295.0 ? 0xffffffffu : (unsigned)tu;
-        for (int k = 0; k <= km[d]; k++) {
-            unsigned V = U * (unsigned)k;
-            float v = (float)(int)V * 4.656612873077393e-10f;  // 2^-31
-            float s, c;
-            sincospif(v, &s, &c);
-            tab[off + (size_t)k * n + a] = make_float2(c, s);
-        }
-        off += (size_t)(km[d] + 1) * n;
+        const double tu = t * 4294967296.0;
+        U[d] = tu >= 4294967295.0 ? 0xffffffffu : (unsigned)tu;
     }
+    for (int k = 0; k <= kx; k++) tab[(size_t)k * n + a] = ew_phase_f(U[0], k);
+    for (int k = 0; k <= ky; k++) tab[(size_t)(kx + 1 + k) * n + a] = ew_phase_f(U[1], k);
+    float4 *zp = (float4 *)(tab + ew_zoff(kx, ky, n));
+    for (int p = 0; p < ew_zpairs(kz); p++) {
+        const float2 z0 = ew_phase_f(U[2], 2 * p);
+        const float2 z1 = 2 * p + 1 <= kz ? ew_phase_f(U[2], 2 * p + 1) : make_float2(0.f, 0.f);
+        zp[(size_t)p * n + a] = make_float4(z0.x, z1.x, z0.y, z1.y);
+    }
+}
+
+// Z^1 of site a from either precision's tables
+template <typename R>
+__device__ inline typename C2<R>::T ew_z1(const void *tab, int kx, int ky, int n, int a);
+template <>
+__device__ inline float2 ew_z1<float>(const void *tab, int kx, int ky, int n, int a) {
+    const float4 v = ((const float4 *)((const float2 *)tab + ew_zoff(kx, ky, n)))[a];
+    return make_float2(v.y, v.w);
+}
+template <>
+__device__ inline double2 ew_z1<double>(const void *tab, int kx, int ky, int n, int a) {
+    return ((const double2 *)tab)[(size_t)(kx + 1 + ky + 1 + 1) * n + a];
 }
 
 __global__ void k_phase_d(int n, const double *__restrict__ x, const double *__restrict__ y,
@@ -215,6 +247,7 @@ struct EwArgs {
     const int4 *tasks;      // row, first |kz|, count, -
     const void *tab;
     const double *q;
+    float *qf;              // [n] FP32 copy of q for the FP32 S(k) pass
     void *spart;            // [site blocks][nslots][2] R
     void *scoef;            // [nslots] R2: plus slots conj(c S), minus slots c S
     double twopi[3];
@@ -373,20 +406,43 @@ __device__ __forceinline__ void sk2_tile(const ulonglong2 *sZ, const float2 *sX,
     }
 }
 
-#ifndef EW_SK2_MINB
-#define EW_SK2_MINB 6  // resident blocks per SM the FP32 S(k) pass is compiled for
-#endif
-__global__ void __launch_bounds__(EW_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
+__device__ __forceinline__ void cp_async(void *dst, const void *src, int bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (bytes == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    else if (bytes == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+#define EW_SK_TPB 256  // tasks (threads) per block of the FP32 S(k) pass
+
+// bytes of one staged tile of the FP32 S(k) pass (Z pairs, X, Y, q), a multiple of 16
+__host__ __device__ inline size_t ew_sk2_stage(int KX, int KY, int KZ) {
+    const size_t b = 16 * (size_t)EW_TILE * ew_zpairs(KZ) + 8 * (size_t)(KX + 1 + KY + 1) * (EW_TILE + 1) + 4 * EW_TILE;
+    return (b + 15) & ~(size_t)15;
+}
+
+__global__ void k_qcast(int n, const double *__restrict__ q, float *__restrict__ qf) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) qf[a] = (float)q[a];
+}
+
+// The tiles of EW_TILE sites are copied into shared memory with cp.async, two stages:
+// the copy of tile t + 1 runs while tile t is summed.
+__global__ void __launch_bounds__(EW_SK_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int P = EW_TILE + 1;      // padded tile pitch
-    const int NPP = (A.kz + 2) / 2;  // |kz| pairs staged per site
-    ulonglong2 *sZ = (ulonglong2 *)smem_raw;
-    float2 *sX = (float2 *)(sZ + (size_t)EW_TILE * NPP);
-    float2 *sY = sX + (size_t)(A.kx + 1) * P;
-    float *sQ = (float *)(sY + (size_t)(A.ky + 1) * P);
+    const int P = EW_TILE + 1;            // padded tile pitch of X and Y
+    const int NPP = ew_zpairs(A.kz);      // |kz| pairs per site
+    const size_t stage = ew_sk2_stage(A.kx, A.ky, A.kz);
     const float2 *tab = (const float2 *)A.tab;
-    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
-    const int task = blockIdx.x * EW_TPB + threadIdx.x;
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
+    const ulonglong2 *tZP = (const ulonglong2 *)(tab + ew_zoff(A.kx, A.ky, A.n));
+    const int task = blockIdx.x * EW_SK_TPB + threadIdx.x;
     int kx = 0, ky = 0, half = 0, kz0 = 0, cnt = 0, slot0 = 0;
     if (task < A.ntasks) {
         const int4 t = A.tasks[task];
@@ -405,28 +461,44 @@ __global__ void __launch_bounds__(EW_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
 #pragma unroll
     for (int h = 0; h < EW_CH / 2; h++) RR[h] = II[h] = RI[h] = IR[h] = 0;
     const int a_begin = blockIdx.y * EW_SITES, a_end = min(A.n, a_begin + EW_SITES);
-    for (int t0 = a_begin; t0 < a_end; t0 += EW_TILE) {
+    const int ntile = (a_end - a_begin + EW_TILE - 1) / EW_TILE;
+    auto copy_tile = [&](int b, int t0) {
+        unsigned char *base = smem_raw + b * stage;
+        ulonglong2 *sZ = (ulonglong2 *)base;
+        float2 *sX = (float2 *)(sZ + (size_t)EW_TILE * NPP);
+        float2 *sY = sX + (size_t)(A.kx + 1) * P;
+        float *sQ = (float *)(sY + (size_t)(A.ky + 1) * P);
         const int tn = min(EW_TILE, a_end - t0);
-        __syncthreads();
-        for (int i = threadIdx.x; i < (A.kx + 1) * EW_TILE; i += EW_TPB) {
-            const int k = i / EW_TILE, s = i % EW_TILE;
-            if (s < tn) sX[k * P + s] = tX[(size_t)k * A.n + t0 + s];
-        }
-        for (int i = threadIdx.x; i < (A.ky + 1) * EW_TILE; i += EW_TPB) {
-            const int k = i / EW_TILE, s = i % EW_TILE;
-            if (s < tn) sY[k * P + s] = tY[(size_t)k * A.n + t0 + s];
-        }
-        for (int i = threadIdx.x; i < NPP * EW_TILE; i += EW_TPB) {
+        for (int i = threadIdx.x; i < NPP * EW_TILE; i += EW_SK_TPB) {
             const int pp = i / EW_TILE, s = i % EW_TILE;
-            if (s < tn) {
-                const int k = 2 * pp;
-                const float2 z0 = tZ[(size_t)k * A.n + t0 + s];
-                const float2 z1 = k + 1 <= A.kz ? tZ[(size_t)(k + 1) * A.n + t0 + s] : make_float2(0.f, 0.f);
-                sZ[s * NPP + pp] = make_ulonglong2(pk2(z0.x, z1.x), pk2(z0.y, z1.y));
-            }
+            if (s < tn) cp_async(&sZ[s * NPP + pp], &tZP[(size_t)pp * A.n + t0 + s], 16);
         }
-        for (int s = threadIdx.x; s < tn; s += EW_TPB) sQ[s] = (float)A.q[t0 + s];
+        for (int i = threadIdx.x; i < (A.kx + 1) * EW_TILE; i += EW_SK_TPB) {
+            const int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) cp_async(&sX[k * P + s], &tX[(size_t)k * A.n + t0 + s], 8);
+        }
+        for (int i = threadIdx.x; i < (A.ky + 1) * EW_TILE; i += EW_SK_TPB) {
+            const int k = i / EW_TILE, s = i % EW_TILE;
+            if (s < tn) cp_async(&sY[k * P + s], &tY[(size_t)k * A.n + t0 + s], 8);
+        }
+        if (threadIdx.x < tn) cp_async(&sQ[threadIdx.x], &A.qf[t0 + threadIdx.x], 4);
+        cp_async_commit();
+    };
+    if (ntile > 0) copy_tile(0, a_begin);
+    for (int t = 0; t < ntile; t++) {
+        const int t0 = a_begin + t * EW_TILE, tn = min(EW_TILE, a_end - t0);
+        if (t + 1 < ntile) {
+            copy_tile((t + 1) & 1, t0 + EW_TILE);  // its buffer was last read before the barrier below
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
         __syncthreads();
+        const unsigned char *base = smem_raw + (t & 1) * stage;
+        const ulonglong2 *sZ = (const ulonglong2 *)base;
+        const float2 *sX = (const float2 *)(sZ + (size_t)EW_TILE * NPP);
+        const float2 *sY = sX + (size_t)(A.kx + 1) * P;
+        const float *sQ = (const float *)(sY + (size_t)(A.ky + 1) * P);
         switch (np) {
         case 4: sk2_tile<4>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
         case 3: sk2_tile<3>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
@@ -434,6 +506,7 @@ __global__ void __launch_bounds__(EW_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
         case 1: sk2_tile<1>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
         default: break;
         }
+        __syncthreads();
     }
     if (task >= A.ntasks || cnt == 0) return;
     float *out = (float *)A.spart + (size_t)blockIdx.y * A.nslots * 2;
@@ -463,15 +536,17 @@ __global__ void __launch_bounds__(EW_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
 // the S(k) pass of one precision over nblk site blocks
 template <typename R>
 cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
-    const dim3 grid((unsigned)((A.ntasks + EW_TPB - 1) / EW_TPB), (unsigned)nblk);
-    const int P = EW_TILE + 1;
     cudaError_t e;
     if constexpr (std::is_same<R, float>::value) {
-        const size_t smem = sizeof(ulonglong2) * EW_TILE * (size_t)((A.kz + 2) / 2) +
-                            sizeof(float2) * (size_t)(A.kx + 1 + A.ky + 1) * P + sizeof(float) * EW_TILE;
+        if (A.n == 0) return cudaSuccess;
+        k_qcast<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.q, A.qf);
+        const dim3 grid((unsigned)((A.ntasks + EW_SK_TPB - 1) / EW_SK_TPB), (unsigned)nblk);
+        const size_t smem = 2 * ew_sk2_stage(A.kx, A.ky, A.kz);
         e = cudaFuncSetAttribute(k_sk2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) k_sk2<<<grid, EW_TPB, smem, s>>>(A);
+        if (e == cudaSuccess) k_sk2<<<grid, EW_SK_TPB, smem, s>>>(A);
     } else {
+        const dim3 grid((unsigned)((A.ntasks + EW_TPB - 1) / EW_TPB), (unsigned)nblk);
+        const int P = EW_TILE + 1;
         const size_t smem = sizeof(double2) * (size_t)(A.kx + 1 + A.ky + 1 + A.kz + 1) * P + sizeof(double) * EW_TILE;
         e = cudaFuncSetAttribute(k_sk<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) k_sk<double><<<grid, EW_TPB, smem, s>>>(A);
@@ -528,10 +603,10 @@ __global__ void __launch_bounds__(FG * EW_FSITES) k_kforce(EwArgs A, int maxa) {
     const int a = blockIdx.x * EW_FSITES + l;
     const bool act = a < A.n;
     const T2 *tab = (const T2 *)A.tab;
-    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
     T2 Z;
     if (act) {
-        Z = tZ[(size_t)1 * A.n + a];
+        Z = ew_z1<R>(A.tab, A.kx, A.ky, A.n, a);
     } else {
         Z.x = (R)1;
         Z.y = (R)0;
@@ -623,8 +698,8 @@ __global__ void __launch_bounds__(FG * EW_FSITES, 16 / FG) k_kforce_f2(EwArgs A,
     const int a = blockIdx.x * EW_FSITES + l;
     const bool act = a < A.n;
     const float2 *tab = (const float2 *)A.tab;
-    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
-    const float2 Z = act ? tZ[(size_t)1 * A.n + a] : make_float2(1.f, 0.f);
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
+    const float2 Z = act ? ew_z1<float>(A.tab, A.kx, A.ky, A.n, a) : make_float2(1.f, 0.f);
     const f32x2 ZX = pk2(Z.x, Z.x), ZY = pk2(Z.y, Z.y), NZY = pk2(-Z.y, -Z.y);
     float Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};  // per-chunk sums accumulated as hi + lo
     const float4 *coef = (const float4 *)A.scoef;
@@ -759,8 +834,13 @@ __global__ void __launch_bounds__(EW_FMM_TPB, EW_FMM_MINB) k_kforce_mm(EwArgs A,
     const bool act = a_site < A.n;
     const int site = act ? a_site : A.n - 1;  // idle threads read a valid site, store nothing
     const float2 *tab = (const float2 *)A.tab;
-    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
-    for (int k = 0; k < maxa; k++) sZ[k * EW_FMM_TPB + threadIdx.x] = tZ[(size_t)k * A.n + site];
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
+    const float4 *tZP = (const float4 *)(tab + ew_zoff(A.kx, A.ky, A.n));
+    for (int pp = 0; 2 * pp < maxa; pp++) {
+        const float4 v = tZP[(size_t)pp * A.n + site];
+        sZ[2 * pp * EW_FMM_TPB + threadIdx.x] = make_float2(v.x, v.z);
+        if (2 * pp + 1 < maxa) sZ[(2 * pp + 1) * EW_FMM_TPB + threadIdx.x] = make_float2(v.y, v.w);
+    }
     float Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};  // per-chunk sums accumulated as hi + lo
     const int c_lo = A.csplit[blockIdx.y], c_hi = A.csplit[blockIdx.y + 1];
     for (int c = c_lo; c < c_hi; c++) {
@@ -1079,9 +1159,9 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     const bool fp64 = c->opt.precision == MG_PREC_FP64;
     const size_t esz = fp64 ? sizeof(double2) : sizeof(float2);
     const int KX = c->kmaxx, KY = c->kmaxy, KZ = std::max(c->kmaxz, 1);
-    const size_t tab_entries = (size_t)(KX + 1 + KY + 1 + KZ + 1) * n;
+    const size_t tab_entries = fp64 ? (size_t)(KX + 1 + KY + 1 + KZ + 1) * n : ew_tabf_entries(KX, KY, KZ, n);
     const int nblk = (n + EW_SITES - 1) / EW_SITES;
-    if (!mg_ensure(c, c->d_phase, esz * tab_entries) ||
+    if ((!fp64 && !mg_ensure(c, c->d_qf, sizeof(float) * (size_t)n)) || !mg_ensure(c, c->d_phase, esz * tab_entries) ||
         !mg_ensure(c, c->d_spart, (esz / 2) * 2 * (size_t)c->nslots * nblk) ||
         !mg_ensure(c, c->d_scoef, esz * (size_t)c->nslots))
         return MG_ERR_ALLOC;
@@ -1105,6 +1185,7 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     A.tasks = (const int4 *)c->d_tasks.p;
     A.tab = c->d_phase.p;
     A.q = (const double *)c->d_site_q.p;
+    A.qf = (float *)c->d_qf.p;
     A.spart = c->d_spart.p;
     A.scoef = c->d_scoef.p;
     A.twopi[0] = p.twopi_lx;
@@ -1354,7 +1435,9 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     const size_t o_tasks = off;
     off += ew_align256(sizeof(int4) * (size_t)ct.ntasks);
     const size_t o_tab = off;
-    off += ew_align256(esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * n);
+    off += ew_align256(fp64 ? esz * (size_t)(KX + 1 + KY + 1 + KZ + 1) * n : esz * ew_tabf_entries(KX, KY, KZ, n));
+    const size_t o_qf = off;
+    if (!fp64) off += ew_align256(sizeof(float) * (size_t)n);
     const size_t o_spart = off;
     off += ew_align256((esz / 2) * 2 * (size_t)ct.nslots * nblk);
     const size_t o_coef = off;
@@ -1401,6 +1484,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     A.tasks = tasks;
     A.tab = tab;
     A.q = d_q;
+    A.qf = (float *)(base + o_qf);
     A.spart = base + o_spart;
     A.scoef = base + o_coef;
     A.twopi[0] = p->twopi_lx;
@@ -1524,6 +1608,7 @@ EwArgs ew_args(mg_ctx *c) {
     A.tasks = (const int4 *)c->d_tasks.p;
     A.tab = c->d_phase.p;
     A.q = (const double *)c->d_site_q.p;
+    A.qf = (float *)c->d_qf.p;
     A.spart = c->d_spart.p;
     A.scoef = c->d_scoef.p;
     A.twopi[0] = p.twopi_lx;
@@ -1624,10 +1709,10 @@ __global__ void __launch_bounds__(EW_FG * EW_FSITES) k_khess(EwArgs A, int maxa,
     const int a = blockIdx.x * EW_FSITES + l;
     const bool act = a < A.n;
     const T2 *tab = (const T2 *)A.tab;
-    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n, *tZ = tY + (size_t)(A.ky + 1) * A.n;
+    const T2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
     T2 Z;
     if (act) {
-        Z = tZ[(size_t)1 * A.n + a];
+        Z = ew_z1<R>(A.tab, A.kx, A.ky, A.n, a);
     } else {
         Z.x = (R)1;
         Z.y = (R)0;

@@ -130,7 +130,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
                       &c->d_adj_class, &c->d_adj, &c->d_adj_g,
                       &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift,
-                      &c->d_md_glog};
+                      &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_qf};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
     for (auto &b : c->myinterp_buf) mg_free(b);

@@ -184,6 +184,7 @@ struct mg_ctx {
     DevBuf d_rows, d_row_slot, d_phase, d_spart, d_scoef, d_tasks;
     std::vector<int> h_chunk_kz;  // kzmax of each chunk of the FP32 table force pass
     DevBuf d_fcoef, d_fpart;      // its coefficients and partial forces
+    DevBuf d_qf;                  // FP32 copy of the S(k) site weights
     int ntasks = 0, sblocks_atoms = 0;
     double ewald_box[3] = {0, 0, 0};
     // energies
