@@ -45,8 +45,33 @@ SM_COUNT_NOMINAL = 152
 FP32_LANES_PER_SM = 128
 # algorithmic work per unit (fixed constants of the work model; FP32 FLOP)
 FLOP_PAIR = 55.0        # LJ + Ewald-real pair, counted once
-FLOP_K_S = 10.0         # per (half-space k-vector, site) in the S(k) pass
-FLOP_K_F = 12.0         # per (half-space k-vector, site) in the force pass
+# Reciprocal space, FP32 table passes, per site: S(k) 4 FMAs per (row, |kz|) for both signs
+# of kz plus q X^kx Y^ky per row; forces 8 FMAs per (row, |kz|) plus the per-row epilogue
+# (A = X^kx Y^ky, gsum, gz and the force sums)
+FLOP_SK_ROWKZ, FLOP_SK_ROW = 8.0, 8.0
+FLOP_KF_ROWKZ, FLOP_KF_ROW = 16.0, 18.0
+
+
+def ewald_rows(kmax, ksqmax):
+    """Rows (kx, ky) of the half-space k-vector set and the sum over rows of kzmax + 1
+    (the |kz| values a row holds), as the engine enumerates them."""
+    kx_max, ky_max, kz_max = kmax
+    nrows = nkz = 0
+    for kx in range(kx_max + 1):
+        for ky in range(-ky_max, ky_max + 1):
+            if kx == 0 and ky < 0:
+                continue
+            rem = ksqmax - kx * kx - ky * ky
+            if rem < 0:
+                continue
+            m = 0
+            while m + 1 <= kz_max and (m + 1) ** 2 <= rem:
+                m += 1
+            if kx == 0 and ky == 0 and m < 1:
+                continue
+            nrows += 1
+            nkz += m + 1
+    return nrows, nkz
 
 
 def parse():
@@ -722,15 +747,17 @@ def run_ours(args, rank, world, local_rank):
 
     # roofline of the dominant stage (FP32 pipe: no stage is a dense contraction)
     kvec = st["kvectors"]
-    stages = {"pair": (kms[1], FLOP_PAIR * npairs), "kspace_sk": (kms[3], FLOP_K_S * kvec * n),
-              "kspace_force": (kms[4], FLOP_K_F * kvec * n)}
+    nrows, nkz = ewald_rows(tuple(system.kmax), system.ksqmax) if kvec else (0, 0)
+    stages = {"pair": (kms[1], FLOP_PAIR * npairs),
+              "kspace_sk": (kms[3], (FLOP_SK_ROWKZ * nkz + FLOP_SK_ROW * nrows) * n),
+              "kspace_force": (kms[4], (FLOP_KF_ROWKZ * nkz + FLOP_KF_ROW * nrows) * n)}
     dom = max(stages, key=lambda k: stages[k][0])
     t_ms, flops = stages[dom]
     peak = SM_COUNT_NOMINAL * FP32_LANES_PER_SM * 2 * 2.07e9 / 1e12
     achieved = flops / (t_ms * 1e-3) / 1e12 if t_ms > 0 else 0.0
     # DRAM bytes per launch of that kernel from the committed ncu summary of this workload
     traffic = None
-    kernel_of = {"pair": "k_pair", "kspace_sk": "k_sk", "kspace_force": "k_kforce"}
+    kernel_of = {"pair": "k_pair", "kspace_sk": "k_sk2", "kspace_force": "k_kforce_mm"}
     tf = os.path.join(ROOT, "profiles", f"kernels_{args.workload}.md")
     if os.path.exists(tf):
         for ln in open(tf):
@@ -745,7 +772,8 @@ def run_ours(args, rank, world, local_rank):
             if args.precision == "mixed" else "f64", "data": "synthetic (seeded lattice water)",
             "config": {"workload": args.workload, "sites": n, "molecules": system.nmole, "box_A": float(system.box[0]),
                        "rc_A": system.rcutoff, "ewald_alpha": system.kappa, "kmax": list(system.kmax),
-                       "ksqmax": system.ksqmax, "kvectors_half_space": kvec, "pairs_in_cutoff": npairs,
+                       "ksqmax": system.ksqmax, "kvectors_half_space": kvec, "kspace_rows": nrows,
+                       "kspace_row_kz": nkz, "pairs_in_cutoff": npairs,
                        "l2": "256 MiB flush before every step; steps timed one by one with CUDA events",
                        "parallelism": f"replicas x{world}",
                        "tuning": {k: tuning[k] for k in ("cell_scale", "zcap_scale", "kforce_threads", "ms_default",

@@ -1152,6 +1152,11 @@ mg_status mg_ewald_setup(mg_ctx *c) {
     return MG_OK;
 }
 
+bool mg_ewald_horner_force(const mg_ctx *c) {
+    const int maxa = c->h_chunk_kz.empty() ? 1 : c->h_chunk_kz[0] + 1;
+    return c->opt.precision == MG_PREC_FP64 || maxa > EW_FMM_MAXA;
+}
+
 mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const double *dz, double *fl) {
     if (c->nrows == 0) return MG_OK;
     const mg_params &p = c->params;

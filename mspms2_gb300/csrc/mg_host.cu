@@ -847,7 +847,9 @@ extern "C" mg_status mg_autotune(mg_ctx *c, const double *x, const double *y, co
     mg_status st = timed(&base);
     MgTuning best = c->tune;
     float best_ms = base;
-    if (!st && c->params.charge_type == MG_ELEC_EWALD && (terms & MG_TERMS_LONG)) {
+    // threads per site matter only to the Horner k-force pass (FP64, or rows too long for
+    // the FP32 table pass)
+    if (!st && c->params.charge_type == MG_ELEC_EWALD && (terms & MG_TERMS_LONG) && mg_ewald_horner_force(c)) {
         for (int fg : {2, 8}) {
             c->tune = best;
             c->tune.kforce_threads = fg;

@@ -208,6 +208,7 @@ struct mg_ctx {
 
 // ---- helpers shared by host translation units --------------------------------------
 mg_status mg_fail(mg_ctx *c, mg_status code, const std::string &msg);
+bool mg_ewald_horner_force(const mg_ctx *c);  // k-space forces by the Horner pass (threads per site apply)
 mg_status mg_cuda_fail(mg_ctx *c, cudaError_t e, const char *what);
 bool mg_ensure(mg_ctx *c, DevBuf &b, size_t bytes);
 // forces of the given terms at device positions into the context's [3][n] blocks fl/fs,

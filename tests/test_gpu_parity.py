@@ -188,7 +188,8 @@ def test_autotune_picks_a_valid_faster_geometry():
     with Engine(s, precision="mixed") as eng:
         t = eng.autotune()
         assert t["kforce_threads"] in (2, 4, 8) and 0.5 <= t["cell_scale"] <= 2 and 0.5 <= t["zcap_scale"] <= 2
-        assert t["configs_tried"] == 11 and 0 < t["ms_tuned"] <= t["ms_default"]
+        # the FP32 table k-force pass has no threads-per-site choice: the 9 list geometries
+        assert t["configs_tried"] == 9 and 0 < t["ms_tuned"] <= t["ms_default"]
         fl, fs, e = eng.compute()
         assert rel(fl, d["ref_fl"]) <= TOL["mixed"]
         from mspms2_gb300.engine import EngineError
@@ -212,3 +213,19 @@ def test_inner_sublist_under_skin_reuse():
         _, fs_b, e_b = b.compute(x1, y1, z1, terms=TERMS_SHORT)
     assert rel(fs_a, fs_b) <= 1e-12, rel(fs_a, fs_b)
     assert abs(e_a["uinter"] - e_b["uinter"]) <= 1e-10 * abs(e_b["uinter"])
+
+
+def test_long_kz_rows_take_the_horner_pass():
+    """Rows of more than 64 |kz| values do not fit the FP32 table force pass's on-chip
+    staging; their forces come from the packed Horner pass, which must agree with the FP64
+    path like the table pass does (KMAXZ 70 against KMAX 3 in x and y)."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.system import ELEC_EWALD
+    s = configs.water_box(4, 12.4, 11, ELEC_EWALD, 0.3, 6.0, kmax=3, ksqmax=4900)
+    s.kmax = (3, 3, 70)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with Engine(s, precision=prec) as eng:
+            out[prec] = eng.compute(terms=TERMS_LONG)
+    assert rel(out["mixed"][0], out["fp64"][0]) <= TOL["mixed"], rel(out["mixed"][0], out["fp64"][0])
+    assert abs(out["mixed"][2]["ufourier"] - out["fp64"][2]["ufourier"]) <= 1e-5 * abs(out["fp64"][2]["ufourier"])
