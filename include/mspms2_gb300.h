@@ -425,6 +425,12 @@ MG_API mg_status mg_checkpoint_apply(mg_ctx *ctx, const mg_checkpoint *ck);
 MG_API mg_status mg_set_md_graphs(mg_ctx *ctx, int enable);
 MG_API mg_status mg_get_md_graphs(const mg_ctx *ctx, int *enabled, int *last_steps);
 
+/* Reciprocal-space overlap: with Ewald, the phase tables, S(k) and k-space force passes of
+ * an evaluation run on a second stream of the context, beside the neighbour list and pair
+ * kernels, and are joined (forces added, energy rows copied) where the serial order adds
+ * them, so that results are identical either way. Enabled by default. */
+MG_API mg_status mg_set_kspace_overlap(mg_ctx *ctx, int enable);
+
 /* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
 /* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
  * first stage whose T is below t_min (the reference tests T < t_min after the stage). A

@@ -108,6 +108,13 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
     return d;
 }
 
+// f += q t (2 pi / L) with each operation rounded on its own (no contraction into an
+// FMA), so that adding the same increment later, from a separate buffer, gives the same
+// bits as adding it here
+__device__ __forceinline__ void ew_addf(double *f, double q, double t, double tw) {
+    *f = __dadd_rn(*f, __dmul_rn(__dmul_rn(q, t), tw));
+}
+
 // FP32 phase tables: X [KMAXX + 1][n] and Y [KMAXY + 1][n] as float2 e^{2 pi i k u}, then,
 // from the first 16-byte boundary, Z as |kz| pairs [(KMAXZ + 2) / 2][n] of
 // {zr_2p, zr_2p+1, zi_2p, zi_2p+1} (zero past KMAXZ), so that one 16-byte load gives a
@@ -673,9 +680,9 @@ __global__ void __launch_bounds__(FG * EW_FSITES) k_kforce(EwArgs A, int maxa) {
         fzs += sF[k][2][l];
     }
     const double q = A.q[a];
-    A.f[a] += q * fxs * A.twopi[0];
-    A.f[A.n + a] += q * fys * A.twopi[1];
-    A.f[2 * A.n + a] += q * fzs * A.twopi[2];
+    ew_addf(&A.f[a], q, fxs, A.twopi[0]);
+    ew_addf(&A.f[A.n + a], q, fys, A.twopi[1]);
+    ew_addf(&A.f[2 * A.n + a], q, fzs, A.twopi[2]);
 }
 
 // FP32 force pass on units of two rows (rows 2u and 2u+1 of the table order), one row
@@ -789,9 +796,9 @@ __global__ void __launch_bounds__(FG * EW_FSITES, 16 / FG) k_kforce_f2(EwArgs A,
         fzs += sF[k][2][l];
     }
     const double q = A.q[a];
-    A.f[a] += q * fxs * A.twopi[0];
-    A.f[A.n + a] += q * fys * A.twopi[1];
-    A.f[2 * A.n + a] += q * fzs * A.twopi[2];
+    ew_addf(&A.f[a], q, fxs, A.twopi[0]);
+    ew_addf(&A.f[A.n + a], q, fys, A.twopi[1]);
+    ew_addf(&A.f[2 * A.n + a], q, fzs, A.twopi[2]);
 }
 
 // FP32 force pass from the phase tables. For one site and one row, with z_a = Z^a from
@@ -903,7 +910,7 @@ __global__ void __launch_bounds__(EW_FMM_TPB, EW_FMM_MINB) k_kforce_mm(EwArgs A,
     if (!act) return;
     if (A.fsplit == 1) {
         const double q = A.q[a_site];
-        for (int d = 0; d < 3; d++) A.f[(size_t)d * A.n + a_site] += q * ((double)Fh[d] + (double)Fl[d]) * A.twopi[d];
+        for (int d = 0; d < 3; d++) ew_addf(&A.f[(size_t)d * A.n + a_site], q, (double)Fh[d] + (double)Fl[d], A.twopi[d]);
     } else {
         for (int d = 0; d < 3; d++)
             A.fpart[((size_t)blockIdx.y * 3 + d) * A.n + a_site] = (double)Fh[d] + (double)Fl[d];
@@ -918,7 +925,7 @@ __global__ void k_kforce_sum(EwArgs A) {
     for (int d = 0; d < 3; d++) {
         double t = 0.0;
         for (int y = 0; y < A.fsplit; y++) t += A.fpart[((size_t)y * 3 + d) * A.n + a];
-        A.f[(size_t)d * A.n + a] += q * t * A.twopi[d];
+        ew_addf(&A.f[(size_t)d * A.n + a], q, t, A.twopi[d]);
     }
 }
 
@@ -1152,6 +1159,68 @@ mg_status mg_ewald_setup(mg_ctx *c) {
     return MG_OK;
 }
 
+namespace {
+__global__ void k_add_forces(size_t m, double *__restrict__ f, const double *__restrict__ g) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) f[i] += g[i];
+}
+}  // namespace
+
+#ifndef MG_KSTREAM_HIGH
+#define MG_KSTREAM_HIGH 0  // the chain's stream at the highest priority (else the lowest)
+#endif
+
+// Starts the reciprocal-space chain on the context's second stream (created on first
+// use): it waits for what the context's stream has enqueued so
+// far, writes its forces into d_fk (zeroed first) and its energy rows into d_erows_k.
+mg_status mg_ewald_fork(mg_ctx *c, const double *dx, const double *dy, const double *dz) {
+    c->forked = false;
+    if (!c->kstream) {
+        int least = 0, greatest = 0;
+        MG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        MG_CUDA(cudaStreamCreateWithPriority(&c->kstream, cudaStreamNonBlocking, MG_KSTREAM_HIGH ? greatest : least));
+        MG_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        MG_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    }
+    const unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
+    if (!mg_ensure(c, c->d_fk, sizeof(double) * 3 * (size_t)c->natom) ||
+        !mg_ensure(c, c->d_erows_k, sizeof(double) * E_NCOMP * (size_t)rblocks))
+        return mg_fail(c, MG_ERR_ALLOC, "k-space chain buffers");
+    cudaStream_t s = c->stream;
+    MG_CUDA(cudaEventRecord(c->ev_fork, s));
+    MG_CUDA(cudaStreamWaitEvent(c->kstream, c->ev_fork, 0));
+    c->stream = c->kstream;
+    if (c->timing) cudaEventRecord(c->ev[3], c->kstream);
+    mg_status st = MG_OK;
+    if (cudaMemsetAsync(c->d_fk.p, 0, sizeof(double) * 3 * (size_t)c->natom, c->kstream) != cudaSuccess)
+        st = mg_fail(c, MG_ERR_CUDA, "cudaMemsetAsync");
+    c->ew_rows = (double *)c->d_erows_k.p;
+    if (!st) st = mg_launch_ewald(c, dx, dy, dz, (double *)c->d_fk.p);
+    c->ew_rows = nullptr;
+    if (c->timing) cudaEventRecord(c->ev[5], c->kstream);
+    cudaEventRecord(c->ev_join, c->kstream);
+    c->stream = s;
+    if (!st) c->forked = true;
+    return st;
+}
+
+// Waits on the context's stream for the chain, adds its forces into fl and copies its
+// energy rows into rows reserved now (where the serial order reserves them).
+mg_status mg_ewald_join(mg_ctx *c, double *fl) {
+    cudaStream_t s = c->stream;
+    MG_CUDA(cudaStreamWaitEvent(s, c->ev_join, 0));
+    const size_t m = 3 * (size_t)c->natom;
+    k_add_forces<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, fl, (const double *)c->d_fk.p);
+    MG_CUDA(cudaGetLastError());
+    const unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
+    const int r0 = mg_reserve_rows(c, rblocks);
+    if (r0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
+    MG_CUDA(cudaMemcpyAsync((double *)c->d_epart.p + (size_t)r0 * E_NCOMP, c->d_erows_k.p,
+                            sizeof(double) * E_NCOMP * rblocks, cudaMemcpyDeviceToDevice, s));
+    c->launches += 1;
+    return MG_OK;
+}
+
 bool mg_ewald_horner_force(const mg_ctx *c) {
     const int maxa = c->h_chunk_kz.empty() ? 1 : c->h_chunk_kz[0] + 1;
     return c->opt.precision == MG_PREC_FP64 || maxa > EW_FMM_MAXA;
@@ -1207,8 +1276,13 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
         MG_CUDA(launch_sk<float>(A, nblk, s));
     const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
     unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
-    A.row0 = mg_reserve_rows(c, rblocks);
-    if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
+    if (c->ew_rows) {  // enqueued on its own stream: rows of its own, copied in at the join
+        A.rows_e = c->ew_rows;
+        A.row0 = 0;
+    } else {
+        A.row0 = mg_reserve_rows(c, rblocks);
+        if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
+    }
     if (fp64)
         k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
     else

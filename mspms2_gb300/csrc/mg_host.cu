@@ -72,6 +72,19 @@ extern "C" const char *mg_last_error(const mg_ctx *c) {
     return c->err.msg.c_str();
 }
 
+#ifndef MG_FORK_AFTER_LIST
+#define MG_FORK_AFTER_LIST 0  // start the reciprocal-space stream after the list build
+#endif
+#ifndef MG_MAIN_HIGH
+#define MG_MAIN_HIGH 1  // the context's own stream at the highest priority
+#endif
+
+static bool own_stream_create(cudaStream_t *out) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return false;
+    return cudaStreamCreateWithPriority(out, cudaStreamNonBlocking, MG_MAIN_HIGH ? greatest : least) == cudaSuccess;
+}
+
 extern "C" mg_status mg_create(mg_ctx **out, const mg_options *opt) {
     if (!out) return MG_ERR_INVALID;
     *out = nullptr;
@@ -96,7 +109,7 @@ extern "C" mg_status mg_create(mg_ctx **out, const mg_options *opt) {
     }
     c->device = c->opt.device;
     if (cudaSetDevice(c->device) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        !own_stream_create(&c->own_stream)) {
         cudaGetLastError();
         delete c;
         return MG_ERR_CUDA;
@@ -116,6 +129,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
     if (!c) return MG_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->kstream) cudaStreamSynchronize(c->kstream);
     mg_traj_destroy(c);
     DevBuf *bufs[] = {&c->d_site_mol, &c->d_site_q, &c->d_site_hsig, &c->d_site_seps, &c->d_site_flags,
                       &c->d_site_interp, &c->d_species, &c->d_intra, &c->d_bonded, &c->d_site_aw,
@@ -130,12 +144,17 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
                       &c->d_adj_class, &c->d_adj, &c->d_adj_g,
                       &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift,
-                      &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_qf};
+                      &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_qf, &c->d_fk, &c->d_erows_k};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
     for (auto &b : c->myinterp_buf) mg_free(b);
     if (c->have_events)
         for (int i = 0; i < 10; i++) cudaEventDestroy(c->ev[i]);
+    if (c->kstream) {
+        cudaStreamDestroy(c->kstream);
+        cudaEventDestroy(c->ev_fork);
+        cudaEventDestroy(c->ev_join);
+    }
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return MG_OK;
@@ -591,6 +610,10 @@ mg_status mg_enqueue_forces(mg_ctx *c, const double *dx, const double *dy, const
     c->launches = 0;
     bool need_pairs = want_long || (split && want_short);
     mg_status st;
+    const bool ewald = want_long && p.charge_type == MG_ELEC_EWALD;
+    c->forked = false;
+    const bool fork = ewald && c->kspace_overlap && c->nrows > 0;
+    if (fork && !MG_FORK_AFTER_LIST && (st = mg_ewald_fork(c, dx, dy, dz))) return st;
     if (need_pairs) {
         if ((st = mg_list_update(c, dx, dy, dz))) return st;
         if ((st = mg_pack_clusters(c, dx, dy, dz))) return st;
@@ -604,6 +627,7 @@ mg_status mg_enqueue_forces(mg_ctx *c, const double *dx, const double *dy, const
         c->epart_rows = 0;
     }
     if (c->timing) cudaEventRecord(c->ev[1], s);
+    if (fork && MG_FORK_AFTER_LIST && (st = mg_ewald_fork(c, dx, dy, dz))) return st;
     if (need_pairs) {
         if ((st = mg_launch_pair(c, want_long, split && want_short, want_long ? fl : nullptr,
                                  (split && want_short) ? fs : nullptr)))
@@ -616,14 +640,18 @@ mg_status mg_enqueue_forces(mg_ctx *c, const double *dx, const double *dy, const
         if (p.charge_type == MG_ELEC_SIMPLE_COULOMB && (st = mg_launch_coulomb_mole(c, dx, dy, dz, fl))) return st;
     }
     if (want_short && (st = mg_launch_bonded(c, dx, dy, dz, fs))) return st;
-    if (c->timing) cudaEventRecord(c->ev[3], s);
-    if (want_long && p.charge_type == MG_ELEC_EWALD) {
-        if ((st = mg_launch_ewald(c, dx, dy, dz, fl))) return st;  // records ev[4] after the S(k) reduction
+    if (c->timing) cudaEventRecord(c->forked ? c->ev[8] : c->ev[3], s);
+    if (ewald) {
+        if (c->forked) {
+            if ((st = mg_ewald_join(c, fl))) return st;
+        } else if ((st = mg_launch_ewald(c, dx, dy, dz, fl))) {  // records ev[4] after the S(k) reduction
+            return st;
+        }
         if (p.ewald_bc == MG_EWALD_BC_VACUUM && (st = mg_launch_vacuum(c, dx, dy, dz, fl))) return st;
     } else if (c->timing) {
         cudaEventRecord(c->ev[4], s);
     }
-    if (c->timing) cudaEventRecord(c->ev[5], s);
+    if (c->timing) cudaEventRecord(c->forked ? c->ev[9] : c->ev[5], s);
     if (want_long && p.sf_type != MG_SF_NONE && (st = mg_launch_sf(c, dx, dy, dz, fl))) return st;
     if (c->timing) cudaEventRecord(c->ev[6], s);
     if ((st = mg_launch_reduce(c))) return st;
@@ -678,6 +706,12 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
         for (int i = 0; i < 7; i++) {
             cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]);
             c->stats.kernel_ms[i] = ms;
+        }
+        if (c->forked) {  // S(k) and k-forces on their own stream (ev 3-5), beside pairs
+            cudaEventElapsedTime(&ms, c->ev[2], c->ev[8]);
+            c->stats.kernel_ms[2] = ms;
+            cudaEventElapsedTime(&ms, c->ev[9], c->ev[6]);
+            c->stats.kernel_ms[5] = ms;
         }
         cudaEventElapsedTime(&ms, c->ev[0], c->ev[7]);
         c->stats.kernel_ms[7] = ms;
@@ -890,6 +924,12 @@ extern "C" mg_status mg_autotune(mg_ctx *c, const double *x, const double *y, co
         out->ms_tuned = best_ms;
         out->configs_tried = tried;
     }
+    return MG_OK;
+}
+
+extern "C" mg_status mg_set_kspace_overlap(mg_ctx *c, int enable) {
+    if (!c) return MG_ERR_INVALID;
+    c->kspace_overlap = enable != 0;
     return MG_OK;
 }
 

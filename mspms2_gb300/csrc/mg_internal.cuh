@@ -185,6 +185,14 @@ struct mg_ctx {
     std::vector<int> h_chunk_kz;  // kzmax of each chunk of the FP32 table force pass
     DevBuf d_fcoef, d_fpart;      // its coefficients and partial forces
     DevBuf d_qf;                  // FP32 copy of the S(k) site weights
+    // the reciprocal-space chain runs on its own stream beside the list and pair kernels,
+    // into its own force buffer and energy rows, joined before the forces are summed
+    bool kspace_overlap = true;
+    bool forked = false;          // the last evaluation ran that chain on kstream
+    cudaStream_t kstream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    DevBuf d_fk, d_erows_k;
+    double *ew_rows = nullptr;    // energy rows of the chain while it is enqueued
     int ntasks = 0, sblocks_atoms = 0;
     double ewald_box[3] = {0, 0, 0};
     // energies
@@ -209,6 +217,8 @@ struct mg_ctx {
 // ---- helpers shared by host translation units --------------------------------------
 mg_status mg_fail(mg_ctx *c, mg_status code, const std::string &msg);
 bool mg_ewald_horner_force(const mg_ctx *c);  // k-space forces by the Horner pass (threads per site apply)
+mg_status mg_ewald_fork(mg_ctx *c, const double *dx, const double *dy, const double *dz);
+mg_status mg_ewald_join(mg_ctx *c, double *fl);
 mg_status mg_cuda_fail(mg_ctx *c, cudaError_t e, const char *what);
 bool mg_ensure(mg_ctx *c, DevBuf &b, size_t bytes);
 // forces of the given terms at device positions into the context's [3][n] blocks fl/fs,

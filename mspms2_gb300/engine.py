@@ -82,6 +82,7 @@ def load_library(path: str = LIB_PATH):
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.mg_sf_tasos_generate.argtypes = [V, I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, D]
     lib.mg_set_md_graphs.argtypes = [V, I]
+    lib.mg_set_kspace_overlap.argtypes = [V, I]
     lib.mg_get_md_graphs.argtypes = [V, C.POINTER(I), C.POINTER(I)]
     lib.mg_autotune.argtypes = [V, _dp, _dp, _dp, I, C.POINTER(capi.MgTuning)]
     lib.mg_set_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
@@ -294,6 +295,10 @@ class Engine:
         c, _keep = _sfgrid_spec(spec)
         self._check(self.lib.mg_sf_tasos_generate(self.ctx, type_id, C.byref(c), nx, ny, nz, float(h[0]), float(h[1]),
                                                   float(h[2]), float(cuc)))
+
+    def set_kspace_overlap(self, enable: bool) -> None:
+        """Reciprocal space on a second stream beside the list and pairs (default) or in line."""
+        self._check(self.lib.mg_set_kspace_overlap(self.ctx, 1 if enable else 0))
 
     def set_md_graphs(self, enable: bool) -> None:
         """Whole integrator steps as a replayed CUDA graph (default) or step by step."""

@@ -229,3 +229,18 @@ def test_long_kz_rows_take_the_horner_pass():
             out[prec] = eng.compute(terms=TERMS_LONG)
     assert rel(out["mixed"][0], out["fp64"][0]) <= TOL["mixed"], rel(out["mixed"][0], out["fp64"][0])
     assert abs(out["mixed"][2]["ufourier"] - out["fp64"][2]["ufourier"]) <= 1e-5 * abs(out["fp64"][2]["ufourier"])
+
+
+@pytest.mark.parametrize("case", ["water_ewald_512", "butane_ewald_switch"])
+def test_kspace_overlap_is_bit_identical(case):
+    """The reciprocal-space chain on its own stream (default) gives the same bits as the
+    chain in line on the context's stream: forces, energies and the per-call statistics."""
+    s, _ = load_system(os.path.join(GOLDEN, case + ".npz"))
+    out = {}
+    for overlap in (True, False):
+        with Engine(s, precision="mixed") as eng:
+            eng.set_kspace_overlap(overlap)
+            out[overlap] = [eng.compute() for _ in range(2)]
+    for a, b in zip(out[True], out[False]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        assert a[2] == b[2]
