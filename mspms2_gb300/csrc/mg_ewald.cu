@@ -1105,7 +1105,10 @@ mg_status mg_ewald_setup(mg_ctx *c) {
             tasks.push_back(make_int4(r, k0, len, 0));
         }
     });
-    std::stable_sort(tasks.begin(), tasks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
+    // longest first; within a length by first |kz|, so that a warp's tasks mostly share their
+    // Z loads (broadcast shared-memory reads)
+    std::stable_sort(tasks.begin(), tasks.end(),
+                     [](const int4 &a, const int4 &b) { return a.z != b.z ? a.z > b.z : a.y < b.y; });
     {  // pad each length group to whole warps with empty tasks (row 0, count 0)
         std::vector<int4> padded;
         padded.reserve(tasks.size() + 32 * EW_CH);
@@ -1352,8 +1355,8 @@ EwCounts ew_count(int KX, int KY, int KZ, int KS) {
 }
 
 // Row table, packed slot table (first slot of each row, then the row of each slot) and
-// the task list sorted by length (longest first, rows ascending) with each length group
-// padded to whole warps: the same tables mg_ewald_setup builds on the host.
+// the task list sorted by length (longest first), then first |kz|, then row, with each
+// length group padded to whole warps: the same tables mg_ewald_setup builds on the host.
 __global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int nslots, int4 *__restrict__ rows,
                             int *__restrict__ row_slot, int4 *__restrict__ tasks) {
     if (threadIdx.x == 0) {
@@ -1364,17 +1367,37 @@ __global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int nslot
             slot += 2 * (kzmax + 1);
             r++;
         });
+        // counting sort by (length descending, first |kz| ascending), ties in row order;
+        // each length group padded to whole warps
+        int pos[EW_CH + 1][128];
+        for (int L = 0; L <= EW_CH; L++)
+            for (int k = 0; k < 128; k++) pos[L][k] = 0;
+        for (int q = 0; q < nrows; q++) {
+            const int nv = rows[q].z + 1;
+            for (int h = 0; h < ew_nchunk(nv); h++) {
+                int k0, len;
+                ew_chunk(nv, h, k0, len);
+                pos[len][k0 / 2]++;
+            }
+        }
         int t = 0;
         for (int L = EW_CH; L >= 1; L--) {
-            for (int q = 0; q < nrows; q++) {
-                const int nv = rows[q].z + 1;
-                for (int h = 0; h < ew_nchunk(nv); h++) {
-                    int k0, len;
-                    ew_chunk(nv, h, k0, len);
-                    if (len == L) tasks[t++] = make_int4(q, k0, len, 0);
-                }
+            const int start = t;
+            for (int k = 0; k < 128; k++) {
+                const int c = pos[L][k];
+                pos[L][k] = t;
+                t += c;
             }
-            while (t % 32) tasks[t++] = make_int4(0, 0, 0, 0);
+            if (t > start)
+                while (t % 32) tasks[t++] = make_int4(0, 0, 0, 0);
+        }
+        for (int q = 0; q < nrows; q++) {
+            const int nv = rows[q].z + 1;
+            for (int h = 0; h < ew_nchunk(nv); h++) {
+                int k0, len;
+                ew_chunk(nv, h, k0, len);
+                tasks[pos[len][k0 / 2]++] = make_int4(q, k0, len, 0);
+            }
         }
         // force order (kzmax descending, ties in row order) and chunk offsets, by a
         // counting sort over kzmax <= 255
