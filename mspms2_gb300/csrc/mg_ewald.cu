@@ -43,13 +43,16 @@
 #define EW_FG 4         // thread groups sharing the rows of a site in the force pass
 #define EW_FSITES 64    // sites per force block (EW_FG * EW_FSITES threads)
 #ifndef EW_FCHUNK
-#define EW_FCHUNK 12    // rows per chunk of the FP32 table force pass (accumulators per site)
+#define EW_FCHUNK 8     // rows per chunk of the FP32 table force pass (accumulators per site)
 #endif
 #ifndef EW_SK2_MINB
 #define EW_SK2_MINB 3   // resident blocks per SM the FP32 S(k) pass is compiled for
 #endif
+#ifndef EW_FMM_NS
+#define EW_FMM_NS 2     // sites per thread of the table force pass
+#endif
 #ifndef EW_FMM_MINB
-#define EW_FMM_MINB 6   // resident blocks per SM the table force pass is compiled for
+#define EW_FMM_MINB 4   // resident blocks per SM the table force pass is compiled for
 #endif
 #define EW_FMM_TPB 128  // sites (threads) per block of the FP32 table force pass
 #define EW_FMM_MAXA 64  // largest kzmax + 1 the table force pass stages on chip
@@ -833,22 +836,29 @@ __global__ void k_fcoef(EwArgs A) {
 }
 
 __global__ void __launch_bounds__(EW_FMM_TPB, EW_FMM_MINB) k_kforce_mm(EwArgs A, int maxa) {
+    constexpr int NS = EW_FMM_NS, NB = EW_FMM_TPB * EW_FMM_NS;  // sites per thread, per block
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ulonglong2 *sK = (ulonglong2 *)smem_raw;                      // [maxa][EW_FCHUNK]
-    float2 *sZ = (float2 *)(sK + (size_t)maxa * EW_FCHUNK);       // [maxa][EW_FMM_TPB]
+    float2 *sZ = (float2 *)(sK + (size_t)maxa * EW_FCHUNK);       // [maxa][NB]
     __shared__ int2 sR[EW_FCHUNK];                                // (kx, ky); (0, 0) pads
-    const int a_site = blockIdx.x * EW_FMM_TPB + threadIdx.x;
-    const bool act = a_site < A.n;
-    const int site = act ? a_site : A.n - 1;  // idle threads read a valid site, store nothing
     const float2 *tab = (const float2 *)A.tab;
     const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
     const float4 *tZP = (const float4 *)(tab + ew_zoff(A.kx, A.ky, A.n));
-    for (int pp = 0; 2 * pp < maxa; pp++) {
-        const float4 v = tZP[(size_t)pp * A.n + site];
-        sZ[2 * pp * EW_FMM_TPB + threadIdx.x] = make_float2(v.x, v.z);
-        if (2 * pp + 1 < maxa) sZ[(2 * pp + 1) * EW_FMM_TPB + threadIdx.x] = make_float2(v.y, v.w);
+    int site[NS];  // idle threads read a valid site and store nothing
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        const int a_site = blockIdx.x * NB + k * EW_FMM_TPB + threadIdx.x;
+        site[k] = a_site < A.n ? a_site : A.n - 1;
+        for (int pp = 0; 2 * pp < maxa; pp++) {
+            const float4 v = tZP[(size_t)pp * A.n + site[k]];
+            sZ[2 * pp * NB + k * EW_FMM_TPB + threadIdx.x] = make_float2(v.x, v.z);
+            if (2 * pp + 1 < maxa) sZ[(2 * pp + 1) * NB + k * EW_FMM_TPB + threadIdx.x] = make_float2(v.y, v.w);
+        }
     }
-    float Fh[3] = {0, 0, 0}, Fl[3] = {0, 0, 0};  // per-chunk sums accumulated as hi + lo
+    float Fh[NS][3], Fl[NS][3];  // per-chunk sums accumulated as hi + lo
+#pragma unroll
+    for (int k = 0; k < NS; k++)
+        for (int d = 0; d < 3; d++) Fh[k][d] = Fl[k][d] = 0.f;
     const int c_lo = A.csplit[blockIdx.y], c_hi = A.csplit[blockIdx.y + 1];
     for (int c = c_lo; c < c_hi; c++) {
         const int m = A.rows[A.forder[c * EW_FCHUNK]].z;
@@ -865,55 +875,75 @@ __global__ void __launch_bounds__(EW_FMM_TPB, EW_FMM_MINB) k_kforce_mm(EwArgs A,
             sR[threadIdx.x] = kk;
         }
         __syncthreads();
-        f32x2 W[EW_FCHUNK];
-        float Pr[EW_FCHUNK], Pi[EW_FCHUNK];
+        f32x2 W[NS][EW_FCHUNK];
+        float Pr[NS][EW_FCHUNK], Pi[NS][EW_FCHUNK];
 #pragma unroll
-        for (int j = 0; j < EW_FCHUNK; j++) {
-            W[j] = 0;
-            Pr[j] = Pi[j] = 0.f;
-        }
+        for (int k = 0; k < NS; k++)
+#pragma unroll
+            for (int j = 0; j < EW_FCHUNK; j++) {
+                W[k][j] = 0;
+                Pr[k][j] = Pi[k][j] = 0.f;
+            }
         for (int a = 0; a <= m; a++) {
-            const float2 z = sZ[a * EW_FMM_TPB + threadIdx.x];
-            const float fa = (float)a, azr = fa * z.x, azi = fa * z.y;
-            const f32x2 ZR = pk2(z.x, z.x), ZI = pk2(z.y, z.y);
+            f32x2 ZR[NS], ZI[NS];
+            float azr[NS], azi[NS];
+#pragma unroll
+            for (int k = 0; k < NS; k++) {
+                const float2 z = sZ[a * NB + k * EW_FMM_TPB + threadIdx.x];
+                azr[k] = (float)a * z.x;
+                azi[k] = (float)a * z.y;
+                ZR[k] = pk2(z.x, z.x);
+                ZI[k] = pk2(z.y, z.y);
+            }
             const ulonglong2 *kr = sK + a * EW_FCHUNK;
 #pragma unroll
             for (int j = 0; j < EW_FCHUNK; j++) {
                 const ulonglong2 kk = kr[j];  // (k0, k2), (k1, k3)
-                W[j] = fma2(ZI, kk.y, fma2(ZR, kk.x, W[j]));
                 float k0, k1, k2, k3;
                 up2(kk.x, k0, k2);
                 up2(kk.y, k1, k3);
-                Pr[j] = fmaf(azr, k3, fmaf(-azi, k2, Pr[j]));
-                Pi[j] = fmaf(azi, k0, fmaf(-azr, k1, Pi[j]));
+#pragma unroll
+                for (int k = 0; k < NS; k++) {
+                    W[k][j] = fma2(ZI[k], kk.y, fma2(ZR[k], kk.x, W[k][j]));
+                    Pr[k][j] = fmaf(azr[k], k3, fmaf(-azi[k], k2, Pr[k][j]));
+                    Pi[k][j] = fmaf(azi[k], k0, fmaf(-azr[k], k1, Pi[k][j]));
+                }
             }
         }
-        float fx = 0, fy = 0, fz = 0;
 #pragma unroll
-        for (int j = 0; j < EW_FCHUNK; j++) {
-            const int2 kk = sR[j];
-            const float2 X = tX[(size_t)kk.x * A.n + site];
-            float2 Y = tY[(size_t)(kk.y < 0 ? -kk.y : kk.y) * A.n + site];
-            if (kk.y < 0) Y.y = -Y.y;
-            const float2 Aa = cmul(X, Y);
-            float wr, wi;
-            up2(W[j], wr, wi);
-            const float gsum = Aa.x * wi + Aa.y * wr;
-            fx += gsum * (float)kk.x;
-            fy += gsum * (float)kk.y;
-            fz += Aa.x * Pi[j] + Aa.y * Pr[j];
+        for (int k = 0; k < NS; k++) {
+            float fx = 0, fy = 0, fz = 0;
+#pragma unroll
+            for (int j = 0; j < EW_FCHUNK; j++) {
+                const int2 kk = sR[j];
+                const float2 X = tX[(size_t)kk.x * A.n + site[k]];
+                float2 Y = tY[(size_t)(kk.y < 0 ? -kk.y : kk.y) * A.n + site[k]];
+                if (kk.y < 0) Y.y = -Y.y;
+                const float2 Aa = cmul(X, Y);
+                float wr, wi;
+                up2(W[k][j], wr, wi);
+                const float gsum = Aa.x * wi + Aa.y * wr;
+                fx += gsum * (float)kk.x;
+                fy += gsum * (float)kk.y;
+                fz += Aa.x * Pi[k][j] + Aa.y * Pr[k][j];
+            }
+            mg_acc2(Fh[k][0], Fl[k][0], fx);
+            mg_acc2(Fh[k][1], Fl[k][1], fy);
+            mg_acc2(Fh[k][2], Fl[k][2], fz);
         }
-        mg_acc2(Fh[0], Fl[0], fx);
-        mg_acc2(Fh[1], Fl[1], fy);
-        mg_acc2(Fh[2], Fl[2], fz);
     }
-    if (!act) return;
-    if (A.fsplit == 1) {
-        const double q = A.q[a_site];
-        for (int d = 0; d < 3; d++) ew_addf(&A.f[(size_t)d * A.n + a_site], q, (double)Fh[d] + (double)Fl[d], A.twopi[d]);
-    } else {
-        for (int d = 0; d < 3; d++)
-            A.fpart[((size_t)blockIdx.y * 3 + d) * A.n + a_site] = (double)Fh[d] + (double)Fl[d];
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        const int a_site = blockIdx.x * NB + k * EW_FMM_TPB + threadIdx.x;
+        if (a_site >= A.n) continue;
+        if (A.fsplit == 1) {
+            const double q = A.q[a_site];
+            for (int d = 0; d < 3; d++)
+                ew_addf(&A.f[(size_t)d * A.n + a_site], q, (double)Fh[k][d] + (double)Fl[k][d], A.twopi[d]);
+        } else {
+            for (int d = 0; d < 3; d++)
+                A.fpart[((size_t)blockIdx.y * 3 + d) * A.n + a_site] = (double)Fh[k][d] + (double)Fl[k][d];
+        }
     }
 }
 
@@ -929,7 +959,9 @@ __global__ void k_kforce_sum(EwArgs A) {
     }
 }
 
-inline size_t fmm_smem(int maxa) { return (size_t)maxa * (EW_FCHUNK * sizeof(ulonglong2) + EW_FMM_TPB * sizeof(float2)); }
+inline size_t fmm_smem(int maxa) {
+    return (size_t)maxa * (EW_FCHUNK * sizeof(ulonglong2) + EW_FMM_NS * EW_FMM_TPB * sizeof(float2));
+}
 
 // resident blocks of k_kforce_mm per SM x SMs, per device and dynamic shared memory size
 int fmm_slots(int maxa) {
@@ -956,7 +988,7 @@ int fmm_slots(int maxa) {
 // waves; returns S and fills csplit[0..S].
 int fmm_split(const std::vector<int> &chunk_kz, int n, int slots, int smax, int *csplit) {
     const int nc = (int)chunk_kz.size();
-    const long long nb = (n + EW_FMM_TPB - 1) / EW_FMM_TPB;
+    const long long nb = (n + EW_FMM_NS * EW_FMM_TPB - 1) / (EW_FMM_NS * EW_FMM_TPB);
     smax = std::max(1, std::min(std::min(smax, EW_MAXSPLIT), nc));
     int best = 1;
     double best_eff = 0.0;
@@ -1041,7 +1073,7 @@ cudaError_t launch_kforce(int fg, unsigned blocks, size_t smem, cudaStream_t s, 
             const size_t msmem = fmm_smem(maxa);
             e = cudaFuncSetAttribute(k_kforce_mm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem);
             if (e != cudaSuccess) return e;
-            const dim3 grid((unsigned)((A.n + EW_FMM_TPB - 1) / EW_FMM_TPB), (unsigned)A.fsplit);
+            const dim3 grid((unsigned)((A.n + EW_FMM_NS * EW_FMM_TPB - 1) / (EW_FMM_NS * EW_FMM_TPB)), (unsigned)A.fsplit);
             k_kforce_mm<<<grid, EW_FMM_TPB, msmem, s>>>(A, maxa);
             if (A.fsplit > 1) k_kforce_sum<<<(A.n + 255) / 256, 256, 0, s>>>(A);
             return cudaGetLastError();
