@@ -564,18 +564,33 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
-// S(k) from the partials in site-block order; energy rows and force coefficients
+// S(k) from the partials: a block of EW_RED_PARTS * 256 threads takes 256 slots; part p
+// sums site blocks [p nblk / PARTS, (p + 1) nblk / PARTS) in order and the parts are
+// added in order (fixed order throughout); then energy rows and force coefficients
+#define EW_RED_PARTS 4
 template <typename R>
-__global__ void k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row) {
+__global__ void __launch_bounds__(EW_RED_PARTS * 256) k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row) {
     typedef typename C2<R>::T T2;
+    __shared__ double2 sp[EW_RED_PARTS][256];
     double e[1] = {0.0};
-    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const int part = threadIdx.x / 256, sl = threadIdx.x % 256;
+    int slot = blockIdx.x * 256 + sl;
     if (slot < A.nslots) {
         double sr = 0.0, si = 0.0;
-        for (int b = 0; b < nblk; b++) {
+        const int b0 = (int)((long long)nblk * part / EW_RED_PARTS), b1 = (int)((long long)nblk * (part + 1) / EW_RED_PARTS);
+        for (int b = b0; b < b1; b++) {
             const R *p = (const R *)A.spart + ((size_t)b * A.nslots + slot) * 2;
             sr += (double)p[0];
             si += (double)p[1];
+        }
+        sp[part][sl] = make_double2(sr, si);
+    }
+    __syncthreads();
+    if (part == 0 && slot < A.nslots) {
+        double sr = sp[0][sl].x, si = sp[0][sl].y;
+        for (int q = 1; q < EW_RED_PARTS; q++) {
+            sr += sp[q][sl].x;
+            si += sp[q][sl].y;
         }
         int r = slot_row[slot];
         int4 row = A.rows[r];
@@ -1319,9 +1334,9 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
         if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
     }
     if (fp64)
-        k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+        k_sk_reduce<double><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
     else
-        k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+        k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
     if (c->timing) cudaEventRecord(c->ev[4], s);
     int maxa = 1;
     for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);
@@ -1653,13 +1668,13 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     const unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
     if (fp64) {
         EWS_CUDA(launch_sk<double>(A, nblk, s), "k_sk launch");
-        k_sk_reduce<double><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+        k_sk_reduce<double><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
         EWS_CUDA(cudaFuncSetAttribute(k_kforce<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem),
                  "cudaFuncSetAttribute");
         k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, ct.maxa);
     } else {
         EWS_CUDA(launch_sk<float>(A, nblk, s), "k_sk launch");
-        k_sk_reduce<float><<<rblocks, 256, 0, s>>>(A, nblk, slot_row);
+        k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
         EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
     }
     if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, d_energy);
