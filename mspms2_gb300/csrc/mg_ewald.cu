@@ -565,8 +565,9 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 }
 
 // S(k) from the partials: a block of EW_RED_PARTS * 256 threads takes 256 slots; part p
-// sums site blocks [p nblk / PARTS, (p + 1) nblk / PARTS) in order and the parts are
-// added in order (fixed order throughout); then energy rows and force coefficients
+// sums site blocks [p nblk / PARTS, (p + 1) nblk / PARTS) in order (FP32 hi + lo on the
+// FP32 path, FP64 on the FP64 path) and the parts are added in order in FP64 (fixed order
+// throughout); then energy rows and force coefficients
 #define EW_RED_PARTS 4
 template <typename R>
 __global__ void __launch_bounds__(EW_RED_PARTS * 256) k_sk_reduce(EwArgs A, int nblk, const int *__restrict__ slot_row) {
@@ -576,14 +577,16 @@ __global__ void __launch_bounds__(EW_RED_PARTS * 256) k_sk_reduce(EwArgs A, int 
     const int part = threadIdx.x / 256, sl = threadIdx.x % 256;
     int slot = blockIdx.x * 256 + sl;
     if (slot < A.nslots) {
-        double sr = 0.0, si = 0.0;
+        // FP32 partials summed as exact hi + lo pairs (no FP64 instruction in the loop;
+        // FP64 arithmetic runs at a small fraction of the FP32 rate on this part)
+        R hr = 0, lr = 0, hi = 0, li = 0;
         const int b0 = (int)((long long)nblk * part / EW_RED_PARTS), b1 = (int)((long long)nblk * (part + 1) / EW_RED_PARTS);
         for (int b = b0; b < b1; b++) {
             const R *p = (const R *)A.spart + ((size_t)b * A.nslots + slot) * 2;
-            sr += (double)p[0];
-            si += (double)p[1];
+            mg_acc2(hr, lr, p[0]);
+            mg_acc2(hi, li, p[1]);
         }
-        sp[part][sl] = make_double2(sr, si);
+        sp[part][sl] = make_double2((double)hr + (double)lr, (double)hi + (double)li);
     }
     __syncthreads();
     if (part == 0 && slot < A.nslots) {
