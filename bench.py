@@ -519,13 +519,14 @@ def force_matching_extras(device, nsnap=64, stride=4, seed=2024):
                     "gradient in (eps_OO, sigma_OO, q_O) with q_H = -q_O/2; central differences h = 1e-4 relative"}
 
 
-def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True):
+def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10):
     """United-atom n-butane in a bundle of 7 (11,11) nanotubes (80,000 sites, LJ rc 14 A,
     Tasos solid-fluid tables at 0.1 A over the 127 x 127 A bundle cell, generated on the
     device): force steps timed like the headline (device-resident positions, L2 flushed,
     CUDA events), the solid-fluid gather against the HBM roofline (64 FP32 table values,
     256 B, per site), ns/day of Nose-Hoover RESPA (2 fs outer, 4 x 0.5 fs inner with the
-    bonded terms) and the plain-FP64 path on the same system."""
+    bonded terms), the reference's simulated annealing 600 K -> 300 K on the system, and the
+    plain-FP64 path on the same system."""
     import torch
     from mspms2_gb300 import configs
     from mspms2_gb300.engine import TERMS_ALL, Engine
@@ -593,6 +594,15 @@ def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True):
         t0 = time.perf_counter()
         eng.md_run(md_steps, md, v1, x=p1[0], y=p1[1], z=p1[2], state={k: st1[k] for k in ("ps", "ss", "pss", "sss")})
         dt_md = time.perf_counter() - t0
+        # the reference's simulated annealing on this system (mg_siman_run): T = 600 K / 1.3^k
+        # until the first stage below 300 K, siman_tries RESPA outer steps per stage
+        sc = dict(t_initial=600.0 / s.epsilon_base, t_min=300.0 / s.epsilon_base, mu_t=1.3, n_tries=siman_tries,
+                  max_stages=8, seed=2024)
+        eng.siman_run(md, dict(sc, n_tries=1, t_min=599.0 / s.epsilon_base, max_stages=2), x=p1[0], y=p1[1],
+                      z=p1[2])  # warm-up: two stages of one step
+        t0 = time.perf_counter()
+        _, _, _, slog = eng.siman_run(md, sc, x=p1[0], y=p1[1], z=p1[2])
+        dt_si = time.perf_counter() - t0
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     nsf = n  # every butane site is of ghost type NONE
@@ -606,7 +616,14 @@ def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True):
                               "peak_basis": "of measured (MEASURED_PEAKS.json hbm_gbs)"},
                 "md": {"scheme": "NVT Nose-Hoover RESPA, 4 x 0.5 fs inner (bonded) + 2 fs outer", "steps": md_steps,
                        "ms_per_outer_step": dt_md / md_steps * 1e3,
-                       "ns_per_day": md_steps * 2.0e-6 / dt_md * 86400.0}})
+                       "ns_per_day": md_steps * 2.0e-6 / dt_md * 86400.0},
+                "siman": {"schedule": "600 K / 1.3^k to the first stage below 300 K (the reference's siman)",
+                          "stages": int(len(slog)), "steps_per_stage": siman_tries,
+                          "T_K": [float(t) * s.epsilon_base for t in slog[:, 0]],
+                          "tinst_K_end_of_stage": [float(t) * s.epsilon_base for t in slog[:, 5]],
+                          "wall_s": dt_si, "ms_per_outer_step": dt_si / (len(slog) * siman_tries) * 1e3,
+                          "note": "one system through the engine; replicas of this size (80,000 sites, "
+                                  "2.6 GB of solid-fluid tables) run as separate contexts, not one launch"}})
     if fp64:
         with Engine(s, precision="fp64", device=device) as e64:
             t0 = time.perf_counter()
