@@ -354,6 +354,81 @@ __global__ void __launch_bounds__(MD_TPB) k_nh_solve_coop(MdArgs A, NhArgs N, in
     }
 }
 
+// The same solve for the mixed path, reduced to one unknown. Given ps_new the per-site
+// equation vn (1 + h ps_new) = v + h f r is linear, so the joint Newton iteration above
+// converges to the root of the scalar equation
+//   G(p) = p - ps - (h/q) (K0 / (1 + h p)^2 - g treq) = 0,  K0 = sum m (v + h f r)^2,
+// and vn = (v + h f r) / (1 + h p). One pass forms v + h f r and K0, Newton on p runs in
+// registers (each block the same steps, so no grid-wide work per iteration), one pass
+// scales the velocities and sums m vn^2. Same convergence test and iteration limit as the
+// reference's solve; the root agrees with the joint iteration's to rounding.
+__global__ void __launch_bounds__(MD_TPB) k_nh_solve_scalar(MdArgs A, NhArgs N, int nb) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    double *pa = A.part, *pb = A.part + nb;
+    const int n = A.n;
+    for (int vb = blockIdx.x; vb < nb; vb += gridDim.x) {  // w = v + h f r and sum m w^2
+        const int a = vb * MD_TPB + threadIdx.x;
+        double m2 = 0.0;
+        if (a < n) {
+            const double r = A.rmass[a];
+            double s = 0.0;
+            for (int d = 0; d < 3; d++) {
+                const double w = A.v[d * n + a] + N.h * N.f[d * n + a] * r;
+                A.vn[d * n + a] = w;
+                s += w * w;
+            }
+            m2 = s / r;
+        }
+        block_partial_at(m2, pa, vb);
+    }
+    grid.sync();
+    const double K0 = sum_partials(pa, nb);
+    __syncthreads();
+    const double ps = nh_ps(A.s, N.inner);
+    double p = ps, pold = ps, dp = 0.0;
+    int iter = 0;
+    bool ready = false;
+    while (!ready) {
+        const double ix = 1.0 / (1.0 + N.h * p), ix2 = ix * ix;
+        const double G = p - ps - (N.h / N.q) * (K0 * ix2 - N.g_treq);
+        const double dG = 1.0 + 2.0 * N.h * N.h * K0 * ix2 * ix / N.q;
+        dp = -G / dG;
+        pold = p;
+        p = pold + dp;
+        iter += 1;
+        ready = !(fabs(dp / p) > MD_ERR) || iter >= MD_MAX_ITER;
+    }
+    const double scale = 1.0 / (1.0 + N.h * p);
+    for (int vb = blockIdx.x; vb < nb; vb += gridDim.x) {  // vn = w / (1 + h p) and sum m vn^2
+        const int a = vb * MD_TPB + threadIdx.x;
+        double m2 = 0.0;
+        if (a < n) {
+            double s = 0.0;
+            for (int d = 0; d < 3; d++) {
+                const double vn = A.vn[d * n + a] * scale;
+                A.vn[d * n + a] = vn;
+                A.v[d * n + a] = vn;
+                s += vn * vn;
+            }
+            m2 = s / A.rmass[a];
+        }
+        block_partial_at(m2, pb, vb);
+    }
+    grid.sync();
+    const double sumv2 = sum_partials(pb, nb);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        MdDev *s = A.s;
+        s->sumv2 = sumv2;
+        s->psn = p;
+        s->pso = pold;
+        s->delps = dp;
+        s->di = -(pold * N.h + 1.0);
+        s->iter = iter;
+        s->ready = 1;
+        nh_ps(s, N.inner) = p;
+    }
+}
+
 // end-of-step scalars: thermostat energies, kinetic energy and temperature
 __global__ void k_md_step_scalars(MdDev *s, int nb_unused, double qq, double qqs, double gg_treq,
                                   double ggs_treq, double nfree, int thermo, double *log_row) {
@@ -578,8 +653,9 @@ mg_status nh_solve(MdRun &R, const double *f, double h, double dt, double q, dou
     if (R.coop_grid > 0) {
         int nb = R.nb;
         void *args[] = {(void *)&R.A, (void *)&N, (void *)&nb};
-        MG_CUDA(cudaLaunchCooperativeKernel((const void *)k_nh_solve_coop, dim3(R.coop_grid), dim3(MD_TPB), args, 0,
-                                            R.s));
+        // the FP64 path keeps the reference's joint iteration; the mixed path solves for ps alone
+        const void *fn = c->opt.precision == MG_PREC_FP64 ? (const void *)k_nh_solve_coop : (const void *)k_nh_solve_scalar;
+        MG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(R.coop_grid), dim3(MD_TPB), args, 0, R.s));
         c->launches += 1;
         return MG_OK;
     }
@@ -628,9 +704,11 @@ mg_status md_prepare(mg_ctx *c, size_t log_rows, MdRun &R) {
         int coop = 0, sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        int per_sm2 = 0;
         if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nh_solve_coop, MD_TPB, 0) == cudaSuccess &&
-            per_sm > 0)
-            R.coop_grid = std::min(nb, per_sm * sms);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_nh_solve_scalar, MD_TPB, 0) == cudaSuccess &&
+            std::min(per_sm, per_sm2) > 0)
+            R.coop_grid = std::min(nb, std::min(per_sm, per_sm2) * sms);
         cudaGetLastError();
     }
     MdArgs &A = R.A;
