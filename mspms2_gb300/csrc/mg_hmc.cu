@@ -29,6 +29,13 @@
 #include "mg_internal.cuh"
 
 #define HMC_TPB 512
+#ifndef HMC_UNROLL
+#define HMC_UNROLL 4     // j candidates per step of the force loop
+#endif
+constexpr int kHmcUnroll = HMC_UNROLL;
+#ifndef HMC_MINB
+#define HMC_MINB 1       // resident blocks per SM the replica kernels are compiled for
+#endif
 
 namespace {
 
@@ -69,9 +76,9 @@ __device__ __forceinline__ void block_sum3(double &a, double &b, double &c) {
 }
 
 struct Smem {
-    float4 *pos;  // [nmax] wrapped FP32 positions; w = cell index
-    int *list;    // [nmax] atoms by cell, index order within a cell
-    int *start;   // [ncmax + 1]
+    float4 *pos;  // [nmax] wrapped FP32 positions sorted by cell (index order inside a cell); w = atom index
+    int *list;    // [nmax] cell of each atom while the cells are built
+    int *start;   // [ncmax + 1] first sorted slot of each cell
     int *cnt;     // [ncmax]
 };
 
@@ -80,30 +87,39 @@ __device__ __forceinline__ int cell_of(float v, float inv_w, int nc) {
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
-// wrapped FP32 positions (and cells) of the replica into shared memory, then the list
+// coordinate w wrapped into [0, L) in FP32: the image count in FP32, the subtraction as one
+// FP64 FMA (FP64 runs at a small fraction of the FP32 rate on this part); a count off by
+// one at the boundary leaves a rounding outside [0, L), folded back here
+__device__ __forceinline__ float wrapf(double w, double L, float Lf, float iLf) {
+    const float nf = floorf((float)w * iLf);
+    float t = (float)fma(-(double)nf, L, w);
+    if (t >= Lf) t -= Lf;
+    if (t < 0.f) t = 0.f;
+    return t;
+}
+
+// Wrapped FP32 positions of the replica into shared memory, sorted by cell with index order
+// inside each cell (fixed order for every sum); without cells (nc == 0), in index order.
 __device__ __forceinline__ void load_positions(const HmcArgs &A, const Smem &S, int off, int n, double L, int nc) {
-    const float Lf = (float)L, inv_w = nc > 0 ? (float)(nc / L) : 0.f;
+    const float Lf = (float)L, iLf = (float)(1.0 / L), inv_w = nc > 0 ? (float)(nc / L) : 0.f;
+    if (nc == 0) {
+        for (int i = threadIdx.x; i < n; i += HMC_TPB)
+            S.pos[i] = make_float4(wrapf(A.x[off + i], L, Lf, iLf), wrapf(A.y[off + i], L, Lf, iLf),
+                                   wrapf(A.z[off + i], L, Lf, iLf), __int_as_float(i));
+        __syncthreads();
+        return;
+    }
     const int ncell = nc * nc * nc;
     for (int c = threadIdx.x; c < ncell; c += HMC_TPB) S.cnt[c] = 0;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += HMC_TPB) {
-        double w[3] = {A.x[off + i], A.y[off + i], A.z[off + i]};
-        float p[3];
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            double t = w[d] - L * floor(w[d] / L);
-            float f = (float)t;
-            p[d] = f < Lf ? f : 0.f;
-        }
-        int cell = 0;
-        if (nc > 0) {
-            cell = (cell_of(p[2], inv_w, nc) * nc + cell_of(p[1], inv_w, nc)) * nc + cell_of(p[0], inv_w, nc);
-            atomicAdd(&S.cnt[cell], 1);
-        }
-        S.pos[i] = make_float4(p[0], p[1], p[2], __int_as_float(cell));
+        const float px = wrapf(A.x[off + i], L, Lf, iLf), py = wrapf(A.y[off + i], L, Lf, iLf);
+        const float pz = wrapf(A.z[off + i], L, Lf, iLf);
+        const int cell = (cell_of(pz, inv_w, nc) * nc + cell_of(py, inv_w, nc)) * nc + cell_of(px, inv_w, nc);
+        S.list[i] = cell;
+        atomicAdd(&S.cnt[cell], 1);
     }
     __syncthreads();
-    if (nc == 0) return;
     // exclusive scan of the counts by warp 0 (lanes own consecutive chunks)
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x, chunk = (ncell + 31) / 32;
@@ -125,101 +141,142 @@ __device__ __forceinline__ void load_positions(const HmcArgs &A, const Smem &S, 
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += HMC_TPB) {
-        const int cell = __float_as_int(S.pos[i].w);
-        const int slot = atomicAdd(&S.cnt[cell], 1);
-        S.list[S.start[cell] + slot] = i;
+        const int cell = S.list[i];
+        const int k = S.start[cell] + atomicAdd(&S.cnt[cell], 1);
+        S.pos[k] = make_float4(wrapf(A.x[off + i], L, Lf, iLf), wrapf(A.y[off + i], L, Lf, iLf),
+                               wrapf(A.z[off + i], L, Lf, iLf), __int_as_float(i));
     }
     __syncthreads();
     for (int c = threadIdx.x; c < ncell; c += HMC_TPB) {  // index order inside each cell
         const int b = S.start[c], e = S.start[c + 1];
         for (int k = b + 1; k < e; k++) {
-            const int v = S.list[k];
+            const float4 v = S.pos[k];
+            const int vi = __float_as_int(v.w);
             int m = k - 1;
-            while (m >= b && S.list[m] > v) {
-                S.list[m + 1] = S.list[m];
+            while (m >= b && __float_as_int(S.pos[m].w) > vi) {
+                S.pos[m + 1] = S.pos[m];
                 m--;
             }
-            S.list[m + 1] = v;
+            S.pos[m + 1] = v;
         }
+    }
+    // chunks of 32 slots per (y, z) row of cells, as a prefix over the rows (S.cnt[0..nc^2])
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int r = 0; r < nc * nc; r++) {
+            S.cnt[r] = t;
+            t += (S.start[r * nc + nc] - S.start[r * nc] + 31) / 32;
+        }
+        S.cnt[nc * nc] = t;
     }
     __syncthreads();
 }
 
-// LJ force on atom i (FP32) and its pair energy / pair count (each pair seen twice)
-__device__ __forceinline__ void lj_add(float3 d, float sig2, float eps, float rc2, float &fx, float &fy, float &fz,
-                                       float &e, int &np) {
-    const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+// LJ force and pair energy (each pair is seen from both sides)
+__device__ __forceinline__ void lj_add(float dx, float dy, float dz, float sig2, float eps, float rc2, float &fx,
+                                       float &fy, float &fz, float &e, int &np) {
+    const float r2 = dx * dx + dy * dy + dz * dz;
     if (!(r2 < rc2)) return;
-    const float s2 = sig2 / r2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+    const float ir2 = __frcp_rn(r2);
+    const float s2 = sig2 * ir2, s6 = s2 * s2 * s2, s12 = s6 * s6;
     e += 4.f * eps * (s12 - s6);
-    const float f = 24.f * eps * (2.f * s12 - s6) / r2;
-    fx += f * d.x;
-    fy += f * d.y;
-    fz += f * d.z;
+    const float f = 24.f * eps * (2.f * s12 - s6) * ir2;
+    fx += f * dx;
+    fy += f * dy;
+    fz += f * dz;
     np += 1;
 }
 
-__device__ __forceinline__ void atom_force(const HmcArgs &A, const Smem &S, int i, int n, double L, int nc, float &fx, float &fy,
-                           float &fz, float &e, int &np) {
-    const float4 pi = S.pos[i];
-    const float Lf = (float)L, sig2 = (float)A.sig2, eps = (float)A.eps, rc2 = (float)A.rc2;
-    fx = fy = fz = e = 0.f;
-    np = 0;
+// Forces on every atom of the replica, warp-cooperatively: a warp takes up to 32 atoms of
+// one (y, z) row of cells (consecutive sorted slots, one atom per lane) and all lanes walk
+// the same j-atoms, those of the 9 neighbour rows over the chunk's x cells +-1, so that
+// each j load is a broadcast and the lanes do not diverge. y and z images come from the
+// row offsets; x takes the minimum image per pair (correct for any chunk, L >= 2 rc). j
+// order is fixed (rows, then cells in x, then slots), so every sum has a fixed order.
+// fn(i, fx, fy, fz, e, np) receives each atom's force, LJ energy and pair count.
+template <typename F>
+__device__ __forceinline__ void replica_forces(const HmcArgs &A, const Smem &S, int n, double L, int nc, F &&fn) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int NW = HMC_TPB / 32;
+    const float Lf = (float)L, iL = (float)(1.0 / L), sig2 = (float)A.sig2, eps = (float)A.eps;
+    const float rc2 = (float)A.rc2;
     if (nc == 0) {  // all pairs, minimum image
-        const float iL = 1.f / Lf;
-        for (int j = 0; j < n; j++) {
-            if (j == i) continue;
-            const float4 pj = S.pos[j];
-            float3 d = make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
-            d.x -= Lf * rintf(d.x * iL);
-            d.y -= Lf * rintf(d.y * iL);
-            d.z -= Lf * rintf(d.z * iL);
-            lj_add(d, sig2, eps, rc2, fx, fy, fz, e, np);
+        for (int base = wid * 32; base < n; base += NW * 32) {
+            const int k = base + lane;
+            const bool act = k < n;
+            const float4 pi = S.pos[act ? k : base];
+            float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+            int np = 0;
+            for (int j = 0; j < n; j++) {
+                const float4 pj = S.pos[j];
+                float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                dx -= Lf * rintf(dx * iL);
+                dy -= Lf * rintf(dy * iL);
+                dz -= Lf * rintf(dz * iL);
+                if (j != k) lj_add(dx, dy, dz, sig2, eps, rc2, fx, fy, fz, e, np);
+            }
+            if (act) fn(__float_as_int(pi.w), fx, fy, fz, e, np);
         }
         return;
     }
-    const int ci = __float_as_int(pi.w);
-    const int cx = ci % nc, cy = (ci / nc) % nc, cz = ci / (nc * nc);
-    for (int dz = -1; dz <= 1; dz++) {
-        int uz = cz + dz;
-        const float sz = uz < 0 ? -Lf : (uz >= nc ? Lf : 0.f);
-        uz = (uz + nc) % nc;
-        for (int dy = -1; dy <= 1; dy++) {
-            int uy = cy + dy;
-            const float sy = uy < 0 ? -Lf : (uy >= nc ? Lf : 0.f);
-            uy = (uy + nc) % nc;
-            for (int dx = -1; dx <= 1; dx++) {
-                int ux = cx + dx;
-                const float sx = ux < 0 ? -Lf : (ux >= nc ? Lf : 0.f);
-                ux = (ux + nc) % nc;
-                const int c = (uz * nc + uy) * nc + ux;
-                for (int k = S.start[c]; k < S.start[c + 1]; k++) {
-                    const int j = S.list[k];
-                    if (j == i) continue;
-                    const float4 pj = S.pos[j];
-                    const float3 d = make_float3(pi.x - (pj.x + sx), pi.y - (pj.y + sy), pi.z - (pj.z + sz));
-                    lj_add(d, sig2, eps, rc2, fx, fy, fz, e, np);
+    const float inv_w = (float)(nc / L);
+    const int nchunk = S.cnt[nc * nc];
+    int r = 0;
+    for (int t = wid; t < nchunk; t += NW) {  // chunks dealt to the warps in order
+        while (S.cnt[r + 1] <= t) r++;
+        const int y = r % nc, z = r / nc;
+        const int re = S.start[r * nc + nc];
+        {
+            const int base = S.start[r * nc] + 32 * (t - S.cnt[r]);
+            const int k = base + lane, klast = min(base + 32, re) - 1;
+            const bool act = k < re;
+            const float4 pi = S.pos[act ? k : base];
+            const int xlo = cell_of(S.pos[base].x, inv_w, nc), xhi = cell_of(S.pos[klast].x, inv_w, nc);
+            const int m = min(xhi - xlo + 3, nc);      // cells of the x range
+            const int xs = (xlo - 1 + nc) % nc;       // its first cell
+            const int run1 = min(m, nc - xs);         // cells before the wrap
+            float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+            int np = 0;
+            for (int dz = -1; dz <= 1; dz++) {
+                int uz = z + dz;
+                const float sz = uz < 0 ? -Lf : (uz >= nc ? Lf : 0.f);
+                uz = (uz + nc) % nc;
+                for (int dy = -1; dy <= 1; dy++) {
+                    int uy = y + dy;
+                    const float sy = uy < 0 ? -Lf : (uy >= nc ? Lf : 0.f);
+                    uy = (uy + nc) % nc;
+                    const int c0 = (uz * nc + uy) * nc;
+                    for (int run = 0; run < 2; run++) {
+                        const int ca = run == 0 ? c0 + xs : c0, cb = run == 0 ? c0 + xs + run1 : c0 + (m - run1);
+                        const int jb = S.start[ca], je = S.start[cb];
+#pragma unroll kHmcUnroll
+                        for (int j = jb; j < je; j++) {
+                            const float4 pj = S.pos[j];
+                            float dx = pi.x - pj.x;
+                            dx -= Lf * rintf(dx * iL);
+                            const float dyy = pi.y - (pj.y + sy), dzz = pi.z - (pj.z + sz);
+                            if (j != k) lj_add(dx, dyy, dzz, sig2, eps, rc2, fx, fy, fz, e, np);
+                        }
+                    }
                 }
             }
+            if (act) fn(__float_as_int(pi.w), fx, fy, fz, e, np);
         }
     }
 }
 
 // forces at the shared-memory positions, v += f h / m; optional energy (U, pair count)
 __device__ __forceinline__ void force_kick(const HmcArgs &A, const Smem &S, int off, int n, double L, int nc, double h,
-                           double *u_out, double *np_out) {
+                                           double *u_out, double *np_out) {
     double esum = 0.0, nsum = 0.0, unused = 0.0;
     const double hm = h / A.mass;
-    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
-        float fx, fy, fz, e;
-        int np;
-        atom_force(A, S, i, n, L, nc, fx, fy, fz, e, np);
+    replica_forces(A, S, n, L, nc, [&](int i, float fx, float fy, float fz, float e, int np) {
         A.vx[off + i] += hm * (double)fx;
         A.vy[off + i] += hm * (double)fy;
         A.vz[off + i] += hm * (double)fz;
         esum += (double)e;
         nsum += (double)np;
-    }
+    });
     if (u_out) {
         block_sum3(esum, nsum, unused);
         *u_out = 0.5 * esum;
@@ -227,7 +284,7 @@ __device__ __forceinline__ void force_kick(const HmcArgs &A, const Smem &S, int 
     }
 }
 
-__global__ void __launch_bounds__(HMC_TPB, 1) k_hmc(HmcArgs A) {
+__global__ void __launch_bounds__(HMC_TPB, HMC_MINB) k_hmc(HmcArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem S;
     S.pos = (float4 *)smem_raw;
@@ -371,16 +428,14 @@ __device__ __forceinline__ void siman_forces(const SimanArgs &A, const HmcArgs &
                                              double L, int nc, double &u, double &np) {
     const int total = A.total;
     double esum = 0.0, nsum = 0.0, unused = 0.0;
-    for (int i = threadIdx.x; i < n; i += HMC_TPB) {
-        float fx, fy, fz, e;
-        int cnt;
-        atom_force(H, S, i, n, L, nc, fx, fy, fz, e, cnt);
+    replica_forces(H, S, n, L, nc, [&](int i, float fx, float fy, float fz, float e, int cnt) {
         A.f[off + i] = (double)fx;
         A.f[total + off + i] = (double)fy;
         A.f[2 * (size_t)total + off + i] = (double)fz;
         esum += (double)e;
         nsum += (double)cnt;
-    }
+    });
+    __syncthreads();
     block_sum3(esum, nsum, unused);
     u = 0.5 * esum;
     np = 0.5 * nsum;
@@ -456,7 +511,7 @@ __device__ double siman_nh_solve(const SimanArgs &A, int off, int n, const doubl
 // One block runs whole replicas (largest first, from a work counter): every stage of the
 // schedule is velinit at T, forces, n_tries vver_nh_3 steps with one inner step (a
 // one-site fluid has no short forces) and the thermostat reset.
-__global__ void __launch_bounds__(HMC_TPB, 1) k_siman_batch(SimanArgs A) {
+__global__ void __launch_bounds__(HMC_TPB, HMC_MINB) k_siman_batch(SimanArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem S;
     S.pos = (float4 *)smem_raw;
