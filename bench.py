@@ -91,6 +91,9 @@ def parse():
     ap.add_argument("--cpu-k-stride", type=int, default=400)
     ap.add_argument("--md-dt-sweep", action="store_true",
                     help="print the NVE drift of the water system against the outer time step and exit")
+    ap.add_argument("--nve-drift", action="store_true",
+                    help="print a long small-step NVE drift run of the 216-water Wolf system on the mixed "
+                         "and FP64 paths and exit")
     return ap.parse_args()
 
 
@@ -306,6 +309,53 @@ def md_extras(system, split_r, precision, device, steps=10, equil_steps=1000, nv
     out["note"] = ("device-resident: positions, velocities and thermostat scalars stay in HBM; timed with the "
                    "wall clock around mg_md_run (host copies of the start and end included); drift from a "
                    "linear fit of ukin + uinter + uintra over the NVE run after the NVT equilibration")
+    return out
+
+
+def nve_drift(device=0, dt_fs=0.25, equil_steps=4000, steps=160000):
+    """Energy drift of plain velocity-Verlet NVE on the 216-water Wolf system (648 sites,
+    rc 9 A, alpha 0.2/A) at a small step, long enough to resolve 1e-4 kT/ns/atom: one state
+    equilibrated by Nose-Hoover NVT at 298 K (tau 100 fs), then `steps` NVE steps on the
+    mixed path and, from the same state, on the FP64 path. The difference of the two
+    energy series isolates what the mixed precision adds."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import Engine
+    from mspms2_gb300.system import md_params, time_base
+    s = configs.water_c1()
+    s.delt_fs, s.nstep_inner, s.treq_K = dt_fs, 1, 298.0
+    md = md_params(s)
+    tau = 100.0 / time_base(s)
+    md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
+    m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
+    v -= (v * m).sum(1, keepdims=True) / m.sum()
+
+    def series(lg):
+        return lg[:, 0] + lg[:, 1] + lg[:, 2]  # ukin + uinter + uintra
+
+    def drift(h):
+        slope = float(np.polyfit(np.arange(len(h)) * dt_fs, h, 1)[0])  # energy per fs
+        return slope * 1e6 / (md["treq"] * s.natom)
+
+    out = {"workload": "water_c1 (216 SPC/Fw, Wolf)", "dt_fs": dt_fs, "steps": steps,
+           "ps": steps * dt_fs * 1e-3, "integrator": "velocity Verlet (vver), NVE"}
+    with Engine(s, precision="mixed", device=device) as eng:
+        md["scheme"] = 1
+        pos, vel, st, _ = eng.md_run(equil_steps, md, v)
+        md["scheme"] = 0
+        t0 = time.perf_counter()
+        _, _, _, lg = eng.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
+        out["wall_s_mixed"] = time.perf_counter() - t0
+    with Engine(s, precision="fp64", device=device) as e64:
+        t0 = time.perf_counter()
+        _, _, _, lg64 = e64.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
+        out["wall_s_fp64"] = time.perf_counter() - t0
+    h, h64 = series(lg), series(lg64)
+    out.update({"drift_kT_per_ns_per_atom_mixed": drift(h), "drift_kT_per_ns_per_atom_fp64": drift(h64),
+                "drift_kT_per_ns_per_atom_mixed_minus_fp64": drift(h - h64),
+                "rms_fluctuation_kT_per_atom_mixed": float(np.std(h)) / (md["treq"] * s.natom),
+                "resolution_kT_per_ns_per_atom": float(np.std(h)) / (md["treq"] * s.natom) / (steps * dt_fs * 1e-6)})
     return out
 
 
@@ -839,6 +889,12 @@ def main():
         build.build()
         if rank == 0:
             print(json.dumps(md_dt_sweep(args.precision, local_rank)), flush=True)
+        return 0
+    if args.nve_drift:
+        from mspms2_gb300 import build
+        build.build()
+        if rank == 0:
+            print(json.dumps(nve_drift(local_rank)), flush=True)
         return 0
     return run_ours(args, rank, world, local_rank)
 

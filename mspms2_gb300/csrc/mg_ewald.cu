@@ -36,7 +36,9 @@
 #include "mg_internal.cuh"
 
 #define EW_TILE 32      // sites per shared-memory tile in the S(k) pass
-#define EW_CH 8         // |kz| values per thread in the S(k) pass (at most)
+#ifndef EW_CH
+#define EW_CH 8         // |kz| values per thread in the S(k) pass (at most; even)
+#endif
 #define EW_TPB 128      // threads per block in the S(k) pass
 #define EW_SITES 512    // sites per block in the S(k) pass (summed in R)
 #define EW_FROWS 32     // rows staged per step in the force pass
@@ -238,11 +240,11 @@ __host__ __device__ inline void ew_for_rows(int KX, int KY, int KZ, int KS, F f)
 }
 
 // Chunks of the S(k) pass for a row with nv |kz| values: the pairs (0, 1), (2, 3), ...
-// split into ceil(pairs / 4) balanced runs, so that chunk h starts at an even |kz| and
-// holds at most EW_CH |kz| values (k0, len).
-__host__ __device__ inline int ew_nchunk(int nv) { return ((nv + 1) / 2 + 3) / 4; }
+// split into ceil(pairs / (EW_CH / 2)) balanced runs, so that chunk h starts at an even
+// |kz| and holds at most EW_CH |kz| values (k0, len).
+__host__ __device__ inline int ew_nchunk(int nv) { return ((nv + 1) / 2 + EW_CH / 2 - 1) / (EW_CH / 2); }
 __host__ __device__ inline void ew_chunk(int nv, int h, int &k0, int &len) {
-    const int np = (nv + 1) / 2, nch = (np + 3) / 4;
+    const int np = (nv + 1) / 2, nch = (np + EW_CH / 2 - 1) / (EW_CH / 2);
     const int p0 = h * (np / nch) + (h < np % nch ? h : np % nch);
     const int pl = np / nch + (h < np % nch ? 1 : 0);
     k0 = 2 * p0;
@@ -358,6 +360,14 @@ __global__ void __launch_bounds__(EW_TPB) k_sk(EwArgs A) {
         for (int s = threadIdx.x; s < tn; s += EW_TPB) sQ[s] = (R)A.q[t0 + s];
         __syncthreads();
         switch (cnt) {
+#if EW_CH >= 12
+        case 12: sk_tile<R, 12>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 11: sk_tile<R, 11>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+#endif
+#if EW_CH >= 10
+        case 10: sk_tile<R, 10>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+        case 9: sk_tile<R, 9>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
+#endif
         case 8: sk_tile<R, 8>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
         case 7: sk_tile<R, 7>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
         case 6: sk_tile<R, 6>(sX, sY, sZ, sQ, P, tn, kx, aky, ysign, kz0, pP, pM); break;
@@ -510,6 +520,12 @@ __global__ void __launch_bounds__(EW_SK_TPB, EW_SK2_MINB) k_sk2(EwArgs A) {
         const float2 *sY = sX + (size_t)(A.kx + 1) * P;
         const float *sQ = (const float *)(sY + (size_t)(A.ky + 1) * P);
         switch (np) {
+#if EW_CH >= 12
+        case 6: sk2_tile<6>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
+#endif
+#if EW_CH >= 10
+        case 5: sk2_tile<5>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
+#endif
         case 4: sk2_tile<4>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
         case 3: sk2_tile<3>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
         case 2: sk2_tile<2>(sZ, sX, sY, sQ, NPP, P, tn, kx, aky, ysign, p0, RR, II, RI, IR); break;
