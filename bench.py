@@ -22,7 +22,7 @@ matching on 4096 waters (64 snapshots, loss + gradient, checked against the FP64
 central differences); 20,000 butane in a nanotube bundle with device-generated Tasos
 tables (pair throughput, solid-fluid gather against HBM, ns/day, FP64 path); the roofline
 of the dominant kernel and a bounded CPU baseline of the reference algorithm (the oracle
-port, single thread, extrapolated from a sampled window).
+port on all host threads, extrapolated from a sampled window).
 """
 from __future__ import annotations
 
@@ -183,39 +183,60 @@ def measured_peaks():
         return {}
 
 
-def cpu_baseline(system, sample_mols, k_stride, threads_note=1):
-    """Reference algorithm (oracle port of src/frclong.c / src/frcshort.c), single thread,
-    on a sampled window: i-molecules [0, sample_mols) of the O(N^2) pair loop and every
-    k_stride-th reciprocal vector; extrapolated to the full call."""
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(system, sample_mols, k_stride, threads=1):
+    """Reference algorithm (oracle port of src/frclong.c / src/frcshort.c) on a sampled
+    window, extrapolated to the full call: i-molecules [0, sample_mols) of the O(N^2) pair
+    loop and every k_stride-th reciprocal vector. With threads > 1 the pair rows are split
+    into contiguous ranges of equal pair count and the sampled k-vectors are dealt round
+    robin, one oracle call per thread (the C oracle keeps no global state and ctypes drops
+    the GIL for the call); each part is timed by its wall clock."""
+    from concurrent.futures import ThreadPoolExecutor
     from oracle.pyoracle import Oracle, OrcWindow
     o = Oracle(system)
     M = system.nmole
-    w_pairs = OrcWindow(0, sample_mols, 1 << 30, 1)   # pair window, ~no k-space, no intra
-    t0 = time.perf_counter()
-    o.frclong(window=w_pairs)
-    t_pairs = time.perf_counter() - t0
-    w_k = OrcWindow(M, M + 1, k_stride, 1)            # no pairs, strided k-space
-    t0 = time.perf_counter()
-    o.frclong(window=w_k)
-    t_k = time.perf_counter() - t0
-    w_intra = OrcWindow(M, M + 1, 1 << 30, 0)         # intra + self terms only
-    t0 = time.perf_counter()
-    o.frclong(window=w_intra)
-    t_intra = time.perf_counter() - t0
+    rows = min(sample_mols, M)
+    T = max(1, int(threads))
+    # pair rows: split points at equal shares of sum_{i<rows} (M-1-i)
+    cum = np.cumsum([M - 1 - i for i in range(rows)])
+    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * (t + 1) / T)) + 1 for t in range(T - 1)] + [rows]
+    cuts = sorted(set(min(max(c, 0), rows) for c in cuts))
+    w_pairs = [OrcWindow(a, b, 1 << 30, 1, 0) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+    w_k = [OrcWindow(M, M + 1, k_stride * T, 1, t * k_stride) for t in range(T)]
+
+    def wall(windows):
+        t0 = time.perf_counter()
+        if len(windows) == 1:
+            o.frclong(window=windows[0])
+        else:
+            with ThreadPoolExecutor(len(windows)) as ex:
+                list(ex.map(lambda w: o.frclong(window=w), windows))
+        return time.perf_counter() - t0
+
+    t_pairs = wall(w_pairs)                           # pair window, ~no k-space, no intra
+    t_k = wall(w_k)                                   # no pairs, strided k-space
+    t_intra = wall([OrcWindow(M, M + 1, 1 << 30, 0, 0)])  # intra + self terms only (serial)
     t0 = time.perf_counter()
     o.frcshort()
     t_short = time.perf_counter() - t0
     # examined molecule pairs: sampled rows vs the whole upper triangle
-    sample = sum(M - 1 - i for i in range(min(sample_mols, M)))
+    sample = int(cum[-1]) if rows else 0
     total = M * (M - 1) // 2
     kx, ky, kz = system.kmax
     kfull = sum(1 for a in range(-kx, kx + 1) for b in range(-ky, ky + 1) for c in range(-kz, kz + 1)
                 if 0 < a * a + b * b + c * c <= system.ksqmax)
     ksample = (kfull + k_stride - 1) // k_stride
     t_full = t_pairs * total / max(sample, 1) + max(t_k - t_intra, 0.0) * kfull / max(ksample, 1) + t_intra + t_short
-    return {"t_step_s": t_full, "t_sampled_s": t_pairs + t_k + t_intra + t_short,
+    return {"t_step_s": t_full, "t_sampled_s": t_pairs + t_k + t_intra + t_short, "threads": T,
             "sample": f"i-molecules 0..{sample_mols} of {M} in the O(N^2) pair loop, every {k_stride}th of "
-                      f"{kfull} k-vectors, full intra/bonded; extrapolated to one full call"}
+                      f"{kfull} k-vectors, full intra/bonded; {T} thread(s) (pair rows split by pair "
+                      f"count, sampled k-vectors dealt round robin); extrapolated to one full call"}
 
 
 def run_reference(args, rank):
@@ -223,13 +244,15 @@ def run_reference(args, rank):
         return 0
     system = make_system(args.workload)
     npairs = pairs_in_cutoff(system)
+    threads = host_threads()
+    kstride = max(1, args.cpu_k_stride // threads)
     vals = []
     for _ in range(args.warmup):
-        cpu_baseline(system, max(8, args.cpu_sample_mols // 8), args.cpu_k_stride * 8)
+        cpu_baseline(system, max(8, args.cpu_sample_mols // 8), kstride * 8, threads)
     t0 = time.perf_counter()
     last = None
     for _ in range(args.steps):
-        last = cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
+        last = cpu_baseline(system, args.cpu_sample_mols * threads, kstride, threads)
         vals.append(npairs / last["t_step_s"])
     wall = time.perf_counter() - t0
     value = statistics.mean(vals)
@@ -238,7 +261,7 @@ def run_reference(args, rank):
             "ms_per_step": 1e3 * last["t_step_s"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "sites": system.natom, "pairs_in_cutoff": npairs},
-            "cpu_baseline": {"value": value, "unit": "pair-interactions/s", "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
                              "sample": last["sample"], "host_cores": os.cpu_count()},
             "e2e": {"value": value, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
@@ -814,8 +837,9 @@ def run_ours(args, rank, world, local_rank):
         extras["derivatives"] = adjoint_extras(system, args.precision, local_rank)
         extras["force_matching"] = force_matching_extras(local_rank)
         extras["c5_butane_tubes"] = c5_extras(local_rank)
-        cpu =cpu_baseline(system, args.cpu_sample_mols, args.cpu_k_stride)
-        extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": 1,
+        threads = host_threads()
+        cpu = cpu_baseline(system, args.cpu_sample_mols * threads, max(1, args.cpu_k_stride // threads), threads)
+        extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": threads,
                                   "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],
                                   "host_cores": os.cpu_count()}
 

@@ -483,6 +483,7 @@ static void ewald_kspace(const orc_system *s, const double *x, const double *y, 
         q[i] = s->sp[sp].charge[rel];
     }
     int stride = (w && w->k_stride > 1) ? w->k_stride : 1;
+    int koff = (w && stride > 1 && w->k_offset > 0) ? w->k_offset % stride : 0;
     long long kcount = 0;
     double ufourier = 0.0;
     for (int kx = -p->kmax[0]; kx <= p->kmax[0]; kx++)
@@ -490,7 +491,7 @@ static void ewald_kspace(const orc_system *s, const double *x, const double *y, 
             for (int kz = -p->kmax[2]; kz <= p->kmax[2]; kz++) {
                 int ksq = kx * kx + ky * ky + kz * kz;
                 if (!(ksq <= p->ksqmax && ksq != 0)) continue;
-                if ((kcount++ % stride) != 0) continue;
+                if ((kcount++ % stride) != koff) continue;
                 double rkx = p->twopi_lx * kx, rky = p->twopi_ly * ky, rkz = p->twopi_lz * kz;
                 double rksq = rkx * rkx + rky * rky + rkz * rkz;
                 double kvec = exp(-p->bfactor_ewald * rksq) / rksq;

@@ -60,6 +60,7 @@ typedef struct orc_window {
     int imol_begin, imol_end;
     int k_stride;
     int skip_intra;
+    int k_offset; /* with k_stride > 1: the k-vectors numbered k_offset mod k_stride */
 } orc_window;
 
 int orc_natom(const orc_system *s);

@@ -51,7 +51,7 @@ class OrcSystem(C.Structure):
 
 class OrcWindow(C.Structure):
     _fields_ = [("imol_begin", C.c_int), ("imol_end", C.c_int), ("k_stride", C.c_int),
-                ("skip_intra", C.c_int)]
+                ("skip_intra", C.c_int), ("k_offset", C.c_int)]
 
 
 def build() -> str:

@@ -60,3 +60,23 @@ def test_derived_params_match_reference(case):
         if (s.charge_type == 3 and k == "kappa") or (s.charge_type == 0 and k in ("kappa", "coulomb_prefactor")):
             continue  # the reference only sets these in init_charge (src/initvars.c:397-472)
         assert want == pytest.approx(ref[k], rel=1e-15, abs=0.0), (case, k)
+
+
+def test_sampling_windows_partition_the_call():
+    """The sampled windows the CPU baseline times in parallel cover the whole call: pair
+    rows split at any point and k-vectors dealt round robin (k_offset) sum to the
+    unwindowed forces and reciprocal energy. Every window with a huge k_stride still
+    evaluates the first k-vector, which is taken out once per such window."""
+    from oracle.pyoracle import OrcWindow
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    o = Oracle(s)
+    M = s.nmole
+    full, e_full, _ = o.frclong()
+    k0 = o.frclong(window=OrcWindow(M, M + 1, 1 << 30, 1, 0))[0]
+    intra = o.frclong(window=OrcWindow(M, M + 1, 1 << 30, 0, 0))[0] - k0
+    pairs = sum(o.frclong(window=OrcWindow(a, b, 1 << 30, 1, 0))[0] - k0
+                for a, b in ((0, 37), (37, 101), (101, M)))
+    ks = [o.frclong(window=OrcWindow(M, M + 1, 3, 1, t)) for t in range(3)]
+    kspace = sum(k[0] for k in ks)
+    assert sum(k[1]["ufourier"] for k in ks) == pytest.approx(e_full["ufourier"], rel=1e-12)
+    assert _close(pairs + kspace + intra, full, rtol=1e-11)
