@@ -763,7 +763,9 @@ def run_ours(args, rank, world, local_rank):
         dist.barrier()
     clk = clocks.stop()
     st = eng.stats()
-    npairs = st["pairs_within_cutoff"]
+    # the numerator both arms share: pairs inside the cutoff by FP64 distance (the engine's
+    # own count, from FP32 distances, can differ by a few pairs at the cutoff shell)
+    npairs = pairs_in_cutoff(system)
     ms_step = statistics.mean(times)
     if dist:
         t = torch.tensor([ms_step], device="cuda")
@@ -873,6 +875,7 @@ def run_ours(args, rank, world, local_rank):
                        "rc_A": system.rcutoff, "ewald_alpha": system.kappa, "kmax": list(system.kmax),
                        "ksqmax": system.ksqmax, "kvectors_half_space": kvec, "kspace_rows": nrows,
                        "kspace_row_kz": nkz, "pairs_in_cutoff": npairs,
+                       "pairs_in_cutoff_engine_fp32": st["pairs_within_cutoff"],
                        "l2": "256 MiB flush before every step; steps timed one by one with CUDA events",
                        "parallelism": f"replicas x{world}",
                        "tuning": {k: tuning[k] for k in ("cell_scale", "zcap_scale", "kforce_threads", "ms_default",

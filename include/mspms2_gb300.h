@@ -431,6 +431,11 @@ MG_API mg_status mg_get_md_graphs(const mg_ctx *ctx, int *enabled, int *last_ste
  * them, so that results are identical either way. Enabled by default. */
 MG_API mg_status mg_set_kspace_overlap(mg_ctx *ctx, int enable);
 
+/* Structure factors on the tensor cores (mixed precision, KMAXZ <= 30): the sum over sites
+ * as TF32 MMAs with a 3-term split product and FP32 accumulation; off, the CUDA-core FP32
+ * pass. Enabled by default; no effect on the FP64 path. The two agree to FP32 rounding. */
+MG_API mg_status mg_set_kspace_tensor(mg_ctx *ctx, int enable);
+
 /* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
 /* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
  * first stage whose T is below t_min (the reference tests T < t_min after the stage). A

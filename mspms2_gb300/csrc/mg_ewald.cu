@@ -580,6 +580,245 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
+// ---------------------------------------------------------------------------------
+// Tensor-core structure factors (FP32 path): the site sum as a GEMM on tcgen05
+// ---------------------------------------------------------------------------------
+// For a tile of 64 rows (taken in force order, longest kzmax first) and a block of
+// EW_MMA_SITES sites, D[m][n] = sum_s A[m][s] B[n][s] with
+//   A[r][s] = Re(q_s X^kx_s Y^ky_s), A[64 + r][s] = Im(...)        (M = 128)
+//   B[kz][s] = Re Z^kz_s, B[H + kz][s] = Im Z^kz_s, H = 16 or 32     (N = 2H)
+// so that lane r of D holds RR (columns kz) and RI (H + kz) and lane 64 + r holds IR and
+// II, and S(+kz) = (RR - II, RI + IR), S(-kz) = (RR + II, IR - RI) as in k_sk2. A is made
+// per chunk of 32 sites by the CUDA cores from the phase tables, B from the Z pairs; both
+// go to shared memory as TF32 hi + lo pairs (round to nearest, then the exact remainder
+// rounded again) in the canonical K-major 128-byte-swizzled layout, and one thread issues
+// kind::tf32 MMAs for hi*hi + hi*lo + lo*hi (the 3-term split product keeps the FP32
+// operands' accuracy; the dropped lo*lo term is below 2^-22 relative). Accumulation is
+// FP32 in tensor memory (64 columns per CTA); partials per site block go to k_sk_reduce,
+// which sums them in fixed order. Two chunk stages: the CUDA cores fill stage c & 1 while
+// the tensor core works on the other; a tcgen05.commit per chunk signals an mbarrier that
+// guards the stage's reuse. Every wait is bounded; on a timeout the CTA records
+// MG_FLAG_WAIT_TIMEOUT, still frees its tensor memory and returns.
+#define EW_MMA_ROWS 64     // rows per CTA (two accumulator lanes each)
+#ifndef EW_MMA_SITES
+#define EW_MMA_SITES 1024  // sites per CTA (a multiple of EW_SITES)
+#endif
+#define EW_MMA_TPB 256
+#define EW_MMA_KC 32       // sites per chunk: one 128-byte TF32 row of the swizzled layout
+#define EW_MMA_MAXKZ 30    // largest KMAXZ the pass takes (Z pairs within 32 columns)
+#define EW_MMA_STAGE 49152 // A hi, A lo (16 KB each), B hi, B lo (8 KB each)
+#define EW_MMA_SMEM (2 * EW_MMA_STAGE + 64 + 1024)
+#define EW_MMA_WAIT (1 << 20)
+
+// byte offset of TF32 element (m, k), k < 32, in a K-major tile with 128-byte rows and the
+// 128-byte swizzle (16-byte chunk index XOR row mod 8; 8-row groups of 1024 bytes)
+__device__ __forceinline__ unsigned sw128(int m, int k) {
+    return (unsigned)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 2) ^ m) & 7) << 4) + (k & 3) * 4);
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
+__device__ __forceinline__ unsigned long long umma_desc(unsigned saddr) {
+    return (unsigned long long)((saddr >> 4) & 0x3FFFu) | (1ull << 16) | ((unsigned long long)(1024 >> 4) << 32) |
+           (1ull << 46) | (2ull << 61);
+}
+
+// instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major, M = 128, N = n
+__host__ __device__ constexpr unsigned umma_idesc_tf32(int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void sts32(unsigned a, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (int i = 0; i < EW_MMA_WAIT; i++) {
+        unsigned ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void umma_tf32(unsigned d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                          unsigned acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *flags) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned raw = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned base = (raw + 1023u) & ~1023u;  // the swizzled tiles need 1024-byte alignment
+    unsigned char *gbase = smem_raw + (base - raw);
+    const unsigned bar0 = base + 2 * EW_MMA_STAGE, tslot = bar0 + 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pos0 = blockIdx.x * EW_MMA_ROWS;
+    const int H = A.rows[A.forder[pos0]].z + 1 <= 16 ? 16 : 32;  // rows sorted by kzmax, longest first
+    const int NPP = min(ew_zpairs(A.kz), (A.rows[A.forder[pos0]].z + 2) / 2);
+    const unsigned idesc = umma_idesc_tf32(2 * H);
+
+    // zero both stages (rows no chunk writes stay zero), barriers, tensor memory
+    for (int i = threadIdx.x; i < 2 * EW_MMA_STAGE / 16; i += EW_MMA_TPB)
+        ((uint4 *)gbase)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar0), "r"(1) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar0 + 8), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot), "r"(64) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *(volatile unsigned *)(gbase + (tslot - base));
+
+    // this warp's 8 rows of the tile
+    int rkx[8], raky[8];
+    float rys[8];
+    bool rok[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int pos = pos0 + warp * 8 + i;
+        rok[i] = pos < A.nrows;
+        const int4 r = rok[i] ? A.rows[A.forder[pos]] : make_int4(0, 0, 0, 0);
+        rkx[i] = r.x;
+        raky[i] = r.y < 0 ? -r.y : r.y;
+        rys[i] = r.y < 0 ? -1.f : 1.f;
+    }
+    const float2 *tab = (const float2 *)A.tab;
+    const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
+    const float4 *tZP = (const float4 *)(tab + ew_zoff(A.kx, A.ky, A.n));
+    const int a_begin = blockIdx.y * EW_MMA_SITES, a_end = min(A.n, a_begin + EW_MMA_SITES);
+    const int nch = (a_end - a_begin + EW_MMA_KC - 1) / EW_MMA_KC;
+    bool timeout = false;
+    for (int c = 0; c < nch; c++) {
+        const int b = c & 1;
+        const unsigned st = base + b * EW_MMA_STAGE;
+        bool to = false;
+        if (c >= 2) to = !mbar_wait(bar0 + 8 * b, ((c - 2) >> 1) & 1);
+        if (__syncthreads_or(to)) {
+            timeout = true;
+            break;
+        }
+        const int s = a_begin + c * EW_MMA_KC + lane;
+        const bool ok = s < a_end;
+        const float q = ok ? A.qf[s] : 0.f;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (!rok[i]) continue;
+            const int r = warp * 8 + i;
+            float2 X = make_float2(0.f, 0.f), Y = make_float2(0.f, 0.f);
+            if (ok) {
+                X = tX[(size_t)rkx[i] * A.n + s];
+                Y = tY[(size_t)raky[i] * A.n + s];
+            }
+            Y.y *= rys[i];
+            float2 Aq = cmul(X, Y);
+            Aq.x *= q;
+            Aq.y *= q;
+            const float hr = tf32_rna(Aq.x), hi = tf32_rna(Aq.y);
+            sts32(st + sw128(r, lane), hr);
+            sts32(st + 16384 + sw128(r, lane), tf32_rna(Aq.x - hr));
+            sts32(st + sw128(64 + r, lane), hi);
+            sts32(st + 16384 + sw128(64 + r, lane), tf32_rna(Aq.y - hi));
+        }
+        for (int p = warp; p < NPP; p += EW_MMA_TPB / 32) {
+            const float4 z = ok ? tZP[(size_t)p * A.n + s] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float v[4] = {z.x, z.y, z.z, z.w};
+            const int nrow[4] = {2 * p, 2 * p + 1, H + 2 * p, H + 2 * p + 1};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float h = tf32_rna(v[j]);
+                sts32(st + 32768 + sw128(nrow[j], lane), h);
+                sts32(st + 40960 + sw128(nrow[j], lane), tf32_rna(v[j] - h));
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int k = 0; k < EW_MMA_KC / 8; k++) {
+                const unsigned long long ah = umma_desc(st + 32 * k), al = umma_desc(st + 16384 + 32 * k);
+                const unsigned long long bh = umma_desc(st + 32768 + 32 * k), bl = umma_desc(st + 40960 + 32 * k);
+                umma_tf32(tmem, ah, bh, idesc, (c > 0 || k > 0) ? 1u : 0u);
+                umma_tf32(tmem, ah, bl, idesc, 1u);
+                umma_tf32(tmem, al, bh, idesc, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar0 + 8 * b)
+                         : "memory");
+        }
+    }
+    if (!timeout && nch > 0) {
+        const bool to = !mbar_wait(bar0 + 8 * ((nch - 1) & 1), ((nch - 1) >> 1) & 1);
+        timeout = __syncthreads_or(to);
+    }
+    if (timeout) {
+        // let issued MMAs finish (bounded) before the tensor memory is released
+        if (threadIdx.x == 0 && flags) atomicOr(flags, MG_FLAG_WAIT_TIMEOUT);
+        for (int c = max(0, nch - 2); c < nch; c++) mbar_wait(bar0 + 8 * (c & 1), (c >> 1) & 1);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    float *D = (float *)gbase;  // 128 x 65 floats over stage 0 (all MMAs have completed)
+    if (!timeout && warp < 4 && nch > 0) {
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) {
+            if (cc * 16 >= 2 * H) break;
+            unsigned v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                : "r"(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(cc * 16)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 16; j++) D[(warp * 32 + lane) * 65 + cc * 16 + j] = __uint_as_float(v[j]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64) : "memory");
+    if (timeout) return;
+    float *out = (float *)A.spart + (size_t)blockIdx.y * A.nslots * 2;
+    for (int idx = threadIdx.x; idx < EW_MMA_ROWS * 32; idx += EW_MMA_TPB) {
+        const int r = idx >> 5, a = idx & 31, pos = pos0 + r;
+        if (pos >= A.nrows) break;
+        const int row = A.forder[pos];
+        const int4 rw = A.rows[row];
+        if (a > rw.z) continue;
+        float RR = 0.f, RI = 0.f, IR = 0.f, II = 0.f;
+        if (nch > 0) {
+            RR = D[r * 65 + a];
+            RI = D[r * 65 + H + a];
+            IR = D[(64 + r) * 65 + a];
+            II = D[(64 + r) * 65 + H + a];
+        }
+        const int sp = A.row_slot[row] + 2 * a, sm = sp + 1;
+        out[2 * sp] = RR - II;
+        out[2 * sp + 1] = RI + IR;
+        const bool has_minus = (a > 0) && !rw.w;
+        out[2 * sm] = has_minus ? RR + II : 0.f;
+        out[2 * sm + 1] = has_minus ? IR - RI : 0.f;
+    }
+}
+
 // S(k) from the partials: a block of EW_RED_PARTS * 256 threads takes 256 slots; part p
 // sums site blocks [p nblk / PARTS, (p + 1) nblk / PARTS) in order (FP32 hi + lo on the
 // FP32 path, FP64 on the FP64 path) and the parts are added in order in FP64 (fixed order
@@ -1290,6 +1529,11 @@ mg_status mg_ewald_join(mg_ctx *c, double *fl) {
     return MG_OK;
 }
 
+bool mg_ewald_sk_tensor(const mg_ctx *c) {
+    static_assert(EW_MMA_SITES % EW_SITES == 0, "tensor-core site blocks must cover whole S(k) partial blocks");
+    return c->opt.precision != MG_PREC_FP64 && c->kspace_tensor && std::max(c->kmaxz, 1) <= EW_MMA_MAXKZ;
+}
+
 bool mg_ewald_horner_force(const mg_ctx *c) {
     const int maxa = c->h_chunk_kz.empty() ? 1 : c->h_chunk_kz[0] + 1;
     return c->opt.precision == MG_PREC_FP64 || maxa > EW_FMM_MAXA;
@@ -1339,10 +1583,20 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     A.coul = p.coulomb_prefactor;
     A.rows_e = (double *)c->d_epart.p;
     A.f = fl;
-    if (fp64)
+    int nblk_red = nblk;
+    if (fp64) {
         MG_CUDA(launch_sk<double>(A, nblk, s));
-    else
+    } else if (mg_ewald_sk_tensor(c)) {
+        k_qcast<<<(n + 255) / 256, 256, 0, s>>>(n, A.q, A.qf);
+        A.forder = (const int *)c->d_row_slot.p + c->nrows + c->nslots;
+        nblk_red = (n + EW_MMA_SITES - 1) / EW_MMA_SITES;
+        MG_CUDA(cudaFuncSetAttribute(k_sk_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, EW_MMA_SMEM));
+        const dim3 grid((unsigned)((c->nrows + EW_MMA_ROWS - 1) / EW_MMA_ROWS), (unsigned)nblk_red);
+        k_sk_mma<<<grid, EW_MMA_TPB, EW_MMA_SMEM, s>>>(A, (unsigned *)c->d_flags.p);
+        MG_CUDA(cudaGetLastError());
+    } else {
         MG_CUDA(launch_sk<float>(A, nblk, s));
+    }
     const int *slot_row = (const int *)c->d_row_slot.p + c->nrows;
     unsigned rblocks = (unsigned)((c->nslots + 255) / 256);
     if (c->ew_rows) {  // enqueued on its own stream: rows of its own, copied in at the join
@@ -1355,7 +1609,7 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     if (fp64)
         k_sk_reduce<double><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
     else
-        k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
+        k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk_red, slot_row);
     if (c->timing) cudaEventRecord(c->ev[4], s);
     int maxa = 1;
     for (int r = 0; r < c->nrows; r++) maxa = std::max(maxa, c->h_rows[4 * r + 2] + 1);

@@ -723,6 +723,7 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
     if (flags[0] & (MG_FLAG_LIST_OVERFLOW | MG_FLAG_COLUMN_OVERFLOW))
         return mg_fail(c, MG_ERR_CAPACITY, "neighbour-list capacity exceeded");
     if (flags[0] & MG_FLAG_NONFINITE) return mg_fail(c, MG_ERR_NONFINITE, "non-finite force");
+    if (flags[0] & MG_FLAG_WAIT_TIMEOUT) return mg_fail(c, MG_ERR_CUDA, "tensor-core S(k) pass: an on-chip wait ran out");
     return MG_OK;
 }
 
@@ -930,6 +931,12 @@ extern "C" mg_status mg_autotune(mg_ctx *c, const double *x, const double *y, co
 extern "C" mg_status mg_set_kspace_overlap(mg_ctx *c, int enable) {
     if (!c) return MG_ERR_INVALID;
     c->kspace_overlap = enable != 0;
+    return MG_OK;
+}
+
+extern "C" mg_status mg_set_kspace_tensor(mg_ctx *c, int enable) {
+    if (!c) return MG_ERR_INVALID;
+    c->kspace_tensor = enable != 0;
     return MG_OK;
 }
 

@@ -35,6 +35,7 @@
 #define MG_FLAG_COLUMN_OVERFLOW 8u
 #define MG_FLAG_IMPROPER_DEGENERATE 16u
 #define MG_FLAG_SMALL_BOX 32u  // a cluster pair needs two images: use the small-box list
+#define MG_FLAG_WAIT_TIMEOUT 64u  // a bounded on-chip wait (mbarrier) gave up
 
 // per-site flags packed next to the molecule id
 #define MG_SITE_LJ 1        // takes part in LJ (ghost type NONE)
@@ -188,6 +189,7 @@ struct mg_ctx {
     // the reciprocal-space chain runs on its own stream beside the list and pair kernels,
     // into its own force buffer and energy rows, joined before the forces are summed
     bool kspace_overlap = true;
+    bool kspace_tensor = true;  // S(k) on the tensor cores (FP32 path, KMAXZ <= 30)
     bool forked = false;          // the last evaluation ran that chain on kstream
     cudaStream_t kstream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -217,6 +219,7 @@ struct mg_ctx {
 // ---- helpers shared by host translation units --------------------------------------
 mg_status mg_fail(mg_ctx *c, mg_status code, const std::string &msg);
 bool mg_ewald_horner_force(const mg_ctx *c);  // k-space forces by the Horner pass (threads per site apply)
+bool mg_ewald_sk_tensor(const mg_ctx *c);     // S(k) by the tensor-core pass
 mg_status mg_ewald_fork(mg_ctx *c, const double *dx, const double *dy, const double *dz);
 mg_status mg_ewald_join(mg_ctx *c, double *fl);
 mg_status mg_cuda_fail(mg_ctx *c, cudaError_t e, const char *what);

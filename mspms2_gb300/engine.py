@@ -83,6 +83,7 @@ def load_library(path: str = LIB_PATH):
     lib.mg_sf_tasos_generate.argtypes = [V, I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, D]
     lib.mg_set_md_graphs.argtypes = [V, I]
     lib.mg_set_kspace_overlap.argtypes = [V, I]
+    lib.mg_set_kspace_tensor.argtypes = [V, I]
     lib.mg_get_md_graphs.argtypes = [V, C.POINTER(I), C.POINTER(I)]
     lib.mg_autotune.argtypes = [V, _dp, _dp, _dp, I, C.POINTER(capi.MgTuning)]
     lib.mg_set_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
@@ -299,6 +300,10 @@ class Engine:
     def set_kspace_overlap(self, enable: bool) -> None:
         """Reciprocal space on a second stream beside the list and pairs (default) or in line."""
         self._check(self.lib.mg_set_kspace_overlap(self.ctx, 1 if enable else 0))
+
+    def set_kspace_tensor(self, enable: bool) -> None:
+        """Structure factors on the tensor cores (default) or on the CUDA cores (mixed path)."""
+        self._check(self.lib.mg_set_kspace_tensor(self.ctx, 1 if enable else 0))
 
     def set_md_graphs(self, enable: bool) -> None:
         """Whole integrator steps as a replayed CUDA graph (default) or step by step."""

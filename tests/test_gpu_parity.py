@@ -244,3 +244,28 @@ def test_kspace_overlap_is_bit_identical(case):
     for a, b in zip(out[True], out[False]):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
         assert a[2] == b[2]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kmax,ksqmax", [((12, 12, 12), 144), ((9, 7, 30), 400)])
+def test_sk_tensor_pass_matches_cuda_core_pass(kmax, ksqmax):
+    """Structure factors on the tensor cores (TF32 3-term split MMAs, FP32 accumulation in
+    tensor memory) against the CUDA-core FP32 pass and the FP64 path. 11^3 waters = 3993
+    sites: four site blocks, the last one ragged within a 32-site chunk; 12^3 rows of
+    KSQMAX 144 give tiles with kzmax above and below 16 (both MMA widths), and KMAXZ 30 is
+    the largest the pass takes."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.system import ELEC_EWALD
+    s = configs.water_box(11, 34.0, 5, ELEC_EWALD, 0.3, 9.0, kmax=kmax[0], ksqmax=ksqmax)
+    s.kmax = kmax
+    out = {}
+    for key, prec, tensor in (("tc", "mixed", True), ("cc", "mixed", False), ("fp64", "fp64", True)):
+        with Engine(s, precision=prec) as eng:
+            eng.set_kspace_tensor(tensor)
+            out[key] = eng.compute(terms=TERMS_LONG)
+    f64, e64 = out["fp64"][0], out["fp64"][2]
+    for key in ("tc", "cc"):
+        assert rel(out[key][0], f64) <= TOL["mixed"], (key, rel(out[key][0], f64))
+        assert abs(out[key][2]["ufourier"] - e64["ufourier"]) <= 2e-6 * abs(e64["ufourier"]), key
+    # the two FP32 passes differ by rounding only
+    assert rel(out["tc"][0], out["cc"][0]) <= 2e-6, rel(out["tc"][0], out["cc"][0])
