@@ -593,9 +593,13 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 // go to shared memory as TF32 hi + lo pairs (round to nearest, then the exact remainder
 // rounded again) in the canonical K-major 128-byte-swizzled layout, and one thread issues
 // kind::tf32 MMAs for hi*hi + hi*lo + lo*hi (the 3-term split product keeps the FP32
-// operands' accuracy; the dropped lo*lo term is below 2^-22 relative). Accumulation is
-// FP32 in tensor memory (64 columns per CTA); partials per site block go to k_sk_reduce,
-// which sums them in fixed order. Two chunk stages: the CUDA cores fill stage c & 1 while
+// operands' accuracy; the dropped lo*lo term is below 2^-22 relative). The tensor core's
+// FP32 accumulation does not round to nearest (over a 1024-site block it shrank |S| by a
+// few 1e-6, the Fourier energy by 1e-5), so each group of EW_MMA_GROUP chunks accumulates
+// in one of two tensor-memory accumulators and is then added, by the CUDA cores in
+// round-to-nearest FP32, to a running total kept in tensor memory: the truncation then
+// acts on 64-site partials of either sign and averages out. Partials per site block go to
+// k_sk_reduce, which sums them in fixed order. Two chunk stages: the CUDA cores fill stage c & 1 while
 // the tensor core works on the other; a tcgen05.commit per chunk signals an mbarrier that
 // guards the stage's reuse. Every wait is bounded; on a timeout the CTA records
 // MG_FLAG_WAIT_TIMEOUT, still frees its tensor memory and returns.
@@ -609,6 +613,10 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 #define EW_MMA_STAGE 49152 // A hi, A lo (16 KB each), B hi, B lo (8 KB each)
 #define EW_MMA_SMEM (2 * EW_MMA_STAGE + 64 + 1024)
 #define EW_MMA_WAIT (1 << 20)
+#ifndef EW_MMA_GROUP
+#define EW_MMA_GROUP 2     // chunks summed in one tensor-memory accumulator before each drain
+#endif
+#define EW_MMA_TCOLS 256   // tensor-memory columns per CTA: two group accumulators and the total
 
 // byte offset of TF32 element (m, k), k < 32, in a K-major tile with 128-byte rows and the
 // 128-byte swizzle (16-byte chunk index XOR row mod 8; 8-row groups of 1024 bytes)
@@ -637,6 +645,11 @@ __device__ __forceinline__ void sts32(unsigned a, float v) {
     asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 
+__device__ __forceinline__ void sts128(unsigned a, const float (&v)[4]) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
+                 : "memory");
+}
+
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
     for (int i = 0; i < EW_MMA_WAIT; i++) {
         unsigned ok;
@@ -656,6 +669,28 @@ __device__ __forceinline__ void umma_tf32(unsigned d, unsigned long long a, unsi
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
         "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(unsigned addr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(addr)
+        : "memory");
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void tmem_st16(unsigned addr, const float (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16};" ::"r"(addr),
+        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+        "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
         : "memory");
 }
 
@@ -680,86 +715,175 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot), "r"(64) : "memory");
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot),
+                     "r"(EW_MMA_TCOLS)
+                     : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = *(volatile unsigned *)(gbase + (tslot - base));
-
-    // this warp's 8 rows of the tile
-    int rkx[8], raky[8];
-    float rys[8];
-    bool rok[8];
+    // group accumulator g & 1 at columns 64 (g & 1); the running total at columns 128..
+    // (lane quarter warp & 3; warps w and w + 4 drain the two column halves)
+    const unsigned tlane = tmem + ((unsigned)((warp & 3) * 32) << 16);
+    int ndrained = 0;
+    auto drain = [&](int g) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int piece = 0; piece < H / 16; piece++) {
+            const unsigned col = (unsigned)((warp >> 2) * H + piece * 16);
+            float v[16], t[16];
+            tmem_ld16(tlane + 64u * (unsigned)(g & 1) + col, v);
+            if (ndrained > 0) tmem_ld16(tlane + 128u + col, t);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const int pos = pos0 + warp * 8 + i;
-        rok[i] = pos < A.nrows;
-        const int4 r = rok[i] ? A.rows[A.forder[pos]] : make_int4(0, 0, 0, 0);
-        rkx[i] = r.x;
-        raky[i] = r.y < 0 ? -r.y : r.y;
-        rys[i] = r.y < 0 ? -1.f : 1.f;
+            for (int j = 0; j < 16; j++) t[j] = ndrained > 0 ? t[j] + v[j] : v[j];
+            tmem_st16(tlane + 128u + col, t);
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        }
+        ndrained++;
+    };
+
+    // A: lane (g = lane & 7, i0 = lane >> 3) makes sites 4g..4g+3 of the warp's rows i0 and
+    // i0 + 4, one 16-byte swizzle chunk per row and operand; B: thread t < 8 NPP makes Z
+    // pair t >> 3 for sites 4 (t & 7)..+3. The loads of chunk c + 1 are issued before the
+    // barrier of chunk c (registers), so their latency overlaps the barrier and the wait.
+    const int g = lane & 7, i0 = lane >> 3;
+    int rkx[2], raky[2];
+    float rys[2];
+    bool rok[2];
+    unsigned aoff[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const int i = i0 + 4 * j, pos = pos0 + warp * 8 + i;
+        rok[j] = pos < A.nrows;
+        const int4 r = rok[j] ? A.rows[A.forder[pos]] : make_int4(0, 0, 0, 0);
+        rkx[j] = r.x;
+        raky[j] = r.y < 0 ? -r.y : r.y;
+        rys[j] = r.y < 0 ? -1.f : 1.f;
+        aoff[j] = (unsigned)(warp * 1024 + i * 128 + ((g ^ i) << 4));
+    }
+    const bool bwork = (int)threadIdx.x < 8 * NPP;
+    const int bp = threadIdx.x >> 3;
+    unsigned boff[4];
+    {
+        const int nrow[4] = {2 * bp, 2 * bp + 1, H + 2 * bp, H + 2 * bp + 1};
+#pragma unroll
+        for (int j = 0; j < 4; j++) boff[j] = (unsigned)((nrow[j] >> 3) * 1024 + (nrow[j] & 7) * 128 + ((g ^ nrow[j]) & 7) * 16);
     }
     const float2 *tab = (const float2 *)A.tab;
     const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
     const float4 *tZP = (const float4 *)(tab + ew_zoff(A.kx, A.ky, A.n));
     const int a_begin = blockIdx.y * EW_MMA_SITES, a_end = min(A.n, a_begin + EW_MMA_SITES);
     const int nch = (a_end - a_begin + EW_MMA_KC - 1) / EW_MMA_KC;
+    const bool even = (A.n & 1) == 0;  // 16-byte loads of two float2 table entries
+    float2 X[2][4], Y[2][4];
+    float Q[4];
+    float4 Z[4];
+    auto load = [&](int c) {
+        const int s0 = a_begin + c * EW_MMA_KC + 4 * g;
+        const bool full = s0 + 3 < a_end;
+        if (full) {
+            const float4 t = *(const float4 *)(A.qf + s0);
+            Q[0] = t.x, Q[1] = t.y, Q[2] = t.z, Q[3] = t.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++) Q[j] = s0 + j < a_end ? A.qf[s0 + j] : 0.f;
+        }
+#pragma unroll
+        for (int jr = 0; jr < 2; jr++) {
+            if (!rok[jr]) continue;
+            const float2 *px = tX + (size_t)rkx[jr] * A.n + s0, *py = tY + (size_t)raky[jr] * A.n + s0;
+            if (full && even) {
+                const float4 x0 = *(const float4 *)px, x1 = *(const float4 *)(px + 2);
+                const float4 y0 = *(const float4 *)py, y1 = *(const float4 *)(py + 2);
+                X[jr][0] = make_float2(x0.x, x0.y), X[jr][1] = make_float2(x0.z, x0.w);
+                X[jr][2] = make_float2(x1.x, x1.y), X[jr][3] = make_float2(x1.z, x1.w);
+                Y[jr][0] = make_float2(y0.x, y0.y), Y[jr][1] = make_float2(y0.z, y0.w);
+                Y[jr][2] = make_float2(y1.x, y1.y), Y[jr][3] = make_float2(y1.z, y1.w);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const bool in = s0 + j < a_end;
+                    X[jr][j] = in ? px[j] : make_float2(0.f, 0.f);
+                    Y[jr][j] = in ? py[j] : make_float2(0.f, 0.f);
+                }
+            }
+        }
+        if (bwork) {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                Z[j] = s0 + j < a_end ? tZP[(size_t)bp * A.n + s0 + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    if (nch > 0) load(0);
     bool timeout = false;
     for (int c = 0; c < nch; c++) {
         const int b = c & 1;
         const unsigned st = base + b * EW_MMA_STAGE;
         bool to = false;
         if (c >= 2) to = !mbar_wait(bar0 + 8 * b, ((c - 2) >> 1) & 1);
+        if (!to) {
+            // chunk c - 2 is complete: if it closed a group, fold that group into the total
+            // before the group two ahead reuses its accumulator
+            if (c >= 2 && (c - 2) % EW_MMA_GROUP == EW_MMA_GROUP - 1) drain((c - 2) / EW_MMA_GROUP);
+#pragma unroll
+            for (int jr = 0; jr < 2; jr++) {
+                if (!rok[jr]) continue;
+                float hr[4], lr[4], hi[4], li[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    float2 y = Y[jr][j];
+                    y.y *= rys[jr];
+                    float2 aq = cmul(X[jr][j], y);
+                    aq.x *= Q[j];
+                    aq.y *= Q[j];
+                    hr[j] = tf32_rna(aq.x);
+                    lr[j] = tf32_rna(aq.x - hr[j]);
+                    hi[j] = tf32_rna(aq.y);
+                    li[j] = tf32_rna(aq.y - hi[j]);
+                }
+                sts128(st + aoff[jr], hr);
+                sts128(st + 16384 + aoff[jr], lr);
+                sts128(st + 8192 + aoff[jr], hi);
+                sts128(st + 16384 + 8192 + aoff[jr], li);
+            }
+            if (bwork) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    float v[4], h[4], l[4];
+                    v[0] = j == 0 ? Z[0].x : j == 1 ? Z[0].y : j == 2 ? Z[0].z : Z[0].w;
+                    v[1] = j == 0 ? Z[1].x : j == 1 ? Z[1].y : j == 2 ? Z[1].z : Z[1].w;
+                    v[2] = j == 0 ? Z[2].x : j == 1 ? Z[2].y : j == 2 ? Z[2].z : Z[2].w;
+                    v[3] = j == 0 ? Z[3].x : j == 1 ? Z[3].y : j == 2 ? Z[3].z : Z[3].w;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        h[e] = tf32_rna(v[e]);
+                        l[e] = tf32_rna(v[e] - h[e]);
+                    }
+                    sts128(st + 32768 + boff[j], h);
+                    sts128(st + 40960 + boff[j], l);
+                }
+            }
+            if (c + 1 < nch) load(c + 1);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         if (__syncthreads_or(to)) {
             timeout = true;
             break;
         }
-        const int s = a_begin + c * EW_MMA_KC + lane;
-        const bool ok = s < a_end;
-        const float q = ok ? A.qf[s] : 0.f;
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            if (!rok[i]) continue;
-            const int r = warp * 8 + i;
-            float2 X = make_float2(0.f, 0.f), Y = make_float2(0.f, 0.f);
-            if (ok) {
-                X = tX[(size_t)rkx[i] * A.n + s];
-                Y = tY[(size_t)raky[i] * A.n + s];
-            }
-            Y.y *= rys[i];
-            float2 Aq = cmul(X, Y);
-            Aq.x *= q;
-            Aq.y *= q;
-            const float hr = tf32_rna(Aq.x), hi = tf32_rna(Aq.y);
-            sts32(st + sw128(r, lane), hr);
-            sts32(st + 16384 + sw128(r, lane), tf32_rna(Aq.x - hr));
-            sts32(st + sw128(64 + r, lane), hi);
-            sts32(st + 16384 + sw128(64 + r, lane), tf32_rna(Aq.y - hi));
-        }
-        for (int p = warp; p < NPP; p += EW_MMA_TPB / 32) {
-            const float4 z = ok ? tZP[(size_t)p * A.n + s] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float v[4] = {z.x, z.y, z.z, z.w};
-            const int nrow[4] = {2 * p, 2 * p + 1, H + 2 * p, H + 2 * p + 1};
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float h = tf32_rna(v[j]);
-                sts32(st + 32768 + sw128(nrow[j], lane), h);
-                sts32(st + 40960 + sw128(nrow[j], lane), tf32_rna(v[j] - h));
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned acc = tmem + 64u * (unsigned)((c / EW_MMA_GROUP) & 1);
+            const bool fresh = c % EW_MMA_GROUP == 0;
 #pragma unroll
             for (int k = 0; k < EW_MMA_KC / 8; k++) {
                 const unsigned long long ah = umma_desc(st + 32 * k), al = umma_desc(st + 16384 + 32 * k);
                 const unsigned long long bh = umma_desc(st + 32768 + 32 * k), bl = umma_desc(st + 40960 + 32 * k);
-                umma_tf32(tmem, ah, bh, idesc, (c > 0 || k > 0) ? 1u : 0u);
-                umma_tf32(tmem, ah, bl, idesc, 1u);
-                umma_tf32(tmem, al, bh, idesc, 1u);
+                umma_tf32(acc, ah, bh, idesc, (fresh && k == 0) ? 0u : 1u);
+                umma_tf32(acc, ah, bl, idesc, 1u);
+                umma_tf32(acc, al, bh, idesc, 1u);
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar0 + 8 * b)
                          : "memory");
@@ -773,28 +897,27 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
         // let issued MMAs finish (bounded) before the tensor memory is released
         if (threadIdx.x == 0 && flags) atomicOr(flags, MG_FLAG_WAIT_TIMEOUT);
         for (int c = max(0, nch - 2); c < nch; c++) mbar_wait(bar0 + 8 * (c & 1), (c >> 1) & 1);
+    } else {
+        const int ngroup = (nch + EW_MMA_GROUP - 1) / EW_MMA_GROUP;
+        while (ndrained < ngroup) drain(ndrained);
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     float *D = (float *)gbase;  // 128 x 65 floats over stage 0 (all MMAs have completed)
     if (!timeout && warp < 4 && nch > 0) {
-#pragma unroll
-        for (int cc = 0; cc < 4; cc++) {
-            if (cc * 16 >= 2 * H) break;
-            unsigned v[16];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15}, [%16];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                : "r"(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(cc * 16)));
+        for (int cc = 0; cc < 2 * H / 16; cc++) {
+            float v[16];
+            tmem_ld16(tlane + 128u + (unsigned)(cc * 16), v);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 16; j++) D[(warp * 32 + lane) * 65 + cc * 16 + j] = __uint_as_float(v[j]);
+            for (int j = 0; j < 16; j++) D[(warp * 32 + lane) * 65 + cc * 16 + j] = v[j];
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64) : "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(EW_MMA_TCOLS) : "memory");
     if (timeout) return;
     float *out = (float *)A.spart + (size_t)blockIdx.y * A.nslots * 2;
     for (int idx = threadIdx.x; idx < EW_MMA_ROWS * 32; idx += EW_MMA_TPB) {
@@ -817,6 +940,18 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
         out[2 * sm] = has_minus ? RR + II : 0.f;
         out[2 * sm + 1] = has_minus ? IR - RI : 0.f;
     }
+}
+
+// the tensor-core S(k) pass (A.forder set); returns the number of site blocks of partials
+cudaError_t launch_sk_mma(const EwArgs &A, unsigned *flags, cudaStream_t s, int *nblk) {
+    *nblk = (A.n + EW_MMA_SITES - 1) / EW_MMA_SITES;
+    if (A.n == 0 || A.nrows == 0) return cudaSuccess;
+    k_qcast<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.q, A.qf);
+    cudaError_t e = cudaFuncSetAttribute(k_sk_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, EW_MMA_SMEM);
+    if (e != cudaSuccess) return e;
+    const dim3 grid((unsigned)((A.nrows + EW_MMA_ROWS - 1) / EW_MMA_ROWS), (unsigned)*nblk);
+    k_sk_mma<<<grid, EW_MMA_TPB, EW_MMA_SMEM, s>>>(A, flags);
+    return cudaGetLastError();
 }
 
 // S(k) from the partials: a block of EW_RED_PARTS * 256 threads takes 256 slots; part p
@@ -1587,13 +1722,8 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     if (fp64) {
         MG_CUDA(launch_sk<double>(A, nblk, s));
     } else if (mg_ewald_sk_tensor(c)) {
-        k_qcast<<<(n + 255) / 256, 256, 0, s>>>(n, A.q, A.qf);
         A.forder = (const int *)c->d_row_slot.p + c->nrows + c->nslots;
-        nblk_red = (n + EW_MMA_SITES - 1) / EW_MMA_SITES;
-        MG_CUDA(cudaFuncSetAttribute(k_sk_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, EW_MMA_SMEM));
-        const dim3 grid((unsigned)((c->nrows + EW_MMA_ROWS - 1) / EW_MMA_ROWS), (unsigned)nblk_red);
-        k_sk_mma<<<grid, EW_MMA_TPB, EW_MMA_SMEM, s>>>(A, (unsigned *)c->d_flags.p);
-        MG_CUDA(cudaGetLastError());
+        MG_CUDA(launch_sk_mma(A, (unsigned *)c->d_flags.p, s, &nblk_red));
     } else {
         MG_CUDA(launch_sk<float>(A, nblk, s));
     }
@@ -1946,8 +2076,12 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
                  "cudaFuncSetAttribute");
         k_kforce<double><<<fblocks, EW_FG * EW_FSITES, fsmem, s>>>(A, ct.maxa);
     } else {
-        EWS_CUDA(launch_sk<float>(A, nblk, s), "k_sk launch");
-        k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk, slot_row);
+        int nblk_red = nblk;
+        if (KZ <= EW_MMA_MAXKZ)
+            EWS_CUDA(launch_sk_mma(A, nullptr, s, &nblk_red), "k_sk_mma launch");
+        else
+            EWS_CUDA(launch_sk<float>(A, nblk, s), "k_sk launch");
+        k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk_red, slot_row);
         EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
     }
     if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, d_energy);
