@@ -43,6 +43,7 @@ import numpy as np  # noqa: E402
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 SM_COUNT_NOMINAL = 152
 FP32_LANES_PER_SM = 128
+TF32_DENSE_NOMINAL = 1100.0  # TFLOP/s, dense TF32 tensor rate of the part
 # algorithmic work per unit (fixed constants of the work model; FP32 FLOP)
 # Fixed work model of the path (the roofline's algorithmic FLOP): a pair inside the cutoff,
 # counted once, is 55 FP32 FLOP (LJ + Ewald real space); reciprocal space is 10 FLOP per
@@ -76,6 +77,35 @@ def ewald_rows(kmax, ksqmax):
             nrows += 1
             nkz += m + 1
     return nrows, nkz
+
+
+def sk_tensor_flops(kmax, ksqmax, n, sites_per_block=1024, rows_per_tile=64, chunk=32):
+    """FLOP the tensor-core S(k) pass (k_sk_mma) issues: rows sorted by kzmax (longest
+    first) in tiles of 64, each tile an M = 128 x N = 2H GEMM (H = 16 if its longest row has
+    kzmax < 16, else 32) over the sites of every block padded to whole 32-site chunks, three
+    TF32 MMAs (hi*hi, hi*lo, lo*hi) per product."""
+    kx_max, ky_max, kz_max = kmax
+    kz = []
+    for kx in range(kx_max + 1):
+        for ky in range(-ky_max, ky_max + 1):
+            if kx == 0 and ky < 0:
+                continue
+            rem = ksqmax - kx * kx - ky * ky
+            if rem < 0:
+                continue
+            m = 0
+            while m + 1 <= kz_max and (m + 1) ** 2 <= rem:
+                m += 1
+            if kx == 0 and ky == 0 and m < 1:
+                continue
+            kz.append(m)
+    kz.sort(reverse=True)
+    padded = sum(-(-min(sites_per_block, n - b) // chunk) * chunk for b in range(0, n, sites_per_block))
+    flop = 0
+    for t in range(0, len(kz), rows_per_tile):
+        h = 16 if kz[t] + 1 <= 16 else 32
+        flop += 3 * 2 * 128 * 2 * h * padded
+    return flop
 
 
 def parse():
@@ -858,7 +888,7 @@ def run_ours(args, rank, world, local_rank):
     achieved = flops / (t_ms * 1e-3) / 1e12 if t_ms > 0 else 0.0
     # DRAM bytes per launch of that kernel from the committed ncu summary of this workload
     traffic = None
-    kernel_of = {"pair": "k_pair", "kspace_sk": "k_sk2", "kspace_force": "k_kforce_mm"}
+    kernel_of = {"pair": "k_pair", "kspace_sk": "k_sk_mma", "kspace_force": "k_kforce_mm"}
     tf = os.path.join(ROOT, "profiles", f"kernels_{args.workload}.md")
     if os.path.exists(tf):
         for ln in open(tf):
@@ -895,6 +925,15 @@ def run_ours(args, rank, world, local_rank):
                          "peak_basis": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz "
                                        "(MEASURED_PEAKS.json holds no FP32 figure)"},
             "clocks": clk}
+    if kvec and args.precision == "mixed" and system.kmax[2] <= 30:
+        tf = sk_tensor_flops(tuple(system.kmax), system.ksqmax, n)
+        line["kspace_sk_tensor"] = {
+            "kernel": "k_sk_mma", "ms": kms[3], "mma_tflop": tf / 1e12,
+            "achieved_tflops": tf / (kms[3] * 1e-3) / 1e12 if kms[3] > 0 else 0.0, "peak_tflops": TF32_DENSE_NOMINAL,
+            "frac": tf / (kms[3] * 1e-3) / 1e12 / TF32_DENSE_NOMINAL if kms[3] > 0 else 0.0,
+            "peak_basis": "nominal dense TF32 (MEASURED_PEAKS.json holds bf16 only)",
+            "note": "structure factors as TF32 MMAs (3-term split product, FP32 accumulation in tensor memory); "
+                    "FLOP issued, padding included; the stage time includes operand generation on the CUDA cores"}
     if "cpu_baseline" in extras:
         line["cpu_baseline"] = extras.pop("cpu_baseline")
     line.update(extras)

@@ -942,10 +942,11 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
     }
 }
 
-// the tensor-core S(k) pass (A.forder set); returns the number of site blocks of partials
+// the tensor-core S(k) pass (A.forder must be set); returns the number of site blocks of partials
 cudaError_t launch_sk_mma(const EwArgs &A, unsigned *flags, cudaStream_t s, int *nblk) {
     *nblk = (A.n + EW_MMA_SITES - 1) / EW_MMA_SITES;
     if (A.n == 0 || A.nrows == 0) return cudaSuccess;
+    if (!A.forder || !A.rows || !A.row_slot || !A.qf) return cudaErrorInvalidValue;
     k_qcast<<<(A.n + 255) / 256, 256, 0, s>>>(A.n, A.q, A.qf);
     cudaError_t e = cudaFuncSetAttribute(k_sk_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, EW_MMA_SMEM);
     if (e != cudaSuccess) return e;
