@@ -598,7 +598,7 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 // few 1e-6, the Fourier energy by 1e-5), so each group of EW_MMA_GROUP chunks accumulates
 // in one of two tensor-memory accumulators and is then added, by the CUDA cores in
 // round-to-nearest FP32, to a running total kept in tensor memory: the truncation then
-// acts on 64-site partials of either sign and averages out. Partials per site block go to
+// acts on 128-site partials of either sign and averages out. Partials per site block go to
 // k_sk_reduce, which sums them in fixed order. Two chunk stages: the CUDA cores fill stage c & 1 while
 // the tensor core works on the other; a tcgen05.commit per chunk signals an mbarrier that
 // guards the stage's reuse. Every wait is bounded; on a timeout the CTA records
@@ -614,7 +614,7 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 #define EW_MMA_SMEM (2 * EW_MMA_STAGE + 64 + 1024)
 #define EW_MMA_WAIT (1 << 20)
 #ifndef EW_MMA_GROUP
-#define EW_MMA_GROUP 2     // chunks summed in one tensor-memory accumulator before each drain
+#define EW_MMA_GROUP 4     // chunks summed in one tensor-memory accumulator before each drain
 #endif
 #define EW_MMA_TCOLS 256   // tensor-memory columns per CTA: two group accumulators and the total
 
