@@ -121,6 +121,8 @@ def parse():
     ap.add_argument("--cpu-k-stride", type=int, default=400)
     ap.add_argument("--md-dt-sweep", action="store_true",
                     help="print the NVE drift of the water system against the outer time step and exit")
+    ap.add_argument("--nve-drift-scan", action="store_true",
+                    help="only the NVE drift of the 216-water system at 0.5, 0.25 and 0.125 fs (20 ps each)")
     ap.add_argument("--nve-drift", action="store_true",
                     help="print a long small-step NVE drift run of the 216-water Wolf system on the mixed "
                          "and FP64 paths and exit")
@@ -363,6 +365,39 @@ def md_extras(system, split_r, precision, device, steps=10, equil_steps=1000, nv
                    "wall clock around mg_md_run (host copies of the start and end included); drift from a "
                    "linear fit of ukin + uinter + uintra over the NVE run after the NVT equilibration")
     return out
+
+
+def nve_drift_scan(device=0, ps=20.0, cases=((0.5, "mixed"), (0.25, "mixed"), (0.125, "mixed"), (0.125, "fp64"))):
+    """NVE drift against the time step on the 216-water Wolf system: for each (step, path),
+    1 ps of Nose-Hoover NVT at 298 K from seeded velocities, then `ps` of velocity-Verlet NVE;
+    drift = slope of ukin + uinter + uintra. Integration error shows as drift ~ dt^2."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import Engine
+    from mspms2_gb300.system import md_params, time_base
+    out = []
+    for dt_fs, prec in cases:
+        steps = int(ps * 1e3 / dt_fs)
+        s = configs.water_c1()
+        s.delt_fs, s.nstep_inner, s.treq_K = dt_fs, 1, 298.0
+        md = md_params(s)
+        tau = 100.0 / time_base(s)
+        md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
+        m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+        rng = np.random.default_rng(11)
+        v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
+        v -= (v * m).sum(1, keepdims=True) / m.sum()
+        with Engine(s, precision=prec, device=device) as eng:
+            md["scheme"] = 1
+            pos, vel, _, _ = eng.md_run(int(1000 / dt_fs), md, v)
+            md["scheme"] = 0
+            _, _, _, lg = eng.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
+        h = lg[:, 0] + lg[:, 1] + lg[:, 2]
+        slope = float(np.polyfit(np.arange(len(h)) * dt_fs, h, 1)[0])
+        fl = float(np.std(h)) / (md["treq"] * s.natom)
+        out.append({"dt_fs": dt_fs, "precision": prec, "ps": ps, "drift_kT_per_ns_per_atom":
+                    slope * 1e6 / (md["treq"] * s.natom), "rms_fluctuation_kT_per_atom": fl,
+                    "resolution_kT_per_ns_per_atom": fl / (ps * 1e-3)})
+    return {"workload": "water_c1 (216 SPC/Fw, Wolf)", "integrator": "velocity Verlet (vver), NVE", "runs": out}
 
 
 def nve_drift(device=0, dt_fs=0.25, equil_steps=4000, steps=160000):
@@ -961,6 +996,12 @@ def main():
         build.build()
         if rank == 0:
             print(json.dumps(nve_drift(local_rank)), flush=True)
+        return 0
+    if args.nve_drift_scan:
+        from mspms2_gb300 import build
+        build.build()
+        if rank == 0:
+            print(json.dumps(nve_drift_scan(local_rank)), flush=True)
         return 0
     return run_ours(args, rank, world, local_rank)
 
