@@ -1878,7 +1878,10 @@ __global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int nslot
 }
 
 // fixed-order sum of the reciprocal energy over the S(k) reduction's block rows
-__global__ void k_ew_energy(const double *__restrict__ erows, int nrows, double *__restrict__ out) {
+// the Fourier energy of the allocation-free pass; NaN when a bounded on-chip wait of the
+// tensor-core S(k) pass ran out (flags), so that the failure shows without a host sync
+__global__ void k_ew_energy(const double *__restrict__ erows, int nrows, const unsigned *__restrict__ flags,
+                            double *__restrict__ out) {
     __shared__ double s[256];
     double t = 0.0;
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) t += erows[(size_t)r * E_NCOMP + E_UFOURIER];
@@ -1888,7 +1891,7 @@ __global__ void k_ew_energy(const double *__restrict__ erows, int nrows, double 
         if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[0] = s[0];
+    if (threadIdx.x == 0) out[0] = (flags && (*flags & MG_FLAG_WAIT_TIMEOUT)) ? __longlong_as_double(0x7ff8000000000000ll) : s[0];
 }
 
 mg_status ew_static_fail(char *err, size_t err_len, mg_status code, const char *fmt, ...) {
@@ -1997,6 +2000,8 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     off += ew_align256(esz * (size_t)ct.nslots);
     const size_t o_erows = off;
     off += ew_align256(sizeof(double) * E_NCOMP * (size_t)rblocks);
+    const size_t o_flags = off;  // status word of the tensor-core S(k) pass
+    off += 256;
     const bool table_force = !fp64 && ct.maxa <= EW_FMM_MAXA;
     size_t ncoef = 0;
     for (int k : ct.chunk_kz) ncoef += (size_t)(k + 1) * EW_FCHUNK;
@@ -2017,6 +2022,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
         std::copy(key, key + 4, dev.key);
     }
     EWS_CUDA(cudaMemsetAsync(d_f, 0, sizeof(double) * 3 * (size_t)n, s), "cudaMemsetAsync");
+    EWS_CUDA(cudaMemsetAsync(base + o_flags, 0, sizeof(unsigned), s), "cudaMemsetAsync");
     const double twopi = 6.283185307179586;
     const double sc[3] = {p->twopi_lx / twopi, p->twopi_ly / twopi, p->twopi_lz / twopi};
     void *tab = base + o_tab;
@@ -2079,13 +2085,13 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     } else {
         int nblk_red = nblk;
         if (KZ <= EW_MMA_MAXKZ)
-            EWS_CUDA(launch_sk_mma(A, nullptr, s, &nblk_red), "k_sk_mma launch");
+            EWS_CUDA(launch_sk_mma(A, (unsigned *)(base + o_flags), s, &nblk_red), "k_sk_mma launch");
         else
             EWS_CUDA(launch_sk<float>(A, nblk, s), "k_sk launch");
         k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk_red, slot_row);
         EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
     }
-    if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, d_energy);
+    if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, (const unsigned *)(base + o_flags), d_energy);
     EWS_CUDA(cudaGetLastError(), "kernel launch");
     return MG_OK;
 #undef EWS_CUDA
