@@ -14,11 +14,14 @@
 // and no recurrence. Tables per site: X[0..KMAXX], Y[0..KMAXY], Z[0..KMAXZ].
 //
 // k-vectors are grouped in rows (kx, ky) holding |kz| = 0..kzmax(kx,ky) with both signs
-// of kz. Structure factors: a thread owns (row, up to 8 consecutive |kz|) = up to 16
+// of kz. Structure factors, mixed path: k_sk_mma runs the sum over sites as TF32 MMAs on
+// the tensor cores ((row, Re/Im of q X Y) x site against site x (|kz|, Re/Im of Z), 3-term
+// split products, accumulators in tensor memory); k_sk2 is the CUDA-core form (KMAXZ > 30,
+// or the tensor pass off): a thread owns (row, up to 8 consecutive |kz|) = up to 16
 // k-vectors, chunks balanced per row; tasks are sorted by length and each length group
 // padded to whole warps, so a warp runs one unrolled loop; the block stages tiles of
-// site tables in shared memory and sums its EW_SITES sites in R; a fixed-order FP64
-// reduction over site blocks gives S(k) (deterministic).
+// site tables in shared memory and sums its EW_SITES sites in R. Either way a fixed-order
+// FP64 reduction over site blocks gives S(k) (deterministic).
 // Forces: for one site and one row the kz sums are two complex polynomials in Z = e^{i
 // theta_z}, P(Z) = sum_a conj(c S+_a) Z^a and Q(Z) = sum_a c S-_a Z^a, and the z force
 // needs their derivatives; all four are evaluated by Horner's rule (16 FMA per |kz|, no
