@@ -21,8 +21,8 @@ of 512 Lennard-Jones replicas; the cost of the adjoint and Hessian-vector produc
 matching on 4096 waters (64 snapshots, loss + gradient, checked against the FP64 path and
 central differences); 20,000 butane in a nanotube bundle with device-generated Tasos
 tables (pair throughput, solid-fluid gather against HBM, ns/day, FP64 path); the roofline
-of the dominant kernel and a bounded CPU baseline of the reference algorithm (the oracle
-port on all host threads, extrapolated from a sampled window).
+of the dominant kernel and a CPU baseline of the reference algorithm: one full, unsampled
+frclong()+frcshort() call of the oracle port on all host threads.
 """
 from __future__ import annotations
 
@@ -41,7 +41,6 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-SM_COUNT_NOMINAL = 152
 FP32_LANES_PER_SM = 128
 TF32_DENSE_NOMINAL = 1100.0  # TFLOP/s, dense TF32 tensor rate of the part
 # algorithmic work per unit (fixed constants of the work model; FP32 FLOP)
@@ -117,8 +116,9 @@ def parse():
     ap.add_argument("--workload", default="water_c2", choices=["water_c2", "water_c4", "water_c1"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-extras", action="store_true", help="skip FP64 path, RESPA and CPU baseline")
-    ap.add_argument("--cpu-sample-mols", type=int, default=256)
-    ap.add_argument("--cpu-k-stride", type=int, default=400)
+    ap.add_argument("--ref-slices", type=int, default=8,
+                    help="reference arm: steps per full CPU call (each step one slice of it)")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the full-call CPU baseline")
     ap.add_argument("--md-dt-sweep", action="store_true",
                     help="print the NVE drift of the water system against the outer time step and exit")
     ap.add_argument("--nve-drift-scan", action="store_true",
@@ -207,6 +207,22 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def fp32_peak_inputs(device, clk):
+    """SM count read from the device and the SM clock ceiling sampled by nvidia-smi during
+    the timed region (else MEASURED_PEAKS.json's sm_max_mhz) for the FP32 FMA-pipe peak:
+    SMs x 128 lanes x 2 FLOP x clock. MEASURED_PEAKS.json holds no FP32 figure."""
+    import torch
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz, src = (clk or {}).get("sm_max_mhz"), "clocks.max.sm sampled during the timed region"
+    if not mhz:
+        mhz, src = measured_peaks().get("sm_max_mhz"), "MEASURED_PEAKS.json sm_max_mhz"
+    if not mhz:
+        mhz, src = 2070.0, "nominal 2070 MHz (no clock reading)"
+    basis = (f"FP32 FMA pipe: {sms} SMs (read from the device) x 128 lanes x 2 FLOP x {mhz:.0f} MHz ({src}); "
+             "MEASURED_PEAKS.json holds no FP32 figure")
+    return sms, float(mhz), basis
+
+
 def measured_peaks():
     try:
         with open(PEAKS_FILE) as f:
@@ -222,79 +238,68 @@ def host_threads() -> int:
         return os.cpu_count() or 1
 
 
-def cpu_baseline(system, sample_mols, k_stride, threads=1):
-    """Reference algorithm (oracle port of src/frclong.c / src/frcshort.c) on a sampled
-    window, extrapolated to the full call: i-molecules [0, sample_mols) of the O(N^2) pair
-    loop and every k_stride-th reciprocal vector. With threads > 1 the pair rows are split
-    into contiguous ranges of equal pair count and the sampled k-vectors are dealt round
-    robin, one oracle call per thread (the C oracle keeps no global state and ctypes drops
-    the GIL for the call); each part is timed by its wall clock."""
-    from concurrent.futures import ThreadPoolExecutor
-    from oracle.pyoracle import Oracle, OrcWindow
+def cpu_baseline(system, threads):
+    """One full, unsampled evaluation of the reference algorithm on the host: the oracle
+    port of src/frclong.c (orc_frclong_mt: the O(N^2) pair rows in ranges of equal pair count
+    and the k-vectors dealt round robin over `threads` host threads, partial sums added in
+    thread order) followed by src/frcshort.c (orc_frcshort, one thread); wall clock of each."""
+    from oracle.pyoracle import Oracle
     o = Oracle(system)
-    M = system.nmole
-    rows = min(sample_mols, M)
-    T = max(1, int(threads))
-    # pair rows: split points at equal shares of sum_{i<rows} (M-1-i)
-    cum = np.cumsum([M - 1 - i for i in range(rows)])
-    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * (t + 1) / T)) + 1 for t in range(T - 1)] + [rows]
-    cuts = sorted(set(min(max(c, 0), rows) for c in cuts))
-    w_pairs = [OrcWindow(a, b, 1 << 30, 1, 0) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
-    w_k = [OrcWindow(M, M + 1, k_stride * T, 1, t * k_stride) for t in range(T)]
-
-    def wall(windows):
-        t0 = time.perf_counter()
-        if len(windows) == 1:
-            o.frclong(window=windows[0])
-        else:
-            with ThreadPoolExecutor(len(windows)) as ex:
-                list(ex.map(lambda w: o.frclong(window=w), windows))
-        return time.perf_counter() - t0
-
-    t_pairs = wall(w_pairs)                           # pair window, ~no k-space, no intra
-    t_k = wall(w_k)                                   # no pairs, strided k-space
-    t_intra = wall([OrcWindow(M, M + 1, 1 << 30, 0, 0)])  # intra + self terms only (serial)
     t0 = time.perf_counter()
+    o.frclong_mt(threads)
+    t1 = time.perf_counter()
     o.frcshort()
-    t_short = time.perf_counter() - t0
-    # examined molecule pairs: sampled rows vs the whole upper triangle
-    sample = int(cum[-1]) if rows else 0
-    total = M * (M - 1) // 2
-    kx, ky, kz = system.kmax
-    kfull = sum(1 for a in range(-kx, kx + 1) for b in range(-ky, ky + 1) for c in range(-kz, kz + 1)
-                if 0 < a * a + b * b + c * c <= system.ksqmax)
-    ksample = (kfull + k_stride - 1) // k_stride
-    t_full = t_pairs * total / max(sample, 1) + max(t_k - t_intra, 0.0) * kfull / max(ksample, 1) + t_intra + t_short
-    return {"t_step_s": t_full, "t_sampled_s": t_pairs + t_k + t_intra + t_short, "threads": T,
-            "sample": f"i-molecules 0..{sample_mols} of {M} in the O(N^2) pair loop, every {k_stride}th of "
-                      f"{kfull} k-vectors, full intra/bonded; {T} thread(s) (pair rows split by pair "
-                      f"count, sampled k-vectors dealt round robin); extrapolated to one full call"}
+    t2 = time.perf_counter()
+    return {"t_step_s": t2 - t0, "t_frclong_s": t1 - t0, "t_frcshort_s": t2 - t1, "threads": threads,
+            "sample": f"one full unsampled frclong()+frcshort() call of the whole workload ({system.natom} sites, "
+                      f"all pair rows and all k-vectors) on {threads} host thread(s); nothing extrapolated"}
 
 
 def run_reference(args, rank):
+    """The reference's CPU implementation of the path (the oracle port; the compiled
+    reference does not exist on the GPU host) on all host threads. One step is slice k mod S
+    of one full call (orc_frclong_mt slices: the k-th of S equal shares of the pair rows and
+    the k-vectors numbered k mod S; slice 0 also runs the O(N) terms and frcshort), so S
+    consecutive steps do one full call's work exactly once and every step is timed as run.
+    S is picked so that a step takes a few seconds."""
     if rank != 0:
         return 0
+    from oracle.pyoracle import Oracle
     system = make_system(args.workload)
+    system.respa_split = 0.0
     npairs = pairs_in_cutoff(system)
     threads = host_threads()
-    kstride = max(1, args.cpu_k_stride // threads)
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(system, max(8, args.cpu_sample_mols // 8), kstride * 8, threads)
+    o = Oracle(system)
+    S = max(1, args.ref_slices)
+
+    def one(k):
+        t0 = time.perf_counter()
+        o.frclong_mt(threads, slice_=k % S, nslices=S)
+        if k % S == 0:
+            o.frcshort()
+        return time.perf_counter() - t0
+
+    for k in range(args.warmup):  # warm-up: slices of a finer partition (untimed)
+        o.frclong_mt(threads, slice_=k % (4 * S), nslices=4 * S)
     t0 = time.perf_counter()
-    last = None
-    for _ in range(args.steps):
-        last = cpu_baseline(system, args.cpu_sample_mols * threads, kstride, threads)
-        vals.append(npairs / last["t_step_s"])
+    ts = [one(k) for k in range(args.steps)]
     wall = time.perf_counter() - t0
-    value = statistics.mean(vals)
+    # pair interactions per second: each slice does 1/S of a full call's work
+    value = npairs * len(ts) / S / sum(ts)
+    full_calls = len(ts) // S
+    full_s = [sum(ts[c * S:(c + 1) * S]) for c in range(full_calls)]
+    sample = (f"each step is one of {S} slices of a full unsampled frclong()+frcshort() call ({system.natom} sites): "
+              f"1/{S} of the pair rows (equal pair count) and every {S}th k-vector, on {threads} host threads; "
+              f"{S} consecutive steps = one full call, timed in parts (nothing extrapolated)")
     line = {"impl": "reference", "metric": "pair_interactions_per_s", "value": value,
             "unit": "pair-interactions/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * last["t_step_s"], "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1e3 * statistics.mean(ts), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload, "sites": system.natom, "pairs_in_cutoff": npairs},
+            "config": {"workload": args.workload, "sites": system.natom, "pairs_in_cutoff": npairs,
+                       "slices_per_full_call": S},
+            "full_call_s": full_s,
             "cpu_baseline": {"value": value, "unit": "pair-interactions/s", "cores": threads, "kind": "port",
-                             "sample": last["sample"], "host_cores": os.cpu_count()},
+                             "sample": sample, "host_cores": os.cpu_count()},
             "e2e": {"value": value, "unit": "pair-interactions/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "wall_s": wall}
@@ -364,6 +369,51 @@ def md_extras(system, split_r, precision, device, steps=10, equil_steps=1000, nv
     out["note"] = ("device-resident: positions, velocities and thermostat scalars stay in HBM; timed with the "
                    "wall clock around mg_md_run (host copies of the start and end included); drift from a "
                    "linear fit of ukin + uinter + uintra over the NVE run after the NVT equilibration")
+    return out
+
+
+def c1_extras(device, steps=1000):
+    """The small CPU-runnable configuration: 216 SPC/Fw waters (648 sites), Wolf alpha 0.2/A,
+    Rc 9 A, Nose-Hoover NVT (vver_nh_3) at 298 K, 0.5 fs, 1000 steps, from one set of
+    seeded velocities: on the device through mg_md_run (both precisions), and on one host
+    core through the oracle port of the same integrator (orc_md_run; the reference is
+    single-threaded). Wall clock around each whole run; the FP64 device run and the CPU
+    run are compared at the end of the trajectory."""
+    from mspms2_gb300 import configs
+    from mspms2_gb300.engine import Engine
+    from mspms2_gb300.system import md_params, time_base
+    from oracle.pyoracle import Oracle
+    s = configs.water_c1()
+    s.delt_fs, s.nstep_inner, s.treq_K = 0.5, 1, 298.0
+    md = md_params(s)
+    md["scheme"] = 1
+    tau = 100.0 / time_base(s)
+    md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
+    m = np.concatenate([np.tile(sp.aw, sp.nmole) for sp in s.species])
+    v = np.random.default_rng(11).normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
+    v -= (v * m).sum(1, keepdims=True) / m.sum()
+    out = {"workload": "water_c1 (216 SPC/Fw, Wolf, NVT 298 K, 0.5 fs)", "steps": steps}
+    ends = {}
+    for prec in ("mixed", "fp64"):
+        with Engine(s, precision=prec, device=device) as eng:
+            eng.md_run(5, md, v)  # warm-up: list, solver, graph capture
+            t0 = time.perf_counter()
+            pos, _, _, lg = eng.md_run(steps, md, v)
+            dt = time.perf_counter() - t0
+        ends[prec] = (pos, lg)
+        out[f"gpu_{prec}"] = {"wall_s": dt, "ms_per_step": dt / steps * 1e3,
+                              "ns_per_day": steps * 0.5e-6 / dt * 86400.0}
+    t0 = time.perf_counter()
+    pos_c, _, _, lg_c = Oracle(s).md_run(steps, md, v)
+    dt = time.perf_counter() - t0
+    out["cpu_port_1_thread"] = {"wall_s": dt, "ms_per_step": dt / steps * 1e3, "ns_per_day": steps * 0.5e-6 / dt * 86400.0}
+    pos64, lg64 = ends["fp64"]
+    out["fp64_gpu_vs_cpu_end"] = {"max_abs_position_diff_A": float(np.abs(pos64 - pos_c).max()),
+                                  "total_energy_rel_diff": float(abs((lg64[-1, :3].sum() - lg_c[-1, :3].sum()) /
+                                                                      lg_c[-1, :3].sum()))}
+    out["gpu_mixed_over_cpu"] = out["cpu_port_1_thread"]["wall_s"] / out["gpu_mixed"]["wall_s"]
+    out["note"] = ("wall clock of the whole run, host copies of the start and end state included; the CPU run is "
+                   "the restated vver_nh_3 with frclong/frcshort of the oracle on one host core")
     return out
 
 
@@ -671,13 +721,11 @@ def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10)
     from mspms2_gb300.system import md_params, time_base
     s, tubes = configs.butane_in_tube_bundle()
     per = tubes["period"]
-    nx = ny = 1271
-    nz = 25
-    h = (0.1, 0.1, per / (nz - 1))
+    nx, ny, nz = configs.C5_TASOS_NODES
+    h = configs.c5_tasos_spacing(tubes)
 
     def spec(sig, eps):
-        return dict(atoms=tubes["atoms"], ucl=(127.0, 127.0, per), f_sigma=sig, f_epsilon=eps, s_sigma=3.4,
-                    s_epsilon=28.0, rcuton=14.0, rcutoff=14.0, lj_switch=0)
+        return configs.c5_tasos_spec(tubes, sig, eps)
 
     n = s.natom
     stream = torch.cuda.current_stream()
@@ -904,11 +952,14 @@ def run_ours(args, rank, world, local_rank):
         extras["derivatives"] = adjoint_extras(system, args.precision, local_rank)
         extras["force_matching"] = force_matching_extras(local_rank)
         extras["c5_butane_tubes"] = c5_extras(local_rank)
-        threads = host_threads()
-        cpu = cpu_baseline(system, args.cpu_sample_mols * threads, max(1, args.cpu_k_stride // threads), threads)
-        extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s", "cores": threads,
-                                  "kind": "port", "sample": cpu["sample"], "t_step_s": cpu["t_step_s"],
-                                  "host_cores": os.cpu_count()}
+        extras["c1_nvt"] = c1_extras(local_rank)
+        if not args.no_cpu_baseline:
+            threads = host_threads()
+            cpu = cpu_baseline(system, threads)
+            extras["cpu_baseline"] = {"value": npairs / cpu["t_step_s"], "unit": "pair-interactions/s",
+                                      "cores": threads, "kind": "port", "sample": cpu["sample"],
+                                      "t_step_s": cpu["t_step_s"], "t_frclong_s": cpu["t_frclong_s"],
+                                      "t_frcshort_s": cpu["t_frcshort_s"], "host_cores": os.cpu_count()}
 
     # roofline of the dominant stage (FP32 pipe: no stage is a dense contraction)
     kvec = st["kvectors"]
@@ -919,7 +970,8 @@ def run_ours(args, rank, world, local_rank):
                 "kspace_force": (FLOP_KF_ROWKZ * nkz + FLOP_KF_ROW * nrows) * n}
     dom = max(stages, key=lambda k: stages[k][0])
     t_ms, flops = stages[dom]
-    peak = SM_COUNT_NOMINAL * FP32_LANES_PER_SM * 2 * 2.07e9 / 1e12
+    sm_count, sm_mhz, peak_basis = fp32_peak_inputs(local_rank, clk)
+    peak = sm_count * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
     achieved = flops / (t_ms * 1e-3) / 1e12 if t_ms > 0 else 0.0
     # DRAM bytes per launch of that kernel from the committed ncu summary of this workload
     traffic = None
@@ -957,8 +1009,7 @@ def run_ours(args, rank, world, local_rank):
                          "executed_tflops": executed[dom] / (t_ms * 1e-3) / 1e12 if t_ms > 0 else 0.0,
                          "executed_note": "FLOP the kernel's algorithm executes (the table passes do fewer than "
                                           "the work model counts per k-vector)",
-                         "peak_basis": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz "
-                                       "(MEASURED_PEAKS.json holds no FP32 figure)"},
+                         "peak_basis": peak_basis},
             "clocks": clk}
     if kvec and args.precision == "mixed" and system.kmax[2] <= 30:
         tf = sk_tensor_flops(tuple(system.kmax), system.ksqmax, n)

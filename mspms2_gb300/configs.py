@@ -278,3 +278,19 @@ def butane_in_tube_bundle(seed: int = 2024, nmole: int = 20000, cell_xy: float =
     s.sf_type = 3  # Tasos tables
     s.treq_K = 300.0
     return s, dict(atoms=atoms, period=period, radius=radius, centres=np.array(centres))
+
+
+# Tasos tables of the butane / nanotube-bundle system: 0.1 A over the 127 x 127 A cell and
+# 24 intervals of one tube period in z; type 1 = CH3 (sigma 3.75 A, eps/k 98 K), type 2 =
+# CH2 (3.95 A, 46 K); tube carbon sigma 3.4 A, eps/k 28 K; LJ cut at 14 A, no switch.
+C5_TASOS_NODES = (1271, 1271, 25)
+C5_TASOS_TYPES = ((3.75, 98.0), (3.95, 46.0))
+
+
+def c5_tasos_spacing(tubes: dict):
+    return (0.1, 0.1, tubes["period"] / (C5_TASOS_NODES[2] - 1))
+
+
+def c5_tasos_spec(tubes: dict, f_sigma: float, f_epsilon: float) -> dict:
+    return dict(atoms=tubes["atoms"], ucl=(127.0, 127.0, tubes["period"]), f_sigma=f_sigma, f_epsilon=f_epsilon,
+                s_sigma=3.4, s_epsilon=28.0, rcuton=14.0, rcutoff=14.0, lj_switch=0)

@@ -1,7 +1,8 @@
 #!/bin/sh
 # Links the mspms2 program with this engine as its force layer: the reference's own C
-# sources, compiled where they lie under the reference checkout ($MSPMS2_REF, default
-# /root/reference), without src/frclong.c and src/frcshort.c (replaced by frc_gb300.c)
+# sources, compiled where they lie under the reference checkout (first argument, else
+# $MSPMS2_REF, else the checkout oracle/build_ref.sh recorded in oracle/_ref/checkout),
+# without src/frclong.c and src/frcshort.c (replaced by frc_gb300.c)
 # and without src/dftmcff.c (the GSL metal-cluster force field, called only from the
 # replaced frclong.c). The mylibtasos Fortran entry points come from frc_gb300.c.
 #
@@ -11,11 +12,14 @@
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 ROOT=$(cd "$HERE/../.." && pwd)
-REF=${MSPMS2_REF:-/root/reference}
+REF=${1:-$MSPMS2_REF}
+if [ -z "$REF" ] && [ -f "$ROOT/oracle/_ref/checkout" ]; then
+  REF=$(cat "$ROOT/oracle/_ref/checkout")
+fi
 OUT="$HERE/_build"
 CC=${CC:-gcc}
-if [ ! -f "$REF/src/frclong.c" ]; then
-  echo "build_md.sh: reference sources not found under $REF; skipping" >&2
+if [ -z "$REF" ] || [ ! -f "$REF/src/frclong.c" ]; then
+  echo "build_md.sh: no reference checkout (argument, MSPMS2_REF or oracle/_ref/checkout); skipping" >&2
   exit 0
 fi
 if [ ! -f "$ROOT/mspms2_gb300/libmspms2_gb300.so" ]; then

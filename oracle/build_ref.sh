@@ -2,8 +2,11 @@
 # Builds the reference mspms2 force layer (C part) into oracle/_ref/ as the pinning
 # oracle for the CPU restatement. TEST INFRASTRUCTURE ONLY.
 #
-# Sources are read where they lie under the reference checkout ($MSPMS2_REF, default
-# /root/reference). Two documented patches are applied to transient copies under
+# Sources are read where they lie under the reference checkout, given as the first
+# argument or as $MSPMS2_REF (no default: without one the script does nothing). The path is
+# recorded in oracle/_ref/checkout for the recipes that link or run against the same
+# checkout later (mspms2_gb300/shim/build_md.sh, tests/golden/gen_golden.py).
+# Two documented patches are applied to transient copies under
 # oracle/_ref/build/, which are deleted after compiling (nothing of the reference is
 # kept in the repository):
 #   1. src/frclong.c:86 - j atoms of molecule iMole+1 (the unpatched line pairs a
@@ -17,13 +20,15 @@
 # C restatement in oracle/mspms_oracle.c.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${MSPMS2_REF:-/root/reference}
+REF=${1:-$MSPMS2_REF}
 OUT="$HERE/_ref"
 CC=${CC:-gcc}
-if [ ! -f "$REF/src/frclong.c" ]; then
-  echo "build_ref.sh: reference sources not found under $REF; skipping" >&2
+if [ -z "$REF" ] || [ ! -f "$REF/src/frclong.c" ]; then
+  echo "build_ref.sh: no reference checkout (argument or MSPMS2_REF); skipping" >&2
   exit 0
 fi
+mkdir -p "$OUT"
+printf '%s\n' "$REF" > "$OUT/checkout"
 rm -rf "$OUT/build"
 mkdir -p "$OUT/build/src"
 for f in "$REF"/src/*.c "$REF"/src/*.h; do

@@ -19,6 +19,7 @@
 #include "mspms_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -472,9 +473,7 @@ static void site_of(const orc_system *s, int abs, int *spec, int *rel) {
 }
 
 /* ---- Ewald reciprocal space, self term, vacuum dipole (src/frclong.c:988-1129) ----- */
-static void ewald_kspace(const orc_system *s, const double *x, const double *y, const double *z,
-                         acc *a, const orc_window *w) {
-    const mg_params *p = &s->p;
+static double *site_charges(const orc_system *s) {
     int n = orc_natom(s);
     double *q = (double *)malloc(sizeof(double) * (size_t)n);
     for (int i = 0; i < n; i++) {
@@ -482,8 +481,15 @@ static void ewald_kspace(const orc_system *s, const double *x, const double *y, 
         site_of(s, i, &sp, &rel);
         q[i] = s->sp[sp].charge[rel];
     }
-    int stride = (w && w->k_stride > 1) ? w->k_stride : 1;
-    int koff = (w && stride > 1 && w->k_offset > 0) ? w->k_offset % stride : 0;
+    return q;
+}
+
+/* The k-vector loop of src/frclong.c:996-1046 over the vectors numbered koff mod stride:
+ * adds the forces into a and returns sum_k kvec |S(k)|^2 (not yet scaled). */
+static double kspace_loop(const orc_system *s, const double *x, const double *y, const double *z,
+                          const double *q, acc *a, int stride, int koff) {
+    const mg_params *p = &s->p;
+    int n = orc_natom(s);
     long long kcount = 0;
     double ufourier = 0.0;
     for (int kx = -p->kmax[0]; kx <= p->kmax[0]; kx++)
@@ -511,6 +517,15 @@ static void ewald_kspace(const orc_system *s, const double *x, const double *y, 
                     a->fz[i] += fij * rkz;
                 }
             }
+    return ufourier;
+}
+
+/* src/frclong.c:1047-1129 after the k-vector loop: scaled Fourier energy, self term,
+ * uelec, vacuum dipole, the Ewald virial. */
+static void ewald_tail(const orc_system *s, const double *x, const double *y, const double *z,
+                       const double *q, acc *a, double ufourier) {
+    const mg_params *p = &s->p;
+    int n = orc_natom(s);
     ufourier *= p->vfactor_ewald * p->coulomb_prefactor;
     a->e->ufourier = ufourier;
     double uself = 0.0;
@@ -556,6 +571,15 @@ static void ewald_kspace(const orc_system *s, const double *x, const double *y, 
         free(ex);
     }
     a->e->virial_inter += a->e->uelec;
+}
+
+static void ewald_kspace(const orc_system *s, const double *x, const double *y, const double *z,
+                         acc *a, const orc_window *w) {
+    double *q = site_charges(s);
+    int stride = (w && w->k_stride > 1) ? w->k_stride : 1;
+    int koff = (w && stride > 1 && w->k_offset > 0) ? w->k_offset % stride : 0;
+    double ufourier = kspace_loop(s, x, y, z, q, a, stride, koff);
+    ewald_tail(s, x, y, z, q, a, ufourier);
     free(q);
 }
 
@@ -847,6 +871,148 @@ int orc_frclong(const orc_system *s, const double *x, const double *y, const dou
     e->ushift *= s->p.shift4;
     if (s->p.charge_type == MG_ELEC_EWALD) {
         ewald_kspace(s, x, y, z, &a, w);
+    } else if (s->p.charge_type == MG_ELEC_WOLF) {
+        double q2 = 0.0;
+        for (int i = 0; i < n; i++) {
+            int sp, rel;
+            site_of(s, i, &sp, &rel);
+            q2 += s->sp[sp].charge[rel] * s->sp[sp].charge[rel];
+        }
+        e->uself = q2 * (s->p.coulomb_prefactor * s->p.wolfvcon3);
+        e->uelec = e->ureal - e->uself - e->uexcl;
+    }
+    int flags = solid_fluid(s, x, y, z, &a);
+    e->uotherff = 0.0;
+    e->uinter = e->uvdw + e->uelec + e->usflj + e->uotherff;
+    return flags;
+}
+
+/* ---- frclong on several host threads ------------------------------------------------
+ * The same terms as orc_frclong, with the two O(N^2)-class loops shared out: the
+ * inter-molecular pair rows (src/frclong.c:56-218) in contiguous ranges of equal pair count
+ * and the k-vectors (src/frclong.c:996-1046) dealt round robin. Each thread accumulates into
+ * its own force block and energies; the blocks are added in thread order, then the serial
+ * remainder (intra-molecular corrections, Ewald tail, Wolf self, solid-fluid) runs as in
+ * orc_frclong. Only the order of the sums differs from the serial call.
+ * With nslices > 1 the call evaluates slice `slice` of that work: the slice-th of nslices
+ * row ranges of equal pair count and the k-vectors numbered slice mod nslices (the O(N)
+ * remainder runs in every slice). The nslices slices together do the pair and k-vector work
+ * of one full call exactly once, so they time a full call in measured parts. */
+typedef struct mt_job {
+    const orc_system *s;
+    const double *x, *y, *z, *q;
+    int imol_begin, imol_end; /* pair rows (global molecule index of the i-molecule) */
+    int kstride, koff;        /* k-vectors koff mod kstride; kstride 0: none */
+    double *f;                /* [3][n] */
+    double *scratch;          /* [3][n] COM offsets of the plain-Coulomb model */
+    mg_energies e;
+    double ufourier;
+} mt_job;
+
+static void *mt_run(void *arg) {
+    mt_job *j = (mt_job *)arg;
+    int n = orc_natom(j->s);
+    acc a = {j->f, j->f + n, j->f + 2 * n, &j->e};
+    if (j->imol_end > j->imol_begin) {
+        orc_window w = {j->imol_begin, j->imol_end, 1, 1, 0};
+        inter_pairs(j->s, j->x, j->y, j->z, &a, &w, j->scratch, j->scratch + n, j->scratch + 2 * n);
+    }
+    if (j->kstride > 0) j->ufourier = kspace_loop(j->s, j->x, j->y, j->z, j->q, &a, j->kstride, j->koff);
+    return NULL;
+}
+
+int orc_frclong_mt(const orc_system *s, const double *x, const double *y, const double *z,
+                   double *fxl, double *fyl, double *fzl, mg_energies *e, int nthreads, int slice, int nslices) {
+    if (nslices < 1) nslices = 1;
+    if (slice < 0 || slice >= nslices) return -1;
+    int n = orc_natom(s), T = nthreads < 1 ? 1 : nthreads, M = 0;
+    for (int i = 0; i < s->nspecies; i++) M += s->sp[i].nmole;
+    /* site pairs each i-molecule row examines, and cuts at equal shares of their sum */
+    double *cum = (double *)malloc(sizeof(double) * (size_t)(M + 1));
+    cum[0] = 0.0;
+    int g = 0;
+    for (int is = 0; is < s->nspecies; is++) {
+        const mg_species *Si = &s->sp[is];
+        double later = 0.0;
+        for (int js = is + 1; js < s->nspecies; js++) later += (double)s->sp[js].nmole * s->sp[js].natom;
+        for (int im = 0; im < Si->nmole; im++, g++)
+            cum[g + 1] = cum[g] + (double)Si->natom * ((double)(Si->nmole - im - 1) * Si->natom + later);
+    }
+    /* rows of this slice: the slice-th of nslices ranges of equal pair count; then T
+     * ranges of equal pair count within it */
+    int r0 = 0, r1 = M;
+    {
+        double lo = cum[M] * slice / nslices, hi = cum[M] * (slice + 1) / nslices;
+        while (r0 < M && cum[r0] < lo) r0++;
+        r1 = r0;
+        while (r1 < M && cum[r1] < hi) r1++;
+        if (slice == nslices - 1) r1 = M;
+        if (slice == 0) r0 = 0;
+    }
+    int *cut = (int *)malloc(sizeof(int) * (size_t)(T + 1));
+    cut[0] = r0;
+    for (int t = 1; t < T; t++) {
+        double want = cum[r0] + (cum[r1] - cum[r0]) * t / T;
+        int c = cut[t - 1];
+        while (c < r1 && cum[c] < want) c++;
+        cut[t] = c;
+    }
+    cut[T] = r1;
+    free(cum);
+    const int ewald = s->p.charge_type == MG_ELEC_EWALD;
+    double *q = ewald ? site_charges(s) : NULL;
+    mt_job *jobs = (mt_job *)calloc((size_t)T, sizeof(mt_job));
+    pthread_t *tid = (pthread_t *)calloc((size_t)T, sizeof(pthread_t));
+    int *started = (int *)calloc((size_t)T, sizeof(int));
+    for (int t = 0; t < T; t++) {
+        mt_job *j = &jobs[t];
+        j->s = s;
+        j->x = x; j->y = y; j->z = z; j->q = q;
+        j->imol_begin = cut[t];
+        j->imol_end = cut[t + 1];
+        j->kstride = ewald ? T * nslices : 0;
+        j->koff = slice + nslices * t;
+        j->f = (double *)calloc((size_t)n * 3, sizeof(double));
+        j->scratch = (double *)calloc((size_t)n * 3 + 3, sizeof(double));
+        started[t] = T > 1 && pthread_create(&tid[t], NULL, mt_run, j) == 0;
+        if (!started[t]) mt_run(j);
+    }
+    for (int t = 0; t < T; t++)
+        if (started[t]) pthread_join(tid[t], NULL);
+    for (int i = 0; i < n; i++) fxl[i] = fyl[i] = fzl[i] = 0.0;
+    memset(e, 0, sizeof(*e));
+    double ufourier = 0.0;
+    for (int t = 0; t < T; t++) {
+        const mt_job *j = &jobs[t];
+        for (int i = 0; i < n; i++) {
+            fxl[i] += j->f[i];
+            fyl[i] += j->f[n + i];
+            fzl[i] += j->f[2 * n + i];
+        }
+        e->uvdw += j->e.uvdw;
+        e->ushift += j->e.ushift;
+        e->ureal += j->e.ureal;
+        e->uelec += j->e.uelec;
+        e->virial_inter += j->e.virial_inter;
+        ufourier += j->ufourier;
+        free(j->f);
+        free(j->scratch);
+    }
+    free(jobs);
+    free(tid);
+    free(started);
+    free(cut);
+    acc a = {fxl, fyl, fzl, e};
+    e->ushift *= s->p.shift4;
+    if (slice != 0) { /* the O(N) remainder belongs to slice 0 */
+        if (ewald) e->ufourier = ufourier * s->p.vfactor_ewald * s->p.coulomb_prefactor;
+        free(q);
+        return 0;
+    }
+    intra_pairs(s, x, y, z, &a);
+    if (ewald) {
+        ewald_tail(s, x, y, z, q, &a, ufourier);
+        free(q);
     } else if (s->p.charge_type == MG_ELEC_WOLF) {
         double q2 = 0.0;
         for (int i = 0; i < n; i++) {

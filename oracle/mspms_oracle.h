@@ -68,6 +68,14 @@ int orc_natom(const orc_system *s);
  * bit 0 = a site left a Tasos/my-interp table. */
 int orc_frclong(const orc_system *s, const double *x, const double *y, const double *z,
                 double *fxl, double *fyl, double *fzl, mg_energies *e, const orc_window *w);
+/* orc_frclong on nthreads host threads (pair rows and k-vectors shared out, per-thread
+ * partial sums added in thread order); the result differs from the serial call only by the
+ * order of the sums. slice/nslices = 0/1 is the full call; slice k of n > 1 evaluates the
+ * k-th of n equal shares of the pair rows and the k-vectors numbered k mod n (the O(N) terms
+ * in slice 0 only), so the slices' forces sum to the full call. Returns the flag word of orc_frclong, or -1 for a bad slice. */
+int orc_frclong_mt(const orc_system *s, const double *x, const double *y, const double *z,
+                   double *fxl, double *fyl, double *fzl, mg_energies *e, int nthreads, int slice,
+                   int nslices);
 int orc_frcshort(const orc_system *s, const double *x, const double *y, const double *z,
                  double *fxs, double *fys, double *fzs, mg_energies *e);
 /* Count of inter-molecular site pairs (different molecules, neither GHOST_FULL) with

@@ -71,6 +71,8 @@ def lib():
         _lib = C.CDLL(build())
         _lib.orc_frclong.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, _dp, _dp, _dp,
                                      C.POINTER(MgEnergies), C.POINTER(OrcWindow)]
+        _lib.orc_frclong_mt.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, _dp, _dp, _dp,
+                                        C.POINTER(MgEnergies), C.c_int, C.c_int, C.c_int]
         _lib.orc_frcshort.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, _dp, _dp, _dp,
                                       C.POINTER(MgEnergies)]
         _lib.orc_count_pairs.argtypes = [C.POINTER(OrcSystem), _dp, _dp, _dp, C.c_double]
@@ -160,6 +162,21 @@ class Oracle:
         e = MgEnergies()
         flags = lib().orc_frclong(C.byref(self.s), _ptr(x), _ptr(y), _ptr(z), _ptr(f[0]), _ptr(f[1]),
                                   _ptr(f[2]), C.byref(e), C.byref(window) if window else None)
+        return f, e.as_dict(), flags
+
+    def frclong_mt(self, threads: int, x=None, y=None, z=None, slice_: int = 0, nslices: int = 1):
+        """frclong on `threads` host threads (orc_frclong_mt): the same terms, with the pair
+        rows and k-vectors shared out; only the order of the sums differs from frclong().
+        slice_/nslices > 1 evaluate one of nslices equal shares of the pair and k-vector work."""
+        sysm = self.system
+        x = np.ascontiguousarray(sysm.x if x is None else x, dtype=np.float64)
+        y = np.ascontiguousarray(sysm.y if y is None else y, dtype=np.float64)
+        z = np.ascontiguousarray(sysm.z if z is None else z, dtype=np.float64)
+        n = len(x)
+        f = np.zeros((3, n))
+        e = MgEnergies()
+        flags = lib().orc_frclong_mt(C.byref(self.s), _ptr(x), _ptr(y), _ptr(z), _ptr(f[0]), _ptr(f[1]),
+                                     _ptr(f[2]), C.byref(e), int(threads), int(slice_), int(nslices))
         return f, e.as_dict(), flags
 
     def frcshort(self, x=None, y=None, z=None):

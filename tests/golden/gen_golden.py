@@ -41,7 +41,18 @@ from mspms2_gb300.system import (ELEC_EWALD, ELEC_NONE, ELEC_SIMPLE_COULOMB, ELE
 from oracle.pyoracle import (reference_available, run_reference_dir, run_reference_md,  # noqa: E402
                              run_reference_sfgridgen)
 
-REF = os.environ.get("MSPMS2_REF", "/root/reference")
+def _checkout() -> str:
+    """The reference checkout: MSPMS2_REF, else the one oracle/build_ref.sh recorded."""
+    ref = os.environ.get("MSPMS2_REF")
+    rec = os.path.join(ROOT, "oracle", "_ref", "checkout")
+    if not ref and os.path.exists(rec):
+        ref = open(rec).read().strip()
+    if not ref:
+        sys.exit("set MSPMS2_REF to the reference checkout (or run oracle/build_ref.sh <checkout> first)")
+    return ref
+
+
+REF = _checkout()
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -80,3 +80,30 @@ def test_sampling_windows_partition_the_call():
     kspace = sum(k[0] for k in ks)
     assert sum(k[1]["ufourier"] for k in ks) == pytest.approx(e_full["ufourier"], rel=1e-12)
     assert _close(pairs + kspace + intra, full, rtol=1e-11)
+
+
+@pytest.mark.parametrize("case", ["water_ewald_512", "water_ewald_vacuum", "custom_wolf", "water_simple_coulomb",
+                                  "sf_tasos", "butane_ewald_switch"])
+def test_threaded_call_matches_serial(case):
+    """orc_frclong_mt (pair rows and k-vectors over host threads, partial sums added in
+    thread order) gives the serial call's forces and energies up to the order of the sums."""
+    s, _ = load_system(os.path.join(GOLDEN, case + ".npz"))
+    o = Oracle(s)
+    f1, e1, fl1 = o.frclong()
+    f5, e5, fl5 = o.frclong_mt(5)
+    assert fl1 == fl5
+    assert _close(f5, f1, rtol=1e-13)
+    for k in LONG:
+        assert e5[k] == pytest.approx(e1[k], rel=1e-11, abs=1e-9), (case, k)
+
+
+def test_threaded_slices_partition_the_call():
+    """Slices 0..n-1 of orc_frclong_mt together do the work of one call exactly once (the
+    O(N) terms in slice 0): their forces and Fourier energies sum to the full call."""
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    o = Oracle(s)
+    full, e_full, _ = o.frclong()
+    parts = [o.frclong_mt(2, slice_=k, nslices=3) for k in range(3)]
+    assert _close(sum(p[0] for p in parts), full, rtol=1e-11)
+    assert sum(p[1]["ufourier"] for p in parts) == pytest.approx(e_full["ufourier"], rel=1e-12)
+    assert sum(p[1]["uvdw"] for p in parts) == pytest.approx(e_full["uvdw"], rel=1e-12)
