@@ -436,6 +436,16 @@ MG_API mg_status mg_set_kspace_overlap(mg_ctx *ctx, int enable);
  * pass. Enabled by default; no effect on the FP64 path. The two agree to FP32 rounding. */
 MG_API mg_status mg_set_kspace_tensor(mg_ctx *ctx, int enable);
 
+/* Bound of each on-chip pipeline wait (mbarrier poll loop) of the tensor-core S(k) pass, in
+ * polls, for every context and mg_ewald_recip_static call of the process from the next
+ * launch on; a negative value restores the default (2^20 polls, well under a second). When a
+ * wait runs out, the pass stops issuing MMAs, waits with the default bound for the ones it
+ * issued, frees its tensor memory and returns: mg_compute and the integrators then fail with
+ * MG_ERR_CUDA, and mg_ewald_recip_static returns NaN forces and energy. 0 makes the first
+ * wait give up at once, which exercises that path without a fault (tests). No reference
+ * counterpart: the reference has no device code. */
+MG_API mg_status mg_set_wait_limit(long long polls);
+
 /* ---- simulated annealing (siman, src/siman.c:62-182) ---------------------------- */
 /* Stages at T = t_initial, t_initial/mu_t, t_initial/mu_t^2, ...; the run ends after the
  * first stage whose T is below t_min (the reference tests T < t_min after the stage). A
@@ -555,14 +565,23 @@ MG_API mg_status mg_sf_tasos_generate(mg_ctx *ctx, int type, const mg_sfgrid_spe
  * device current (which may load the device code there); make it before any stream
  * capture. Every call selects `device` for its duration and restores the caller's. A call
  * whose scratch would exceed the limit returns MG_ERR_CAPACITY and launches nothing.
- * Nothing in the scratch needs to start at zero. Calls on one device share the scratch:
- * two calls that are not ordered on the device (issued from different threads, or on
- * streams not ordered by events) race on it and give wrong results. */
+ * Nothing in the scratch needs to start at zero: the k-vector tables are rebuilt on the
+ * device whenever KMAX/KSQMAX differ from those of the tables in place (their key is kept
+ * in the scratch), and the call clears its status word. Calls on one device share the
+ * scratch: two calls that are not ordered on the device (issued from different threads, or
+ * on streams not ordered by events) race on it and give wrong results.
+ * On the mixed path the structure factors come from the tensor-core pass (KMAXZ <= 30).
+ * If one of its bounded on-chip waits runs out (mg_set_wait_limit), every force of d_f and
+ * *d_energy are NaN: the failure shows in the outputs, without a host synchronisation. */
 #define MG_EWALD_STATIC_SCRATCH_BYTES (32u << 20)
 MG_API mg_status mg_ewald_recip_static(int device, void *stream, int precision, int natom,
                                        const double *d_x, const double *d_y, const double *d_z,
                                        const double *d_q, const mg_params *p, double *d_f,
                                        double *d_energy, char *err, size_t err_len);
+/* For tests, no reference counterpart: the number of row ranges the k-space force pass of
+ * the last successful mg_ewald_recip_static call of the process split its rows into (their
+ * partial forces live in the scratch left after the tables; 1 = no split, 0 = no call yet). */
+MG_API int mg_ewald_recip_static_last_split(void);
 
 /* ---- adjoint: parameter gradients of a force loss ----------------------------- */
 /* No counterpart in the reference (which has no derivatives with respect to force-field

@@ -32,6 +32,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <numeric>
 #include <type_traits>
@@ -281,6 +282,10 @@ struct EwArgs {
     int csplit[EW_MAXSPLIT + 1];
     float4 *fcoef;
     double *fpart;
+    // status word of the call (MG_FLAG_*): the tensor-core S(k) pass sets its bits, the
+    // S(k) reduction reads them (coefficients and energy turn NaN after a give-up)
+    const unsigned *flags;
+    long long mma_wait;  // polls of each pipeline wait of the tensor-core S(k) pass
 };
 
 // One tile of sites for a thread owning CH consecutive |kz| of one row (FP64 path):
@@ -604,8 +609,15 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 // acts on 128-site partials of either sign and averages out. Partials per site block go to
 // k_sk_reduce, which sums them in fixed order. Two chunk stages: the CUDA cores fill stage c & 1 while
 // the tensor core works on the other; a tcgen05.commit per chunk signals an mbarrier that
-// guards the stage's reuse. Every wait is bounded; on a timeout the CTA records
-// MG_FLAG_WAIT_TIMEOUT, still frees its tensor memory and returns.
+// guards the stage's reuse. Every wait is bounded (A.mma_wait polls). When one runs out the
+// CTA stops issuing, records MG_FLAG_WAIT_TIMEOUT, waits with the full default bound for the
+// commits of the last two chunks it issued (one per barrier; a commit covers every earlier
+// MMA of the issuing thread), so that no MMA still reads its shared memory or writes its
+// tensor memory, then frees the tensor memory and returns without writing partials. If that
+// wait runs out too it also records MG_FLAG_MMA_UNDRAINED: tensor memory of the SM may then be
+// overwritten by MMAs still in flight for the rest of the launch, and the call's results are
+// invalid as a whole (the host fails the call; the S(k) reduction turns every coefficient
+// and the energy into NaN).
 #define EW_MMA_ROWS 64     // rows per CTA (two accumulator lanes each)
 #ifndef EW_MMA_SITES
 #define EW_MMA_SITES 1024  // sites per CTA (a multiple of EW_SITES)
@@ -615,7 +627,7 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 #define EW_MMA_MAXKZ 30    // largest KMAXZ the pass takes (Z pairs within 32 columns)
 #define EW_MMA_STAGE 49152 // A hi, A lo (16 KB each), B hi, B lo (8 KB each)
 #define EW_MMA_SMEM (2 * EW_MMA_STAGE + 64 + 1024)
-#define EW_MMA_WAIT (1 << 20)
+#define EW_MMA_WAIT (1ll << 20)  // default polls of each pipeline wait (mg_set_wait_limit)
 #ifndef EW_MMA_GROUP
 #define EW_MMA_GROUP 4     // chunks summed in one tensor-memory accumulator before each drain
 #endif
@@ -653,8 +665,8 @@ __device__ __forceinline__ void sts128(unsigned a, const float (&v)[4]) {
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    for (int i = 0; i < EW_MMA_WAIT; i++) {
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long long limit) {
+    for (long long i = 0; i < limit; i++) {
         unsigned ok;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -821,11 +833,14 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
     };
     if (nch > 0) load(0);
     bool timeout = false;
+    int issued = 0;  // chunks whose MMAs were issued and committed
     for (int c = 0; c < nch; c++) {
         const int b = c & 1;
         const unsigned st = base + b * EW_MMA_STAGE;
         bool to = false;
-        if (c >= 2) to = !mbar_wait(bar0 + 8 * b, ((c - 2) >> 1) & 1);
+        if (c >= 2) to = !mbar_wait(bar0 + 8 * b, ((c - 2) >> 1) & 1, A.mma_wait);
+        // one decision per warp: drain() runs warp-wide tcgen05 loads and stores
+        to = __any_sync(0xffffffffu, to);
         if (!to) {
             // chunk c - 2 is complete: if it closed a group, fold that group into the total
             // before the group two ahead reuses its accumulator
@@ -891,15 +906,19 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar0 + 8 * b)
                          : "memory");
         }
+        issued = c + 1;
     }
     if (!timeout && nch > 0) {
-        const bool to = !mbar_wait(bar0 + 8 * ((nch - 1) & 1), ((nch - 1) >> 1) & 1);
+        const bool to = !mbar_wait(bar0 + 8 * ((nch - 1) & 1), ((nch - 1) >> 1) & 1, A.mma_wait);
         timeout = __syncthreads_or(to);
     }
     if (timeout) {
-        // let issued MMAs finish (bounded) before the tensor memory is released
-        if (threadIdx.x == 0 && flags) atomicOr(flags, MG_FLAG_WAIT_TIMEOUT);
-        for (int c = max(0, nch - 2); c < nch; c++) mbar_wait(bar0 + 8 * (c & 1), (c >> 1) & 1);
+        // the MMAs of the issued chunks may still run: wait, with the full default bound, for
+        // the commits of the last two issued chunks before the tensor memory is released
+        bool done = true;
+        for (int c = max(0, issued - 2); c < issued; c++) done &= mbar_wait(bar0 + 8 * (c & 1), (c >> 1) & 1, EW_MMA_WAIT);
+        done = __syncthreads_and(done);
+        if (threadIdx.x == 0 && flags) atomicOr(flags, done ? MG_FLAG_WAIT_TIMEOUT : MG_FLAG_WAIT_TIMEOUT | MG_FLAG_MMA_UNDRAINED);
     } else {
         const int ngroup = (nch + EW_MMA_GROUP - 1) / EW_MMA_GROUP;
         while (ndrained < ngroup) drain(ndrained);
@@ -996,7 +1015,12 @@ __global__ void __launch_bounds__(EW_RED_PARTS * 256) k_sk_reduce(EwArgs A, int 
         bool valid = a <= row.z && !(minus && (a == 0 || row.w)) && !(row.w && a == 0);
         T2 c;
         c.x = c.y = (R)0;
-        if (valid) {
+        if (A.flags && (*A.flags & MG_FLAG_WAIT_TIMEOUT)) {
+            // the tensor-core pass gave up: its partials are incomplete, so the coefficients
+            // (and with them every force of the pass) and the energy become NaN
+            c.x = c.y = (R)NAN;
+            e[0] = NAN;
+        } else if (valid) {
             double kz = minus ? -a : a;
             double rkx = A.twopi[0] * row.x, rky = A.twopi[1] * row.y, rkz = A.twopi[2] * kz;
             double rksq = rkx * rkx + rky * rky + rkz * rkz;
@@ -1722,6 +1746,8 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     A.coul = p.coulomb_prefactor;
     A.rows_e = (double *)c->d_epart.p;
     A.f = fl;
+    A.flags = (const unsigned *)c->d_flags.p;
+    A.mma_wait = mg_wait_limit();
     int nblk_red = nblk;
     if (fp64) {
         MG_CUDA(launch_sk<double>(A, nblk, s));
@@ -1763,12 +1789,14 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
 // mg_ewald_recip_static: the same reciprocal-space pass with no device allocation
 // ---------------------------------------------------------------------------------
 // Every piece of scratch (k-vector row and task tables, phase tables, S(k) partials and
-// coefficients, energy rows) is carved out of g_ew_scratch. Its device address is looked
-// up once per device, with that device current, and handed to the kernels as a plain
-// pointer. Each byte a kernel reads was written before in the same call, or (the row and
-// task tables) by an earlier call on the device with the same KMAX/KSQMAX, so nothing
-// has to start at zero. Calls on one device share the array; calls that are not ordered
-// on the device race on it.
+// coefficients, energy rows, the status word) is carved out of g_ew_scratch. Its device
+// address is looked up once per device, with that device current, and handed to the
+// kernels as a plain pointer. The row and task tables depend on KMAX/KSQMAX only; the key
+// they were built for is kept in the first words of the scratch, and the table kernel,
+// launched by every call, compares it on the device and rebuilds only on a change, so the
+// check holds in stream order and inside a captured graph alike. Every other byte a kernel
+// reads was written before in the same call (the status word is cleared per call). Calls on
+// one device share the array; calls that are not ordered on the device race on it.
 namespace {
 
 static __device__ __align__(256) unsigned char g_ew_scratch[MG_EWALD_STATIC_SCRATCH_BYTES];
@@ -1777,10 +1805,11 @@ constexpr int EW_STATIC_MAX_DEVICES = 64;
 
 struct EwStaticDevice {
     unsigned char *base = nullptr;  // device address of g_ew_scratch on this device
-    int key[4] = {-1, -1, -1, -1};  // KMAXX, KMAXY, KMAXZ, KSQMAX of the tables now in scratch
 };
+constexpr int EW_STATIC_KEY_MAGIC = 0x6d677374;  // marks a key word block the table kernel wrote
 EwStaticDevice g_ew_static[EW_STATIC_MAX_DEVICES];
 std::mutex g_ew_static_mutex;
+std::atomic<int> g_ew_static_split{0};  // row split of the last call's force pass
 
 struct EwCounts {
     int nrows = 0, nslots = 0, ntasks = 0, maxa = 1;
@@ -1811,8 +1840,22 @@ EwCounts ew_count(int KX, int KY, int KZ, int KS) {
 // Row table, packed slot table (first slot of each row, then the row of each slot) and
 // the task list sorted by length (longest first), then first |kz|, then row, with each
 // length group padded to whole warps: the same tables mg_ewald_setup builds on the host.
+// With key != null (the allocation-free pass) the kernel first compares key[0..4] with
+// (magic, KX, KY, KZ, KS) and returns when the tables in place were built for them.
 __global__ void k_ew_tables(int KX, int KY, int KZ, int KS, int nrows, int nslots, int4 *__restrict__ rows,
-                            int *__restrict__ row_slot, int4 *__restrict__ tasks) {
+                            int *__restrict__ row_slot, int4 *__restrict__ tasks, int *__restrict__ key) {
+    if (key) {
+        const bool same = key[0] == EW_STATIC_KEY_MAGIC && key[1] == KX && key[2] == KY && key[3] == KZ && key[4] == KS;
+        if (same) return;  // uniform over the block: every thread reads the same words
+        __syncthreads();   // all threads have read the old key before thread 0 rewrites it
+        if (threadIdx.x == 0) {
+            key[0] = EW_STATIC_KEY_MAGIC;
+            key[1] = KX;
+            key[2] = KY;
+            key[3] = KZ;
+            key[4] = KS;
+        }
+    }
     if (threadIdx.x == 0) {
         int r = 0, slot = 0;
         ew_for_rows(KX, KY, KZ, KS, [&](int kx, int ky, int kzmax, int half) {
@@ -1985,7 +2028,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     const int KZ = std::max(KZ0, 1);
     const int nblk = (n + EW_SITES - 1) / EW_SITES;
     const unsigned rblocks = (unsigned)((ct.nslots + 255) / 256);
-    size_t off = 0;
+    size_t off = 256;  // words 0..4: the key of the row and task tables (k_ew_tables)
     const size_t o_rows = off;
     off += ew_align256(sizeof(int4) * (size_t)ct.nrows);
     const int nchunk = (int)ct.chunk_kz.size();
@@ -2018,12 +2061,8 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     int4 *rows = (int4 *)(base + o_rows);
     int *row_slot = (int *)(base + o_slot);
     int4 *tasks = (int4 *)(base + o_tasks);
-    const int key[4] = {KX, KY, KZ0, KS};
-    if (!std::equal(key, key + 4, dev.key)) {
-        k_ew_tables<<<1, 256, 0, s>>>(KX, KY, KZ0, KS, ct.nrows, ct.nslots, rows, row_slot, tasks);
-        EWS_CUDA(cudaGetLastError(), "k_ew_tables launch");
-        std::copy(key, key + 4, dev.key);
-    }
+    k_ew_tables<<<1, 256, 0, s>>>(KX, KY, KZ0, KS, ct.nrows, ct.nslots, rows, row_slot, tasks, (int *)base);
+    EWS_CUDA(cudaGetLastError(), "k_ew_tables launch");
     EWS_CUDA(cudaMemsetAsync(d_f, 0, sizeof(double) * 3 * (size_t)n, s), "cudaMemsetAsync");
     EWS_CUDA(cudaMemsetAsync(base + o_flags, 0, sizeof(unsigned), s), "cudaMemsetAsync");
     const double twopi = 6.283185307179586;
@@ -2058,6 +2097,8 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     A.rows_e = (double *)(base + o_erows);
     A.row0 = 0;
     A.f = d_f;
+    A.flags = (const unsigned *)(base + o_flags);
+    A.mma_wait = mg_wait_limit();
     A.forder = row_slot + ct.nrows + ct.nslots;
     A.rpos = A.forder + ct.nrows;
     A.coff = A.rpos + ct.nrows;
@@ -2096,9 +2137,12 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     }
     if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, (const unsigned *)(base + o_flags), d_energy);
     EWS_CUDA(cudaGetLastError(), "kernel launch");
+    g_ew_static_split.store(A.fsplit);
     return MG_OK;
 #undef EWS_CUDA
 }
+
+extern "C" int mg_ewald_recip_static_last_split(void) { return g_ew_static_split.load(); }
 
 // ---------------------------------------------------------------------------------
 // adjoint support: structure factors with arbitrary site weights, the k-space field and

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 
 #include "mg_internal.cuh"
@@ -722,8 +723,12 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
         return mg_fail(c, MG_ERR_INVALID, "degenerate CHARMM improper (src/impfrc.c:96-134 exits here)");
     if (flags[0] & (MG_FLAG_LIST_OVERFLOW | MG_FLAG_COLUMN_OVERFLOW))
         return mg_fail(c, MG_ERR_CAPACITY, "neighbour-list capacity exceeded");
-    if (flags[0] & MG_FLAG_NONFINITE) return mg_fail(c, MG_ERR_NONFINITE, "non-finite force");
+    // a give-up of the tensor-core S(k) pass also makes the forces NaN: report the cause
+    if (flags[0] & MG_FLAG_MMA_UNDRAINED)
+        return mg_fail(c, MG_ERR_CUDA, "tensor-core S(k) pass: an on-chip wait ran out and issued MMAs did not finish "
+                                       "within the bound (tensor memory of the launch may have been overwritten)");
     if (flags[0] & MG_FLAG_WAIT_TIMEOUT) return mg_fail(c, MG_ERR_CUDA, "tensor-core S(k) pass: an on-chip wait ran out");
+    if (flags[0] & MG_FLAG_NONFINITE) return mg_fail(c, MG_ERR_NONFINITE, "non-finite force");
     return MG_OK;
 }
 
@@ -937,6 +942,17 @@ extern "C" mg_status mg_set_kspace_overlap(mg_ctx *c, int enable) {
 extern "C" mg_status mg_set_kspace_tensor(mg_ctx *c, int enable) {
     if (!c) return MG_ERR_INVALID;
     c->kspace_tensor = enable != 0;
+    return MG_OK;
+}
+
+// polls of each on-chip pipeline wait of the tensor-core S(k) pass, process-wide; read at
+// every launch (the default bounds a wait to well under a second)
+static std::atomic<long long> g_wait_limit{1ll << 20};
+
+long long mg_wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+
+extern "C" mg_status mg_set_wait_limit(long long polls) {
+    g_wait_limit.store(polls < 0 ? (1ll << 20) : polls, std::memory_order_relaxed);
     return MG_OK;
 }
 

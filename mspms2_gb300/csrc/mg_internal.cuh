@@ -36,6 +36,7 @@
 #define MG_FLAG_IMPROPER_DEGENERATE 16u
 #define MG_FLAG_SMALL_BOX 32u  // a cluster pair needs two images: use the small-box list
 #define MG_FLAG_WAIT_TIMEOUT 64u  // a bounded on-chip wait (mbarrier) gave up
+#define MG_FLAG_MMA_UNDRAINED 128u  // ...and MMAs it had issued did not finish within the bound either
 
 // per-site flags packed next to the molecule id
 #define MG_SITE_LJ 1        // takes part in LJ (ghost type NONE)
@@ -218,6 +219,7 @@ struct mg_ctx {
 
 // ---- helpers shared by host translation units --------------------------------------
 mg_status mg_fail(mg_ctx *c, mg_status code, const std::string &msg);
+long long mg_wait_limit();  // polls of each on-chip pipeline wait (mg_set_wait_limit)
 bool mg_ewald_horner_force(const mg_ctx *c);  // k-space forces by the Horner pass (threads per site apply)
 bool mg_ewald_sk_tensor(const mg_ctx *c);     // S(k) by the tensor-core pass
 mg_status mg_ewald_fork(mg_ctx *c, const double *dx, const double *dy, const double *dz);

@@ -84,6 +84,7 @@ def load_library(path: str = LIB_PATH):
     lib.mg_set_md_graphs.argtypes = [V, I]
     lib.mg_set_kspace_overlap.argtypes = [V, I]
     lib.mg_set_kspace_tensor.argtypes = [V, I]
+    lib.mg_set_wait_limit.argtypes = [C.c_longlong]
     lib.mg_get_md_graphs.argtypes = [V, C.POINTER(I), C.POINTER(I)]
     lib.mg_autotune.argtypes = [V, _dp, _dp, _dp, I, C.POINTER(capi.MgTuning)]
     lib.mg_set_tuning.argtypes = [V, C.POINTER(capi.MgTuning)]
@@ -431,6 +432,14 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+def set_wait_limit(polls: int) -> None:
+    """Bound of each on-chip pipeline wait of the tensor-core S(k) pass, process-wide
+    (mg_set_wait_limit); a negative value restores the default."""
+    st = load_library().mg_set_wait_limit(int(polls))
+    if st != MG_OK:
+        raise EngineError(st, "mg_set_wait_limit")
 
 
 def _sfgrid_spec(spec: dict):

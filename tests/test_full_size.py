@@ -10,8 +10,10 @@ against the CPU cluster-list builder.
       GPU by mg_sfgrid_tasos and handed to the oracle and the engine alike)
 
 Tolerances are those of test_gpu_parity: norm-wise relative force error 1e-5 (mixed) and
-1e-10 (FP64); each energy relative to the terms it is made of. The oracle call of each
-system runs once per session and is shared by both precisions.
+1e-10 (FP64); each energy relative to the terms it is made of. The benchmark molecules sit
+at their template geometry, where the bonded (short) forces nearly vanish; that block's
+error is judged against the system's force scale (the norm of the long forces). The oracle
+call of each system runs once per session and is shared by both precisions.
 """
 import os
 
@@ -74,7 +76,8 @@ def test_full_size_matches_oracle(name, prec):
         st = eng.stats()
     tol = TOL[prec]
     assert rel(fl, fl_ref) <= tol, (name, prec, rel(fl, fl_ref))
-    assert rel(fs, fs_ref) <= tol, (name, prec, rel(fs, fs_ref))
+    err_s = np.linalg.norm(fs - fs_ref) / max(np.linalg.norm(fs_ref), np.linalg.norm(fl_ref))
+    assert err_s <= tol, (name, prec, err_s)
     scale = energy_scale(ref)
     for k in LONG_E + SHORT_E:
         assert abs(e[k] - ref[k]) <= tol * max(component_scale(ref, k), FLOOR[prec] * scale) + 1e-9, \

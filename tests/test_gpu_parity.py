@@ -269,3 +269,24 @@ def test_sk_tensor_pass_matches_cuda_core_pass(kmax, ksqmax):
         assert abs(out[key][2]["ufourier"] - e64["ufourier"]) <= 2e-6 * abs(e64["ufourier"]), key
     # the two FP32 passes differ by rounding only
     assert rel(out["tc"][0], out["cc"][0]) <= 2e-6, rel(out["tc"][0], out["cc"][0])
+
+
+def test_sk_wait_give_up_fails_the_call_and_recovers():
+    """With the pipeline-wait bound at 0 polls every CTA of the tensor-core S(k) pass gives
+    up at its first wait: it stops issuing, waits (with the default bound) for the MMAs it
+    issued, frees its tensor memory and returns. The call then fails with MG_ERR_CUDA; with
+    the bound restored, the next call on the same context gives the same bits as before."""
+    from mspms2_gb300.engine import EngineError, set_wait_limit
+    s, _ = load_system(os.path.join(GOLDEN, "water_ewald_512.npz"))
+    with Engine(s, precision="mixed") as eng:
+        before = eng.compute()
+        try:
+            set_wait_limit(0)
+            with pytest.raises(EngineError) as ei:
+                eng.compute()
+            assert ei.value.status == 2 and "wait ran out" in str(ei.value)
+        finally:
+            set_wait_limit(-1)
+        after = eng.compute()
+    assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+    assert before[2] == after[2]
