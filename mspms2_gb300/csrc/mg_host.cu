@@ -138,13 +138,13 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_col_count, &c->d_col_start, &c->d_col_fill, &c->d_col_cl_start,
                       &c->d_col_sorted, &c->d_cl_atom, &c->d_cl_ref, &c->d_cl_bb, &c->d_cl_col,
                       &c->d_pair_start, &c->d_pair_count, &c->d_pair_j, &c->d_pair_shift,
-                      &c->d_pack_pos, &c->d_pack_lj, &c->d_pack_info, &c->d_rows, &c->d_row_slot,
+                      &c->d_pack_pos, &c->d_pack_lj, &c->d_pack_info, &c->d_pack_xi, &c->d_pack_qp, &c->d_rows, &c->d_row_slot,
                       &c->d_phase, &c->d_spart, &c->d_scoef, &c->d_tasks, &c->d_epart, &c->d_eout,
                       &c->d_flags, &c->d_tasos, &c->d_myinterp, &c->d_tubes, &c->d_solid,
                       &c->d_meta, &c->d_pair_img, &c->d_cl_bbf, &c->d_col_ncl, &c->d_counter,
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
                       &c->d_adj_class, &c->d_adj, &c->d_adj_g,
-                      &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift,
+                      &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift, &c->d_sub_img, &c->d_facc,
                       &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_qf, &c->d_fk, &c->d_erows_k};
     for (DevBuf *b : bufs) mg_free(*b);
     for (auto &b : c->tasos_buf) mg_free(b);
@@ -684,6 +684,15 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
     c->last_flags = flags[0];
     if (need_pairs) {
         if (mg_list_retry(c, flags[0], meta)) {
+            *retry = true;
+            return MG_OK;
+        }
+        if (flags[0] & MG_FLAG_FIXED_RANGE) {
+            // a pair force outside the range of the fixed-point force sums: a coarser unit
+            // (2^-32, then 2^-16, then 1), kept by the context for later calls, and the call again
+            if (c->fixed_bits <= 0)
+                return mg_fail(c, MG_ERR_NONFINITE, "pair force beyond the range of the fixed-point force sums");
+            c->fixed_bits -= 16;
             *retry = true;
             return MG_OK;
         }

@@ -37,6 +37,7 @@
 #define MG_FLAG_SMALL_BOX 32u  // a cluster pair needs two images: use the small-box list
 #define MG_FLAG_WAIT_TIMEOUT 64u  // a bounded on-chip wait (mbarrier) gave up
 #define MG_FLAG_MMA_UNDRAINED 128u  // ...and MMAs it had issued did not finish within the bound either
+#define MG_FLAG_FIXED_RANGE 256u    // a pair force beyond the range of the fixed-point force sums
 
 // per-site flags packed next to the molecule id
 #define MG_SITE_LJ 1        // takes part in LJ (ghost type NONE)
@@ -167,9 +168,14 @@ struct mg_ctx {
     long long pair_cap = 0;    // cluster-pair entry capacity
     DevBuf d_pair_start, d_pair_count, d_pair_j, d_pair_shift;
     // inner sub-list of the distance split (cluster pairs within respa_split + skin)
-    DevBuf d_sub_start, d_sub_count, d_sub_j, d_sub_shift;
+    DevBuf d_sub_start, d_sub_count, d_sub_j, d_sub_shift, d_sub_img;
+    // mixed-precision pair kernel: 64-bit fixed-point forces per cluster slot
+    // [bucket][3][slots] in units of 2^-fixed_bits (lowered by 16 when a force leaves the range)
+    DevBuf d_facc;
+    int fixed_bits = 32;
     bool sub_ready = false;
     DevBuf d_pack_pos, d_pack_lj, d_pack_info;
+    DevBuf d_pack_xi, d_pack_qp;  // mixed pair kernel: (x, y, z, info bits), (q, half-sigma, sqrt-eps, 0)
     // integration (mg_md_run): velocities, solver work arrays, 1/mass, partial sums,
     // thermostat scalars, per-step records
     DevBuf d_md_v, d_md_work, d_md_rmass, d_md_part, d_md_dev, d_md_log;

@@ -836,7 +836,7 @@ mg_status md_graph_steps(MdRun &R, const mg_md_params *mp, int nsteps, double *d
     c->launches += 1;
     const unsigned bad = MG_FLAG_OUT_OF_GRID | MG_FLAG_NONFINITE | MG_FLAG_LIST_OVERFLOW | MG_FLAG_COLUMN_OVERFLOW |
                          MG_FLAG_SMALL_BOX | MG_FLAG_IMPROPER_DEGENERATE | MG_FLAG_WAIT_TIMEOUT |
-                         MG_FLAG_MMA_UNDRAINED;
+                         MG_FLAG_MMA_UNDRAINED | MG_FLAG_FIXED_RANGE;
     if (!launched || (flags & bad)) {
         cudaGetLastError();
         return restore();

@@ -500,7 +500,8 @@ __global__ void k_sublist(const int *__restrict__ meta, const int *__restrict__ 
                           const void *__restrict__ pair_shift, const int *__restrict__ pair_img,
                           const float *__restrict__ bbf, float lx, float ly, float lz, float rsub2, int fp64,
                           int *__restrict__ sub_start, int *__restrict__ sub_cnt, int *__restrict__ sub_j,
-                          void *__restrict__ sub_shift, unsigned long long *__restrict__ counter) {
+                          void *__restrict__ sub_shift, int *__restrict__ sub_img,
+                          unsigned long long *__restrict__ counter) {
     if (!meta[META_NEED]) return;
     const int lane = threadIdx.x & 31;
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -538,6 +539,7 @@ __global__ void k_sublist(const int *__restrict__ meta, const int *__restrict__ 
             const long long o = run + __popc(m & ((1u << lane) - 1u));
             const int e = e0 + b + lane;
             sub_j[o] = pair_j[e];
+            sub_img[o] = pair_img[e];
             if (fp64)
                 ((double4 *)sub_shift)[o] = ((const double4 *)pair_shift)[e];
             else
@@ -599,14 +601,22 @@ __global__ void k_displacement(int n, const double *__restrict__ x, const double
     if (__any_sync(0xffffffffu, move) && (threadIdx.x & 31) == 0) atomicOr(&meta[META_NEED], 1);
 }
 
-// Pack the per-slot pair-kernel operands from the current positions.
+// the info word (molecule << 2 | flags) carried in the fourth lane of a packed position
+__device__ __forceinline__ float info_lane(int v, float) { return __int_as_float(v); }
+__device__ __forceinline__ double info_lane(int v, double) { return __longlong_as_double((long long)v); }
+
+// Pack the per-slot pair-kernel operands from the current positions: pos (x, y, z relative
+// to the cluster reference, charge), lj (half-sigma, sqrt-epsilon) and info for the FP64 pair
+// kernel and the adjoint passes; xi (x, y, z, info bits) and qp (charge, half-sigma,
+// sqrt-epsilon, 0) for the mixed-precision pair kernel, which stages both rows into shared
+// memory as they are.
 template <typename R4, typename R2, typename R>
 __global__ void k_pack(int n, const int *__restrict__ meta, const int *__restrict__ cl_atom,
                        const double *__restrict__ cl_ref, const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ z, const double *__restrict__ img, const double *__restrict__ q,
                        const double *__restrict__ hsig, const double *__restrict__ seps,
                        const int *__restrict__ mol, const int *__restrict__ sflags, R4 *__restrict__ pos,
-                       R2 *__restrict__ lj, int *__restrict__ info) {
+                       R2 *__restrict__ lj, int *__restrict__ info, R4 *__restrict__ xi, R4 *__restrict__ qp) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= meta[META_NCL] * MG_CL) return;
     int a = cl_atom[s];
@@ -619,6 +629,9 @@ __global__ void k_pack(int n, const int *__restrict__ meta, const int *__restric
         l.x = l.y = (R)0;
         lj[s] = l;
         info[s] = MG_SITE_DEAD;
+        qp[s] = p;
+        p.w = info_lane(MG_SITE_DEAD, (R)0);
+        xi[s] = p;
         return;
     }
     R4 p;
@@ -632,7 +645,16 @@ __global__ void k_pack(int n, const int *__restrict__ meta, const int *__restric
     l.y = (R)seps[a];
     lj[s] = l;
     int f = sflags[a];
-    info[s] = (mol[a] << 2) | (f & (MG_SITE_LJ | MG_SITE_DEAD));
+    const int inf = (mol[a] << 2) | (f & (MG_SITE_LJ | MG_SITE_DEAD));
+    info[s] = inf;
+    R4 v = p;
+    v.w = info_lane(inf, (R)0);
+    xi[s] = v;
+    v.x = p.w;
+    v.y = l.x;
+    v.z = l.y;
+    v.w = (R)0;
+    qp[s] = v;
 }
 
 }  // namespace
@@ -790,7 +812,8 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         if (!mg_ensure(c, c->d_sub_start, sizeof(int) * ((size_t)c->cl_cap + 1)) ||
             !mg_ensure(c, c->d_sub_count, sizeof(int) * ((size_t)c->cl_cap + 1)) ||
             !mg_ensure(c, c->d_sub_j, sizeof(int) * (size_t)c->pair_cap) ||
-            !mg_ensure(c, c->d_sub_shift, ent * (size_t)c->pair_cap))
+            !mg_ensure(c, c->d_sub_shift, ent * (size_t)c->pair_cap) ||
+            !mg_ensure(c, c->d_sub_img, sizeof(int) * (size_t)c->pair_cap))
             return MG_ERR_ALLOC;
         const double rsub = p.respa_split + std::max(c->opt.skin, 0.0);
         const float rsub2 = (float)(rsub * rsub) * 1.0001f + 1e-4f;
@@ -799,7 +822,7 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
                                          (int *)c->d_pair_j.p, c->d_pair_shift.p, (int *)c->d_pair_img.p,
                                          (float *)c->d_cl_bbf.p, (float)c->lx, (float)c->ly, (float)c->lz, rsub2,
                                          fp64 ? 1 : 0, (int *)c->d_sub_start.p, (int *)c->d_sub_count.p,
-                                         (int *)c->d_sub_j.p, c->d_sub_shift.p,
+                                         (int *)c->d_sub_j.p, c->d_sub_shift.p, (int *)c->d_sub_img.p,
                                          (unsigned long long *)c->d_counter.p + 1);
         c->launches += 1;
         c->sub_ready = true;
@@ -816,7 +839,9 @@ mg_status mg_pack_clusters(mg_ctx *c, const double *dx, const double *dy, const 
     size_t slots = (size_t)c->cl_cap * MG_CL;
     if (!mg_ensure(c, c->d_pack_pos, slots * (fp64 ? sizeof(double4) : sizeof(float4))) ||
         !mg_ensure(c, c->d_pack_lj, slots * (fp64 ? sizeof(double2) : sizeof(float2))) ||
-        !mg_ensure(c, c->d_pack_info, slots * sizeof(int)))
+        !mg_ensure(c, c->d_pack_info, slots * sizeof(int)) ||
+        !mg_ensure(c, c->d_pack_xi, slots * (fp64 ? sizeof(double4) : sizeof(float4))) ||
+        !mg_ensure(c, c->d_pack_qp, slots * (fp64 ? sizeof(double4) : sizeof(float4))))
         return MG_ERR_ALLOC;
     unsigned blocks = (unsigned)((slots + 255) / 256);
     const int *meta = (const int *)c->d_meta.p;
@@ -824,12 +849,14 @@ mg_status mg_pack_clusters(mg_ctx *c, const double *dx, const double *dy, const 
         k_pack<double4, double2, double><<<blocks, 256, 0, c->stream>>>(
             n, meta, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, dx, dy, dz, (double *)c->d_img.p,
             (double *)c->d_site_q.p, (double *)c->d_site_hsig.p, (double *)c->d_site_seps.p, (int *)c->d_site_mol.p,
-            (int *)c->d_site_flags.p, (double4 *)c->d_pack_pos.p, (double2 *)c->d_pack_lj.p, (int *)c->d_pack_info.p);
+            (int *)c->d_site_flags.p, (double4 *)c->d_pack_pos.p, (double2 *)c->d_pack_lj.p, (int *)c->d_pack_info.p,
+            (double4 *)c->d_pack_xi.p, (double4 *)c->d_pack_qp.p);
     else
         k_pack<float4, float2, float><<<blocks, 256, 0, c->stream>>>(
             n, meta, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, dx, dy, dz, (double *)c->d_img.p,
             (double *)c->d_site_q.p, (double *)c->d_site_hsig.p, (double *)c->d_site_seps.p, (int *)c->d_site_mol.p,
-            (int *)c->d_site_flags.p, (float4 *)c->d_pack_pos.p, (float2 *)c->d_pack_lj.p, (int *)c->d_pack_info.p);
+            (int *)c->d_site_flags.p, (float4 *)c->d_pack_pos.p, (float2 *)c->d_pack_lj.p, (int *)c->d_pack_info.p,
+            (float4 *)c->d_pack_xi.p, (float4 *)c->d_pack_qp.p);
     MG_CUDA(cudaGetLastError());
     c->launches += 1;
     return MG_OK;

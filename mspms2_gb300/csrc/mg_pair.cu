@@ -8,24 +8,25 @@
 // shift4 factor); Ewald real space or Wolf when r^2 < rcutoffelec^2. Ewald pairs add no
 // pair virial (the reference adds the total Ewald energy instead, src/frclong.c:1128).
 //
-// Execution: one warp per i-cluster (8 sites). Lane l owns i-site l%8 and j-slots l/8
-// and l/8+4 of each j-cluster. Four j-clusters (32 sites: one float4 position, one
-// float2 LJ pair and one int per lane) are staged in shared memory per step with
-// coalesced loads. The list is a full list (each pair seen from both clusters), so no
-// j-force scatter or atomic is needed: a lane accumulates only its own i-site force in
-// FP32 over at most 64 j-clusters, then flushes it into an FP32 hi+lo pair by an exact
-// two-sum (about 48 significant bits, and no FP64 instruction, which is far slower than
-// FP32 on this part); the four lanes of an i-site are combined in FP64 with warp
-// shuffles at the end. A lane's energy sums stay in FP32 over its list, are summed
-// across the warp in FP32 and across warps and blocks in FP64; they are halved for the
-// double counting. The FP64 path accumulates in FP64 throughout. Every reduction has a
-// fixed order, so results are bit-reproducible.
+// Mixed precision (k_pair): Newton's third law over the half of the cluster-pair list with
+// J >= I, one warp per i-cluster, each unordered site pair evaluated once in FP32; i-forces
+// accumulate in registers (FP32 within two super-steps, then FP64), j-forces go through a
+// per-warp shared matrix of pair forces whose column sums are added, as 64-bit fixed point,
+// to slot-ordered accumulators (integer adds, so the result does not depend on the order in
+// which warps arrive); k_fixed_forces turns those into the FP64 force blocks. Energies and
+// virials: FP32 over at most eight super-steps of one lane, then FP64. Details at k_pair.
+//
+// FP64 (k_pair_full, the plain-FP64 path): the full list, each pair from both sides, FP64
+// throughout and no atomics. Lane l owns i-site l % 8 and j-slots l / 8 and l / 8 + 4 of
+// each j-cluster; four j-clusters are staged in shared memory per step.
+//
+// Every reduction has a fixed order, so results are bit-reproducible.
 #include <math.h>
 
 #include "mg_internal.cuh"
 
 #define PAIR_WPB 4       // warps (i-clusters) per block
-#define PAIR_FLUSH 16    // list steps (4 j-clusters each) between force flushes
+#define PAIR_FLUSH 16    // list steps of k_pair_full (4 j-clusters each) between force flushes
 
 namespace {
 
@@ -51,15 +52,6 @@ __device__ __forceinline__ float erfc_from_exp(float x, float ex) {
 }
 
 template <>
-struct RT<float> {
-    typedef float4 V4;
-    typedef float2 V2;
-    __device__ static float rs(float x) { return rsqrtf(x); }
-    __device__ static float erfc_ex(float x, float ex) { return erfc_from_exp(x, ex); }
-    __device__ static float exp_(float x) { return expf(x); }
-    __device__ static float rint_(float x) { return rintf(x); }
-};
-template <>
 struct RT<double> {
     typedef double4 V4;
     typedef double2 V2;
@@ -69,7 +61,7 @@ struct RT<double> {
     __device__ static double rint_(double x) { return rint(x); }
 };
 
-struct PairArgs {
+struct PairFullArgs {
     int n;
     const int *meta;  // meta[0] = number of clusters of the current build
     const int *pair_start, *pair_cnt, *pair_j, *info, *cl_atom;
@@ -84,7 +76,7 @@ struct PairArgs {
 };
 
 template <typename R, int ELEC, bool MIC, bool SPLIT>
-__global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
+__global__ void __launch_bounds__(PAIR_WPB * 32) k_pair_full(PairFullArgs A) {
     typedef typename RT<R>::V4 V4;
     typedef typename RT<R>::V2 V2;
     __shared__ V4 s_pos[PAIR_WPB][32];
@@ -262,22 +254,430 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     mg_block_row<9>(eng, ids, A.rows, A.row0 + blockIdx.x);
 }
 
-template <typename R, int ELEC>
-void launch_pair_elec(const PairArgs &A, bool mic, bool split, unsigned blocks, cudaStream_t s) {
+template <int ELEC>
+void launch_pair_full_elec(const PairFullArgs &A, bool mic, bool split, unsigned blocks, cudaStream_t s) {
     if (mic) {
-        if (split) k_pair<R, ELEC, true, true><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
-        else k_pair<R, ELEC, true, false><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
+        if (split) k_pair_full<double, ELEC, true, true><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
+        else k_pair_full<double, ELEC, true, false><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
     } else {
-        if (split) k_pair<R, ELEC, false, true><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
-        else k_pair<R, ELEC, false, false><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
+        if (split) k_pair_full<double, ELEC, false, true><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
+        else k_pair_full<double, ELEC, false, false><<<blocks, PAIR_WPB * 32, 0, s>>>(A);
     }
 }
 
-template <typename R>
-void launch_pair(const PairArgs &A, int elec, bool mic, bool split, unsigned blocks, cudaStream_t s) {
-    if (elec == 1) launch_pair_elec<R, 1>(A, mic, split, blocks, s);
-    else if (elec == 2) launch_pair_elec<R, 2>(A, mic, split, blocks, s);
-    else launch_pair_elec<R, 0>(A, mic, split, blocks, s);
+// ---------------------------------------------------------------------------------
+// mixed precision: half list, fixed-point forces
+// ---------------------------------------------------------------------------------
+#define PAIR_SS 8       // j-cluster entries per super-step
+#define PAIR_NJ (PAIR_SS * MG_CL)
+#define PAIR_WIN 128    // list entries compacted per window (the kept ones: J >= I)
+#define PAIR_FFLUSH 2   // super-steps between the FP64 flushes of a lane's i-force partials
+#define PAIR_EFLUSH 8   // super-steps between the FP64 flushes of a lane's energy partials
+
+struct PairArgs {
+    int n;
+    const int *meta;  // meta[0] = number of clusters of the current build
+    const int *pair_start, *pair_cnt, *pair_j, *pair_img, *cl_atom;
+    const float4 *pair_shift, *xi, *qp;
+    unsigned long long *facc_l, *facc_s;  // 64-bit fixed-point forces per cluster slot [3][slots]
+    long long fstride;                    // slots of one component block
+    float fscale, flimit;                 // 2^bits and 2^(52 - bits): unit 2^-bits, largest value
+    unsigned *flags;
+    // the pair parameters, rounded to FP32 once on the host
+    float rc2, rce2, rs2, rmax2;
+    float lx, ly, lz, ilx, ily, ilz;
+    float kappa, coul, shift1, ron2, roff2, sw_denom, rce, v1, v2, f1, f2;
+    int ljsw, mode;  // mode bit 0: long bucket, bit 1: short bucket
+    double *rows;
+    int row0;
+};
+
+__device__ __forceinline__ int info_of(float v) { return __float_as_int(v); }
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// force component -> 64-bit fixed point in units of 1/scale; false when out of range or not
+// finite (the limit, 2^52 units, leaves room for 2048 contributions of that size in one sum)
+__device__ __forceinline__ bool to_fixed(float v, long long &o, float scale, float limit) {
+    o = __float2ll_rn(v * scale);
+    return fabsf(v) < limit;
+}
+__device__ __forceinline__ bool to_fixed(double v, long long &o, float scale, float limit) {
+    o = __double2ll_rn(v * (double)scale);
+    return fabs(v) < (double)limit;
+}
+
+struct PairOut {
+    float fx, fy, fz, r2, ulj, ush, uel, vir;
+};
+
+// One site pair (i at pi + sh, j at pj) in FP32: LJ (Lorentz-Berthelot, energy switch or
+// shift energy) where both sites take part in LJ and r^2 < rc^2, Ewald real space (ELEC 1) or
+// Wolf (ELEC 2) where r^2 < rce^2. Terms that do not apply are multiplied by zero rather than
+// branched around, since the lanes of a warp hold different pairs.
+template <int ELEC, bool MIC>
+__device__ __forceinline__ PairOut pair_math(const PairArgs &A, const float4 &pi, const float4 &qi, int infi,
+                                             const float4 &pj, const float4 &qj, const float4 &sh) {
+    PairOut o;
+    float dx = (pi.x + sh.x) - pj.x, dy = (pi.y + sh.y) - pj.y, dz = (pi.z + sh.z) - pj.z;
+    if (MIC) {
+        dx -= A.lx * rintf(dx * A.ilx);
+        dy -= A.ly * rintf(dy * A.ily);
+        dz -= A.lz * rintf(dz * A.ilz);
+    }
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const int infj = info_of(pj.w);
+    const float rinv = rsqrtf(r2);
+    const float rinv2 = rinv * rinv;
+    const bool lj_on = (infi & infj & MG_SITE_LJ) && r2 < A.rc2;
+    const float eps = lj_on ? qi.z * qj.z : 0.f;
+    const float sig = qi.y + qj.y;
+    const float sig2 = sig * sig;
+    float s6 = sig2 * rinv2;
+    s6 = s6 * s6 * s6;
+    const float s12 = s6 * s6;
+    float ulj = 4.f * eps * (s12 - s6);
+    float flj = 24.f * eps * (2.f * s12 - s6) * rinv2;
+    float ush = 0.f;
+    if (A.ljsw) {  // uniform over the launch
+        if (!(r2 < A.ron2)) {
+            const float d = A.roff2 - r2;
+            const float sw = d * d * (A.roff2 + 2.f * r2 - 3.f * A.ron2) / A.sw_denom;
+            flj = flj * sw - ulj * 12.f * d * (A.ron2 - r2) / A.sw_denom;
+            ulj *= sw;
+        }
+    } else {
+        const float sg6 = sig2 * sig2 * sig2;
+        ush = eps * sg6 * (sg6 * A.shift1 - 1.f);
+    }
+    float f = flj, vir = flj * r2, uel = 0.f;
+    if (ELEC != 0) {
+        const float qq = r2 < A.rce2 ? qi.x * qj.x : 0.f;
+        const float rr = r2 * rinv;
+        const float kr = A.kappa * rr;
+        const float ex = expf(-kr * kr);
+        const float ec = erfc_from_exp(kr, ex);
+        if (ELEC == 1) {
+            const float bare = A.coul * qq * rinv;
+            uel = bare * ec;
+            f += (uel + bare * kr * ex * 1.1283791670955126f) * rinv2;
+        } else {
+            uel = A.coul * qq * (ec * rinv + A.v1 + A.v2 * (rr - A.rce));
+            const float fe = A.coul * qq * rinv * (ec * rinv2 + A.f1 * ex * rinv + A.f2);
+            f += fe;
+            vir += fe * r2;
+        }
+    }
+    o.fx = f * dx;
+    o.fy = f * dy;
+    o.fz = f * dz;
+    o.r2 = r2;
+    o.ulj = ulj;
+    o.ush = ush;
+    o.uel = uel;
+    o.vir = vir;
+    return o;
+}
+
+template <int NB>
+struct PairSmem {
+    float4 xj[PAIR_WPB][2][PAIR_NJ];  // x, y, z (cluster-relative), info bits
+    float4 qj[PAIR_WPB][2][PAIR_NJ];  // q, half-sigma, sqrt-eps
+    float4 sh[PAIR_WPB][2][PAIR_SS];  // periodic shift of each entry
+    float fm[PAIR_WPB][NB][3][PAIR_NJ][MG_CL];  // pair forces by (bucket, component, j-slot, i-site)
+    int ent[PAIR_WPB][PAIR_WIN];      // kept entries of the window
+    int jf[PAIR_WPB][PAIR_WIN];       // their j-cluster << 1 | (self entry: only i-site < j-site)
+    unsigned char list[PAIR_WPB][MG_CL][PAIR_NJ];
+};
+
+// One warp per i-cluster I over the half of its list with J >= I: each unordered site pair
+// once (Newton's third law). A cluster's entry with itself is kept for the zero image (site
+// pairs a < b) and, when the cluster meets its own periodic image, for one of the images
+// +s / -s (all site pairs). Per window of PAIR_WIN list entries the kept ones are compacted
+// into shared memory in list order; per super-step of PAIR_SS of them:
+//   1. the j-rows (positions with info bits; charge and LJ rows; shifts) arrive by cp.async,
+//      one super-step ahead;
+//   2. lane (site a = lane & 7, q = lane >> 3) tests site a against j-slots 8e + 4h + q of each
+//      entry e (distance, molecule, ghost flags, RESPA bucket, a < b on the zero-image self
+//      entry);
+//   3. each site's active slots are listed (lane q's after those of lanes q' < q) and the
+//      site's four lanes take them in turn: the pair force goes to the lane's i-force partial
+//      and to fm[bucket][.][jj][a] (one writer per cell);
+//   4. the column sums of fm, in site order, are the j-forces of the super-step; they are
+//      added as 64-bit fixed point (units 2^-fixed_bits) to the slot-ordered accumulators.
+// At the end of the row the site's i-force (FP64, its four lanes summed in a fixed order) goes
+// to the same accumulators. A value outside the fixed-point range raises MG_FLAG_FIXED_RANGE:
+// the host then repeats the call with a coarser unit.
+template <int ELEC, bool MIC, bool SPLIT>
+__global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
+    constexpr int NB = SPLIT ? 2 : 1;  // force buckets
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PairSmem<NB> &S = *reinterpret_cast<PairSmem<NB> *>(smem_raw);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int a = lane & 7, q = lane >> 3;
+    const int I = blockIdx.x * PAIR_WPB + w;
+    double FL[3] = {0, 0, 0}, FS[3] = {0, 0, 0};
+    double E[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // uvdw ushift ureal vir (long bucket), then short
+    int npair = 0;
+    bool range_ok = true;
+    if (I < A.meta[0]) {
+        const float4 pi = A.xi[I * MG_CL + a];
+        const float4 qi = A.qp[I * MG_CL + a];
+        const int infi = info_of(pi.w);
+        const bool use_long = (A.mode & 1) != 0, use_short = (A.mode & 2) != 0;
+        const int e0 = A.pair_start[I], ne = A.pair_cnt[I];
+        float eL[4] = {0, 0, 0, 0}, eS[4] = {0, 0, 0, 0};  // energy partials since the last FP64 flush
+        float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;  // i-force partials since the last flush
+        int sstep = 0;
+        for (int r0 = 0; r0 < ne; r0 += PAIR_WIN) {
+            // compact the kept entries of window [r0, r0 + PAIR_WIN) in list order
+            int nk = 0;
+            for (int k0 = 0; k0 < PAIR_WIN && r0 + k0 < ne; k0 += 32) {
+                const int k = r0 + k0 + lane;
+                bool keep = false;
+                int jf = 0;
+                if (k < ne) {
+                    const int J = A.pair_j[e0 + k];
+                    bool self0 = false;
+                    keep = J > I;
+                    if (J == I) {
+                        const int img = A.pair_img[e0 + k];
+                        const int ix = (img & 1023) - 512, iy = ((img >> 10) & 1023) - 512,
+                                  iz = ((img >> 20) & 1023) - 512;
+                        self0 = ix == 0 && iy == 0 && iz == 0;
+                        keep = iz > 0 || (iz == 0 && (iy > 0 || (iy == 0 && ix >= 0)));
+                    }
+                    jf = (J << 1) | (self0 ? 1 : 0);
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int o = nk + __popc(bal & ((1u << lane) - 1u));
+                    S.ent[w][o] = e0 + k;
+                    S.jf[w][o] = jf;
+                }
+                nk += __popc(bal);
+            }
+            __syncwarp();
+            const int nss = (nk + PAIR_SS - 1) / PAIR_SS;
+            auto stage = [&](int ss, int buf) {
+                const int cnt = min(PAIR_SS, nk - ss * PAIR_SS);
+#pragma unroll
+                for (int k = 0; k < PAIR_NJ / 32; k++) {
+                    const int t = lane + 32 * k, e = t >> 3;
+                    if (e < cnt) {
+                        const int J = S.jf[w][ss * PAIR_SS + e] >> 1;
+                        cp_async16(&S.xj[w][buf][t], &A.xi[J * MG_CL + (t & 7)]);
+                        cp_async16(&S.qj[w][buf][t], &A.qp[J * MG_CL + (t & 7)]);
+                    }
+                }
+                if (lane < cnt) cp_async16(&S.sh[w][buf][lane], &A.pair_shift[S.ent[w][ss * PAIR_SS + lane]]);
+                asm volatile("cp.async.commit_group;" ::: "memory");
+            };
+            if (nss > 0) stage(0, 0);
+            for (int ss = 0; ss < nss; ss++, sstep++) {
+                const int b = ss & 1;
+                if (ss + 1 < nss) {
+                    stage(ss + 1, b ^ 1);
+                    asm volatile("cp.async.wait_group 1;" ::: "memory");
+                } else {
+                    asm volatile("cp.async.wait_group 0;" ::: "memory");
+                }
+                {  // clear the pair-force matrix of this super-step
+                    uint4 *fm = reinterpret_cast<uint4 *>(&S.fm[w][0][0][0][0]);
+                    constexpr int NF = (int)(NB * 3 * MG_CL * PAIR_NJ * sizeof(float) / 16);
+#pragma unroll 4
+                    for (int k = lane; k < NF; k += 32) fm[k] = make_uint4(0u, 0u, 0u, 0u);
+                }
+                __syncwarp();
+                const int cnt = min(PAIR_SS, nk - ss * PAIR_SS);
+                // 1. test
+                unsigned m = 0u;
+#pragma unroll
+                for (int e = 0; e < PAIR_SS; e++) {
+                    if (e < cnt) {
+                        const float4 sh = S.sh[w][b][e];
+                        const bool self0 = (S.jf[w][ss * PAIR_SS + e] & 1) != 0;
+                        const float xs = pi.x + sh.x, ys = pi.y + sh.y, zs = pi.z + sh.z;
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const int slot = 4 * h + q;
+                            const float4 pj = S.xj[w][b][8 * e + slot];
+                            float dx = xs - pj.x, dy = ys - pj.y, dz = zs - pj.z;
+                            if (MIC) {
+                                dx -= A.lx * rintf(dx * A.ilx);
+                                dy -= A.ly * rintf(dy * A.ily);
+                                dz -= A.lz * rintf(dz * A.ilz);
+                            }
+                            const float r2 = dx * dx + dy * dy + dz * dz;
+                            const int infj = info_of(pj.w);
+                            bool ok = !((infi | infj) & MG_SITE_DEAD) && ((infi ^ infj) >> 2) != 0 && r2 < A.rmax2 &&
+                                      !(self0 && slot <= a);
+                            if (SPLIT) ok = ok && (r2 < A.rs2 ? use_short : use_long);
+                            m |= (ok ? 1u : 0u) << (2 * e + h);
+                        }
+                    }
+                }
+                // 2. list the site's active slots
+                const int c0 = __popc(m);
+                int incl = c0;
+                int up = __shfl_up_sync(0xffffffffu, incl, 8);
+                if (q >= 1) incl += up;
+                up = __shfl_up_sync(0xffffffffu, incl, 16);
+                if (q >= 2) incl += up;
+                const int na = __shfl_sync(0xffffffffu, incl, 24 + a);
+                int off = incl - c0;
+                for (unsigned mm = m; mm; mm &= mm - 1u) {
+                    const int t = __ffs(mm) - 1;
+                    S.list[w][a][off++] = (unsigned char)(8 * (t >> 1) + 4 * (t & 1) + q);
+                }
+                __syncwarp();
+                const int rounds = __reduce_max_sync(0xffffffffu, (na + 3) >> 2);
+                // 3. pairs
+                for (int r = 0; r < rounds; r++) {
+                    const int k = 4 * r + q;
+                    if (k >= na) continue;
+                    const int jj = S.list[w][a][k];
+                    const PairOut o = pair_math<ELEC, MIC>(A, pi, qi, infi, S.xj[w][b][jj], S.qj[w][b][jj],
+                                                          S.sh[w][b][jj >> 3]);
+                    const bool inner = SPLIT && o.r2 < A.rs2;
+                    npair += 2;  // counted as in a full list
+                    const int bk = inner ? 1 : 0;
+                    S.fm[w][bk][0][jj][a] = o.fx;
+                    S.fm[w][bk][1][jj][a] = o.fy;
+                    S.fm[w][bk][2][jj][a] = o.fz;
+                    if (inner) {
+                        bx += o.fx; by += o.fy; bz += o.fz;
+                        eS[0] += o.ulj; eS[1] += o.ush; eS[2] += o.uel; eS[3] += o.vir;
+                    } else {
+                        ax += o.fx; ay += o.fy; az += o.fz;
+                        eL[0] += o.ulj; eL[1] += o.ush; eL[2] += o.uel; eL[3] += o.vir;
+                    }
+                }
+                if ((sstep + 1) % PAIR_FFLUSH == 0) {
+                    FL[0] += (double)ax; FL[1] += (double)ay; FL[2] += (double)az;
+                    ax = ay = az = 0;
+                    if (SPLIT) {
+                        FS[0] += (double)bx; FS[1] += (double)by; FS[2] += (double)bz;
+                        bx = by = bz = 0;
+                    }
+                }
+                if ((sstep + 1) % PAIR_EFLUSH == 0) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        E[k] += (double)eL[k];
+                        eL[k] = 0;
+                        if (SPLIT) {
+                            E[4 + k] += (double)eS[k];
+                            eS[k] = 0;
+                        }
+                    }
+                }
+                __syncwarp();
+                // 4. j-forces of the super-step: minus the column sums, in site order
+                for (int t = lane; t < cnt * MG_CL; t += 32) {
+                    const int J = S.jf[w][ss * PAIR_SS + (t >> 3)] >> 1;
+                    const long long slot = (long long)J * MG_CL + (t & 7);
+#pragma unroll
+                    for (int bk = 0; bk < NB; bk++) {
+                        unsigned long long *acc = bk ? A.facc_s : A.facc_l;
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            const float *col = S.fm[w][bk][c][t];
+                            float v = col[0];
+#pragma unroll
+                            for (int i = 1; i < MG_CL; i++) v += col[i];
+                            if (v != 0.f) {
+                                long long o;
+                                range_ok &= to_fixed(-v, o, A.fscale, A.flimit);
+                                atomicAdd(acc + c * A.fstride + slot, (unsigned long long)o);
+                            }
+                        }
+                    }
+                }
+                __syncwarp();  // buffer b and the matrix are free for the next super-step
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {  // the last partials
+            E[k] += (double)eL[k];
+            if (SPLIT) E[4 + k] += (double)eS[k];
+        }
+        FL[0] += (double)ax; FL[1] += (double)ay; FL[2] += (double)az;
+        if (SPLIT) {
+            FS[0] += (double)bx; FS[1] += (double)by; FS[2] += (double)bz;
+        }
+        // i-forces: the site's four lanes in FP64, a fixed order, then fixed point
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            FL[k] += __shfl_xor_sync(0xffffffffu, FL[k], 8);
+            FL[k] += __shfl_xor_sync(0xffffffffu, FL[k], 16);
+            if (SPLIT) {
+                FS[k] += __shfl_xor_sync(0xffffffffu, FS[k], 8);
+                FS[k] += __shfl_xor_sync(0xffffffffu, FS[k], 16);
+            }
+        }
+        if (q == 0 && !(infi & MG_SITE_DEAD)) {
+            const long long slot = (long long)I * MG_CL + a;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                long long o;
+                if (FL[c] != 0.0) {
+                    range_ok &= to_fixed(FL[c], o, A.fscale, A.flimit);
+                    atomicAdd(A.facc_l + c * A.fstride + slot, (unsigned long long)o);
+                }
+                if (SPLIT && FS[c] != 0.0) {
+                    range_ok &= to_fixed(FS[c], o, A.fscale, A.flimit);
+                    atomicAdd(A.facc_s + c * A.fstride + slot, (unsigned long long)o);
+                }
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, !range_ok) && lane == 0) atomicOr(A.flags, MG_FLAG_FIXED_RANGE);
+    double eng[9];
+#pragma unroll
+    for (int k = 0; k < 8; k++) eng[k] = E[k];
+    eng[8] = (double)npair;
+    const int ids[9] = {E_UVDW, E_USHIFT, E_UREAL, E_VIR, E_UVDW_S, E_USHIFT_S, E_UREAL_S, E_VIR_S, E_NPAIR};
+    mg_block_row<9>(eng, ids, A.rows, A.row0 + blockIdx.x);
+}
+
+// The fixed-point slot accumulators into FP64 forces in site order (overwriting fl / fs, when
+// given), clearing every accumulator for the next evaluation.
+__global__ void k_fixed_forces(const int *__restrict__ meta, const int *__restrict__ cl_atom, int n,
+                               unsigned long long *__restrict__ facc_l, unsigned long long *__restrict__ facc_s,
+                               long long fstride, double unit, double *__restrict__ fl, double *__restrict__ fs) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= fstride) return;
+    const int at = s < (long long)meta[0] * MG_CL ? cl_atom[s] : -1;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const long long vl = (long long)facc_l[c * fstride + s];
+        facc_l[c * fstride + s] = 0ull;
+        if (at >= 0 && fl) fl[(size_t)c * n + at] = (double)vl * unit;
+        if (facc_s) {
+            const long long vs = (long long)facc_s[c * fstride + s];
+            facc_s[c * fstride + s] = 0ull;
+            if (at >= 0 && fs) fs[(size_t)c * n + at] = (double)vs * unit;
+        }
+    }
+}
+
+template <int ELEC, bool MIC, bool SPLIT>
+cudaError_t launch_pair_one(const PairArgs &A, unsigned blocks, cudaStream_t s) {
+    const int smem = (int)sizeof(PairSmem<SPLIT ? 2 : 1>);
+    cudaError_t e = cudaFuncSetAttribute(k_pair<ELEC, MIC, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_pair<ELEC, MIC, SPLIT><<<blocks, PAIR_WPB * 32, smem, s>>>(A);
+    return cudaGetLastError();
+}
+
+template <int ELEC>
+cudaError_t launch_pair_elec(const PairArgs &A, bool mic, bool split, unsigned blocks, cudaStream_t s) {
+    if (mic) return split ? launch_pair_one<ELEC, true, true>(A, blocks, s) : launch_pair_one<ELEC, true, false>(A, blocks, s);
+    return split ? launch_pair_one<ELEC, false, true>(A, blocks, s) : launch_pair_one<ELEC, false, false>(A, blocks, s);
 }
 
 // fixed-order reduction of the partial rows: one block per component
@@ -305,60 +705,114 @@ __global__ void k_check(const double *__restrict__ f, int n3, unsigned *__restri
 
 mg_status mg_launch_pair(mg_ctx *c, int want_long, int want_short, double *fl, double *fs) {
     const mg_params &p = c->params;
+    const int elec = p.charge_type == MG_ELEC_EWALD ? 1 : (p.charge_type == MG_ELEC_WOLF ? 2 : 0);
+    const bool split = p.respa_split > 0;
+    const double rs2 = split ? p.respa_split * p.respa_split : 0.0;
+    double rmax2 = elec ? fmax(p.rcutoffsq, p.rcutoffelecsq) : p.rcutoffsq;
+    if (split && !want_long) rmax2 = fmin(rmax2, rs2);
+    // the inner pass of the distance split walks only the inner sub-list
+    const bool sub = want_short && !want_long && c->sub_ready;
+    const int *pstart = (const int *)(sub ? c->d_sub_start.p : c->d_pair_start.p);
+    const int *pcnt = (const int *)(sub ? c->d_sub_count.p : c->d_pair_count.p);
+    const int *pj = (const int *)(sub ? c->d_sub_j.p : c->d_pair_j.p);
+    const void *pshift = sub ? c->d_sub_shift.p : c->d_pair_shift.p;
+    const int *pimg = (const int *)(sub ? c->d_sub_img.p : c->d_pair_img.p);
+    const unsigned blocks = (unsigned)((c->cl_cap + PAIR_WPB - 1) / PAIR_WPB);
+    if (blocks == 0) return MG_OK;
+    const int row0 = mg_reserve_rows(c, blocks);
+    if (row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
+    const int mode = (want_long ? 1 : 0) | (want_short ? 2 : 0);
+    if (c->opt.precision == MG_PREC_FP64) {  // the plain-FP64 path: full list, FP64 sums, no atomics
+        PairFullArgs F;
+        F.n = c->natom;
+        F.meta = (const int *)c->d_meta.p;
+        F.pair_start = pstart;
+        F.pair_cnt = pcnt;
+        F.pair_j = pj;
+        F.info = (const int *)c->d_pack_info.p;
+        F.cl_atom = (const int *)c->d_cl_atom.p;
+        F.pair_shift = pshift;
+        F.pos = c->d_pack_pos.p;
+        F.lj = c->d_pack_lj.p;
+        F.fl = want_long ? fl : nullptr;
+        F.fs = want_short ? fs : nullptr;
+        F.rc2 = p.rcutoffsq, F.rce2 = p.rcutoffelecsq, F.rs2 = rs2, F.rmax2 = rmax2;
+        F.lx = c->lx, F.ly = c->ly, F.lz = c->lz;
+        F.kappa = p.kappa, F.coul = p.coulomb_prefactor, F.shift1 = p.shift1, F.ron2 = p.rcutonsq;
+        F.roff2 = p.rcutoffsq, F.sw_denom = p.roff2_minus_ron2_cube, F.rce = p.rcutoffelec;
+        F.v1 = p.wolfvcon1, F.v2 = p.wolfvcon2, F.f1 = p.wolffcon1, F.f2 = p.wolffcon2;
+        F.ljsw = p.lj_switch;
+        F.mode = mode;
+        F.rows = (double *)c->d_epart.p;
+        F.row0 = row0;
+        if (elec == 1) launch_pair_full_elec<1>(F, c->small_box, split, blocks, c->stream);
+        else if (elec == 2) launch_pair_full_elec<2>(F, c->small_box, split, blocks, c->stream);
+        else launch_pair_full_elec<0>(F, c->small_box, split, blocks, c->stream);
+        MG_CUDA(cudaGetLastError());
+        c->launches += 1;
+        return MG_OK;
+    }
     PairArgs A;
     A.n = c->natom;
     A.meta = (const int *)c->d_meta.p;
-    A.pair_start = (int *)c->d_pair_start.p;
-    A.pair_cnt = (int *)c->d_pair_count.p;
-    A.pair_j = (int *)c->d_pair_j.p;
-    A.pair_shift = c->d_pair_shift.p;
-    if (want_short && !want_long && c->sub_ready) {
-        // the inner pass of the distance split walks only the inner sub-list
-        A.pair_start = (int *)c->d_sub_start.p;
-        A.pair_cnt = (int *)c->d_sub_count.p;
-        A.pair_j = (int *)c->d_sub_j.p;
-        A.pair_shift = c->d_sub_shift.p;
+    A.pair_start = pstart;
+    A.pair_cnt = pcnt;
+    A.pair_j = pj;
+    A.pair_img = pimg;
+    A.pair_shift = (const float4 *)pshift;
+    A.xi = (const float4 *)c->d_pack_xi.p;
+    A.qp = (const float4 *)c->d_pack_qp.p;
+    A.cl_atom = (const int *)c->d_cl_atom.p;
+    // fixed-point force accumulators per cluster slot, one [3][slots] block per bucket: zero
+    // when allocated, cleared again by k_fixed_forces after every use
+    A.fstride = (long long)c->cl_cap * MG_CL;
+    const size_t fbytes = sizeof(unsigned long long) * 3 * (size_t)A.fstride;
+    if (c->d_facc.bytes < 2 * fbytes) {
+        if (!mg_ensure(c, c->d_facc, 2 * fbytes)) return MG_ERR_ALLOC;
+        MG_CUDA(cudaMemsetAsync(c->d_facc.p, 0, c->d_facc.bytes, c->stream));
     }
-    A.pos = c->d_pack_pos.p;
-    A.lj = c->d_pack_lj.p;
-    A.info = (int *)c->d_pack_info.p;
-    A.cl_atom = (int *)c->d_cl_atom.p;
-    A.fl = want_long ? fl : nullptr;
-    A.fs = want_short ? fs : nullptr;
-    int elec = p.charge_type == MG_ELEC_EWALD ? 1 : (p.charge_type == MG_ELEC_WOLF ? 2 : 0);
-    A.rc2 = p.rcutoffsq;
-    A.rce2 = p.rcutoffelecsq;
-    bool split = p.respa_split > 0;
-    A.rs2 = split ? p.respa_split * p.respa_split : 0.0;
-    A.rmax2 = elec ? fmax(p.rcutoffsq, p.rcutoffelecsq) : p.rcutoffsq;
-    if (split && !want_long) A.rmax2 = fmin(A.rmax2, A.rs2);
-    A.lx = c->lx;
-    A.ly = c->ly;
-    A.lz = c->lz;
-    A.kappa = p.kappa;
-    A.coul = p.coulomb_prefactor;
-    A.shift1 = p.shift1;
-    A.ron2 = p.rcutonsq;
-    A.roff2 = p.rcutoffsq;
-    A.sw_denom = p.roff2_minus_ron2_cube;
-    A.rce = p.rcutoffelec;
-    A.v1 = p.wolfvcon1;
-    A.v2 = p.wolfvcon2;
-    A.f1 = p.wolffcon1;
-    A.f2 = p.wolffcon2;
+    A.facc_l = (unsigned long long *)c->d_facc.p;
+    A.facc_s = A.facc_l + 3 * A.fstride;
+    A.fscale = ldexpf(1.0f, c->fixed_bits);
+    A.flimit = ldexpf(1.0f, 52 - c->fixed_bits);
+    A.flags = (unsigned *)c->d_flags.p;
+    A.rc2 = (float)p.rcutoffsq;
+    A.rce2 = (float)p.rcutoffelecsq;
+    A.rs2 = (float)rs2;
+    A.rmax2 = (float)rmax2;
+    A.lx = (float)c->lx;
+    A.ly = (float)c->ly;
+    A.lz = (float)c->lz;
+    A.ilx = (float)(1.0 / c->lx);
+    A.ily = (float)(1.0 / c->ly);
+    A.ilz = (float)(1.0 / c->lz);
+    A.kappa = (float)p.kappa;
+    A.coul = (float)p.coulomb_prefactor;
+    A.shift1 = (float)p.shift1;
+    A.ron2 = (float)p.rcutonsq;
+    A.roff2 = (float)p.rcutoffsq;
+    A.sw_denom = (float)p.roff2_minus_ron2_cube;
+    A.rce = (float)p.rcutoffelec;
+    A.v1 = (float)p.wolfvcon1;
+    A.v2 = (float)p.wolfvcon2;
+    A.f1 = (float)p.wolffcon1;
+    A.f2 = (float)p.wolffcon2;
     A.ljsw = p.lj_switch;
-    A.mode = (want_long ? 1 : 0) | (want_short ? 2 : 0);
-    unsigned blocks = (unsigned)((c->cl_cap + PAIR_WPB - 1) / PAIR_WPB);
-    if (blocks == 0) return MG_OK;
+    A.mode = mode;
     A.rows = (double *)c->d_epart.p;
-    A.row0 = mg_reserve_rows(c, blocks);
-    if (A.row0 < 0) return mg_fail(c, MG_ERR_ALLOC, "energy partial rows exhausted");
-    if (c->opt.precision == MG_PREC_FP64)
-        launch_pair<double>(A, elec, c->small_box, split, blocks, c->stream);
-    else
-        launch_pair<float>(A, elec, c->small_box, split, blocks, c->stream);
+    A.row0 = row0;
+    cudaError_t e;
+    if (elec == 1) e = launch_pair_elec<1>(A, c->small_box, split, blocks, c->stream);
+    else if (elec == 2) e = launch_pair_elec<2>(A, c->small_box, split, blocks, c->stream);
+    else e = launch_pair_elec<0>(A, c->small_box, split, blocks, c->stream);
+    MG_CUDA(e);
+    // both buckets the kernel may have written are cleared, whether or not they are wanted
+    const unsigned fblocks = (unsigned)((A.fstride + 255) / 256);
+    k_fixed_forces<<<fblocks, 256, 0, c->stream>>>(A.meta, A.cl_atom, A.n, A.facc_l, split ? A.facc_s : nullptr,
+                                                   A.fstride, ldexp(1.0, -c->fixed_bits), want_long ? fl : nullptr,
+                                                   want_short ? fs : nullptr);
     MG_CUDA(cudaGetLastError());
-    c->launches += 1;
+    c->launches += 2;
     return MG_OK;
 }
 
