@@ -270,7 +270,12 @@ void launch_pair_full_elec(const PairFullArgs &A, bool mic, bool split, unsigned
 // ---------------------------------------------------------------------------------
 #define PAIR_SS 8       // j-cluster entries per super-step
 #define PAIR_NJ (PAIR_SS * MG_CL)
+#ifndef PAIR_WIN
 #define PAIR_WIN 128    // list entries compacted per window (the kept ones: J >= I)
+#endif
+#ifndef PAIR_ILP
+#define PAIR_ILP 1      // listed pairs a lane evaluates per round
+#endif
 #define PAIR_FFLUSH 2   // super-steps between the FP64 flushes of a lane's i-force partials
 #define PAIR_EFLUSH 8   // super-steps between the FP64 flushes of a lane's energy partials
 
@@ -299,15 +304,25 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
 }
 
+// x rounded to the nearest integer (ties to even) as a 64-bit integer, for |x| < 2^53, with
+// integer and FP32 operations only (the 64-bit conversion instructions run on the FP64 pipe,
+// which is slow on this part): x = m 2^e with a 24-bit integer mantissa m; for e >= 0 the
+// value is m << e, for |x| < 2^23 adding 2^23 rounds it to an integer held in the low
+// mantissa bits.
+__device__ __forceinline__ long long f2ll_rn(float x) {
+    const unsigned u = __float_as_uint(x);
+    const int e = (int)((u >> 23) & 255u) - 150;
+    const long long big = (long long)((u & 0x7fffffu) | 0x800000u) << (e > 0 ? (e < 40 ? e : 40) : 0);
+    const long long small = (long long)(__float_as_uint(fabsf(x) + 8388608.0f) - 0x4B000000u);
+    const long long r = e >= 0 ? big : small;
+    return (u >> 31) ? -r : r;
+}
+
 // force component -> 64-bit fixed point in units of 1/scale; false when out of range or not
 // finite (the limit, 2^52 units, leaves room for 2048 contributions of that size in one sum)
 __device__ __forceinline__ bool to_fixed(float v, long long &o, float scale, float limit) {
-    o = __float2ll_rn(v * scale);
+    o = f2ll_rn(v * scale);
     return fabsf(v) < limit;
-}
-__device__ __forceinline__ bool to_fixed(double v, long long &o, float scale, float limit) {
-    o = __double2ll_rn(v * (double)scale);
-    return fabs(v) < (double)limit;
 }
 
 struct PairOut {
@@ -387,7 +402,9 @@ struct PairSmem {
     float4 xj[PAIR_WPB][2][PAIR_NJ];  // x, y, z (cluster-relative), info bits
     float4 qj[PAIR_WPB][2][PAIR_NJ];  // q, half-sigma, sqrt-eps
     float4 sh[PAIR_WPB][2][PAIR_SS];  // periodic shift of each entry
-    float fm[PAIR_WPB][NB][3][PAIR_NJ][MG_CL];  // pair forces by (bucket, component, j-slot, i-site)
+    // pair forces by (bucket, component, j-slot, i-site a ^ ((j-slot >> 2) & 7)): the four lanes
+    // of a site write j-slots of one residue mod 4, which the XOR spreads over the banks
+    float fm[PAIR_WPB][NB][3][PAIR_NJ][MG_CL];
     int ent[PAIR_WPB][PAIR_WIN];      // kept entries of the window
     int jf[PAIR_WPB][PAIR_WIN];       // their j-cluster << 1 | (self entry: only i-site < j-site)
     unsigned char list[PAIR_WPB][MG_CL][PAIR_NJ];
@@ -419,7 +436,7 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int a = lane & 7, q = lane >> 3;
     const int I = blockIdx.x * PAIR_WPB + w;
-    double FL[3] = {0, 0, 0}, FS[3] = {0, 0, 0};
+    long long FL[3] = {0, 0, 0}, FS[3] = {0, 0, 0};  // i-force sums in fixed point
     double E[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // uvdw ushift ureal vir (long bucket), then short
     int npair = 0;
     bool range_ok = true;
@@ -534,33 +551,48 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                     S.list[w][a][off++] = (unsigned char)(8 * (t >> 1) + 4 * (t & 1) + q);
                 }
                 __syncwarp();
-                const int rounds = __reduce_max_sync(0xffffffffu, (na + 3) >> 2);
-                // 3. pairs
+                // 3. pairs: the site's four lanes take its listed pairs in turn, PAIR_ILP at a time
+                //    as independent chains
+                const int rounds = __reduce_max_sync(0xffffffffu, (na + 4 * PAIR_ILP - 1) / (4 * PAIR_ILP));
                 for (int r = 0; r < rounds; r++) {
-                    const int k = 4 * r + q;
-                    if (k >= na) continue;
-                    const int jj = S.list[w][a][k];
-                    const PairOut o = pair_math<ELEC, MIC>(A, pi, qi, infi, S.xj[w][b][jj], S.qj[w][b][jj],
-                                                          S.sh[w][b][jj >> 3]);
-                    const bool inner = SPLIT && o.r2 < A.rs2;
-                    npair += 2;  // counted as in a full list
-                    const int bk = inner ? 1 : 0;
-                    S.fm[w][bk][0][jj][a] = o.fx;
-                    S.fm[w][bk][1][jj][a] = o.fy;
-                    S.fm[w][bk][2][jj][a] = o.fz;
-                    if (inner) {
-                        bx += o.fx; by += o.fy; bz += o.fz;
-                        eS[0] += o.ulj; eS[1] += o.ush; eS[2] += o.uel; eS[3] += o.vir;
-                    } else {
-                        ax += o.fx; ay += o.fy; az += o.fz;
-                        eL[0] += o.ulj; eL[1] += o.ush; eL[2] += o.uel; eL[3] += o.vir;
+                    PairOut o[PAIR_ILP];
+                    int jl[PAIR_ILP];
+#pragma unroll
+                    for (int u = 0; u < PAIR_ILP; u++) {
+                        const int k = 4 * (PAIR_ILP * r + u) + q;
+                        jl[u] = k < na ? S.list[w][a][k] : -1;
+                        const int jj = jl[u] < 0 ? 0 : jl[u];
+                        o[u] = pair_math<ELEC, MIC>(A, pi, qi, infi, S.xj[w][b][jj], S.qj[w][b][jj], S.sh[w][b][jj >> 3]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < PAIR_ILP; u++) {
+                        const int jj = jl[u];
+                        if (jj < 0) continue;
+                        const bool inner = SPLIT && o[u].r2 < A.rs2;
+                        npair += 2;  // counted as in a full list
+                        const int bk = inner ? 1 : 0, col = a ^ ((jj >> 2) & 7);
+                        S.fm[w][bk][0][jj][col] = o[u].fx;
+                        S.fm[w][bk][1][jj][col] = o[u].fy;
+                        S.fm[w][bk][2][jj][col] = o[u].fz;
+                        if (inner) {
+                            bx += o[u].fx; by += o[u].fy; bz += o[u].fz;
+                            eS[0] += o[u].ulj; eS[1] += o[u].ush; eS[2] += o[u].uel; eS[3] += o[u].vir;
+                        } else {
+                            ax += o[u].fx; ay += o[u].fy; az += o[u].fz;
+                            eL[0] += o[u].ulj; eL[1] += o[u].ush; eL[2] += o[u].uel; eL[3] += o[u].vir;
+                        }
                     }
                 }
                 if ((sstep + 1) % PAIR_FFLUSH == 0) {
-                    FL[0] += (double)ax; FL[1] += (double)ay; FL[2] += (double)az;
+                    long long o;
+                    range_ok &= to_fixed(ax, o, A.fscale, A.flimit); FL[0] += o;
+                    range_ok &= to_fixed(ay, o, A.fscale, A.flimit); FL[1] += o;
+                    range_ok &= to_fixed(az, o, A.fscale, A.flimit); FL[2] += o;
                     ax = ay = az = 0;
                     if (SPLIT) {
-                        FS[0] += (double)bx; FS[1] += (double)by; FS[2] += (double)bz;
+                        range_ok &= to_fixed(bx, o, A.fscale, A.flimit); FS[0] += o;
+                        range_ok &= to_fixed(by, o, A.fscale, A.flimit); FS[1] += o;
+                        range_ok &= to_fixed(bz, o, A.fscale, A.flimit); FS[2] += o;
                         bx = by = bz = 0;
                     }
                 }
@@ -605,11 +637,18 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
             E[k] += (double)eL[k];
             if (SPLIT) E[4 + k] += (double)eS[k];
         }
-        FL[0] += (double)ax; FL[1] += (double)ay; FL[2] += (double)az;
-        if (SPLIT) {
-            FS[0] += (double)bx; FS[1] += (double)by; FS[2] += (double)bz;
+        {
+            long long o;
+            range_ok &= to_fixed(ax, o, A.fscale, A.flimit); FL[0] += o;
+            range_ok &= to_fixed(ay, o, A.fscale, A.flimit); FL[1] += o;
+            range_ok &= to_fixed(az, o, A.fscale, A.flimit); FL[2] += o;
+            if (SPLIT) {
+                range_ok &= to_fixed(bx, o, A.fscale, A.flimit); FS[0] += o;
+                range_ok &= to_fixed(by, o, A.fscale, A.flimit); FS[1] += o;
+                range_ok &= to_fixed(bz, o, A.fscale, A.flimit); FS[2] += o;
+            }
         }
-        // i-forces: the site's four lanes in FP64, a fixed order, then fixed point
+        // i-forces: the site's four lanes (integer sums, exact in any order)
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             FL[k] += __shfl_xor_sync(0xffffffffu, FL[k], 8);
@@ -623,15 +662,8 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
             const long long slot = (long long)I * MG_CL + a;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                long long o;
-                if (FL[c] != 0.0) {
-                    range_ok &= to_fixed(FL[c], o, A.fscale, A.flimit);
-                    atomicAdd(A.facc_l + c * A.fstride + slot, (unsigned long long)o);
-                }
-                if (SPLIT && FS[c] != 0.0) {
-                    range_ok &= to_fixed(FS[c], o, A.fscale, A.flimit);
-                    atomicAdd(A.facc_s + c * A.fstride + slot, (unsigned long long)o);
-                }
+                if (FL[c] != 0) atomicAdd(A.facc_l + c * A.fstride + slot, (unsigned long long)FL[c]);
+                if (SPLIT && FS[c] != 0) atomicAdd(A.facc_s + c * A.fstride + slot, (unsigned long long)FS[c]);
             }
         }
     }
@@ -645,23 +677,31 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
 }
 
 // The fixed-point slot accumulators into FP64 forces in site order (overwriting fl / fs, when
-// given), clearing every accumulator for the next evaluation.
+// given), clearing every accumulator for the next evaluation. All loads are issued before the
+// stores.
 __global__ void k_fixed_forces(const int *__restrict__ meta, const int *__restrict__ cl_atom, int n,
                                unsigned long long *__restrict__ facc_l, unsigned long long *__restrict__ facc_s,
                                long long fstride, double unit, double *__restrict__ fl, double *__restrict__ fs) {
     const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= fstride) return;
     const int at = s < (long long)meta[0] * MG_CL ? cl_atom[s] : -1;
+    long long vl[3], vs[3] = {0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 3; c++) vl[c] = (long long)__ldcg(facc_l + c * fstride + s);
+    if (facc_s) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) vs[c] = (long long)__ldcg(facc_s + c * fstride + s);
+    }
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const long long vl = (long long)facc_l[c * fstride + s];
         facc_l[c * fstride + s] = 0ull;
-        if (at >= 0 && fl) fl[(size_t)c * n + at] = (double)vl * unit;
-        if (facc_s) {
-            const long long vs = (long long)facc_s[c * fstride + s];
-            facc_s[c * fstride + s] = 0ull;
-            if (at >= 0 && fs) fs[(size_t)c * n + at] = (double)vs * unit;
-        }
+        if (facc_s) facc_s[c * fstride + s] = 0ull;
+    }
+    if (at < 0) return;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (fl) fl[(size_t)c * n + at] = (double)vl[c] * unit;
+        if (fs) fs[(size_t)c * n + at] = (double)vs[c] * unit;
     }
 }
 
