@@ -506,16 +506,17 @@ def _fmt(v: float) -> str:
     return repr(float(v))
 
 
-def write_reference_dir(s: System, path: str, grid_names=None) -> None:
+def write_reference_dir(s: System, path: str, grid_names=None, nstep_trj: int = 0) -> None:
     """Write in.mspms / cfg.mspms / xyz.mspms that src/readins.c reads back to `s`
-    (values written in input units: A, K, kg/mol)."""
+    (values written in input units: A, K, kg/mol); nstep_trj > 0 asks the program for a
+    trajectory frame (trj.mspms) every nstep_trj steps."""
     os.makedirs(path, exist_ok=True)
     sb, eb = s.sigma_base, s.epsilon_base
     L = s.box * sb
     lines = [s.title, f"{s.seeds[0]}", f"{s.seeds[1]}", _fmt(sb), _fmt(eb), _fmt(s.mass_base),
              _fmt(s.treq_K), _fmt(s.preq_bar), _fmt(L[0]), _fmt(L[1]), _fmt(L[2]),
              _fmt(s.rcuton * sb), _fmt(s.rcutoff * sb), _fmt(s.rcutoffelec * sb), f"{s.lj_lrc}",
-             f"{s.lj_switch}", "1", f"{s.nstep}", "0", "1", "1", "1000000", "1000000", "0",
+             f"{s.lj_switch}", "1", f"{s.nstep}", "0", "1", "1", "1000000", "1000000", f"{int(nstep_trj)}",
              _fmt(s.delt_fs), f"{s.nstep_inner}", _fmt(s.f0), f"{s.what_simulation}",
              f"{s.what_ensemble}", f"{s.nconstraint}", "0", f"{s.charge_type}", f"{s.sf_type}", "0",
              ""]

@@ -13,9 +13,10 @@
 #      molecule with itself for iMole >= 1 and returns NaN);
 #   2. src/molevars.h:6-13 - NATOM_MAX/NMOLE_MAX/NBOND_MAX/NANGLE_MAX raised so the
 #      benchmark systems fit.
-# Also built: tools/sfgridgen.c (the solid-fluid grid generator) as oracle/_ref/sfgridgen.
-# Left out: src/mspms2.c (its main() is replaced by oracle/ref_harness.c) and
-# src/dftmcff.c (needs GSL). The Fortran grid library mylibtasos/ cannot be compiled
+# Also built: tools/sfgridgen.c (the solid-fluid grid generator) as oracle/_ref/sfgridgen, and
+# the reference program itself (src/mspms2.c's main) as oracle/_ref/mspms2_ref.
+# Left out of mspms_ref_force: src/mspms2.c (its main() is replaced by oracle/ref_harness.c);
+# left out of both: src/dftmcff.c (needs GSL). The Fortran grid library mylibtasos/ cannot be compiled
 # here (no gfortran); oracle/ref_stubs.c supplies its four entry points on top of the
 # C restatement in oracle/mspms_oracle.c.
 set -e
@@ -53,8 +54,14 @@ for f in "$OUT"/build/src/*.c "$HERE/ref_harness.c" "$HERE/ref_stubs.c" "$HERE/m
   OBJS="$OBJS $o"
 done
 $CC -o "$OUT/mspms_ref_force" $OBJS -lm
-rm -rf "$OUT/build"
 echo "built $OUT/mspms_ref_force"
+# the reference program itself (its main, src/mspms2.c, with the same two patches and the
+# same stand-ins): the CPU side of the drop-in comparison in mspms2_gb300/shim/compare_md.py
+cp "$REF/src/mspms2.c" "$OUT/build/src/mspms2.c"
+$CC $CFLAGS -I"$OUT/build/src" -c "$OUT/build/src/mspms2.c" -o "$OUT/build/mspms2.o"
+$CC -o "$OUT/mspms2_ref" $(echo $OBJS | tr ' ' '\n' | grep -v '/ref_harness.o$' | tr '\n' ' ') "$OUT/build/mspms2.o" -lm
+echo "built $OUT/mspms2_ref"
+rm -rf "$OUT/build"
 # the reference's solid-fluid grid generator, unchanged, read where it lies
 if [ -f "$REF/tools/sfgridgen.c" ]; then
   $CC -O2 -ffp-contract=off -w -o "$OUT/sfgridgen" "$REF/tools/sfgridgen.c" -lm
