@@ -220,6 +220,62 @@ int orc_md_run(const orc_system *s, const mg_md_params *mp, int nsteps, double *
 /* ---- the canonical HMC move of one replica (src/hmc.c:23-40, src/dispmd.c:12-103) ------ */
 #include "../include/mg_philox.h"
 
+/* velinit (src/initvars.c:151-229) of move mv of a replica with the Philox streams of the
+ * engine: Gaussian velocities sqrt(T/m) g, the total momentum removed and, with rescale, the
+ * kinetic energy set to exactly treq nfree / 2; returns that kinetic energy */
+static double hmc_velinit(const mg_hmc_params *hp, int replica, int move, int n, double *vx, double *vy,
+                          double *vz) {
+    const uint32_t key[2] = {(uint32_t)(hp->seed & 0xffffffffull), (uint32_t)(hp->seed >> 32)};
+    const uint32_t mv = (uint32_t)move;
+    const double nfree = (double)(3 * n - hp->nconstraint);
+    const double stdv = sqrt(hp->treq) / sqrt(hp->mass);
+    double px = 0.0, py = 0.0, pz = 0.0, sysm = 0.0;
+    for (int i = 0; i < n; i++) {
+        const uint32_t c0[4] = {(uint32_t)i, mv, 0u, (uint32_t)replica}, c1[4] = {(uint32_t)i, mv, 1u, (uint32_t)replica};
+        uint32_t w0[4], w1[4];
+        double g0, g1, g2, g3;
+        mg_philox4x32_10(c0, key, w0);
+        mg_philox4x32_10(c1, key, w1);
+        mg_gauss2(w0, &g0, &g1);
+        mg_gauss2(w1, &g2, &g3);
+        vx[i] = stdv * g0;
+        vy[i] = stdv * g1;
+        vz[i] = stdv * g2;
+        px += vx[i] * hp->mass;
+        py += vy[i] * hp->mass;
+        pz += vz[i] * hp->mass;
+        sysm += hp->mass;
+    }
+    px /= sysm;
+    py /= sysm;
+    pz /= sysm;
+    double ukin = 0.0;
+    for (int i = 0; i < n; i++) {
+        vx[i] -= px;
+        vy[i] -= py;
+        vz[i] -= pz;
+        ukin += hp->mass * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+    }
+    ukin = 0.5 * ukin;
+    if (hp->rescale) {
+        const double tinst = 2.0 * ukin / nfree, scaling = sqrt(hp->treq / tinst);
+        ukin = 0.0;
+        for (int i = 0; i < n; i++) {
+            vx[i] *= scaling;
+            vy[i] *= scaling;
+            vz[i] *= scaling;
+            ukin += hp->mass * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        }
+        ukin = 0.5 * ukin;
+    }
+    return ukin;
+}
+
+int orc_hmc_velocities(const mg_hmc_params *hp, int replica, int move, int n, double *vx, double *vy, double *vz) {
+    hmc_velinit(hp, replica, move, n, vx, vy, vz);
+    return 0;
+}
+
 int orc_hmc_replica(const orc_system *s, const mg_hmc_params *hp, int replica, int move0, int nmoves, double *xx,
                     double *yy, double *zz, int *accepted, double *dh_log, double *energy) {
     const int n = orc_natom(s);
@@ -238,49 +294,11 @@ int orc_hmc_replica(const orc_system *s, const mg_hmc_params *hp, int replica, i
     double e_cur = 0.0;
     for (int m = 0; m < nmoves; m++) {
         const uint32_t mv = (uint32_t)(move0 + m);
-        /* velinit (src/initvars.c:151-229) with the Philox streams */
-        const double stdv = sqrt(hp->treq) / sqrt(hp->mass);
-        double px = 0.0, py = 0.0, pz = 0.0, sysm = 0.0;
+        const double ukin = hmc_velinit(hp, replica, move0 + m, n, vx, vy, vz);
         for (int i = 0; i < n; i++) {
-            const uint32_t c0[4] = {(uint32_t)i, mv, 0u, (uint32_t)replica}, c1[4] = {(uint32_t)i, mv, 1u, (uint32_t)replica};
-            uint32_t w0[4], w1[4];
-            double g0, g1, g2, g3;
-            mg_philox4x32_10(c0, key, w0);
-            mg_philox4x32_10(c1, key, w1);
-            mg_gauss2(w0, &g0, &g1);
-            mg_gauss2(w1, &g2, &g3);
-            vx[i] = stdv * g0;
-            vy[i] = stdv * g1;
-            vz[i] = stdv * g2;
-            px += vx[i] * hp->mass;
-            py += vy[i] * hp->mass;
-            pz += vz[i] * hp->mass;
-            sysm += hp->mass;
             ox[i] = xx[i];
             oy[i] = yy[i];
             oz[i] = zz[i];
-        }
-        px /= sysm;
-        py /= sysm;
-        pz /= sysm;
-        double ukin = 0.0;
-        for (int i = 0; i < n; i++) {
-            vx[i] -= px;
-            vy[i] -= py;
-            vz[i] -= pz;
-            ukin += hp->mass * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
-        }
-        ukin = 0.5 * ukin;
-        if (hp->rescale) {
-            const double tinst = 2.0 * ukin / mp.nfree, scaling = sqrt(hp->treq / tinst);
-            ukin = 0.0;
-            for (int i = 0; i < n; i++) {
-                vx[i] *= scaling;
-                vy[i] *= scaling;
-                vz[i] *= scaling;
-                ukin += hp->mass * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
-            }
-            ukin = 0.5 * ukin;
         }
         /* frclong + frcshort, then md_move over vver: orc_md_run evaluates the forces at
          * the start and records U0 and U1 */

@@ -109,6 +109,9 @@ int orc_md_run(const orc_system *s, const mg_md_params *p, int nsteps, double *x
 int orc_hmc_replica(const orc_system *s, const mg_hmc_params *p, int replica, int move0, int nmoves, double *x,
                     double *y, double *z, int *accepted, double *dh_log, double *energy);
 
+/* The velocities mg_hmc_batch draws for move `move` of replica `replica` (velinit with the
+ * Philox streams, the momentum removed, rescaled with hp->rescale), for n sites. */
+int orc_hmc_velocities(const mg_hmc_params *hp, int replica, int move, int n, double *vx, double *vy, double *vz);
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 int orc_npt_run(const orc_system *s, const mg_npt_params *p, int nsteps, double *x, double *y, double *z,
                 double *vx, double *vy, double *vz, double *box, mg_npt_state *st, double *log);

@@ -304,6 +304,44 @@ def run_reference_md(path: str, nsteps: int, trj_every: int = 0) -> dict:
     return {"md": md, "state": state, "start": start, "log": log, "end": end, "nsteps": ns, **files}
 
 
+def run_reference_hmc(path: str, velocities, nstep_md: int) -> dict:
+    """Canonical HMC moves through the compiled reference's own md_move() over vver()
+    (harness hmc mode, oracle/ref_harness.c), move m starting from velocities[m] ([3, n])
+    in place of velinit()'s draw. Returns per move the energies before ({ukin, uinter,
+    uintra, ushift}), dH, the accept decision, the energies after, the energies and the
+    positions of the proposal (after the last vver step, kept even on rejection) and the
+    final positions."""
+    v = np.ascontiguousarray(np.asarray(velocities, dtype=np.float64))
+    nm, _, n = v.shape
+    with tempfile.TemporaryDirectory() as td:
+        out, hb, vb = os.path.join(td, "out.bin"), os.path.join(td, "hmc.bin"), os.path.join(td, "vel.bin")
+        v.tofile(vb)
+        p = subprocess.run([REF_BIN, path, out, "0", "hmc", str(nm), str(nstep_md), hb, vb], capture_output=True,
+                           text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"reference hmc run failed: {p.stderr[-2000:]}")
+        b = open(hb, "rb").read()
+    n2, nm2, ns = (int(x) for x in np.frombuffer(b[:12], np.int32))
+    assert n2 == n and nm2 == nm and ns == nstep_md
+    rec = 8 * (12 + 6 * n)
+    res = []
+    for m in range(nm):
+        a = np.frombuffer(b, np.float64, 12 + 6 * n, 12 + m * rec)
+        res.append({"pre": a[:4].copy(), "dh": float(a[4]), "accept": bool(a[5]), "post": a[6:8].copy(),
+                    "proposal_energies": a[8:12].copy(), "proposal": a[12:12 + 3 * n].reshape(3, n).copy(),
+                    "final": a[12 + 3 * n:].reshape(3, n).copy()})
+    return {"moves": res}
+
+
+def hmc_velocities(hp: dict, replica: int, move: int, n: int):
+    """The velocities mg_hmc_batch draws for one move of one replica ([3, n])."""
+    v = np.zeros((3, n))
+    L = lib()
+    L.orc_hmc_velocities.argtypes = [C.POINTER(MgHmcParams), C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+    L.orc_hmc_velocities(C.byref(MgHmcParams(**hp)), replica, move, n, _ptr(v[0]), _ptr(v[1]), _ptr(v[2]))
+    return v
+
+
 SFGRIDGEN_BIN = os.path.join(HERE, "_ref", "sfgridgen")
 
 

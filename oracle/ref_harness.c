@@ -21,6 +21,16 @@
  * For NPT the scalars are {delt, treq, Qts, Qbs, preq, isLJlrcOn, nfree, vts, vbs, rts,
  * boxlx, pljlrc} and the per-step record {ukin, uinter, uintra, ushift, vts, vbs, rts,
  * utsbs, tinst, pinst, boxlx, boxv}.
+ * With "hmc <nmoves> <nstep_md> <hmc.bin> <vel.bin>" after the repeat count it runs nmoves
+ * canonical HMC moves through the reference's own md_move() over vver() (src/dispmd.c:12-103,
+ * src/md.c:22-85), each from velocities read from vel.bin (per move vx, vy, vz [n]) in
+ * place of velinit()'s draw, with the kinetic energy formed as velinit() ends
+ * (src/initvars.c:198-228), then frclong() and frcshort() as hmc() calls them
+ * (src/hmc.c:31-36). md_move() runs unchanged; the vver() it calls is wrapped to copy the
+ * positions after its last step, so the proposal is kept even when the move is rejected.
+ * Writes int32 natom, nmoves, nstep_md; per move double {ukin, uinter, uintra, ushift}
+ * before, {dH, isAccept, uinter, ushift} after, {ukin, uinter, uintra, ushift} of the
+ * proposal, then the proposal and the final x, y, z [n].
  * A further argument trj_every > 0 makes the run write the reference's trajectory file
  * (trj.mspms in the input directory, trajectory() of src/dumpxyz.c) the way its main loop
  * does (src/mspms2.c:57-60, :123-126), and its checkpoint (saveit(), sav.mspms) after the
@@ -38,6 +48,24 @@ int fnValidateInput();
 int vver();
 int vver_nh_3();
 int npt_respa();
+bool md_move(int (*pfn_md_scheme)(), int nStepMD);
+
+/* vver() that keeps the positions after the last step of an HMC trajectory */
+static int rec_steps, rec_k;
+static double *rec_x, *rec_y, *rec_z, rec_e[4];
+static int vver_rec(void) {
+    int r = vver();
+    if (++rec_k == rec_steps) {
+        memcpy(rec_x, xx, sizeof(double) * natom);
+        memcpy(rec_y, yy, sizeof(double) * natom);
+        memcpy(rec_z, zz, sizeof(double) * natom);
+        rec_e[0] = ukin;
+        rec_e[1] = uinter;
+        rec_e[2] = uintra;
+        rec_e[3] = ushift;
+    }
+    return r;
+}
 int trajectory();
 int saveit();
 
@@ -76,16 +104,22 @@ static double now_s(void) {
 
 int main(int argc, char **argv) {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s <dir> <out.bin> [repeat [md <nsteps> <md.bin>]]\n", argv[0]);
+        fprintf(stderr, "usage: %s <dir> <out.bin> [repeat [md <nsteps> <md.bin> | hmc <nmoves> <nstep_md> <hmc.bin> "
+                        "<vel.bin>]]\n", argv[0]);
         return 2;
     }
     char outabs[4096];
     abs_path(argv[2], outabs, sizeof(outabs));
     int repeat = argc > 3 ? atoi(argv[3]) : 0;
-    int md_steps = 0;
-    char mdabs[4096] = {0};
+    int md_steps = 0, hmc_moves = 0, hmc_steps = 0;
+    char mdabs[4096] = {0}, velabs[4096] = {0};
     int trj_every = 0;
-    if (argc > 6 && !strcmp(argv[4], "md")) {
+    if (argc > 8 && !strcmp(argv[4], "hmc")) {
+        hmc_moves = atoi(argv[5]);
+        hmc_steps = atoi(argv[6]);
+        abs_path(argv[7], mdabs, sizeof(mdabs));
+        abs_path(argv[8], velabs, sizeof(velabs));
+    } else if (argc > 6 && !strcmp(argv[4], "md")) {
         md_steps = atoi(argv[5]);
         abs_path(argv[6], mdabs, sizeof(mdabs));
         if (argc > 7) trj_every = atoi(argv[7]);
@@ -124,6 +158,48 @@ int main(int argc, char **argv) {
         for (int r = 0; r < repeat; r++) frcshort();
         double t2 = now_s();
         printf("frclong_s=%.9g frcshort_s=%.9g\n", (t1 - t0) / repeat, (t2 - t1) / repeat);
+    }
+    if (hmc_moves > 0) {
+        FILE *fv = fopen(velabs, "rb"), *fh = fopen(mdabs, "wb");
+        if (!fv || !fh) { perror("hmc files"); return 2; }
+        int hdr[3] = {n, hmc_moves, hmc_steps};
+        fwrite(hdr, sizeof(int), 3, fh);
+        rec_x = (double *)malloc(sizeof(double) * n);
+        rec_y = (double *)malloc(sizeof(double) * n);
+        rec_z = (double *)malloc(sizeof(double) * n);
+        for (int m = 0; m < hmc_moves; m++) {
+            if (fread(vx, sizeof(double), n, fv) != (size_t)n || fread(vy, sizeof(double), n, fv) != (size_t)n ||
+                fread(vz, sizeof(double), n, fv) != (size_t)n) {
+                fprintf(stderr, "hmc: short velocity file\n");
+                return 2;
+            }
+            int specie_id, sample_atom_id;
+            ukin = 0.0;
+            for (int ii = 0; ii < n; ii++) {
+                get_specie_and_relative_atom_id(ii, &specie_id, &sample_atom_id);
+                ukin += sample_mole[specie_id].aw[sample_atom_id] * (vx[ii] * vx[ii] + vy[ii] * vy[ii] + vz[ii] * vz[ii]);
+            }
+            ukin = 0.5 * ukin;
+            tinst = 2.0 * ukin / nfree;
+            frclong();
+            frcshort();
+            double pre[4] = {ukin, uinter, uintra, ushift};
+            rec_steps = hmc_steps;
+            rec_k = 0;
+            bool acc = md_move(&vver_rec, hmc_steps);
+            double post[4] = {dH, acc ? 1.0 : 0.0, uinter, ushift};
+            fwrite(pre, sizeof(double), 4, fh);
+            fwrite(post, sizeof(double), 4, fh);
+            fwrite(rec_e, sizeof(double), 4, fh);
+            fwrite(rec_x, sizeof(double), n, fh);
+            fwrite(rec_y, sizeof(double), n, fh);
+            fwrite(rec_z, sizeof(double), n, fh);
+            fwrite(xx, sizeof(double), n, fh);
+            fwrite(yy, sizeof(double), n, fh);
+            fwrite(zz, sizeof(double), n, fh);
+        }
+        fclose(fv);
+        fclose(fh);
     }
     if (md_steps > 0) {
         int (*scheme)() = what_ensemble == NVT ? vver_nh_3

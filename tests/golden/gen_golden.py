@@ -351,10 +351,60 @@ def gen_md(only):
               f"-> {os.path.getsize(fn)} bytes")
 
 
+# the canonical HMC move of Lennard-Jones replicas (mg_hmc_batch's workload): parameters,
+# replica sizes and Philox key shared with tests/test_hmc.py
+HMC_HP = dict(eps=1.0, sigma=1.0, rcutoff=2.5, mass=1.0, treq=1.0, delt=0.001, nstep_md=10, seed=0x1234ABCD5678,
+              rescale=1, nconstraint=0)
+HMC_SIZES = (200, 500, 864)
+
+
+def gen_hmc(only):
+    """hmc_lj_ref: one canonical move of each of three LJ replicas through the compiled
+    reference's own md_move() over vver(), started from the velocities mg_hmc_batch draws for
+    move 0 of that replica (replica r of the batch: orc_hmc_velocities)."""
+    name = "hmc_lj_ref"
+    if only and name not in only:
+        return
+    from mspms2_gb300.system import time_base
+    from oracle.pyoracle import hmc_velocities, run_reference_hmc
+    rec = {k: [] for k in ("natom", "box", "pos", "vel", "dh", "accept", "pre", "prop_e", "prop", "final")}
+    for r, n in enumerate(HMC_SIZES):
+        s = configs.lj_replica(n, seed=40 + r)
+        s.treq_K, s.delt_fs, s.nstep_inner = HMC_HP["treq"], HMC_HP["delt"] * time_base(s), 1
+        s.what_simulation, s.what_ensemble = 1, 0  # HMC: the reference sets up md_move's state
+        v = hmc_velocities(HMC_HP, r, 0, n)
+        with tempfile.TemporaryDirectory() as td:
+            write_reference_dir(s, td)
+            mv = run_reference_hmc(td, [v], HMC_HP["nstep_md"])["moves"][0]
+        rec["natom"].append(n)
+        rec["box"].append(float(s.box[0]))
+        rec["pos"].append(np.stack([s.x, s.y, s.z]))
+        rec["vel"].append(v)
+        rec["dh"].append(mv["dh"])
+        rec["accept"].append(int(mv["accept"]))
+        rec["pre"].append(mv["pre"])
+        rec["prop_e"].append(mv["proposal_energies"])
+        rec["prop"].append(mv["proposal"])
+        rec["final"].append(mv["final"])
+        print(f"{name}[{r}]: natom={n} dH={mv['dh']:.10g} accept={mv['accept']}")
+    arrays = {"natom": np.array(rec["natom"], np.int32), "box": np.array(rec["box"]),
+              "dh": np.array(rec["dh"]), "accept": np.array(rec["accept"], np.int32), "pre": np.array(rec["pre"]),
+              "prop_e": np.array(rec["prop_e"]),
+              "hp": np.array([HMC_HP[k] for k in ("eps", "sigma", "rcutoff", "mass", "treq", "delt")]),
+              "hp_int": np.array([HMC_HP["nstep_md"], HMC_HP["seed"], HMC_HP["rescale"], HMC_HP["nconstraint"]],
+                                 np.int64)}
+    for k in ("pos", "vel", "prop", "final"):
+        arrays[k] = np.concatenate(rec[k], axis=1)
+    fn = os.path.join(OUT, f"{name}.npz")
+    np.savez_compressed(fn, **arrays)
+    print(f"{name} -> {os.path.getsize(fn)} bytes")
+
+
 def main():
     if not reference_available():
         sys.exit("oracle/_ref/mspms_ref_force missing: run `sh oracle/build_ref.sh` first")
     only = set(sys.argv[1:])
+    gen_hmc(only)
     gen_md(only)
     gen_sfgrid(only)
     for name, (kind, obj) in cases().items():

@@ -96,3 +96,60 @@ def test_gpu_batch_is_reproducible_and_resumable():
     h2 = hmc_batch(HP, natom, box, h1[0], h1[1], h1[2], 2, move0=2)
     assert np.array_equal(h2[0], a[0]) and np.array_equal(h2[1], a[1]) and np.array_equal(h2[2], a[2])
     assert np.array_equal(h1[3] + h2[3], a[3])
+
+
+def ref_golden():
+    """hmc_lj_ref (tests/golden/gen_golden.py): one canonical move of three LJ replicas through
+    the compiled reference's own md_move() over vver() (src/dispmd.c:12-103, src/md.c:22-85),
+    each started from the velocities mg_hmc_batch draws for move 0 of that replica."""
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "hmc_lj_ref.npz"))
+    hp = dict(zip(("eps", "sigma", "rcutoff", "mass", "treq", "delt"), (float(v) for v in d["hp"])))
+    hp.update(zip(("nstep_md", "seed", "rescale", "nconstraint"), (int(v) for v in d["hp_int"])))
+    return d, hp
+
+
+def test_oracle_move_matches_reference_md_move():
+    """The oracle's restated move (velinit with the Philox streams, frclong, vver, dH with
+    +d ushift) against the compiled reference's md_move from the same velocities: the
+    velocities the golden file injected are those the streams give, and dH agrees to FP64
+    rounding."""
+    from oracle.pyoracle import Oracle, hmc_velocities
+    d, hp = ref_golden()
+    off = 0
+    for r, n in enumerate(d["natom"]):
+        n = int(n)
+        assert np.array_equal(hmc_velocities(hp, r, 0, n), d["vel"][:, off:off + n])
+        s = configs.lj_replica(n, seed=40 + r)
+        assert np.array_equal(np.stack([s.x, s.y, s.z]), d["pos"][:, off:off + n])
+        _, _, _, dh = Oracle(s).hmc_replica(hp, r, 0, 1)
+        assert abs(dh[0] - d["dh"][r]) <= 1e-9 * max(1.0, abs(d["dh"][r])), (r, dh[0], d["dh"][r])
+        off += n
+
+
+@pytest.mark.gpu
+def test_gpu_batch_matches_reference_md_move():
+    """mg_hmc_batch, one move of the three replicas in one launch, against the compiled
+    reference's md_move from the same velocities: dH to 5e-4 + 1e-6 N (FP32 pair forces over
+    the 10-step trajectory against FP64); where the batch accepts, its positions are the
+    reference's proposal to 1e-5 and its energy (potential plus shift) the proposal's; where
+    it rejects (its own uniform draw), the positions are the start, unchanged."""
+    from mspms2_gb300 import build
+    from mspms2_gb300.engine import hmc_batch
+    build.build()
+    d, hp = ref_golden()
+    natom = [int(v) for v in d["natom"]]
+    gx, gy, gz, acc, energy, dh = hmc_batch(hp, natom, d["box"], d["pos"][0], d["pos"][1], d["pos"][2], 1)
+    off = 0
+    for r, n in enumerate(natom):
+        assert abs(dh[r, 0] - d["dh"][r]) <= 5e-4 + 1e-6 * n, (r, dh[r, 0], d["dh"][r])
+        gp = np.stack([gx[off:off + n], gy[off:off + n], gz[off:off + n]])
+        if acc[r]:
+            prop = d["prop"][:, off:off + n]
+            assert np.abs(gp - prop).max() <= 1e-5 * max(1.0, np.abs(prop).max()), r
+            want = d["prop_e"][r][1] + d["prop_e"][r][3]
+            assert abs(energy[r] - want) <= 1e-5 * abs(want) + 1e-3, (r, energy[r], want)
+        else:
+            assert np.array_equal(gp, d["pos"][:, off:off + n]), r
+        off += n
