@@ -450,12 +450,42 @@ def nve_drift_scan(device=0, ps=20.0, cases=((0.5, "mixed"), (0.25, "mixed"), (0
     return {"workload": "water_c1 (216 SPC/Fw, Wolf)", "integrator": "velocity Verlet (vver), NVE", "runs": out}
 
 
-def nve_drift(device=0, dt_fs=0.25, equil_steps=4000, steps=160000):
+def drift_fit(t_ns, h, natom_kT):
+    """Linear drift of an energy series h(t) in kT/ns/atom with its standard error, the
+    residuals' autocorrelation taken into account (integrated autocorrelation time up to
+    the first zero of the autocorrelation; effective samples N dt / 2 tau), and the
+    conservative resolution (RMS fluctuation / duration)."""
+    t = np.asarray(t_ns, dtype=float)
+    y = np.asarray(h, dtype=float) / natom_kT
+    A = np.stack([t, np.ones_like(t)], 1)
+    coef, *_ = np.linalg.lstsq(A, y, rcond=None)
+    res = y - A @ coef
+    r = res - res.mean()
+    n = len(r)
+    f = np.fft.rfft(r, 2 * n)
+    ac = np.fft.irfft(f * np.conj(f))[:n]
+    ac = ac / ac[0]
+    cut = int(np.argmax(ac <= 0.0)) if np.any(ac <= 0.0) else n
+    tau = 0.5 + float(ac[1:max(cut, 1)].sum())  # in samples
+    neff = max(n / (2.0 * tau), 2.0)
+    span = t[-1] - t[0]
+    se = float(np.std(res)) * np.sqrt(12.0 / neff) / span
+    return {"drift_kT_per_ns_per_atom": float(coef[0]), "stderr_kT_per_ns_per_atom": se,
+            "rms_fluctuation_kT_per_atom": float(np.std(y)), "resolution_rms_over_span": float(np.std(y)) / span,
+            "autocorrelation_samples": tau, "ns": float(span)}
+
+
+def nve_drift(device=0, dt_fs=0.25, equil_steps=4000, steps=7_000_000, chunk=4000, every=40):
     """Energy drift of plain velocity-Verlet NVE on the 216-water Wolf system (648 sites,
-    rc 9 A, alpha 0.2/A) at a small step, long enough to resolve 1e-4 kT/ns/atom: one state
-    equilibrated by Nose-Hoover NVT at 298 K (tau 100 fs), then `steps` NVE steps on the
-    mixed path and, from the same state, on the FP64 path. The difference of the two
-    energy series isolates what the mixed precision adds."""
+    rc 9 A, alpha 0.2/A) at a small step, long enough to resolve 1e-4 kT/ns/atom, and the
+    mixed path's own share of it. One state is equilibrated by Nose-Hoover NVT at 298 K (tau
+    100 fs); then `steps` NVE steps on the mixed path run in chunks of the graph-replayed
+    integrator (mg_md_run), the total energy sampled every `every` steps and fitted with an
+    autocorrelation-aware standard error. At the end of every chunk the power of the mixed
+    forces' error at that state, P = sum_i v_i . (F_mixed(x) - F_FP64(x)), is taken from a
+    mixed and an FP64 context: its mean is the rate at which the mixed path's force error
+    changes the total energy (the rest of the drift is the integrator's and the model's,
+    the same on both paths), with a standard error from the spread of P over the chunks."""
     from mspms2_gb300 import configs
     from mspms2_gb300.engine import Engine
     from mspms2_gb300.system import md_params, time_base
@@ -468,32 +498,37 @@ def nve_drift(device=0, dt_fs=0.25, equil_steps=4000, steps=160000):
     rng = np.random.default_rng(11)
     v = rng.normal(size=(3, s.natom)) * np.sqrt(md["treq"] / m)
     v -= (v * m).sum(1, keepdims=True) / m.sum()
-
-    def series(lg):
-        return lg[:, 0] + lg[:, 1] + lg[:, 2]  # ukin + uinter + uintra
-
-    def drift(h):
-        slope = float(np.polyfit(np.arange(len(h)) * dt_fs, h, 1)[0])  # energy per fs
-        return slope * 1e6 / (md["treq"] * s.natom)
-
-    out = {"workload": "water_c1 (216 SPC/Fw, Wolf)", "dt_fs": dt_fs, "steps": steps,
-           "ps": steps * dt_fs * 1e-3, "integrator": "velocity Verlet (vver), NVE"}
-    with Engine(s, precision="mixed", device=device) as eng:
+    natom_kT = md["treq"] * s.natom
+    per_ns = 1.0e6 / time_base(s)  # reduced time units in one ns
+    out = {"workload": "water_c1 (216 SPC/Fw, Wolf)", "dt_fs": dt_fs, "integrator": "velocity Verlet (vver), NVE",
+           "sampled_every_steps": every, "power_samples_every_steps": chunk}
+    t, h, power, fnorm = [], [], [], []
+    with Engine(s, precision="mixed", device=device) as eng, Engine(s, precision="fp64", device=device) as e64:
         md["scheme"] = 1
-        pos, vel, st, _ = eng.md_run(equil_steps, md, v)
-        md["scheme"] = 0
+        pos, vel, _, _ = eng.md_run(equil_steps, md, v)
         t0 = time.perf_counter()
-        _, _, _, lg = eng.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
-        out["wall_s_mixed"] = time.perf_counter() - t0
-    with Engine(s, precision="fp64", device=device) as e64:
-        t0 = time.perf_counter()
-        _, _, _, lg64 = e64.md_run(steps, md, vel, x=pos[0], y=pos[1], z=pos[2])
-        out["wall_s_fp64"] = time.perf_counter() - t0
-    h, h64 = series(lg), series(lg64)
-    out.update({"drift_kT_per_ns_per_atom_mixed": drift(h), "drift_kT_per_ns_per_atom_fp64": drift(h64),
-                "drift_kT_per_ns_per_atom_mixed_minus_fp64": drift(h - h64),
-                "rms_fluctuation_kT_per_atom_mixed": float(np.std(h)) / (md["treq"] * s.natom),
-                "resolution_kT_per_ns_per_atom": float(np.std(h)) / (md["treq"] * s.natom) / (steps * dt_fs * 1e-6)})
+        done = 0
+        while done < steps:
+            k = min(chunk, steps - done)
+            pos, vel, _, lg = eng.md_run(k, dict(md, scheme=0), vel, x=pos[0], y=pos[1], z=pos[2])
+            e = lg[:, 0] + lg[:, 1] + lg[:, 2]
+            idx = np.arange(0 if done == 0 else every, k + 1, every)
+            t.append((done + idx) * dt_fs * 1e-6)
+            h.append(e[idx])
+            done += k
+            fl, fs, _ = eng.compute(pos[0], pos[1], pos[2])
+            gl, gs, _ = e64.compute(pos[0], pos[1], pos[2])
+            df = (fl + fs) - (gl + gs)
+            power.append(float((vel * df).sum()))
+            fnorm.append(float(np.linalg.norm(df) / np.linalg.norm(gl + gs)))
+        wall = time.perf_counter() - t0
+    fit = drift_fit(np.concatenate(t), np.concatenate(h), natom_kT)
+    p = np.asarray(power) * per_ns / natom_kT
+    out.update({"mixed": dict(fit, steps=steps, wall_s=wall),
+                "mixed_force_error_power": {
+                    "drift_kT_per_ns_per_atom": float(p.mean()),
+                    "stderr_kT_per_ns_per_atom": float(p.std(ddof=1) / np.sqrt(len(p))),
+                    "samples": len(p), "rms_rel_force_err": float(np.sqrt(np.mean(np.square(fnorm))))}})
     return out
 
 
@@ -707,7 +742,49 @@ def force_matching_extras(device, nsnap=64, stride=4, seed=2024):
                     "gradient in (eps_OO, sigma_OO, q_O) with q_H = -q_O/2; central differences h = 1e-4 relative"}
 
 
-def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10):
+def siman_batch_contexts(eng, s, md, sc, pos, nrep, device):
+    """nrep annealing runs of the C5 system side by side on one GPU: the context eng and
+    nrep - 1 more that use its Tasos tables (mg_sf_tasos_share), each on its own stream and
+    driven by its own host thread, replica r with seed sc.seed + r. Reports the wall time of
+    the batch against nrep runs one after another (the single run timed just before)."""
+    import threading
+    from mspms2_gb300.engine import Engine
+    engs = [eng]
+    for _ in range(nrep - 1):
+        e = Engine(s, precision="mixed", device=device)
+        e.sf_tasos_share(eng)
+        engs.append(e)
+    warm = dict(sc, n_tries=1, t_min=sc["t_initial"] * 0.999, max_stages=2)
+    logs = [None] * nrep
+
+    def work(r, schedule):
+        logs[r] = engs[r].siman_run(md, dict(schedule, seed=sc["seed"] + r), x=pos[0], y=pos[1], z=pos[2])[3]
+
+    def batch(schedule):
+        th = [threading.Thread(target=work, args=(r, schedule)) for r in range(nrep)]
+        t0 = time.perf_counter()
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        return time.perf_counter() - t0
+
+    batch(warm)
+    wall = batch(sc)
+    t0 = time.perf_counter()
+    work(1, sc)
+    solo = time.perf_counter() - t0
+    for e in engs[1:]:
+        e.close()
+    steps = sum(len(lg) for lg in logs) * sc["n_tries"]
+    return {"replicas": nrep, "form": "one context per replica, each on its own stream and host thread (not one launch)",
+            "tables": "one copy shared by all contexts (mg_sf_tasos_share)",
+            "wall_s": wall, "solo_wall_s": solo, "outer_steps": steps,
+            "ms_per_outer_step": wall / steps * 1e3, "speedup_over_sequential": nrep * solo / wall,
+            "stages": [int(len(lg)) for lg in logs]}
+
+
+def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10, replicas=8):
     """United-atom n-butane in a bundle of 7 (11,11) nanotubes (80,000 sites, LJ rc 14 A,
     Tasos solid-fluid tables at 0.1 A over the 127 x 127 A bundle cell, generated on the
     device): force steps timed like the headline (device-resident positions, L2 flushed,
@@ -789,6 +866,7 @@ def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10)
         t0 = time.perf_counter()
         _, _, _, slog = eng.siman_run(md, sc, x=p1[0], y=p1[1], z=p1[2])
         dt_si = time.perf_counter() - t0
+        batch = siman_batch_contexts(eng, s, md, sc, p1, replicas, device) if replicas > 1 else None
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     nsf = n  # every butane site is of ghost type NONE
@@ -808,8 +886,9 @@ def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10)
                           "T_K": [float(t) * s.epsilon_base for t in slog[:, 0]],
                           "tinst_K_end_of_stage": [float(t) * s.epsilon_base for t in slog[:, 5]],
                           "wall_s": dt_si, "ms_per_outer_step": dt_si / (len(slog) * siman_tries) * 1e3,
-                          "note": "one system through the engine; replicas of this size (80,000 sites, "
-                                  "2.6 GB of solid-fluid tables) run as separate contexts, not one launch"}})
+                          "note": "one system through the engine; replicas of this size run as separate "
+                                  "contexts sharing one copy of the tables (siman_batch), not one launch"},
+                "siman_batch": batch})
     if fp64:
         with Engine(s, precision="fp64", device=device) as e64:
             t0 = time.perf_counter()
@@ -923,7 +1002,7 @@ def run_ours(args, rank, world, local_rank):
         # plain FP64 GPU path, same workload
         eng64 = Engine(system, precision="fp64", device=local_rank)
         eng64.set_stream(stream.cuda_stream)
-        eng64.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
+        e64 = eng64.compute_device(*ptrs, fl.data_ptr(), fs.data_ptr(), TERMS_ALL)
         t64 = []
         for k in range(max(2, min(3, args.steps))):
             flush.fill_(float(k))
@@ -935,12 +1014,23 @@ def run_ours(args, rank, world, local_rank):
             t64.append(a.elapsed_time(b))
         f64 = torch.cat([fl, fs]).clone()
         eng64.close()
-        step()
+        e32 = step()
         torch.cuda.synchronize()
         f32 = torch.cat([fl, fs])
         err = float(torch.linalg.vector_norm(f32 - f64) / torch.linalg.vector_norm(f64))
         ms64 = statistics.mean(t64)
+        # each energy of the mixed path against the FP64 path, relative to the FP64 value and
+        # to the sum of magnitudes of the terms the derived energies are made of
+        elec_scale = sum(abs(e64[k]) for k in ("ureal", "ufourier", "uself", "uexcl", "uvacuum"))
+        e_err = {}
+        for k in ("uvdw", "ushift", "ureal", "uexcl", "ufourier", "uself", "uelec", "uinter", "virial_inter",
+                  "ubond", "uangle", "uintra", "virial_intra"):
+            d = abs(e32[k] - e64[k])
+            ref = abs(e64[k])
+            scale = elec_scale if k in ("uelec", "uinter", "virial_inter") else ref
+            e_err[k] = {"rel": d / ref if ref > 0 else None, "rel_to_components": d / scale if scale > 0 else None}
         extras["fp64_path"] = {"value": npairs / (ms64 * 1e-3), "ms_per_step": ms64,
+                               "energy_err_mixed_vs_fp64": e_err,
                                "mixed_over_fp64": ms64 / ms_step, "rms_rel_force_err_mixed_vs_fp64": err}
         # device-resident NVT Nose-Hoover RESPA (mg_md_run, the reference's vver_nh_3):
         # inner steps of 0.5 fs with bonded + pairs inside 7 A, outer 2 fs step with the
@@ -982,6 +1072,26 @@ def run_ours(args, rank, world, local_rank):
             parts = ln.split()
             if len(parts) == 4 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel_of[dom]:
                 traffic = float(parts[3])
+    # per-stage figures of the pair and list kernels: the pair stage by the work model (55 FLOP
+    # per pair, counted once) and as neighbour streaming against HBM (per listed entry 4 B index
+    # + 16 B shift, per j-cluster of the half list its 8 slots x 32 B, per site 16 B position and
+    # 24 B force), the list stage by the bytes it writes and reads (per entry 4 B index, 16 B
+    # shift, 4 B image; per site its FP64 position and wrapped position)
+    hbm = measured_peaks().get("hbm_gbs")
+    nent = st["cluster_pairs"]
+    pair_bytes = nent * 20.0 + 0.5 * nent * 8 * 32.0 + n * 40.0
+    list_bytes = nent * 24.0 + n * 3 * 8.0 * 3
+    stage_roofline = {
+        "pair": {"ms": kms[1], "tflops_work_model": FLOP_PAIR * npairs / (kms[1] * 1e-3) / 1e12 if kms[1] else None,
+                 "frac_fp32": FLOP_PAIR * npairs / (kms[1] * 1e-3) / 1e12 / peak if kms[1] else None,
+                 "neighbour_streaming_gbs": pair_bytes / (kms[1] * 1e-3) / 1e9 if kms[1] else None,
+                 "hbm_frac": pair_bytes / (kms[1] * 1e-3) / 1e9 / hbm if (kms[1] and hbm) else None,
+                 "bytes_per_call": pair_bytes},
+        "list": {"ms": kms[0], "gbs": list_bytes / (kms[0] * 1e-3) / 1e9 if kms[0] else None,
+                 "hbm_frac": list_bytes / (kms[0] * 1e-3) / 1e9 / hbm if (kms[0] and hbm) else None,
+                 "bytes_per_call": list_bytes},
+        "peak_basis": "FP32 as in roofline; HBM of measured (MEASURED_PEAKS.json hbm_gbs); the list and "
+                      "packed operands mostly stay in the 129 MB L2, so these rates exceed what DRAM moves"}
     if rank != 0:
         return 0
     line = {"metric": "pair_interactions_per_s", "value": value, "unit": "pair-interactions/s", "n_gpus": world,
@@ -1010,7 +1120,7 @@ def run_ours(args, rank, world, local_rank):
                          "executed_note": "FLOP the kernel's algorithm executes (the table passes do fewer than "
                                           "the work model counts per k-vector)",
                          "peak_basis": peak_basis},
-            "clocks": clk}
+            "clocks": clk, "stage_roofline": stage_roofline}
     if kvec and args.precision == "mixed" and system.kmax[2] <= 30:
         tf = sk_tensor_flops(tuple(system.kmax), system.ksqmax, n)
         line["kspace_sk_tensor"] = {

@@ -539,6 +539,12 @@ MG_API mg_status mg_sfgrid_tasos(int device, const mg_sfgrid_spec *spec, int nx,
 /* The same table evaluated on the context's device straight into its Tasos table `type`
  * (as mg_sfgrid_tasos at the context's precision followed by mg_sf_tasos_set_grid with
  * cell length cuc), with no copy through host memory. */
+/* No reference counterpart: ctx uses the Tasos tables of src (same device and precision)
+ * without a copy. Replicas of one system (annealing runs, for instance) then hold one copy
+ * of tables that can reach gigabytes; the storage is freed with the last context holding
+ * it. A later mg_sf_tasos_set_grid / mg_sf_tasos_generate on either context gives that
+ * context a storage of its own for that table. */
+MG_API mg_status mg_sf_tasos_share(mg_ctx *ctx, const mg_ctx *src);
 MG_API mg_status mg_sf_tasos_generate(mg_ctx *ctx, int type, const mg_sfgrid_spec *spec, int nx, int ny, int nz,
                                       double hx, double hy, double hz, double cuc);
 

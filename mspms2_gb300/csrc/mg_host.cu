@@ -136,7 +136,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_site_interp, &c->d_species, &c->d_intra, &c->d_bonded, &c->d_site_aw,
                       &c->d_x, &c->d_y, &c->d_z, &c->d_fl, &c->d_fs, &c->d_xbuild, &c->d_img,
                       &c->d_col_count, &c->d_col_start, &c->d_col_fill, &c->d_col_cl_start,
-                      &c->d_col_sorted, &c->d_cl_atom, &c->d_cl_ref, &c->d_cl_bb, &c->d_cl_col,
+                      &c->d_col_sorted, &c->d_cl_atom, &c->d_cl_ref, &c->d_cl_refh, &c->d_cl_bb, &c->d_cl_col,
                       &c->d_pair_start, &c->d_pair_count, &c->d_pair_j, &c->d_pair_shift,
                       &c->d_pack_pos, &c->d_pack_lj, &c->d_pack_info, &c->d_pack_xi, &c->d_pack_qp, &c->d_rows, &c->d_row_slot,
                       &c->d_phase, &c->d_spart, &c->d_scoef, &c->d_tasks, &c->d_epart, &c->d_eout,
@@ -147,7 +147,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift, &c->d_sub_img, &c->d_facc,
                       &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_qf, &c->d_fk, &c->d_erows_k};
     for (DevBuf *b : bufs) mg_free(*b);
-    for (auto &b : c->tasos_buf) mg_free(b);
+    c->tasos_buf.clear();  // shared storage is freed by its last holder
     for (auto &b : c->myinterp_buf) mg_free(b);
     if (c->have_events)
         for (int i = 0; i < 10; i++) cudaEventDestroy(c->ev[i]);
@@ -458,15 +458,37 @@ extern "C" mg_status mg_sf_tasos_set_grid(mg_ctx *c, int type, int nx, int ny, i
     t.nx = nx; t.ny = ny; t.nz = nz;
     t.hx = hx; t.hy = hy; t.hz = hz; t.cuc = cuc; t.min_pe = mn;
     mg_status st;
+    DevBuf &buf = mg_tasos_storage(c, type);
     if (c->opt.precision == MG_PREC_FP64) {
-        if ((st = upload(c, c->tasos_buf[type - 1], values, sizeof(double) * 8 * nn))) return st;
+        if ((st = upload(c, buf, values, sizeof(double) * 8 * nn))) return st;
     } else {
         std::vector<float> f(8 * nn);
         for (size_t i = 0; i < 8 * nn; i++) f[i] = (float)values[i];
-        if ((st = upload(c, c->tasos_buf[type - 1], f.data(), sizeof(float) * 8 * nn))) return st;
+        if ((st = upload(c, buf, f.data(), sizeof(float) * 8 * nn))) return st;
     }
-    t.values = c->tasos_buf[type - 1].p;
+    t.values = buf.p;
     return upload(c, c->d_tasos, c->tasos.data(), sizeof(TasosDev) * c->tasos.size());
+}
+
+DevBuf &mg_tasos_storage(mg_ctx *c, int type) {
+    std::shared_ptr<DevBuf> &p = c->tasos_buf[type - 1];
+    if (!p || p.use_count() > 1)
+        p = std::shared_ptr<DevBuf>(new DevBuf(), [](DevBuf *b) {
+            mg_free(*b);
+            delete b;
+        });
+    return *p;
+}
+
+extern "C" mg_status mg_sf_tasos_share(mg_ctx *dst, const mg_ctx *src) {
+    if (!dst || !src || dst == src) return MG_ERR_INVALID;
+    if (dst->device != src->device || dst->opt.precision != src->opt.precision)
+        return mg_fail(dst, MG_ERR_INVALID, "Tasos tables can be shared only between contexts of one device and precision");
+    cudaSetDevice(dst->device);
+    dst->tasos = src->tasos;
+    dst->tasos_buf = src->tasos_buf;
+    if (dst->tasos.empty()) return MG_OK;
+    return upload(dst, dst->d_tasos, dst->tasos.data(), sizeof(TasosDev) * dst->tasos.size());
 }
 
 extern "C" mg_status mg_sf_hypergeo_set(mg_ctx *c, int ntube, const double *cx, const double *cy,

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -160,7 +161,7 @@ struct mg_ctx {
     bool list_valid = false;
     int list_builds = 0, list_rebuilt = 0;
     DevBuf d_col_count, d_col_start, d_col_fill, d_col_cl_start, d_col_sorted;
-    DevBuf d_cl_atom, d_cl_ref, d_cl_bb, d_cl_col, d_cl_bbf, d_col_ncl, d_counter;
+    DevBuf d_cl_atom, d_cl_ref, d_cl_refh, d_cl_bb, d_cl_col, d_cl_bbf, d_col_ncl, d_counter;
     double zcap = 0;           // largest z extent of a cluster
     bool small_box_forced = false;
     int col_refine = 0;        // column-grid refinements after overflows
@@ -209,7 +210,8 @@ struct mg_ctx {
     int epart_rows = 0, epart_cap = 0;
     // solid-fluid
     std::vector<TasosDev> tasos;   // index = AtomID - 1
-    std::vector<DevBuf> tasos_buf;
+    // table storage, shared by the contexts mg_sf_tasos_share links (freed with the last)
+    std::vector<std::shared_ptr<DevBuf>> tasos_buf;
     DevBuf d_tasos;
     std::vector<MyInterpDev> myinterp;
     std::vector<DevBuf> myinterp_buf;
@@ -232,6 +234,9 @@ mg_status mg_ewald_fork(mg_ctx *c, const double *dx, const double *dy, const dou
 mg_status mg_ewald_join(mg_ctx *c, double *fl);
 mg_status mg_cuda_fail(mg_ctx *c, cudaError_t e, const char *what);
 bool mg_ensure(mg_ctx *c, DevBuf &b, size_t bytes);
+// the storage of Tasos table `type` (1-based) that this context may write: a fresh buffer
+// when the table has none or shares its buffer with another context
+DevBuf &mg_tasos_storage(mg_ctx *c, int type);
 // forces of the given terms at device positions into the context's [3][n] blocks fl/fs,
 // repeating the call when the neighbour-list set-up has to grow (mg_host.cu)
 mg_status mg_compute_forces(mg_ctx *c, const double *dx, const double *dy, const double *dz, int terms,

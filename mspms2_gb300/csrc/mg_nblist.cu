@@ -36,36 +36,42 @@
 #define META_BUILDS 3
 #define META_NPAIRS 4
 #define META_NCL_TOTAL 6
+#define MG_WIN_MARGIN 1e-9  // columns added on each side of a search window
 
 namespace {
 
-__device__ __forceinline__ double wrap_coord(double x, double L, double *img) {
-    double n = floor(__ddiv_rn(x, L));
+// Image count and column index by a product with the reciprocal rounded once on the host
+// (a division takes many FP64 instructions, and FP64 is slow on this part). The CPU builder
+// uses the same products, so the two stay bit-identical; a wrapped coordinate may lie an
+// ulp outside [0, L), which the column clamp and the cluster boxes take as it is.
+__device__ __forceinline__ double wrap_coord(double x, double L, double invL, double *img) {
+    double n = floor(__dmul_rn(x, invL));
     *img = __dmul_rn(n, L);
     return __dsub_rn(x, *img);
 }
 
-__device__ __forceinline__ int column_of(double w, double cw, int nc) {
-    int c = (int)floor(__ddiv_rn(w, cw));
+__device__ __forceinline__ int column_of(double w, double icw, int nc) {
+    int c = (int)floor(__dmul_rn(w, icw));
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
 __global__ void k_bin(int n, int ncol, const double *__restrict__ x, const double *__restrict__ y,
-                      const double *__restrict__ z, double lx, double ly, double lz, double cwx, double cwy,
-                      int ncx, int ncy, double *__restrict__ xb, double *__restrict__ img,
-                      int *__restrict__ col_of, int *__restrict__ col_count, const int *__restrict__ meta) {
+                      const double *__restrict__ z, double lx, double ly, double lz, double ilx, double ily,
+                      double ilz, double icwx, double icwy, int ncx, int ncy, double *__restrict__ xb,
+                      double *__restrict__ img, int *__restrict__ col_of, int *__restrict__ col_count,
+                      const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     double ix, iy, iz;
-    double wx = wrap_coord(x[a], lx, &ix), wy = wrap_coord(y[a], ly, &iy), wz = wrap_coord(z[a], lz, &iz);
+    double wx = wrap_coord(x[a], lx, ilx, &ix), wy = wrap_coord(y[a], ly, ily, &iy), wz = wrap_coord(z[a], lz, ilz, &iz);
     xb[a] = wx;
     xb[n + a] = wy;
     xb[2 * n + a] = wz;
     img[a] = ix;
     img[n + a] = iy;
     img[2 * n + a] = iz;
-    int col = column_of(wy, cwy, ncy) * ncx + column_of(wx, cwx, ncx);
+    int col = column_of(wy, icwy, ncy) * ncx + column_of(wx, icwx, ncx);
     col_of[a] = col;
     atomicAdd(&col_count[col], 1);
 }
@@ -129,6 +135,13 @@ __global__ void k_scatter(int n, const int *__restrict__ col_of, const int *__re
     sorted[start[col] + slot] = a;
 }
 
+// A 64-bit integer with the order of the FP64 value d (and -0 equal to +0): comparisons of
+// these run on the integer pipes, those of doubles on the slow FP64 pipe.
+__device__ __forceinline__ long long order_key(double d) {
+    const long long b = __double_as_longlong(d);
+    return (b << 1) == 0 ? 0 : (b < 0 ? b ^ 0x7fffffffffffffffLL : b);
+}
+
 // One block per column: sort its sites by (wrapped z, index) in place, count the clusters
 // the cutting rule makes and record where each starts (cut[start + k] = first sorted
 // position of the column's cluster k).
@@ -168,7 +181,8 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
                     bool up = (i & k) == 0;
                     double zi = kz[i], zp = kz[p];
                     int ii = ki[i], ip = ki[p];
-                    bool gt = (zi > zp) || (zi == zp && ii > ip);
+                    const long long bi = order_key(zi), bp = order_key(zp);
+                    bool gt = (bi > bp) || (bi == bp && ii > ip);
                     if (gt == up) {
                         kz[i] = zp;
                         kz[p] = zi;
@@ -199,7 +213,8 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
 __global__ void k_write_clusters(int n, const int *__restrict__ start, const int *__restrict__ sorted,
                                  const int *__restrict__ cut, const int *__restrict__ col_ncl,
                                  const int *__restrict__ cl_start, const double *__restrict__ xb, int cl_cap,
-                                 int *__restrict__ cl_atom, double *__restrict__ cl_ref, double *__restrict__ cl_bb,
+                                 int *__restrict__ cl_atom, double *__restrict__ cl_ref, float *__restrict__ cl_refh,
+                                 double *__restrict__ cl_bb,
                                  float *__restrict__ cl_bbf, unsigned *__restrict__ flags,
                                  const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
@@ -231,7 +246,11 @@ __global__ void k_write_clusters(int n, const int *__restrict__ start, const int
             cl_bb[(size_t)c * 6 + 3 + d] = hi[d];
             cl_bbf[(size_t)c * 6 + d] = (float)lo[d];
             cl_bbf[(size_t)c * 6 + 3 + d] = (float)hi[d];
-            cl_ref[(size_t)c * 3 + d] = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
+            const double r = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
+            cl_ref[(size_t)c * 3 + d] = r;
+            const float rh = __double2float_rn(r);
+            cl_refh[(size_t)c * 6 + d] = rh;
+            cl_refh[(size_t)c * 6 + 3 + d] = __double2float_rn(__dsub_rn(r, (double)rh));
         }
     }
 }
@@ -254,13 +273,15 @@ __device__ __forceinline__ float gap2f(float loi, float hii, float loj, float hi
 
 struct SearchArgs {
     int ncx, ncy;
-    double lx, ly, lz, cwx, cwy, rlist, rlist2;
+    double lx, ly, lz, cwx, cwy, icwx, icwy, rlist, rlist2;
     double nlx, nly, nlz;         // -lx, -ly, -lz: image shifts picked without FP64 arithmetic
     float lxf, lyf, lzf, cwxf, cwyf;  // FP32 copies for the prefilters
     float flo, fhi, fmarg;  // FP32 band [rlist^2 - m, rlist^2 + m] and a length margin
     const int *meta;
     int *meta_w;
     const double *bb, *ref;
+    const float *refh;            // cluster references as FP32 hi, lo pairs [ncl][6]
+    float lxh, lyh, lzh, lxl, lyl, lzl;  // box lengths as FP32 hi + lo
     const float *bbf;
     const int *col_cl_start;
     int *pair_start, *pair_cnt, *pair_j, *pair_img;
@@ -337,19 +358,43 @@ __device__ __forceinline__ ColumnView column_view(const SearchArgs &A, const flo
 
 __device__ __forceinline__ double image_shift(int i, double l, double nl) { return i == 0 ? 0.0 : (i > 0 ? l : nl); }
 
-// writes entry o: j-cluster J in image (ix, iy, iz) of i-cluster I (reference point ri)
-__device__ __forceinline__ void put_entry(const SearchArgs &A, long long o, const double *ri, int J, int ix, int iy,
-                                          int iz) {
-    const double *rj = A.ref + (size_t)J * 3;
-    const double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], image_shift(ix, A.lx, A.nlx)));
-    const double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], image_shift(iy, A.ly, A.nly)));
-    const double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], image_shift(iz, A.lz, A.nlz)));
+// a + b = s + e exactly (Knuth's two-sum, FP32)
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b), bp = __fsub_rn(s, a), ap = __fsub_rn(s, bp);
+    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+    return s;
+}
+
+// ref_i - (ref_j + img L) from FP32 hi + lo pairs: the large parts subtracted exactly by
+// two-sums, the small ones added, one final rounding (within about an ulp of the FP64 value
+// rounded to FP32), with no FP64 instruction
+__device__ __forceinline__ float shift_f32(float ih, float il, float jh, float jl, int img, float lh, float ll) {
+    float e1, e2;
+    const float h = two_sum(ih, -jh, e1);
+    const float h2 = two_sum(h, img == 0 ? 0.f : (img > 0 ? -lh : lh), e2);
+    const float lo = __fadd_rn(__fadd_rn(__fsub_rn(il, jl), img == 0 ? 0.f : (img > 0 ? -ll : ll)), __fadd_rn(e1, e2));
+    return __fadd_rn(h2, lo);
+}
+
+// writes entry o: j-cluster J in image (ix, iy, iz) of i-cluster I (reference point ri, and
+// rih as FP32 hi, lo); the FP64 path's shift in FP64, the mixed path's from the FP32 pairs
+__device__ __forceinline__ void put_entry(const SearchArgs &A, long long o, const double *ri, const float *rih, int J,
+                                          int ix, int iy, int iz) {
     A.pair_j[o] = J;
     A.pair_img[o] = ((ix + 512) & 1023) | (((iy + 512) & 1023) << 10) | (((iz + 512) & 1023) << 20);
-    if (A.fp64)
+    if (A.fp64) {
+        const double *rj = A.ref + (size_t)J * 3;
+        const double s0 = __dsub_rn(ri[0], __dadd_rn(rj[0], image_shift(ix, A.lx, A.nlx)));
+        const double s1 = __dsub_rn(ri[1], __dadd_rn(rj[1], image_shift(iy, A.ly, A.nly)));
+        const double s2 = __dsub_rn(ri[2], __dadd_rn(rj[2], image_shift(iz, A.lz, A.nlz)));
         ((double4 *)A.pair_shift)[o] = make_double4(s0, s1, s2, 0.0);
-    else
-        ((float4 *)A.pair_shift)[o] = make_float4((float)s0, (float)s1, (float)s2, 0.f);
+    } else {
+        const float *rj = A.refh + (size_t)J * 6;
+        ((float4 *)A.pair_shift)[o] =
+            make_float4(shift_f32(rih[0], rih[3], rj[0], rj[3], ix, A.lxh, A.lxl),
+                        shift_f32(rih[1], rih[4], rj[1], rj[4], iy, A.lyh, A.lyl),
+                        shift_f32(rih[2], rih[5], rj[2], rj[5], iz, A.lzh, A.lzl), 0.f);
+    }
 }
 
 // One warp per i-cluster. Entries are ordered by candidate column (row-major over the
@@ -372,10 +417,12 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
         bi[d] = A.bb[(size_t)I * 6 + d];
         bif[d] = A.bbf[(size_t)I * 6 + d];
     }
-    const int cx0 = (int)floor(__ddiv_rn(__dsub_rn(bi[0], A.rlist), A.cwx));
-    const int cx1 = (int)floor(__ddiv_rn(__dadd_rn(bi[3], A.rlist), A.cwx));
-    const int cy0 = (int)floor(__ddiv_rn(__dsub_rn(bi[1], A.rlist), A.cwy));
-    const int cy1 = (int)floor(__ddiv_rn(__dadd_rn(bi[4], A.rlist), A.cwy));
+    // the column window, widened by MG_WIN_MARGIN columns against the rounding of the product
+    // (an extra column holds no cluster within rlist, so the entries and their order stay)
+    const int cx0 = (int)floor(__dsub_rn(__dmul_rn(__dsub_rn(bi[0], A.rlist), A.icwx), MG_WIN_MARGIN));
+    const int cx1 = (int)floor(__dadd_rn(__dmul_rn(__dadd_rn(bi[3], A.rlist), A.icwx), MG_WIN_MARGIN));
+    const int cy0 = (int)floor(__dsub_rn(__dmul_rn(__dsub_rn(bi[1], A.rlist), A.icwy), MG_WIN_MARGIN));
+    const int cy1 = (int)floor(__dadd_rn(__dmul_rn(__dadd_rn(bi[4], A.rlist), A.icwy), MG_WIN_MARGIN));
     const int nx = cx1 - cx0 + 1, ny = cy1 - cy0 + 1;
     if (nx > A.ncx || ny > A.ncy) {  // a column would be visited twice: small-box mode
         if (lane == 0) {
@@ -387,6 +434,9 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
     }
     const int ncand = nx * ny;
     const double *ri = A.ref + (size_t)I * 3;
+    float rih[6];
+    if (!A.fp64)
+        for (int d = 0; d < 6; d++) rih[d] = A.refh[(size_t)I * 6 + d];
     // mode 0: into shared memory; 1: count only (buffer too small); 2: write from run
     long long run = 0;
     bool multi = false;
@@ -446,7 +496,7 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
                                 s_code[w][o] = (ixk + 1) | ((iyk + 1) << 2) | (b << 4);
                             }
                         } else if (mode == 2) {
-                            put_entry(A, o, ri, J, ixk, iyk, b - 1);
+                            put_entry(A, o, ri, rih, J, ixk, iyk, b - 1);
                         }
                         o++;
                     }
@@ -476,7 +526,7 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
                 __syncwarp();
                 for (int e = lane; e < (int)total; e += 32) {
                     const int code = s_code[w][e];
-                    put_entry(A, (long long)off + e, ri, s_j[w][e], (code & 3) - 1, ((code >> 2) & 3) - 1,
+                    put_entry(A, (long long)off + e, ri, rih, s_j[w][e], (code & 3) - 1, ((code >> 2) & 3) - 1,
                               ((code >> 4) & 3) - 1);
                 }
                 return;
@@ -693,6 +743,7 @@ static mg_status size_list(mg_ctx *c) {
         !mg_ensure(c, c->d_col_ncl, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_sorted, sizeof(int) * (size_t)n * 2) ||
         !mg_ensure(c, c->d_xbuild, sizeof(double) * 3 * (size_t)n) || !mg_ensure(c, c->d_img, sizeof(double) * 3 * (size_t)n) ||
         !mg_ensure(c, c->d_cl_atom, sizeof(int) * (size_t)ncl * MG_CL) || !mg_ensure(c, c->d_cl_ref, sizeof(double) * 3 * (size_t)ncl) ||
+        !mg_ensure(c, c->d_cl_refh, sizeof(float) * 6 * (size_t)ncl) ||
         !mg_ensure(c, c->d_cl_bb, sizeof(double) * 6 * (size_t)ncl) || !mg_ensure(c, c->d_cl_bbf, sizeof(float) * 6 * (size_t)ncl) ||
         !mg_ensure(c, c->d_pair_start, sizeof(int) * (size_t)(ncl + 1)) || !mg_ensure(c, c->d_pair_count, sizeof(int) * (size_t)(ncl + 1)) ||
         !mg_ensure(c, c->d_pair_j, sizeof(int) * (size_t)c->pair_cap) || !mg_ensure(c, c->d_pair_shift, ent * (size_t)c->pair_cap) ||
@@ -735,7 +786,8 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
     const bool fp64 = c->opt.precision == MG_PREC_FP64;
     k_zero<<<(ncol + 255) / 256, 256, 0, s>>>((int *)c->d_col_count.p, ncol + 1, meta);
     k_zero<<<1, 32, 0, s>>>((int *)c->d_counter.p, 4, meta);
-    k_bin<<<(n + 255) / 256, 256, 0, s>>>(n, ncol, dx, dy, dz, c->lx, c->ly, c->lz, cwx, cwy, ncx, ncy,
+    k_bin<<<(n + 255) / 256, 256, 0, s>>>(n, ncol, dx, dy, dz, c->lx, c->ly, c->lz, 1.0 / c->lx, 1.0 / c->ly,
+                                           1.0 / c->lz, 1.0 / cwx, 1.0 / cwy, ncx, ncy,
                                            (double *)c->d_xbuild.p, (double *)c->d_img.p, col_of,
                                            (int *)c->d_col_count.p, meta);
     k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_count.p, (int *)c->d_col_start.p, (int *)c->d_col_fill.p, nullptr,
@@ -750,7 +802,7 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
                               c->cl_cap, meta + META_NCL_TOTAL, meta);
     k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, cut,
                                          (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p,
-                                         c->cl_cap, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p,
+                                         c->cl_cap, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, (float *)c->d_cl_refh.p,
                                          (double *)c->d_cl_bb.p, (float *)c->d_cl_bbf.p, (unsigned *)c->d_flags.p,
                                          meta);
     if (c->small_box) {
@@ -768,6 +820,8 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         A.lz = c->lz;
         A.cwx = cwx;
         A.cwy = cwy;
+        A.icwx = 1.0 / cwx;
+        A.icwy = 1.0 / cwy;
         A.nlx = -c->lx;
         A.nly = -c->ly;
         A.nlz = -c->lz;
@@ -791,6 +845,13 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         A.bb = (double *)c->d_cl_bb.p;
         A.bbf = (float *)c->d_cl_bbf.p;
         A.ref = (double *)c->d_cl_ref.p;
+        A.refh = (const float *)c->d_cl_refh.p;
+        A.lxh = (float)c->lx;
+        A.lyh = (float)c->ly;
+        A.lzh = (float)c->lz;
+        A.lxl = (float)(c->lx - (double)A.lxh);
+        A.lyl = (float)(c->ly - (double)A.lyh);
+        A.lzl = (float)(c->lz - (double)A.lzh);
         A.col_cl_start = (int *)c->d_col_cl_start.p;
         A.pair_start = (int *)c->d_pair_start.p;
         A.pair_cnt = (int *)c->d_pair_count.p;

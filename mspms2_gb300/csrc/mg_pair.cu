@@ -9,12 +9,13 @@
 // pair virial (the reference adds the total Ewald energy instead, src/frclong.c:1128).
 //
 // Mixed precision (k_pair): Newton's third law over the half of the cluster-pair list with
-// J >= I, one warp per i-cluster, each unordered site pair evaluated once in FP32; i-forces
-// accumulate in registers (FP32 within two super-steps, then FP64), j-forces go through a
-// per-warp shared matrix of pair forces whose column sums are added, as 64-bit fixed point,
-// to slot-ordered accumulators (integer adds, so the result does not depend on the order in
-// which warps arrive); k_fixed_forces turns those into the FP64 force blocks. Energies and
-// virials: FP32 over at most eight super-steps of one lane, then FP64. Details at k_pair.
+// J >= I, one warp per i-cluster, each unordered site pair evaluated once in FP32 and its
+// force written to a per-warp shared matrix (i-site x j-slot). The row sums are the
+// i-forces (FP32 within two super-steps, then 64-bit fixed point in registers); the column
+// sums are the j-forces, added as 64-bit fixed point to slot-ordered accumulators (integer
+// adds, so the result does not depend on the order in which warps arrive); k_fixed_forces
+// turns those into the FP64 force blocks. Energies and virials: FP32 over at most eight
+// super-steps of one lane, then FP64. Details at k_pair.
 //
 // FP64 (k_pair_full, the plain-FP64 path): the full list, each pair from both sides, FP64
 // throughout and no atomics. Lane l owns i-site l % 8 and j-slots l / 8 and l / 8 + 4 of
@@ -273,9 +274,6 @@ void launch_pair_full_elec(const PairFullArgs &A, bool mic, bool split, unsigned
 #ifndef PAIR_WIN
 #define PAIR_WIN 128    // list entries compacted per window (the kept ones: J >= I)
 #endif
-#ifndef PAIR_ILP
-#define PAIR_ILP 1      // listed pairs a lane evaluates per round
-#endif
 #define PAIR_FFLUSH 2   // super-steps between the FP64 flushes of a lane's i-force partials
 #define PAIR_EFLUSH 8   // super-steps between the FP64 flushes of a lane's energy partials
 
@@ -397,17 +395,22 @@ __device__ __forceinline__ PairOut pair_math(const PairArgs &A, const float4 &pi
     return o;
 }
 
+
 template <int NB>
 struct PairSmem {
     float4 xj[PAIR_WPB][2][PAIR_NJ];  // x, y, z (cluster-relative), info bits
     float4 qj[PAIR_WPB][2][PAIR_NJ];  // q, half-sigma, sqrt-eps
     float4 sh[PAIR_WPB][2][PAIR_SS];  // periodic shift of each entry
-    // pair forces by (bucket, component, j-slot, i-site a ^ ((j-slot >> 2) & 7)): the four lanes
-    // of a site write j-slots of one residue mod 4, which the XOR spreads over the banks
-    float fm[PAIR_WPB][NB][3][PAIR_NJ][MG_CL];
+    float4 xs[PAIR_WPB][MG_CL];       // the i-cluster's sites, as xj and qj
+    float4 qs[PAIR_WPB][MG_CL];
+    // pair forces by (bucket, component, i-site a, j-slot jj ^ 4a): the column pass (one lane
+    // per j-slot, the sites in turn) and the row pass (16-byte loads) read without bank
+    // conflicts, and the XOR spreads the stores of a round, which hold the pairs of one or two
+    // sites, over the banks
+    float fm[PAIR_WPB][NB][3][MG_CL][PAIR_NJ];
     int ent[PAIR_WPB][PAIR_WIN];      // kept entries of the window
     int jf[PAIR_WPB][PAIR_WIN];       // their j-cluster << 1 | (self entry: only i-site < j-site)
-    unsigned char list[PAIR_WPB][MG_CL][PAIR_NJ];
+    unsigned short plist[PAIR_WPB][MG_CL * PAIR_NJ];  // the super-step's pairs: i-site << 6 | j-slot
 };
 
 // One warp per i-cluster I over the half of its list with J >= I: each unordered site pair
@@ -420,14 +423,18 @@ struct PairSmem {
 //   2. lane (site a = lane & 7, q = lane >> 3) tests site a against j-slots 8e + 4h + q of each
 //      entry e (distance, molecule, ghost flags, RESPA bucket, a < b on the zero-image self
 //      entry);
-//   3. each site's active slots are listed (lane q's after those of lanes q' < q) and the
-//      site's four lanes take them in turn: the pair force goes to the lane's i-force partial
-//      and to fm[bucket][.][jj][a] (one writer per cell);
-//   4. the column sums of fm, in site order, are the j-forces of the super-step; they are
+//   3. the active pairs are listed for the whole warp, site after site, and lane l takes
+//      pairs l, l + 32, ... (the busiest site no longer sets the number of rounds): the pair
+//      force goes to fm[bucket][.][a][jj ^ 4a] (one writer per cell), the energies to the
+//      lane's partials;
+//   4. the row sums of fm are the i-forces of the super-step: site a's four lanes a quarter
+//      of the row each, into the lane's FP32 partial (64-bit fixed point every PAIR_FFLUSH
+//      super-steps);
+//   5. the column sums of fm, in site order, are the j-forces of the super-step; they are
 //      added as 64-bit fixed point (units 2^-fixed_bits) to the slot-ordered accumulators.
-// At the end of the row the site's i-force (FP64, its four lanes summed in a fixed order) goes
-// to the same accumulators. A value outside the fixed-point range raises MG_FLAG_FIXED_RANGE:
-// the host then repeats the call with a coarser unit.
+// At the end of the row the site's i-force (its four lanes' integers summed) goes to the same
+// accumulators. A value outside the fixed-point range raises MG_FLAG_FIXED_RANGE: the host
+// then repeats the call with a coarser unit.
 template <int ELEC, bool MIC, bool SPLIT>
 __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     constexpr int NB = SPLIT ? 2 : 1;  // force buckets
@@ -449,6 +456,10 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
         float eL[4] = {0, 0, 0, 0}, eS[4] = {0, 0, 0, 0};  // energy partials since the last FP64 flush
         float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;  // i-force partials since the last flush
         int sstep = 0;
+        if (q == 0) {
+            S.xs[w][a] = pi;
+            S.qs[w][a] = qi;
+        }
         for (int r0 = 0; r0 < ne; r0 += PAIR_WIN) {
             // compact the kept entries of window [r0, r0 + PAIR_WIN) in list order
             int nk = 0;
@@ -545,42 +556,65 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                 up = __shfl_up_sync(0xffffffffu, incl, 16);
                 if (q >= 2) incl += up;
                 const int na = __shfl_sync(0xffffffffu, incl, 24 + a);
-                int off = incl - c0;
-                for (unsigned mm = m; mm; mm &= mm - 1u) {
-                    const int t = __ffs(mm) - 1;
-                    S.list[w][a][off++] = (unsigned char)(8 * (t >> 1) + 4 * (t & 1) + q);
+                // one list for the warp, site after site (lane q's slots after those of q' < q)
+                int sa = na;  // pairs of sites 0..a
+                up = __shfl_up_sync(0xffffffffu, sa, 1, 8);
+                if (a >= 1) sa += up;
+                up = __shfl_up_sync(0xffffffffu, sa, 2, 8);
+                if (a >= 2) sa += up;
+                up = __shfl_up_sync(0xffffffffu, sa, 4, 8);
+                if (a >= 4) sa += up;
+                const int tot = __shfl_sync(0xffffffffu, sa, 7);
+                {
+                    int off = sa - na + incl - c0;
+                    for (unsigned mm = m; mm; mm &= mm - 1u) {
+                        const int t = __ffs(mm) - 1;
+                        S.plist[w][off++] = (unsigned short)((a << 6) | (8 * (t >> 1) + 4 * (t & 1) + q));
+                    }
                 }
                 __syncwarp();
-                // 3. pairs: the site's four lanes take its listed pairs in turn, PAIR_ILP at a time
-                //    as independent chains
-                const int rounds = __reduce_max_sync(0xffffffffu, (na + 4 * PAIR_ILP - 1) / (4 * PAIR_ILP));
-                for (int r = 0; r < rounds; r++) {
-                    PairOut o[PAIR_ILP];
-                    int jl[PAIR_ILP];
-#pragma unroll
-                    for (int u = 0; u < PAIR_ILP; u++) {
-                        const int k = 4 * (PAIR_ILP * r + u) + q;
-                        jl[u] = k < na ? S.list[w][a][k] : -1;
-                        const int jj = jl[u] < 0 ? 0 : jl[u];
-                        o[u] = pair_math<ELEC, MIC>(A, pi, qi, infi, S.xj[w][b][jj], S.qj[w][b][jj], S.sh[w][b][jj >> 3]);
+                // 3. pairs: lane l takes pairs l, l + 32, ... of the list; the pair force goes into
+                //    fm (one writer per cell), the energies into the lane's partials
+                for (int k = lane; k < tot; k += 32) {
+                    const int code = S.plist[w][k];
+                    const int ia = code >> 6, jj = code & 63;
+                    const float4 xa = S.xs[w][ia];
+                    const PairOut o = pair_math<ELEC, MIC>(A, xa, S.qs[w][ia], info_of(xa.w), S.xj[w][b][jj],
+                                                           S.qj[w][b][jj], S.sh[w][b][jj >> 3]);
+                    const bool inner = SPLIT && o.r2 < A.rs2;
+                    npair += 2;  // counted as in a full list
+                    const int bk = inner ? 1 : 0, col = jj ^ (ia << 2);
+                    S.fm[w][bk][0][ia][col] = o.fx;
+                    S.fm[w][bk][1][ia][col] = o.fy;
+                    S.fm[w][bk][2][ia][col] = o.fz;
+                    if (inner) {
+                        eS[0] += o.ulj; eS[1] += o.ush; eS[2] += o.uel; eS[3] += o.vir;
+                    } else {
+                        eL[0] += o.ulj; eL[1] += o.ush; eL[2] += o.uel; eL[3] += o.vir;
                     }
+                }
+                __syncwarp();
+                // 4. i-forces of the super-step: the row sums of site a, its four lanes a quarter
+                //    of the row each (16-byte loads, rotated by a so that the lanes of one load
+                //    fall on different banks)
 #pragma unroll
-                    for (int u = 0; u < PAIR_ILP; u++) {
-                        const int jj = jl[u];
-                        if (jj < 0) continue;
-                        const bool inner = SPLIT && o[u].r2 < A.rs2;
-                        npair += 2;  // counted as in a full list
-                        const int bk = inner ? 1 : 0, col = a ^ ((jj >> 2) & 7);
-                        S.fm[w][bk][0][jj][col] = o[u].fx;
-                        S.fm[w][bk][1][jj][col] = o[u].fy;
-                        S.fm[w][bk][2][jj][col] = o[u].fz;
-                        if (inner) {
-                            bx += o[u].fx; by += o[u].fy; bz += o[u].fz;
-                            eS[0] += o[u].ulj; eS[1] += o[u].ush; eS[2] += o[u].uel; eS[3] += o[u].vir;
-                        } else {
-                            ax += o[u].fx; ay += o[u].fy; az += o[u].fz;
-                            eL[0] += o[u].ulj; eL[1] += o[u].ush; eL[2] += o[u].uel; eL[3] += o[u].vir;
+                for (int bk = 0; bk < NB; bk++) {
+                    float v[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const float4 *row = reinterpret_cast<const float4 *>(S.fm[w][bk][c][a]);
+                        float s = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const float4 f = row[4 * q + ((k + a) & 3)];
+                            s += (f.x + f.y) + (f.z + f.w);
                         }
+                        v[c] = s;
+                    }
+                    if (bk == 0) {
+                        ax += v[0]; ay += v[1]; az += v[2];
+                    } else {
+                        bx += v[0]; by += v[1]; bz += v[2];
                     }
                 }
                 if ((sstep + 1) % PAIR_FFLUSH == 0) {
@@ -617,10 +651,9 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                         unsigned long long *acc = bk ? A.facc_s : A.facc_l;
 #pragma unroll
                         for (int c = 0; c < 3; c++) {
-                            const float *col = S.fm[w][bk][c][t];
-                            float v = col[0];
+                            float v = S.fm[w][bk][c][0][t];
 #pragma unroll
-                            for (int i = 1; i < MG_CL; i++) v += col[i];
+                            for (int i = 1; i < MG_CL; i++) v += S.fm[w][bk][c][i][t ^ (i << 2)];
                             if (v != 0.f) {
                                 long long o;
                                 range_ok &= to_fixed(-v, o, A.fscale, A.flimit);

@@ -306,7 +306,8 @@ extern "C" mg_status mg_sf_tasos_generate(mg_ctx *c, int type, const mg_sfgrid_s
     }
     const bool fp64 = c->opt.precision == MG_PREC_FP64;
     const size_t nn = (size_t)nx * ny * nz;
-    if (!mg_ensure(c, c->tasos_buf[type - 1], (fp64 ? sizeof(double) : sizeof(float)) * 8 * nn)) return MG_ERR_ALLOC;
+    DevBuf &buf = mg_tasos_storage(c, type);
+    if (!mg_ensure(c, buf, (fp64 ? sizeof(double) : sizeof(float)) * 8 * nn)) return MG_ERR_ALLOC;
     SgArgs A = base_args(sp, 1.0);  // K
     A.tasos = 1;
     A.nx = nx;
@@ -316,8 +317,8 @@ extern "C" mg_status mg_sf_tasos_generate(mg_ctx *c, int type, const mg_sfgrid_s
     A.hx = hx;
     A.hy = hy;
     A.hz = hz;
-    if (fp64) A.out = (double *)c->tasos_buf[type - 1].p;
-    else A.out_f32 = (float *)c->tasos_buf[type - 1].p;
+    if (fp64) A.out = (double *)buf.p;
+    else A.out_f32 = (float *)buf.p;
     const size_t ns = (size_t)sp->nsolid;
     std::vector<double> solid(3 * (ns ? ns : 1));
     for (size_t i = 0; i < ns; i++) {
@@ -354,7 +355,7 @@ extern "C" mg_status mg_sf_tasos_generate(mg_ctx *c, int type, const mg_sfgrid_s
             t.hz = hz;
             t.cuc = cuc;
             t.min_pe = mn;
-            t.values = c->tasos_buf[type - 1].p;
+            t.values = buf.p;
         }
     }
     if (d_solid) cudaFree(d_solid);

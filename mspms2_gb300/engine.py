@@ -81,6 +81,7 @@ def load_library(path: str = LIB_PATH):
     lib.mg_adjoint_params.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(I)]
     lib.mg_adjoint_hvp.argtypes = [V, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.mg_sf_tasos_generate.argtypes = [V, I, C.POINTER(capi.MgSfgridSpec), I, I, I, D, D, D, D]
+    lib.mg_sf_tasos_share.argtypes = [V, V]
     lib.mg_set_md_graphs.argtypes = [V, I]
     lib.mg_set_kspace_overlap.argtypes = [V, I]
     lib.mg_set_kspace_tensor.argtypes = [V, I]
@@ -297,6 +298,11 @@ class Engine:
         c, _keep = _sfgrid_spec(spec)
         self._check(self.lib.mg_sf_tasos_generate(self.ctx, type_id, C.byref(c), nx, ny, nz, float(h[0]), float(h[1]),
                                                   float(h[2]), float(cuc)))
+
+    def sf_tasos_share(self, other: "Engine") -> None:
+        """Use the Tasos tables of another engine (same device and precision) without a copy
+        (mg_sf_tasos_share)."""
+        self._check(self.lib.mg_sf_tasos_share(self.ctx, other.ctx))
 
     def set_kspace_overlap(self, enable: bool) -> None:
         """Reciprocal space on a second stream beside the list and pairs (default) or in line."""

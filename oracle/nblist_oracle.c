@@ -24,10 +24,12 @@ static int key_cmp(const void *a, const void *b) {
     return (p->i > q->i) - (p->i < q->i);
 }
 
-static int column_of(double w, double cw, int nc) {
-    int c = (int)floor(w / cw);
+/* products with reciprocals rounded once, as the GPU build takes them */
+static int column_of(double w, double icw, int nc) {
+    int c = (int)floor(w * icw);
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
+#define WIN_MARGIN 1e-9 /* columns added on each side of a search window */
 
 static double gap2(double loi, double hii, double loj, double hij, double s) {
     double a = (loj + s) - hii;
@@ -47,12 +49,13 @@ int orc_nblist_build2(const double *x, const double *y, const double *z, int n, 
     int *col = (int *)malloc(sizeof(int) * (size_t)n);
     int *cnt = (int *)calloc((size_t)ncol + 1, sizeof(int));
     double cwx = lx / ncx, cwy = ly / ncy;
+    double iL[3] = {1.0 / lx, 1.0 / ly, 1.0 / lz}, icwx = 1.0 / cwx, icwy = 1.0 / cwy;
     for (int a = 0; a < n; a++) {
         for (int d = 0; d < 3; d++) {
-            double m = floor(P[d][a] / L[d]);
+            double m = floor(P[d][a] * iL[d]);
             w[(size_t)d * n + a] = P[d][a] - m * L[d];
         }
-        col[a] = column_of(w[(size_t)n + a], cwy, ncy) * ncx + column_of(w[a], cwx, ncx);
+        col[a] = column_of(w[(size_t)n + a], icwy, ncy) * ncx + column_of(w[a], icwx, ncx);
         cnt[col[a]]++;
     }
     int *start = (int *)calloc((size_t)ncol + 1, sizeof(int));
@@ -121,8 +124,8 @@ int orc_nblist_build2(const double *x, const double *y, const double *z, int n, 
             continue;
         }
         const double *bi = bb + (size_t)I * 6;
-        int cx0 = (int)floor((bi[0] - rlist) / cwx), cx1 = (int)floor((bi[3] + rlist) / cwx);
-        int cy0 = (int)floor((bi[1] - rlist) / cwy), cy1 = (int)floor((bi[4] + rlist) / cwy);
+        int cx0 = (int)floor((bi[0] - rlist) * icwx - WIN_MARGIN), cx1 = (int)floor((bi[3] + rlist) * icwx + WIN_MARGIN);
+        int cy0 = (int)floor((bi[1] - rlist) * icwy - WIN_MARGIN), cy1 = (int)floor((bi[4] + rlist) * icwy + WIN_MARGIN);
         for (int uy = cy0; uy <= cy1; uy++) {
             int wy = uy % ncy;
             if (wy < 0) wy += ncy;

@@ -17,7 +17,7 @@ def pytest_configure(config):
 def golden_cases():
     """Force fixtures (frclong/frcshort outputs of the compiled reference)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("md_", "sfgrid_")))
+                  if f.endswith(".npz") and not f.startswith(("md_", "sfgrid_", "hmc_")))
 
 
 def md_golden_cases():

@@ -92,7 +92,7 @@ def test_full_size_matches_oracle(name, prec):
 @pytest.mark.parametrize("name", ["c2", "c5"])
 def test_full_size_list_bit_exact(name):
     """The device cluster-pair list of the whole system equals the CPU builder's, cluster by
-    cluster and entry by entry (order, image and FP32-rounded shift included)."""
+    cluster and entry by entry (order and periodic image included)."""
     from oracle.pyoracle import nblist
     s = configs.water_c2() if name == "c2" else configs.butane_in_tube_bundle()[0]
     s.respa_split = 0.0

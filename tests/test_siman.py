@@ -138,3 +138,62 @@ def test_siman_batch_matches_oracle_per_replica():
         pos = np.stack([bx[off[r]:off[r + 1]], by[off[r]:off[r + 1]], bz[off[r]:off[r + 1]]])
         d = np.linalg.norm((pos - start) - (rpos - start)) / np.linalg.norm(rpos - start)
         assert d <= 1e-5, (r, d)
+
+
+def tasos_replicas(nrep):
+    """Replicas of the Tasos golden system (12 sites in a 12 A box over a 4.2 x 4.2 A grid),
+    cooled briefly from a low temperature so that no site leaves the grid."""
+    import os
+    from conftest import GOLDEN
+    from mspms2_gb300.system import load_system, md_params, time_base
+    s, _ = load_system(os.path.join(GOLDEN, "sf_tasos.npz"))
+    s.delt_fs, s.nstep_inner, s.treq_K = 0.5, 1, 30.0
+    md = md_params(s)
+    md["scheme"] = 1
+    tau = 50.0 / time_base(s)
+    md["qq"] = md["qqs"] = md["gg"] * md["treq"] * tau * tau
+    scheds = [dict(t_initial=30.0 / s.epsilon_base, t_min=20.0 / s.epsilon_base, mu_t=1.2, n_tries=4, max_stages=4,
+                   seed=1000 + r) for r in range(nrep)]
+    return s, md, scheds
+
+
+@pytest.mark.gpu
+def test_shared_tasos_tables_and_concurrent_replicas():
+    """Replicas that share one copy of the Tasos tables (mg_sf_tasos_share): the forces are
+    the same bits as with tables of their own; the storage outlives the context that made
+    it; and annealing runs of several replicas, each a context on its own stream driven from
+    its own host thread, give each replica's result alone."""
+    import threading
+    from mspms2_gb300 import build
+    from mspms2_gb300.engine import Engine
+    build.build()
+    s, md, scheds = tasos_replicas(3)
+    own = Engine(s, precision="mixed")
+    f_own = own.compute()
+    own.close()
+    alone = []
+    for sc in scheds:  # a fresh context each, as the concurrent ones below
+        with Engine(s, precision="mixed") as e:
+            alone.append(e.siman_run(md, sc))
+    src = Engine(s, precision="mixed")
+    engs = [Engine(s, precision="mixed") for _ in scheds]
+    for e in engs:
+        e.sf_tasos_share(src)
+    src.close()  # the tables stay with the contexts that share them
+    f_sh = engs[0].compute()
+    assert np.array_equal(f_own[0], f_sh[0]) and np.array_equal(f_own[1], f_sh[1]) and f_own[2] == f_sh[2]
+    out = [None] * len(engs)
+
+    def work(r):
+        out[r] = engs[r].siman_run(md, scheds[r])
+
+    th = [threading.Thread(target=work, args=(r,)) for r in range(len(engs))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for r in range(len(engs)):
+        for a, b in zip(out[r][:2] + (out[r][3],), alone[r][:2] + (alone[r][3],)):
+            assert np.array_equal(a, b), r
+    for e in engs:
+        e.close()
