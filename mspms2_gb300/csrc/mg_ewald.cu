@@ -37,6 +37,8 @@
 #include <numeric>
 #include <type_traits>
 
+#include <cuda_fp16.h>
+
 #include "mg_internal.cuh"
 
 #define EW_TILE 32      // sites per shared-memory tile in the S(k) pass
@@ -1399,6 +1401,501 @@ inline size_t fmm_smem(int maxa) {
     return (size_t)maxa * (EW_FCHUNK * sizeof(ulonglong2) + EW_FMM_NS * EW_FMM_TPB * sizeof(float2));
 }
 
+// ---------------------------------------------------------------------------------
+// Tensor-core k-space forces (FP32 path, KMAXZ <= 30). The four kz sums of one site and
+// one row that k_kforce_mm forms with FMAs,
+//   W_r = sum_a zr s_r - zi s_i         W_i = sum_a zr d_i + zi d_r
+//   W'_r = sum_a a (zr d_r - zi d_i)     W'_i = sum_a a (zr s_i + zi s_r)
+// (z = Z^a of the site, s = u + v and d = u - v from the row's S(k) coefficients at |kz| a),
+// are, for a tile of KF_SITES sites and KF_ROWS rows, one product
+//   D[site][4 row + c] = sum_k A[site][k] B[k][4 row + c],  k = 2a (real part), 2a + 1 (imaginary)
+// with A the sites' Z table and B the rows' coefficients, K = 2 (kzmax + 1) <= 64.
+// Operands are FP16 hi + lo pairs (hi = x rounded to FP16, lo = the remainder rounded again;
+// 22 significant bits, as a TF32 pair) and the MMAs kind::f16 with FP32 accumulation: hi*hi +
+// hi*lo + lo*hi, the dropped lo*lo term below 2^-22 relative. |z| <= 1; each row's B is
+// scaled by a power of two that brings its largest value into [1/2, 1) (exact, undone in the
+// epilogue), so every coefficient of the row is within FP16's range.
+// k_fcoef_mma writes every row tile once per call as the shared-memory image the MMAs read
+// (K-major, 128-byte swizzle: one 64-wide K atom), and per row its table offsets, wave
+// numbers and scale. k_kforce_mma takes KF_SITES sites per CTA: A, the sites' X and Y tables
+// and the rows of its range go to shared memory once, then the row tiles stream through,
+// warp-specialised:
+//   - one thread of the last warp brings each tile's B in by one bulk copy into one of
+//     KF_NST stages, KF_NST - 1 tiles ahead, and issues the MMAs into one of two
+//     tensor-memory accumulators (128 lanes x KF_N columns), a tcgen05.commit per tile;
+//   - eight epilogue warps (warp w: sites 32 (w & 3).., rows 16 (w >> 2)..) wait for a
+//     tile's commit, read its accumulator, release it (an mbarrier the MMA thread waits on
+//     before it reuses it), and finish the rows on the CUDA cores: A_k = X^kx Y^ky,
+//     gsum = Im(A_k W), Fx += kx gsum, Fy += ky gsum, Fz += Im(A_k W').
+// So the tensor core has the next tile queued while the CUDA cores finish the last one.
+// A CTA takes its range's tiles in a rotated order (from tile blockIdx.x mod range). Per-tile
+// FP32 sums go into hi + lo pairs; the two row halves of a site are added in fixed order at
+// the end. Every wait is bounded; a wait that runs out (or sees another role give up) sets a shared abort word that the other waits also poll, so every role stops; then
+// the CTA waits (default bound) for its last commit and any copy in flight, records
+// MG_FLAG_WAIT_TIMEOUT (and MG_FLAG_MMA_UNDRAINED if that wait ran out too), frees its
+// tensor memory and writes NaN forces for its sites.
+#define KF_SITES 128
+#define KF_ROWS 32
+#define KF_N (4 * KF_ROWS)      // MMA N: four sums per row
+#define KF_EPI_WARPS 8          // epilogue warps; one more warp issues the copies and MMAs
+#define KF_TPB (32 * (KF_EPI_WARPS + 1))
+#define KF_MAXKZ 30             // K = 2 (kzmax + 1) <= 64: one 64-wide FP16 atom
+#define KF_A_BYTES 16384        // A: 128 sites x 128 bytes (hi or lo)
+#define KF_B_BYTES 16384        // B: 128 (row, sum) x 128 bytes (hi or lo)
+#define KF_BTILE (2 * KF_B_BYTES) // a row tile's B: hi then lo
+#define KF_NST 3                // B stages (freed when the tile's MMAs complete)
+#define KF_OFF_B (2 * KF_A_BYTES) // the B stages after A (hi, lo)
+#define KF_OFF_XY (KF_OFF_B + KF_NST * KF_BTILE)
+#define KF_TCOLS 256            // two accumulators of KF_N columns
+#define KF_MAXSPLIT 2           // row-tile ranges (each CTA stages its sites' tables once per range)
+
+inline size_t kf_smem(int KX, int KY, int ntiles_range) {
+    return 1024 + KF_OFF_XY + (size_t)(KX + 1 + KY + 1) * KF_SITES * sizeof(float2) +
+           (size_t)ntiles_range * KF_ROWS * sizeof(uint4) + (((size_t)4 * ntiles_range + 15) & ~(size_t)15) + 128;
+}
+
+// device layout of the force pass's tiles: B of each row tile, the tiles' kzmax, then per row
+// (X offset | Y offset << 16, kx scale, ky scale, scale; the last three as FP32 bits), the
+// offsets in float2 units of the staged tables
+inline size_t kf_off_tkz(int ntiles) { return (size_t)KF_BTILE * ntiles; }
+inline size_t kf_off_rinfo(int ntiles) { return (kf_off_tkz(ntiles) + sizeof(int) * (size_t)ntiles + 15) & ~(size_t)15; }
+inline size_t kf_bytes(int ntiles) { return kf_off_rinfo(ntiles) + sizeof(uint4) * (size_t)ntiles * KF_ROWS; }
+
+// byte offset of 16-byte chunk c (elements 8c..8c+7 of a 64-wide FP16 row) of row m in a
+// K-major tile with 128-byte rows and the 128-byte swizzle
+__device__ __forceinline__ unsigned kf_chunk(int m, int c) {
+    return (unsigned)((m >> 3) * 1024 + (m & 7) * 128 + (((c ^ m) & 7) << 4));
+}
+
+// FP16 hi + lo of eight FP32 values, as two 16-byte chunks
+__device__ __forceinline__ void kf_split8(const float (&x)[8], uint4 &hi, uint4 &lo) {
+    unsigned h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        const __half h0 = __float2half_rn(x[2 * e]), h1 = __float2half_rn(x[2 * e + 1]);
+        const __half l0 = __float2half_rn(x[2 * e] - __half2float(h0)), l1 = __float2half_rn(x[2 * e + 1] - __half2float(h1));
+        h[e] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
+        l[e] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// instruction descriptor of kind::f16: D F32, A and B F16, both K-major, M = 128, N = n
+__host__ __device__ constexpr unsigned umma_idesc_f16(int n) {
+    return (1u << 4) | ((unsigned)(n >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(unsigned d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                         unsigned acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+// one block per row tile: each row's scale (the power of two taking its largest |B| into
+// [1/2, 1)), then B as FP16 hi + lo chunks, and the rows' table data
+__global__ void k_fcoef_mma(EwArgs A, unsigned char *__restrict__ fb, int *__restrict__ tkz, uint4 *__restrict__ rinfo) {
+    __shared__ int s_max[KF_ROWS];
+    const int T = blockIdx.x, p0 = T * KF_ROWS;
+    if (threadIdx.x == 0) tkz[T] = A.rows[A.forder[p0]].z;  // rows run by kzmax, longest first
+    if (threadIdx.x < KF_ROWS) s_max[threadIdx.x] = 0;
+    __syncthreads();
+    const float4 *coef = (const float4 *)A.scoef;
+    // B value of (row j of the tile, sum comp, k)
+    auto bval = [&](int r, int kzr, int comp, int k) -> float {
+        const int a = k >> 1, im = k & 1;
+        if (a > kzr) return 0.f;
+        const float4 uv = coef[A.row_slot[r] / 2 + a];  // u_r, u_i, v_r, v_i
+        const float sr = uv.x + uv.z, si = uv.y + uv.w, dr = uv.x - uv.z, di = uv.y - uv.w;
+        const float fa = (float)a;
+        return comp == 0 ? (im ? -si : sr)
+             : comp == 1 ? (im ? dr : di)
+             : comp == 2 ? (im ? -fa * di : fa * dr)
+                         : (im ? fa * sr : fa * si);
+    };
+    // items: (B row n = 4 j + comp, chunk c of 8 k)
+    for (int it = threadIdx.x; it < KF_N * 8; it += blockDim.x) {
+        const int n = it >> 3, c = it & 7, j = n >> 2, p = p0 + j;
+        if (p >= A.nrows) continue;
+        const int r = A.forder[p], kzr = A.rows[r].z;
+        float m = 0.f;
+        for (int e = 0; e < 8; e++) m = fmaxf(m, fabsf(bval(r, kzr, n & 3, 8 * c + e)));
+        atomicMax(&s_max[j], __float_as_int(m));  // non-negative floats order as integers
+    }
+    __syncthreads();
+    unsigned char *out = fb + (size_t)T * KF_BTILE;
+    for (int it = threadIdx.x; it < KF_N * 8; it += blockDim.x) {
+        const int n = it >> 3, c = it & 7, j = n >> 2, p = p0 + j;
+        float x[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (p < A.nrows) {
+            const int r = A.forder[p], kzr = A.rows[r].z;
+            int e2 = 0;
+            frexpf(__int_as_float(s_max[j]), &e2);
+            const float inv = ldexpf(1.f, -e2);  // exact power of two
+            for (int e = 0; e < 8; e++) x[e] = bval(r, kzr, n & 3, 8 * c + e) * inv;
+        }
+        uint4 hi, lo;
+        kf_split8(x, hi, lo);
+        const unsigned off = kf_chunk(n, c);
+        *(uint4 *)(out + off) = hi;
+        *(uint4 *)(out + KF_B_BYTES + off) = lo;
+    }
+    if (threadIdx.x < KF_ROWS) {
+        const int p = p0 + threadIdx.x;
+        uint4 info = make_uint4(0u, 0u, 0u, 0u);  // padding rows: X^0 Y^0 against zero sums
+        if (p < A.nrows) {
+            const int4 r = A.rows[A.forder[p]];
+            int e2 = 0;
+            frexpf(__int_as_float(s_max[threadIdx.x]), &e2);
+            const float sc = ldexpf(1.f, e2);  // exact: the products below round nothing
+            info = make_uint4((unsigned)(r.x * KF_SITES) | ((unsigned)((r.y < 0 ? -r.y : r.y) * KF_SITES) << 16),
+                              __float_as_uint((float)r.x * sc), __float_as_uint((float)r.y * sc), __float_as_uint(sc));
+        }
+        rinfo[p] = info;
+    }
+}
+
+// a bounded mbarrier wait that also gives up when another role of the CTA has given up:
+// the non-blocking test (the MMA thread, whose phases are mostly complete already), or the
+// potentially blocking try (the epilogue's pollers, which mostly wait and should not flood
+// the shared-memory pipe with tests)
+template <bool BLOCKING>
+__device__ __forceinline__ bool kf_wait(unsigned bar, unsigned parity, long long limit, const volatile int *abort_word) {
+    for (long long i = 0; i < limit; i++) {
+        unsigned ok;
+        if (BLOCKING)
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(bar), "r"(parity)
+                : "memory");
+        else
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(ok)
+                : "r"(bar), "r"(parity)
+                : "memory");
+        if (ok) return true;
+        if ((i & 63) == 63 && *abort_word) return false;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(KF_TPB, 1)
+    k_kforce_mma(EwArgs A, const unsigned char *__restrict__ fb, const int *__restrict__ tkz,
+                 const uint4 *__restrict__ rinfo, unsigned *flags) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned raw = (unsigned)__cvta_generic_to_shared(smem_raw);
+    const unsigned base = (raw + 1023u) & ~1023u;  // the swizzled tiles need 1024-byte alignment
+    unsigned char *gbase = smem_raw + (base - raw);
+    const int KXn = A.kx + 1, KYn = A.ky + 1;
+    const int T0 = A.csplit[blockIdx.y], nt = A.csplit[blockIdx.y + 1] - T0;
+    // CTAs take the range's tiles starting at different tiles (by site tile), so that at any
+    // moment they read different coefficient tiles from L2
+    const int rot = nt > 0 ? (int)(blockIdx.x % (unsigned)nt) : 0;
+    const unsigned o_rs = KF_OFF_XY + (unsigned)(KXn + KYn) * KF_SITES * 8u;  // the range's rows
+    const unsigned o_tkz = o_rs + (unsigned)(nt * KF_ROWS) * 16u;
+    const unsigned o_bar = (o_tkz + 4u * (unsigned)nt + 15u) & ~15u;
+    // barriers: bfull[KF_NST] (copy landed), mdone[2] (tile's MMAs done), afree[2] (tile's
+    // accumulator read); then the tensor-memory address and the abort word
+    const unsigned bfull = base + o_bar, mdone = bfull + 8 * KF_NST, afree = mdone + 16, tslot = afree + 16;
+    volatile int *abort_word = (volatile int *)(gbase + (tslot - base) + 8);
+    float2 *sX = (float2 *)(gbase + KF_OFF_XY), *sY = sX + KXn * KF_SITES;
+    uint4 *sRow = (uint4 *)(gbase + o_rs);
+    int *sT = (int *)(gbase + o_tkz);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int site0 = blockIdx.x * KF_SITES;
+    const unsigned idesc = umma_idesc_f16(KF_N);
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < KF_NST + 2; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bfull + 8 * b), "r"(1) : "memory");
+        for (int b = 0; b < 2; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(afree + 8 * b), "r"(KF_EPI_WARPS) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *abort_word = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot), "r"(KF_TCOLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // the sites' X and Y tables and the range's rows by cp.async (all in flight at once), then
+    // A: Z^a of the tile's sites as (zr, zi) pairs along k, FP16 hi + lo (zero past the table
+    // and past the last site), each thread's loads issued before their stores
+    {
+        const float2 *tab = (const float2 *)A.tab;
+        const float4 *tZP = (const float4 *)(tab + ew_zoff(A.kx, A.ky, A.n));
+        const float2 *tX = tab, *tY = tab + (size_t)KXn * A.n;
+        for (int it = threadIdx.x; it < (KXn + KYn) * KF_SITES; it += KF_TPB) {
+            const int k = it / KF_SITES, sl = it % KF_SITES;
+            if (site0 + sl < A.n)
+                cp_async(sX + it, k < KXn ? tX + (size_t)k * A.n + site0 + sl : tY + (size_t)(k - KXn) * A.n + site0 + sl,
+                         8);
+            else
+                sX[it] = make_float2(0.f, 0.f);
+        }
+        for (int i = threadIdx.x; i < nt * KF_ROWS; i += KF_TPB) {  // in the CTA's tile order
+            const int li = i / KF_ROWS, T = T0 + (li + rot) % nt;
+            cp_async(sRow + i, rinfo + (size_t)T * KF_ROWS + i % KF_ROWS, 16);
+        }
+        cp_async_commit();
+        const int NPP = ew_zpairs(A.kz);
+        constexpr int NI = KF_SITES * 8, NJ = (NI + KF_TPB - 1) / KF_TPB;  // (site, chunk of four |kz|)
+        float4 z[NJ][2];
+#pragma unroll
+        for (int j = 0; j < NJ; j++) {
+            const int it = threadIdx.x + j * KF_TPB, sl = it % KF_SITES, c = it / KF_SITES;
+            const bool in = it < NI && site0 + sl < A.n;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int pp = 2 * c + h;
+                z[j][h] = (in && pp < NPP) ? tZP[(size_t)pp * A.n + site0 + sl] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; j++) {
+            const int it = threadIdx.x + j * KF_TPB, sl = it % KF_SITES, c = it / KF_SITES;
+            if (it >= NI) continue;
+            // k = 8c..8c+7: (zr, zi) of |kz| 4c, 4c+1 (pair 2c), 4c+2, 4c+3 (pair 2c + 1)
+            const float x[8] = {z[j][0].x, z[j][0].z, z[j][0].y, z[j][0].w, z[j][1].x, z[j][1].z, z[j][1].y, z[j][1].w};
+            uint4 hi, lo;
+            kf_split8(x, hi, lo);
+            const unsigned off = kf_chunk(sl, c);
+            *(uint4 *)(gbase + off) = hi;
+            *(uint4 *)(gbase + KF_A_BYTES + off) = lo;
+        }
+        for (int i = threadIdx.x; i < nt; i += KF_TPB) sT[i] = tkz[T0 + (i + rot) % nt];
+        cp_async_wait<0>();
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *(volatile unsigned *)(gbase + (tslot - base));
+
+    float Fh[3] = {0.f, 0.f, 0.f}, Fl[3] = {0.f, 0.f, 0.f};
+    int copied = 0, issued = 0;  // tiles whose copies / MMAs were issued (MMA thread)
+    if (warp == KF_EPI_WARPS) {
+        if (lane == 0) {
+            // row tile li: its B (hi, lo) into stage li % KF_NST
+            auto copy_tile = [&](int li) {
+                const unsigned bar = bfull + 8 * (li % KF_NST);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(KF_BTILE) : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        base + KF_OFF_B + (unsigned)(li % KF_NST) * KF_BTILE),
+                    "l"(fb + (size_t)(T0 + (li + rot) % nt) * KF_BTILE), "r"(KF_BTILE), "r"(bar)
+                    : "memory");
+            };
+            for (; copied < min(nt, KF_NST - 1); copied++) copy_tile(copied);
+            // descriptors differ from the first one by the byte offset / 16 (all shared
+            // addresses here are below 2^18, so the 14-bit address field never carries)
+            const unsigned long long dA0 = umma_desc(base), dB0 = umma_desc(base + KF_OFF_B);
+            for (int li = 0; li < nt; li++) {
+                bool ok = kf_wait<false>(bfull + 8 * (li % KF_NST), (li / KF_NST) & 1, A.mma_wait, abort_word);
+                // accumulator li & 1 was read by tile li - 2's epilogue
+                if (ok && li >= 2) ok = kf_wait<false>(afree + 8 * (li & 1), ((li - 2) >> 1) & 1, A.mma_wait, abort_word);
+                if (!ok) {
+                    *abort_word = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const int nks = (2 * (sT[li] + 1) + 15) / 16;
+                const unsigned acc = tmem + (unsigned)(li & 1) * KF_N;
+                const unsigned long long dB = dB0 + (unsigned)(li % KF_NST) * (KF_BTILE >> 4);
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++) {
+                    if (ks < nks) {
+                        const unsigned long long ah = dA0 + 2 * ks, al = ah + (KF_A_BYTES >> 4);
+                        const unsigned long long bh = dB + 2 * ks, bl = bh + (KF_B_BYTES >> 4);
+                        umma_f16(acc, ah, bh, idesc, ks > 0 ? 1u : 0u);
+                        umma_f16(acc, ah, bl, idesc, 1u);
+                        umma_f16(acc, al, bh, idesc, 1u);
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 mdone + 8 * (li & 1))
+                             : "memory");
+                issued = li + 1;
+                if (li + KF_NST - 1 < nt) {
+                    // stage (li + KF_NST - 1) % KF_NST was read by tile li - 1's MMAs
+                    if (li >= 1 && !kf_wait<false>(mdone + 8 * ((li - 1) & 1), ((li - 1) >> 1) & 1, A.mma_wait, abort_word)) {
+                        *abort_word = 1;
+                        break;
+                    }
+                    copy_tile(li + KF_NST - 1);
+                    copied = li + KF_NST;
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        const int qd = warp & 3, hh = warp >> 2, s = 32 * qd + lane;
+        const unsigned tl = tmem + ((unsigned)(32 * qd) << 16) + (unsigned)(KF_N / 2) * (unsigned)hh;
+        for (int li = 0; li < nt; li++) {
+            // lane 0 polls; its answer is the warp's one decision before the warp-wide loads
+            int ok = 0;
+            if (lane == 0) ok = kf_wait<true>(mdone + 8 * (li & 1), (li >> 1) & 1, A.mma_wait, abort_word);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0) *abort_word = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            float v[4][16];
+            const unsigned col = tl + (unsigned)(li & 1) * KF_N;
+#pragma unroll
+            for (int q = 0; q < 4; q++) tmem_ld16(col + 16u * q, v[q]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(afree + 8 * (li & 1)) : "memory");
+            const uint4 *rr = sRow + li * KF_ROWS + (KF_ROWS / 2) * hh;
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+            for (int jj = 0; jj < KF_ROWS / 2; jj++) {
+                const uint4 info = rr[jj];
+                const float kxs = __uint_as_float(info.y), kys = __uint_as_float(info.z), sc = __uint_as_float(info.w);
+                const float2 X = sX[(info.x & 0xffffu) + s];
+                float2 Y = sY[(info.x >> 16) + s];
+                Y.y = kys < 0.f ? -Y.y : Y.y;
+                const float2 Ak = cmul(X, Y);
+                const float *w = v[jj >> 2] + 4 * (jj & 3);
+                const float g = Ak.x * w[1] + Ak.y * w[0];
+                fx += g * kxs;
+                fy += g * kys;
+                fz += (Ak.x * w[3] + Ak.y * w[2]) * sc;
+            }
+            mg_acc2(Fh[0], Fl[0], fx);
+            mg_acc2(Fh[1], Fl[1], fy);
+            mg_acc2(Fh[2], Fl[2], fz);
+        }
+    }
+    __syncthreads();
+    const bool timeout = *abort_word != 0;
+    if (timeout) {
+        // MMAs and copies may still run: wait, with the full default bound, for the commit of
+        // the last issued tile (it covers every earlier MMA) and for copies not yet waited on
+        bool done = true;
+        if (warp == KF_EPI_WARPS && lane == 0) {
+            if (issued > 0) done &= mbar_wait(mdone + 8 * ((issued - 1) & 1), ((issued - 1) >> 1) & 1, EW_MMA_WAIT);
+            for (int li = issued; li < copied; li++)
+                done &= mbar_wait(bfull + 8 * (li % KF_NST), (li / KF_NST) & 1, EW_MMA_WAIT);
+        }
+        done = __syncthreads_and(done);
+        if (threadIdx.x == 0 && flags)
+            atomicOr(flags, done ? MG_FLAG_WAIT_TIMEOUT : MG_FLAG_WAIT_TIMEOUT | MG_FLAG_MMA_UNDRAINED);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(KF_TCOLS) : "memory");
+    if (warp >= KF_EPI_WARPS) return;
+    const int hh = warp >> 2, s = 32 * (warp & 3) + lane, a_site = site0 + s;
+    if (timeout) {  // the sites' forces carry the failure
+        if (hh == 0 && a_site < A.n) {
+            const double nan = __longlong_as_double(0x7ff8000000000000ll);
+            for (int d = 0; d < 3; d++) {
+                if (A.fsplit == 1) A.f[(size_t)d * A.n + a_site] = nan;
+                else A.fpart[((size_t)blockIdx.y * 3 + d) * A.n + a_site] = nan;
+            }
+        }
+        return;
+    }
+    // the second row half of each site (warps 4..7) joins the first, over A (no MMA reads it now)
+    float *cmb = (float *)gbase;
+    if (hh == 1)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            cmb[(2 * d) * KF_SITES + s] = Fh[d];
+            cmb[(2 * d + 1) * KF_SITES + s] = Fl[d];
+        }
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * KF_EPI_WARPS) : "memory");  // the epilogue warps only
+    if (hh == 0 && a_site < A.n) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const double F = ((double)Fh[d] + (double)Fl[d]) +
+                             ((double)cmb[(2 * d) * KF_SITES + s] + (double)cmb[(2 * d + 1) * KF_SITES + s]);
+            if (A.fsplit == 1) ew_addf(&A.f[(size_t)d * A.n + a_site], A.q[a_site], F, A.twopi[d]);
+            else A.fpart[((size_t)blockIdx.y * 3 + d) * A.n + a_site] = F;
+        }
+    }
+}
+
+// Row-tile ranges for k_kforce_mma: S ranges of about equal work (K steps of a tile plus a
+// fixed share for its CUDA-core pass), S in [1, smax] chosen so that site tiles x S fill the
+// SMs (one CTA each) in whole waves; fills csplit[0..S] in tiles and returns S.
+int kf_split(const std::vector<int> &tile_kz, int n, int nsm, int smax, int *csplit) {
+    const int nt = (int)tile_kz.size();
+    const long long nb = (n + KF_SITES - 1) / KF_SITES;
+    smax = std::max(1, std::min(std::min(smax, EW_MAXSPLIT), nt));
+    int best = 1;
+    double best_eff = 0.0;
+    for (int S = 1; S <= smax; S++) {
+        const long long items = nb * S, rounds = (items + nsm - 1) / nsm;
+        const double eff = (double)items / (double)(rounds * nsm);
+        if (eff > best_eff + 0.02) {
+            best_eff = eff;
+            best = S;
+        }
+    }
+    auto work = [](int kz) { return (long long)((2 * (kz + 1) + 15) / 16) + 4; };
+    long long total = 0;
+    for (int k : tile_kz) total += work(k);
+    csplit[0] = 0;
+    long long acc = 0;
+    int c = 0;
+    for (int y = 1; y < best; y++) {
+        const long long target = total * y / best;
+        while (c < nt && acc + work(tile_kz[c]) <= target) acc += work(tile_kz[c++]);
+        csplit[y] = std::max(c, csplit[y - 1]);
+    }
+    csplit[best] = nt;
+    return best;
+}
+
+int device_sms() {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(1, nsm);
+}
+
+// whether the tensor-core force pass takes these tables (KMAXZ and the shared-memory budget)
+bool kf_fits(int KX, int KY, int KZ, int nrows) {
+    return nrows > 0 && std::max(KZ, 1) <= KF_MAXKZ &&
+           kf_smem(KX, KY, (nrows + KF_ROWS - 1) / KF_ROWS) <= (size_t)227 * 1024;
+}
+
+// kzmax of each row tile (its first row) from the kzmax of each EW_FCHUNK-row chunk
+std::vector<int> kf_tile_kz(const std::vector<int> &chunk_kz, int nrows) {
+    std::vector<int> t((nrows + KF_ROWS - 1) / KF_ROWS);
+    for (size_t T = 0; T < t.size(); T++) t[T] = chunk_kz[T * KF_ROWS / EW_FCHUNK];
+    return t;
+}
+
+// launches of the tensor-core force pass for A (A.csplit / A.fsplit in row tiles; fb holds
+// the B tiles, then their kzmax): B tiles, forces and, for a split, the sum
+cudaError_t kf_launch(const EwArgs &A, unsigned char *fb, int ntiles, unsigned *flags, cudaStream_t s) {
+    int *tkz = (int *)(fb + kf_off_tkz(ntiles));
+    uint4 *rinfo = (uint4 *)(fb + kf_off_rinfo(ntiles));
+    int range = 0;
+    for (int y = 0; y < A.fsplit; y++) range = std::max(range, A.csplit[y + 1] - A.csplit[y]);
+    const size_t smem = kf_smem(A.kx, A.ky, range);
+    k_fcoef_mma<<<ntiles, 256, 0, s>>>(A, fb, tkz, rinfo);
+    cudaError_t e = cudaFuncSetAttribute(k_kforce_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const dim3 grid((unsigned)((A.n + KF_SITES - 1) / KF_SITES), (unsigned)A.fsplit);
+    k_kforce_mma<<<grid, KF_TPB, smem, s>>>(A, fb, tkz, rinfo, flags);
+    if (A.fsplit > 1) k_kforce_sum<<<(A.n + 255) / 256, 256, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
 // resident blocks of k_kforce_mm per SM x SMs, per device and dynamic shared memory size
 int fmm_slots(int maxa) {
     static std::mutex mu;
@@ -1697,6 +2194,32 @@ bool mg_ewald_sk_tensor(const mg_ctx *c) {
     return c->opt.precision != MG_PREC_FP64 && c->kspace_tensor && std::max(c->kmaxz, 1) <= EW_MMA_MAXKZ;
 }
 
+// the k-space forces on the tensor cores (k_kforce_mma): FP32 path, tensor passes on,
+// KMAXZ <= 30, and the sites' X and Y tables fit in shared memory beside the operands
+bool mg_ewald_kf_tensor(const mg_ctx *c) {
+    return c->opt.precision != MG_PREC_FP64 && c->kspace_tensor && kf_fits(c->kmaxx, c->kmaxy, c->kmaxz, c->nrows);
+}
+
+// the tensor-core force pass of a context: B tiles, row-tile ranges, launches
+static mg_status launch_kforce_mma(mg_ctx *c, EwArgs &A, cudaStream_t s, int *launches) {
+    const std::vector<int> tile_kz = kf_tile_kz(c->h_chunk_kz, c->nrows);
+    const int ntiles = (int)tile_kz.size();
+    if (!mg_ensure(c, c->d_kfb, kf_bytes(ntiles)))
+        return mg_fail(c, MG_ERR_ALLOC, "k-space force tiles");
+    A.forder = (const int *)c->d_row_slot.p + c->nrows + c->nslots;
+    A.fcoef = nullptr;
+    A.fpart = nullptr;
+    A.fsplit = kf_split(tile_kz, A.n, device_sms(), KF_MAXSPLIT, A.csplit);
+    if (A.fsplit > 1) {
+        if (!mg_ensure(c, c->d_fpart, sizeof(double) * 3 * (size_t)A.fsplit * A.n))
+            return mg_fail(c, MG_ERR_ALLOC, "k-space partial forces");
+        A.fpart = (double *)c->d_fpart.p;
+    }
+    MG_CUDA(kf_launch(A, (unsigned char *)c->d_kfb.p, ntiles, (unsigned *)c->d_flags.p, s));
+    *launches = A.fsplit > 1 ? 3 : 2;
+    return MG_OK;
+}
+
 bool mg_ewald_horner_force(const mg_ctx *c) {
     const int maxa = c->h_chunk_kz.empty() ? 1 : c->h_chunk_kz[0] + 1;
     return c->opt.precision == MG_PREC_FP64 || maxa > EW_FMM_MAXA;
@@ -1777,11 +2300,17 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     unsigned fblocks = (unsigned)((n + EW_FSITES - 1) / EW_FSITES);
     if (fp64) {
         MG_CUDA(launch_kforce<double>(c->tune.kforce_threads, fblocks, fsmem, s, A, maxa));
+        c->launches += 4;
+    } else if (mg_ewald_kf_tensor(c)) {
+        int nl = 0;
+        const mg_status st = launch_kforce_mma(c, A, s, &nl);
+        if (st) return st;
+        c->launches += 3 + nl;
     } else {
         if (!ew_force_fields(c, A, maxa)) return mg_fail(c, MG_ERR_ALLOC, "k-space force buffers");
         MG_CUDA(launch_kforce<float>(c->tune.kforce_threads, fblocks, fsmem, s, A, maxa));
+        c->launches += 3 + fmm_launches(A, maxa);
     }
-    c->launches += 3 + (fp64 ? 1 : fmm_launches(A, maxa));
     return MG_OK;
 }
 
@@ -2048,11 +2577,17 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     off += ew_align256(sizeof(double) * E_NCOMP * (size_t)rblocks);
     const size_t o_flags = off;  // status word of the tensor-core S(k) pass
     off += 256;
-    const bool table_force = !fp64 && ct.maxa <= EW_FMM_MAXA;
+    // the force pass: on the tensor cores where the context's mixed path takes it there
+    // (the same kernels, so both entry points give the same bits), else the FP32 table pass
+    const bool kf_tensor = !fp64 && kf_fits(KX, KY, KZ0, ct.nrows);
+    const bool table_force = !fp64 && !kf_tensor && ct.maxa <= EW_FMM_MAXA;
     size_t ncoef = 0;
     for (int k : ct.chunk_kz) ncoef += (size_t)(k + 1) * EW_FCHUNK;
     const size_t o_fcoef = off;
     if (table_force) off += ew_align256(sizeof(float4) * ncoef);
+    const int kf_ntiles = (ct.nrows + KF_ROWS - 1) / KF_ROWS;
+    const size_t o_kfb = off;
+    if (kf_tensor) off += ew_align256(kf_bytes(kf_ntiles));
     if (off > (size_t)MG_EWALD_STATIC_SCRATCH_BYTES)
         return ew_static_fail(err, err_len, MG_ERR_CAPACITY,
                               "%d sites with kmax (%d,%d,%d), ksqmax %d need %zu bytes of scratch; the limit is %u",
@@ -2106,13 +2641,16 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     A.fsplit = 1;
     A.csplit[0] = 0;
     A.csplit[1] = nchunk;
-    if (table_force) {
-        A.fcoef = (float4 *)(base + o_fcoef);
+    if (table_force || kf_tensor) {
+        if (table_force) A.fcoef = (float4 *)(base + o_fcoef);
         // partial forces of a row split in what scratch is left
         const size_t left = (size_t)MG_EWALD_STATIC_SCRATCH_BYTES - off;
         const size_t per = sizeof(double) * 3 * (size_t)n;
-        const int smax = (int)std::min<size_t>(EW_MAXSPLIT, per ? left / per : 1);
-        if (smax >= 2) {
+        const int smax = (int)std::min<size_t>(kf_tensor ? KF_MAXSPLIT : EW_MAXSPLIT, per ? left / per : 1);
+        if (kf_tensor) {
+            A.fsplit = kf_split(kf_tile_kz(ct.chunk_kz, ct.nrows), n, device_sms(), std::max(smax, 1), A.csplit);
+            if (A.fsplit > 1) A.fpart = (double *)(base + ew_align256(off));
+        } else if (smax >= 2) {
             A.fsplit = fmm_split(ct.chunk_kz, n, fmm_slots(ct.maxa), smax, A.csplit);
             if (A.fsplit > 1) A.fpart = (double *)(base + ew_align256(off));
         }
@@ -2133,7 +2671,10 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
         else
             EWS_CUDA(launch_sk<float>(A, nblk, s), "k_sk launch");
         k_sk_reduce<float><<<rblocks, EW_RED_PARTS * 256, 0, s>>>(A, nblk_red, slot_row);
-        EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
+        if (kf_tensor)
+            EWS_CUDA(kf_launch(A, base + o_kfb, kf_ntiles, (unsigned *)(base + o_flags), s), "k_kforce_mma launch");
+        else
+            EWS_CUDA(launch_kforce<float>(EW_FG, fblocks, fsmem, s, A, ct.maxa), "k_kforce launch");
     }
     if (d_energy) k_ew_energy<<<1, 256, 0, s>>>(A.rows_e, (int)rblocks, (const unsigned *)(base + o_flags), d_energy);
     EWS_CUDA(cudaGetLastError(), "kernel launch");

@@ -145,7 +145,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
                       &c->d_md_v, &c->d_md_work, &c->d_md_rmass, &c->d_md_part, &c->d_md_dev, &c->d_md_log,
                       &c->d_adj_class, &c->d_adj, &c->d_adj_g,
                       &c->d_sub_start, &c->d_sub_count, &c->d_sub_j, &c->d_sub_shift, &c->d_sub_img, &c->d_facc,
-                      &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_qf, &c->d_fk, &c->d_erows_k};
+                      &c->d_md_glog, &c->d_fcoef, &c->d_fpart, &c->d_kfb, &c->d_qf, &c->d_fk, &c->d_erows_k};
     for (DevBuf *b : bufs) mg_free(*b);
     c->tasos_buf.clear();  // shared storage is freed by its last holder
     for (auto &b : c->myinterp_buf) mg_free(b);
@@ -754,11 +754,12 @@ static mg_status compute_once(mg_ctx *c, const double *dx, const double *dy, con
         return mg_fail(c, MG_ERR_INVALID, "degenerate CHARMM improper (src/impfrc.c:96-134 exits here)");
     if (flags[0] & (MG_FLAG_LIST_OVERFLOW | MG_FLAG_COLUMN_OVERFLOW))
         return mg_fail(c, MG_ERR_CAPACITY, "neighbour-list capacity exceeded");
-    // a give-up of the tensor-core S(k) pass also makes the forces NaN: report the cause
+    // a give-up of a tensor-core reciprocal-space pass (S(k) or forces) spoils the forces: report the cause
     if (flags[0] & MG_FLAG_MMA_UNDRAINED)
-        return mg_fail(c, MG_ERR_CUDA, "tensor-core S(k) pass: an on-chip wait ran out and issued MMAs did not finish "
-                                       "within the bound (tensor memory of the launch may have been overwritten)");
-    if (flags[0] & MG_FLAG_WAIT_TIMEOUT) return mg_fail(c, MG_ERR_CUDA, "tensor-core S(k) pass: an on-chip wait ran out");
+        return mg_fail(c, MG_ERR_CUDA, "tensor-core reciprocal-space pass: an on-chip wait ran out and issued MMAs did "
+                                       "not finish within the bound (tensor memory of the launch may have been overwritten)");
+    if (flags[0] & MG_FLAG_WAIT_TIMEOUT)
+        return mg_fail(c, MG_ERR_CUDA, "tensor-core reciprocal-space pass: an on-chip wait ran out");
     if (flags[0] & MG_FLAG_NONFINITE) return mg_fail(c, MG_ERR_NONFINITE, "non-finite force");
     return MG_OK;
 }

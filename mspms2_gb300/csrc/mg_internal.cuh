@@ -193,6 +193,7 @@ struct mg_ctx {
     DevBuf d_rows, d_row_slot, d_phase, d_spart, d_scoef, d_tasks;
     std::vector<int> h_chunk_kz;  // kzmax of each chunk of the FP32 table force pass
     DevBuf d_fcoef, d_fpart;      // its coefficients and partial forces
+    DevBuf d_kfb;                 // the tensor-core force pass's coefficient tiles and their kzmax
     DevBuf d_qf;                  // FP32 copy of the S(k) site weights
     // the reciprocal-space chain runs on its own stream beside the list and pair kernels,
     // into its own force buffer and energy rows, joined before the forces are summed

@@ -249,11 +249,12 @@ def test_kspace_overlap_is_bit_identical(case):
 @pytest.mark.gpu
 @pytest.mark.parametrize("kmax,ksqmax", [((12, 12, 12), 144), ((9, 7, 30), 400)])
 def test_sk_tensor_pass_matches_cuda_core_pass(kmax, ksqmax):
-    """Structure factors on the tensor cores (TF32 3-term split MMAs, FP32 accumulation in
-    tensor memory) against the CUDA-core FP32 pass and the FP64 path. 11^3 waters = 3993
-    sites: four site blocks, the last one ragged within a 32-site chunk; 12^3 rows of
-    KSQMAX 144 give tiles with kzmax above and below 16 (both MMA widths), and KMAXZ 30 is
-    the largest the pass takes."""
+    """Structure factors and k-space forces on the tensor cores (TF32 3-term split MMAs, FP32
+    accumulation in tensor memory) against the CUDA-core FP32 passes and the FP64 path.
+    11^3 waters = 3993 sites: four S(k) site blocks, the last one ragged within a 32-site
+    chunk, and 32 force tiles of 128 sites, the last one ragged; 12^3 rows of KSQMAX 144 give
+    S(k) tiles with kzmax above and below 16 (both MMA widths) and force row tiles with one
+    and two K atoms; KMAXZ 30 is the largest the passes take."""
     from mspms2_gb300 import configs
     from mspms2_gb300.system import ELEC_EWALD
     s = configs.water_box(11, 34.0, 5, ELEC_EWALD, 0.3, 9.0, kmax=kmax[0], ksqmax=ksqmax)
