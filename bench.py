@@ -154,7 +154,7 @@ def parse():
                     help="only the NVE drift of the 216-water system at 0.5, 0.25 and 0.125 fs (20 ps each)")
     ap.add_argument("--nve-drift", action="store_true",
                     help="print a long small-step NVE drift run of the 216-water Wolf system on the mixed "
-                         "and FP64 paths and exit")
+                         "path (with the power of its force error against the FP64 path) and exit")
     return ap.parse_args()
 
 

@@ -631,7 +631,7 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 #define EW_MMA_SMEM (2 * EW_MMA_STAGE + 64 + 1024)
 #define EW_MMA_WAIT (1ll << 20)  // default polls of each pipeline wait (mg_set_wait_limit)
 #ifndef EW_MMA_GROUP
-#define EW_MMA_GROUP 4     // chunks summed in one tensor-memory accumulator before each drain
+#define EW_MMA_GROUP 2     // chunks summed in one tensor-memory accumulator before each drain
 #endif
 #define EW_MMA_TCOLS 256   // tensor-memory columns per CTA: two group accumulators and the total
 
