@@ -15,7 +15,8 @@
 // sums are the j-forces, added as 64-bit fixed point to slot-ordered accumulators (integer
 // adds, so the result does not depend on the order in which warps arrive); k_fixed_forces
 // turns those into the FP64 force blocks. Energies and virials: FP32 over at most eight
-// super-steps of one lane, then FP64. Details at k_pair.
+// super-steps of one lane, then exact FP32 hi + lo pairs (two-sum: FP64 operations are slow
+// on this part), converted to FP64 once per lane. Details at k_pair.
 //
 // FP64 (k_pair_full, the plain-FP64 path): the full list, each pair from both sides, FP64
 // throughout and no atomics. Lane l owns i-site l % 8 and j-slots l / 8 and l / 8 + 4 of
@@ -302,18 +303,26 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
 }
 
-// x rounded to the nearest integer (ties to even) as a 64-bit integer, for |x| < 2^53, with
-// integer and FP32 operations only (the 64-bit conversion instructions run on the FP64 pipe,
-// which is slow on this part): x = m 2^e with a 24-bit integer mantissa m; for e >= 0 the
-// value is m << e, for |x| < 2^23 adding 2^23 rounds it to an integer held in the low
-// mantissa bits.
+// x rounded to the nearest integer (ties to even) as a 64-bit two's-complement integer, for
+// |x| < 2^55, built from its two 32-bit halves with 32-bit integer and FP32 operations only
+// (64-bit conversions and 64-bit integer work run on the FP64 pipe or its neighbours, which
+// are slow on this part): x = m 2^e with a 24-bit integer mantissa m; for e >= 0 the value is
+// m << e (lo = m << e, hi = the bits shifted out), for |x| < 2^23 adding 2^23 rounds x to an
+// integer held in the low mantissa bits; a negative value is the complement plus one, with
+// the carry from lo into hi.
 __device__ __forceinline__ long long f2ll_rn(float x) {
     const unsigned u = __float_as_uint(x);
     const int e = (int)((u >> 23) & 255u) - 150;
-    const long long big = (long long)((u & 0x7fffffu) | 0x800000u) << (e > 0 ? (e < 40 ? e : 40) : 0);
-    const long long small = (long long)(__float_as_uint(fabsf(x) + 8388608.0f) - 0x4B000000u);
-    const long long r = e >= 0 ? big : small;
-    return (u >> 31) ? -r : r;
+    const unsigned m = (u & 0x7fffffu) | 0x800000u;
+    const unsigned ec = (unsigned)min(max(e, 0), 31);
+    const unsigned small = __float_as_uint(fabsf(x) + 8388608.0f) - 0x4B000000u;
+    unsigned lo = e >= 0 ? m << ec : small;
+    unsigned hi = e >= 0 ? __funnelshift_l(m, 0u, ec) : 0u;
+    if (u >> 31) {
+        lo = ~lo + 1u;
+        hi = ~hi + (lo == 0u ? 1u : 0u);
+    }
+    return (long long)(((unsigned long long)hi << 32) | lo);
 }
 
 // force component -> 64-bit fixed point in units of 1/scale; false when out of range or not
@@ -444,7 +453,8 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     const int a = lane & 7, q = lane >> 3;
     const int I = blockIdx.x * PAIR_WPB + w;
     long long FL[3] = {0, 0, 0}, FS[3] = {0, 0, 0};  // i-force sums in fixed point
-    double E[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // uvdw ushift ureal vir (long bucket), then short
+    // uvdw ushift ureal vir (long bucket), then short: exact FP32 hi + lo pairs (no FP64 in the loop)
+    float Eh[8] = {0, 0, 0, 0, 0, 0, 0, 0}, El[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int npair = 0;
     bool range_ok = true;
     if (I < A.meta[0]) {
@@ -633,10 +643,10 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                 if ((sstep + 1) % PAIR_EFLUSH == 0) {
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
-                        E[k] += (double)eL[k];
+                        mg_acc2(Eh[k], El[k], eL[k]);
                         eL[k] = 0;
                         if (SPLIT) {
-                            E[4 + k] += (double)eS[k];
+                            mg_acc2(Eh[4 + k], El[4 + k], eS[k]);
                             eS[k] = 0;
                         }
                     }
@@ -645,7 +655,7 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                 // 4. j-forces of the super-step: minus the column sums, in site order
                 for (int t = lane; t < cnt * MG_CL; t += 32) {
                     const int J = S.jf[w][ss * PAIR_SS + (t >> 3)] >> 1;
-                    const long long slot = (long long)J * MG_CL + (t & 7);
+                    const unsigned slot = (unsigned)(J * MG_CL + (t & 7));
 #pragma unroll
                     for (int bk = 0; bk < NB; bk++) {
                         unsigned long long *acc = bk ? A.facc_s : A.facc_l;
@@ -667,8 +677,8 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
         }
 #pragma unroll
         for (int k = 0; k < 4; k++) {  // the last partials
-            E[k] += (double)eL[k];
-            if (SPLIT) E[4 + k] += (double)eS[k];
+            mg_acc2(Eh[k], El[k], eL[k]);
+            if (SPLIT) mg_acc2(Eh[4 + k], El[4 + k], eS[k]);
         }
         {
             long long o;
@@ -703,7 +713,7 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
     if (__any_sync(0xffffffffu, !range_ok) && lane == 0) atomicOr(A.flags, MG_FLAG_FIXED_RANGE);
     double eng[9];
 #pragma unroll
-    for (int k = 0; k < 8; k++) eng[k] = E[k];
+    for (int k = 0; k < 8; k++) eng[k] = (double)Eh[k] + (double)El[k];
     eng[8] = (double)npair;
     const int ids[9] = {E_UVDW, E_USHIFT, E_UREAL, E_VIR, E_UVDW_S, E_USHIFT_S, E_UREAL_S, E_VIR_S, E_NPAIR};
     mg_block_row<9>(eng, ids, A.rows, A.row0 + blockIdx.x);
