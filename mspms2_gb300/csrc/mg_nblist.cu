@@ -142,15 +142,19 @@ __device__ __forceinline__ long long order_key(double d) {
     return (b << 1) == 0 ? 0 : (b < 0 ? b ^ 0x7fffffffffffffffLL : b);
 }
 
-// One block per column: sort its sites by (wrapped z, index) in place, count the clusters
-// the cutting rule makes and record where each starts (cut[start + k] = first sorted
-// position of the column's cluster k).
+// One block per column: sort its sites by (wrapped z, index) in place (bitonic, on integer
+// keys with the order of z), count the clusters the cutting rule makes and record where
+// each starts (cut[start + k] = first sorted position of the column's cluster k). The rule
+// (a cluster ends after MG_CL sites or before the first site more than zcap above its first
+// one) is sequential; each position's successor cut is found in parallel first, so that
+// the walk from cut to cut is a chain of table reads.
 __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__restrict__ sorted,
                                const double *__restrict__ xb, double zcap, int *__restrict__ col_ncl,
                                int *__restrict__ cut, unsigned *__restrict__ flags, const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
-    __shared__ double kz[MG_MAX_COLUMN];
+    __shared__ long long kk[MG_MAX_COLUMN];  // order keys of z, then the sorted z themselves
     __shared__ int ki[MG_MAX_COLUMN];
+    __shared__ short nxt[MG_MAX_COLUMN];
     int col = blockIdx.x;
     int s0 = start[col], cnt = start[col + 1] - s0;
     if (cnt > MG_MAX_COLUMN) {
@@ -166,10 +170,10 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
         if (i < cnt) {
             int a = sorted[s0 + i];
             ki[i] = a;
-            kz[i] = xb[2 * (size_t)n + a];
+            kk[i] = order_key(xb[2 * (size_t)n + a]);
         } else {
             ki[i] = 0x7fffffff;
-            kz[i] = INFINITY;
+            kk[i] = 0x7fffffffffffffffLL;
         }
     }
     __syncthreads();
@@ -179,13 +183,12 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
                 int p = i ^ j;
                 if (p > i) {
                     bool up = (i & k) == 0;
-                    double zi = kz[i], zp = kz[p];
-                    int ii = ki[i], ip = ki[p];
-                    const long long bi = order_key(zi), bp = order_key(zp);
+                    const long long bi = kk[i], bp = kk[p];
+                    const int ii = ki[i], ip = ki[p];
                     bool gt = (bi > bp) || (bi == bp && ii > ip);
                     if (gt == up) {
-                        kz[i] = zp;
-                        kz[p] = zi;
+                        kk[i] = bp;
+                        kk[p] = bi;
                         ki[i] = ip;
                         ki[p] = ii;
                     }
@@ -194,16 +197,28 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
             __syncthreads();
         }
     }
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) sorted[s0 + i] = ki[i];
-    if (threadIdx.x == 0) {
-        int ncl = 0, first = 0;
-        for (int i = 0; i < cnt; i++) {
-            if (i == 0 || i - first == MG_CL || __dsub_rn(kz[i], kz[first]) > zcap) {
-                cut[s0 + ncl] = i;
-                ncl++;
-                first = i;
+    double *kz = reinterpret_cast<double *>(kk);  // the sorted z, over the keys
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const int a = ki[i];
+        sorted[s0 + i] = a;
+        kz[i] = xb[2 * (size_t)n + a];
+    }
+    __syncthreads();
+    // the successor cut of a cluster starting at i: i + MG_CL, or the first site within the
+    // next MG_CL - 1 that lies more than zcap above site i (the CPU builder's FP64 test)
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        int nx = min(i + MG_CL, cnt);
+        for (int j = i + 1; j < nx; j++)
+            if (__dsub_rn(kz[j], kz[i]) > zcap) {
+                nx = j;
+                break;
             }
-        }
+        nxt[i] = (short)nx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ncl = 0;
+        for (int first = 0; first < cnt; first = nxt[first]) cut[s0 + ncl++] = first;
         col_ncl[col] = ncl;
     }
 }
