@@ -135,7 +135,7 @@ extern "C" mg_status mg_destroy(mg_ctx *c) {
     DevBuf *bufs[] = {&c->d_site_mol, &c->d_site_q, &c->d_site_hsig, &c->d_site_seps, &c->d_site_flags,
                       &c->d_site_interp, &c->d_species, &c->d_intra, &c->d_bonded, &c->d_site_aw,
                       &c->d_x, &c->d_y, &c->d_z, &c->d_fl, &c->d_fs, &c->d_xbuild, &c->d_img,
-                      &c->d_col_count, &c->d_col_start, &c->d_col_fill, &c->d_col_cl_start,
+                      &c->d_col_count, &c->d_col_start, &c->d_col_fill, &c->d_col_cl_start, &c->d_col_bkt,
                       &c->d_col_sorted, &c->d_cl_atom, &c->d_cl_ref, &c->d_cl_refh, &c->d_cl_bb, &c->d_cl_col,
                       &c->d_pair_start, &c->d_pair_count, &c->d_pair_j, &c->d_pair_shift,
                       &c->d_pack_pos, &c->d_pack_lj, &c->d_pack_info, &c->d_pack_xi, &c->d_pack_qp, &c->d_rows, &c->d_row_slot,

@@ -28,6 +28,7 @@
 
 #define MG_CL 8             // sites per cluster
 #define MG_MAX_COLUMN 2048  // sites per grid column the on-chip sort handles
+#define MG_ZB 32            // z buckets per column of the cluster search
 
 // device status word bits (mg_get_device_flags)
 #define MG_FLAG_OUT_OF_GRID 1u
@@ -161,6 +162,7 @@ struct mg_ctx {
     bool list_valid = false;
     int list_builds = 0, list_rebuilt = 0;
     DevBuf d_col_count, d_col_start, d_col_fill, d_col_cl_start, d_col_sorted;
+    DevBuf d_col_bkt;  // per column and z bucket: the cluster range that can reach the bucket
     DevBuf d_cl_atom, d_cl_ref, d_cl_refh, d_cl_bb, d_cl_col, d_cl_bbf, d_col_ncl, d_counter;
     double zcap = 0;           // largest z extent of a cluster
     bool small_box_forced = false;

@@ -224,14 +224,18 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
 }
 
 // One block per column, one thread per cluster of the column: write the clusters (sites,
-// FP64 and FP32 boxes, centre) from the cuts k_sort_columns recorded.
+// FP64 and FP32 boxes, centre) from the cuts k_sort_columns recorded; then, one thread per z
+// bucket b (z in [b lz / MG_ZB, (b + 1) lz / MG_ZB)), the range of the column's clusters that
+// can overlap the bucket: from the first whose top lies above the bucket's bottom to the last
+// whose bottom lies below the bucket's top, both widened by zmarg. Along a column the clusters
+// are runs of z-sorted sites, so both bounds grow with the cluster index.
 __global__ void k_write_clusters(int n, const int *__restrict__ start, const int *__restrict__ sorted,
                                  const int *__restrict__ cut, const int *__restrict__ col_ncl,
                                  const int *__restrict__ cl_start, const double *__restrict__ xb, int cl_cap,
                                  int *__restrict__ cl_atom, double *__restrict__ cl_ref, float *__restrict__ cl_refh,
                                  double *__restrict__ cl_bb,
-                                 float *__restrict__ cl_bbf, unsigned *__restrict__ flags,
-                                 const int *__restrict__ meta) {
+                                 float *__restrict__ cl_bbf, float lzf, float zmarg, int2 *__restrict__ col_bkt,
+                                 unsigned *__restrict__ flags, const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
     const int col = blockIdx.x;
     const int s0 = start[col], cnt = start[col + 1] - s0;
@@ -268,6 +272,18 @@ __global__ void k_write_clusters(int n, const int *__restrict__ start, const int
             cl_refh[(size_t)c * 6 + 3 + d] = __double2float_rn(__dsub_rn(r, (double)rh));
         }
     }
+    __syncthreads();  // the column's boxes are written
+    const int nw = max(0, min(ncl, cl_cap - c0));
+    for (int b = threadIdx.x; b < MG_ZB; b += blockDim.x) {
+        const float z0 = (float)b * (lzf / MG_ZB) - zmarg, z1 = (float)(b + 1) * (lzf / MG_ZB) + zmarg;
+        int lo = nw, hi = -1;
+        for (int k = 0; k < nw; k++) {
+            const float *bf = cl_bbf + (size_t)(c0 + k) * 6;
+            if (lo == nw && bf[5] >= z0) lo = k;
+            if (bf[2] <= z1) hi = k;
+        }
+        col_bkt[(size_t)col * MG_ZB + b] = make_int2(c0 + lo, c0 + hi);
+    }
 }
 
 // FP64 squared gap between two boxes along one axis, J shifted by s (same op order as
@@ -299,6 +315,8 @@ struct SearchArgs {
     float lxh, lyh, lzh, lxl, lyl, lzl;  // box lengths as FP32 hi + lo
     const float *bbf;
     const int *col_cl_start;
+    const int2 *col_bkt;          // per column and z bucket: cluster range (k_write_clusters)
+    float zr, zbs;                // rlist + margin; buckets per unit z
     int *pair_start, *pair_cnt, *pair_j, *pair_img;
     void *pair_shift;
     unsigned long long *counter;
@@ -412,11 +430,61 @@ __device__ __forceinline__ void put_entry(const SearchArgs &A, long long o, cons
     }
 }
 
+// The clusters of column col that can lie within rlist of an i-cluster with FP32 box bif in
+// z, in any of the images J + s, s = +lz, 0, -lz: for each image the z interval J must reach,
+// mapped through the column's bucket table to a cluster range (a superset of the clusters
+// that overlap it), the ranges merged in increasing cluster order (their starts already run
+// that way). Up to three ranges (ra[k], rn[k] clusters), zero-length at the end.
+__device__ __forceinline__ void column_ranges(const SearchArgs &A, int col, const float *bif, int (&ra)[3],
+                                              int (&rn)[3]) {
+    const int2 *bk = A.col_bkt + (size_t)col * MG_ZB;
+    int s[3], e[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {  // s = +lz, 0, -lz
+        const float sh = (float)(1 - k) * A.lzf;
+        const float q0 = fmaxf(bif[2] - A.zr - sh, 0.f), q1 = fminf(bif[5] + A.zr - sh, A.lzf);
+        s[k] = 0;
+        e[k] = -1;
+        if (q0 <= q1) {
+            const int b0 = min(max((int)(q0 * A.zbs), 0), MG_ZB - 1), b1 = min(max((int)(q1 * A.zbs), 0), MG_ZB - 1);
+            s[k] = bk[b0].x;
+            e[k] = bk[b1].y;
+        }
+    }
+    int m = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        ra[k] = 0;
+        rn[k] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (s[k] > e[k]) continue;  // empty
+        // merge into the last range when it overlaps or touches
+        bool merged = false;
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+            if (r == m - 1 && s[k] <= ra[r] + rn[r]) {
+                rn[r] = max(ra[r] + rn[r], e[k] + 1) - ra[r];
+                merged = true;
+            }
+        if (!merged) {
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+                if (r == m) {
+                    ra[r] = s[k];
+                    rn[r] = e[k] - s[k] + 1;
+                }
+            m++;
+        }
+    }
+}
+
 // One warp per i-cluster. Entries are ordered by candidate column (row-major over the
 // column window), then j-cluster, then z image (-1, 0, 1), as the CPU builder orders them.
-// The warp takes 32 columns at a time (one lane per column: its rejection test and its
-// cluster range), lays their clusters out in that order and tests 32 of them at a time,
-// one per lane, so that many loads are in flight. Hits go to a shared-memory buffer and
+// The warp takes 32 columns at a time (one lane per column: its rejection test and the
+// ranges of its clusters that can reach the i-cluster in z), lays those clusters out in that
+// order and tests 32 of them at a time, one per lane, so that many loads are in flight. Hits go to a shared-memory buffer and
 // are written after one reservation; a warp whose buffer would overflow counts and writes
 // in two passes instead.
 __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
@@ -458,15 +526,16 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
     for (int mode = 0; mode < 3; mode++) {
         for (int base = 0; base < ncand; base += 32) {
             const int c = base + lane;
-            int cnt = 0, j0 = 0;
+            int cnt = 0;
+            int ra[3] = {0, 0, 0}, rn[3] = {0, 0, 0};
             ColumnView v;
             v.ix = v.iy = 0;
             v.sxf = v.syf = 0.f;
             if (c < ncand) {
                 v = column_view(A, bif, cx0, cy0, nx, c);
                 if (!v.reject) {
-                    j0 = A.col_cl_start[v.col];
-                    cnt = A.col_cl_start[v.col + 1] - j0;
+                    column_ranges(A, v.col, bif, ra, rn);
+                    cnt = rn[0] + rn[1] + rn[2];
                 }
             }
             int incl = cnt;
@@ -485,10 +554,14 @@ __global__ void __launch_bounds__(SEARCH_WPB * 32) k_search(SearchArgs A) {
                     if (probe <= t) k += step;
                 }
                 k = min(k, 31);
-                const int jk = __shfl_sync(0xffffffffu, j0, k), ek = __shfl_sync(0xffffffffu, excl, k);
+                const int ek = __shfl_sync(0xffffffffu, excl, k);
+                const int a0 = __shfl_sync(0xffffffffu, ra[0], k), n0 = __shfl_sync(0xffffffffu, rn[0], k);
+                const int a1 = __shfl_sync(0xffffffffu, ra[1], k), n1 = __shfl_sync(0xffffffffu, rn[1], k);
+                const int a2 = __shfl_sync(0xffffffffu, ra[2], k);
                 const int ixk = __shfl_sync(0xffffffffu, v.ix, k), iyk = __shfl_sync(0xffffffffu, v.iy, k);
                 const float sxf = __shfl_sync(0xffffffffu, v.sxf, k), syf = __shfl_sync(0xffffffffu, v.syf, k);
-                const int J = jk + (t - ek);
+                const int off = t - ek;  // the item's place among its column's clusters
+                const int J = off < n0 ? a0 + off : (off < n0 + n1 ? a1 + off - n0 : a2 + off - n0 - n1);
                 unsigned m = 0u;
                 if (t < T)
                     m = cluster_images(A, bi, bif, J, image_shift(ixk, A.lx, A.nlx), image_shift(iyk, A.ly, A.nly),
@@ -755,6 +828,7 @@ static mg_status size_list(mg_ctx *c) {
     size_t ent = fp64 ? sizeof(double4) : sizeof(float4);
     if (!mg_ensure(c, c->d_col_count, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_start, sizeof(int) * (ncol + 1)) ||
         !mg_ensure(c, c->d_col_fill, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_cl_start, sizeof(int) * (ncol + 1)) ||
+        !mg_ensure(c, c->d_col_bkt, sizeof(int2) * (size_t)ncol * MG_ZB) ||
         !mg_ensure(c, c->d_col_ncl, sizeof(int) * (ncol + 1)) || !mg_ensure(c, c->d_col_sorted, sizeof(int) * (size_t)n * 2) ||
         !mg_ensure(c, c->d_xbuild, sizeof(double) * 3 * (size_t)n) || !mg_ensure(c, c->d_img, sizeof(double) * 3 * (size_t)n) ||
         !mg_ensure(c, c->d_cl_atom, sizeof(int) * (size_t)ncl * MG_CL) || !mg_ensure(c, c->d_cl_ref, sizeof(double) * 3 * (size_t)ncl) ||
@@ -815,11 +889,14 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
                                        c->zcap, (int *)c->d_col_ncl.p, cut, (unsigned *)c->d_flags.p, meta);
     k_scan<<<1, 1024, 0, s>>>(ncol, (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, nullptr, meta + META_NCL, nullptr,
                               c->cl_cap, meta + META_NCL_TOTAL, meta);
+    // z margin of the bucket tables and queries: far above the FP32 rounding of boxes and
+    // bounds (a few ulp of the box length)
+    const float zmarg = (float)(64.0 * 5.960464477539063e-08 * 2.0 * std::max(c->lx, std::max(c->ly, c->lz)) + 1e-4 * rlist);
     k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, cut,
                                          (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p,
                                          c->cl_cap, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, (float *)c->d_cl_refh.p,
-                                         (double *)c->d_cl_bb.p, (float *)c->d_cl_bbf.p, (unsigned *)c->d_flags.p,
-                                         meta);
+                                         (double *)c->d_cl_bb.p, (float *)c->d_cl_bbf.p, (float)c->lz, zmarg,
+                                         (int2 *)c->d_col_bkt.p, (unsigned *)c->d_flags.p, meta);
     if (c->small_box) {
         long long tot = (long long)c->cl_cap * c->cl_cap;
         unsigned blocks = (unsigned)std::min<long long>((tot + 255) / 256, 65535);
@@ -868,6 +945,9 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
         A.lyl = (float)(c->ly - (double)A.lyh);
         A.lzl = (float)(c->lz - (double)A.lzh);
         A.col_cl_start = (int *)c->d_col_cl_start.p;
+        A.col_bkt = (const int2 *)c->d_col_bkt.p;
+        A.zr = (float)rlist + zmarg;
+        A.zbs = (float)MG_ZB / (float)c->lz;
         A.pair_start = (int *)c->d_pair_start.p;
         A.pair_cnt = (int *)c->d_pair_count.p;
         A.pair_j = (int *)c->d_pair_j.p;
