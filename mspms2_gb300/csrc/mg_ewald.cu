@@ -762,8 +762,9 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
     };
 
     // A: lane (g = lane & 7, i0 = lane >> 3) makes sites 4g..4g+3 of the warp's rows i0 and
-    // i0 + 4, one 16-byte swizzle chunk per row and operand; B: thread t < 8 NPP makes Z
-    // pair t >> 3 for sites 4 (t & 7)..+3. The loads of chunk c + 1 are issued before the
+    // i0 + 4, one 16-byte swizzle chunk per row and operand; B: thread t, renumbered
+    // t' = (t + 128) mod 256, makes Z pair t' >> 3 for sites 4 (t & 7)..+3 when t' < 8 NPP.
+    // The loads of chunk c + 1 are issued before the
     // barrier of chunk c (registers), so their latency overlaps the barrier and the wait.
     const int g = lane & 7, i0 = lane >> 3;
     int rkx[2], raky[2];
@@ -780,8 +781,11 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
         rys[j] = r.y < 0 ? -1.f : 1.f;
         aoff[j] = (unsigned)(warp * 1024 + i * 128 + ((g ^ i) << 4));
     }
-    const bool bwork = (int)threadIdx.x < 8 * NPP;
-    const int bp = threadIdx.x >> 3;
+    // the B (Z) chunks go to the upper warps first: warp 0 also issues the MMAs (C2: S(k)
+    // 0.336 -> 0.322 ms against giving them to warps 0..3)
+    const int tb = (int)((threadIdx.x + EW_MMA_TPB / 2) % EW_MMA_TPB);
+    const bool bwork = tb < 8 * NPP;
+    const int bp = tb >> 3;
     unsigned boff[4];
     {
         const int nrow[4] = {2 * bp, 2 * bp + 1, H + 2 * bp, H + 2 * bp + 1};
