@@ -107,9 +107,9 @@ def sk_tensor_flops(kmax, ksqmax, n, sites_per_block=1024, rows_per_tile=64, chu
     return flop
 
 
-def kf_tensor_flops(kmax, ksqmax, n, sites_per_tile=128, rows_per_tile=32):
+def kf_tensor_flops(kmax, ksqmax, n, sites_per_tile=128, rows_per_tile=64):
     """FLOP the tensor-core k-space force pass (k_kforce_mma) issues: rows sorted by kzmax
-    (longest first) in tiles of 32, each tile an M = 128 (sites) x N = 128 (four sums per
+    (longest first) in tiles of 64, each tile an M = 128 (sites) x N = 256 (four sums per
     row) GEMM over K = 2 (kzmax + 1) rounded up to 16, for every 128-site tile, three FP16
     MMAs (hi*hi, hi*lo, lo*hi) per product."""
     kx_max, ky_max, kz_max = kmax

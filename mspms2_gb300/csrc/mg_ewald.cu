@@ -1427,9 +1427,10 @@ inline size_t fmm_smem(int maxa) {
 //   - one thread of the last warp brings each tile's B in by one bulk copy into one of
 //     KF_NST stages, KF_NST - 1 tiles ahead, and issues the MMAs into one of two
 //     tensor-memory accumulators (128 lanes x KF_N columns), a tcgen05.commit per tile;
-//   - eight epilogue warps (warp w: sites 32 (w & 3).., rows 16 (w >> 2)..) wait for a
-//     tile's commit, read its accumulator, release it (an mbarrier the MMA thread waits on
-//     before it reuses it), and finish the rows on the CUDA cores: A_k = X^kx Y^ky,
+//   - eight epilogue warps (warp w: sites 32 (w & 3).., rows 32 (w >> 2)..) wait for a
+//     tile's commit, read its accumulator (two passes of 16 rows), release it (an mbarrier
+//     the MMA thread waits on before it reuses it), and finish the rows on the CUDA cores:
+//     A_k = X^kx Y^ky,
 //     gsum = Im(A_k W), Fx += kx gsum, Fy += ky gsum, Fz += Im(A_k W').
 // So the tensor core has the next tile queued while the CUDA cores finish the last one.
 // A CTA takes its range's tiles in a rotated order (from tile blockIdx.x mod range). Per-tile
@@ -1439,18 +1440,18 @@ inline size_t fmm_smem(int maxa) {
 // MG_FLAG_WAIT_TIMEOUT (and MG_FLAG_MMA_UNDRAINED if that wait ran out too), frees its
 // tensor memory and writes NaN forces for its sites.
 #define KF_SITES 128
-#define KF_ROWS 32
+#define KF_ROWS 64
 #define KF_N (4 * KF_ROWS)      // MMA N: four sums per row
 #define KF_EPI_WARPS 8          // epilogue warps; one more warp issues the copies and MMAs
 #define KF_TPB (32 * (KF_EPI_WARPS + 1))
 #define KF_MAXKZ 30             // K = 2 (kzmax + 1) <= 64: one 64-wide FP16 atom
 #define KF_A_BYTES 16384        // A: 128 sites x 128 bytes (hi or lo)
-#define KF_B_BYTES 16384        // B: 128 (row, sum) x 128 bytes (hi or lo)
+#define KF_B_BYTES 32768        // B: 256 (row, sum) x 128 bytes (hi or lo)
 #define KF_BTILE (2 * KF_B_BYTES) // a row tile's B: hi then lo
-#define KF_NST 3                // B stages (freed when the tile's MMAs complete)
+#define KF_NST 2                // B stages (freed when the tile's MMAs complete)
 #define KF_OFF_B (2 * KF_A_BYTES) // the B stages after A (hi, lo)
 #define KF_OFF_XY (KF_OFF_B + KF_NST * KF_BTILE)
-#define KF_TCOLS 256            // two accumulators of KF_N columns
+#define KF_TCOLS 512            // two accumulators of KF_N columns (all of an SM's tensor memory)
 #define KF_MAXSPLIT 2           // row-tile ranges (each CTA stages its sites' tables once per range)
 
 inline size_t kf_smem(int KX, int KY, int ntiles_range) {
@@ -1741,6 +1742,8 @@ __global__ void __launch_bounds__(KF_TPB, 1)
         const int qd = warp & 3, hh = warp >> 2, s = 32 * qd + lane;
         const unsigned tl = tmem + ((unsigned)(32 * qd) << 16) + (unsigned)(KF_N / 2) * (unsigned)hh;
         for (int li = 0; li < nt; li++) {
+            const uint4 *rr = sRow + li * KF_ROWS + (KF_ROWS / 2) * hh;
+            float fx = 0.f, fy = 0.f, fz = 0.f;
             // lane 0 polls; its answer is the warp's one decision before the warp-wide loads
             int ok = 0;
             if (lane == 0) ok = kf_wait<true>(mdone + 8 * (li & 1), (li >> 1) & 1, A.mma_wait, abort_word);
@@ -1750,19 +1753,23 @@ __global__ void __launch_bounds__(KF_TPB, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // the warp's 32 rows in two passes of 16 (64 accumulator columns each); the
+            // accumulator is released once the second pass has been read
+#pragma unroll 1
+            for (int pass = 0; pass < 2; pass++) {
             float v[4][16];
-            const unsigned col = tl + (unsigned)(li & 1) * KF_N;
+            const unsigned col = tl + (unsigned)(li & 1) * KF_N + 64u * (unsigned)pass;
 #pragma unroll
             for (int q = 0; q < 4; q++) tmem_ld16(col + 16u * q, v[q]);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(afree + 8 * (li & 1)) : "memory");
-            const uint4 *rr = sRow + li * KF_ROWS + (KF_ROWS / 2) * hh;
-            float fx = 0.f, fy = 0.f, fz = 0.f;
+            if (pass == 1) {
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(afree + 8 * (li & 1)) : "memory");
+            }
 #pragma unroll
-            for (int jj = 0; jj < KF_ROWS / 2; jj++) {
-                const uint4 info = rr[jj];
+            for (int jj = 0; jj < 16; jj++) {
+                const uint4 info = rr[16 * pass + jj];
                 const float kxs = __uint_as_float(info.y), kys = __uint_as_float(info.z), sc = __uint_as_float(info.w);
                 const float2 X = sX[(info.x & 0xffffu) + s];
                 float2 Y = sY[(info.x >> 16) + s];
@@ -1773,6 +1780,7 @@ __global__ void __launch_bounds__(KF_TPB, 1)
                 fx += g * kxs;
                 fy += g * kys;
                 fz += (Ak.x * w[3] + Ak.y * w[2]) * sc;
+            }
             }
             mg_acc2(Fh[0], Fl[0], fx);
             mg_acc2(Fh[1], Fl[1], fy);
