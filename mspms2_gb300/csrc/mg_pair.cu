@@ -463,6 +463,9 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
         const int infi = info_of(pi.w);
         const bool use_long = (A.mode & 1) != 0, use_short = (A.mode & 2) != 0;
         const int e0 = A.pair_start[I], ne = A.pair_cnt[I];
+        // lanes whose pairs precede lane (a, q)'s in the warp's list: every lane of sites
+        // a' < a, and the lanes q' < q of site a (lane = a + 8 q)
+        const unsigned lmask = ((1u << a) - 1u) * 0x01010101u | (((1u << (8 * q)) - 1u) & (0x01010101u << a));
         float eL[4] = {0, 0, 0, 0}, eS[4] = {0, 0, 0, 0};  // energy partials since the last FP64 flush
         float ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;  // i-force partials since the last flush
         int sstep = 0;
@@ -558,33 +561,28 @@ __global__ void __launch_bounds__(PAIR_WPB * 32) k_pair(PairArgs A) {
                         }
                     }
                 }
-                // 2. list the site's active slots
+                // 2. one list for the warp, site after site (lane q's slots after those of q' < q):
+                //    lane (a, q)'s offset is the sum of the counts of the lanes in lmask (sites
+                //    a' < a, and site a's lanes q' < q), taken bit by bit from five ballots of
+                //    the counts (no chain of dependent shuffles); the stores are unrolled over
+                //    the 16 possible slots
                 const int c0 = __popc(m);
-                int incl = c0;
-                int up = __shfl_up_sync(0xffffffffu, incl, 8);
-                if (q >= 1) incl += up;
-                up = __shfl_up_sync(0xffffffffu, incl, 16);
-                if (q >= 2) incl += up;
-                const int na = __shfl_sync(0xffffffffu, incl, 24 + a);
-                // one list for the warp, site after site (lane q's slots after those of q' < q)
-                int sa = na;  // pairs of sites 0..a
-                up = __shfl_up_sync(0xffffffffu, sa, 1, 8);
-                if (a >= 1) sa += up;
-                up = __shfl_up_sync(0xffffffffu, sa, 2, 8);
-                if (a >= 2) sa += up;
-                up = __shfl_up_sync(0xffffffffu, sa, 4, 8);
-                if (a >= 4) sa += up;
-                const int tot = __shfl_sync(0xffffffffu, sa, 7);
-                {
-                    int off = sa - na + incl - c0;
-                    for (unsigned mm = m; mm; mm &= mm - 1u) {
-                        const int t = __ffs(mm) - 1;
-                        S.plist[w][off++] = (unsigned short)((a << 6) | (8 * (t >> 1) + 4 * (t & 1) + q));
-                    }
+                int off = 0, tot = 0;
+#pragma unroll
+                for (int bit = 0; bit < 5; bit++) {
+                    const unsigned bb = __ballot_sync(0xffffffffu, (c0 >> bit) & 1);
+                    off += __popc(bb & lmask) << bit;
+                    tot += __popc(bb) << bit;
                 }
+#pragma unroll
+                for (int t = 0; t < 2 * PAIR_SS; t++)
+                    if (m & (1u << t))
+                        S.plist[w][off + __popc(m & ((1u << t) - 1u))] =
+                            (unsigned short)((a << 6) | (8 * (t >> 1) + 4 * (t & 1) + q));
                 __syncwarp();
                 // 3. pairs: lane l takes pairs l, l + 32, ... of the list; the pair force goes into
-                //    fm (one writer per cell), the energies into the lane's partials
+                //    fm (one writer per cell), the energies into the lane's partials (two pairs
+                //    a lane per round as independent chains ran slower: 0.39 against 0.37 ms)
                 for (int k = lane; k < tot; k += 32) {
                     const int code = S.plist[w][k];
                     const int ia = code >> 6, jj = code & 63;
