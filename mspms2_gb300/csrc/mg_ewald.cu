@@ -1500,65 +1500,54 @@ __device__ __forceinline__ void umma_f16(unsigned d, unsigned long long a, unsig
         : "memory");
 }
 
-// one block per row tile: each row's scale (the power of two taking its largest |B| into
-// [1/2, 1)), then B as FP16 hi + lo chunks, and the rows' table data
-__global__ void k_fcoef_mma(EwArgs A, unsigned char *__restrict__ fb, int *__restrict__ tkz, uint4 *__restrict__ rinfo) {
-    __shared__ int s_max[KF_ROWS];
-    const int T = blockIdx.x, p0 = T * KF_ROWS;
-    if (threadIdx.x == 0) tkz[T] = A.rows[A.forder[p0]].z;  // rows run by kzmax, longest first
-    if (threadIdx.x < KF_ROWS) s_max[threadIdx.x] = 0;
-    __syncthreads();
+// one warp per row of a tile (grid: tiles x KF_ROWS / 8, eight warps a block): lane (c, ch)
+// takes the row's sum c = lane >> 3 and 16-byte chunk ch = lane & 7 (k = 8 ch..8 ch + 7); the
+// row's scale (the power of two taking its largest |B| into [1/2, 1)) is the warp's maximum;
+// then B as FP16 hi + lo chunks, and the row's table data
+__global__ void __launch_bounds__(256) k_fcoef_mma(EwArgs A, unsigned char *__restrict__ fb, int *__restrict__ tkz,
+                                                   uint4 *__restrict__ rinfo) {
+    const int T = blockIdx.x, lane = threadIdx.x & 31, j = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const int p = T * KF_ROWS + j, comp = lane >> 3, ch = lane & 7, n = 4 * j + comp;
+    if (blockIdx.y == 0 && threadIdx.x == 0) tkz[T] = A.rows[A.forder[T * KF_ROWS]].z;  // rows run by kzmax
     const float4 *coef = (const float4 *)A.scoef;
-    // B value of (row j of the tile, sum comp, k)
-    auto bval = [&](int r, int kzr, int comp, int k) -> float {
-        const int a = k >> 1, im = k & 1;
-        if (a > kzr) return 0.f;
-        const float4 uv = coef[A.row_slot[r] / 2 + a];  // u_r, u_i, v_r, v_i
-        const float sr = uv.x + uv.z, si = uv.y + uv.w, dr = uv.x - uv.z, di = uv.y - uv.w;
-        const float fa = (float)a;
-        return comp == 0 ? (im ? -si : sr)
-             : comp == 1 ? (im ? dr : di)
-             : comp == 2 ? (im ? -fa * di : fa * dr)
-                         : (im ? fa * sr : fa * si);
-    };
-    // items: (B row n = 4 j + comp, chunk c of 8 k)
-    for (int it = threadIdx.x; it < KF_N * 8; it += blockDim.x) {
-        const int n = it >> 3, c = it & 7, j = n >> 2, p = p0 + j;
-        if (p >= A.nrows) continue;
-        const int r = A.forder[p], kzr = A.rows[r].z;
-        float m = 0.f;
-        for (int e = 0; e < 8; e++) m = fmaxf(m, fabsf(bval(r, kzr, n & 3, 8 * c + e)));
-        atomicMax(&s_max[j], __float_as_int(m));  // non-negative floats order as integers
+    float x[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int4 row = make_int4(0, 0, -1, 0);
+    if (p < A.nrows) {
+        const int r = A.forder[p];
+        row = A.rows[r];
+        const int slot = A.row_slot[r] / 2;
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+            const int a = 4 * ch + e / 2;  // k = 8 ch + e (real part), + 1 (imaginary part)
+            if (a > row.z) continue;
+            const float4 uv = coef[slot + a];  // u_r, u_i, v_r, v_i
+            const float sr = uv.x + uv.z, si = uv.y + uv.w, dr = uv.x - uv.z, di = uv.y - uv.w;
+            const float fa = (float)a;
+            x[e] = comp == 0 ? sr : comp == 1 ? di : comp == 2 ? fa * dr : fa * si;
+            x[e + 1] = comp == 0 ? -si : comp == 1 ? dr : comp == 2 ? -fa * di : fa * sr;
+        }
     }
-    __syncthreads();
+    float m = 0.f;
+#pragma unroll
+    for (int e = 0; e < 8; e++) m = fmaxf(m, fabsf(x[e]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    int e2 = 0;
+    frexpf(m, &e2);
+    const float inv = ldexpf(1.f, -e2), sc = ldexpf(1.f, e2);  // exact powers of two
+#pragma unroll
+    for (int e = 0; e < 8; e++) x[e] *= inv;
+    uint4 hi, lo;
+    kf_split8(x, hi, lo);
     unsigned char *out = fb + (size_t)T * KF_BTILE;
-    for (int it = threadIdx.x; it < KF_N * 8; it += blockDim.x) {
-        const int n = it >> 3, c = it & 7, j = n >> 2, p = p0 + j;
-        float x[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (p < A.nrows) {
-            const int r = A.forder[p], kzr = A.rows[r].z;
-            int e2 = 0;
-            frexpf(__int_as_float(s_max[j]), &e2);
-            const float inv = ldexpf(1.f, -e2);  // exact power of two
-            for (int e = 0; e < 8; e++) x[e] = bval(r, kzr, n & 3, 8 * c + e) * inv;
-        }
-        uint4 hi, lo;
-        kf_split8(x, hi, lo);
-        const unsigned off = kf_chunk(n, c);
-        *(uint4 *)(out + off) = hi;
-        *(uint4 *)(out + KF_B_BYTES + off) = lo;
-    }
-    if (threadIdx.x < KF_ROWS) {
-        const int p = p0 + threadIdx.x;
+    const unsigned off = kf_chunk(n, ch);
+    *(uint4 *)(out + off) = hi;
+    *(uint4 *)(out + KF_B_BYTES + off) = lo;
+    if (lane == 0) {
         uint4 info = make_uint4(0u, 0u, 0u, 0u);  // padding rows: X^0 Y^0 against zero sums
-        if (p < A.nrows) {
-            const int4 r = A.rows[A.forder[p]];
-            int e2 = 0;
-            frexpf(__int_as_float(s_max[threadIdx.x]), &e2);
-            const float sc = ldexpf(1.f, e2);  // exact: the products below round nothing
-            info = make_uint4((unsigned)(r.x * KF_SITES) | ((unsigned)((r.y < 0 ? -r.y : r.y) * KF_SITES) << 16),
-                              __float_as_uint((float)r.x * sc), __float_as_uint((float)r.y * sc), __float_as_uint(sc));
-        }
+        if (p < A.nrows)  // the products with the power of two are exact
+            info = make_uint4((unsigned)(row.x * KF_SITES) | ((unsigned)((row.y < 0 ? -row.y : row.y) * KF_SITES) << 16),
+                              __float_as_uint((float)row.x * sc), __float_as_uint((float)row.y * sc), __float_as_uint(sc));
         rinfo[p] = info;
     }
 }
@@ -1899,7 +1888,7 @@ cudaError_t kf_launch(const EwArgs &A, unsigned char *fb, int ntiles, unsigned *
     int range = 0;
     for (int y = 0; y < A.fsplit; y++) range = std::max(range, A.csplit[y + 1] - A.csplit[y]);
     const size_t smem = kf_smem(A.kx, A.ky, range);
-    k_fcoef_mma<<<ntiles, 256, 0, s>>>(A, fb, tkz, rinfo);
+    k_fcoef_mma<<<dim3((unsigned)ntiles, KF_ROWS / 8), 256, 0, s>>>(A, fb, tkz, rinfo);
     cudaError_t e = cudaFuncSetAttribute(k_kforce_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const dim3 grid((unsigned)((A.n + KF_SITES - 1) / KF_SITES), (unsigned)A.fsplit);
