@@ -55,6 +55,19 @@ __device__ __forceinline__ int column_of(double w, double icw, int nc) {
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
+// counter[key] += 1 for every calling lane, one atomic per distinct key of the warp (sites in
+// molecule order put about three a warp in each column); returns the lane's value of the
+// counter before its own increment (lanes of one key in lane order)
+__device__ __forceinline__ int warp_add1(int *__restrict__ counter, int key) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, key);
+    const int lane = (int)(threadIdx.x & 31), leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&counter[key], __popc(peers));
+    base = __shfl_sync(act, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 __global__ void k_bin(int n, int ncol, const double *__restrict__ x, const double *__restrict__ y,
                       const double *__restrict__ z, double lx, double ly, double lz, double ilx, double ily,
                       double ilz, double icwx, double icwy, int ncx, int ncy, double *__restrict__ xb,
@@ -73,7 +86,7 @@ __global__ void k_bin(int n, int ncol, const double *__restrict__ x, const doubl
     img[2 * n + a] = iz;
     int col = column_of(wy, icwy, ncy) * ncx + column_of(wx, icwx, ncx);
     col_of[a] = col;
-    atomicAdd(&col_count[col], 1);
+    warp_add1(col_count, col);
 }
 
 __global__ void k_zero(int *__restrict__ p, int count, const int *__restrict__ meta) {
@@ -131,7 +144,7 @@ __global__ void k_scatter(int n, const int *__restrict__ col_of, const int *__re
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     int col = col_of[a];
-    int slot = atomicAdd(&fill[col], 1);
+    int slot = warp_add1(fill, col);  // the order within a column is undone by the z sort
     sorted[start[col] + slot] = a;
 }
 
