@@ -104,33 +104,51 @@ __global__ void k_scan(int nc, const int *__restrict__ count, int *__restrict__ 
                        int *__restrict__ total_out, int *__restrict__ max_out, int cap, int *__restrict__ total_raw,
                        const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
-    __shared__ int s_sum[1024], s_max[1024];
-    int t = threadIdx.x, nt = blockDim.x;
-    int per = (nc + nt - 1) / nt;
-    int b = t * per, e = min(nc, b + per);
+    __shared__ int s_sum[32], s_max[32];
+    const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, w = t >> 5;
+    const int per = (nc + nt - 1) / nt;
+    const int b = t * per, e = min(nc, b + per);
     int sum = 0, mx = 0;
     for (int i = b; i < e; i++) {
         sum += count[i];
         mx = max(mx, count[i]);
     }
-    s_sum[t] = sum;
-    s_max[t] = mx;
+    // exclusive scan of the per-thread sums: within each warp by shuffles, then over the
+    // warps' totals by the first warp
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    int wm = mx;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+    if (lane == 31) s_sum[w] = incl;
+    if (lane == 0) s_max[w] = wm;
     __syncthreads();
-    if (t == 0) {
-        int a = 0, m = 0;
-        for (int i = 0; i < nt; i++) {
-            int v = s_sum[i];
-            s_sum[i] = a;
-            a += v;
-            m = max(m, s_max[i]);
+    if (w == 0) {
+        const int nw = nt >> 5;
+        int v = lane < nw ? s_sum[lane] : 0, m = lane < nw ? s_max[lane] : 0;
+        int vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, vi, o);
+            if (lane >= o) vi += u;
         }
-        start[nc] = a;
-        if (total_out) *total_out = (cap >= 0 && a > cap) ? 0 : a;
-        if (total_raw) *total_raw = a;
-        if (max_out) *max_out = m;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane < nw) s_sum[lane] = vi - v;  // exclusive prefix of the warps
+        if (lane == 31) {
+            const int a = vi;  // the total (warps beyond nw add zero)
+            start[nc] = a;
+            if (total_out) *total_out = (cap >= 0 && a > cap) ? 0 : a;
+            if (total_raw) *total_raw = a;
+            if (max_out) *max_out = m;
+        }
     }
     __syncthreads();
-    int a = s_sum[t];
+    int a = s_sum[w] + incl - sum;
     for (int i = b; i < e; i++) {
         start[i] = a;
         if (fill) fill[i] = 0;
