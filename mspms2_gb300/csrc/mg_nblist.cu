@@ -254,13 +254,14 @@ __global__ void k_sort_columns(int n, const int *__restrict__ start, int *__rest
     }
 }
 
-// One block per column, one thread per cluster of the column: write the clusters (sites,
-// FP64 and FP32 boxes, centre) from the cuts k_sort_columns recorded; then, one thread per z
-// bucket b (z in [b lz / MG_ZB, (b + 1) lz / MG_ZB)), the range of the column's clusters that
-// can overlap the bucket: from the first whose top lies above the bucket's bottom to the last
-// whose bottom lies below the bucket's top, both widened by zmarg. Along a column the clusters
-// are runs of z-sorted sites, so both bounds grow with the cluster index.
-__global__ void k_write_clusters(int n, const int *__restrict__ start, const int *__restrict__ sorted,
+// One block per column, eight lanes per cluster of the column (one per site): write the
+// clusters (sites, FP64 and FP32 boxes, centre) from the cuts k_sort_columns recorded, the
+// box bounds as the exact FP64 minimum and maximum over the eight lanes; then, one thread
+// per z bucket b (z in [b lz / MG_ZB, (b + 1) lz / MG_ZB)), the range of the column's
+// clusters that can overlap the bucket: from the first whose top lies above the bucket's
+// bottom to the last whose bottom lies below the bucket's top, both widened by zmarg. Along a
+// column the clusters are runs of z-sorted sites, so both bounds grow with the cluster index.
+__global__ void __launch_bounds__(256) k_write_clusters(int n, const int *__restrict__ start, const int *__restrict__ sorted,
                                  const int *__restrict__ cut, const int *__restrict__ col_ncl,
                                  const int *__restrict__ cl_start, const double *__restrict__ xb, int cl_cap,
                                  int *__restrict__ cl_atom, double *__restrict__ cl_ref, float *__restrict__ cl_refh,
@@ -268,50 +269,58 @@ __global__ void k_write_clusters(int n, const int *__restrict__ start, const int
                                  float *__restrict__ cl_bbf, float lzf, float zmarg, int2 *__restrict__ col_bkt,
                                  unsigned *__restrict__ flags, const int *__restrict__ meta) {
     if (!meta[META_NEED]) return;
+    __shared__ float s_zlo[MG_MAX_COLUMN], s_zhi[MG_MAX_COLUMN];
     const int col = blockIdx.x;
     const int s0 = start[col], cnt = start[col + 1] - s0;
     if (cnt > MG_MAX_COLUMN) return;
     const int ncl = col_ncl[col], c0 = cl_start[col];
-    for (int k = threadIdx.x; k < ncl; k += blockDim.x) {
-        const int c = c0 + k;
-        if (c >= cl_cap) {
-            atomicOr(flags, MG_FLAG_LIST_OVERFLOW);
-            break;
-        }
-        const int first = cut[s0 + k], end = k + 1 < ncl ? cut[s0 + k + 1] : cnt;
-        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (int s = 0; s < MG_CL; s++) {
-            const int idx = first + s;
-            const int a = idx < end ? sorted[s0 + idx] : -1;
-            cl_atom[(size_t)c * MG_CL + s] = a;
-            if (a < 0) continue;
-            for (int d = 0; d < 3; d++) {
-                const double v = xb[(size_t)d * n + a];
-                lo[d] = fmin(lo[d], v);
-                hi[d] = fmax(hi[d], v);
+    const int nw = max(0, min(ncl, cl_cap - c0));
+    if (threadIdx.x == 0 && ncl > nw) atomicOr(flags, MG_FLAG_LIST_OVERFLOW);
+    const int sl = threadIdx.x & 7;
+    for (int k0 = 0; k0 < nw; k0 += blockDim.x >> 3) {  // whole warps stay in the loop (shuffles)
+        const int k = k0 + (int)(threadIdx.x >> 3), c = c0 + k;
+        const bool on = k < nw;
+        const int first = on ? cut[s0 + k] : 0, end = on ? (k + 1 < ncl ? cut[s0 + k + 1] : cnt) : 0;
+        const int idx = first + sl;
+        const int a = on && idx < end ? sorted[s0 + idx] : -1;
+        if (on) cl_atom[(size_t)c * MG_CL + sl] = a;
+        double lo[3], hi[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const double v = a >= 0 ? xb[(size_t)d * n + a] : 0.0;
+            lo[d] = a >= 0 ? v : INFINITY;
+            hi[d] = a >= 0 ? v : -INFINITY;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {  // over the cluster's eight lanes
+                lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+                hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
             }
         }
-        for (int d = 0; d < 3; d++) {
-            cl_bb[(size_t)c * 6 + d] = lo[d];
-            cl_bb[(size_t)c * 6 + 3 + d] = hi[d];
-            cl_bbf[(size_t)c * 6 + d] = (float)lo[d];
-            cl_bbf[(size_t)c * 6 + 3 + d] = (float)hi[d];
-            const double r = __dmul_rn(0.5, __dadd_rn(lo[d], hi[d]));
+        if (on && sl < 3) {
+            const int d = sl;
+            const double l = d == 0 ? lo[0] : d == 1 ? lo[1] : lo[2], h = d == 0 ? hi[0] : d == 1 ? hi[1] : hi[2];
+            cl_bb[(size_t)c * 6 + d] = l;
+            cl_bb[(size_t)c * 6 + 3 + d] = h;
+            cl_bbf[(size_t)c * 6 + d] = (float)l;
+            cl_bbf[(size_t)c * 6 + 3 + d] = (float)h;
+            if (d == 2) {
+                s_zlo[k] = (float)l;
+                s_zhi[k] = (float)h;
+            }
+            const double r = __dmul_rn(0.5, __dadd_rn(l, h));
             cl_ref[(size_t)c * 3 + d] = r;
             const float rh = __double2float_rn(r);
             cl_refh[(size_t)c * 6 + d] = rh;
             cl_refh[(size_t)c * 6 + 3 + d] = __double2float_rn(__dsub_rn(r, (double)rh));
         }
     }
-    __syncthreads();  // the column's boxes are written
-    const int nw = max(0, min(ncl, cl_cap - c0));
+    __syncthreads();  // the column's z bounds are in shared memory
     for (int b = threadIdx.x; b < MG_ZB; b += blockDim.x) {
         const float z0 = (float)b * (lzf / MG_ZB) - zmarg, z1 = (float)(b + 1) * (lzf / MG_ZB) + zmarg;
         int lo = nw, hi = -1;
         for (int k = 0; k < nw; k++) {
-            const float *bf = cl_bbf + (size_t)(c0 + k) * 6;
-            if (lo == nw && bf[5] >= z0) lo = k;
-            if (bf[2] <= z1) hi = k;
+            if (lo == nw && s_zhi[k] >= z0) lo = k;
+            if (s_zlo[k] <= z1) hi = k;
         }
         col_bkt[(size_t)col * MG_ZB + b] = make_int2(c0 + lo, c0 + hi);
     }
@@ -923,7 +932,7 @@ mg_status mg_list_update(mg_ctx *c, const double *dx, const double *dy, const do
     // z margin of the bucket tables and queries: far above the FP32 rounding of boxes and
     // bounds (a few ulp of the box length)
     const float zmarg = (float)(64.0 * 5.960464477539063e-08 * 2.0 * std::max(c->lx, std::max(c->ly, c->lz)) + 1e-4 * rlist);
-    k_write_clusters<<<ncol, 32, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, cut,
+    k_write_clusters<<<ncol, 256, 0, s>>>(n, (int *)c->d_col_start.p, (int *)c->d_col_sorted.p, cut,
                                          (int *)c->d_col_ncl.p, (int *)c->d_col_cl_start.p, (double *)c->d_xbuild.p,
                                          c->cl_cap, (int *)c->d_cl_atom.p, (double *)c->d_cl_ref.p, (float *)c->d_cl_refh.p,
                                          (double *)c->d_cl_bb.p, (float *)c->d_cl_bbf.p, (float)c->lz, zmarg,
