@@ -42,7 +42,6 @@ import numpy as np  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP32_LANES_PER_SM = 128
-TF32_DENSE_NOMINAL = 1100.0  # TFLOP/s, dense TF32 tensor rate of the part
 # algorithmic work per unit (fixed constants of the work model; FP32 FLOP)
 # Fixed work model of the path (the roofline's algorithmic FLOP): a pair inside the cutoff,
 # counted once, is 55 FP32 FLOP (LJ + Ewald real space); reciprocal space is 10 FLOP per
@@ -82,7 +81,7 @@ def sk_tensor_flops(kmax, ksqmax, n, sites_per_block=1024, rows_per_tile=64, chu
     """FLOP the tensor-core S(k) pass (k_sk_mma) issues: rows sorted by kzmax (longest
     first) in tiles of 64, each tile an M = 128 x N = 2H GEMM (H = 16 if its longest row has
     kzmax < 16, else 32) over the sites of every block padded to whole 32-site chunks, three
-    TF32 MMAs (hi*hi, hi*lo, lo*hi) per product."""
+    FP16 MMAs (hi*hi, hi*lo, lo*hi) per product."""
     kx_max, ky_max, kz_max = kmax
     kz = []
     for kx in range(kx_max + 1):
@@ -1167,12 +1166,14 @@ def run_ours(args, rank, world, local_rank):
                           "one rate)" if measured_peaks().get("bf16_tflops") else "of fallback (1.9 PFLOP/s bf16)"}
     if kvec and args.precision == "mixed" and system.kmax[2] <= 30:
         tf = sk_tensor_flops(tuple(system.kmax), system.ksqmax, n)
+        f16_peak = measured_peaks().get("bf16_tflops") or 1900.0
         line["kspace_sk_tensor"] = {
-            "kernel": "k_sk_mma", "ms": kms[3], "mma_tflop": tf / 1e12,
-            "achieved_tflops": tf / (kms[3] * 1e-3) / 1e12 if kms[3] > 0 else 0.0, "peak_tflops": TF32_DENSE_NOMINAL,
-            "frac": tf / (kms[3] * 1e-3) / 1e12 / TF32_DENSE_NOMINAL if kms[3] > 0 else 0.0,
-            "peak_basis": "nominal dense TF32 (MEASURED_PEAKS.json holds bf16 only)",
-            "note": "structure factors as TF32 MMAs (3-term split product, FP32 accumulation in tensor memory); "
+            "kernel": "k_sk_mma", "ms": kms[3], "mma_tflop": tf / 1e12, "operands": "FP16 hi + lo, kind::f16",
+            "achieved_tflops": tf / (kms[3] * 1e-3) / 1e12 if kms[3] > 0 else 0.0, "peak_tflops": f16_peak,
+            "frac": tf / (kms[3] * 1e-3) / 1e12 / f16_peak if kms[3] > 0 else 0.0,
+            "peak_basis": "of measured: MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 burst; FP16 and BF16 MMAs run at "
+                          "one rate)" if measured_peaks().get("bf16_tflops") else "of fallback (1.9 PFLOP/s bf16)",
+            "note": "structure factors as FP16 MMAs (3-term split product, FP32 accumulation in tensor memory); "
                     "FLOP issued, padding included; the stage time includes operand generation on the CUDA cores"}
     if "cpu_baseline" in extras:
         line["cpu_baseline"] = extras.pop("cpu_baseline")

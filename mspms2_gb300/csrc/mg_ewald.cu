@@ -14,7 +14,7 @@
 // and no recurrence. Tables per site: X[0..KMAXX], Y[0..KMAXY], Z[0..KMAXZ].
 //
 // k-vectors are grouped in rows (kx, ky) holding |kz| = 0..kzmax(kx,ky) with both signs
-// of kz. Structure factors, mixed path: k_sk_mma runs the sum over sites as TF32 MMAs on
+// of kz. Structure factors, mixed path: k_sk_mma runs the sum over sites as FP16 MMAs on
 // the tensor cores ((row, Re/Im of q X Y) x site against site x (|kz|, Re/Im of Z), 3-term
 // split products, accumulators in tensor memory); k_sk2 is the CUDA-core form (KMAXZ > 30,
 // or the tensor pass off): a thread owns (row, up to 8 consecutive |kz|) = up to 16
@@ -599,11 +599,13 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 //   B[kz][s] = Re Z^kz_s, B[H + kz][s] = Im Z^kz_s, H = 16 or 32     (N = 2H)
 // so that lane r of D holds RR (columns kz) and RI (H + kz) and lane 64 + r holds IR and
 // II, and S(+kz) = (RR - II, RI + IR), S(-kz) = (RR + II, IR - RI) as in k_sk2. A is made
-// per chunk of 32 sites by the CUDA cores from the phase tables, B from the Z pairs; both
-// go to shared memory as TF32 hi + lo pairs (round to nearest, then the exact remainder
-// rounded again) in the canonical K-major 128-byte-swizzled layout, and one thread issues
-// kind::tf32 MMAs for hi*hi + hi*lo + lo*hi (the 3-term split product keeps the FP32
-// operands' accuracy; the dropped lo*lo term is below 2^-22 relative). The tensor core's
+// per chunk of 32 sites by the CUDA cores from the phase tables (the charges scaled by the
+// power of two that brings the CTA's largest |q| into [1/2, 1), undone on the partials), B
+// from the Z pairs (|Z| = 1); both go to shared memory as FP16 hi + lo pairs (round to
+// nearest, then the exact remainder rounded again: 22 significant bits) in the canonical
+// K-major 128-byte-swizzled layout, and one thread issues kind::f16 MMAs (K = 16) for
+// hi*hi + hi*lo + lo*hi (the 3-term split product keeps the FP32 operands' accuracy; the
+// dropped lo*lo term is below 2^-22 relative). The tensor core's
 // FP32 accumulation does not round to nearest (over a 1024-site block it shrank |S| by a
 // few 1e-6, the Fourier energy by 1e-5), so each group of EW_MMA_GROUP chunks accumulates
 // in one of two tensor-memory accumulators and is then added, by the CUDA cores in
@@ -625,7 +627,7 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 #define EW_MMA_SITES 1024  // sites per CTA (a multiple of EW_SITES)
 #endif
 #define EW_MMA_TPB 256
-#define EW_MMA_KC 32       // sites per chunk: one 128-byte TF32 row of the swizzled layout
+#define EW_MMA_KC 32       // sites per chunk: 32 FP16 values of each 128-byte row of the swizzled layout
 #define EW_MMA_MAXKZ 30    // largest KMAXZ the pass takes (Z pairs within 32 columns)
 #define EW_MMA_STAGE 49152 // A hi, A lo (16 KB each), B hi, B lo (8 KB each)
 #define EW_MMA_SMEM (2 * EW_MMA_STAGE + 64 + 1024)
@@ -635,36 +637,10 @@ cudaError_t launch_sk(const EwArgs &A, int nblk, cudaStream_t s) {
 #endif
 #define EW_MMA_TCOLS 256   // tensor-memory columns per CTA: two group accumulators and the total
 
-// byte offset of TF32 element (m, k), k < 32, in a K-major tile with 128-byte rows and the
-// 128-byte swizzle (16-byte chunk index XOR row mod 8; 8-row groups of 1024 bytes)
-__device__ __forceinline__ unsigned sw128(int m, int k) {
-    return (unsigned)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 2) ^ m) & 7) << 4) + (k & 3) * 4);
-}
-
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
 __device__ __forceinline__ unsigned long long umma_desc(unsigned saddr) {
     return (unsigned long long)((saddr >> 4) & 0x3FFFu) | (1ull << 16) | ((unsigned long long)(1024 >> 4) << 32) |
            (1ull << 46) | (2ull << 61);
-}
-
-// instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major, M = 128, N = n
-__host__ __device__ constexpr unsigned umma_idesc_tf32(int n) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
-}
-
-__device__ __forceinline__ float tf32_rna(float x) {
-    unsigned r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void sts32(unsigned a, float v) {
-    asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
-}
-
-__device__ __forceinline__ void sts128(unsigned a, const float (&v)[4]) {
-    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
-                 : "memory");
 }
 
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long long limit) {
@@ -680,13 +656,36 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long lo
     return false;
 }
 
-__device__ __forceinline__ void umma_tf32(unsigned d, unsigned long long a, unsigned long long b, unsigned idesc,
-                                          unsigned acc) {
+// instruction descriptor of kind::f16: D F32, A and B F16, both K-major, M = 128, N = n
+__host__ __device__ constexpr unsigned umma_idesc_f16(int n) {
+    return (1u << 4) | ((unsigned)(n >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(unsigned d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                         unsigned acc) {
     asm volatile(
         "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
         "l"(a), "l"(b), "r"(idesc), "r"(acc)
         : "memory");
+}
+
+// FP16 hi + lo of four FP32 values, as two 8-byte pieces
+__device__ __forceinline__ void f16_split4(const float (&x)[4], uint2 &hi, uint2 &lo) {
+    unsigned h[2], l[2];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        const __half h0 = __float2half_rn(x[2 * e]), h1 = __float2half_rn(x[2 * e + 1]);
+        const __half l0 = __float2half_rn(x[2 * e] - __half2float(h0)), l1 = __float2half_rn(x[2 * e + 1] - __half2float(h1));
+        h[e] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
+        l[e] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
+    }
+    hi = make_uint2(h[0], h[1]);
+    lo = make_uint2(l[0], l[1]);
+}
+
+__device__ __forceinline__ void sts64(unsigned a, uint2 v) {
+    asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(unsigned addr, float (&v)[16]) {
@@ -721,7 +720,7 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
     const int pos0 = blockIdx.x * EW_MMA_ROWS;
     const int H = A.rows[A.forder[pos0]].z + 1 <= 16 ? 16 : 32;  // rows sorted by kzmax, longest first
     const int NPP = min(ew_zpairs(A.kz), (A.rows[A.forder[pos0]].z + 2) / 2);
-    const unsigned idesc = umma_idesc_tf32(2 * H);
+    const unsigned idesc = umma_idesc_f16(2 * H);
 
     // zero both stages (rows no chunk writes stay zero), barriers, tensor memory
     for (int i = threadIdx.x; i < 2 * EW_MMA_STAGE / 16; i += EW_MMA_TPB)
@@ -741,6 +740,26 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = *(volatile unsigned *)(gbase + (tslot - base));
+    // the power of two that brings the largest |q| of the CTA's sites into [1/2, 1): the A
+    // operand (|q X Y| <= |q|) then stays within FP16's range; the partials are scaled back
+    float qs, qus;
+    {
+        float *s_qmax = (float *)(gbase + (tslot - base) + 16);  // eight words after the barriers
+        const int a0 = blockIdx.y * EW_MMA_SITES, a1 = min(A.n, a0 + EW_MMA_SITES);
+        float m = 0.f;
+        for (int a = a0 + (int)threadIdx.x; a < a1; a += EW_MMA_TPB) m = fmaxf(m, fabsf(A.qf[a]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) s_qmax[warp] = m;
+        __syncthreads();
+        m = 0.f;
+#pragma unroll
+        for (int k = 0; k < EW_MMA_TPB / 32; k++) m = fmaxf(m, s_qmax[k]);
+        int e2 = 0;
+        frexpf(m, &e2);
+        qs = ldexpf(1.f, -e2);
+        qus = ldexpf(1.f, e2);
+    }
     // group accumulator g & 1 at columns 64 (g & 1); the running total at columns 128..
     // (lane quarter warp & 3; warps w and w + 4 drain the two column halves)
     const unsigned tlane = tmem + ((unsigned)((warp & 3) * 32) << 16);
@@ -779,7 +798,7 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
         rkx[j] = r.x;
         raky[j] = r.y < 0 ? -r.y : r.y;
         rys[j] = r.y < 0 ? -1.f : 1.f;
-        aoff[j] = (unsigned)(warp * 1024 + i * 128 + ((g ^ i) << 4));
+        aoff[j] = (unsigned)(warp * 1024 + i * 128 + ((((g >> 1) ^ i) & 7) << 4) + (g & 1) * 8);
     }
     // the B (Z) chunks go to the upper warps first: warp 0 also issues the MMAs (C2: S(k)
     // 0.336 -> 0.322 ms against giving them to warps 0..3)
@@ -790,7 +809,8 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
     {
         const int nrow[4] = {2 * bp, 2 * bp + 1, H + 2 * bp, H + 2 * bp + 1};
 #pragma unroll
-        for (int j = 0; j < 4; j++) boff[j] = (unsigned)((nrow[j] >> 3) * 1024 + (nrow[j] & 7) * 128 + ((g ^ nrow[j]) & 7) * 16);
+        for (int j = 0; j < 4; j++)
+            boff[j] = (unsigned)((nrow[j] >> 3) * 1024 + (nrow[j] & 7) * 128 + ((((g >> 1) ^ nrow[j]) & 7) << 4) + (g & 1) * 8);
     }
     const float2 *tab = (const float2 *)A.tab;
     const float2 *tX = tab, *tY = tab + (size_t)(A.kx + 1) * A.n;
@@ -854,39 +874,36 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
 #pragma unroll
             for (int jr = 0; jr < 2; jr++) {
                 if (!rok[jr]) continue;
-                float hr[4], lr[4], hi[4], li[4];
+                float re[4], im[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     float2 y = Y[jr][j];
                     y.y *= rys[jr];
-                    float2 aq = cmul(X[jr][j], y);
-                    aq.x *= Q[j];
-                    aq.y *= Q[j];
-                    hr[j] = tf32_rna(aq.x);
-                    lr[j] = tf32_rna(aq.x - hr[j]);
-                    hi[j] = tf32_rna(aq.y);
-                    li[j] = tf32_rna(aq.y - hi[j]);
+                    const float2 aq = cmul(X[jr][j], y);
+                    const float qj = Q[j] * qs;
+                    re[j] = aq.x * qj;
+                    im[j] = aq.y * qj;
                 }
-                sts128(st + aoff[jr], hr);
-                sts128(st + 16384 + aoff[jr], lr);
-                sts128(st + 8192 + aoff[jr], hi);
-                sts128(st + 16384 + 8192 + aoff[jr], li);
+                uint2 hr, lr, hi, li;
+                f16_split4(re, hr, lr);
+                f16_split4(im, hi, li);
+                sts64(st + aoff[jr], hr);
+                sts64(st + 16384 + aoff[jr], lr);
+                sts64(st + 8192 + aoff[jr], hi);
+                sts64(st + 16384 + 8192 + aoff[jr], li);
             }
             if (bwork) {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    float v[4], h[4], l[4];
+                    float v[4];
                     v[0] = j == 0 ? Z[0].x : j == 1 ? Z[0].y : j == 2 ? Z[0].z : Z[0].w;
                     v[1] = j == 0 ? Z[1].x : j == 1 ? Z[1].y : j == 2 ? Z[1].z : Z[1].w;
                     v[2] = j == 0 ? Z[2].x : j == 1 ? Z[2].y : j == 2 ? Z[2].z : Z[2].w;
                     v[3] = j == 0 ? Z[3].x : j == 1 ? Z[3].y : j == 2 ? Z[3].z : Z[3].w;
-#pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        h[e] = tf32_rna(v[e]);
-                        l[e] = tf32_rna(v[e] - h[e]);
-                    }
-                    sts128(st + 32768 + boff[j], h);
-                    sts128(st + 40960 + boff[j], l);
+                    uint2 h, l;
+                    f16_split4(v, h, l);
+                    sts64(st + 32768 + boff[j], h);
+                    sts64(st + 40960 + boff[j], l);
                 }
             }
             if (c + 1 < nch) load(c + 1);
@@ -902,12 +919,12 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
             const unsigned acc = tmem + 64u * (unsigned)((c / EW_MMA_GROUP) & 1);
             const bool fresh = c % EW_MMA_GROUP == 0;
 #pragma unroll
-            for (int k = 0; k < EW_MMA_KC / 8; k++) {
+            for (int k = 0; k < EW_MMA_KC / 16; k++) {  // K = 16 FP16 values (32 bytes) per MMA
                 const unsigned long long ah = umma_desc(st + 32 * k), al = umma_desc(st + 16384 + 32 * k);
                 const unsigned long long bh = umma_desc(st + 32768 + 32 * k), bl = umma_desc(st + 40960 + 32 * k);
-                umma_tf32(acc, ah, bh, idesc, (fresh && k == 0) ? 0u : 1u);
-                umma_tf32(acc, ah, bl, idesc, 1u);
-                umma_tf32(acc, al, bh, idesc, 1u);
+                umma_f16(acc, ah, bh, idesc, (fresh && k == 0) ? 0u : 1u);
+                umma_f16(acc, ah, bl, idesc, 1u);
+                umma_f16(acc, al, bh, idesc, 1u);
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar0 + 8 * b)
                          : "memory");
@@ -955,11 +972,11 @@ __global__ void __launch_bounds__(EW_MMA_TPB, 2) k_sk_mma(EwArgs A, unsigned *fl
         const int4 rw = A.rows[row];
         if (a > rw.z) continue;
         float RR = 0.f, RI = 0.f, IR = 0.f, II = 0.f;
-        if (nch > 0) {
-            RR = D[r * 65 + a];
-            RI = D[r * 65 + H + a];
-            IR = D[(64 + r) * 65 + a];
-            II = D[(64 + r) * 65 + H + a];
+        if (nch > 0) {  // back from the charge scale (exact)
+            RR = D[r * 65 + a] * qus;
+            RI = D[r * 65 + H + a] * qus;
+            IR = D[(64 + r) * 65 + a] * qus;
+            II = D[(64 + r) * 65 + H + a] * qus;
         }
         const int sp = A.row_slot[row] + 2 * a, sm = sp + 1;
         out[2 * sp] = RR - II;
@@ -1484,20 +1501,6 @@ __device__ __forceinline__ void kf_split8(const float (&x)[8], uint4 &hi, uint4 
     }
     hi = make_uint4(h[0], h[1], h[2], h[3]);
     lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
-
-// instruction descriptor of kind::f16: D F32, A and B F16, both K-major, M = 128, N = n
-__host__ __device__ constexpr unsigned umma_idesc_f16(int n) {
-    return (1u << 4) | ((unsigned)(n >> 3) << 17) | ((unsigned)(128 >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma_f16(unsigned d, unsigned long long a, unsigned long long b, unsigned idesc,
-                                         unsigned acc) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
 }
 
 // one warp per row of a tile (grid: tiles x KF_ROWS / 8, eight warps a block): lane (c, ch)
