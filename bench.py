@@ -157,6 +157,24 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(dist, v, device):
+    """The largest of the ranks' values, on every rank (a replica job takes as long as its
+    slowest rank); v itself without a process group. device is where the collective's
+    tensor lives: "cuda" under NCCL, "cpu" under gloo."""
+    if dist is None:
+        return float(v)
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, ms):
+    """Whole-job throughput: every rank processes units_per_rank per step (replicas, weak
+    scaling) and a step takes ms milliseconds (the maximum over ranks)."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def make_system(name):
     from mspms2_gb300 import configs
     return {"water_c2": configs.water_c2, "water_c4": configs.water_c4, "water_c1": configs.water_c1}[name]()
@@ -986,12 +1004,8 @@ def run_ours(args, rank, world, local_rank):
     # the numerator both arms share: pairs inside the cutoff by FP64 distance (the engine's
     # own count, from FP32 distances, can differ by a few pairs at the cutoff shell)
     npairs = pairs_in_cutoff(system)
-    ms_step = statistics.mean(times)
-    if dist:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * npairs / (ms_step * 1e-3)
+    ms_step = max_over_ranks(dist, statistics.mean(times), "cuda")
+    value = job_rate(world, npairs, ms_step)
 
     launches = st["kernel_launches"]
     # per-stage device times: one more call with stage events on and the reciprocal-space
@@ -1022,8 +1036,8 @@ def run_ours(args, rank, world, local_rank):
         b.record(stream)
         b.synchronize()
         e2e_times.append(a.elapsed_time(b))
-    e2e_ms = statistics.mean(e2e_times)
-    e2e_value = world * npairs / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(dist, statistics.mean(e2e_times), "cuda")
+    e2e_value = job_rate(world, npairs, e2e_ms)
 
     extras = {}
     if not args.no_extras and rank == 0:

@@ -6,6 +6,7 @@ without a GPU; creating a context there returns MG_ERR_NO_DEVICE.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -41,6 +42,16 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
+    # one build at a time: the ranks of a multi-process run all call this; the others wait,
+    # then find the library current
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and not _stale():
+            return LIB
+        return _build_locked(verbose, extra)
+
+
+def _build_locked(verbose: bool, extra: list | None) -> str:
     cc = nvcc()
     extra = extra or []
 
