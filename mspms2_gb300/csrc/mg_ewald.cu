@@ -144,27 +144,28 @@ __device__ __forceinline__ float2 ew_phase_f(unsigned U, int k) {
     return make_float2(c, s);
 }
 
+// one thread per (site, axis), the axis blockIdx.y (0: X, 1: Y, 2: the Z pairs): three
+// times the threads of one thread per site, each with a third of the serial work
 __global__ void k_phase_f(int n, const double *__restrict__ x, const double *__restrict__ y,
                           const double *__restrict__ z, double sx, double sy, double sz, int kx, int ky, int kz,
                           float2 *__restrict__ tab) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x, d = blockIdx.y;
     if (a >= n) return;
-    const double pos[3] = {x[a], y[a], z[a]};
-    const double sc[3] = {sx, sy, sz};
-    unsigned U[3];
-    for (int d = 0; d < 3; d++) {
-        double t = pos[d] * sc[d];
-        t = t - floor(t);
-        const double tu = t * 4294967296.0;
-        U[d] = tu >= 4294967295.0 ? 0xffffffffu : (unsigned)tu;
-    }
-    for (int k = 0; k <= kx; k++) tab[(size_t)k * n + a] = ew_phase_f(U[0], k);
-    for (int k = 0; k <= ky; k++) tab[(size_t)(kx + 1 + k) * n + a] = ew_phase_f(U[1], k);
-    float4 *zp = (float4 *)(tab + ew_zoff(kx, ky, n));
-    for (int p = 0; p < ew_zpairs(kz); p++) {
-        const float2 z0 = ew_phase_f(U[2], 2 * p);
-        const float2 z1 = 2 * p + 1 <= kz ? ew_phase_f(U[2], 2 * p + 1) : make_float2(0.f, 0.f);
-        zp[(size_t)p * n + a] = make_float4(z0.x, z1.x, z0.y, z1.y);
+    double t = d == 0 ? x[a] * sx : d == 1 ? y[a] * sy : z[a] * sz;
+    t = t - floor(t);
+    const double tu = t * 4294967296.0;
+    const unsigned U = tu >= 4294967295.0 ? 0xffffffffu : (unsigned)tu;
+    if (d == 0) {
+        for (int k = 0; k <= kx; k++) tab[(size_t)k * n + a] = ew_phase_f(U, k);
+    } else if (d == 1) {
+        for (int k = 0; k <= ky; k++) tab[(size_t)(kx + 1 + k) * n + a] = ew_phase_f(U, k);
+    } else {
+        float4 *zp = (float4 *)(tab + ew_zoff(kx, ky, n));
+        for (int p = 0; p < ew_zpairs(kz); p++) {
+            const float2 z0 = ew_phase_f(U, 2 * p);
+            const float2 z1 = 2 * p + 1 <= kz ? ew_phase_f(U, 2 * p + 1) : make_float2(0.f, 0.f);
+            zp[(size_t)p * n + a] = make_float4(z0.x, z1.x, z0.y, z1.y);
+        }
     }
 }
 
@@ -670,18 +671,22 @@ __device__ __forceinline__ void umma_f16(unsigned d, unsigned long long a, unsig
         : "memory");
 }
 
+// FP16 hi + lo of two FP32 values a, b, each pair packed (a in the low 16 bits): hi rounded
+// to nearest, lo the exact remainder rounded to nearest. One packed conversion converts both
+// values (conversions to narrower types issue at a fraction of the FP32 rate); the bits are
+// those of two scalar round-to-nearest conversions.
+__device__ __forceinline__ void f16x2_split(float a, float b, unsigned &hi, unsigned &lo) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const unsigned *>(&h);
+    lo = *reinterpret_cast<const unsigned *>(&l);
+}
+
 // FP16 hi + lo of four FP32 values, as two 8-byte pieces
 __device__ __forceinline__ void f16_split4(const float (&x)[4], uint2 &hi, uint2 &lo) {
-    unsigned h[2], l[2];
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-        const __half h0 = __float2half_rn(x[2 * e]), h1 = __float2half_rn(x[2 * e + 1]);
-        const __half l0 = __float2half_rn(x[2 * e] - __half2float(h0)), l1 = __float2half_rn(x[2 * e + 1] - __half2float(h1));
-        h[e] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
-        l[e] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
-    }
-    hi = make_uint2(h[0], h[1]);
-    lo = make_uint2(l[0], l[1]);
+    f16x2_split(x[0], x[1], hi.x, lo.x);
+    f16x2_split(x[2], x[3], hi.y, lo.y);
 }
 
 __device__ __forceinline__ void sts64(unsigned a, uint2 v) {
@@ -1491,16 +1496,10 @@ __device__ __forceinline__ unsigned kf_chunk(int m, int c) {
 
 // FP16 hi + lo of eight FP32 values, as two 16-byte chunks
 __device__ __forceinline__ void kf_split8(const float (&x)[8], uint4 &hi, uint4 &lo) {
-    unsigned h[4], l[4];
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-        const __half h0 = __float2half_rn(x[2 * e]), h1 = __float2half_rn(x[2 * e + 1]);
-        const __half l0 = __float2half_rn(x[2 * e] - __half2float(h0)), l1 = __float2half_rn(x[2 * e + 1] - __half2float(h1));
-        h[e] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
-        l[e] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
-    }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
+    f16x2_split(x[0], x[1], hi.x, lo.x);
+    f16x2_split(x[2], x[3], hi.y, lo.y);
+    f16x2_split(x[4], x[5], hi.z, lo.z);
+    f16x2_split(x[6], x[7], hi.w, lo.w);
 }
 
 // one warp per row of a tile (grid: tiles x KF_ROWS / 8, eight warps a block): lane (c, ch)
@@ -2248,7 +2247,7 @@ mg_status mg_launch_ewald(mg_ctx *c, const double *dx, const double *dy, const d
     if (fp64)
         k_phase_d<<<(n + 127) / 128, 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (double2 *)c->d_phase.p);
     else
-        k_phase_f<<<(n + 127) / 128, 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)c->d_phase.p);
+        k_phase_f<<<dim3((n + 127) / 128, 3), 128, 0, s>>>(n, dx, dy, dz, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)c->d_phase.p);
     EwArgs A = {};
     A.n = n;
     A.nrows = c->nrows;
@@ -2610,7 +2609,7 @@ extern "C" mg_status mg_ewald_recip_static(int device, void *stream, int precisi
     if (fp64)
         k_phase_d<<<(n + 127) / 128, 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (double2 *)tab);
     else
-        k_phase_f<<<(n + 127) / 128, 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)tab);
+        k_phase_f<<<dim3((n + 127) / 128, 3), 128, 0, s>>>(n, d_x, d_y, d_z, sc[0], sc[1], sc[2], KX, KY, KZ, (float2 *)tab);
     EwArgs A = {};
     A.n = n;
     A.nrows = ct.nrows;
