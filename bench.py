@@ -42,17 +42,10 @@ import numpy as np  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP32_LANES_PER_SM = 128
-# algorithmic work per unit (fixed constants of the work model; FP32 FLOP)
-# Fixed work model of the path (the roofline's algorithmic FLOP): a pair inside the cutoff,
-# counted once, is 55 FP32 FLOP (LJ + Ewald real space); reciprocal space is 10 FLOP per
-# (half-space k-vector, site) in the S(k) pass and 12 in the force pass.
-FLOP_PAIR = 55.0
-FLOP_K_S = 10.0
-FLOP_K_F = 12.0
-# FLOP the FP32 table passes execute, per site: S(k) 4 FMAs per (row, |kz|) for both signs of
-# kz plus q X^kx Y^ky per row; forces 8 FMAs per (row, |kz|) plus the per-row epilogue
-FLOP_SK_ROWKZ, FLOP_SK_ROW = 8.0, 8.0
-FLOP_KF_ROWKZ, FLOP_KF_ROW = 16.0, 18.0
+# algorithmic work per unit: the fixed constants of the work model (perf/work_model.py)
+from perf.work_model import (FLOP_K_F, FLOP_K_S, FLOP_KF_ROW, FLOP_KF_ROWKZ, FLOP_PAIR,  # noqa: E402
+                             FLOP_SK_ROW, FLOP_SK_ROWKZ, SF_BYTES_PER_SITE, list_build_bytes,
+                             neighbour_streaming_bytes)
 
 
 def ewald_rows(kmax, ksqmax):
@@ -916,12 +909,12 @@ def c5_extras(device, steps=10, warmup=3, md_steps=5, fp64=True, siman_tries=10,
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     nsf = n  # every butane site is of ghost type NONE
-    sf_gbs = nsf * 256.0 / (kms[5] * 1e-3) / 1e9 if kms[5] > 0 else None
+    sf_gbs = nsf * SF_BYTES_PER_SITE / (kms[5] * 1e-3) / 1e9 if kms[5] > 0 else None
     out.update({"ms_per_step": ms, "pairs_in_cutoff": npairs, "value": npairs / (ms * 1e-3),
                 "unit": "pair-interactions/s",
                 "stage_ms": {"list": kms[0], "pair": kms[1], "intra_bonded": kms[2], "solid_fluid": kms[5],
                              "total": kms[7]},
-                "sf_gather": {"bound": "hbm", "bytes_per_site": 256, "achieved_gbs": sf_gbs, "peak_gbs": hbm,
+                "sf_gather": {"bound": "hbm", "bytes_per_site": int(SF_BYTES_PER_SITE), "achieved_gbs": sf_gbs, "peak_gbs": hbm,
                               "frac": (sf_gbs / hbm) if (sf_gbs and hbm) else None,
                               "peak_basis": "of measured (MEASURED_PEAKS.json hbm_gbs)"},
                 "md": {"scheme": "NVT Nose-Hoover RESPA, 4 x 0.5 fs inner (bonded) + 2 fs outer", "steps": md_steps,
@@ -1127,8 +1120,8 @@ def run_ours(args, rank, world, local_rank):
     # shift, 4 B image; per site its FP64 position and wrapped position)
     hbm = measured_peaks().get("hbm_gbs")
     nent = st["cluster_pairs"]
-    pair_bytes = nent * 20.0 + 0.5 * nent * 8 * 32.0 + n * 40.0
-    list_bytes = nent * 24.0 + n * 3 * 8.0 * 3
+    pair_bytes = neighbour_streaming_bytes(nent, n)
+    list_bytes = list_build_bytes(nent, n)
     stage_roofline = {
         "pair": {"ms": kms[1], "tflops_work_model": FLOP_PAIR * npairs / (kms[1] * 1e-3) / 1e12 if kms[1] else None,
                  "frac_fp32": FLOP_PAIR * npairs / (kms[1] * 1e-3) / 1e12 / peak if kms[1] else None,
