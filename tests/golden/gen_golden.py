@@ -38,6 +38,7 @@ from mspms2_gb300.system import (ELEC_EWALD, ELEC_NONE, ELEC_SIMPLE_COULOMB, ELE
                                  GHOST_FULL, SF_ATOM_EXPLICIT, SF_HYPERGEO, SF_MY_INTERP, SF_TASOS,
                                  MyInterpGrid, Species, System, TasosGrid, read_reference_dir,
                                  system_to_arrays, tasos_dims, write_reference_dir)
+from golden_systems import custom_molecule_system, lj_gas, tasos_test_grid  # noqa: E402
 from oracle.pyoracle import (reference_available, run_reference_dir, run_reference_md,  # noqa: E402
                              run_reference_sfgridgen)
 
@@ -54,100 +55,6 @@ def _checkout() -> str:
 
 REF = _checkout()
 OUT = os.path.dirname(os.path.abspath(__file__))
-
-
-def lj_gas(n, box, seed, sigma=3.5, eps=50.0, xy_range=None, rc=None, avoid=None):
-    """n LJ sites on a jittered cubic lattice (spacing >= 1.05 sigma) inside the box, or
-    inside xy_range in x and y; `avoid(p)` rejects lattice points (near solid walls)."""
-    rng = np.random.default_rng(seed)
-    lo, hi = (0.0, box) if xy_range is None else xy_range
-    a = 1.05 * sigma
-    gx = np.arange(lo + 0.5 * a, hi - 0.25 * a, a)
-    gz = np.arange(0.5 * a, box - 0.25 * a, a)
-    X, Y, Z = np.meshgrid(gx, gx, gz, indexing="ij")
-    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
-    if avoid is not None:
-        pts = pts[[not avoid(p) for p in pts]]
-    if len(pts) < n:
-        raise ValueError(f"lattice holds {len(pts)} sites < {n}")
-    pts = pts[rng.permutation(len(pts))[:n]] + rng.uniform(-0.05 * sigma, 0.05 * sigma, size=(n, 3))
-    sp = configs.lj_species(n)
-    sp.sigma = np.array([sigma])
-    sp.epsilon = np.array([eps])
-    rc = rc if rc is not None else 0.5 * box - 1e-6
-    return System(species=[sp], box=np.array([box, box, box]), x=pts[:, 0].copy(), y=pts[:, 1].copy(),
-                  z=pts[:, 2].copy(), rcuton=rc, rcutoff=rc, rcutoffelec=rc, name=f"ljgas{n}")
-
-
-def tasos_test_grid(auc, buc, cuc, seed):
-    """Smooth analytic field with exact derivatives, Dxyz perturbed so the reference's
-    corner pairing of Dxyz is visible."""
-    ngx, ngy, ngz, hx, hy, hz = tasos_dims(auc, buc, cuc)
-    x = np.arange(ngx + 2) * hx
-    y = np.arange(ngy + 2) * hy
-    z = np.arange(ngz + 2) * hz
-    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
-    a, b, c = 1.3, 0.9, 2 * np.pi / cuc
-    A = 400.0
-    sx, cx = np.sin(a * X), np.cos(a * X)
-    sy, cy = np.sin(b * Y), np.cos(b * Y)
-    sz, cz = np.sin(c * Z), np.cos(c * Z)
-    F = A * sx * cy * cz - 900.0 + 30.0 * (X - auc / 2) ** 2
-    v = np.zeros(F.shape + (8,))
-    v[..., 0] = F
-    v[..., 1] = A * a * cx * cy * cz + 60.0 * (X - auc / 2)
-    v[..., 2] = -A * b * sx * sy * cz
-    v[..., 3] = -A * c * sx * cy * sz
-    v[..., 4] = -A * a * b * cx * sy * cz
-    v[..., 5] = -A * a * c * cx * cy * sz
-    v[..., 6] = A * b * c * sx * sy * sz
-    rng = np.random.default_rng(seed)
-    v[..., 7] = A * a * b * c * cx * sy * sz + rng.normal(scale=50.0, size=F.shape)
-    return TasosGrid(ngx + 2, ngy + 2, ngz + 2, hx, hy, hz, cuc, v)
-
-
-def custom_molecule_system(seed, with_nbp=False):
-    """A 6-site molecule with ghosts (LJ and FULL), nbp pairs, CHARMM dihedral and
-    improper, FENE/harmonic/Morse bonds, harmonic angles; Wolf electrostatics."""
-    rng = np.random.default_rng(seed)
-    tmpl = np.array([[0, 0, 0], [1.5, 0, 0], [2.1, 1.3, 0], [3.5, 1.4, 0.4], [1.4, -1.2, 0.5],
-                     [4.2, 2.5, 0.3]], dtype=float)
-    sp = Species(name="hexa", nmole=0, atom_names=["A", "B", "C", "D", "E", "F"],
-                 atom_type=np.arange(6, dtype=np.int32),
-                 ghost=np.array([0, 0, 1, 0, 2, 0], np.int32), interp=np.ones(6, np.int32),
-                 epsilon=np.array([60.0, 45.0, 30.0, 80.0, 20.0, 55.0]),
-                 sigma=np.array([3.4, 3.6, 2.5, 3.8, 2.0, 3.3]),
-                 charge=np.array([-0.4, 0.3, 0.2, -0.3, 0.1, 0.1]),
-                 aw=np.array([12.0, 14.0, 1.0, 16.0, 1.0, 12.0]) * 1.66054,
-                 aw_input=np.array([12.0, 14.0, 1.0, 16.0, 1.0, 12.0]) * 1e-3, template_xyz=tmpl)
-    sp.aw = (sp.aw_input / 6.0221415e23) / 1.0e-27
-    sp.bond_idx = np.array([[0, 1], [1, 2], [2, 3], [1, 4], [3, 5]], np.int32)
-    sp.bond_type = np.array([1, 2, 3, 1, 1], np.int32)
-    sp.bond_param = np.array([[100000.0, 1.5, 0.0], [30000.0, 1.45, 2.0], [5000.0, 2.5, 0.0],
-                              [90000.0, 1.3, 0.0], [80000.0, 1.4, 0.0]])
-    sp.angle_idx = np.array([[0, 1, 2], [1, 2, 3], [0, 1, 4], [2, 3, 5]], np.int32)
-    sp.angle_type = np.ones(4, np.int32)
-    sp.angle_param = np.array([[40000.0, 1.9, 0, 0, 0], [35000.0, 2.0, 0, 0, 0], [30000.0, 1.95, 0, 0, 0],
-                               [20000.0, 2.1, 0, 0, 0]])
-    sp.dih_idx = np.array([[0, 1, 2, 3], [1, 2, 3, 5], [4, 1, 2, 3]], np.int32)
-    sp.dih_type = np.array([1, 2, 1], np.int32)
-    sp.dih_param = np.array([[0.0, 700.0, -130.0, 1500.0], [300.0, 3.0, 0.0, 0.0], [10.0, 200.0, 50.0, 300.0]])
-    sp.imp_idx = np.array([[1, 0, 2, 4]], np.int32)
-    sp.imp_type = np.array([1], np.int32)
-    sp.imp_param = np.array([[150.0, 35.0]])
-    if with_nbp:
-        sp.nbp_idx = np.array([[0, 3], [0, 5], [4, 5], [2, 5]], np.int32)
-    nside = 3
-    box = 16.0
-    sp.nmole = nside ** 3
-    g = np.arange(nside)
-    cx, cy, cz = np.meshgrid(g, g, g, indexing="ij")
-    cen = (np.stack([cx.ravel(), cy.ravel(), cz.ravel()], 1) + 0.5) * (box / nside)
-    rot = configs._random_rotations(rng, sp.nmole)
-    xyz = (cen[:, None, :] + np.einsum("mij,aj->mai", rot, tmpl - tmpl.mean(0))).reshape(-1, 3)
-    return System(species=[sp], box=np.array([box] * 3), x=xyz[:, 0].copy(), y=xyz[:, 1].copy(),
-                  z=xyz[:, 2].copy(), rcuton=6.0, rcutoff=7.9, rcutoffelec=7.9, lj_switch=1, f0=0.5,
-                  charge_type=ELEC_WOLF, kappa=0.25, name="custom")
 
 
 def cases():
