@@ -291,3 +291,32 @@ def test_sk_wait_give_up_fails_the_call_and_recovers():
         after = eng.compute()
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
     assert before[2] == after[2]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("elec", ["wolf", "ewald"])
+@pytest.mark.parametrize("nbp_index_quirk", [True, False])
+def test_nbp_pairs_match_oracle(prec, elec, nbp_index_quirk):
+    """Molecules with a non-bonded pair list (nbp, src/frclong.c:791-977): the engine
+    against the oracle, with the reference's nbp_idx[ndih] index (MG_COMPAT_NBP_INDEX) and
+    with the loop's own index. The compiled reference gives no finite output to compare
+    here (its nbp indices are doubles read with %d), so the oracle is the check."""
+    import sys
+    from oracle.pyoracle import Oracle
+    from mspms2_gb300.system import ELEC_EWALD
+    sys.path.insert(0, GOLDEN)
+    from golden_systems import custom_molecule_system
+    s = custom_molecule_system(41, with_nbp=True)
+    if elec == "ewald":
+        s.charge_type, s.kappa, s.kmax, s.ksqmax = ELEC_EWALD, 0.3, (4, 4, 4), 24
+    if not nbp_index_quirk:
+        s.compat &= ~1
+    o = Oracle(s)
+    f_ref, e_ref, _ = o.frclong()
+    with Engine(s, precision=prec) as eng:
+        fl, _, e = eng.compute(terms=TERMS_LONG)
+    assert rel(fl, f_ref) <= TOL[prec], rel(fl, f_ref)
+    scale = energy_scale(e_ref)
+    for k in LONG_E:
+        assert abs(e[k] - e_ref[k]) <= TOL[prec] * max(component_scale(e_ref, k), FLOOR[prec] * scale) + 1e-9, \
+            (k, e[k], e_ref[k])
