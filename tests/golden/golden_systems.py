@@ -209,3 +209,46 @@ def random_variant(seed: int) -> System:
         s.myinterp = [MyInterpGrid(ncx, ncy, ncz, (1.0, 1.0, 1.0), 0.0, 0.0, 3.0, coeff)]
     s.name = f"live_{fam}_{seed}"
     return s
+
+
+MD_FAMILIES = ("water", "lj", "butane", "ions")
+
+
+def random_md_variant(seed: int) -> System:
+    """Seeded random start for the reference's own integrators: family
+    MD_FAMILIES[seed % 4], ensemble NVE (vver), NVT (vver_nh_3) or NPT (npt_respa), with
+    random time step, inner steps, thermostat and barostat masses, pressure, LJ
+    long-range correction and velocity seeds."""
+    rng = np.random.default_rng(9000 + seed)
+    fam = MD_FAMILIES[seed % len(MD_FAMILIES)]
+    ens = int(rng.integers(0, 3))
+    if fam == "water":
+        nside = int(rng.integers(3, 5))
+        box = float(rng.uniform(3.0, 3.3) * nside)
+        elec = (ELEC_NONE, ELEC_WOLF, ELEC_EWALD)[rng.integers(3)]
+        s = configs.water_small(nside, box, seed=seed, charge_type=elec, kappa=0.3, rc=0.45 * box, kmax=4, ksqmax=20)
+        s.delt_fs = float(rng.uniform(0.2, 0.6))
+    elif fam == "lj":
+        s = configs.lj_replica(int(rng.integers(150, 300)), seed=seed)
+        s.treq_K = float(rng.uniform(0.8, 1.5))
+        s.delt_fs = float(rng.uniform(2.0, 5.0))
+    elif fam == "butane":
+        s = configs.butane_box(3, float(rng.uniform(17.0, 19.0)), seed=seed, rc=7.0, site_jitter=0.05)
+        s.delt_fs = float(rng.uniform(0.5, 1.5))
+    else:
+        s = configs.ion_box(3, seed=seed, kmax=4, ksqmax=16, rc=4.0, spacing=3.5, jitter=0.2)
+        for sp in s.species:
+            sp.epsilon, sp.sigma = np.array([float(rng.uniform(30, 100))]), np.array([float(rng.uniform(2.6, 3.2))])
+            sp.aw_input = sp.aw_input * 30.0
+            sp.aw = sp.aw * 30.0
+        s.delt_fs = float(rng.uniform(0.5, 2.0))
+    s.what_ensemble = ens
+    s.nstep_inner = int(rng.integers(1, 5)) if ens else 1
+    s.nh_qq, s.nh_qqs = float(rng.uniform(200, 5000)), float(rng.uniform(200, 5000))
+    s.seeds = (int(rng.integers(1, 30000)), int(rng.integers(1, 30000)))
+    if ens == 2:
+        s.preq_bar = float(rng.uniform(1, 1000))
+        s.npt_qts, s.npt_qbs = float(rng.uniform(1e3, 5e4)), float(rng.uniform(1e3, 5e4))
+        s.lj_lrc = int(rng.integers(2))
+    s.name = f"md_live_{fam}_{seed}"
+    return s
