@@ -185,6 +185,9 @@ typedef struct mg_stats {
 } mg_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */
+/* Every entry point checks its handles: a NULL context or required pointer returns
+ * MG_ERR_INVALID (mg_destroy(NULL) is a no-op returning MG_OK; the two void helpers
+ * below ignore a NULL struct). */
 MG_API void mg_options_default(mg_options *opt);
 MG_API mg_status mg_create(mg_ctx **ctx, const mg_options *opt);
 MG_API mg_status mg_destroy(mg_ctx *ctx);

@@ -60,6 +60,7 @@ static mg_status upload(mg_ctx *c, DevBuf &b, const void *src, size_t bytes) {
 // lifecycle
 // ---------------------------------------------------------------------------------
 extern "C" void mg_options_default(mg_options *o) {
+    if (!o) return;
     o->device = 0;
     o->precision = MG_PREC_MIXED;
     o->skin = 0.0;
@@ -177,6 +178,7 @@ extern "C" mg_status mg_set_timing(mg_ctx *c, int enable) {
 // parameters (src/initvars.c:591-599, :421-462)
 // ---------------------------------------------------------------------------------
 extern "C" void mg_params_derive(mg_params *p, double lx, double ly, double lz) {
+    if (!p) return;
     const double pi = 3.141592653589793;
     p->rcutoffsq = p->rcutoff * p->rcutoff;
     p->rcutoffelecsq = p->rcutoffelec * p->rcutoffelec;

@@ -69,3 +69,41 @@ def test_params_derive_matches_python_and_reference(lib, case):
         assert getattr(q, k) == pytest.approx(py[k], rel=1e-15, abs=0), (case, k)
     ref = d["ref_derived"]
     assert q.shift1 == ref[4] and q.twopi_lx == ref[13] and q.vfactor_ewald == ref[12]
+
+
+NULL_OK = {"mg_destroy": 0, "mg_abi_version": None, "mg_set_wait_limit": 0, "mg_siman_stage_count": None,
+           "mg_ewald_recip_static_last_split": None, "mg_last_error": None, "mg_options_default": None,
+           "mg_params_derive": None}
+
+
+def test_every_entry_point_survives_null_arguments():
+    """Each function of the ABI, called with every argument NULL or zero, returns an error
+    status (or, for the few that take no handle, its plain result) instead of crashing; run
+    in a child process, so that a crash fails this test rather than the session."""
+    import json
+    import subprocess
+    import sys
+    src = open(os.path.join(ROOT, "include", "mspms2_gb300.h")).read()
+    decls = re.findall(r"MG_API\s+[\w\s\*]+?\b(mg_\w+)\s*\(([^)]*)\)", src)
+    calls = [(name, 0 if p.strip() in ("", "void") else p.count(",") + 1) for name, p in decls]
+    child = f"""
+import ctypes as C, json
+lib = C.CDLL({build.LIB!r})
+out = {{}}
+for name, n in {calls!r}:
+    f = getattr(lib, name)
+    f.restype = C.c_int
+    out[name] = f(*([None] * n))
+print(json.dumps(out))
+"""
+    build.build()
+    p = subprocess.run([sys.executable, "-c", child], capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stderr[-2000:]
+    got = json.loads(p.stdout.strip().splitlines()[-1])
+    assert set(got) == {n for n, _ in calls}
+    for name, status in got.items():
+        if name in NULL_OK:
+            if NULL_OK[name] is not None:
+                assert status == NULL_OK[name], (name, status)
+        else:
+            assert status != 0, name
