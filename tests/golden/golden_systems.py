@@ -135,7 +135,24 @@ def _stretch(s: System, rng):
 
 
 FAMILIES = ("water", "water_wrapped", "butane", "ions", "custom", "hypergeo", "atom_explicit", "tasos",
-            "myinterp")
+            "myinterp", "two_species")
+
+
+def _split_species(s: System, rng) -> System:
+    """The water molecules as two species: the first k keep the template, the rest get
+    their own LJ parameters and charges (scaled, still neutral), so that the pair loop's
+    cross-species branch runs."""
+    import copy
+    sp = s.species[0]
+    k = int(rng.integers(1, sp.nmole))
+    b = copy.deepcopy(sp)
+    b.name = sp.name + "_b"
+    sp.nmole, b.nmole = k, sp.nmole - k
+    b.epsilon = sp.epsilon * float(rng.uniform(0.7, 1.3))
+    b.sigma = sp.sigma * float(rng.uniform(0.9, 1.1))
+    b.charge = sp.charge * float(rng.uniform(0.8, 1.2))
+    s.species = [sp, b]
+    return s
 
 
 def random_variant(seed: int) -> System:
@@ -153,6 +170,14 @@ def random_variant(seed: int) -> System:
         if fam == "water_wrapped":  # per-site wrap: molecules straddle the box faces
             for a, v in enumerate((s.x, s.y, s.z)):
                 v -= s.box[a] * np.floor(v / s.box[a])
+    elif fam == "two_species":
+        nside = int(rng.integers(3, 5))
+        box = float(rng.uniform(3.1, 3.6) * nside)
+        s = configs.water_small(nside, box, seed=seed, charge_type=ELEC_EWALD, kappa=0.3, rc=0.45 * box, kmax=4,
+                                ksqmax=20)
+        _split_species(s, rng)
+        _stretch(s, rng)
+        _elec_and_cutoffs(s, rng)
     elif fam == "butane":
         s = configs.butane_box(3, float(rng.uniform(15.0, 17.0)), seed=seed, rc=7.0, charged=True,
                                site_jitter=0.05)

@@ -3,8 +3,8 @@
 Where the reference's force layer has been compiled (oracle/_ref/mspms_ref_force, built
 by oracle/build_ref.sh from a reference checkout), each case builds a random system of one
 family (water, water with molecules wrapped across the faces, charged butane, ions, a
-six-site molecule with ghosts, 1-4 pairs and every bonded form, and the four solid-fluid
-models), with random electrostatics (none, Wolf, Ewald with tin-foil or vacuum
+six-site molecule with ghosts, 1-4 pairs and every bonded form, the four solid-fluid
+models, and water split into two species with their own parameters), with random electrostatics (none, Wolf, Ewald with tin-foil or vacuum
 boundaries, plain Coulomb), LJ switch, 1-4 scale, cutoffs, k-vector set and a non-cubic
 box. It writes the system in the reference's input format, runs the reference's
 frclong()/frcshort(), and compares the oracle's forces and all 18 energies (1e-12
