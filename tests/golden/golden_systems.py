@@ -111,13 +111,20 @@ def custom_molecule_system(seed, with_nbp=False):
 def _elec_and_cutoffs(s: System, rng, elec_choices=(ELEC_NONE, ELEC_WOLF, ELEC_EWALD, ELEC_EWALD,
                                                    ELEC_SIMPLE_COULOMB)):
     """Random electrostatics (with its kappa, k-vector set and boundary condition), LJ
-    switch, 1-4 scale and cutoffs below half the shortest box edge."""
+    switch, 1-4 scale and cutoffs below half the shortest box edge; about one case in six
+    each has the cutoff at 0.4999 of the shortest edge, an extreme kappa, no k-vectors along
+    one axis, or the whole cube of k-vectors."""
     s.charge_type = int(elec_choices[rng.integers(len(elec_choices))])
-    rc = float(rng.uniform(0.3, 0.48)) * float(np.min(s.box))
+    edge = int(rng.integers(6))  # 0-3: one edge case each (below), else none
+    rc = (0.4999 if edge == 0 else float(rng.uniform(0.3, 0.48))) * float(np.min(s.box))
     s.rcutoff = s.rcutoffelec = rc
-    s.kappa = float(rng.uniform(0.2, 0.4))
+    s.kappa = float(rng.choice([0.05, 0.9])) if edge == 1 else float(rng.uniform(0.2, 0.4))
     s.kmax = tuple(int(v) for v in rng.integers(2, 6, size=3))
+    if edge == 2:  # no k-vectors along one axis
+        s.kmax = tuple(0 if a == int(rng.integers(3)) else k for a, k in enumerate(s.kmax))
     s.ksqmax = int(rng.integers(4, max(s.kmax) ** 2 + 2))
+    if edge == 3:  # a bound above every corner of the box of k-vectors: the whole cube
+        s.ksqmax = sum(k * k for k in s.kmax) + 1
     s.ewald_bc = int(rng.integers(1, 3)) if s.charge_type == ELEC_EWALD else 1
     s.lj_switch = int(rng.integers(2))
     s.rcuton = rc * float(rng.uniform(0.6, 0.9)) if s.lj_switch else rc

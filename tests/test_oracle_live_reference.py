@@ -62,13 +62,18 @@ def test_oracle_equals_reference_on_random_system(seed):
 
 def test_variants_reach_every_switch():
     """The seeds above reach every family, electrostatics type, both Ewald boundary
-    conditions and both LJ forms."""
+    conditions, both LJ forms, an Ewald axis without k-vectors and the whole cube."""
     seen = set()
     for seed in SEEDS:
         s = random_variant(seed)
         seen.add(("family", seed % len(FAMILIES)))
         seen.add(("elec", s.charge_type, s.ewald_bc if s.charge_type == 1 else 0))
         seen.add(("switch", s.lj_switch))
+        if s.charge_type == 1 and 0 in s.kmax:
+            seen.add("zero kmax")
+        if s.charge_type == 1 and s.ksqmax > sum(k * k for k in s.kmax):
+            seen.add("cube")
+    assert {"zero kmax", "cube"} <= seen
     assert {("family", f) for f in range(len(FAMILIES))} <= seen
     assert {("elec", 0, 0), ("elec", 1, 1), ("elec", 1, 2), ("elec", 2, 0), ("elec", 3, 0)} <= seen
     assert {("switch", 0), ("switch", 1)} <= seen
